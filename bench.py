@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""Benchmark of the ten open-earth-benchmarks stencils on GB300.
+
+Workload (one "step"): each of the ten stencils once, FP64, on a 128 x 128 x 80 interior with
+a 3-cell halo -- the all-ten-kernels configuration of the reference benchmark -- with seeded
+synthetic inputs (fields.py, workload "physical", seed 1).  Metric: grid-point updates per
+second over the ten kernels (10 x 1,310,720 interior points per step), in GPts/s.
+
+* ``value``        device-resident inputs, CUDA events around K steps on the launch stream.
+                   Two input sets (1.65 GB) alternate between steps; one step reads 827 MB of
+                   distinct fields, so no kernel finds its inputs in the 129 MB L2.
+* ``e2e``          the same step through the host entry points (oeb_<k>_f64_host) on pinned
+                   host buffers: every call copies its inputs in and its outputs out.
+* ``roofline``     the kernel with the largest share of the step: algorithmic bytes per
+                   launch / its CUDA-event duration, against the measured HBM copy bandwidth.
+* ``cpu_baseline`` the oracle's restatement of the reference OpenMP kernels on this host's
+                   cores (bounded sample), rank 0 only.
+
+``--impl reference`` times the reference's CPU implementation of the step instead (the
+oracle restatement, OpenMP on all host cores; the reference's own headers are compiled
+only where its source tree exists, which is not the GPU host) and prints its JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__ as graft  # noqa: E402
+
+NX, NY, NZ, HALO, SEED = 128, 128, 80, 3, 1
+WORKLOAD = "ten stencils FP64, 128x128x80 interior + 3-cell halo, physical inputs seed 1"
+METRIC = "GPts/s (grid-point updates/s over the ten stencils)"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def _dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _make_set(pkg, fields, torch, dev, seed, pinned=False):
+    """Per kernel: (field Storages, scalars), every field a separate allocation."""
+    out = {}
+    for name in pkg.KERNELS:
+        inputs = fields.make_inputs(name, NX, NY, NZ, seed=seed)
+        outs = fields.make_outputs(name, NX, NY, NZ)
+        st = {}
+        for k, v in {**inputs, **outs}.items():
+            t = torch.from_numpy(v)
+            if dev is not None:
+                t = t.to(dev)
+            elif pinned:
+                t = t.pin_memory()
+            st[k] = pkg.Storage(t, HALO)
+        out[name] = (st, fields.make_scalars(name, seed=seed))
+    return out
+
+
+def _algorithmic_bytes(pkg, name):
+    return pkg.KERNELS[name].bytes_per_point(8) * NX * NY * NZ
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = _dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pkg = graft.load_package()
+    import importlib
+    fields = importlib.import_module("oeb_gb300.fields")
+    lib = pkg.load_library()
+    names = list(pkg.KERNELS)
+    sets = [_make_set(pkg, fields, torch, dev, SEED + r) for r in range(2)]
+    stream = torch.cuda.current_stream(dev)
+    dom = (NX, NY, NZ)
+
+    def step(s, ev=None):
+        for idx, name in enumerate(names):
+            st, sc = s[name]
+            if ev is not None:
+                ev[idx][0].record(stream)
+            pkg.call(name, st, sc, domain=dom, stream=stream)
+            if ev is not None:
+                ev[idx][1].record(stream)
+
+    for w in range(args.warmup):
+        step(sets[w % 2])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    # per-kernel events in every timed step
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in names]
+           for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    launches0 = lib.oeb_launch_count()
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for s in range(args.steps):
+            step(sets[s % 2], evs[s])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.oeb_launch_count() - launches0
+    ms_total = t0.elapsed_time(t1)
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+        torch.distributed.barrier()
+    ms_step = ms_total / args.steps
+    pts_step = len(names) * NX * NY * NZ
+    value = world * pts_step * args.steps / (ms_total * 1e-3) / 1e9
+
+    per_kernel = {}
+    for idx, name in enumerate(names):
+        per_kernel[name] = statistics.mean(evs[s][idx][0].elapsed_time(evs[s][idx][1]) for s in range(args.steps))
+    total_k = sum(per_kernel.values())
+    dom_k = max(per_kernel, key=per_kernel.get)
+    peak, peak_src = _measured_peak()
+    achieved = _algorithmic_bytes(pkg, dom_k) / (per_kernel[dom_k] * 1e-3) / 1e9
+    traffic = _ncu_traffic(dom_k)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = _e2e(pkg, fields, torch, args, names)
+
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "GPts/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; fields.py 'physical')",
+        "config": {"workload": WORKLOAD, "kernels": names, "interior": [NX, NY, NZ], "halo": HALO,
+                   "points_per_step": pts_step,
+                   "l2": "inputs larger than L2: two 827 MB input sets alternate between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": dom_k, "achieved": round(achieved, 2), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": _algorithmic_bytes(pkg, dom_k),
+                     "launch_ms": round(per_kernel[dom_k], 5)},
+        "per_kernel_ms": {k: round(v, 5) for k, v in per_kernel.items()},
+        "per_kernel_gbs": {k: round(_algorithmic_bytes(pkg, k) / (v * 1e-3) / 1e9, 1) for k, v in per_kernel.items()},
+        "kernel_share": {k: round(v / total_k, 4) for k, v in per_kernel.items()},
+        "clocks": clocks.summary(),
+        "gpu_launches": int(launches),
+    }
+    if e2e is not None:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = _cpu_baseline(pkg, fields, budget_s=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _ncu_traffic(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if there is one."""
+    p = ROOT / "profiles" / ("ncu_%s_128x128x80.md" % kernel)
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("dram_bytes_per_launch:"):
+            try:
+                return int(float(ln.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+def _e2e(pkg, fields, torch, args, names):
+    """The step through the host entry points with pinned host buffers."""
+    hs = _make_set(pkg, fields, torch, None, SEED, pinned=True)
+    dom = (NX, NY, NZ)
+    h2d = d2h = 0
+    for name in names:
+        spec = pkg.KERNELS[name]
+        st, _ = hs[name]
+        for a in spec.args:
+            if a.role in ("in3", "in1"):
+                h2d += st[a.name].data.numel() * 8
+            elif a.role == "out3":
+                ilo, ihi, jlo, jhi, klo, khi = a.reach
+                d2h += (NX + ilo + ihi) * (NY + jlo + jhi) * (NZ + klo + khi) * 8
+
+    def step():
+        for name in names:
+            st, sc = hs[name]
+            pkg.call(name, st, sc, domain=dom)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    t = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t) / steps
+    return {"value": round(len(names) * NX * NY * NZ / dt / 1e9, 4), "unit": "GPts/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(dt * 1e3, 3),
+            "path": "oeb_<k>_f64_host, pinned host buffers, synchronous per call"}
+
+
+def _cpu_baseline(pkg, fields, budget_s=15.0, threads=None):
+    """The oracle (restated reference OpenMP kernels) on this host's cores, bounded sample."""
+    from oracle import oracle as orc
+    threads = threads or os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    sets = {}
+    for name, spec in pkg.KERNELS.items():
+        inputs = fields.make_inputs(name, NX, NY, NZ, seed=SEED)
+        outs = fields.make_outputs(name, NX, NY, NZ, include_scratch=True)
+        sets[name] = ({**inputs, **outs}, fields.make_scalars(name, seed=SEED))
+    per = {}
+    steps = 0
+    t_all = time.perf_counter()
+    while True:
+        for name, spec in pkg.KERNELS.items():
+            buf, sc = sets[name]
+            t = time.perf_counter()
+            orc.run_oracle(spec, buf, sc, NX, NY, NZ, HALO)
+            per.setdefault(name, []).append(time.perf_counter() - t)
+        steps += 1
+        if time.perf_counter() - t_all > budget_s or steps >= 50:
+            break
+    step_s = sum(statistics.mean(v) for v in per.values())
+    return {"value": round(len(per) * NX * NY * NZ / step_s / 1e9, 5), "unit": "GPts/s", "cores": threads,
+            "kind": "port",
+            "sample": "%d steps of the ten-kernel FP64 step at 128x128x80 (oracle restatement of the reference "
+                      "_openmp kernels, serial fvtp2d; OMP_NUM_THREADS=%s)" % (steps, os.environ["OMP_NUM_THREADS"]),
+            "per_kernel_ms": {k: round(statistics.mean(v) * 1e3, 3) for k, v in per.items()}}
+
+
+def run_reference(args):
+    rank, world, _ = _dist_env()
+    if rank != 0:
+        return
+    pkg = graft.load_package()
+    import importlib
+    fields = importlib.import_module("oeb_gb300.fields")
+    threads = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    from oracle import oracle as orc
+    from oracle import build as ob
+    use_ref = orc.reference_available()
+    sets = {}
+    for name in pkg.KERNELS:
+        inputs = fields.make_inputs(name, NX, NY, NZ, seed=SEED)
+        outs = fields.make_outputs(name, NX, NY, NZ, include_scratch=True)
+        sets[name] = ({**inputs, **outs}, fields.make_scalars(name, seed=SEED))
+
+    def one_step():
+        for name, spec in pkg.KERNELS.items():
+            buf, sc = sets[name]
+            if use_ref:
+                orc.run_reference(spec, buf, sc, NX, NZ, HALO, "openmp")
+            else:
+                orc.run_oracle(spec, buf, sc, NX, NY, NZ, HALO)
+
+    for _ in range(args.warmup):
+        one_step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    dt = (time.perf_counter() - t) / args.steps
+    value = len(pkg.KERNELS) * NX * NY * NZ / dt / 1e9
+    kind = "reference" if use_ref else "port"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "GPts/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; fields.py 'physical')",
+            "config": {"workload": WORKLOAD, "interior": [NX, NY, NZ], "halo": HALO},
+            "cpu_baseline": {"value": round(value, 5), "unit": "GPts/s", "cores": threads, "kind": kind,
+                             "sample": "each step = the ten reference kernels once at 128x128x80 (_openmp "
+                                       "variants, serial fvtp2d), %s, OMP_NUM_THREADS=%s" %
+                                       ("reference headers compiled from source" if use_ref else
+                                        "oracle restatement (reference sources absent on this host)",
+                                        os.environ["OMP_NUM_THREADS"])},
+            "e2e": {"value": round(value, 5), "unit": "GPts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        sys.stderr.write("warning: fewer than 3 warm-up steps\n")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

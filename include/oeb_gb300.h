@@ -1,0 +1,275 @@
+/*
+ * oeb_gb300.h -- C ABI of the GB300 (sm_103a) open-earth-benchmarks stencils.
+ *
+ * Every entry point takes field descriptors laid out exactly like the reference's
+ * strided Storage<T,R> (include/util.h:24-31): {allocatedPtr, alignedPtr, offset,
+ * sizes[R], strides[R]}, with element (i,j,k) at
+ *     aligned[offset + strides[2]*i + strides[1]*j + strides[0]*k]
+ * (include/util.h:82-94), i.e. i is the unit-stride axis and sizes/strides are
+ * stored k-first.  The descriptor of the reference's allocateStorage
+ * (include/util.h:126-141) is accepted as is; any row/plane padding is also
+ * accepted as long as strides[2] == 1.
+ *
+ * The reference reads the interior extents from the globals domain_size and
+ * domain_height (src/<k>.cpp:4-5); here they are the explicit oeb_domain
+ * {nx, ny, nz}, which also allows nx != ny.
+ *
+ * Device entry points (oeb_<k>_f64 / _f32) take DEVICE pointers and are
+ * asynchronous on the given cudaStream_t (passed as void*, NULL = legacy default
+ * stream).  Host entry points (oeb_<k>_f64_host) take HOST pointers, stage the
+ * fields through device memory and return after the outputs are back in host
+ * memory.  No entry point writes the scratch fields of the reference signatures
+ * (lap/flx/fly, T_sqr_s, uatupos..., ppgk..., wk, du, dv, fxx, al, ...): they are
+ * not parameters of this ABI.  Cells outside each output's written box are left
+ * untouched, as in the reference.
+ *
+ * All functions return an oeb_status; nothing aborts the process.
+ */
+#ifndef OEB_GB300_H
+#define OEB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define OEB_API __attribute__((visibility("default")))
+#else
+#define OEB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum oeb_status {
+  OEB_OK = 0,
+  OEB_ERR_NULL = 1,        /* a required descriptor or pointer is NULL                     */
+  OEB_ERR_DOMAIN = 2,      /* nx, ny or nz < 1, or the domain exceeds the 2^31 index limit */
+  OEB_ERR_LAYOUT = 3,      /* strides[2] != 1, strides not nested, or the 3-D fields of     */
+                           /* one call do not share strides                                 */
+  OEB_ERR_HALO = 4,        /* a field's halo is smaller than the kernel's reach             */
+  OEB_ERR_ALIGNMENT = 5,   /* a pointer is not aligned to its element size                  */
+  OEB_ERR_CUDA = 6,        /* a CUDA runtime call failed; see oeb_last_cuda_error()         */
+  OEB_ERR_ALLOC = 7,       /* device or pinned allocation failed                            */
+  OEB_ERR_ALIAS = 8,       /* an output field overlaps an input field                       */
+  OEB_ERR_UNSUPPORTED = 9, /* unknown kernel or variant                                      */
+  OEB_ERR_TIMEOUT = 10,    /* a bounded device-side wait gave up                             */
+  OEB_ERR_TOO_LARGE = 11,  /* a request exceeds a documented fixed capacity                  */
+  OEB_ERR_ARGUMENT = 12    /* a scalar argument is out of its documented range               */
+} oeb_status;
+
+typedef struct oeb_memref3d_f64 {
+  double* allocated;
+  double* aligned;
+  int64_t offset;
+  int64_t sizes[3];   /* {k extent, j extent, i extent} incl. halo (util.h:129-131) */
+  int64_t strides[3]; /* {k stride, j stride, i stride == 1}    (util.h:133-135) */
+} oeb_memref3d_f64;
+
+typedef struct oeb_memref1d_f64 {
+  double* allocated;
+  double* aligned;
+  int64_t offset;
+  int64_t sizes[1];
+  int64_t strides[1];
+} oeb_memref1d_f64;
+
+typedef struct oeb_memref3d_f32 {
+  float* allocated;
+  float* aligned;
+  int64_t offset;
+  int64_t sizes[3];
+  int64_t strides[3];
+} oeb_memref3d_f32;
+
+typedef struct oeb_memref1d_f32 {
+  float* allocated;
+  float* aligned;
+  int64_t offset;
+  int64_t sizes[1];
+  int64_t strides[1];
+} oeb_memref1d_f32;
+
+/* Interior extents: nx = ny = domain_size and nz = domain_height in the reference. */
+typedef struct oeb_domain {
+  int64_t nx;
+  int64_t ny;
+  int64_t nz;
+} oeb_domain;
+
+/* ------------------------------------------------------------------------- */
+/* Library information and errors                                             */
+/* ------------------------------------------------------------------------- */
+
+/* ABI version: major * 10000 + minor * 100 + patch. */
+OEB_API int oeb_abi_version(void);
+/* Static, NUL-terminated description of a status code. */
+OEB_API const char* oeb_status_string(int status);
+/* Text of the last CUDA error seen by this thread ("" if none). */
+OEB_API const char* oeb_last_cuda_error(void);
+/* Number of kernel launches this library has issued (all threads) since load.  */
+OEB_API uint64_t oeb_launch_count(void);
+
+/* ------------------------------------------------------------------------- */
+/* Device storage (the device twin of allocateStorage/freeStorage,           */
+/* include/util.h:99-148).  The element layout is the reference's, with the  */
+/* row pitch rounded up to pitch_multiple elements (1 = no padding).          */
+/* ------------------------------------------------------------------------- */
+
+OEB_API oeb_status oeb_storage3d_alloc_f64(int64_t nx, int64_t ny, int64_t nz, int64_t halo, int64_t pitch_multiple,
+                                   oeb_memref3d_f64* out);
+OEB_API oeb_status oeb_storage1d_alloc_f64(int64_t n, int64_t halo, oeb_memref1d_f64* out);
+OEB_API oeb_status oeb_storage3d_alloc_f32(int64_t nx, int64_t ny, int64_t nz, int64_t halo, int64_t pitch_multiple,
+                                   oeb_memref3d_f32* out);
+OEB_API oeb_status oeb_storage1d_alloc_f32(int64_t n, int64_t halo, oeb_memref1d_f32* out);
+/* Frees a descriptor returned by oeb_storage*_alloc_* and clears its pointers. */
+OEB_API oeb_status oeb_storage_free(void* memref);
+/* Bytes spanned by a descriptor: from allocated to one past the last element. */
+OEB_API int64_t oeb_memref3d_span_bytes_f64(const oeb_memref3d_f64* m);
+OEB_API int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m);
+
+/* ------------------------------------------------------------------------- */
+/* FP64 forward stencils, device pointers, asynchronous on `stream`.          */
+/* Argument order is the reference signature's with the scratch fields and    */
+/* the globals made explicit.                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* kernels/laplace.h:4 -- laplace(in, out) */
+OEB_API oeb_status oeb_laplace_f64(const oeb_memref3d_f64* in, const oeb_memref3d_f64* out, const oeb_domain* dom,
+                           void* stream);
+
+/* kernels/hdiffsa.h:4-5 -- hdiffsa(out, in, mask, crlato, crlatu, lap, flx, fly) */
+OEB_API oeb_status oeb_hdiffsa_f64(const oeb_memref3d_f64* out, const oeb_memref3d_f64* in, const oeb_memref3d_f64* mask,
+                           const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_domain* dom,
+                           void* stream);
+
+/* kernels/hdiffsmag.h:4-7 -- hdiffsmag(uout, vout, uin, vin, mask, crlavo, crlavu, crlato, crlatu,
+ *                                      acrlat0, T_sqr_s, S_sqr_uv, eddlat, eddlon, tau_smag, weight_smag) */
+OEB_API oeb_status oeb_hdiffsmag_f64(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                             const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                             const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlavo,
+                             const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato,
+                             const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0, double eddlat,
+                             double eddlon, double tau_smag, double weight_smag, const oeb_domain* dom,
+                             void* stream);
+
+/* kernels/hadvuv.h:29-32 -- hadvuv(uout, vout, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1,
+ *                                  uatupos, vatupos, uatvpos, vatvpos, uavg, vavg, ures, vres, eddlat, eddlon) */
+OEB_API oeb_status oeb_hadvuv_f64(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout, const oeb_memref3d_f64* uin,
+                          const oeb_memref3d_f64* vin, const oeb_memref1d_f64* acrlat0,
+                          const oeb_memref1d_f64* acrlat1, const oeb_memref1d_f64* tgrlatda0,
+                          const oeb_memref1d_f64* tgrlatda1, double eddlat, double eddlon, const oeb_domain* dom,
+                          void* stream);
+
+/* kernels/hadvuv5th.h:41-44 -- hadvuv5th(same arguments as hadvuv) */
+OEB_API oeb_status oeb_hadvuv5th_f64(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                             const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                             const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                             const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1, double eddlat,
+                             double eddlon, const oeb_domain* dom, void* stream);
+
+/* kernels/fastwavesuv.h:4-7 -- fastwavesuv(uout, vout, uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho, fx,
+ *                                          ppgk, ppgc, ppgu, ppgv, edadlat, dt) */
+OEB_API oeb_status oeb_fastwavesuv_f64(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                               const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                               const oeb_memref3d_f64* utens, const oeb_memref3d_f64* vtens,
+                               const oeb_memref3d_f64* wgtfac, const oeb_memref3d_f64* ppuv,
+                               const oeb_memref3d_f64* hhl, const oeb_memref3d_f64* rho, const oeb_memref1d_f64* fx,
+                               double edadlat, double dt, const oeb_domain* dom, void* stream);
+
+/* kernels/uvbke.h:4-5 -- uvbke(ub, vb, uc, vc, cosa, rsina); dt5 is the driver global (src/uvbke.cpp:11-12) */
+OEB_API oeb_status oeb_uvbke_f64(const oeb_memref3d_f64* ub, const oeb_memref3d_f64* vb, const oeb_memref3d_f64* uc,
+                         const oeb_memref3d_f64* vc, const oeb_memref3d_f64* cosa, const oeb_memref3d_f64* rsina,
+                         double dt5, const oeb_domain* dom, void* stream);
+
+/* kernels/nh_p_grad.h:4-6 -- nh_p_grad(uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, wk, du, dv, dt) */
+OEB_API oeb_status oeb_nh_p_grad_f64(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                             const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* rdx,
+                             const oeb_memref3d_f64* rdy, const oeb_memref3d_f64* gz, const oeb_memref3d_f64* pp,
+                             const oeb_memref3d_f64* pk3, const oeb_memref3d_f64* wk1, double dt,
+                             const oeb_domain* dom, void* stream);
+
+/* kernels/p_grad_c.h:4-6 -- p_grad_c(uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc, wk, dt2) */
+OEB_API oeb_status oeb_p_grad_c_f64(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                            const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* rdxc,
+                            const oeb_memref3d_f64* rdyc, const oeb_memref3d_f64* delpc, const oeb_memref3d_f64* gz,
+                            const oeb_memref3d_f64* pkc, double dt2, const oeb_domain* dom, void* stream);
+
+/* kernels/fvtp2d.h:4-7 -- fvtp2d(q_i, q_j, fx1, fx2, fy1, fy2, q, crx, cry, ra_x, ra_y, xfx, yfx, area,
+ *                                fxx, fyy, al, almq, br, b0, smt5); p1, p2 are the driver macros
+ * (src/fvtp2d.cpp:11-12).  q_i, q_j, fx2 and fy2 are written over the same extended ranges as the
+ * reference (fvtp2d.h:26-27, 46-47, 102-103, 122-123), so they need a 3-cell halo. */
+OEB_API oeb_status oeb_fvtp2d_f64(const oeb_memref3d_f64* q_i, const oeb_memref3d_f64* q_j, const oeb_memref3d_f64* fx1,
+                          const oeb_memref3d_f64* fx2, const oeb_memref3d_f64* fy1, const oeb_memref3d_f64* fy2,
+                          const oeb_memref3d_f64* q, const oeb_memref3d_f64* crx, const oeb_memref3d_f64* cry,
+                          const oeb_memref3d_f64* ra_x, const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx,
+                          const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, double p1, double p2,
+                          const oeb_domain* dom, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* FP64 forward stencils, HOST pointers, synchronous.  Same arguments as the  */
+/* device entry points; each call stages its fields through device memory    */
+/* (inputs: the whole descriptor span; outputs: exactly the written box) and  */
+/* returns once the outputs are in host memory.  Any host memory works;       */
+/* pinned memory makes the copies DMA transfers.                              */
+/* ------------------------------------------------------------------------- */
+
+OEB_API oeb_status oeb_laplace_f64_host(const oeb_memref3d_f64* in, const oeb_memref3d_f64* out,
+                                        const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsa_f64_host(const oeb_memref3d_f64* out, const oeb_memref3d_f64* in,
+                                        const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlato,
+                                        const oeb_memref1d_f64* crlatu, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsmag_f64_host(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                          const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                          const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlavo,
+                                          const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato,
+                                          const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0,
+                                          double eddlat, double eddlon, double tau_smag, double weight_smag,
+                                          const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv_f64_host(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                       const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                       const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                                       const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1,
+                                       double eddlat, double eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv5th_f64_host(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                          const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                          const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                                          const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1,
+                                          double eddlat, double eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fastwavesuv_f64_host(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                            const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                            const oeb_memref3d_f64* utens, const oeb_memref3d_f64* vtens,
+                                            const oeb_memref3d_f64* wgtfac, const oeb_memref3d_f64* ppuv,
+                                            const oeb_memref3d_f64* hhl, const oeb_memref3d_f64* rho,
+                                            const oeb_memref1d_f64* fx, double edadlat, double dt,
+                                            const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_uvbke_f64_host(const oeb_memref3d_f64* ub, const oeb_memref3d_f64* vb,
+                                      const oeb_memref3d_f64* uc, const oeb_memref3d_f64* vc,
+                                      const oeb_memref3d_f64* cosa, const oeb_memref3d_f64* rsina, double dt5,
+                                      const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_nh_p_grad_f64_host(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                          const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                          const oeb_memref3d_f64* rdx, const oeb_memref3d_f64* rdy,
+                                          const oeb_memref3d_f64* gz, const oeb_memref3d_f64* pp,
+                                          const oeb_memref3d_f64* pk3, const oeb_memref3d_f64* wk1, double dt,
+                                          const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_p_grad_c_f64_host(const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                         const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                         const oeb_memref3d_f64* rdxc, const oeb_memref3d_f64* rdyc,
+                                         const oeb_memref3d_f64* delpc, const oeb_memref3d_f64* gz,
+                                         const oeb_memref3d_f64* pkc, double dt2, const oeb_domain* dom,
+                                         void* stream);
+OEB_API oeb_status oeb_fvtp2d_f64_host(const oeb_memref3d_f64* q_i, const oeb_memref3d_f64* q_j,
+                                       const oeb_memref3d_f64* fx1, const oeb_memref3d_f64* fx2,
+                                       const oeb_memref3d_f64* fy1, const oeb_memref3d_f64* fy2,
+                                       const oeb_memref3d_f64* q, const oeb_memref3d_f64* crx,
+                                       const oeb_memref3d_f64* cry, const oeb_memref3d_f64* ra_x,
+                                       const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx,
+                                       const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, double p1,
+                                       double p2, const oeb_domain* dom, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OEB_GB300_H */

@@ -1,0 +1,85 @@
+"""Builds liboeb_gb300.so, the sm_103a stencil library, in-tree.
+
+One nvcc invocation per translation unit (run in parallel), then one link.  Only
+``-gencode arch=compute_103a,code=sm_103a`` is emitted.  The FP64 translation units are
+compiled with ``--fmad=false`` so that no multiply-add is contracted, which keeps every
+FP64 result bit-identical to the reference compiled without FP contraction.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+REPO = PKG.parent
+BUILD_DIR = PKG / "_build"
+LIB = PKG / "liboeb_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+BASE_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "--expt-relaxed-constexpr", "-I", str(REPO / "include")]
+
+# Translation units and their extra flags.
+UNITS = {
+    "abi_common.cu": [],
+    "host_staging.cu": [],
+    "k_pointwise_f64.cu": ["--fmad=false"],
+    "k_hdiff_f64.cu": ["--fmad=false"],
+    "k_fastwavesuv_f64.cu": ["--fmad=false"],
+    "k_fvtp2d_f64.cu": ["--fmad=false"],
+}
+
+
+def nvcc() -> str:
+    cand = os.environ.get("NVCC") or "/usr/local/cuda/bin/nvcc"
+    return cand if Path(cand).exists() else "nvcc"
+
+
+def _run(cmd):
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("nvcc failed: %s\n%s\n%s" % (" ".join(cmd), proc.stdout, proc.stderr))
+    return proc.stdout + proc.stderr
+
+
+def _stale(target: Path, deps) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+    """Compile every unit that changed and link liboeb_gb300.so; returns its path."""
+    BUILD_DIR.mkdir(exist_ok=True)
+    headers = list(CSRC.glob("*.cuh")) + [REPO / "include" / "oeb_gb300.h"]
+    units = [u for u in UNITS if (CSRC / u).exists()]
+    jobs = []
+    for u in units:
+        src = CSRC / u
+        obj = BUILD_DIR / (src.stem + ".o")
+        if force or _stale(obj, [src, *headers]):
+            flags = BASE_FLAGS + UNITS[u] + (["-Xptxas", "-v"] if verbose_ptxas else [])
+            jobs.append((u, [nvcc(), *ARCH, *flags, "-c", str(src), "-o", str(obj)]))
+    logs = {}
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            for (u, _), out in zip(jobs, ex.map(lambda j: _run(j[1]), jobs)):
+                logs[u] = out
+    objs = [BUILD_DIR / (Path(u).stem + ".o") for u in units]
+    if force or jobs or _stale(LIB, objs):
+        tmp = LIB.with_suffix(".so.tmp")
+        _run([nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])
+        os.replace(tmp, LIB)
+    if verbose_ptxas:
+        for u, out in logs.items():
+            sys.stderr.write("==== %s\n%s" % (u, out))
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))

@@ -1,0 +1,263 @@
+// abi_common.cu -- status strings, error bookkeeping, descriptor validation and device
+// storage allocation for the C ABI declared in include/oeb_gb300.h.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <limits>
+#include <mutex>
+#include <set>
+#include <utility>
+#include <vector>
+
+#include "oeb_common.cuh"
+
+namespace oeb {
+
+namespace {
+thread_local char g_last_cuda_error[256] = "";
+thread_local int g_validate_only = 0;
+std::atomic<uint64_t> g_launches{0};
+}  // namespace
+
+bool validating() { return g_validate_only > 0; }
+ValidateOnly::ValidateOnly() { ++g_validate_only; }
+ValidateOnly::~ValidateOnly() { --g_validate_only; }
+
+oeb_status cuda_fail(cudaError_t err) {
+  snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s: %s", cudaGetErrorName(err), cudaGetErrorString(err));
+  return OEB_ERR_CUDA;
+}
+
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+oeb_status after_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e);
+  count_launches(1);
+  return OEB_OK;
+}
+
+oeb_status ensure_dyn_smem(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e);
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({kernel, dev})) return OEB_OK;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return cuda_fail(e);
+  done.insert({kernel, dev});
+  return OEB_OK;
+}
+
+oeb_status check_domain(const oeb_domain* dom) {
+  if (!dom) return OEB_ERR_NULL;
+  const int64_t lim = std::numeric_limits<int32_t>::max() / 2;
+  if (dom->nx < 1 || dom->ny < 1 || dom->nz < 1) return OEB_ERR_DOMAIN;
+  if (dom->nx > lim || dom->ny > lim || dom->nz > lim) return OEB_ERR_DOMAIN;
+  return OEB_OK;
+}
+
+// A descriptor is accepted when strides[2] == 1, rows do not overlap
+// (strides[1] >= sizes[2]) and planes do not overlap (strides[0] >= strides[1]*sizes[1]).
+// Its offset then splits uniquely into the halo widths hk*strides[0] + hj*strides[1] + hi,
+// as allocateStorage builds it (include/util.h:136).  The required box must lie inside
+// [-h, size-h) on each axis.
+template <class T, class M>
+oeb_status check_field3(const M* m, const oeb_domain& d, const Reach& r, Grid<T>* g) {
+  if (!m || !m->aligned) return OEB_ERR_NULL;
+  if (reinterpret_cast<uintptr_t>(m->aligned) % alignof(T) != 0) return OEB_ERR_ALIGNMENT;
+  const int64_t szk = m->sizes[0], szj = m->sizes[1], szi = m->sizes[2];
+  const int64_t sk = m->strides[0], sj = m->strides[1], si = m->strides[2];
+  if (si != 1) return OEB_ERR_LAYOUT;
+  if (szi < 1 || szj < 1 || szk < 1) return OEB_ERR_LAYOUT;
+  if (sj < szi || sk < sj * szj) return OEB_ERR_LAYOUT;
+  // 32-bit in-plane index arithmetic in the kernels.
+  if (sk > std::numeric_limits<int32_t>::max()) return OEB_ERR_DOMAIN;
+  if (m->offset < 0) return OEB_ERR_HALO;
+  const int64_t hk = m->offset / sk;
+  const int64_t rem = m->offset % sk;
+  const int64_t hj = rem / sj;
+  const int64_t hi = rem % sj;
+  if (hi >= szi || hj >= szj || hk >= szk) return OEB_ERR_HALO;
+  // box [-lo, n-1+hi] on each axis must fit in [-h, size-h-1]
+  if (r.ilo > hi || r.jlo > hj || r.klo > hk) return OEB_ERR_HALO;
+  if (d.nx + r.ihi > szi - hi || d.ny + r.jhi > szj - hj || d.nz + r.khi > szk - hk) return OEB_ERR_HALO;
+  g->origin = m->aligned + m->offset;
+  g->sj = sj;
+  g->sk = sk;
+  const int64_t first = -(int64_t)r.ilo - (int64_t)r.jlo * sj - (int64_t)r.klo * sk;
+  const int64_t last = (d.nx - 1 + r.ihi) + (d.ny - 1 + r.jhi) * sj + (d.nz - 1 + r.khi) * sk;
+  g->lo = reinterpret_cast<const char*>(g->origin + first);
+  g->hi = reinterpret_cast<const char*>(g->origin + last + 1);
+  return OEB_OK;
+}
+
+template <class T, class M>
+oeb_status check_field1(const M* m, const oeb_domain& d, int jlo, int jhi, Line<T>* l) {
+  if (!m || !m->aligned) return OEB_ERR_NULL;
+  if (reinterpret_cast<uintptr_t>(m->aligned) % alignof(T) != 0) return OEB_ERR_ALIGNMENT;
+  const int64_t s = m->strides[0];
+  if (s < 1 || m->sizes[0] < 1) return OEB_ERR_LAYOUT;
+  if (m->offset < 0 || m->offset % s != 0) return OEB_ERR_HALO;
+  const int64_t h = m->offset / s;
+  if (jlo > h || d.ny + jhi > m->sizes[0] - h) return OEB_ERR_HALO;
+  l->origin = m->aligned + m->offset;
+  l->s = s;
+  l->lo = reinterpret_cast<const char*>(l->origin - (int64_t)jlo * s);
+  l->hi = reinterpret_cast<const char*>(l->origin + (d.ny - 1 + jhi) * s + 1);
+  return OEB_OK;
+}
+
+template <class T>
+oeb_status check_same_strides(std::initializer_list<const Grid<T>*> grids) {
+  const Grid<T>* first = *grids.begin();
+  for (const Grid<T>* g : grids)
+    if (g->sj != first->sj || g->sk != first->sk) return OEB_ERR_LAYOUT;
+  return OEB_OK;
+}
+
+// Ranges come as flat lists of (lo, hi) pairs.
+oeb_status check_no_alias(std::initializer_list<const char*> outs, std::initializer_list<const char*> ins) {
+  std::vector<const char*> o(outs), in(ins);
+  for (size_t a = 0; a + 1 < o.size(); a += 2) {
+    for (size_t b = a + 2; b + 1 < o.size(); b += 2)
+      if (o[a] < o[b + 1] && o[b] < o[a + 1]) return OEB_ERR_ALIAS;
+    for (size_t b = 0; b + 1 < in.size(); b += 2)
+      if (o[a] < in[b + 1] && in[b] < o[a + 1]) return OEB_ERR_ALIAS;
+  }
+  return OEB_OK;
+}
+
+template oeb_status check_field3<double, oeb_memref3d_f64>(const oeb_memref3d_f64*, const oeb_domain&, const Reach&,
+                                                          Grid<double>*);
+template oeb_status check_field3<float, oeb_memref3d_f32>(const oeb_memref3d_f32*, const oeb_domain&, const Reach&,
+                                                         Grid<float>*);
+template oeb_status check_field1<double, oeb_memref1d_f64>(const oeb_memref1d_f64*, const oeb_domain&, int, int,
+                                                          Line<double>*);
+template oeb_status check_field1<float, oeb_memref1d_f32>(const oeb_memref1d_f32*, const oeb_domain&, int, int,
+                                                         Line<float>*);
+template oeb_status check_same_strides<double>(std::initializer_list<const Grid<double>*>);
+template oeb_status check_same_strides<float>(std::initializer_list<const Grid<float>*>);
+
+}  // namespace oeb
+
+// ---------------------------------------------------------------------------------------
+// C ABI: information, errors, storage
+// ---------------------------------------------------------------------------------------
+
+extern "C" int oeb_abi_version(void) { return 10000; }
+
+extern "C" const char* oeb_status_string(int status) {
+  switch (status) {
+    case OEB_OK: return "ok";
+    case OEB_ERR_NULL: return "a required descriptor or pointer is NULL";
+    case OEB_ERR_DOMAIN: return "invalid interior extents";
+    case OEB_ERR_LAYOUT: return "unsupported or mismatched field layout";
+    case OEB_ERR_HALO: return "field halo smaller than the kernel's reach";
+    case OEB_ERR_ALIGNMENT: return "pointer not aligned to its element size";
+    case OEB_ERR_CUDA: return "CUDA runtime error";
+    case OEB_ERR_ALLOC: return "allocation failed";
+    case OEB_ERR_ALIAS: return "an output overlaps another field";
+    case OEB_ERR_UNSUPPORTED: return "unsupported kernel or variant";
+    case OEB_ERR_TIMEOUT: return "bounded device wait gave up";
+    case OEB_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
+    case OEB_ERR_ARGUMENT: return "scalar argument out of range";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char* oeb_last_cuda_error(void) { return oeb::g_last_cuda_error; }
+
+extern "C" uint64_t oeb_launch_count(void) { return oeb::g_launches.load(std::memory_order_relaxed); }
+
+namespace {
+
+template <class T, class M>
+oeb_status alloc3(int64_t nx, int64_t ny, int64_t nz, int64_t halo, int64_t pitch_multiple, M* out) {
+  if (!out) return OEB_ERR_NULL;
+  if (nx < 1 || ny < 1 || nz < 1 || halo < 0 || pitch_multiple < 1) return OEB_ERR_ARGUMENT;
+  const int64_t szi = nx + 2 * halo, szj = ny + 2 * halo, szk = nz + 2 * halo;
+  const int64_t pitch = (szi + pitch_multiple - 1) / pitch_multiple * pitch_multiple;
+  const int64_t n = pitch * szj * szk;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, (size_t)n * sizeof(T));
+  if (e != cudaSuccess) {
+    oeb::cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  out->allocated = static_cast<T*>(p);
+  out->aligned = static_cast<T*>(p);
+  out->sizes[0] = szk;
+  out->sizes[1] = szj;
+  out->sizes[2] = szi;
+  out->strides[2] = 1;
+  out->strides[1] = pitch;
+  out->strides[0] = pitch * szj;
+  out->offset = halo * out->strides[0] + halo * out->strides[1] + halo;  // util.h:136
+  return OEB_OK;
+}
+
+template <class T, class M>
+oeb_status alloc1(int64_t n, int64_t halo, M* out) {
+  if (!out) return OEB_ERR_NULL;
+  if (n < 1 || halo < 0) return OEB_ERR_ARGUMENT;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, (size_t)(n + 2 * halo) * sizeof(T));
+  if (e != cudaSuccess) {
+    oeb::cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  out->allocated = static_cast<T*>(p);
+  out->aligned = static_cast<T*>(p);
+  out->sizes[0] = n + 2 * halo;
+  out->strides[0] = 1;
+  out->offset = halo;  // util.h:105
+  return OEB_OK;
+}
+
+}  // namespace
+
+extern "C" oeb_status oeb_storage3d_alloc_f64(int64_t nx, int64_t ny, int64_t nz, int64_t halo, int64_t pm,
+                                              oeb_memref3d_f64* out) {
+  return alloc3<double>(nx, ny, nz, halo, pm, out);
+}
+extern "C" oeb_status oeb_storage1d_alloc_f64(int64_t n, int64_t halo, oeb_memref1d_f64* out) {
+  return alloc1<double>(n, halo, out);
+}
+extern "C" oeb_status oeb_storage3d_alloc_f32(int64_t nx, int64_t ny, int64_t nz, int64_t halo, int64_t pm,
+                                              oeb_memref3d_f32* out) {
+  return alloc3<float>(nx, ny, nz, halo, pm, out);
+}
+extern "C" oeb_status oeb_storage1d_alloc_f32(int64_t n, int64_t halo, oeb_memref1d_f32* out) {
+  return alloc1<float>(n, halo, out);
+}
+
+// All four descriptor types start with {allocated, aligned}; freeing needs only those.
+extern "C" oeb_status oeb_storage_free(void* memref) {
+  if (!memref) return OEB_ERR_NULL;
+  void** ptrs = static_cast<void**>(memref);
+  if (ptrs[0]) {
+    cudaError_t e = cudaFree(ptrs[0]);
+    if (e != cudaSuccess) return oeb::cuda_fail(e);
+  }
+  ptrs[0] = nullptr;
+  ptrs[1] = nullptr;
+  return OEB_OK;
+}
+
+// Bytes from `allocated` to one past the last element of the descriptor's box; the box
+// starts at aligned[0] for every allocateStorage-style descriptor (include/util.h:136-139).
+template <class M, class T>
+static int64_t span_bytes(const M* m) {
+  if (!m || !m->aligned || !m->allocated) return 0;
+  const int64_t last = (m->sizes[0] - 1) * m->strides[0] + (m->sizes[1] - 1) * m->strides[1] +
+                       (m->sizes[2] - 1) * m->strides[2];
+  return (int64_t)((m->aligned + last + 1) - m->allocated) * (int64_t)sizeof(T);
+}
+
+extern "C" int64_t oeb_memref3d_span_bytes_f64(const oeb_memref3d_f64* m) { return span_bytes<oeb_memref3d_f64, double>(m); }
+extern "C" int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m) { return span_bytes<oeb_memref3d_f32, float>(m); }

@@ -1,0 +1,318 @@
+// host_staging.cu -- host-buffer entry points oeb_<k>_f64_host.
+//
+// These take the same descriptors as the device entry points, but pointing to HOST memory
+// (for instance fields made by the reference's allocateStorage, include/util.h:126-141).
+// Each call copies every input descriptor's whole span (allocatedPtr to its last element)
+// to device memory from a library-owned stream-ordered pool, rebases the descriptors, runs
+// the device entry point, copies back exactly the box each output is written over (one
+// cudaMemcpy3DAsync per output), returns the device memory to the pool and synchronises
+// the stream.  Cells outside the written boxes are never written, as in the reference.
+// Pinned host memory makes the copies DMA transfers; pageable memory also works.
+#include <mutex>
+#include <vector>
+
+#include "oeb_reach.cuh"
+
+namespace oeb {
+namespace {
+
+// One memory pool per device, kept for the life of the process (release threshold at the
+// maximum, so repeated calls reuse the same device memory).
+oeb_status pool_for_current_device(cudaMemPool_t* out) {
+  static std::mutex mu;
+  static std::vector<cudaMemPool_t> pools;
+  int dev = 0;
+  OEB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)pools.size() <= dev) pools.resize(dev + 1, nullptr);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    OEB_CUDA_TRY(cudaMemPoolCreate(&p, &props));
+    uint64_t threshold = ~0ull;
+    OEB_CUDA_TRY(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &threshold));
+    pools[dev] = p;
+  }
+  *out = pools[dev];
+  return OEB_OK;
+}
+
+template <class T>
+const T* span_start(const T* allocated, const T* aligned) {
+  return (allocated && allocated <= aligned) ? allocated : aligned;
+}
+
+// Number of elements from the span start to one past the descriptor's last element; the
+// descriptor's box starts at aligned[0] (include/util.h:136-139).
+template <class M>
+int64_t span_elems3(const M* m) {
+  const int64_t last = (m->sizes[0] - 1) * m->strides[0] + (m->sizes[1] - 1) * m->strides[1] +
+                       (m->sizes[2] - 1) * m->strides[2];
+  return (int64_t)(m->aligned - span_start(m->allocated, m->aligned)) + last + 1;
+}
+template <class M>
+int64_t span_elems1(const M* m) {
+  return (int64_t)(m->aligned - span_start(m->allocated, m->aligned)) + (m->sizes[0] - 1) * m->strides[0] + 1;
+}
+
+template <class M>
+bool sane3(const M* m) {
+  return m && m->aligned && m->sizes[0] > 0 && m->sizes[1] > 0 && m->sizes[2] > 0 && m->strides[0] > 0 &&
+         m->strides[1] > 0 && m->strides[2] > 0;
+}
+template <class M>
+bool sane1(const M* m) {
+  return m && m->aligned && m->sizes[0] > 0 && m->strides[0] > 0;
+}
+
+template <class M3>
+struct OutSpec {
+  const M3* host;
+  Reach box;
+};
+
+// Stream-ordered staging of one call.  Device buffers are returned to the pool on every
+// exit path, after all work that uses them has been enqueued.
+template <class T>
+class Stager {
+ public:
+  Stager(cudaStream_t s, cudaMemPool_t pool) : s_(s), pool_(pool) {}
+  ~Stager() {
+    for (void* p : bufs_) cudaFreeAsync(p, s_);
+  }
+
+  template <class M>
+  oeb_status in(const M* host, int64_t elems, M* dev, bool copy) {
+    void* buf = nullptr;
+    const size_t bytes = (size_t)elems * sizeof(T);
+    cudaError_t e = cudaMallocFromPoolAsync(&buf, bytes, pool_, s_);
+    if (e != cudaSuccess) {
+      cuda_fail(e);
+      return OEB_ERR_ALLOC;
+    }
+    bufs_.push_back(buf);
+    const T* start = span_start(host->allocated, host->aligned);
+    if (copy) OEB_CUDA_TRY(cudaMemcpyAsync(buf, start, bytes, cudaMemcpyHostToDevice, s_));
+    *dev = *host;
+    T* base = static_cast<T*>(buf);
+    dev->aligned = base + (host->aligned - start);
+    dev->allocated = base;
+    return OEB_OK;
+  }
+
+ private:
+  cudaStream_t s_;
+  cudaMemPool_t pool_;
+  std::vector<void*> bufs_;
+};
+
+// Copies the written box of one output from device to host.
+template <class T, class M3>
+oeb_status copy_box_back(const M3* host, const M3* dev, const oeb_domain& d, const Reach& r, cudaStream_t s) {
+  const int64_t sj = host->strides[1], sk = host->strides[0];
+  const int64_t first = host->offset - r.ilo - r.jlo * sj - r.klo * sk;
+  const size_t width = (size_t)(d.nx + r.ilo + r.ihi) * sizeof(T);
+  const size_t rows = (size_t)(d.ny + r.jlo + r.jhi);
+  const size_t planes = (size_t)(d.nz + r.klo + r.khi);
+  T* hsrc = host->aligned + first;
+  T* dsrc = dev->aligned + first;
+  if (sk % sj == 0) {
+    cudaMemcpy3DParms p = {};
+    p.srcPtr = make_cudaPitchedPtr(dsrc, (size_t)sj * sizeof(T), width, (size_t)(sk / sj));
+    p.dstPtr = make_cudaPitchedPtr(hsrc, (size_t)sj * sizeof(T), width, (size_t)(sk / sj));
+    p.extent = make_cudaExtent(width, rows, planes);
+    p.kind = cudaMemcpyDeviceToHost;
+    OEB_CUDA_TRY(cudaMemcpy3DAsync(&p, s));
+  } else {
+    for (size_t k = 0; k < planes; ++k)
+      OEB_CUDA_TRY(cudaMemcpy2DAsync(hsrc + k * sk, (size_t)sj * sizeof(T), dsrc + k * sk, (size_t)sj * sizeof(T),
+                                     width, rows, cudaMemcpyDeviceToHost, s));
+  }
+  return OEB_OK;
+}
+
+constexpr int kMaxFields = 16;
+
+// Stages the inputs (3-D and 1-D) and outputs of one call, runs `launch` on the device
+// descriptors and copies the outputs back.
+template <class T, class M3, class M1, class Launch>
+oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<const M3*> in3,
+                    std::initializer_list<const M1*> in1, std::initializer_list<OutSpec<M3>> out3, Launch&& launch) {
+  OEB_TRY(check_domain(dom));
+  for (const M3* m : in3)
+    if (!sane3(m)) return m ? OEB_ERR_LAYOUT : OEB_ERR_NULL;
+  for (const M1* m : in1)
+    if (!sane1(m)) return m ? OEB_ERR_LAYOUT : OEB_ERR_NULL;
+  for (const OutSpec<M3>& o : out3)
+    if (!sane3(o.host)) return o.host ? OEB_ERR_LAYOUT : OEB_ERR_NULL;
+  if (in3.size() > (size_t)kMaxFields || in1.size() > (size_t)kMaxFields || out3.size() > (size_t)kMaxFields)
+    return OEB_ERR_TOO_LARGE;
+  M3 d3[kMaxFields];
+  M1 d1[kMaxFields];
+  M3 o3[kMaxFields];
+  {
+    // Validate the host descriptors with the device entry point's own checks, before any
+    // allocation or copy (the descriptors are identical up to the base pointers).
+    int n = 0;
+    for (const M3* m : in3) d3[n++] = *m;
+    n = 0;
+    for (const M1* m : in1) d1[n++] = *m;
+    n = 0;
+    for (const OutSpec<M3>& o : out3) o3[n++] = *o.host;
+    ValidateOnly guard;
+    OEB_TRY(launch(d3, d1, o3));
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaMemPool_t pool = nullptr;
+  OEB_TRY(pool_for_current_device(&pool));
+  oeb_status st = OEB_OK;
+  {
+    Stager<T> stage(s, pool);
+    int n = 0;
+    for (const M3* m : in3) {
+      st = stage.in(m, span_elems3(m), &d3[n++], true);
+      if (st != OEB_OK) break;
+    }
+    n = 0;
+    for (const M1* m : in1) {
+      if (st != OEB_OK) break;
+      st = stage.in(m, span_elems1(m), &d1[n++], true);
+    }
+    n = 0;
+    for (const OutSpec<M3>& o : out3) {
+      if (st != OEB_OK) break;
+      st = stage.in(o.host, span_elems3(o.host), &o3[n++], false);
+    }
+    if (st == OEB_OK) st = launch(d3, d1, o3);
+    if (st == OEB_OK) {
+      n = 0;
+      for (const OutSpec<M3>& o : out3) {
+        st = copy_box_back<T>(o.host, &o3[n++], *dom, o.box, s);
+        if (st != OEB_OK) break;
+      }
+    }
+  }  // device buffers returned to the pool here (stream-ordered)
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (st == OEB_OK && e != cudaSuccess) st = cuda_fail(e);
+  return st;
+}
+
+using M3 = oeb_memref3d_f64;
+using M1 = oeb_memref1d_f64;
+
+}  // namespace
+}  // namespace oeb
+
+using namespace oeb;
+
+extern "C" oeb_status oeb_laplace_f64_host(const M3* in, const M3* out, const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {in}, {}, {{out, kInterior}},
+                                  [&](const M3* i3, const M1*, const M3* o3) {
+                                    return oeb_laplace_f64(&i3[0], &o3[0], dom, stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_hdiffsa_f64_host(const M3* out, const M3* in, const M3* mask, const M1* crlato,
+                                           const M1* crlatu, const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {in, mask}, {crlato, crlatu}, {{out, kInterior}},
+                                  [&](const M3* i3, const M1* i1, const M3* o3) {
+                                    return oeb_hdiffsa_f64(&o3[0], &i3[0], &i3[1], &i1[0], &i1[1], dom, stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_hdiffsmag_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
+                                             const M3* mask, const M1* crlavo, const M1* crlavu, const M1* crlato,
+                                             const M1* crlatu, const M1* acrlat0, double eddlat, double eddlon,
+                                             double tau_smag, double weight_smag, const oeb_domain* dom,
+                                             void* stream) {
+  return run_host<double, M3, M1>(
+      dom, stream, {uin, vin, mask}, {crlavo, crlavu, crlato, crlatu, acrlat0}, {{uout, kInterior}, {vout, kInterior}},
+      [&](const M3* i3, const M1* i1, const M3* o3) {
+        return oeb_hdiffsmag_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i1[0], &i1[1], &i1[2], &i1[3], &i1[4],
+                                 eddlat, eddlon, tau_smag, weight_smag, dom, stream);
+      });
+}
+
+extern "C" oeb_status oeb_hadvuv_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
+                                          const M1* acrlat0, const M1* acrlat1, const M1* tgrlatda0,
+                                          const M1* tgrlatda1, double eddlat, double eddlon, const oeb_domain* dom,
+                                          void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1},
+                                  {{uout, kInterior}, {vout, kInterior}},
+                                  [&](const M3* i3, const M1* i1, const M3* o3) {
+                                    return oeb_hadvuv_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2],
+                                                          &i1[3], eddlat, eddlon, dom, stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_hadvuv5th_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
+                                             const M1* acrlat0, const M1* acrlat1, const M1* tgrlatda0,
+                                             const M1* tgrlatda1, double eddlat, double eddlon, const oeb_domain* dom,
+                                             void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1},
+                                  {{uout, kInterior}, {vout, kInterior}},
+                                  [&](const M3* i3, const M1* i1, const M3* o3) {
+                                    return oeb_hadvuv5th_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2],
+                                                             &i1[3], eddlat, eddlon, dom, stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_fastwavesuv_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
+                                               const M3* utens, const M3* vtens, const M3* wgtfac, const M3* ppuv,
+                                               const M3* hhl, const M3* rho, const M1* fx, double edadlat, double dt,
+                                               const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho}, {fx},
+                                  {{uout, kInterior}, {vout, kInterior}},
+                                  [&](const M3* i3, const M1* i1, const M3* o3) {
+                                    return oeb_fastwavesuv_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
+                                                               &i3[5], &i3[6], &i3[7], &i1[0], edadlat, dt, dom,
+                                                               stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_uvbke_f64_host(const M3* ub, const M3* vb, const M3* uc, const M3* vc, const M3* cosa,
+                                         const M3* rsina, double dt5, const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {uc, vc, cosa, rsina}, {}, {{ub, kInterior}, {vb, kInterior}},
+                                  [&](const M3* i3, const M1*, const M3* o3) {
+                                    return oeb_uvbke_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], dt5, dom,
+                                                         stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_nh_p_grad_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
+                                             const M3* rdx, const M3* rdy, const M3* gz, const M3* pp, const M3* pk3,
+                                             const M3* wk1, double dt, const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {uin, vin, rdx, rdy, gz, pp, pk3, wk1}, {},
+                                  {{uout, kInterior}, {vout, kInterior}},
+                                  [&](const M3* i3, const M1*, const M3* o3) {
+                                    return oeb_nh_p_grad_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
+                                                             &i3[5], &i3[6], &i3[7], dt, dom, stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_p_grad_c_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
+                                            const M3* rdxc, const M3* rdyc, const M3* delpc, const M3* gz,
+                                            const M3* pkc, double dt2, const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(dom, stream, {uin, vin, rdxc, rdyc, delpc, gz, pkc}, {},
+                                  {{uout, kInterior}, {vout, kInterior}},
+                                  [&](const M3* i3, const M1*, const M3* o3) {
+                                    return oeb_p_grad_c_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
+                                                            &i3[5], &i3[6], dt2, dom, stream);
+                                  });
+}
+
+extern "C" oeb_status oeb_fvtp2d_f64_host(const M3* q_i, const M3* q_j, const M3* fx1, const M3* fx2, const M3* fy1,
+                                          const M3* fy2, const M3* q, const M3* crx, const M3* cry, const M3* ra_x,
+                                          const M3* ra_y, const M3* xfx, const M3* yfx, const M3* area, double p1,
+                                          double p2, const oeb_domain* dom, void* stream) {
+  return run_host<double, M3, M1>(
+      dom, stream, {q, crx, cry, ra_x, ra_y, xfx, yfx, area}, {},
+      {{q_i, kFvQi}, {q_j, kFvQj}, {fx1, kInterior}, {fx2, kFvFx2}, {fy1, kInterior}, {fy2, kFvFy2}},
+      [&](const M3* i3, const M1*, const M3* o3) {
+        return oeb_fvtp2d_f64(&o3[0], &o3[1], &o3[2], &o3[3], &o3[4], &o3[5], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
+                              &i3[5], &i3[6], &i3[7], p1, p2, dom, stream);
+      });
+}

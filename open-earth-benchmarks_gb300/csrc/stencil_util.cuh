@@ -1,0 +1,55 @@
+// stencil_util.cuh -- device helpers shared by the stencil kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "oeb_common.cuh"
+
+namespace oeb {
+
+// Threads per CTA of every tiled kernel: 32 lanes along i times 8 rows along j.
+constexpr int kTX = 32;
+constexpr int kTY = 8;
+constexpr int kThreads = kTX * kTY;
+
+// Runs f(a, b) for every cell (a, b) of a W x H region of a shared-memory tile, spread
+// over the CTA's threads (a along i, fastest).
+template <int W, int H, class F>
+__device__ __forceinline__ void for_region(F&& f) {
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+#pragma unroll 1
+  for (int e = tid; e < W * H; e += kThreads) {
+    const int b = e / W;
+    const int a = e - b * W;
+    f(a, b);
+  }
+}
+
+// Read-only global load through the non-coherent path.
+template <class T>
+__device__ __forceinline__ T ld(const T* p) {
+  return __ldg(p);
+}
+
+// std::min(0.5, std::max(0.0, x)) with libstdc++'s comparisons (hdiffsmag.h:236, :251):
+// max(a,b) = (a < b) ? b : a, min(a,b) = (b < a) ? b : a.
+template <class T>
+__device__ __forceinline__ T clamp_smag(T x) {
+  const T lo = (T(0.0) < x) ? x : T(0.0);
+  return (lo < T(0.5)) ? lo : T(0.5);
+}
+
+// 1 / EARTH_RADIUS folded at compile time in the element type (include/util.h:17-18).
+template <class T>
+__host__ __device__ constexpr T earth_radius_recip() {
+  return T(1.0) / T(6371.229e3);
+}
+
+// Grid of a tiled kernel: one CTA per TI x TJ tile of the (i, j) region
+// [ilo, ilo+ni) x [jlo, jlo+nj) and per kb k-levels.
+inline dim3 tile_grid(int ni, int nj, int nz, int ti, int tj, int kb) {
+  return dim3((unsigned)((ni + ti - 1) / ti), (unsigned)((nj + tj - 1) / tj), (unsigned)((nz + kb - 1) / kb));
+}
+
+}  // namespace oeb

@@ -1,0 +1,224 @@
+"""Seeded synthetic inputs for the stencils.
+
+The reference fills its inputs analytically (``fillMath``, include/util.h:150-188) over the
+i/j halo but leaves the k-halo planes unset (util.h:159), although fastwavesuv, nh_p_grad
+and p_grad_c read k-1 or k+1 there.  Every generator here fills every cell of the
+allocation, halo included on all three axes, deterministically from a seed.
+
+Workloads (sizes are interior extents; the halo is 3 cells on every side):
+
+* ``smooth``   -- 64x64x60-style field for laplace/hdiffsa: a sum of three random-phase
+                  sin(2 pi kx i/N) cos(2 pi ky j/N) modes (kx, ky in 1..4) plus U[0, 1e-3)
+                  noise; crlato/crlatu = 1 + 0.1 U[0,1); mask = U[0, 0.025).
+* ``physical`` -- all ten kernels: velocities 10 x smooth modes + N(0, 0.1); pressure-like
+                  and geopotential-like fields monotone in k (1000 -> 100 hPa) with a 1 %
+                  smooth perturbation, so the thickness denominators stay away from 0;
+                  fvtp2d Courant numbers and mass fluxes scaled to |c| <= 0.8 with a
+                  zero-mean tracer q so the PPM limiter fires; scalars U[0.01, 0.1).
+* ``fronts``   -- ``physical`` plus steep tanh fronts (width 2 cells) on every dynamic
+                  field, so limiters and upwind switches change branch often.
+"""
+from __future__ import annotations
+
+from typing import Dict, Optional
+
+import numpy as np
+
+from .specs import KERNELS, DRIVER_SCALARS
+
+HALO = 3
+
+
+class Grid:
+    """Index arrays over the whole allocation: i, j, k run over [-h, n+h)."""
+
+    def __init__(self, nx, ny, nz, halo):
+        self.nx, self.ny, self.nz, self.h = nx, ny, nz, halo
+        self.i = np.arange(-halo, nx + halo, dtype=np.float64)[None, None, :]
+        self.j = np.arange(-halo, ny + halo, dtype=np.float64)[None, :, None]
+        self.k = np.arange(-halo, nz + halo, dtype=np.float64)[:, None, None]
+        self.shape = (nz + 2 * halo, ny + 2 * halo, nx + 2 * halo)
+
+    def jline(self):
+        return np.arange(-self.h, self.ny + self.h, dtype=np.float64)
+
+
+def smooth_modes(g: Grid, rng: np.random.Generator, nmodes=3, kmax=4, vertical=True) -> np.ndarray:
+    """Sum of random-phase sin(kx i) cos(ky j) modes with a smooth vertical modulation."""
+    out = np.zeros(g.shape)
+    for _ in range(nmodes):
+        kx, ky = rng.integers(1, kmax + 1, size=2)
+        phi, psi, chi = rng.uniform(0, 2 * np.pi, size=3)
+        mode = np.sin(2 * np.pi * kx * g.i / g.nx + phi) * np.cos(2 * np.pi * ky * g.j / g.ny + psi)
+        if vertical:
+            kz = rng.integers(1, 3)
+            mode = mode * (1.0 + 0.5 * np.sin(2 * np.pi * kz * g.k / max(g.nz, 1) + chi))
+        out += mode
+    return out
+
+
+def tanh_front(g: Grid, rng: np.random.Generator, width=2.0) -> np.ndarray:
+    """A straight tanh front of the given width (cells) in a random direction and position."""
+    theta = rng.uniform(0, 2 * np.pi)
+    c = np.array([rng.uniform(0.25, 0.75) * g.nx, rng.uniform(0.25, 0.75) * g.ny])
+    dist = (g.i - c[0]) * np.cos(theta) + (g.j - c[1]) * np.sin(theta)
+    return np.broadcast_to(np.tanh(dist / width), g.shape).copy()
+
+
+def pressure_profile(g: Grid, rng, top=100.0, bottom=1000.0, pert=0.01) -> np.ndarray:
+    """Monotone in k from `bottom` (k=0) to `top` (k=nz-1), continued into the k-halo, with a
+    `pert` relative smooth perturbation."""
+    frac = g.k / max(g.nz - 1, 1)
+    base = bottom + (top - bottom) * frac
+    return base * (1.0 + pert * smooth_modes(g, rng, vertical=False) / 3.0)
+
+
+def _velocity(g, rng, fronts):
+    v = 10.0 * smooth_modes(g, rng) + rng.normal(0.0, 0.1, size=g.shape)
+    if fronts:
+        v += 10.0 * tanh_front(g, rng)
+    return v
+
+
+def _tracer(g, rng, fronts):
+    q = smooth_modes(g, rng) + rng.normal(0.0, 0.05, size=g.shape)
+    q -= q.mean()
+    if fronts:
+        q += tanh_front(g, rng)
+    return q
+
+
+def _courant(g, rng, fronts):
+    c = smooth_modes(g, rng) + rng.normal(0.0, 0.05, size=g.shape)
+    if fronts:
+        c += tanh_front(g, rng)
+    return 0.8 * c / np.max(np.abs(c))
+
+
+def _metric(g, rng):
+    return 1.0 + 0.1 * rng.uniform(0.0, 1.0, size=g.jline().shape)
+
+
+# Field classes per kernel input (physical/fronts workloads).
+_CLASSES = {
+    "laplace": {"in": "vel"},
+    "hdiffsa": {"in": "vel", "mask": "mask", "crlato": "metric", "crlatu": "metric"},
+    "hdiffsmag": {"uin": "vel", "vin": "vel", "mask": "unit", "crlavo": "metric", "crlavu": "metric",
+                  "crlato": "metric", "crlatu": "metric", "acrlat0": "metric"},
+    "hadvuv": {"uin": "vel", "vin": "vel", "acrlat0": "metric", "acrlat1": "metric", "tgrlatda0": "metric",
+               "tgrlatda1": "metric"},
+    "fastwavesuv": {"uin": "vel", "vin": "vel", "utens": "tend", "vtens": "tend", "wgtfac": "weight",
+                    "ppuv": "ppert", "hhl": "height", "rho": "density", "fx": "metric"},
+    "uvbke": {"uc": "vel", "vc": "vel", "cosa": "cosa", "rsina": "rsina"},
+    "nh_p_grad": {"uin": "vel", "vin": "vel", "rdx": "rdx", "rdy": "rdx", "gz": "geopot", "pp": "pres",
+                  "pk3": "pres", "wk1": "thick"},
+    "p_grad_c": {"uin": "vel", "vin": "vel", "rdxc": "rdx", "rdyc": "rdx", "delpc": "thick", "gz": "geopot",
+                 "pkc": "pres"},
+    "fvtp2d": {"q": "tracer", "crx": "courant", "cry": "courant", "ra_x": "area", "ra_y": "area", "xfx": "courant",
+               "yfx": "courant", "area": "area"},
+}
+_CLASSES["hadvuv5th"] = _CLASSES["hadvuv"]
+
+
+def _make(cls: str, g: Grid, rng, fronts: bool, rank: int) -> np.ndarray:
+    if rank == 1:
+        return _metric(g, rng)
+    if cls == "vel":
+        return _velocity(g, rng, fronts)
+    if cls == "tend":
+        return 1e-3 * _velocity(g, rng, fronts)
+    if cls == "mask":
+        return rng.uniform(0.0, 0.025, size=g.shape)
+    if cls == "unit":
+        return rng.uniform(0.0, 1.0, size=g.shape)
+    if cls == "weight":
+        return rng.uniform(0.4, 0.6, size=g.shape)
+    if cls == "ppert":
+        return 100.0 * smooth_modes(g, rng) + rng.normal(0.0, 1.0, size=g.shape)
+    if cls == "height":  # half-level heights decreasing with k, like COSMO's hhl
+        frac = g.k / max(g.nz, 1)
+        return 20000.0 * (1.0 - frac) * (1.0 + 0.01 * smooth_modes(g, rng, vertical=False) / 3.0)
+    if cls == "density":
+        return 1.2 * (1.0 + 0.01 * smooth_modes(g, rng))
+    if cls == "cosa":
+        return 0.2 * smooth_modes(g, rng) / 3.0
+    if cls == "rsina":
+        return 1.0 + 0.05 * smooth_modes(g, rng) / 3.0
+    if cls == "rdx":
+        return 1.0 + 0.1 * rng.uniform(0.0, 1.0, size=g.shape)
+    if cls == "geopot":  # g z with z rising from 1 km to 16 km over the column
+        return 9.81 * pressure_profile(g, rng, top=16000.0, bottom=1000.0)
+    if cls == "pres":
+        return pressure_profile(g, rng)
+    if cls == "thick":
+        return 10.0 * (1.0 + 0.01 * smooth_modes(g, rng))
+    if cls == "tracer":
+        return _tracer(g, rng, fronts)
+    if cls == "courant":
+        return _courant(g, rng, fronts)
+    if cls == "area":
+        return 1.0 + 0.1 * smooth_modes(g, rng) / 3.0
+    raise KeyError(cls)
+
+
+def smooth_config1(g: Grid, rng) -> np.ndarray:
+    """Sum of 3 random-phase sin cos modes + U[0, 1e-3) noise (the 64x64x60 workload)."""
+    return smooth_modes(g, rng, vertical=True) + rng.uniform(0.0, 1e-3, size=g.shape)
+
+
+def make_inputs(kernel: str, nx: int, ny: int, nz: int, seed: int, workload: str = "physical",
+                halo: int = HALO, dtype=np.float64) -> Dict[str, np.ndarray]:
+    """Input buffers (whole allocations, halo included) of `kernel`, keyed by argument name."""
+    spec = KERNELS[kernel]
+    g = Grid(nx, ny, nz, halo)
+    # one independent stream per (kernel, field) so a field does not depend on the others
+    out = {}
+    for idx, a in enumerate(spec.args):
+        if a.role not in ("in3", "in1"):
+            continue
+        rng = np.random.default_rng([seed, sum(map(ord, kernel)), idx])
+        rank = 3 if a.role == "in3" else 1
+        if workload == "smooth":
+            if rank == 1:
+                arr = _metric(g, rng)
+            elif a.name == "mask":
+                arr = rng.uniform(0.0, 0.025, size=g.shape)
+            else:
+                arr = smooth_config1(g, rng)
+        else:
+            arr = _make(_CLASSES[kernel][a.name], g, rng, workload == "fronts", rank)
+        out[a.name] = np.ascontiguousarray(arr, dtype=dtype)
+    return out
+
+
+def make_scalars(kernel: str, seed: int, workload: str = "physical") -> Dict[str, float]:
+    """Scalars: the reference drivers' values for ``driver``, else U[0.01, 0.1) (p1/p2 keep the
+    driver macros)."""
+    spec = KERNELS[kernel]
+    if workload == "driver":
+        return dict(DRIVER_SCALARS.get(kernel, {}))
+    rng = np.random.default_rng([seed, sum(map(ord, kernel)), 999])
+    vals = {}
+    for s in spec.scalars:
+        vals[s.name] = float(rng.uniform(0.01, 0.1))
+    if kernel == "fvtp2d":
+        vals.update(DRIVER_SCALARS["fvtp2d"])
+    return vals
+
+
+SENTINEL = -7.0e5  # fill of every output before a call: cells outside the written box keep it
+
+
+def make_outputs(kernel: str, nx: int, ny: int, nz: int, halo: int = HALO, dtype=np.float64,
+                 include_scratch: bool = False) -> Dict[str, np.ndarray]:
+    spec = KERNELS[kernel]
+    shape = (nz + 2 * halo, ny + 2 * halo, nx + 2 * halo)
+    out = {}
+    for a in spec.args:
+        if a.role == "out3" or (include_scratch and a.role == "scratch3"):
+            out[a.name] = np.full(shape, SENTINEL, dtype=dtype)
+    return out
+
+
+def points(nx, ny, nz) -> int:
+    return nx * ny * nz

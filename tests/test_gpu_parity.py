@@ -1,0 +1,131 @@
+"""Parity of the CUDA stencils with the oracle, through the C ABI, on the GPU.
+
+FP64 results must be bit-identical to the oracle (the C restatement of the reference's
+``_openmp`` kernels, itself pinned bit-exact to the reference in
+test_oracle_vs_reference.py): the FP64 kernels are compiled without FP contraction and
+IEEE division and square root round identically on both sides.  Every output buffer is
+compared whole, so cells outside the written box must also keep their pre-call value.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import assert_bitwise_equal
+
+pytestmark = pytest.mark.gpu
+
+H = 3
+KERNELS = ("laplace", "hdiffsa", "hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "uvbke", "nh_p_grad",
+           "p_grad_c", "fvtp2d")
+
+
+def _run_both(pkg, fields, orc, cuda, name, nx, ny, nz, seed, workload="physical", halo=H, pitch_multiple=1,
+              scalars=None):
+    import torch
+    spec = pkg.KERNELS[name]
+    inputs = fields.make_inputs(name, nx, ny, nz, seed=seed, workload=workload, halo=halo)
+    sc = scalars if scalars is not None else fields.make_scalars(name, seed=seed)
+    outs = fields.make_outputs(name, nx, ny, nz, halo=halo)
+    want = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+    orc.run_oracle(spec, want, sc, nx, ny, nz, halo)
+    dev = {}
+    for k, v in {**inputs, **outs}.items():
+        if v.ndim == 3 and pitch_multiple > 1:
+            st = pkg.Storage.allocate3d(nx, ny, nz, halo, device=cuda, pitch_multiple=pitch_multiple)
+            st.data[:, :, :v.shape[2]] = torch.from_numpy(v).to(cuda)
+            dev[k] = st
+        else:
+            dev[k] = pkg.Storage(torch.from_numpy(v).to(cuda), halo, nx=nx if v.ndim == 3 else None)
+    pkg.call(name, dev, sc, domain=(nx, ny, nz))
+    torch.cuda.synchronize()
+    for a in spec.by_role("out3"):
+        got = dev[a.name].numpy()[:, :, :nx + 2 * halo]
+        assert_bitwise_equal(np.ascontiguousarray(got), want[a.name], "%s.%s" % (name, a.name))
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_small_nonsquare(pkg, fields, orc, cuda, name):
+    _run_both(pkg, fields, orc, cuda, name, 40, 36, 5, seed=3)
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_tiny_domain(pkg, fields, orc, cuda, name):
+    _run_both(pkg, fields, orc, cuda, name, 1, 1, 1, seed=4)
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_ragged_multitile_fronts(pkg, fields, orc, cuda, name):
+    _run_both(pkg, fields, orc, cuda, name, 70, 97, 9, seed=5, workload="fronts")
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_halo4_padded_pitch(pkg, fields, orc, cuda, name):
+    # the reference drivers' halo of 4 (src/<k>.cpp:6) and rows padded to 16 elements
+    _run_both(pkg, fields, orc, cuda, name, 33, 31, 4, seed=6, halo=4, pitch_multiple=16)
+
+
+@pytest.mark.parametrize("name", ("laplace", "hdiffsa"))
+def test_config_64x64x60_smooth(pkg, fields, orc, cuda, name):
+    _run_both(pkg, fields, orc, cuda, name, 64, 64, 60, seed=0, workload="smooth")
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_config_128x128x80(pkg, fields, orc, cuda, name):
+    _run_both(pkg, fields, orc, cuda, name, 128, 128, 80, seed=1)
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_driver_scalars(pkg, fields, orc, cuda, name):
+    # the reference drivers' own scalar values (src/<k>.cpp)
+    _run_both(pkg, fields, orc, cuda, name, 48, 48, 6, seed=7, scalars=fields.make_scalars(name, 7, "driver"))
+
+
+@pytest.mark.parametrize("name", KERNELS)
+def test_host_entry_points(pkg, fields, orc, name):
+    """oeb_<k>_f64_host with host buffers: same bits, untouched cells preserved."""
+    spec = pkg.KERNELS[name]
+    nx, ny, nz = 37, 29, 4
+    inputs = fields.make_inputs(name, nx, ny, nz, seed=8)
+    sc = fields.make_scalars(name, seed=8)
+    outs = fields.make_outputs(name, nx, ny, nz)
+    want = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+    orc.run_oracle(spec, want, sc, nx, ny, nz, H)
+    host = {k: pkg.Storage(v.copy(), H) for k, v in {**inputs, **outs}.items()}
+    pkg.call(name, host, sc, domain=(nx, ny, nz))
+    for a in spec.by_role("out3"):
+        assert_bitwise_equal(host[a.name].data, want[a.name], "%s.%s (host path)" % (name, a.name))
+    for a in spec.by_role("in3"):
+        assert_bitwise_equal(host[a.name].data, inputs[a.name], "%s.%s input unchanged" % (name, a.name))
+
+
+def test_reference_named_api(pkg, fields, orc, cuda):
+    """The reference-named functions and their variants, with the module's domain globals."""
+    import torch
+    k = pkg.kernels
+    old = (k.domain_size, k.domain_height)
+    k.domain_size, k.domain_height = 24, 3
+    try:
+        inputs = fields.make_inputs("hdiffsa", 24, 24, 3, seed=9)
+        outs = fields.make_outputs("hdiffsa", 24, 24, 3)
+        want = {n: v.copy() for n, v in {**inputs, **outs}.items()}
+        orc.run_oracle(pkg.KERNELS["hdiffsa"], want, {}, 24, 24, 3, H)
+        for variant in ("hdiffsa", "hdiffsa_fullfusion", "hdiffsa_partialfusion", "hdiffsa_openmp"):
+            d = {n: pkg.Storage(torch.from_numpy(v).to(cuda), H) for n, v in {**inputs, **outs}.items()}
+            getattr(k, variant)(d["out"], d["in"], d["mask"], d["crlato"], d["crlatu"])
+            torch.cuda.synchronize()
+            assert_bitwise_equal(d["out"].numpy(), want["out"], variant)
+    finally:
+        k.domain_size, k.domain_height = old
+
+
+def test_launches_are_counted(pkg, fields, cuda):
+    import torch
+    lib = pkg.load_library()
+    before = lib.oeb_launch_count()
+    inputs = fields.make_inputs("laplace", 16, 16, 2, seed=1)
+    outs = fields.make_outputs("laplace", 16, 16, 2)
+    d = {n: pkg.Storage(torch.from_numpy(v).to(cuda), H) for n, v in {**inputs, **outs}.items()}
+    pkg.call("laplace", d, {}, domain=(16, 16, 2))
+    torch.cuda.synchronize()
+    assert lib.oeb_launch_count() == before + 1
