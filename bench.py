@@ -118,10 +118,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def _make_set(pkg, fields, torch, dev, seed, pinned=False):
+def _make_set(pkg, fields, torch, dev, seed, names, pinned=False):
     """Per kernel: (field Storages, scalars), every field a separate allocation."""
     out = {}
-    for name in pkg.KERNELS:
+    for name in names:
         inputs = fields.make_inputs(name, NX, NY, NZ, seed=seed)
         outs = fields.make_outputs(name, NX, NY, NZ)
         st = {}
@@ -152,8 +152,8 @@ def run_ours(args):
     import importlib
     fields = importlib.import_module("oeb_gb300.fields")
     lib = pkg.load_library()
-    names = list(pkg.KERNELS)
-    sets = [_make_set(pkg, fields, torch, dev, SEED + r) for r in range(2)]
+    names = [k for k in pkg.KERNELS if not args.kernels or k in args.kernels]
+    sets = [_make_set(pkg, fields, torch, dev, SEED + r, names) for r in range(2)]
     stream = torch.cuda.current_stream(dev)
     dom = (NX, NY, NZ)
 
@@ -253,7 +253,7 @@ def _ncu_traffic(kernel):
 
 def _e2e(pkg, fields, torch, args, names):
     """The step through the host entry points with pinned host buffers."""
-    hs = _make_set(pkg, fields, torch, None, SEED, pinned=True)
+    hs = _make_set(pkg, fields, torch, None, SEED, names, pinned=True)
     dom = (NX, NY, NZ)
     h2d = d2h = 0
     for name in names:
@@ -372,6 +372,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--kernels", nargs="*", default=None,
+                    help="run only these stencils in the step (profiling); the default line uses all ten")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         sys.stderr.write("warning: fewer than 3 warm-up steps\n")
