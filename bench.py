@@ -118,7 +118,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def _make_set(pkg, fields, torch, dev, seed, names, pinned=False):
+def _make_set(pkg, fields, torch, dev, seed, names, pinned=False, dtype=np.float64):
     """Per kernel: (field Storages, scalars), every field a separate allocation."""
     out = {}
     for name in names:
@@ -126,18 +126,54 @@ def _make_set(pkg, fields, torch, dev, seed, names, pinned=False):
         outs = fields.make_outputs(name, NX, NY, NZ)
         st = {}
         for k, v in {**inputs, **outs}.items():
-            t = torch.from_numpy(v)
+            t = torch.from_numpy(v.astype(dtype))
             if dev is not None:
                 t = t.to(dev)
             elif pinned:
                 t = t.pin_memory()
             st[k] = pkg.Storage(t, HALO)
-        out[name] = (st, fields.make_scalars(name, seed=seed))
+        sc = fields.make_scalars(name, seed=seed)
+        if dtype == np.float32:
+            sc = {k: (v if k == "dt5" else float(np.float32(v))) for k, v in sc.items()}
+        out[name] = (st, sc)
     return out
 
 
-def _algorithmic_bytes(pkg, name):
-    return pkg.KERNELS[name].bytes_per_point(8) * NX * NY * NZ
+def _time_steps(pkg, torch, sets, names, steps, warmup, stream, dom, clocks=None):
+    """Runs warm-up steps, then `steps` timed steps; returns total ms, per-kernel mean ms, launches."""
+    lib = pkg.load_library()
+
+    def step(s, ev=None):
+        for idx, name in enumerate(names):
+            st, sc = s[name]
+            if ev is not None:
+                ev[idx][0].record(stream)
+            pkg.call(name, st, sc, domain=dom, stream=stream)
+            if ev is not None:
+                ev[idx][1].record(stream)
+
+    for w in range(warmup):
+        step(sets[w % len(sets)])
+    torch.cuda.synchronize()
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in names]
+           for _ in range(steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    launches0 = lib.oeb_launch_count()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for s in range(steps):
+        step(sets[s % len(sets)], evs[s])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.oeb_launch_count() - launches0
+    per_kernel = {name: statistics.mean(evs[s][idx][0].elapsed_time(evs[s][idx][1]) for s in range(steps))
+                  for idx, name in enumerate(names)}
+    return t0.elapsed_time(t1), per_kernel, launches
+
+
+def _algorithmic_bytes(pkg, name, elem=8):
+    return pkg.KERNELS[name].bytes_per_point(elem) * NX * NY * NZ
 
 
 def run_ours(args):
@@ -156,36 +192,10 @@ def run_ours(args):
     sets = [_make_set(pkg, fields, torch, dev, SEED + r, names) for r in range(2)]
     stream = torch.cuda.current_stream(dev)
     dom = (NX, NY, NZ)
-
-    def step(s, ev=None):
-        for idx, name in enumerate(names):
-            st, sc = s[name]
-            if ev is not None:
-                ev[idx][0].record(stream)
-            pkg.call(name, st, sc, domain=dom, stream=stream)
-            if ev is not None:
-                ev[idx][1].record(stream)
-
-    for w in range(args.warmup):
-        step(sets[w % 2])
-    torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    # per-kernel events in every timed step
-    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in names]
-           for _ in range(args.steps)]
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    launches0 = lib.oeb_launch_count()
     with ClockSampler(local) as clocks:
-        torch.cuda.synchronize()
-        t0.record(stream)
-        for s in range(args.steps):
-            step(sets[s % 2], evs[s])
-        t1.record(stream)
-        torch.cuda.synchronize()
-    launches = lib.oeb_launch_count() - launches0
-    ms_total = t0.elapsed_time(t1)
+        ms_total, per_kernel, launches = _time_steps(pkg, torch, sets, names, args.steps, args.warmup, stream, dom)
     if world > 1:
         t = torch.tensor([ms_total], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -194,15 +204,34 @@ def run_ours(args):
     ms_step = ms_total / args.steps
     pts_step = len(names) * NX * NY * NZ
     value = world * pts_step * args.steps / (ms_total * 1e-3) / 1e9
-
-    per_kernel = {}
-    for idx, name in enumerate(names):
-        per_kernel[name] = statistics.mean(evs[s][idx][0].elapsed_time(evs[s][idx][1]) for s in range(args.steps))
     total_k = sum(per_kernel.values())
     dom_k = max(per_kernel, key=per_kernel.get)
     peak, peak_src = _measured_peak()
     achieved = _algorithmic_bytes(pkg, dom_k) / (per_kernel[dom_k] * 1e-3) / 1e9
     traffic = _ncu_traffic(dom_k)
+
+    del sets
+    torch.cuda.empty_cache()
+    f32 = None
+    if not args.no_f32:
+        sets32 = [_make_set(pkg, fields, torch, dev, SEED + r, names, dtype=np.float32) for r in range(2)]
+        ms32, pk32, l32 = _time_steps(pkg, torch, sets32, names, args.steps, args.warmup, stream, dom)
+        del sets32
+        torch.cuda.empty_cache()
+        d32 = max(pk32, key=pk32.get)
+        ach32 = _algorithmic_bytes(pkg, d32, 4) / (pk32[d32] * 1e-3) / 1e9
+        step_bytes32 = sum(_algorithmic_bytes(pkg, k, 4) for k in names)
+        f32 = {"value": round(pts_step * args.steps / (ms32 * 1e-3) / 1e9, 4), "unit": "GPts/s",
+               "ms_per_step": round(ms32 / args.steps, 4), "speedup_vs_f64": round(ms_total / ms32, 3),
+               "step_hbm_gbs": round(step_bytes32 / (ms32 / args.steps * 1e-3) / 1e9, 1),
+               "roofline": {"bound": "hbm", "kernel": d32, "achieved": round(ach32, 2), "peak": _measured_peak()[0],
+                            "unit": "GB/s", "frac": round(ach32 / _measured_peak()[0], 4)},
+               "per_kernel_ms": {k: round(v, 5) for k, v in pk32.items()},
+               "per_kernel_gbs": {k: round(_algorithmic_bytes(pkg, k, 4) / (v * 1e-3) / 1e9, 1)
+                                  for k, v in pk32.items()},
+               "gpu_launches": int(l32),
+               "note": "FP32 storage and arithmetic, exact limiter sign tests, compensated flux sums; "
+                       "normwise error vs the FP64 oracle is stated per kernel by tests/test_gpu_fp32.py"}
 
     e2e = None
     if not args.no_e2e:
@@ -229,6 +258,8 @@ def run_ours(args):
     }
     if e2e is not None:
         line["e2e"] = e2e
+    if f32 is not None:
+        line["f32"] = f32
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_baseline(pkg, fields, budget_s=args.cpu_seconds)
     if rank == 0:
@@ -371,6 +402,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-f32", action="store_true", help="skip the FP32-storage leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--kernels", nargs="*", default=None,
                     help="run only these stencils in the step (profiling); the default line uses all ten")

@@ -109,6 +109,11 @@ OEB_API const char* oeb_status_string(int status);
 OEB_API const char* oeb_last_cuda_error(void);
 /* Number of kernel launches this library has issued (all threads) since load.  */
 OEB_API uint64_t oeb_launch_count(void);
+/* 1 if `p` points to device (or managed) memory, 0 if to host memory; used by the C++
+ * drop-in headers to pick the device or the host-buffer entry point. */
+OEB_API int oeb_is_device_pointer(const void* p);
+/* Blocks until all work on `stream` has finished (NULL = legacy default stream). */
+OEB_API oeb_status oeb_stream_synchronize(void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* Device storage (the device twin of allocateStorage/freeStorage,           */
@@ -203,7 +208,7 @@ OEB_API oeb_status oeb_fvtp2d_f64(const oeb_memref3d_f64* q_i, const oeb_memref3
                           const oeb_memref3d_f64* fx2, const oeb_memref3d_f64* fy1, const oeb_memref3d_f64* fy2,
                           const oeb_memref3d_f64* q, const oeb_memref3d_f64* crx, const oeb_memref3d_f64* cry,
                           const oeb_memref3d_f64* ra_x, const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx,
-                          const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, double p1, double p2,
+                          const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, double ppm_p1, double ppm_p2,
                           const oeb_domain* dom, void* stream);
 
 /* ------------------------------------------------------------------------- */
@@ -265,8 +270,147 @@ OEB_API oeb_status oeb_fvtp2d_f64_host(const oeb_memref3d_f64* q_i, const oeb_me
                                        const oeb_memref3d_f64* q, const oeb_memref3d_f64* crx,
                                        const oeb_memref3d_f64* cry, const oeb_memref3d_f64* ra_x,
                                        const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx,
-                                       const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, double p1,
-                                       double p2, const oeb_domain* dom, void* stream);
+                                       const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, double ppm_p1,
+                                       double ppm_p2, const oeb_domain* dom, void* stream);
+
+
+/* ------------------------------------------------------------------------- */
+/* FP32 forward stencils: fields stored and computed in FP32.  Same arguments */
+/* as the FP64 entry points with float scalars (dt5 stays a double, as in     */
+/* the reference, src/uvbke.cpp:11-12).  Branch tests on the sign of a        */
+/* product (hdiffsa limiter, fvtp2d PPM flag) are decided on the exact        */
+/* product, and the hdiffsmag and advection flux sums are compensated, so the */
+/* results differ from the FP64 ones only by FP32 rounding of the data; they  */
+/* are not the reference compiled with ElementType = float.                   */
+/* ------------------------------------------------------------------------- */
+
+/* FP32 of kernels/laplace.h:4 -- laplace(in, out) */
+OEB_API oeb_status oeb_laplace_f32(const oeb_memref3d_f32* in, const oeb_memref3d_f32* out, const oeb_domain* dom,
+                           void* stream);
+
+/* FP32 of kernels/hdiffsa.h:4-5 -- hdiffsa(out, in, mask, crlato, crlatu, lap, flx, fly) */
+OEB_API oeb_status oeb_hdiffsa_f32(const oeb_memref3d_f32* out, const oeb_memref3d_f32* in, const oeb_memref3d_f32* mask,
+                           const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_domain* dom,
+                           void* stream);
+
+/* FP32 of kernels/hdiffsmag.h:4-7 -- hdiffsmag(uout, vout, uin, vin, mask, crlavo, crlavu, crlato, crlatu,
+ *                                      acrlat0, T_sqr_s, S_sqr_uv, eddlat, eddlon, tau_smag, weight_smag) */
+OEB_API oeb_status oeb_hdiffsmag_f32(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                             const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                             const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlavo,
+                             const oeb_memref1d_f32* crlavu, const oeb_memref1d_f32* crlato,
+                             const oeb_memref1d_f32* crlatu, const oeb_memref1d_f32* acrlat0, float eddlat,
+                             float eddlon, float tau_smag, float weight_smag, const oeb_domain* dom,
+                             void* stream);
+
+/* FP32 of kernels/hadvuv.h:29-32 -- hadvuv(uout, vout, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1,
+ *                                  uatupos, vatupos, uatvpos, vatvpos, uavg, vavg, ures, vres, eddlat, eddlon) */
+OEB_API oeb_status oeb_hadvuv_f32(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout, const oeb_memref3d_f32* uin,
+                          const oeb_memref3d_f32* vin, const oeb_memref1d_f32* acrlat0,
+                          const oeb_memref1d_f32* acrlat1, const oeb_memref1d_f32* tgrlatda0,
+                          const oeb_memref1d_f32* tgrlatda1, float eddlat, float eddlon, const oeb_domain* dom,
+                          void* stream);
+
+/* FP32 of kernels/hadvuv5th.h:41-44 -- hadvuv5th(same arguments as hadvuv) */
+OEB_API oeb_status oeb_hadvuv5th_f32(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                             const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                             const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                             const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1, float eddlat,
+                             float eddlon, const oeb_domain* dom, void* stream);
+
+/* FP32 of kernels/fastwavesuv.h:4-7 -- fastwavesuv(uout, vout, uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho, fx,
+ *                                          ppgk, ppgc, ppgu, ppgv, edadlat, dt) */
+OEB_API oeb_status oeb_fastwavesuv_f32(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                               const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                               const oeb_memref3d_f32* utens, const oeb_memref3d_f32* vtens,
+                               const oeb_memref3d_f32* wgtfac, const oeb_memref3d_f32* ppuv,
+                               const oeb_memref3d_f32* hhl, const oeb_memref3d_f32* rho, const oeb_memref1d_f32* fx,
+                               float edadlat, float dt, const oeb_domain* dom, void* stream);
+
+/* FP32 of kernels/uvbke.h:4-5 -- uvbke(ub, vb, uc, vc, cosa, rsina); dt5 is the driver global (src/uvbke.cpp:11-12) */
+OEB_API oeb_status oeb_uvbke_f32(const oeb_memref3d_f32* ub, const oeb_memref3d_f32* vb, const oeb_memref3d_f32* uc,
+                         const oeb_memref3d_f32* vc, const oeb_memref3d_f32* cosa, const oeb_memref3d_f32* rsina,
+                         double dt5, const oeb_domain* dom, void* stream);
+
+/* FP32 of kernels/nh_p_grad.h:4-6 -- nh_p_grad(uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, wk, du, dv, dt) */
+OEB_API oeb_status oeb_nh_p_grad_f32(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                             const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* rdx,
+                             const oeb_memref3d_f32* rdy, const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp,
+                             const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1, float dt,
+                             const oeb_domain* dom, void* stream);
+
+/* FP32 of kernels/p_grad_c.h:4-6 -- p_grad_c(uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc, wk, dt2) */
+OEB_API oeb_status oeb_p_grad_c_f32(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                            const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* rdxc,
+                            const oeb_memref3d_f32* rdyc, const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz,
+                            const oeb_memref3d_f32* pkc, float dt2, const oeb_domain* dom, void* stream);
+
+/* FP32 of kernels/fvtp2d.h:4-7 -- fvtp2d(q_i, q_j, fx1, fx2, fy1, fy2, q, crx, cry, ra_x, ra_y, xfx, yfx, area,
+ *                                fxx, fyy, al, almq, br, b0, smt5); p1, p2 are the driver macros
+ * (src/fvtp2d.cpp:11-12).  q_i, q_j, fx2 and fy2 are written over the same extended ranges as the
+ * reference (fvtp2d.h:26-27, 46-47, 102-103, 122-123), so they need a 3-cell halo. */
+OEB_API oeb_status oeb_fvtp2d_f32(const oeb_memref3d_f32* q_i, const oeb_memref3d_f32* q_j, const oeb_memref3d_f32* fx1,
+                          const oeb_memref3d_f32* fx2, const oeb_memref3d_f32* fy1, const oeb_memref3d_f32* fy2,
+                          const oeb_memref3d_f32* q, const oeb_memref3d_f32* crx, const oeb_memref3d_f32* cry,
+                          const oeb_memref3d_f32* ra_x, const oeb_memref3d_f32* ra_y, const oeb_memref3d_f32* xfx,
+                          const oeb_memref3d_f32* yfx, const oeb_memref3d_f32* area, float ppm_p1, float ppm_p2,
+                          const oeb_domain* dom, void* stream);
+
+
+OEB_API oeb_status oeb_laplace_f32_host(const oeb_memref3d_f32* in, const oeb_memref3d_f32* out,
+                                        const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsa_f32_host(const oeb_memref3d_f32* out, const oeb_memref3d_f32* in,
+                                        const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlato,
+                                        const oeb_memref1d_f32* crlatu, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsmag_f32_host(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                          const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                          const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlavo,
+                                          const oeb_memref1d_f32* crlavu, const oeb_memref1d_f32* crlato,
+                                          const oeb_memref1d_f32* crlatu, const oeb_memref1d_f32* acrlat0,
+                                          float eddlat, float eddlon, float tau_smag, float weight_smag,
+                                          const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv_f32_host(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                       const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                       const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                                       const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1,
+                                       float eddlat, float eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv5th_f32_host(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                          const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                          const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                                          const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1,
+                                          float eddlat, float eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fastwavesuv_f32_host(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                            const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                            const oeb_memref3d_f32* utens, const oeb_memref3d_f32* vtens,
+                                            const oeb_memref3d_f32* wgtfac, const oeb_memref3d_f32* ppuv,
+                                            const oeb_memref3d_f32* hhl, const oeb_memref3d_f32* rho,
+                                            const oeb_memref1d_f32* fx, float edadlat, float dt,
+                                            const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_uvbke_f32_host(const oeb_memref3d_f32* ub, const oeb_memref3d_f32* vb,
+                                      const oeb_memref3d_f32* uc, const oeb_memref3d_f32* vc,
+                                      const oeb_memref3d_f32* cosa, const oeb_memref3d_f32* rsina, double dt5,
+                                      const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_nh_p_grad_f32_host(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                          const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                          const oeb_memref3d_f32* rdx, const oeb_memref3d_f32* rdy,
+                                          const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp,
+                                          const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1, float dt,
+                                          const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_p_grad_c_f32_host(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                         const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                         const oeb_memref3d_f32* rdxc, const oeb_memref3d_f32* rdyc,
+                                         const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz,
+                                         const oeb_memref3d_f32* pkc, float dt2, const oeb_domain* dom,
+                                         void* stream);
+OEB_API oeb_status oeb_fvtp2d_f32_host(const oeb_memref3d_f32* q_i, const oeb_memref3d_f32* q_j,
+                                       const oeb_memref3d_f32* fx1, const oeb_memref3d_f32* fx2,
+                                       const oeb_memref3d_f32* fy1, const oeb_memref3d_f32* fy2,
+                                       const oeb_memref3d_f32* q, const oeb_memref3d_f32* crx,
+                                       const oeb_memref3d_f32* cry, const oeb_memref3d_f32* ra_x,
+                                       const oeb_memref3d_f32* ra_y, const oeb_memref3d_f32* xfx,
+                                       const oeb_memref3d_f32* yfx, const oeb_memref3d_f32* area, float ppm_p1,
+                                       float ppm_p2, const oeb_domain* dom, void* stream);
+
 
 #ifdef __cplusplus
 }

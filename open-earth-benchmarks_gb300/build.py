@@ -27,10 +27,10 @@ BASE_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 UNITS = {
     "abi_common.cu": [],
     "host_staging.cu": [],
-    "k_pointwise_f64.cu": ["--fmad=false"],
-    "k_hdiff_f64.cu": ["--fmad=false"],
-    "k_fastwavesuv_f64.cu": ["--fmad=false"],
-    "k_fvtp2d_f64.cu": ["--fmad=false"],
+    "k_pointwise.cu": ["--fmad=false"],
+    "k_hdiff.cu": ["--fmad=false"],
+    "k_fastwavesuv.cu": ["--fmad=false"],
+    "k_fvtp2d.cu": ["--fmad=false"],
 }
 
 

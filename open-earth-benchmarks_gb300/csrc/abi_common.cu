@@ -174,6 +174,22 @@ extern "C" const char* oeb_last_cuda_error(void) { return oeb::g_last_cuda_error
 
 extern "C" uint64_t oeb_launch_count(void) { return oeb::g_launches.load(std::memory_order_relaxed); }
 
+extern "C" int oeb_is_device_pointer(const void* p) {
+  if (!p) return 0;
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // unregistered host memory on some drivers: clear the sticky-free error
+    return 0;
+  }
+  return (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) ? 1 : 0;
+}
+
+extern "C" oeb_status oeb_stream_synchronize(void* stream) {
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  return e == cudaSuccess ? OEB_OK : oeb::cuda_fail(e);
+}
+
 namespace {
 
 template <class T, class M>

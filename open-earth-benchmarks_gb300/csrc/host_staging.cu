@@ -200,119 +200,123 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
   return st;
 }
 
-using M3 = oeb_memref3d_f64;
-using M1 = oeb_memref1d_f64;
-
 }  // namespace
 }  // namespace oeb
 
 using namespace oeb;
 
-extern "C" oeb_status oeb_laplace_f64_host(const M3* in, const M3* out, const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {in}, {}, {{out, kInterior}},
-                                  [&](const M3* i3, const M1*, const M3* o3) {
-                                    return oeb_laplace_f64(&i3[0], &o3[0], dom, stream);
-                                  });
+#define OEB_HM3(S) oeb_memref3d_##S
+#define OEB_HM1(S) oeb_memref1d_##S
+
+#define OEB_HOST_ENTRIES(S, T) \
+extern "C" oeb_status oeb_laplace_##S##_host(const OEB_HM3(S)* in, const OEB_HM3(S)* out, const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {in}, {}, {{out, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+                                    return oeb_laplace_##S(&i3[0], &o3[0], dom, stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_hdiffsa_##S##_host(const OEB_HM3(S)* out, const OEB_HM3(S)* in, const OEB_HM3(S)* mask, const OEB_HM1(S)* crlato, \
+                                           const OEB_HM1(S)* crlatu, const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {in, mask}, {crlato, crlatu}, {{out, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                    return oeb_hdiffsa_##S(&o3[0], &i3[0], &i3[1], &i1[0], &i1[1], dom, stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_hdiffsmag_##S##_host(const OEB_HM3(S)* uout, const OEB_HM3(S)* vout, const OEB_HM3(S)* uin, const OEB_HM3(S)* vin, \
+                                             const OEB_HM3(S)* mask, const OEB_HM1(S)* crlavo, const OEB_HM1(S)* crlavu, const OEB_HM1(S)* crlato, \
+                                             const OEB_HM1(S)* crlatu, const OEB_HM1(S)* acrlat0, T eddlat, T eddlon, \
+                                             T tau_smag, T weight_smag, const oeb_domain* dom, \
+                                             void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>( \
+      dom, stream, {uin, vin, mask}, {crlavo, crlavu, crlato, crlatu, acrlat0}, {{uout, kInterior}, {vout, kInterior}}, \
+      [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+        return oeb_hdiffsmag_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i1[0], &i1[1], &i1[2], &i1[3], &i1[4], \
+                                 eddlat, eddlon, tau_smag, weight_smag, dom, stream); \
+      }); \
+} \
+ \
+extern "C" oeb_status oeb_hadvuv_##S##_host(const OEB_HM3(S)* uout, const OEB_HM3(S)* vout, const OEB_HM3(S)* uin, const OEB_HM3(S)* vin, \
+                                          const OEB_HM1(S)* acrlat0, const OEB_HM1(S)* acrlat1, const OEB_HM1(S)* tgrlatda0, \
+                                          const OEB_HM1(S)* tgrlatda1, T eddlat, T eddlon, const oeb_domain* dom, \
+                                          void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1}, \
+                                  {{uout, kInterior}, {vout, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                    return oeb_hadvuv_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2], \
+                                                          &i1[3], eddlat, eddlon, dom, stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_hadvuv5th_##S##_host(const OEB_HM3(S)* uout, const OEB_HM3(S)* vout, const OEB_HM3(S)* uin, const OEB_HM3(S)* vin, \
+                                             const OEB_HM1(S)* acrlat0, const OEB_HM1(S)* acrlat1, const OEB_HM1(S)* tgrlatda0, \
+                                             const OEB_HM1(S)* tgrlatda1, T eddlat, T eddlon, const oeb_domain* dom, \
+                                             void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1}, \
+                                  {{uout, kInterior}, {vout, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                    return oeb_hadvuv5th_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2], \
+                                                             &i1[3], eddlat, eddlon, dom, stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_fastwavesuv_##S##_host(const OEB_HM3(S)* uout, const OEB_HM3(S)* vout, const OEB_HM3(S)* uin, const OEB_HM3(S)* vin, \
+                                               const OEB_HM3(S)* utens, const OEB_HM3(S)* vtens, const OEB_HM3(S)* wgtfac, const OEB_HM3(S)* ppuv, \
+                                               const OEB_HM3(S)* hhl, const OEB_HM3(S)* rho, const OEB_HM1(S)* fx, T edadlat, T dt, \
+                                               const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho}, {fx}, \
+                                  {{uout, kInterior}, {vout, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                    return oeb_fastwavesuv_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
+                                                               &i3[5], &i3[6], &i3[7], &i1[0], edadlat, dt, dom, \
+                                                               stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_uvbke_##S##_host(const OEB_HM3(S)* ub, const OEB_HM3(S)* vb, const OEB_HM3(S)* uc, const OEB_HM3(S)* vc, const OEB_HM3(S)* cosa, \
+                                         const OEB_HM3(S)* rsina, double dt5, const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uc, vc, cosa, rsina}, {}, {{ub, kInterior}, {vb, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+                                    return oeb_uvbke_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], dt5, dom, \
+                                                         stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_nh_p_grad_##S##_host(const OEB_HM3(S)* uout, const OEB_HM3(S)* vout, const OEB_HM3(S)* uin, const OEB_HM3(S)* vin, \
+                                             const OEB_HM3(S)* rdx, const OEB_HM3(S)* rdy, const OEB_HM3(S)* gz, const OEB_HM3(S)* pp, const OEB_HM3(S)* pk3, \
+                                             const OEB_HM3(S)* wk1, T dt, const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin, rdx, rdy, gz, pp, pk3, wk1}, {}, \
+                                  {{uout, kInterior}, {vout, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+                                    return oeb_nh_p_grad_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
+                                                             &i3[5], &i3[6], &i3[7], dt, dom, stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_p_grad_c_##S##_host(const OEB_HM3(S)* uout, const OEB_HM3(S)* vout, const OEB_HM3(S)* uin, const OEB_HM3(S)* vin, \
+                                            const OEB_HM3(S)* rdxc, const OEB_HM3(S)* rdyc, const OEB_HM3(S)* delpc, const OEB_HM3(S)* gz, \
+                                            const OEB_HM3(S)* pkc, T dt2, const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin, rdxc, rdyc, delpc, gz, pkc}, {}, \
+                                  {{uout, kInterior}, {vout, kInterior}}, \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+                                    return oeb_p_grad_c_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
+                                                            &i3[5], &i3[6], dt2, dom, stream); \
+                                  }); \
+} \
+ \
+extern "C" oeb_status oeb_fvtp2d_##S##_host(const OEB_HM3(S)* q_i, const OEB_HM3(S)* q_j, const OEB_HM3(S)* fx1, const OEB_HM3(S)* fx2, const OEB_HM3(S)* fy1, \
+                                          const OEB_HM3(S)* fy2, const OEB_HM3(S)* q, const OEB_HM3(S)* crx, const OEB_HM3(S)* cry, const OEB_HM3(S)* ra_x, \
+                                          const OEB_HM3(S)* ra_y, const OEB_HM3(S)* xfx, const OEB_HM3(S)* yfx, const OEB_HM3(S)* area, T p1, \
+                                          T p2, const oeb_domain* dom, void* stream) { \
+  return run_host<T, OEB_HM3(S), OEB_HM1(S)>( \
+      dom, stream, {q, crx, cry, ra_x, ra_y, xfx, yfx, area}, {}, \
+      {{q_i, kFvQi}, {q_j, kFvQj}, {fx1, kInterior}, {fx2, kFvFx2}, {fy1, kInterior}, {fy2, kFvFy2}}, \
+      [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+        return oeb_fvtp2d_##S(&o3[0], &o3[1], &o3[2], &o3[3], &o3[4], &o3[5], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
+                              &i3[5], &i3[6], &i3[7], p1, p2, dom, stream); \
+      }); \
 }
 
-extern "C" oeb_status oeb_hdiffsa_f64_host(const M3* out, const M3* in, const M3* mask, const M1* crlato,
-                                           const M1* crlatu, const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {in, mask}, {crlato, crlatu}, {{out, kInterior}},
-                                  [&](const M3* i3, const M1* i1, const M3* o3) {
-                                    return oeb_hdiffsa_f64(&o3[0], &i3[0], &i3[1], &i1[0], &i1[1], dom, stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_hdiffsmag_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
-                                             const M3* mask, const M1* crlavo, const M1* crlavu, const M1* crlato,
-                                             const M1* crlatu, const M1* acrlat0, double eddlat, double eddlon,
-                                             double tau_smag, double weight_smag, const oeb_domain* dom,
-                                             void* stream) {
-  return run_host<double, M3, M1>(
-      dom, stream, {uin, vin, mask}, {crlavo, crlavu, crlato, crlatu, acrlat0}, {{uout, kInterior}, {vout, kInterior}},
-      [&](const M3* i3, const M1* i1, const M3* o3) {
-        return oeb_hdiffsmag_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i1[0], &i1[1], &i1[2], &i1[3], &i1[4],
-                                 eddlat, eddlon, tau_smag, weight_smag, dom, stream);
-      });
-}
-
-extern "C" oeb_status oeb_hadvuv_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
-                                          const M1* acrlat0, const M1* acrlat1, const M1* tgrlatda0,
-                                          const M1* tgrlatda1, double eddlat, double eddlon, const oeb_domain* dom,
-                                          void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1},
-                                  {{uout, kInterior}, {vout, kInterior}},
-                                  [&](const M3* i3, const M1* i1, const M3* o3) {
-                                    return oeb_hadvuv_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2],
-                                                          &i1[3], eddlat, eddlon, dom, stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_hadvuv5th_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
-                                             const M1* acrlat0, const M1* acrlat1, const M1* tgrlatda0,
-                                             const M1* tgrlatda1, double eddlat, double eddlon, const oeb_domain* dom,
-                                             void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1},
-                                  {{uout, kInterior}, {vout, kInterior}},
-                                  [&](const M3* i3, const M1* i1, const M3* o3) {
-                                    return oeb_hadvuv5th_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2],
-                                                             &i1[3], eddlat, eddlon, dom, stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_fastwavesuv_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
-                                               const M3* utens, const M3* vtens, const M3* wgtfac, const M3* ppuv,
-                                               const M3* hhl, const M3* rho, const M1* fx, double edadlat, double dt,
-                                               const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho}, {fx},
-                                  {{uout, kInterior}, {vout, kInterior}},
-                                  [&](const M3* i3, const M1* i1, const M3* o3) {
-                                    return oeb_fastwavesuv_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
-                                                               &i3[5], &i3[6], &i3[7], &i1[0], edadlat, dt, dom,
-                                                               stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_uvbke_f64_host(const M3* ub, const M3* vb, const M3* uc, const M3* vc, const M3* cosa,
-                                         const M3* rsina, double dt5, const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {uc, vc, cosa, rsina}, {}, {{ub, kInterior}, {vb, kInterior}},
-                                  [&](const M3* i3, const M1*, const M3* o3) {
-                                    return oeb_uvbke_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], dt5, dom,
-                                                         stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_nh_p_grad_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
-                                             const M3* rdx, const M3* rdy, const M3* gz, const M3* pp, const M3* pk3,
-                                             const M3* wk1, double dt, const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {uin, vin, rdx, rdy, gz, pp, pk3, wk1}, {},
-                                  {{uout, kInterior}, {vout, kInterior}},
-                                  [&](const M3* i3, const M1*, const M3* o3) {
-                                    return oeb_nh_p_grad_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
-                                                             &i3[5], &i3[6], &i3[7], dt, dom, stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_p_grad_c_f64_host(const M3* uout, const M3* vout, const M3* uin, const M3* vin,
-                                            const M3* rdxc, const M3* rdyc, const M3* delpc, const M3* gz,
-                                            const M3* pkc, double dt2, const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(dom, stream, {uin, vin, rdxc, rdyc, delpc, gz, pkc}, {},
-                                  {{uout, kInterior}, {vout, kInterior}},
-                                  [&](const M3* i3, const M1*, const M3* o3) {
-                                    return oeb_p_grad_c_f64(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
-                                                            &i3[5], &i3[6], dt2, dom, stream);
-                                  });
-}
-
-extern "C" oeb_status oeb_fvtp2d_f64_host(const M3* q_i, const M3* q_j, const M3* fx1, const M3* fx2, const M3* fy1,
-                                          const M3* fy2, const M3* q, const M3* crx, const M3* cry, const M3* ra_x,
-                                          const M3* ra_y, const M3* xfx, const M3* yfx, const M3* area, double p1,
-                                          double p2, const oeb_domain* dom, void* stream) {
-  return run_host<double, M3, M1>(
-      dom, stream, {q, crx, cry, ra_x, ra_y, xfx, yfx, area}, {},
-      {{q_i, kFvQi}, {q_j, kFvQj}, {fx1, kInterior}, {fx2, kFvFx2}, {fy1, kInterior}, {fy2, kFvFy2}},
-      [&](const M3* i3, const M1*, const M3* o3) {
-        return oeb_fvtp2d_f64(&o3[0], &o3[1], &o3[2], &o3[3], &o3[4], &o3[5], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4],
-                              &i3[5], &i3[6], &i3[7], p1, p2, dom, stream);
-      });
-}
+OEB_HOST_ENTRIES(f64, double)
+OEB_HOST_ENTRIES(f32, float)

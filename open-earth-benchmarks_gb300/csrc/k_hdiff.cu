@@ -1,0 +1,293 @@
+// k_hdiff.cu -- horizontal diffusion stencils whose intermediates are shared by neighbouring
+// points: hdiffsa (kernels/hdiffsa.h:95-123) and hdiffsmag (kernels/hdiffsmag.h:205-263), in
+// FP64 (bit-identical to the reference) and FP32 (exact limiter sign tests, compensated
+// laplacian sums; precision.cuh).
+//
+// The reference's OpenMP variants recompute each intermediate for every point that uses it
+// (three laplacians per point in hdiffsa, three T^2 and three S^2 per point in hdiffsmag).
+// On GB300 the FP64 pipe, not HBM, bounds these kernels, so here every intermediate is
+// computed once per (i, j, k) into a shared-memory tile (plus a one- or two-cell apron) and
+// read by its neighbours.  Reusing a value is exact: it is the same expression on the same
+// operands.  Differences are stored once and their negations used where the reference
+// subtracts in the other order (x - y == -(y - x) exactly in IEEE round-to-nearest).
+//
+// Compiled with --fmad=false (see k_pointwise.cu).  One CTA of 32 x 8 threads per
+// 32 x 32 tile and KB k-levels.
+#include "precision.cuh"
+#include "stencil_util.cuh"
+
+namespace oeb {
+namespace {
+
+constexpr int kT = 32;  // tile edge
+
+// ============================== hdiffsa ===========================================
+// Shared layout (per k-level), tile origin (i0, j0):
+//   in  : 36 x 36, (i0-2+a, j0-2+b)
+//   dy  : 34 x 35, (i0-1+a, j0-2+b)   dy(i,j)  = in(i,j+1) - in(i,j)
+//   lap : 34 x 34, (i0-1+a, j0-1+b)
+//   flx : 33 x 32, (i0-1+a, j0+b)
+//   fly : 32 x 33, (i0+a,   j0-1+b)
+template <class T>
+struct HdiffsaSmem {
+  T in[36][36];
+  T dy[35][34];
+  T lap[34][34];
+  T flx[32][33];
+  T fly[33][32];
+  T crlato[34];  // j0-1+b
+  T crlatu[34];
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) hdiffsa_kernel(T* __restrict__ out, const T* __restrict__ in,
+                                                           const T* __restrict__ mask, const T* __restrict__ crlato,
+                                                           const T* __restrict__ crlatu, int64_t s1d, Dims d,
+                                                           int kb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  HdiffsaSmem<T>& s = *reinterpret_cast<HdiffsaSmem<T>*>(smem_raw);
+  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
+  const int sj = (int)d.sj;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  if (tid < 34) {
+    const int j = j0 - 1 + tid;
+    const bool ok = j >= -1 && j < d.ny + 1;
+    s.crlato[tid] = ok ? ld(crlato + (int64_t)j * s1d) : T(0);
+    s.crlatu[tid] = ok ? ld(crlatu + (int64_t)j * s1d) : T(0);
+  }
+  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    const int64_t kofs = (int64_t)k * d.sk;
+    const T* pin = in + kofs;
+    for_region<36, 36>([&](int a, int b) {
+      const int i = i0 - 2 + a, j = j0 - 2 + b;
+      const bool ok = i >= -2 && i < d.nx + 2 && j >= -2 && j < d.ny + 2;
+      s.in[b][a] = ok ? ld(pin + i + j * sj) : T(0);
+    });
+    __syncthreads();
+    for_region<34, 35>([&](int a, int b) { s.dy[b][a] = s.in[b + 1][a + 1] - s.in[b][a + 1]; });
+    __syncthreads();
+    // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
+    for_region<34, 34>([&](int a, int b) {
+      const T c = s.in[b + 1][a + 1];
+      s.lap[b][a] = (((s.in[b + 1][a] + s.in[b + 1][a + 2]) - T(2.0) * c) + s.crlato[b] * s.dy[b + 1][a]) +
+                    s.crlatu[b] * (-s.dy[b][a]);
+    });
+    __syncthreads();
+    // hdiffsa.h:106-113: limited fluxes
+    for_region<33, 32>([&](int a, int b) {
+      T f = s.lap[b + 1][a + 1] - s.lap[b + 1][a];
+      if (Prec<T>::prod_gt0(f, s.in[b + 2][a + 2] - s.in[b + 2][a + 1])) f = 0;
+      s.flx[b][a] = f;
+    });
+    for_region<32, 33>([&](int a, int b) {
+      T f = s.crlato[b] * (s.lap[b + 1][a + 1] - s.lap[b][a + 1]);
+      if (Prec<T>::prod_gt0(f, s.dy[b + 1][a + 1])) f = 0;
+      s.fly[b][a] = f;
+    });
+    __syncthreads();
+    // hdiffsa.h:118-119
+    for_region<32, 32>([&](int a, int b) {
+      const int i = i0 + a, j = j0 + b;
+      if (i < d.nx && j < d.ny) {
+        const int64_t o = kofs + i + j * sj;
+        out[o] = s.in[b + 2][a + 2] + (((s.flx[b][a] - s.flx[b][a + 1]) + s.fly[b][a]) - s.fly[b + 1][a]) * ld(mask + o);
+      }
+    });
+    __syncthreads();
+  }
+}
+
+// ============================== hdiffsmag =========================================
+// Shared layout (per k-level), tile origin (i0, j0):
+//   u, v : 34 x 34, (i0-1+a, j0-1+b)
+//   dxu  : 33 x 33, (i0-1+a, j0+b)     u(i+1,j) - u(i,j)
+//   dyv  : 33 x 33, (i0+a,   j0-1+b)   v(i,j+1) - v(i,j)
+//   dyu  : 33 x 33, (i0-1+a, j0-1+b)   u(i,j+1) - u(i,j)
+//   dxv  : 33 x 33, (i0-1+a, j0-1+b)   v(i+1,j) - v(i,j)
+//   tsq  : 33 x 33, (i0+a,   j0+b)     T_s^2
+//   ssq  : 33 x 33, (i0-1+a, j0-1+b)   S_uv^2
+template <class T>
+struct HdiffsmagSmem {
+  T u[34][34];
+  T v[34][34];
+  T dxu[33][33];
+  T dyv[33][33];
+  T dyu[33][33];
+  T dxv[33][33];
+  T tsq[33][33];
+  T ssq[33][33];
+  T acrlat0[34];  // j0-1+b
+  T crlato[32], crlatu[32], crlavo[32], crlavu[32];
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) hdiffsmag_kernel(
+    T* __restrict__ uout, T* __restrict__ vout, const T* __restrict__ uin, const T* __restrict__ vin,
+    const T* __restrict__ mask, const T* __restrict__ crlavo, const T* __restrict__ crlavu,
+    const T* __restrict__ crlato, const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d, T eddlat,
+    T eddlon, T tau_smag, T weight_smag, Dims d, int kb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  HdiffsmagSmem<T>& s = *reinterpret_cast<HdiffsmagSmem<T>*>(smem_raw);
+  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
+  const int sj = (int)d.sj;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  constexpr T rr = earth_radius_recip<T>();
+  if (tid < 34) {
+    const int j = j0 - 1 + tid;
+    s.acrlat0[tid] = (j >= -1 && j < d.ny + 1) ? ld(acrlat0 + (int64_t)j * s1d) : T(0);
+  } else if (tid >= 64 && tid < 96) {
+    const int b = tid - 64, j = j0 + b;
+    const bool ok = j < d.ny;
+    const int64_t jo = (int64_t)j * s1d;
+    s.crlato[b] = ok ? ld(crlato + jo) : T(0);
+    s.crlatu[b] = ok ? ld(crlatu + jo) : T(0);
+    s.crlavo[b] = ok ? ld(crlavo + jo) : T(0);
+    s.crlavu[b] = ok ? ld(crlavu + jo) : T(0);
+  }
+  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    const int64_t kofs = (int64_t)k * d.sk;
+    for_region<34, 34>([&](int a, int b) {
+      const int i = i0 - 1 + a, j = j0 - 1 + b;
+      const bool ok = i >= -1 && i < d.nx + 1 && j >= -1 && j < d.ny + 1;
+      const int64_t o = kofs + i + j * sj;
+      s.u[b][a] = ok ? ld(uin + o) : T(0);
+      s.v[b][a] = ok ? ld(vin + o) : T(0);
+    });
+    __syncthreads();
+    for_region<33, 33>([&](int a, int b) {
+      s.dxu[b][a] = s.u[b + 1][a + 1] - s.u[b + 1][a];
+      s.dyv[b][a] = s.v[b + 1][a + 1] - s.v[b][a + 1];
+      s.dyu[b][a] = s.u[b + 1][a] - s.u[b][a];
+      s.dxv[b][a] = s.v[b][a + 1] - s.v[b][a];
+    });
+    __syncthreads();
+    // hdiffsmag.h:213 T_s = (v(j-1)-v) eddlat R^-1 - (u(i-1)-u) acrlat0(j) eddlon
+    //              :221 S_uv = (u(j+1)-u) eddlat R^-1 + (v(i+1)-v) acrlat0(j) eddlon
+    for_region<33, 33>([&](int a, int b) {
+      const T ts = ((-s.dyv[b][a]) * eddlat) * rr - ((-s.dxu[b][a]) * s.acrlat0[b + 1]) * eddlon;
+      s.tsq[b][a] = ts * ts;
+      const T su = (s.dyu[b][a] * eddlat) * rr + (s.dxv[b][a] * s.acrlat0[b]) * eddlon;
+      s.ssq[b][a] = su * su;
+    });
+    __syncthreads();
+    for_region<32, 32>([&](int a, int b) {
+      const int i = i0 + a, j = j0 + b;
+      if (i < d.nx && j < d.ny) {
+        const int64_t o = kofs + i + j * sj;
+        const T hdweight = weight_smag * ld(mask + o);
+        // hdiffsmag.h:233-244
+        T smag_u = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b][a + 1] + s.tsq[b][a]) +
+                                             T(0.5) * (s.ssq[b][a + 1] + s.ssq[b + 1][a + 1])) -
+                   hdweight;
+        smag_u = clamp_smag(smag_u);
+        const T uc = s.u[b + 1][a + 1];
+        // u(i+1) + u(i-1) - 2u + crlato (u(j+1) - u) + crlatu (u(j-1) - u)
+        Acc<T> lu(s.u[b + 1][a + 2]);
+        lu.add(s.u[b + 1][a]);
+        lu.add(-(T(2.0) * uc));
+        lu.add_prod(s.crlato[b], s.dyu[b + 1][a + 1]);
+        lu.add_prod(s.crlatu[b], -s.dyu[b][a + 1]);
+        uout[o] = uc + smag_u * lu.get();
+        // hdiffsmag.h:248-259
+        T smag_v = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b + 1][a] + s.tsq[b][a]) +
+                                             T(0.5) * (s.ssq[b + 1][a] + s.ssq[b + 1][a + 1])) -
+                   hdweight;
+        smag_v = clamp_smag(smag_v);
+        const T vc = s.v[b + 1][a + 1];
+        Acc<T> lv(s.v[b + 1][a + 2]);
+        lv.add(s.v[b + 1][a]);
+        lv.add(-(T(2.0) * vc));
+        lv.add_prod(s.crlavo[b], s.dyv[b + 1][a]);
+        lv.add_prod(s.crlavu[b], -s.dyv[b][a]);
+        vout[o] = vc + smag_v * lv.get();
+      }
+    });
+    __syncthreads();
+  }
+}
+
+constexpr int kKB = 4;
+
+
+template <class T, class M3, class M1>
+oeb_status hdiffsa_entry(const M3* out, const M3* in, const M3* mask, const M1* crlato, const M1* crlatu,
+                         const oeb_domain* dom, void* stream) {
+  OEB_TRY(check_domain(dom));
+  Grid<T> gout, gin, gmask;
+  Line<T> lo, lu;
+  OEB_TRY((check_field3<T>(out, *dom, kInterior, &gout)));
+  OEB_TRY((check_field3<T>(in, *dom, Reach{2, 2, 2, 2, 0, 0}, &gin)));
+  OEB_TRY((check_field3<T>(mask, *dom, kInterior, &gmask)));
+  OEB_TRY((check_field1<T>(crlato, *dom, 1, 1, &lo)));
+  OEB_TRY((check_field1<T>(crlatu, *dom, 1, 1, &lu)));
+  if (lo.s != lu.s) return OEB_ERR_LAYOUT;
+  OEB_TRY(check_same_strides<T>({&gout, &gin, &gmask}));
+  OEB_TRY(check_no_alias({gout.lo, gout.hi}, {gin.lo, gin.hi, gmask.lo, gmask.hi, lo.lo, lo.hi, lu.lo, lu.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  const size_t smem = sizeof(HdiffsaSmem<T>);
+  OEB_TRY(ensure_dyn_smem((const void*)hdiffsa_kernel<T>, (int)smem));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gin.sj, gin.sk};
+  hdiffsa_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), smem, (cudaStream_t)stream>>>(
+      gout.origin, gin.origin, gmask.origin, lo.origin, lu.origin, lo.s, d, kKB);
+  return after_launch();
+}
+
+template <class T, class M3, class M1>
+oeb_status hdiffsmag_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* mask,
+                           const M1* crlavo, const M1* crlavu, const M1* crlato, const M1* crlatu, const M1* acrlat0,
+                           T eddlat, T eddlon, T tau_smag, T weight_smag, const oeb_domain* dom, void* stream) {
+  OEB_TRY(check_domain(dom));
+  Grid<T> gu, gv, gui, gvi, gm;
+  Line<T> lvo, lvu, lto, ltu, la0;
+  OEB_TRY((check_field3<T>(uout, *dom, kInterior, &gu)));
+  OEB_TRY((check_field3<T>(vout, *dom, kInterior, &gv)));
+  OEB_TRY((check_field3<T>(uin, *dom, Reach{1, 1, 1, 1, 0, 0}, &gui)));
+  OEB_TRY((check_field3<T>(vin, *dom, Reach{1, 1, 1, 1, 0, 0}, &gvi)));
+  OEB_TRY((check_field3<T>(mask, *dom, kInterior, &gm)));
+  OEB_TRY((check_field1<T>(crlavo, *dom, 0, 0, &lvo)));
+  OEB_TRY((check_field1<T>(crlavu, *dom, 0, 0, &lvu)));
+  OEB_TRY((check_field1<T>(crlato, *dom, 0, 0, &lto)));
+  OEB_TRY((check_field1<T>(crlatu, *dom, 0, 0, &ltu)));
+  OEB_TRY((check_field1<T>(acrlat0, *dom, 1, 1, &la0)));
+  if (lvu.s != lvo.s || lto.s != lvo.s || ltu.s != lvo.s || la0.s != lvo.s) return OEB_ERR_LAYOUT;
+  OEB_TRY(check_same_strides<T>({&gu, &gv, &gui, &gvi, &gm}));
+  OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi},
+                         {gui.lo, gui.hi, gvi.lo, gvi.hi, gm.lo, gm.hi, lvo.lo, lvo.hi, lvu.lo, lvu.hi, lto.lo,
+                          lto.hi, ltu.lo, ltu.hi, la0.lo, la0.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  const size_t smem = sizeof(HdiffsmagSmem<T>);
+  OEB_TRY(ensure_dyn_smem((const void*)hdiffsmag_kernel<T>, (int)smem));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
+  hdiffsmag_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), smem, (cudaStream_t)stream>>>(
+      gu.origin, gv.origin, gui.origin, gvi.origin, gm.origin, lvo.origin, lvu.origin, lto.origin, ltu.origin,
+      la0.origin, lvo.s, eddlat, eddlon, tau_smag, weight_smag, d, kKB);
+  return after_launch();
+}
+
+}  // namespace
+}  // namespace oeb
+
+using namespace oeb;
+
+#define OEB_HDIFF_ENTRIES(S, T)                                                                                     \
+  extern "C" oeb_status oeb_hdiffsa_##S(const oeb_memref3d_##S* out, const oeb_memref3d_##S* in,                   \
+                                        const oeb_memref3d_##S* mask, const oeb_memref1d_##S* crlato,             \
+                                        const oeb_memref1d_##S* crlatu, const oeb_domain* dom, void* stream) {    \
+    return hdiffsa_entry<T>(out, in, mask, crlato, crlatu, dom, stream);                                          \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hdiffsmag_##S(                                                                         \
+      const oeb_memref3d_##S* uout, const oeb_memref3d_##S* vout, const oeb_memref3d_##S* uin,                      \
+      const oeb_memref3d_##S* vin, const oeb_memref3d_##S* mask, const oeb_memref1d_##S* crlavo,                    \
+      const oeb_memref1d_##S* crlavu, const oeb_memref1d_##S* crlato, const oeb_memref1d_##S* crlatu,               \
+      const oeb_memref1d_##S* acrlat0, T eddlat, T eddlon, T tau_smag, T weight_smag, const oeb_domain* dom,       \
+      void* stream) {                                                                                              \
+    return hdiffsmag_entry<T>(uout, vout, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, eddlat, eddlon,\
+                              tau_smag, weight_smag, dom, stream);                                                 \
+  }
+
+OEB_HDIFF_ENTRIES(f64, double)
+OEB_HDIFF_ENTRIES(f32, float)
