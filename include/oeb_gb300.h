@@ -412,6 +412,103 @@ OEB_API oeb_status oeb_fvtp2d_f32_host(const oeb_memref3d_f32* q_i, const oeb_me
                                        float ppm_p2, const oeb_domain* dom, void* stream);
 
 
+
+/* ------------------------------------------------------------------------- */
+/* Tangent-linear stencils: dy = J(x) dx, the Jacobian of the forward stencil */
+/* at the state x (every upwind/limiter/PPM/clamp branch frozen at x) applied */
+/* to a perturbation dx of the active inputs.  Device pointers, asynchronous; */
+/* each dx field must have the layout of its state field.  dy is written over */
+/* the forward output's written box.  Device scratch from the library pool.   */
+/*   hdiffsmag, hadvuv, hadvuv5th : active (uin, vin)                          */
+/*   fastwavesuv                  : active (uin, vin, utens, vtens, ppuv)      */
+/*   fvtp2d                       : active q; dy = all six outputs            */
+/* ------------------------------------------------------------------------- */
+
+OEB_API oeb_status oeb_hdiffsmag_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask,
+                                       const oeb_memref1d_f64* crlavo, const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0,
+                                       const oeb_memref3d_f64* duin, const oeb_memref3d_f64* dvin, double eddlat, double eddlon, double tau_smag, double weight_smag,
+                                       const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                                    const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1, const oeb_memref3d_f64* duin, const oeb_memref3d_f64* dvin, double eddlat, double eddlon,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv5th_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                                       const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1, const oeb_memref3d_f64* duin, const oeb_memref3d_f64* dvin, double eddlat, double eddlon,
+                                       const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fastwavesuv_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* utens, const oeb_memref3d_f64* vtens,
+                                         const oeb_memref3d_f64* wgtfac, const oeb_memref3d_f64* ppuv, const oeb_memref3d_f64* hhl, const oeb_memref3d_f64* rho, const oeb_memref1d_f64* fx, const oeb_memref3d_f64* duin, const oeb_memref3d_f64* dvin,
+                                         const oeb_memref3d_f64* dutens, const oeb_memref3d_f64* dvtens, const oeb_memref3d_f64* dppuv, double edadlat, double dt,
+                                         const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fvtp2d_tl_f64(const oeb_memref3d_f64* dq_i, const oeb_memref3d_f64* dq_j, const oeb_memref3d_f64* dfx1, const oeb_memref3d_f64* dfx2, const oeb_memref3d_f64* dfy1, const oeb_memref3d_f64* dfy2, const oeb_memref3d_f64* q,
+                                    const oeb_memref3d_f64* crx, const oeb_memref3d_f64* cry, const oeb_memref3d_f64* ra_x, const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx, const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area,
+                                    const oeb_memref3d_f64* dq, double ppm_p1, double ppm_p2, const oeb_domain* dom, void* stream);
+
+OEB_API oeb_status oeb_hdiffsmag_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* mask,
+                                       const oeb_memref1d_f32* crlavo, const oeb_memref1d_f32* crlavu, const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_memref1d_f32* acrlat0,
+                                       const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin, float eddlat, float eddlon, float tau_smag, float weight_smag,
+                                       const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                                    const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1, const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin, float eddlat, float eddlon,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv5th_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                                       const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1, const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin, float eddlat, float eddlon,
+                                       const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fastwavesuv_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* utens, const oeb_memref3d_f32* vtens,
+                                         const oeb_memref3d_f32* wgtfac, const oeb_memref3d_f32* ppuv, const oeb_memref3d_f32* hhl, const oeb_memref3d_f32* rho, const oeb_memref1d_f32* fx, const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin,
+                                         const oeb_memref3d_f32* dutens, const oeb_memref3d_f32* dvtens, const oeb_memref3d_f32* dppuv, float edadlat, float dt,
+                                         const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fvtp2d_tl_f32(const oeb_memref3d_f32* dq_i, const oeb_memref3d_f32* dq_j, const oeb_memref3d_f32* dfx1, const oeb_memref3d_f32* dfx2, const oeb_memref3d_f32* dfy1, const oeb_memref3d_f32* dfy2, const oeb_memref3d_f32* q,
+                                    const oeb_memref3d_f32* crx, const oeb_memref3d_f32* cry, const oeb_memref3d_f32* ra_x, const oeb_memref3d_f32* ra_y, const oeb_memref3d_f32* xfx, const oeb_memref3d_f32* yfx, const oeb_memref3d_f32* area,
+                                    const oeb_memref3d_f32* dq, float ppm_p1, float ppm_p2, const oeb_domain* dom, void* stream);
+
+
+/* ------------------------------------------------------------------------- */
+/* Adjoint (transpose) stencils: xb = J(x)^T yb, the transpose of the         */
+/* tangent-linear map above at the state x, branches frozen at x.  Written    */
+/* as gathers (no atomics) over per-point terms recomputed from the state,    */
+/* in device scratch from the library pool.  Each xb is written over the      */
+/* reach box of its input (the cells its forward output depends on) and is    */
+/* overwritten, not accumulated.  Device pointers, asynchronous.              */
+/*   hdiffsmag: xb = (uinb, vinb) on halo 1;  hadvuv / hadvuv5th: halo 2 / 3  */
+/*   fastwavesuv: uinb, vinb, utensb, vtensb on the interior, ppuvb on        */
+/*     i,j in [0,N], k in [-1,N_z];  fvtp2d: qb on halo 3 from (fx1b, fy1b)   */
+/* ------------------------------------------------------------------------- */
+
+OEB_API oeb_status oeb_hdiffsmag_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlavo,
+                                        const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0, const oeb_memref3d_f64* uoutb,
+                                        const oeb_memref3d_f64* voutb, double eddlat, double eddlon, double tau_smag, double weight_smag,
+                                        const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                                     const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat,
+                                     double eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv5th_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
+                                        const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat,
+                                        double eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fastwavesuv_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* utensb, const oeb_memref3d_f64* vtensb, const oeb_memref3d_f64* ppuvb, const oeb_memref3d_f64* uin,
+                                          const oeb_memref3d_f64* vin, const oeb_memref3d_f64* utens, const oeb_memref3d_f64* vtens, const oeb_memref3d_f64* wgtfac, const oeb_memref3d_f64* ppuv, const oeb_memref3d_f64* hhl,
+                                          const oeb_memref3d_f64* rho, const oeb_memref1d_f64* fx, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double edadlat, double dt,
+                                          const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fvtp2d_adj_f64(const oeb_memref3d_f64* qb, const oeb_memref3d_f64* q, const oeb_memref3d_f64* crx, const oeb_memref3d_f64* cry, const oeb_memref3d_f64* ra_x, const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx,
+                                     const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, const oeb_memref3d_f64* fx1b, const oeb_memref3d_f64* fy1b, double ppm_p1, double ppm_p2,
+                                     const oeb_domain* dom, void* stream);
+
+OEB_API oeb_status oeb_hdiffsmag_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlavo,
+                                        const oeb_memref1d_f32* crlavu, const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_memref1d_f32* acrlat0, const oeb_memref3d_f32* uoutb,
+                                        const oeb_memref3d_f32* voutb, float eddlat, float eddlon, float tau_smag, float weight_smag,
+                                        const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                                     const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1, const oeb_memref3d_f32* uoutb, const oeb_memref3d_f32* voutb, float eddlat,
+                                     float eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hadvuv5th_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref1d_f32* acrlat0, const oeb_memref1d_f32* acrlat1,
+                                        const oeb_memref1d_f32* tgrlatda0, const oeb_memref1d_f32* tgrlatda1, const oeb_memref3d_f32* uoutb, const oeb_memref3d_f32* voutb, float eddlat,
+                                        float eddlon, const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fastwavesuv_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* utensb, const oeb_memref3d_f32* vtensb, const oeb_memref3d_f32* ppuvb, const oeb_memref3d_f32* uin,
+                                          const oeb_memref3d_f32* vin, const oeb_memref3d_f32* utens, const oeb_memref3d_f32* vtens, const oeb_memref3d_f32* wgtfac, const oeb_memref3d_f32* ppuv, const oeb_memref3d_f32* hhl,
+                                          const oeb_memref3d_f32* rho, const oeb_memref1d_f32* fx, const oeb_memref3d_f32* uoutb, const oeb_memref3d_f32* voutb, float edadlat, float dt,
+                                          const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_fvtp2d_adj_f32(const oeb_memref3d_f32* qb, const oeb_memref3d_f32* q, const oeb_memref3d_f32* crx, const oeb_memref3d_f32* cry, const oeb_memref3d_f32* ra_x, const oeb_memref3d_f32* ra_y, const oeb_memref3d_f32* xfx,
+                                     const oeb_memref3d_f32* yfx, const oeb_memref3d_f32* area, const oeb_memref3d_f32* fx1b, const oeb_memref3d_f32* fy1b, float ppm_p1, float ppm_p2,
+                                     const oeb_domain* dom, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

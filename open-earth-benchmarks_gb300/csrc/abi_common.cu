@@ -53,6 +53,31 @@ oeb_status ensure_dyn_smem(const void* kernel, int bytes) {
   return OEB_OK;
 }
 
+// One stream-ordered memory pool per device for the library's own scratch (host staging,
+// tangent-linear dual arrays), kept for the life of the process with the release threshold
+// at the maximum so repeated calls reuse the same device memory.
+oeb_status device_pool(cudaMemPool_t* out) {
+  static std::mutex mu;
+  static std::vector<cudaMemPool_t> pools;
+  int dev = 0;
+  OEB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)pools.size() <= dev) pools.resize(dev + 1, nullptr);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    OEB_CUDA_TRY(cudaMemPoolCreate(&p, &props));
+    uint64_t threshold = ~0ull;
+    OEB_CUDA_TRY(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &threshold));
+    pools[dev] = p;
+  }
+  *out = pools[dev];
+  return OEB_OK;
+}
+
 oeb_status check_domain(const oeb_domain* dom) {
   if (!dom) return OEB_ERR_NULL;
   const int64_t lim = std::numeric_limits<int32_t>::max() / 2;

@@ -16,30 +16,6 @@
 namespace oeb {
 namespace {
 
-// One memory pool per device, kept for the life of the process (release threshold at the
-// maximum, so repeated calls reuse the same device memory).
-oeb_status pool_for_current_device(cudaMemPool_t* out) {
-  static std::mutex mu;
-  static std::vector<cudaMemPool_t> pools;
-  int dev = 0;
-  OEB_CUDA_TRY(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(mu);
-  if ((int)pools.size() <= dev) pools.resize(dev + 1, nullptr);
-  if (!pools[dev]) {
-    cudaMemPoolProps props = {};
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = dev;
-    cudaMemPool_t p = nullptr;
-    OEB_CUDA_TRY(cudaMemPoolCreate(&p, &props));
-    uint64_t threshold = ~0ull;
-    OEB_CUDA_TRY(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &threshold));
-    pools[dev] = p;
-  }
-  *out = pools[dev];
-  return OEB_OK;
-}
-
 template <class T>
 const T* span_start(const T* allocated, const T* aligned) {
   return (allocated && allocated <= aligned) ? allocated : aligned;
@@ -167,7 +143,7 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
   }
   cudaStream_t s = (cudaStream_t)stream;
   cudaMemPool_t pool = nullptr;
-  OEB_TRY(pool_for_current_device(&pool));
+  OEB_TRY(device_pool(&pool));
   oeb_status st = OEB_OK;
   {
     Stager<T> stage(s, pool);

@@ -10,6 +10,7 @@
 // Compiled with --fmad=false (see k_pointwise.cu).
 #include "precision.cuh"
 #include "stencil_util.cuh"
+#include "tangent.cuh"
 
 namespace oeb {
 namespace {
@@ -32,7 +33,8 @@ __global__ void __launch_bounds__(kThreads) fastwavesuv_kernel(
     const T* __restrict__ utens, const T* __restrict__ vtens, const T* __restrict__ wgtfac,
     const T* __restrict__ ppuv, const T* __restrict__ hhl, const T* __restrict__ rho, const T* __restrict__ fx,
     int64_t s1d, T ed2, T dt, Dims d, int kb) {
-  __shared__ FastwavesSmem<T> s;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FastwavesSmem<T>& s = *reinterpret_cast<FastwavesSmem<T>*>(smem_raw);
   const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
   const int sj = (int)d.sj;
   const int64_t sk = d.sk;
@@ -137,9 +139,202 @@ oeb_status fastwavesuv_entry(const M3* uout, const M3* vout, const M3* uin, cons
   OEB_RETURN_IF_VALIDATING();
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gu.sj, gu.sk};
   const T ed2 = T(2.0) * edadlat;  // ElementType(2.0) * edadlat, fastwavesuv.h:186
-  fastwavesuv_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
+  OEB_TRY(ensure_dyn_smem((const void*)fastwavesuv_kernel<T>, (int)sizeof(FastwavesSmem<T>)));
+  fastwavesuv_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FastwavesSmem<T>),
+                          (cudaStream_t)stream>>>(
       gu.origin, gv.origin, gui.origin, gvi.origin, gut.origin, gvt.origin, gw.origin, gp.origin, gh.origin,
       gr.origin, lfx.origin, lfx.s, ed2, dt, d, kKB);
+  return after_launch();
+}
+
+// Tangent-linear fastwavesuv with respect to (uin, vin, utens, vtens, ppuv); wgtfac, hhl,
+// rho and fx are parameters.  The map is linear in these inputs, so this is also the
+// forward stencil applied to the perturbation; it runs on Dual<T> like the others.
+template <class T, class M3, class M1>
+oeb_status fastwavesuv_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M3* utens,
+                                const M3* vtens, const M3* wgtfac, const M3* ppuv, const M3* hhl, const M3* rho,
+                                const M1* fx, const M3* duin, const M3* dvin, const M3* dutens, const M3* dvtens,
+                                const M3* dppuv, T edadlat, T dt, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(fastwavesuv_entry<T>(duout, dvout, uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho, fx, edadlat, dt, dom,
+                                 stream));
+    OEB_TRY(fastwavesuv_entry<T>(duout, dvout, duin, dvin, dutens, dvtens, wgtfac, dppuv, hhl, rho, fx, edadlat, dt,
+                                 dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *u, *v, *ut, *vt, *w, *p, *h, *r, *f, *ou, *ov;
+  OEB_TRY(arr.pack(uin, duin, &u));
+  OEB_TRY(arr.pack(vin, dvin, &v));
+  OEB_TRY(arr.pack(utens, dutens, &ut));
+  OEB_TRY(arr.pack(vtens, dvtens, &vt));
+  OEB_TRY(arr.pack(wgtfac, (const M3*)nullptr, &w));
+  OEB_TRY(arr.pack(ppuv, dppuv, &p));
+  OEB_TRY(arr.pack(hhl, (const M3*)nullptr, &h));
+  OEB_TRY(arr.pack(rho, (const M3*)nullptr, &r));
+  OEB_TRY(arr.pack(fx, (const M1*)nullptr, &f));
+  OEB_TRY(arr.alloc(duout, &ou));
+  OEB_TRY(arr.alloc(dvout, &ov));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
+  const D ed2 = D(T(2.0) * edadlat);
+  OEB_TRY(ensure_dyn_smem((const void*)fastwavesuv_kernel<D>, (int)sizeof(FastwavesSmem<D>)));
+  fastwavesuv_kernel<D><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FastwavesSmem<D>),
+                          (cudaStream_t)stream>>>(ou, ov, u, v, ut, vt, w, p, h, r, f, fx->strides[0], ed2, D(dt), d,
+                                                  kKB);
+  OEB_TRY(after_launch());
+  OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
+}
+
+// ============================== adjoint ===========================================
+// fastwavesuv is linear in x = (uin, vin, utens, vtens, ppuv) for fixed wgtfac, hhl, rho, fx:
+//   uout = uin + dt (utens - ppgu qx),  qx = 2 fx(j) / (rho(i+1) + rho(i))
+//   ppgu = (ppuv(i+1) - ppuv(i)) + (ppgc(i+1) + ppgc(i)) gx,  gx = 0.5 Hs / Hd   (fastwavesuv.h:172-175)
+//   ppgc(k) = ppgk(k+1) - ppgk(k),  ppgk(k) = w(k) ppuv(k) + (1 - w(k)) ppuv(k-1)
+// and likewise in j.  Its transpose, written as gathers (no atomics), for ybar = (uoutb, voutb):
+//   uinb = uoutb, utensb = dt uoutb (and v), and with au = -dt qx uoutb, av = -dt qy voutb,
+//   cb(i,j,k)  = au(i) gx(i) + au(i-1) gx(i-1) + av(j) gy(j) + av(j-1) gy(j-1)     (ppgc adjoint)
+//   kb(k)      = cb(k-1) - cb(k)                                                   (ppgk adjoint)
+//   ppuvb(k)   = w(k) kb(k) + (1 - w(k+1)) kb(k+1) + au(i-1) - au(i) + av(j-1) - av(j)
+// with every coefficient zero off the interior.  ppuvb covers i in [0,N], j in [0,N],
+// k in [-1,N_z] (the reach of ppuv).  One CTA marches a 32 x 32 tile of that box through a
+// chunk of k-levels, keeping cb at three levels in registers.
+template <class T>
+struct FastwavesAdjSmem {
+  T ax[kT][kR];  // au(i0-1+a, j0+b) gx, then au itself in the second half
+  T au[kT][kR];
+  T ay[kR][kT];  // av(i0+a, j0-1+b) gy
+  T av[kR][kT];
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) fastwavesuv_adj_kernel(
+    T* __restrict__ uinb, T* __restrict__ vinb, T* __restrict__ utensb, T* __restrict__ vtensb,
+    T* __restrict__ ppuvb, const T* __restrict__ wgtfac, const T* __restrict__ hhl, const T* __restrict__ rho,
+    const T* __restrict__ fx, int64_t s1d, const T* __restrict__ uoutb, const T* __restrict__ voutb, T ed2, T dt,
+    Dims d, int kb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FastwavesAdjSmem<T>& s = *reinterpret_cast<FastwavesAdjSmem<T>*>(smem_raw);
+  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
+  const int sj = (int)d.sj;
+  const int64_t sk = d.sk;
+  // output levels K in [Ks, Ke) of the extended range [-1, nz+1)
+  const int Ks = -1 + (int)blockIdx.z * kb, Ke = min(Ks + kb, d.nz + 1);
+  constexpr int kPts = kT * kT / kThreads;
+  T cm2[kPts], cm1[kPts], dir[kPts];  // cb(L-2), cb(L-1), direct terms of level L-1
+#pragma unroll
+  for (int t = 0; t < kPts; ++t) cm2[t] = cm1[t] = dir[t] = T(0);
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  // adjoint of ppgu (au) and of ppgv (av) at an interior point, times g when asked
+  auto au_at = [&](int i, int j, int k, bool with_g) -> T {
+    if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
+    const int64_t o = (int64_t)k * sk + i + j * sj;
+    const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
+    const T a = -(dt * qx) * ld(uoutb + o);
+    if (!with_g) return a;
+    const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
+    const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
+    return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+  };
+  auto av_at = [&](int i, int j, int k, bool with_g) -> T {
+    if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
+    const int64_t o = (int64_t)k * sk + i + j * sj;
+    const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
+    const T a = -(dt * qy) * ld(voutb + o);
+    if (!with_g) return a;
+    const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
+    const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
+    return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+  };
+#pragma unroll 1
+  for (int L = Ks - 1; L <= Ke; ++L) {
+    // au, av and their g-weighted versions at level L over the tile plus the low apron
+    for_region<kR, kT>([&](int a, int b) {
+      const int i = i0 - 1 + a, j = j0 + b;
+      const T raw = au_at(i, j, L, false);
+      s.au[b][a] = raw;
+      s.ax[b][a] = (raw == T(0)) ? T(0) : au_at(i, j, L, true);
+    });
+    for_region<kT, kR>([&](int a, int b) {
+      const int i = i0 + a, j = j0 - 1 + b;
+      const T raw = av_at(i, j, L, false);
+      s.av[b][a] = raw;
+      s.ay[b][a] = (raw == T(0)) ? T(0) : av_at(i, j, L, true);
+    });
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < kPts; ++t) {
+      const int e = tid + t * kThreads;
+      const int b = e / kT, a = e - b * kT;
+      const int i = i0 + a, j = j0 + b;
+      // cb(L) at (i, j): ppgc(i) feeds ppgu(i), ppgu(i-1), ppgv(j), ppgv(j-1)
+      const T cl = (L >= 0 && L < d.nz) ? ((s.ax[b][a + 1] + s.ax[b][a]) + (s.ay[b + 1][a] + s.ay[b][a])) : T(0);
+      const int K = L - 1;  // output level
+      if (K >= Ks && K < Ke && i <= d.nx && j <= d.ny) {
+        const int64_t o = (int64_t)K * sk + i + j * sj;
+        const T kbK = cm2[t] - cm1[t];  // kb(K)   = cb(K-1) - cb(K)
+        const T kbK1 = cm1[t] - cl;     // kb(K+1) = cb(K)   - cb(K+1)
+        T acc = dir[t];
+        if (K >= 0) acc = acc + ld(wgtfac + o) * kbK;
+        if (K + 1 <= d.nz) acc = acc + (T(1.0) - ld(wgtfac + o + sk)) * kbK1;
+        ppuvb[o] = acc;
+        if (K >= 0 && K < d.nz && i < d.nx && j < d.ny) {
+          const T ub = ld(uoutb + o), vb = ld(voutb + o);
+          uinb[o] = ub;
+          vinb[o] = vb;
+          utensb[o] = dt * ub;
+          vtensb[o] = dt * vb;
+        }
+      }
+      // direct terms of level L: au(i-1) - au(i) + av(j-1) - av(j)
+      dir[t] = (s.au[b][a] - s.au[b][a + 1]) + (s.av[b][a] - s.av[b + 1][a]);
+      cm2[t] = cm1[t];
+      cm1[t] = cl;
+    }
+    __syncthreads();
+  }
+}
+
+template <class T, class M3, class M1>
+oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utensb, const M3* vtensb,
+                                 const M3* ppuvb, const M3* uin, const M3* vin, const M3* utens, const M3* vtens,
+                                 const M3* wgtfac, const M3* ppuv, const M3* hhl, const M3* rho, const M1* fx,
+                                 const M3* uoutb, const M3* voutb, T edadlat, T dt, const oeb_domain* dom,
+                                 void* stream) {
+  {
+    // the state as the forward sees it, with the adjoint seeds in the outputs' places
+    ValidateOnly guard;
+    OEB_TRY(fastwavesuv_entry<T>(uoutb, voutb, uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho, fx, edadlat, dt, dom,
+                                 stream));
+  }
+  OEB_TRY(check_domain(dom));
+  Grid<T> gub, gvb, gutb, gvtb, gpb, gw, gh, gr, guo, gvo;
+  Line<T> lfx;
+  OEB_TRY((check_field3<T>(uinb, *dom, kInterior, &gub)));
+  OEB_TRY((check_field3<T>(vinb, *dom, kInterior, &gvb)));
+  OEB_TRY((check_field3<T>(utensb, *dom, kInterior, &gutb)));
+  OEB_TRY((check_field3<T>(vtensb, *dom, kInterior, &gvtb)));
+  OEB_TRY((check_field3<T>(ppuvb, *dom, Reach{0, 1, 0, 1, 1, 1}, &gpb)));
+  OEB_TRY((check_field3<T>(wgtfac, *dom, Reach{0, 1, 0, 1, 0, 1}, &gw)));
+  OEB_TRY((check_field3<T>(hhl, *dom, Reach{0, 1, 0, 1, 0, 1}, &gh)));
+  OEB_TRY((check_field3<T>(rho, *dom, Reach{0, 1, 0, 1, 0, 0}, &gr)));
+  OEB_TRY((check_field3<T>(uoutb, *dom, kInterior, &guo)));
+  OEB_TRY((check_field3<T>(voutb, *dom, kInterior, &gvo)));
+  OEB_TRY((check_field1<T>(fx, *dom, 0, 0, &lfx)));
+  OEB_TRY(check_same_strides<T>({&gub, &gvb, &gutb, &gvtb, &gpb, &gw, &gh, &gr, &guo, &gvo}));
+  OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi, gutb.lo, gutb.hi, gvtb.lo, gvtb.hi, gpb.lo, gpb.hi},
+                         {gw.lo, gw.hi, gh.lo, gh.hi, gr.lo, gr.hi, guo.lo, guo.hi, gvo.lo, gvo.hi, lfx.lo, lfx.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gw.sj, gw.sk};
+  const T ed2 = T(2.0) * edadlat;
+  const size_t smem = sizeof(FastwavesAdjSmem<T>);
+  OEB_TRY(ensure_dyn_smem((const void*)fastwavesuv_adj_kernel<T>, (int)smem));
+  fastwavesuv_adj_kernel<T><<<tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kKB), dim3(kTX, kTY), smem,
+                              (cudaStream_t)stream>>>(gub.origin, gvb.origin, gutb.origin, gvtb.origin, gpb.origin,
+                                                      gw.origin, gh.origin, gr.origin, lfx.origin, lfx.s, guo.origin,
+                                                      gvo.origin, ed2, dt, d, kKB);
   return after_launch();
 }
 
@@ -157,6 +352,26 @@ using namespace oeb;
       void* stream) {                                                                                              \
     return fastwavesuv_entry<T>(uout, vout, uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho, fx, edadlat, dt, dom,  \
                                 stream);                                                                           \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_fastwavesuv_tl_##S(                                                                    \
+      const oeb_memref3d_##S* duout, const oeb_memref3d_##S* dvout, const oeb_memref3d_##S* uin,                    \
+      const oeb_memref3d_##S* vin, const oeb_memref3d_##S* utens, const oeb_memref3d_##S* vtens,                    \
+      const oeb_memref3d_##S* wgtfac, const oeb_memref3d_##S* ppuv, const oeb_memref3d_##S* hhl,                    \
+      const oeb_memref3d_##S* rho, const oeb_memref1d_##S* fx, const oeb_memref3d_##S* duin,                        \
+      const oeb_memref3d_##S* dvin, const oeb_memref3d_##S* dutens, const oeb_memref3d_##S* dvtens,                 \
+      const oeb_memref3d_##S* dppuv, T edadlat, T dt, const oeb_domain* dom, void* stream) {                        \
+    return fastwavesuv_tl_entry<T>(duout, dvout, uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho, fx, duin, dvin,    \
+                                   dutens, dvtens, dppuv, edadlat, dt, dom, stream);                               \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_fastwavesuv_adj_##S(                                                                   \
+      const oeb_memref3d_##S* uinb, const oeb_memref3d_##S* vinb, const oeb_memref3d_##S* utensb,                   \
+      const oeb_memref3d_##S* vtensb, const oeb_memref3d_##S* ppuvb, const oeb_memref3d_##S* uin,                   \
+      const oeb_memref3d_##S* vin, const oeb_memref3d_##S* utens, const oeb_memref3d_##S* vtens,                    \
+      const oeb_memref3d_##S* wgtfac, const oeb_memref3d_##S* ppuv, const oeb_memref3d_##S* hhl,                    \
+      const oeb_memref3d_##S* rho, const oeb_memref1d_##S* fx, const oeb_memref3d_##S* uoutb,                       \
+      const oeb_memref3d_##S* voutb, T edadlat, T dt, const oeb_domain* dom, void* stream) {                        \
+    return fastwavesuv_adj_entry<T>(uinb, vinb, utensb, vtensb, ppuvb, uin, vin, utens, vtens, wgtfac, ppuv, hhl,   \
+                                    rho, fx, uoutb, voutb, edadlat, dt, dom, stream);                              \
   }
 
 OEB_FW_ENTRY(f64, double)

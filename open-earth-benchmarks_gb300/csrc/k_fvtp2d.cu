@@ -17,6 +17,7 @@
 #include "oeb_reach.cuh"
 #include "precision.cuh"
 #include "stencil_util.cuh"
+#include "tangent.cuh"
 
 namespace oeb {
 namespace {
@@ -302,6 +303,359 @@ oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* f
   return after_launch();
 }
 
+// Tangent-linear fvtp2d with respect to q (the PPM flags frozen at q; the Courant numbers,
+// fluxes and areas are parameters): derivatives of all six outputs, on Dual<T>.
+template <class T, class M3>
+oeb_status fvtp2d_tl_entry(const M3* dq_i, const M3* dq_j, const M3* dfx1, const M3* dfx2, const M3* dfy1,
+                           const M3* dfy2, const M3* q, const M3* crx, const M3* cry, const M3* ra_x, const M3* ra_y,
+                           const M3* xfx, const M3* yfx, const M3* area, const M3* dq, T p1, T p2,
+                           const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(fvtp2d_entry<T>(dq_i, dq_j, dfx1, dfx2, dfy1, dfy2, q, crx, cry, ra_x, ra_y, xfx, yfx, area, p1, p2, dom,
+                            stream));
+    OEB_TRY(fvtp2d_entry<T>(dq_i, dq_j, dfx1, dfx2, dfy1, dfy2, dq, crx, cry, ra_x, ra_y, xfx, yfx, area, p1, p2, dom,
+                            stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  cudaStream_t st = (cudaStream_t)stream;
+  DualArrays<T> arr(st);
+  D *x, *cx, *cy, *rx, *ry, *xf, *yf, *ar, *oqi, *oqj, *ofx1, *ofx2, *ofy1, *ofy2;
+  OEB_TRY(arr.pack(q, dq, &x));
+  OEB_TRY(arr.pack(crx, (const M3*)nullptr, &cx));
+  OEB_TRY(arr.pack(cry, (const M3*)nullptr, &cy));
+  OEB_TRY(arr.pack(ra_x, (const M3*)nullptr, &rx));
+  OEB_TRY(arr.pack(ra_y, (const M3*)nullptr, &ry));
+  OEB_TRY(arr.pack(xfx, (const M3*)nullptr, &xf));
+  OEB_TRY(arr.pack(yfx, (const M3*)nullptr, &yf));
+  OEB_TRY(arr.pack(area, (const M3*)nullptr, &ar));
+  OEB_TRY(arr.alloc(dq_i, &oqi));
+  OEB_TRY(arr.alloc(dq_j, &oqj));
+  OEB_TRY(arr.alloc(dfx1, &ofx1));
+  OEB_TRY(arr.alloc(dfx2, &ofx2));
+  OEB_TRY(arr.alloc(dfy1, &ofy1));
+  OEB_TRY(arr.alloc(dfy2, &ofy2));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, q->strides[1], q->strides[0]};
+  OEB_TRY(ensure_dyn_smem((const void*)fvtp2d_q_kernel<D>, (int)sizeof(FvQSmem<D>)));
+  OEB_TRY(ensure_dyn_smem((const void*)fvtp2d_flux_kernel<D>, (int)sizeof(FvFluxSmem<D>)));
+  fvtp2d_q_kernel<D><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvQSmem<D>), st>>>(
+      oqi, oqj, ofx2, ofy2, x, cx, cy, rx, ry, xf, yf, ar, D(p1), D(p2), d, kKB);
+  OEB_TRY(after_launch());
+  fvtp2d_flux_kernel<D><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvFluxSmem<D>), st>>>(
+      ofx1, ofy1, oqi, oqj, ofx2, ofy2, cx, cy, xf, yf, D(p1), D(p2), d, kKB);
+  OEB_TRY(after_launch());
+  OEB_TRY(arr.unpack(dq_i->aligned + dq_i->offset, oqi, *dom, kFvQi, d.sj, d.sk));
+  OEB_TRY(arr.unpack(dq_j->aligned + dq_j->offset, oqj, *dom, kFvQj, d.sj, d.sk));
+  OEB_TRY(arr.unpack(dfx1->aligned + dfx1->offset, ofx1, *dom, kInterior, d.sj, d.sk));
+  OEB_TRY(arr.unpack(dfx2->aligned + dfx2->offset, ofx2, *dom, kFvFx2, d.sj, d.sk));
+  OEB_TRY(arr.unpack(dfy1->aligned + dfy1->offset, ofy1, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dfy2->aligned + dfy2->offset, ofy2, *dom, kFvFy2, d.sj, d.sk);
+}
+
+// ============================== adjoint ===========================================
+// fvtp2d is linear in q once the PPM flags smt5 (and the upwind choice c > 0) are frozen
+// at the state.  With ybar = (fx1b, fy1b) on the interior and gx = xfx fx1b / 2,
+// gy = yfx fy1b / 2, the transpose is (fvtp2d.h:39-51, 115-127, 160-176 read backwards):
+//   q_ib = PPMx^T(gx) on q_i's flags,  q_jb = PPMy^T(gy) on q_j's flags
+//   fy2b = gy + yfx (q_ib / ra_y - q_ib(j-1) / ra_y(j-1)),  fx2b = gx + xfx (q_jb / ra_x - q_jb(i-1) / ra_x(i-1))
+//   qb   = area/ra_y q_ib + area/ra_x q_jb + PPMy^T(fy2b) + PPMx^T(fx2b)
+// q_i and q_j are recomputed by the forward kernel (recompute, not store).  The transpose
+// of one PPM sweep (fvtp2d.h:20-34) is, per flux point j with tb = s (1 -+ c) Fb:
+//   B0(j) = [c(j+1)>0] (-c(j+1)) tb(j+1) + [c(j)<=0] c(j) tb(j),  ALM(j) = [c(j)<=0] tb(j) + B0(j)
+//   BR(j) = [c(j+1)>0] tb(j+1) + B0(j),  AL(j) = ALM(j) + BR(j-1)
+//   gb(j) = [c(j+1)>0] Fb(j+1) + [c(j)<=0] Fb(j) - ALM(j) - BR(j)
+//           + p1 (AL(j+1) + AL(j)) + p2 (AL(j+2) + AL(j-1))
+// computed per CTA on a 32-line x 44-position shared window (positions A-5 .. A+38 along the
+// sweep axis for the 32 outputs A .. A+31).
+
+constexpr int kW = 44;  // window along the sweep axis: outputs A..A+31 need A-5 .. A+38
+
+template <class T>
+struct PpmAdjSmem {
+  T gs[32][kW];   // state values of the swept field
+  T als[32][kW];  // state edge values al
+  T tb[32][kW];
+  T alm[32][kW];
+  T br[32][kW];
+  T al[32][kW];
+  unsigned char smt[32][kW];
+};
+
+// One transposed PPM sweep along AXIS (0: i, 1: j) for outputs A..A+31 on lines L0..L0+31.
+// gst(p, l): state value at axis position p of line l (0 where the field is not defined);
+// cv(p, l): Courant number at flux point p (any value elsewhere);
+// fb(p, l): flux adjoint at p (0 off the flux points);  put(a, l, v): receives gbar(a).
+template <class T, int AXIS, class GS, class CV, class FB, class PUT>
+__device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L0, T p1, T p2, GS&& gst, CV&& cv,
+                                                  FB&& fb, PUT&& put) {
+  auto region = [&](int w0, int w1, auto&& f) {
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    const int W = w1 - w0;
+    for (int e = tid; e < W * 32; e += kThreads) {
+      int w, l;
+      if (AXIS == 0) {
+        l = e / W;
+        w = w0 + (e - l * W);
+      } else {
+        w = w0 + e / 32;
+        l = e - (e / 32) * 32;
+      }
+      f(w, l);
+    }
+  };
+  region(0, kW, [&](int w, int l) { s.gs[l][w] = gst(A - 5 + w, L0 + l); });
+  __syncthreads();
+  region(2, kW - 1, [&](int w, int l) {
+    s.als[l][w] = (p1 * (s.gs[l][w - 1] + s.gs[l][w])) + (p2 * (s.gs[l][w - 2] + s.gs[l][w + 1]));
+  });
+  __syncthreads();
+  region(2, kW - 2, [&](int w, int l) {
+    s.smt[l][w] = Prec<T>::prod_lt0(s.als[l][w] - s.gs[l][w], s.als[l][w + 1] - s.gs[l][w]);
+  });
+  __syncthreads();
+  region(3, kW - 2, [&](int w, int l) {
+    const int p = A - 5 + w;
+    const T f = fb(p, L0 + l);
+    T t = T(0);
+    if (f != T(0) && (s.smt[l][w - 1] | s.smt[l][w])) {
+      const T c = cv(p, L0 + l);
+      t = f * ((c > T(0)) ? (T(1) - c) : (T(1) + c));
+    }
+    s.tb[l][w] = t;
+  });
+  __syncthreads();
+  region(3, kW - 3, [&](int w, int l) {
+    const int p = A - 5 + w;
+    const T t0 = s.tb[l][w], t1 = s.tb[l][w + 1];
+    T b0 = T(0), am = T(0), bb = T(0);
+    if (t1 != T(0)) {
+      const T c1 = cv(p + 1, L0 + l);
+      if (c1 > T(0)) {
+        b0 = -c1 * t1;
+        bb = t1;
+      }
+    }
+    if (t0 != T(0)) {
+      const T c0 = cv(p, L0 + l);
+      if (!(c0 > T(0))) {
+        b0 = b0 + c0 * t0;
+        am = t0;
+      }
+    }
+    s.alm[l][w] = am + b0;
+    s.br[l][w] = bb + b0;
+  });
+  __syncthreads();
+  region(4, kW - 3, [&](int w, int l) { s.al[l][w] = s.alm[l][w] + s.br[l][w - 1]; });
+  __syncthreads();
+  region(5, 5 + 32, [&](int w, int l) {
+    const int a = A - 5 + w;
+    T g = (p1 * (s.al[l][w + 1] + s.al[l][w])) + (p2 * (s.al[l][w + 2] + s.al[l][w - 1])) - s.alm[l][w] - s.br[l][w];
+    const T f1 = fb(a + 1, L0 + l);
+    if (f1 != T(0) && cv(a + 1, L0 + l) > T(0)) g = g + f1;
+    const T f0 = fb(a, L0 + l);
+    if (f0 != T(0) && !(cv(a, L0 + l) > T(0))) g = g + f0;
+    put(a, L0 + l, g);
+  });
+  __syncthreads();
+}
+
+// Pass 1: q_ib over i in [-3,N+2), j in [0,N) and q_jb over i in [0,N), j in [-3,N+2).
+template <class T>
+__global__ void __launch_bounds__(kThreads) fvtp2d_adj_qij_kernel(
+    T* __restrict__ qib, T* __restrict__ qjb, const T* __restrict__ q_i, const T* __restrict__ q_j,
+    const T* __restrict__ crx, const T* __restrict__ cry, const T* __restrict__ xfx, const T* __restrict__ yfx,
+    const T* __restrict__ fx1b, const T* __restrict__ fy1b, T p1, T p2, Dims d, int AXIS_Y) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
+  const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
+  const int64_t kofs = (int64_t)blockIdx.z * d.sk;
+  if (!AXIS_Y) {
+    // x sweep of fx1 on q_i: outputs i in [-3, nx+2), lines j in [0, ny)
+    const int A = -3 + (int)blockIdx.x * 32, L0 = (int)blockIdx.y * 32;
+    ppm_sweep_adjoint<T, 0>(
+        s, A, L0, p1, p2,
+        [&](int p, int l) { return (p >= -3 && p < nx + 2 && l < ny) ? ld(q_i + kofs + p + l * sj) : T(0); },
+        [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
+        [&](int p, int l) {
+          return (p >= 0 && p < nx && l < ny) ? (T(0.5) * ld(xfx + kofs + p + l * sj)) * ld(fx1b + kofs + p + l * sj)
+                                             : T(0);
+        },
+        [&](int a, int l, T v) {
+          if (a >= -3 && a < nx + 2 && l < ny) qib[kofs + a + l * sj] = v;
+        });
+  } else {
+    // y sweep of fy1 on q_j: outputs j in [-3, ny+2), lines i in [0, nx)
+    const int A = -3 + (int)blockIdx.x * 32, L0 = (int)blockIdx.y * 32;
+    ppm_sweep_adjoint<T, 1>(
+        s, A, L0, p1, p2,
+        [&](int p, int l) { return (p >= -3 && p < ny + 2 && l < nx) ? ld(q_j + kofs + l + p * sj) : T(0); },
+        [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
+        [&](int p, int l) {
+          return (p >= 0 && p < ny && l < nx) ? (T(0.5) * ld(yfx + kofs + l + p * sj)) * ld(fy1b + kofs + l + p * sj)
+                                             : T(0);
+        },
+        [&](int a, int l, T v) {
+          if (a >= -3 && a < ny + 2 && l < nx) qjb[kofs + l + a * sj] = v;
+        });
+  }
+}
+
+// Pass 2: fy2b on [-3,N+2) x [0,N+1) and fx2b on [0,N+1) x [-3,N+2).
+template <class T>
+__global__ void __launch_bounds__(kThreads) fvtp2d_adj_f2_kernel(
+    T* __restrict__ fx2b, T* __restrict__ fy2b, const T* __restrict__ qib, const T* __restrict__ qjb,
+    const T* __restrict__ xfx, const T* __restrict__ yfx, const T* __restrict__ ra_x, const T* __restrict__ ra_y,
+    const T* __restrict__ fx1b, const T* __restrict__ fy1b, Dims d, int kb) {
+  const int nx = d.nx, ny = d.ny;
+  const int64_t sj = d.sj;
+  for_box(d, -3, -3, nx + 5, ny + 5, kb, [&](int64_t o, int i, int j) {
+    const bool interior = i >= 0 && i < nx && j >= 0 && j < ny;
+    if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {
+      T g = interior ? (T(0.5) * ld(yfx + o)) * ld(fy1b + o) : T(0);
+      const T a = (j < ny) ? qib[o] / ld(ra_y + o) : T(0);
+      const T b = (j >= 1) ? qib[o - sj] / ld(ra_y + o - sj) : T(0);
+      fy2b[o] = g + ld(yfx + o) * (a - b);
+    }
+    if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {
+      T g = interior ? (T(0.5) * ld(xfx + o)) * ld(fx1b + o) : T(0);
+      const T a = (i < nx) ? qjb[o] / ld(ra_x + o) : T(0);
+      const T b = (i >= 1) ? qjb[o - 1] / ld(ra_x + o - 1) : T(0);
+      fx2b[o] = g + ld(xfx + o) * (a - b);
+    }
+  });
+}
+
+// Pass 3: qb on [-3,N+3)^2: area terms + PPMx^T(fx2b) (x sweep, writes), then
+// pass 4: + PPMy^T(fy2b) (y sweep, adds).
+template <class T>
+__global__ void __launch_bounds__(kThreads) fvtp2d_adj_q_kernel(
+    T* __restrict__ qb, const T* __restrict__ q, const T* __restrict__ crx, const T* __restrict__ cry,
+    const T* __restrict__ area, const T* __restrict__ ra_x, const T* __restrict__ ra_y, const T* __restrict__ qib,
+    const T* __restrict__ qjb, const T* __restrict__ fx2b, const T* __restrict__ fy2b, T p1, T p2, Dims d,
+    int AXIS_Y) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
+  const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
+  const int64_t kofs = (int64_t)blockIdx.z * d.sk;
+  auto qval = [&](int i, int j) {
+    return (i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3) ? ld(q + kofs + i + j * sj) : T(0);
+  };
+  const int A = -3 + (int)blockIdx.x * 32, L0 = -3 + (int)blockIdx.y * 32;
+  if (!AXIS_Y) {
+    // x sweep of fx2 on q: flux points i in [0, nx+1), lines j in [-3, ny+2)
+    ppm_sweep_adjoint<T, 0>(
+        s, A, L0, p1, p2, [&](int p, int l) { return qval(p, l); },
+        [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
+        [&](int p, int l) {
+          return (p >= 0 && p < nx + 1 && l >= -3 && l < ny + 2) ? fx2b[kofs + p + l * sj] : T(0);
+        },
+        [&](int a, int l, T v) {
+          if (a >= -3 && a < nx + 3 && l >= -3 && l < ny + 3) {
+            const int64_t o = kofs + a + l * sj;
+            T acc = v;
+            if (a >= -3 && a < nx + 2 && l >= 0 && l < ny) acc = acc + (ld(area + o) / ld(ra_y + o)) * qib[o];
+            if (a >= 0 && a < nx && l >= -3 && l < ny + 2) acc = acc + (ld(area + o) / ld(ra_x + o)) * qjb[o];
+            qb[o] = acc;
+          }
+        });
+  } else {
+    // y sweep of fy2 on q: flux points j in [0, ny+1), lines i in [-3, nx+2); adds to qb
+    ppm_sweep_adjoint<T, 1>(
+        s, A, L0, p1, p2, [&](int p, int l) { return qval(l, p); },
+        [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
+        [&](int p, int l) {
+          return (p >= 0 && p < ny + 1 && l >= -3 && l < nx + 2) ? fy2b[kofs + l + p * sj] : T(0);
+        },
+        [&](int a, int l, T v) {
+          if (a >= -3 && a < ny + 3 && l >= -3 && l < nx + 3) qb[kofs + l + a * sj] = qb[kofs + l + a * sj] + v;
+        });
+  }
+}
+
+template <class T, class M3>
+oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* cry, const M3* ra_x, const M3* ra_y,
+                            const M3* xfx, const M3* yfx, const M3* area, const M3* fx1b, const M3* fy1b, T p1, T p2,
+                            const oeb_domain* dom, void* stream) {
+  OEB_TRY(check_domain(dom));
+  Grid<T> gqb, gq, gcx, gcy, grx, gry, gxf, gyf, gar, gf1, gg1;
+  OEB_TRY((check_field3<T>(qb, *dom, Reach{3, 3, 3, 3, 0, 0}, &gqb)));
+  OEB_TRY((check_field3<T>(q, *dom, Reach{3, 3, 3, 3, 0, 0}, &gq)));
+  OEB_TRY((check_field3<T>(crx, *dom, kFvFx2, &gcx)));
+  OEB_TRY((check_field3<T>(cry, *dom, kFvFy2, &gcy)));
+  OEB_TRY((check_field3<T>(ra_x, *dom, Reach{0, 0, 3, 2, 0, 0}, &grx)));
+  OEB_TRY((check_field3<T>(ra_y, *dom, Reach{3, 2, 0, 0, 0, 0}, &gry)));
+  OEB_TRY((check_field3<T>(xfx, *dom, kFvFx2, &gxf)));
+  OEB_TRY((check_field3<T>(yfx, *dom, kFvFy2, &gyf)));
+  OEB_TRY((check_field3<T>(area, *dom, Reach{3, 2, 3, 2, 0, 0}, &gar)));
+  OEB_TRY((check_field3<T>(fx1b, *dom, kInterior, &gf1)));
+  OEB_TRY((check_field3<T>(fy1b, *dom, kInterior, &gg1)));
+  OEB_TRY(check_same_strides<T>({&gqb, &gq, &gcx, &gcy, &grx, &gry, &gxf, &gyf, &gar, &gf1, &gg1}));
+  OEB_TRY(check_no_alias({gqb.lo, gqb.hi}, {gq.lo, gq.hi, gcx.lo, gcx.hi, gcy.lo, gcy.hi, grx.lo, grx.hi, gry.lo,
+                                            gry.hi, gxf.lo, gxf.hi, gyf.lo, gyf.hi, gar.lo, gar.hi, gf1.lo, gf1.hi,
+                                            gg1.lo, gg1.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  OEB_TRY(device_pool(&pool));
+  // scratch in q's layout: q_i, q_j, fx2, fy2 (forward recompute), q_ib, q_jb, fx2b, fy2b
+  const T* start = (q->allocated && q->allocated <= q->aligned) ? q->allocated : q->aligned;
+  const int64_t last = (q->sizes[0] - 1) * q->strides[0] + (q->sizes[1] - 1) * q->strides[1] +
+                       (q->sizes[2] - 1) * q->strides[2];
+  const int64_t n = (int64_t)(q->aligned - start) + last + 1;
+  const int64_t org = (int64_t)(q->aligned - start) + q->offset;
+  void* buf = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&buf, (size_t)n * 8 * sizeof(T), pool, st);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  T* base = static_cast<T*>(buf);
+  T *sqi = base + org, *sqj = base + n + org, *sfx2 = base + 2 * n + org, *sfy2 = base + 3 * n + org,
+    *qib = base + 4 * n + org, *qjb = base + 5 * n + org, *fx2b = base + 6 * n + org, *fy2b = base + 7 * n + org;
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
+  oeb_status stt = ensure_dyn_smem((const void*)fvtp2d_q_kernel<T>, (int)sizeof(FvQSmem<T>));
+  if (stt == OEB_OK) stt = ensure_dyn_smem((const void*)fvtp2d_adj_qij_kernel<T>, (int)sizeof(PpmAdjSmem<T>));
+  if (stt == OEB_OK) stt = ensure_dyn_smem((const void*)fvtp2d_adj_q_kernel<T>, (int)sizeof(PpmAdjSmem<T>));
+  if (stt == OEB_OK) {
+    fvtp2d_q_kernel<T><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvQSmem<T>), st>>>(
+        sqi, sqj, sfx2, sfy2, gq.origin, gcx.origin, gcy.origin, grx.origin, gry.origin, gxf.origin, gyf.origin,
+        gar.origin, p1, p2, d, kKB);
+    stt = after_launch();
+  }
+  const size_t ps = sizeof(PpmAdjSmem<T>);
+  if (stt == OEB_OK) {
+    fvtp2d_adj_qij_kernel<T><<<dim3((d.nx + 5 + 31) / 32, (d.ny + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
+        qib, qjb, sqi, sqj, gcx.origin, gcy.origin, gxf.origin, gyf.origin, gf1.origin, gg1.origin, p1, p2, d, 0);
+    stt = after_launch();
+  }
+  if (stt == OEB_OK) {
+    fvtp2d_adj_qij_kernel<T><<<dim3((d.ny + 5 + 31) / 32, (d.nx + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
+        qib, qjb, sqi, sqj, gcx.origin, gcy.origin, gxf.origin, gyf.origin, gf1.origin, gg1.origin, p1, p2, d, 1);
+    stt = after_launch();
+  }
+  if (stt == OEB_OK) {
+    fvtp2d_adj_f2_kernel<T><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
+        fx2b, fy2b, qib, qjb, gxf.origin, gyf.origin, grx.origin, gry.origin, gf1.origin, gg1.origin, d, kKB);
+    stt = after_launch();
+  }
+  if (stt == OEB_OK) {
+    fvtp2d_adj_q_kernel<T><<<dim3((d.nx + 6 + 31) / 32, (d.ny + 6 + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
+        gqb.origin, gq.origin, gcx.origin, gcy.origin, gar.origin, grx.origin, gry.origin, qib, qjb, fx2b, fy2b, p1,
+        p2, d, 0);
+    stt = after_launch();
+  }
+  if (stt == OEB_OK) {
+    fvtp2d_adj_q_kernel<T><<<dim3((d.ny + 6 + 31) / 32, (d.nx + 6 + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
+        gqb.origin, gq.origin, gcx.origin, gcy.origin, gar.origin, grx.origin, gry.origin, qib, qjb, fx2b, fy2b, p1,
+        p2, d, 1);
+    stt = after_launch();
+  }
+  cudaFreeAsync(buf, st);
+  return stt;
+}
+
 }  // namespace
 }  // namespace oeb
 
@@ -316,6 +670,24 @@ using namespace oeb;
       const oeb_memref3d_##S* yfx, const oeb_memref3d_##S* area, T p1, T p2, const oeb_domain* dom, void* stream) {  \
     return fvtp2d_entry<T>(q_i, q_j, fx1, fx2, fy1, fy2, q, crx, cry, ra_x, ra_y, xfx, yfx, area, p1, p2, dom,       \
                            stream);                                                                                \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_fvtp2d_tl_##S(                                                                         \
+      const oeb_memref3d_##S* dq_i, const oeb_memref3d_##S* dq_j, const oeb_memref3d_##S* dfx1,                     \
+      const oeb_memref3d_##S* dfx2, const oeb_memref3d_##S* dfy1, const oeb_memref3d_##S* dfy2,                     \
+      const oeb_memref3d_##S* q, const oeb_memref3d_##S* crx, const oeb_memref3d_##S* cry,                          \
+      const oeb_memref3d_##S* ra_x, const oeb_memref3d_##S* ra_y, const oeb_memref3d_##S* xfx,                      \
+      const oeb_memref3d_##S* yfx, const oeb_memref3d_##S* area, const oeb_memref3d_##S* dq, T p1, T p2,            \
+      const oeb_domain* dom, void* stream) {                                                                       \
+    return fvtp2d_tl_entry<T>(dq_i, dq_j, dfx1, dfx2, dfy1, dfy2, q, crx, cry, ra_x, ra_y, xfx, yfx, area, dq, p1,  \
+                              p2, dom, stream);                                                                    \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_fvtp2d_adj_##S(                                                                        \
+      const oeb_memref3d_##S* qb, const oeb_memref3d_##S* q, const oeb_memref3d_##S* crx,                          \
+      const oeb_memref3d_##S* cry, const oeb_memref3d_##S* ra_x, const oeb_memref3d_##S* ra_y,                      \
+      const oeb_memref3d_##S* xfx, const oeb_memref3d_##S* yfx, const oeb_memref3d_##S* area,                       \
+      const oeb_memref3d_##S* fx1b, const oeb_memref3d_##S* fy1b, T p1, T p2, const oeb_domain* dom,                \
+      void* stream) {                                                                                              \
+    return fvtp2d_adj_entry<T>(qb, q, crx, cry, ra_x, ra_y, xfx, yfx, area, fx1b, fy1b, p1, p2, dom, stream);      \
   }
 
 OEB_FV_ENTRY(f64, double)

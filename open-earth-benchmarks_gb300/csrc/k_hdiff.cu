@@ -15,6 +15,7 @@
 // 32 x 32 tile and KB k-levels.
 #include "precision.cuh"
 #include "stencil_util.cuh"
+#include "tangent.cuh"
 
 namespace oeb {
 namespace {
@@ -268,6 +269,240 @@ oeb_status hdiffsmag_entry(const M3* uout, const M3* vout, const M3* uin, const 
   return after_launch();
 }
 
+// Tangent-linear hdiffsmag: d(uout, vout) = J(uin, vin) d(uin, vin), the kernel on Dual<T>.
+template <class T, class M3, class M1>
+oeb_status hdiffsmag_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M3* mask,
+                              const M1* crlavo, const M1* crlavu, const M1* crlato, const M1* crlatu,
+                              const M1* acrlat0, const M3* duin, const M3* dvin, T eddlat, T eddlon, T tau_smag,
+                              T weight_smag, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(hdiffsmag_entry<T>(duout, dvout, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, eddlat, eddlon,
+                               tau_smag, weight_smag, dom, stream));
+    OEB_TRY(hdiffsmag_entry<T>(duout, dvout, duin, dvin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, eddlat,
+                               eddlon, tau_smag, weight_smag, dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *u, *v, *m, *l0, *l1, *l2, *l3, *l4, *ou, *ov;
+  OEB_TRY(arr.pack(uin, duin, &u));
+  OEB_TRY(arr.pack(vin, dvin, &v));
+  OEB_TRY(arr.pack(mask, (const M3*)nullptr, &m));
+  OEB_TRY(arr.pack(crlavo, (const M1*)nullptr, &l0));
+  OEB_TRY(arr.pack(crlavu, (const M1*)nullptr, &l1));
+  OEB_TRY(arr.pack(crlato, (const M1*)nullptr, &l2));
+  OEB_TRY(arr.pack(crlatu, (const M1*)nullptr, &l3));
+  OEB_TRY(arr.pack(acrlat0, (const M1*)nullptr, &l4));
+  OEB_TRY(arr.alloc(duout, &ou));
+  OEB_TRY(arr.alloc(dvout, &ov));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
+  const size_t smem = sizeof(HdiffsmagSmem<D>);
+  OEB_TRY(ensure_dyn_smem((const void*)hdiffsmag_kernel<D>, (int)smem));
+  hdiffsmag_kernel<D><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), smem, (cudaStream_t)stream>>>(
+      ou, ov, u, v, m, l0, l1, l2, l3, l4, crlavo->strides[0], D(eddlat), D(eddlon), D(tau_smag), D(weight_smag), d,
+      kKB);
+  OEB_TRY(after_launch());
+  OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
+}
+
+// ============================== hdiffsmag adjoint ================================
+// Linearised at (uin, vin) with the clamp of hdiffsmag.h:236/251 frozen:
+//   uout = u + su Lu,  su = clamp(tau sqrt(Xu) - w mask),  Xu = (T(i+1)^2 + T^2)/2 + (S(j-1)^2 + S^2)/2
+//   T = c1 (v(j-1) - v) - c2 (u(i-1) - u),  S = c1 (u(j+1) - u) + c2 (v(i+1) - v),
+//   c1 = eddlat R^-1, c2(j) = acrlat0(j) eddlon, and likewise vout.
+// The transpose for (uoutb, voutb), in three gather passes over scratch:
+//   1. at interior points: LU = su uoutb, LV = sv voutb, and XU = Lu uoutb tau / (2 sqrt Xu)
+//      where the clamp is open (0 < smag < 0.5), else 0; XV likewise;
+//   2. TB = T (XU(i-1) + XU + XV(j-1) + XV) on [0,N]^2, SB = S (XU(j+1) + XU + XV(i+1) + XV)
+//      on [-1,N)^2 (the T and S adjoints);
+//   3. ubar, vbar on [-1,N+1)^2: identity, the transposed laplacians of LU/LV, and the T/S
+//      differences of TB/SB.
+template <class T>
+struct SmagTerms {
+  T *lu, *lv, *xu, *xv, *tb, *sb;
+};
+
+template <class T>
+__device__ __forceinline__ T smag_T(const T* __restrict__ u, const T* __restrict__ v, int64_t o, int64_t sj, T c1,
+                                    T c2) {
+  return c1 * (ld(v + o - sj) - ld(v + o)) - c2 * (ld(u + o - 1) - ld(u + o));
+}
+template <class T>
+__device__ __forceinline__ T smag_S(const T* __restrict__ u, const T* __restrict__ v, int64_t o, int64_t sj, T c1,
+                                    T c2) {
+  return c1 * (ld(u + o + sj) - ld(u + o)) + c2 * (ld(v + o + 1) - ld(v + o));
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) hdiffsmag_adj_terms_kernel(
+    SmagTerms<T> tm, const T* __restrict__ uin, const T* __restrict__ vin, const T* __restrict__ mask,
+    const T* __restrict__ crlavo, const T* __restrict__ crlavu, const T* __restrict__ crlato,
+    const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d, const T* __restrict__ uoutb,
+    const T* __restrict__ voutb, T eddlat, T eddlon, T tau_smag, T weight_smag, Dims d, int kb) {
+  constexpr T rr = earth_radius_recip<T>();
+  const T c1 = eddlat * rr;
+  const int64_t sj = d.sj;
+  for_box(d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
+    const T c2m = ld(acrlat0 + (int64_t)(j - 1) * s1d) * eddlon, c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon,
+            c2p = ld(acrlat0 + (int64_t)(j + 1) * s1d) * eddlon;
+    const T t0 = smag_T(uin, vin, o, sj, c1, c2), ti = smag_T(uin, vin, o + 1, sj, c1, c2),
+            tj = smag_T(uin, vin, o + sj, sj, c1, c2p);
+    const T s0 = smag_S(uin, vin, o, sj, c1, c2), sjm = smag_S(uin, vin, o - sj, sj, c1, c2m),
+            sim = smag_S(uin, vin, o - 1, sj, c1, c2);
+    const T hdw = weight_smag * ld(mask + o);
+    const T xu = T(0.5) * (ti * ti + t0 * t0) + T(0.5) * (sjm * sjm + s0 * s0);
+    const T xv = T(0.5) * (tj * tj + t0 * t0) + T(0.5) * (sim * sim + s0 * s0);
+    const T ru = Prec<T>::sqrt_(xu), rv = Prec<T>::sqrt_(xv);
+    const T smu = tau_smag * ru - hdw, smv = tau_smag * rv - hdw;
+    const T su = clamp_smag(smu), sv = clamp_smag(smv);
+    const int64_t jo = (int64_t)j * s1d;
+    const T u0 = ld(uin + o), v0 = ld(vin + o);
+    const T lapu = (ld(uin + o + 1) + ld(uin + o - 1) - T(2) * u0) + ld(crlato + jo) * (ld(uin + o + sj) - u0) +
+                   ld(crlatu + jo) * (ld(uin + o - sj) - u0);
+    const T lapv = (ld(vin + o + 1) + ld(vin + o - 1) - T(2) * v0) + ld(crlavo + jo) * (ld(vin + o + sj) - v0) +
+                   ld(crlavu + jo) * (ld(vin + o - sj) - v0);
+    const T yu = ld(uoutb + o), yv = ld(voutb + o);
+    tm.lu[o] = su * yu;
+    tm.lv[o] = sv * yv;
+    tm.xu[o] = (smu > T(0) && smu < T(0.5)) ? (lapu * yu) * (tau_smag / (T(2) * ru)) : T(0);
+    tm.xv[o] = (smv > T(0) && smv < T(0.5)) ? (lapv * yv) * (tau_smag / (T(2) * rv)) : T(0);
+  });
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) hdiffsmag_adj_ts_kernel(SmagTerms<T> tm, const T* __restrict__ uin,
+                                                                    const T* __restrict__ vin,
+                                                                    const T* __restrict__ acrlat0, int64_t s1d,
+                                                                    T eddlat, T eddlon, Dims d, int kb) {
+  constexpr T rr = earth_radius_recip<T>();
+  const T c1 = eddlat * rr;
+  const int64_t sj = d.sj;
+  auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+  for_box(d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int i, int j) {
+    const T c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon;
+    if (i >= 0 && i <= d.nx && j >= 0 && j <= d.ny) {
+      T w = T(0);
+      if (in(i - 1, j)) w = w + tm.xu[o - 1];
+      if (in(i, j)) w = w + tm.xu[o] + tm.xv[o];
+      if (in(i, j - 1)) w = w + tm.xv[o - sj];
+      tm.tb[o] = (w == T(0)) ? T(0) : smag_T(uin, vin, o, sj, c1, c2) * w;
+    }
+    if (i >= -1 && i < d.nx && j >= -1 && j < d.ny) {
+      T w = T(0);
+      if (in(i, j + 1)) w = w + tm.xu[o + sj];
+      if (in(i, j)) w = w + tm.xu[o] + tm.xv[o];
+      if (in(i + 1, j)) w = w + tm.xv[o + 1];
+      tm.sb[o] = (w == T(0)) ? T(0) : smag_S(uin, vin, o, sj, c1, c2) * w;
+    }
+  });
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) hdiffsmag_adj_gather_kernel(
+    T* __restrict__ uinb, T* __restrict__ vinb, SmagTerms<T> tm, const T* __restrict__ uoutb,
+    const T* __restrict__ voutb, const T* __restrict__ crlavo, const T* __restrict__ crlavu,
+    const T* __restrict__ crlato, const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d, T eddlat,
+    T eddlon, Dims d, int kb) {
+  constexpr T rr = earth_radius_recip<T>();
+  const T c1 = eddlat * rr;
+  const int64_t sj = d.sj;
+  auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+  auto inT = [&](int i, int j) { return i >= 0 && i <= d.nx && j >= 0 && j <= d.ny; };
+  auto inS = [&](int i, int j) { return i >= -1 && i < d.nx && j >= -1 && j < d.ny; };
+  for_box(d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int a, int b) {
+    const T c2 = ld(acrlat0 + (int64_t)b * s1d) * eddlon;
+    T ub = T(0), vb = T(0);
+    if (in(a, b)) {
+      const int64_t bo = (int64_t)b * s1d;
+      ub = ld(uoutb + o) - (T(2) + ld(crlato + bo) + ld(crlatu + bo)) * tm.lu[o];
+      vb = ld(voutb + o) - (T(2) + ld(crlavo + bo) + ld(crlavu + bo)) * tm.lv[o];
+    }
+    if (in(a - 1, b)) ub = ub + tm.lu[o - 1], vb = vb + tm.lv[o - 1];
+    if (in(a + 1, b)) ub = ub + tm.lu[o + 1], vb = vb + tm.lv[o + 1];
+    if (in(a, b - 1)) {
+      const int64_t bo = (int64_t)(b - 1) * s1d;
+      ub = ub + ld(crlato + bo) * tm.lu[o - sj];
+      vb = vb + ld(crlavo + bo) * tm.lv[o - sj];
+    }
+    if (in(a, b + 1)) {
+      const int64_t bo = (int64_t)(b + 1) * s1d;
+      ub = ub + ld(crlatu + bo) * tm.lu[o + sj];
+      vb = vb + ld(crlavu + bo) * tm.lv[o + sj];
+    }
+    const T tb0 = inT(a, b) ? tm.tb[o] : T(0);
+    const T sb0 = inS(a, b) ? tm.sb[o] : T(0);
+    if (inT(a + 1, b)) ub = ub - c2 * tm.tb[o + 1];
+    ub = ub + c2 * tb0 - c1 * sb0;
+    if (inS(a, b - 1)) ub = ub + c1 * tm.sb[o - sj];
+    if (inT(a, b + 1)) vb = vb + c1 * tm.tb[o + sj];
+    vb = vb - c1 * tb0 - c2 * sb0;
+    if (inS(a - 1, b)) vb = vb + c2 * tm.sb[o - 1];
+    uinb[o] = ub;
+    vinb[o] = vb;
+  });
+}
+
+template <class T, class M3, class M1>
+oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M3* mask,
+                               const M1* crlavo, const M1* crlavu, const M1* crlato, const M1* crlatu,
+                               const M1* acrlat0, const M3* uoutb, const M3* voutb, T eddlat, T eddlon, T tau_smag,
+                               T weight_smag, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(hdiffsmag_entry<T>(uoutb, voutb, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, eddlat, eddlon,
+                               tau_smag, weight_smag, dom, stream));
+  }
+  Grid<T> gub, gvb, gui, guo;
+  OEB_TRY((check_field3<T>(uinb, *dom, Reach{1, 1, 1, 1, 0, 0}, &gub)));
+  OEB_TRY((check_field3<T>(vinb, *dom, Reach{1, 1, 1, 1, 0, 0}, &gvb)));
+  OEB_TRY((check_field3<T>(uin, *dom, Reach{1, 1, 1, 1, 0, 0}, &gui)));
+  OEB_TRY((check_field3<T>(uoutb, *dom, kInterior, &guo)));
+  OEB_TRY(check_same_strides<T>({&gub, &gvb, &gui, &guo}));
+  OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi}, {gui.lo, gui.hi, guo.lo, guo.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  OEB_TRY(device_pool(&pool));
+  const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
+  const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +
+                       (uin->sizes[2] - 1) * uin->strides[2];
+  const int64_t n = (int64_t)(uin->aligned - start) + last + 1;
+  const int64_t org = (int64_t)(uin->aligned - start) + uin->offset;
+  void* buf = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&buf, (size_t)n * 6 * sizeof(T), pool, st);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  T* base = static_cast<T*>(buf);
+  SmagTerms<T> tm{base + org, base + n + org, base + 2 * n + org, base + 3 * n + org, base + 4 * n + org,
+                  base + 5 * n + org};
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
+  auto org1 = [](const M1* m) { return (const T*)m->aligned + m->offset; };
+  const int64_t s1d = acrlat0->strides[0];
+  cudaStream_t s0 = st;
+  hdiffsmag_adj_terms_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, s0>>>(
+      tm, gui.origin, (const T*)vin->aligned + vin->offset, (const T*)mask->aligned + mask->offset, org1(crlavo),
+      org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d, guo.origin,
+      (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kKB);
+  oeb_status stt = after_launch();
+  if (stt == OEB_OK) {
+    hdiffsmag_adj_ts_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, s0>>>(
+        tm, gui.origin, (const T*)vin->aligned + vin->offset, org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
+    stt = after_launch();
+  }
+  if (stt == OEB_OK) {
+    hdiffsmag_adj_gather_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, s0>>>(
+        gub.origin, gvb.origin, tm, guo.origin, (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu),
+        org1(crlato), org1(crlatu), org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
+    stt = after_launch();
+  }
+  cudaFreeAsync(buf, st);
+  return stt;
+}
+
 }  // namespace
 }  // namespace oeb
 
@@ -287,6 +522,24 @@ using namespace oeb;
       void* stream) {                                                                                              \
     return hdiffsmag_entry<T>(uout, vout, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, eddlat, eddlon,\
                               tau_smag, weight_smag, dom, stream);                                                 \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hdiffsmag_tl_##S(                                                                      \
+      const oeb_memref3d_##S* duout, const oeb_memref3d_##S* dvout, const oeb_memref3d_##S* uin,                    \
+      const oeb_memref3d_##S* vin, const oeb_memref3d_##S* mask, const oeb_memref1d_##S* crlavo,                    \
+      const oeb_memref1d_##S* crlavu, const oeb_memref1d_##S* crlato, const oeb_memref1d_##S* crlatu,               \
+      const oeb_memref1d_##S* acrlat0, const oeb_memref3d_##S* duin, const oeb_memref3d_##S* dvin, T eddlat,        \
+      T eddlon, T tau_smag, T weight_smag, const oeb_domain* dom, void* stream) {                                  \
+    return hdiffsmag_tl_entry<T>(duout, dvout, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, duin, dvin, \
+                                 eddlat, eddlon, tau_smag, weight_smag, dom, stream);                             \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hdiffsmag_adj_##S(                                                                     \
+      const oeb_memref3d_##S* uinb, const oeb_memref3d_##S* vinb, const oeb_memref3d_##S* uin,                      \
+      const oeb_memref3d_##S* vin, const oeb_memref3d_##S* mask, const oeb_memref1d_##S* crlavo,                    \
+      const oeb_memref1d_##S* crlavu, const oeb_memref1d_##S* crlato, const oeb_memref1d_##S* crlatu,               \
+      const oeb_memref1d_##S* acrlat0, const oeb_memref3d_##S* uoutb, const oeb_memref3d_##S* voutb, T eddlat,      \
+      T eddlon, T tau_smag, T weight_smag, const oeb_domain* dom, void* stream) {                                  \
+    return hdiffsmag_adj_entry<T>(uinb, vinb, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, uoutb,     \
+                                  voutb, eddlat, eddlon, tau_smag, weight_smag, dom, stream);                     \
   }
 
 OEB_HDIFF_ENTRIES(f64, double)

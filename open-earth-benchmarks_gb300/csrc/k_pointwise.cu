@@ -6,13 +6,15 @@
 // round-to-nearest on both sides, so the results are bit-identical to the reference
 // OpenMP kernels.  Expression trees keep the reference's order and parenthesisation; a
 // subexpression that occurs twice in the reference is computed once here (same operands,
-// same value).  FP32: the same trees in float, with the advection flux sums compensated
-// (precision.cuh).
+// same value).  FP32: the same trees in float, with the sums that cancel compensated
+// (precision.cuh): the advection flux sums, the laplacian, and the paired products of the
+// pressure-gradient stencils.
 //
 // One CTA of 32 x 8 threads covers a 32 x 32 (i, j) tile and KB k-levels; each thread
 // computes 4 rows.  Neighbour reads go through L1.
 #include "precision.cuh"
 #include "stencil_util.cuh"
+#include "tangent.cuh"
 
 namespace oeb {
 namespace {
@@ -45,7 +47,18 @@ __global__ void __launch_bounds__(kThreads) laplace_kernel(const T* __restrict__
                                                            int kb) {
   const int64_t sj = d.sj;
   for_points(d, kb, [&](int64_t o, int) {
-    out[o] = T(-4.0) * ld(in + o) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
+    if constexpr (Prec<T>::kCompensated) {
+      // -4 in nearly cancels the neighbour sum on smooth fields: sum all five terms
+      // compensated (-4 in is exact)
+      Acc<T> acc(ld(in + o - 1));
+      acc.add(ld(in + o + 1));
+      acc.add(ld(in + o + sj));
+      acc.add(ld(in + o - sj));
+      acc.add(T(-4.0) * ld(in + o));
+      out[o] = acc.get();
+    } else {
+      out[o] = T(-4.0) * ld(in + o) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
+    }
   });
 }
 
@@ -77,12 +90,14 @@ __global__ void __launch_bounds__(kThreads) p_grad_c_kernel(T* __restrict__ uout
   for_points(d, kb, [&](int64_t o, int) {
     const T wk = ld(delpc + o);
     const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
-    uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) *
-                              (((ld(gz + o - 1 + sk) - gz0) * (pk1 - ld(pkc + o - 1))) +
-                               ((ld(gz + o - 1) - gz1) * (ld(pkc + o - 1 + sk) - pk0)))));
-    vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) *
-                              (((ld(gz + o - sj + sk) - gz0) * (pk1 - ld(pkc + o - sj))) +
-                               ((ld(gz + o - sj) - gz1) * (ld(pkc + o - sj + sk) - pk0)))));
+    // the two products nearly cancel (a small pressure-gradient residual): Acc keeps the
+    // reference's a*b + c*d in FP64 and sums them compensated in FP32
+    Acc<T> fu = Acc<T>::prod(ld(gz + o - 1 + sk) - gz0, pk1 - ld(pkc + o - 1));
+    fu.add_prod(ld(gz + o - 1) - gz1, ld(pkc + o - 1 + sk) - pk0);
+    uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) * fu.get()));
+    Acc<T> fv = Acc<T>::prod(ld(gz + o - sj + sk) - gz0, pk1 - ld(pkc + o - sj));
+    fv.add_prod(ld(gz + o - sj) - gz1, ld(pkc + o - sj + sk) - pk0);
+    vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) * fv.get()));
   });
 }
 
@@ -107,10 +122,12 @@ __global__ void __launch_bounds__(kThreads) nh_p_grad_kernel(T* __restrict__ uou
       const T wkx = pkx1 - pkx0;
       const T ga = gz1 - ld(gz + o + 1);
       const T gb = gz0 - ld(gz + o + 1 + sk);
-      const T du = ((dt / (wk + wkx)) * ((ga * (pkx1 - pk0)) + (gb * (pk1 - pkx0))));
-      uout[o] = (((ld(uin + o) + du) +
-                  ((dt / (w1 + ld(wk1 + o + 1))) * ((ga * (ld(pp + o + 1 + sk) - pp0)) + (gb * (pp1 - ld(pp + o + 1)))))) *
-                 ld(rdx + o));
+      Acc<T> fk = Acc<T>::prod(ga, pkx1 - pk0);  // the two products nearly cancel
+      fk.add_prod(gb, pk1 - pkx0);
+      Acc<T> fp = Acc<T>::prod(ga, ld(pp + o + 1 + sk) - pp0);
+      fp.add_prod(gb, pp1 - ld(pp + o + 1));
+      const T du = ((dt / (wk + wkx)) * fk.get());
+      uout[o] = (((ld(uin + o) + du) + ((dt / (w1 + ld(wk1 + o + 1))) * fp.get())) * ld(rdx + o));
     }
     // v: neighbour j+1
     {
@@ -118,11 +135,12 @@ __global__ void __launch_bounds__(kThreads) nh_p_grad_kernel(T* __restrict__ uou
       const T wky = pky1 - pky0;
       const T ga = gz1 - ld(gz + o + sj);
       const T gb = gz0 - ld(gz + o + sj + sk);
-      const T dv = ((dt / (wk + wky)) * ((ga * (pky1 - pk0)) + (gb * (pk1 - pky0))));
-      vout[o] = (((ld(vin + o) + dv) +
-                  ((dt / (w1 + ld(wk1 + o + sj))) *
-                   ((ga * (ld(pp + o + sj + sk) - pp0)) + (gb * (pp1 - ld(pp + o + sj)))))) *
-                 ld(rdy + o));
+      Acc<T> fk = Acc<T>::prod(ga, pky1 - pk0);
+      fk.add_prod(gb, pk1 - pky0);
+      Acc<T> fp = Acc<T>::prod(ga, ld(pp + o + sj + sk) - pp0);
+      fp.add_prod(gb, pp1 - ld(pp + o + sj));
+      const T dv = ((dt / (wk + wky)) * fk.get());
+      vout[o] = (((ld(vin + o) + dv) + ((dt / (w1 + ld(wk1 + o + sj))) * fp.get())) * ld(rdy + o));
     }
   });
 }
@@ -344,6 +362,245 @@ oeb_status hadv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* v
   return after_launch();
 }
 
+// Tangent-linear hadvuv / hadvuv5th: d(uout, vout) = J(uin, vin) d(uin, vin), on Dual<T>.
+template <class T, int ORDER, class M3, class M1>
+oeb_status hadv_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M1* acrlat0,
+                         const M1* acrlat1, const M1* tgrlatda0, const M1* tgrlatda1, const M3* duin, const M3* dvin,
+                         T eddlat, T eddlon, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY((hadv_entry<T, ORDER>(duout, dvout, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, eddlat, eddlon, dom,
+                                  stream)));
+    OEB_TRY((hadv_entry<T, ORDER>(duout, dvout, duin, dvin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, eddlat, eddlon,
+                                  dom, stream)));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *u, *v, *a0, *a1, *t0, *t1, *ou, *ov;
+  OEB_TRY(arr.pack(uin, duin, &u));
+  OEB_TRY(arr.pack(vin, dvin, &v));
+  OEB_TRY(arr.pack(acrlat0, (const M1*)nullptr, &a0));
+  OEB_TRY(arr.pack(acrlat1, (const M1*)nullptr, &a1));
+  OEB_TRY(arr.pack(tgrlatda0, (const M1*)nullptr, &t0));
+  OEB_TRY(arr.pack(tgrlatda1, (const M1*)nullptr, &t1));
+  OEB_TRY(arr.alloc(duout, &ou));
+  OEB_TRY(arr.alloc(dvout, &ov));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
+  hadv_kernel<D, ORDER><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
+      ou, ov, u, v, a0, a1, t0, t1, acrlat0->strides[0], D(eddlat), D(eddlon), d, kKB);
+  OEB_TRY(after_launch());
+  OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
+}
+
+// ============================== hadvuv / hadvuv5th adjoint ==========================
+// With Ax = acrlat0 ua, Ay = R^-1 va, Bx = acrlat1 ub, By = R^-1 vb (the u/v averages of
+// hadvuv.h:186-201) and the signed upwind sums Px, Py (of u) and Qx, Qy (of v) -- r = A P --
+//   uout = eddlat Ax Px + eddlon Ay Py + tgr0 u va
+//   vout = eddlat Bx Qx + eddlon By Qy - tgr1 ub^2
+// the transpose for ybar = (uoutb, voutb), branches frozen, is a gather of per-point terms:
+//   ax = eddlat Ax uoutb          -> ubar(i+m)  with the x upwind weights of point i
+//   ay = eddlon Ay uoutb          -> ubar(j+m)  with the y upwind weights
+//   bx = eddlat Px acrlat0 uoutb/3 -> ubar(i-1), ubar(i), ubar(i+1)
+//   by = (eddlon Py R^-1 + tgr0 u) uoutb/4 -> vbar at the 4 points of va
+//   dd = tgr0 va uoutb            -> ubar(i)
+//   gx = eddlat Bx voutb, gy = eddlon By voutb -> vbar along the v upwind stencils
+//   ex = (eddlat Qx acrlat1 - 2 tgr1 ub) voutb/4 -> ubar at the 4 points of ub
+//   ey = eddlon Qy R^-1 voutb/3   -> vbar(j-1), vbar(j), vbar(j+1)
+// Pass 1 writes the nine terms and the four branch flags of every interior point to
+// scratch; pass 2 makes each input cell gather the terms of the points that read it.
+
+template <class T>
+struct HadvTerms {
+  T *ax, *ay, *bx, *by, *dd, *gx, *gy, *ex, *ey;
+  unsigned char* fl;  // bit 0: Ax > 0, 1: Ay > 0, 2: Bx > 0, 3: By > 0
+};
+
+// Upwind weights of the advection drivers as the weight of field(i + m) in the signed sum
+// (branch B carries the leading minus of hadvuv.h:14 / hadvuv5th.h:17).
+template <class T, int ORDER>
+__device__ __forceinline__ T upwind_weight(bool pos, int m) {
+  if (ORDER == 3) {
+    constexpr T c6 = T(-1.0) / T(6.0), c3 = T(-1.0) / T(3.0), ch = T(-0.5);
+    if (pos) return m == -2 ? c6 : m == -1 ? T(1) : m == 0 ? ch : m == 1 ? c3 : T(0);
+    return m == -1 ? -c3 : m == 0 ? -ch : m == 1 ? T(-1) : m == 2 ? -c6 : T(0);
+  } else {
+    constexpr T c30 = T(1.0) / T(30.0), c4 = T(-1.0) / T(4.0), c3 = T(-1.0) / T(3.0), c2 = T(-1.0) / T(2.0),
+                c20 = T(1.0) / T(20.0);
+    if (pos)
+      return m == -3 ? c30 : m == -2 ? c4 : m == -1 ? T(1) : m == 0 ? c3 : m == 1 ? c2 : m == 2 ? c20 : T(0);
+    return m == -2 ? -c20 : m == -1 ? -c2 : m == 0 ? -c3 : m == 1 ? T(-1) : m == 2 ? -c4 : m == 3 ? -c30 : T(0);
+  }
+}
+
+// signed upwind sum: r = a * adv_sum(...)
+template <class T, int ORDER>
+__device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t s, bool pos) {
+  constexpr int lo = ORDER == 3 ? -2 : -3;
+  T acc = T(0);
+#pragma unroll
+  for (int m = lo; m <= -lo; ++m) {
+    const T w = upwind_weight<T, ORDER>(pos, m);
+    if (w != T(0)) acc = acc + w * ld(f + o + m * s);
+  }
+  return acc;
+}
+
+template <class T, int ORDER>
+__global__ void __launch_bounds__(kThreads) hadv_adj_terms_kernel(
+    HadvTerms<T> tm, const T* __restrict__ uin, const T* __restrict__ vin, const T* __restrict__ acrlat0,
+    const T* __restrict__ acrlat1, const T* __restrict__ tgrlatda0, const T* __restrict__ tgrlatda1, int64_t s1d,
+    const T* __restrict__ uoutb, const T* __restrict__ voutb, T eddlat, T eddlon, Dims d, int kb) {
+  const int64_t sj = d.sj;
+  constexpr T third = T(1.0) / T(3.0);
+  constexpr T rr = earth_radius_recip<T>();
+  for_points(d, kb, [&](int64_t o, int j) {
+    const int64_t jo = (int64_t)j * s1d;
+    const T u0 = ld(uin + o), v0 = ld(vin + o);
+    const T um = ld(uin + o - 1) + u0;
+    const T ua = third * (um + ld(uin + o + 1));
+    const T va = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
+    const T ub = T(0.25) * ((um + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
+    const T vb = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
+    const T a0 = ld(acrlat0 + jo), a1 = ld(acrlat1 + jo), t0 = ld(tgrlatda0 + jo), t1 = ld(tgrlatda1 + jo);
+    const T Ax = a0 * ua, Ay = rr * va, Bx = a1 * ub, By = rr * vb;
+    const bool px = Ax > 0, py = Ay > 0, qx = Bx > 0, qy = By > 0;
+    const T Px = adv_sum<T, ORDER>(uin, o, 1, px), Py = adv_sum<T, ORDER>(uin, o, sj, py);
+    const T Qx = adv_sum<T, ORDER>(vin, o, 1, qx), Qy = adv_sum<T, ORDER>(vin, o, sj, qy);
+    const T yu = ld(uoutb + o), yv = ld(voutb + o);
+    tm.ax[o] = (eddlat * Ax) * yu;
+    tm.ay[o] = (eddlon * Ay) * yu;
+    tm.bx[o] = ((eddlat * Px) * a0) * (third * yu);
+    tm.by[o] = ((eddlon * Py) * rr + t0 * u0) * (T(0.25) * yu);
+    tm.dd[o] = (t0 * va) * yu;
+    tm.gx[o] = (eddlat * Bx) * yv;
+    tm.gy[o] = (eddlon * By) * yv;
+    tm.ex[o] = ((eddlat * Qx) * a1 - (T(2) * t1) * ub) * (T(0.25) * yv);
+    tm.ey[o] = ((eddlon * Qy) * rr) * (third * yv);
+    tm.fl[o] = (unsigned char)((px ? 1 : 0) | (py ? 2 : 0) | (qx ? 4 : 0) | (qy ? 8 : 0));
+  });
+}
+
+// Visits every cell of the box [-h, nx+h) x [-h, ny+h) x [0, nz) owned by this thread.
+template <class F>
+__device__ __forceinline__ void for_box_points(const Dims& d, int h, int kb, F&& f) {
+  const int i = -h + (int)(blockIdx.x * kTI + threadIdx.x);
+  if (i >= d.nx + h) return;
+  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
+  const int sj = (int)d.sj;
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      const int j = -h + (int)(blockIdx.y * kTJ + threadIdx.y) + kTY * r;
+      if (j < d.ny + h) f(kofs + i + j * sj, i, j);
+    }
+  }
+}
+
+template <class T, int ORDER>
+__global__ void __launch_bounds__(kThreads) hadv_adj_gather_kernel(T* __restrict__ uinb, T* __restrict__ vinb,
+                                                                   HadvTerms<T> tm, Dims d, int kb) {
+  constexpr int h = ORDER == 3 ? 2 : 3;
+  const int64_t sj = d.sj;
+  for_box_points(d, h, kb, [&](int64_t o, int a, int b) {
+    auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+    T ub = T(0), vb = T(0);
+    // upwind stencils: point (a - m, b) reads (a, b) with offset m, and likewise in j
+#pragma unroll
+    for (int m = -h; m <= h; ++m) {
+      if (in(a - m, b)) {
+        const int64_t q = o - m;
+        const unsigned char f = tm.fl[q];
+        ub = ub + upwind_weight<T, ORDER>(f & 1, m) * tm.ax[q];
+        vb = vb + upwind_weight<T, ORDER>(f & 4, m) * tm.gx[q];
+      }
+      if (in(a, b - m)) {
+        const int64_t q = o - m * sj;
+        const unsigned char f = tm.fl[q];
+        ub = ub + upwind_weight<T, ORDER>(f & 2, m) * tm.ay[q];
+        vb = vb + upwind_weight<T, ORDER>(f & 8, m) * tm.gy[q];
+      }
+    }
+    // u average of point i (i-1, i, i+1) and the ub average (i-1..i, j..j+1)
+    if (in(a - 1, b)) ub = ub + tm.bx[o - 1];
+    if (in(a, b)) ub = (ub + tm.bx[o]) + (tm.dd[o] + tm.ex[o]);
+    if (in(a + 1, b)) ub = (ub + tm.bx[o + 1]) + tm.ex[o + 1];
+    if (in(a, b - 1)) ub = ub + tm.ex[o - sj];
+    if (in(a + 1, b - 1)) ub = ub + tm.ex[o + 1 - sj];
+    // v average va of point (i, j): (i+1, j), (i+1, j-1), (i, j), (i, j-1); vb: (i, j-1..j+1)
+    if (in(a - 1, b)) vb = vb + tm.by[o - 1];
+    if (in(a - 1, b + 1)) vb = vb + tm.by[o - 1 + sj];
+    if (in(a, b)) vb = (vb + tm.by[o]) + tm.ey[o];
+    if (in(a, b + 1)) vb = (vb + tm.by[o + sj]) + tm.ey[o + sj];
+    if (in(a, b - 1)) vb = vb + tm.ey[o - sj];
+    uinb[o] = ub;
+    vinb[o] = vb;
+  });
+}
+
+template <class T, int ORDER, class M3, class M1>
+oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M1* acrlat0,
+                          const M1* acrlat1, const M1* tgrlatda0, const M1* tgrlatda1, const M3* uoutb,
+                          const M3* voutb, T eddlat, T eddlon, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY((hadv_entry<T, ORDER>(uoutb, voutb, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, eddlat, eddlon,
+                                  dom, stream)));
+  }
+  const int h = ORDER == 3 ? 2 : 3;
+  Grid<T> gub, gvb, gui, gvi, guo, gvo;
+  OEB_TRY((check_field3<T>(uinb, *dom, Reach{h, h, h, h, 0, 0}, &gub)));
+  OEB_TRY((check_field3<T>(vinb, *dom, Reach{h, h, h, h, 0, 0}, &gvb)));
+  OEB_TRY((check_field3<T>(uin, *dom, Reach{h, h, h, h, 0, 0}, &gui)));
+  OEB_TRY((check_field3<T>(vin, *dom, Reach{h, h, h, h, 0, 0}, &gvi)));
+  OEB_TRY((check_field3<T>(uoutb, *dom, kInterior, &guo)));
+  OEB_TRY((check_field3<T>(voutb, *dom, kInterior, &gvo)));
+  OEB_TRY(check_same_strides<T>({&gub, &gvb, &gui, &gvi, &guo, &gvo}));
+  OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi},
+                         {gui.lo, gui.hi, gvi.lo, gvi.hi, guo.lo, guo.hi, gvo.lo, gvo.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemPool_t pool;
+  OEB_TRY(device_pool(&pool));
+  // scratch: nine term fields and the flags, in uin's layout (terms are read at interior points only)
+  const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
+  const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +
+                       (uin->sizes[2] - 1) * uin->strides[2];
+  const int64_t n = (int64_t)(uin->aligned - start) + last + 1;
+  const int64_t org = (int64_t)(uin->aligned - start) + uin->offset;
+  void* buf = nullptr;
+  const size_t bytes = (size_t)n * (9 * sizeof(T) + 1);
+  cudaError_t e = cudaMallocFromPoolAsync(&buf, bytes, pool, st);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  HadvTerms<T> tm;
+  T* base = static_cast<T*>(buf);
+  T** fields[9] = {&tm.ax, &tm.ay, &tm.bx, &tm.by, &tm.dd, &tm.gx, &tm.gy, &tm.ex, &tm.ey};
+  for (int q = 0; q < 9; ++q) *fields[q] = base + q * n + org;
+  tm.fl = reinterpret_cast<unsigned char*>(base + 9 * n) + org;
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
+  oeb_status stt = OEB_OK;
+  hadv_adj_terms_kernel<T, ORDER><<<grid_for(*dom), dim3(kTX, kTY), 0, st>>>(
+      tm, gui.origin, gvi.origin, (const T*)acrlat0->aligned + acrlat0->offset,
+      (const T*)acrlat1->aligned + acrlat1->offset, (const T*)tgrlatda0->aligned + tgrlatda0->offset,
+      (const T*)tgrlatda1->aligned + tgrlatda1->offset, acrlat0->strides[0], guo.origin, gvo.origin, eddlat, eddlon, d,
+      kKB);
+  stt = after_launch();
+  if (stt == OEB_OK) {
+    hadv_adj_gather_kernel<T, ORDER>
+        <<<tile_grid(d.nx + 2 * h, d.ny + 2 * h, d.nz, kTI, kTJ, kKB), dim3(kTX, kTY), 0, st>>>(gub.origin, gvb.origin,
+                                                                                              tm, d, kKB);
+    stt = after_launch();
+  }
+  cudaFreeAsync(buf, st);
+  return stt;
+}
+
 }  // namespace
 }  // namespace oeb
 
@@ -388,6 +645,39 @@ using namespace oeb;
                                           void* stream) {                                                          \
     return hadv_entry<T, 5>(uout, vout, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, eddlat, eddlon, dom,     \
                             stream);                                                                               \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hadvuv_tl_##S(const OEB_M3(S) * duout, const OEB_M3(S) * dvout, const OEB_M3(S) * uin, \
+                                          const OEB_M3(S) * vin, const OEB_M1(S) * acrlat0,                        \
+                                          const OEB_M1(S) * acrlat1, const OEB_M1(S) * tgrlatda0,                  \
+                                          const OEB_M1(S) * tgrlatda1, const OEB_M3(S) * duin,                     \
+                                          const OEB_M3(S) * dvin, T eddlat, T eddlon, const oeb_domain* dom,       \
+                                          void* stream) {                                                          \
+    return hadv_tl_entry<T, 3>(duout, dvout, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, duin, dvin, eddlat, \
+                               eddlon, dom, stream);                                                               \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hadvuv5th_tl_##S(                                                                      \
+      const OEB_M3(S) * duout, const OEB_M3(S) * dvout, const OEB_M3(S) * uin, const OEB_M3(S) * vin,               \
+      const OEB_M1(S) * acrlat0, const OEB_M1(S) * acrlat1, const OEB_M1(S) * tgrlatda0,                           \
+      const OEB_M1(S) * tgrlatda1, const OEB_M3(S) * duin, const OEB_M3(S) * dvin, T eddlat, T eddlon,             \
+      const oeb_domain* dom, void* stream) {                                                                       \
+    return hadv_tl_entry<T, 5>(duout, dvout, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, duin, dvin, eddlat, \
+                               eddlon, dom, stream);                                                               \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hadvuv_adj_##S(                                                                        \
+      const OEB_M3(S) * uinb, const OEB_M3(S) * vinb, const OEB_M3(S) * uin, const OEB_M3(S) * vin,                 \
+      const OEB_M1(S) * acrlat0, const OEB_M1(S) * acrlat1, const OEB_M1(S) * tgrlatda0,                           \
+      const OEB_M1(S) * tgrlatda1, const OEB_M3(S) * uoutb, const OEB_M3(S) * voutb, T eddlat, T eddlon,           \
+      const oeb_domain* dom, void* stream) {                                                                       \
+    return hadv_adj_entry<T, 3>(uinb, vinb, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, uoutb, voutb,       \
+                                eddlat, eddlon, dom, stream);                                                      \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hadvuv5th_adj_##S(                                                                     \
+      const OEB_M3(S) * uinb, const OEB_M3(S) * vinb, const OEB_M3(S) * uin, const OEB_M3(S) * vin,                 \
+      const OEB_M1(S) * acrlat0, const OEB_M1(S) * acrlat1, const OEB_M1(S) * tgrlatda0,                           \
+      const OEB_M1(S) * tgrlatda1, const OEB_M3(S) * uoutb, const OEB_M3(S) * voutb, T eddlat, T eddlon,           \
+      const oeb_domain* dom, void* stream) {                                                                       \
+    return hadv_adj_entry<T, 5>(uinb, vinb, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, uoutb, voutb,       \
+                                eddlat, eddlon, dom, stream);                                                      \
   }
 
 OEB_POINTWISE_ENTRIES(f64, double)

@@ -42,6 +42,8 @@ struct ValidateOnly {
 // Raises a kernel's dynamic shared-memory limit to `bytes` on the current device, once per
 // (kernel, device); thread-safe.
 oeb_status ensure_dyn_smem(const void* kernel, int bytes);
+// The library's stream-ordered device memory pool for the current device.
+oeb_status device_pool(cudaMemPool_t* out);
 
 #define OEB_TRY(expr)                   \
   do {                                  \

@@ -8,8 +8,10 @@
 //    and the fvtp2d PPM monotonicity flag (fvtp2d.h:23) -- are decided on the exact
 //    product, which is what an FP64 product of two floats gives (it is exact in FP64 and
 //    cannot underflow); here without any FP64 instruction, from the operands' signs;
-//  * the flux sums of hdiffsmag (its laplacians, hdiffsmag.h:239-241, 254-256) and of the
-//    advection drivers (hadvuv.h:10-24, hadvuv5th.h:10-36) are accumulated with
+//  * the sums whose large terms cancel -- the flux sums of hdiffsmag (its laplacians,
+//    hdiffsmag.h:239-241, 254-256) and of the advection drivers (hadvuv.h:10-24,
+//    hadvuv5th.h:10-36), the laplacian (laplace.h:39) and the paired products of the
+//    pressure gradients (nh_p_grad.h:126-142, p_grad_c.h:90-97) -- are accumulated with
 //    error-free transformations (TwoSum, and TwoProduct via fmaf), i.e. compensated
 //    summation, so cancellation between their large terms does not cost FP32 digits.
 #pragma once

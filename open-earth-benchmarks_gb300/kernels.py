@@ -25,7 +25,7 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 from .abi import check, entry
-from .specs import DRIVER_SCALARS, KERNELS
+from .specs import ACTIVE, DRIVER_SCALARS, KERNELS
 from .storage import Domain, Storage
 
 # Module globals of the reference drivers (src/<k>.cpp:4-6).
@@ -91,6 +91,65 @@ def call(kernel: str, fields: Dict[str, Storage], scalars: Optional[Dict[str, fl
     check(entry(name)(*cargs), name)
 
 
+def _scalar_args(spec, vals, precision):
+    out = []
+    for s in spec.scalars:
+        if s.name not in vals:
+            raise ValueError("%s: missing scalar %r" % (spec.name, s.name))
+        ctype = ctypes.c_double if (precision == "f64" or s.always_double) else ctypes.c_float
+        out.append(ctype(vals[s.name]))
+    return out
+
+
+def _device_fields(kernel, groups):
+    flat = [f for g in groups for f in g]
+    if any(not isinstance(f, Storage) for f in flat):
+        raise TypeError("%s: every field must be a Storage" % kernel)
+    if not all(f.is_cuda for f in flat):
+        raise ValueError("%s: the tangent-linear and adjoint entry points take device fields" % kernel)
+    dtypes = {f.dtype for f in flat}
+    if len(dtypes) != 1:
+        raise TypeError("%s: mixed element types" % kernel)
+    return "f64" if flat[0].dtype == np.float64 else "f32"
+
+
+def tangent_linear(kernel: str, state: Dict[str, Storage], dx: Dict[str, Storage], dy: Dict[str, Storage],
+                   scalars: Optional[Dict[str, float]] = None, domain=None, stream=None) -> None:
+    """dy = J(state) dx: the stencil's Jacobian at `state` (branches frozen) applied to dx.
+
+    dx holds a perturbation of each active input (ACTIVE[kernel]); dy receives the
+    perturbation of every output, over the output's written box."""
+    spec = KERNELS[kernel]
+    outs = [dy[a.name] for a in spec.by_role("out3")]
+    ins = [state[a.name] for a in spec.args if a.role in ("in3", "in1")]
+    dxs = [dx[n] for n in ACTIVE[kernel]]
+    precision = _device_fields(kernel, (outs, ins, dxs))
+    vals = dict(DRIVER_SCALARS.get(kernel, {}))
+    vals.update(scalars or {})
+    cargs = [ctypes.byref(f.memref()) for f in outs + ins + dxs] + _scalar_args(spec, vals, precision)
+    dom = _domain(domain)
+    cargs += [ctypes.byref(dom), ctypes.c_void_p(_stream_handle(stream, True))]
+    name = "oeb_%s_tl_%s" % (kernel, precision)
+    check(entry(name)(*cargs), name)
+
+
+def adjoint(kernel: str, state: Dict[str, Storage], ybar: Dict[str, Storage], xbar: Dict[str, Storage],
+            scalars: Optional[Dict[str, float]] = None, domain=None, stream=None) -> None:
+    """xbar = J(state)^T ybar for the active inputs; ybar seeds the semantic outputs."""
+    spec = KERNELS[kernel]
+    xbs = [xbar[n] for n in ACTIVE[kernel]]
+    ins = [state[a.name] for a in spec.args if a.role in ("in3", "in1")]
+    ybs = [ybar[n] for n in spec.semantic_outputs]
+    precision = _device_fields(kernel, (xbs, ins, ybs))
+    vals = dict(DRIVER_SCALARS.get(kernel, {}))
+    vals.update(scalars or {})
+    cargs = [ctypes.byref(f.memref()) for f in xbs + ins + ybs] + _scalar_args(spec, vals, precision)
+    dom = _domain(domain)
+    cargs += [ctypes.byref(dom), ctypes.c_void_p(_stream_handle(stream, True))]
+    name = "oeb_%s_adj_%s" % (kernel, precision)
+    check(entry(name)(*cargs), name)
+
+
 def _make(kernel: str):
     spec = KERNELS[kernel]
     names = [a.name for a in spec.args]
@@ -147,5 +206,5 @@ def variant_kernel(name: str) -> str:
     return VARIANTS[name]
 
 
-__all__ = ["call", "domain_size", "domain_height", "halo_width", "VARIANTS", "variant_kernel",
+__all__ = ["call", "tangent_linear", "adjoint", "domain_size", "domain_height", "halo_width", "VARIANTS", "variant_kernel",
            *KERNELS.keys(), *[v for v in VARIANTS if v not in KERNELS]]

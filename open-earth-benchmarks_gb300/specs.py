@@ -183,3 +183,17 @@ DRIVER_SCALARS = {
     "p_grad_c": {"dt2": 0.1},
     "fvtp2d": {"p1": 0.583333, "p2": 0.083333},
 }
+
+
+# Tangent-linear / adjoint pairs: the active (differentiated) inputs of each stencil.  Every
+# other input is a parameter held fixed.  The TL entry point oeb_<k>_tl_<p> takes
+# (dy for every out3, the forward inputs, dx for each active input, scalars); the adjoint
+# oeb_<k>_adj_<p> takes (xbar for each active input, the forward inputs, ybar for each
+# semantic output, scalars).  xbar is written over the active input's reach box.
+ACTIVE = {
+    "hdiffsmag": ("uin", "vin"),
+    "hadvuv": ("uin", "vin"),
+    "hadvuv5th": ("uin", "vin"),
+    "fastwavesuv": ("uin", "vin", "utens", "vtens", "ppuv"),
+    "fvtp2d": ("q",),
+}
