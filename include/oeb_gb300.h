@@ -477,6 +477,20 @@ OEB_API oeb_status oeb_hdiffsmag_adj_f64(const oeb_memref3d_f64* uinb, const oeb
                                         const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0, const oeb_memref3d_f64* uoutb,
                                         const oeb_memref3d_f64* voutb, double eddlat, double eddlon, double tau_smag, double weight_smag,
                                         const oeb_domain* dom, void* stream);
+/* No counterpart in the reference.  oeb_hdiffsmag_adj_f64 without any allocation: the same   */
+/* arguments, checks and results, with its scratch in one fixed array inside the library,     */
+/* for callers that cannot allocate device memory while they run (a host whose allocator has  */
+/* claimed the GPU's memory up front, or a step loop that must not allocate).  Limit: uin's  */
+/* allocation span (halo and padding included) at most 2^21 cells, else OEB_ERR_TOO_LARGE    */
+/* before anything runs; the array (96 MiB) is held on every GPU that loads the library until */
+/* the process exits.  All calls share it and it keeps the last call's contents (nothing in   */
+/* it needs to start at zero); calls that overlap on the GPU race.  The first call on a       */
+/* device looks up the array's device address with that device current: make that first call */
+/* before any stream capture.                                                                 */
+OEB_API oeb_status oeb_hdiffsmag_adj_noalloc_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask,
+                                                const oeb_memref1d_f64* crlavo, const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu,
+                                                const oeb_memref1d_f64* acrlat0, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat, double eddlon,
+                                                double tau_smag, double weight_smag, const oeb_domain* dom, void* stream);
 OEB_API oeb_status oeb_hadvuv_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref1d_f64* acrlat0, const oeb_memref1d_f64* acrlat1,
                                      const oeb_memref1d_f64* tgrlatda0, const oeb_memref1d_f64* tgrlatda1, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat,
                                      double eddlon, const oeb_domain* dom, void* stream);

@@ -13,6 +13,9 @@
 //
 // Compiled with --fmad=false (see k_pointwise.cu).  One CTA of 32 x 8 threads per
 // 32 x 32 tile and KB k-levels.
+#include <mutex>
+#include <vector>
+
 #include "precision.cuh"
 #include "stencil_util.cuh"
 #include "tangent.cuh"
@@ -503,6 +506,94 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
   return stt;
 }
 
+// ==================== hdiffsmag adjoint without any allocation (FP64) ====================
+// oeb_hdiffsmag_adj_noalloc_f64 is for callers that cannot allocate device memory while they
+// run: a host whose own allocator has already claimed the GPU's memory up front (an
+// allocation from this library's pool could then fail in the middle of a run), or a
+// time-stepping loop that must not take an allocation inside its step.  It runs the same three
+// kernels as oeb_hdiffsmag_adj_f64, on the same validated arguments, but its six term fields
+// live in one fixed array compiled into the library instead of coming from the pool.
+//
+//  * Limit: each term field holds kNoAllocCells = 2^21 cells, so the span of uin's
+//    allocation (halo and padding included) may be at most 2^21 cells; a larger field is
+//    rejected with OEB_ERR_TOO_LARGE before anything runs.  The array is 6 x 2^21 doubles =
+//    96 MiB, and every GPU that loads the library holds it until the process exits.
+//  * Every call uses the same array, which keeps the last call's contents.  Each cell the
+//    kernels read is written earlier in the same call (the terms on the interior, the T/S
+//    adjoints on their boxes), so nothing has to start at zero and nothing is cleared.  Calls
+//    that overlap on the GPU -- on two streams, or from two host threads -- race on the array.
+//  * Set-up: the array's name is only a host-side stand-in for the device variable.  The first
+//    call on a device looks up its device address with cudaGetSymbolAddress, with that device
+//    current, and keeps it for later calls; make that first call before any stream capture.
+constexpr int64_t kNoAllocCells = int64_t(1) << 21;
+static __device__ __align__(256) double g_hdiffsmag_adj_scratch[6 * kNoAllocCells];
+
+oeb_status hdiffsmag_adj_scratch_address(double** out) {
+  static std::mutex mu;
+  static std::vector<double*> addr;  // per device
+  int dev = 0;
+  OEB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)addr.size() <= dev) addr.resize(dev + 1, nullptr);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_hdiffsmag_adj_scratch);
+    if (e != cudaSuccess) return cuda_fail(e);
+    addr[dev] = static_cast<double*>(p);
+  }
+  *out = addr[dev];
+  return OEB_OK;
+}
+
+oeb_status hdiffsmag_adj_noalloc_entry(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb,
+                                       const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin,
+                                       const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlavo,
+                                       const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato,
+                                       const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0,
+                                       const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat,
+                                       double eddlon, double tau_smag, double weight_smag, const oeb_domain* dom,
+                                       void* stream) {
+  using T = double;
+  {
+    // every check of the pool-backed entry point, nothing launched
+    ValidateOnly guard;
+    OEB_TRY(hdiffsmag_adj_entry<T>(uinb, vinb, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, uoutb, voutb,
+                                   eddlat, eddlon, tau_smag, weight_smag, dom, stream));
+  }
+  Grid<T> gub, gvb, gui, guo;
+  OEB_TRY((check_field3<T>(uinb, *dom, Reach{1, 1, 1, 1, 0, 0}, &gub)));
+  OEB_TRY((check_field3<T>(vinb, *dom, Reach{1, 1, 1, 1, 0, 0}, &gvb)));
+  OEB_TRY((check_field3<T>(uin, *dom, Reach{1, 1, 1, 1, 0, 0}, &gui)));
+  OEB_TRY((check_field3<T>(uoutb, *dom, kInterior, &guo)));
+  const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
+  const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +
+                       (uin->sizes[2] - 1) * uin->strides[2];
+  const int64_t n = (int64_t)(uin->aligned - start) + last + 1;
+  const int64_t org = (int64_t)(uin->aligned - start) + uin->offset;
+  if (n > kNoAllocCells) return OEB_ERR_TOO_LARGE;
+  OEB_RETURN_IF_VALIDATING();
+  T* base = nullptr;
+  OEB_TRY(hdiffsmag_adj_scratch_address(&base));
+  SmagTerms<T> tm{base + org, base + kNoAllocCells + org, base + 2 * kNoAllocCells + org,
+                  base + 3 * kNoAllocCells + org, base + 4 * kNoAllocCells + org, base + 5 * kNoAllocCells + org};
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
+  auto org1 = [](const oeb_memref1d_f64* m) { return (const T*)m->aligned + m->offset; };
+  const int64_t s1d = acrlat0->strides[0];
+  cudaStream_t st = (cudaStream_t)stream;
+  hdiffsmag_adj_terms_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
+      tm, gui.origin, (const T*)vin->aligned + vin->offset, (const T*)mask->aligned + mask->offset, org1(crlavo),
+      org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d, guo.origin,
+      (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kKB);
+  OEB_TRY(after_launch());
+  hdiffsmag_adj_ts_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
+      tm, gui.origin, (const T*)vin->aligned + vin->offset, org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
+  OEB_TRY(after_launch());
+  hdiffsmag_adj_gather_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
+      gub.origin, gvb.origin, tm, guo.origin, (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu),
+      org1(crlato), org1(crlatu), org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
+  return after_launch();
+}
+
 }  // namespace
 }  // namespace oeb
 
@@ -544,3 +635,13 @@ using namespace oeb;
 
 OEB_HDIFF_ENTRIES(f64, double)
 OEB_HDIFF_ENTRIES(f32, float)
+
+extern "C" oeb_status oeb_hdiffsmag_adj_noalloc_f64(
+    const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin,
+    const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlavo,
+    const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu,
+    const oeb_memref1d_f64* acrlat0, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat,
+    double eddlon, double tau_smag, double weight_smag, const oeb_domain* dom, void* stream) {
+  return hdiffsmag_adj_noalloc_entry(uinb, vinb, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, uoutb, voutb,
+                                     eddlat, eddlon, tau_smag, weight_smag, dom, stream);
+}
