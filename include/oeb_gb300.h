@@ -523,6 +523,125 @@ OEB_API oeb_status oeb_fvtp2d_adj_f32(const oeb_memref3d_f32* qb, const oeb_memr
                                      const oeb_memref3d_f32* yfx, const oeb_memref3d_f32* area, const oeb_memref3d_f32* fx1b, const oeb_memref3d_f32* fy1b, float ppm_p1, float ppm_p2,
                                      const oeb_domain* dom, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Chained dycore step (no counterpart in the reference: its drivers,        */
+/* src/<k>.cpp, run each stencil alone).  One step maps (u, v) to            */
+/* (uout, vout, fx1, fy1):                                                   */
+/*   1. (u1, v1)     = fastwavesuv(u, v, utens, vtens, wgtfac, ppuv, hhl,      */
+/*                                 rho, fx; edadlat, dt)                     */
+/*   2. (tu, tv)     = hadvuv5th(u1, v1, acrlat0, acrlat1, tgrlatda0,          */
+/*                               tgrlatda1; eddlat, eddlon)                  */
+/*   3. (u2, v2)     = (u1 + dt_adv tu, v1 + dt_adv tv)                       */
+/*   4. (uout, vout) = hdiffsmag(u2, v2, mask, crlavo, crlavu, crlato, crlatu,  */
+/*                               smag_acrlat0; eddlat, eddlon, tau_smag,     */
+/*                               weight_smag)                                */
+/*   5. (fx1, fy1)   = fvtp2d(q = uout, crx, cry, ra_x, ra_y, xfx, yfx, area;    */
+/*                            ppm_p1, ppm_p2): PPM fluxes of the new u       */
+/* Stage s runs over the interior widened in i and j by what the later        */
+/* stages read (7, 4, 4, 3 and 0 cells), so one step needs no halo exchange:  */
+/* the inputs need an i/j halo of 8 (7 below, 8 above for wgtfac, ppuv, hhl,  */
+/* rho; 7 for the 1-D fields) and a k halo of 1; uout and vout are written    */
+/* over the interior widened by 3, fx1 and fy1 over the interior.             */
+/*                                                                           */
+/* The tangent-linear step maps (du, dv) to (duout, dvout, dfx1, dfy1); the   */
+/* adjoint maps (uoutb, voutb, fx1b, fy1b), seeds on the interior, to         */
+/* (ub, vb) written over the interior widened by 7.  Both take only the      */
+/* step's inputs: the intermediate states (u1, v1, u2, v2, the new u) are    */
+/* recomputed inside the call, never stored between calls.                   */
+/*                                                                           */
+/* A plan owns the step's workspace: fields laid out like `like` (same        */
+/* sizes, strides and offset, which every field of the step must share),     */
+/* allocated once by oeb_chain_plan_create_* for the modes asked for, on the */
+/* current device.  The step calls allocate only the scratch of the adjoint   */
+/* and tangent-linear stencils they run (stream-ordered pool).  One plan      */
+/* serves one stream at a time.                                              */
+/* ------------------------------------------------------------------------- */
+typedef struct oeb_chain_plan oeb_chain_plan;
+
+#define OEB_CHAIN_FORWARD 1
+#define OEB_CHAIN_TL 2
+#define OEB_CHAIN_ADJOINT 4
+
+typedef struct oeb_chain_fields_f64 {
+  const oeb_memref3d_f64 *u, *v;
+  const oeb_memref3d_f64 *utens, *vtens, *wgtfac, *ppuv, *hhl, *rho; /* fastwavesuv */
+  const oeb_memref1d_f64* fx;
+  const oeb_memref1d_f64 *acrlat0, *acrlat1, *tgrlatda0, *tgrlatda1; /* hadvuv5th */
+  const oeb_memref3d_f64* mask;                                       /* hdiffsmag */
+  const oeb_memref1d_f64 *crlavo, *crlavu, *crlato, *crlatu, *smag_acrlat0;
+  const oeb_memref3d_f64 *crx, *cry, *ra_x, *ra_y, *xfx, *yfx, *area; /* fvtp2d */
+} oeb_chain_fields_f64;
+
+typedef struct oeb_chain_fields_f32 {
+  const oeb_memref3d_f32 *u, *v;
+  const oeb_memref3d_f32 *utens, *vtens, *wgtfac, *ppuv, *hhl, *rho;
+  const oeb_memref1d_f32* fx;
+  const oeb_memref1d_f32 *acrlat0, *acrlat1, *tgrlatda0, *tgrlatda1;
+  const oeb_memref3d_f32* mask;
+  const oeb_memref1d_f32 *crlavo, *crlavu, *crlato, *crlatu, *smag_acrlat0;
+  const oeb_memref3d_f32 *crx, *cry, *ra_x, *ra_y, *xfx, *yfx, *area;
+} oeb_chain_fields_f32;
+
+/* Scalars of the step, in double; the FP32 step rounds them to float. */
+typedef struct oeb_chain_scalars {
+  double edadlat, dt;            /* fastwavesuv */
+  double eddlat, eddlon;         /* hadvuv5th and hdiffsmag */
+  double dt_adv;                 /* stage 3 */
+  double tau_smag, weight_smag;  /* hdiffsmag */
+  double ppm_p1, ppm_p2;         /* fvtp2d */
+} oeb_chain_scalars;
+
+OEB_API oeb_status oeb_chain_plan_create_f64(const oeb_memref3d_f64* like, const oeb_domain* dom, int modes,
+                                             oeb_chain_plan** out);
+OEB_API oeb_status oeb_chain_plan_create_f32(const oeb_memref3d_f32* like, const oeb_domain* dom, int modes,
+                                             oeb_chain_plan** out);
+/* Device bytes held by the plan's workspace. */
+OEB_API size_t oeb_chain_plan_bytes(const oeb_chain_plan* plan);
+/* Frees the workspace (after synchronising the device). */
+OEB_API oeb_status oeb_chain_plan_destroy(oeb_chain_plan* plan);
+
+OEB_API oeb_status oeb_chain_forward_f64(oeb_chain_plan* plan, const oeb_chain_fields_f64* f, const oeb_chain_scalars* s,
+                                         const oeb_memref3d_f64* uout, const oeb_memref3d_f64* vout,
+                                         const oeb_memref3d_f64* fx1, const oeb_memref3d_f64* fy1, void* stream);
+OEB_API oeb_status oeb_chain_tl_f64(oeb_chain_plan* plan, const oeb_chain_fields_f64* f, const oeb_chain_scalars* s,
+                                    const oeb_memref3d_f64* du, const oeb_memref3d_f64* dv,
+                                    const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout,
+                                    const oeb_memref3d_f64* dfx1, const oeb_memref3d_f64* dfy1, void* stream);
+OEB_API oeb_status oeb_chain_adj_f64(oeb_chain_plan* plan, const oeb_chain_fields_f64* f, const oeb_chain_scalars* s,
+                                     const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb,
+                                     const oeb_memref3d_f64* fx1b, const oeb_memref3d_f64* fy1b,
+                                     const oeb_memref3d_f64* ub, const oeb_memref3d_f64* vb, void* stream);
+OEB_API oeb_status oeb_chain_forward_f32(oeb_chain_plan* plan, const oeb_chain_fields_f32* f, const oeb_chain_scalars* s,
+                                         const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                         const oeb_memref3d_f32* fx1, const oeb_memref3d_f32* fy1, void* stream);
+OEB_API oeb_status oeb_chain_tl_f32(oeb_chain_plan* plan, const oeb_chain_fields_f32* f, const oeb_chain_scalars* s,
+                                    const oeb_memref3d_f32* du, const oeb_memref3d_f32* dv,
+                                    const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout,
+                                    const oeb_memref3d_f32* dfx1, const oeb_memref3d_f32* dfy1, void* stream);
+OEB_API oeb_status oeb_chain_adj_f32(oeb_chain_plan* plan, const oeb_chain_fields_f32* f, const oeb_chain_scalars* s,
+                                     const oeb_memref3d_f32* uoutb, const oeb_memref3d_f32* voutb,
+                                     const oeb_memref3d_f32* fx1b, const oeb_memref3d_f32* fy1b,
+                                     const oeb_memref3d_f32* ub, const oeb_memref3d_f32* vb, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* CUDA graphs of library calls.  oeb_graph_begin starts capturing `stream`   */
+/* (thread-local capture mode; not the legacy NULL stream); every library call */
+/* made on it by this thread until oeb_graph_end is recorded, not run, and    */
+/* oeb_graph_end instantiates the graph.  oeb_graph_launch replays it on any  */
+/* stream.  The descriptors' pointers are baked in at capture, so a replay    */
+/* reads and writes the same buffers.  Run each captured call once outside    */
+/* capture first: one-time set-up (shared-memory limits, the scratch pool)   */
+/* then happens before capture.  oeb_launch_count() counts the graph's       */
+/* kernels at each launch, not at capture.                                   */
+/* ------------------------------------------------------------------------- */
+typedef struct oeb_graph oeb_graph;
+
+OEB_API oeb_status oeb_graph_begin(void* stream);
+OEB_API oeb_status oeb_graph_end(void* stream, oeb_graph** out);
+OEB_API oeb_status oeb_graph_launch(oeb_graph* graph, void* stream);
+OEB_API uint64_t oeb_graph_kernel_count(const oeb_graph* graph);
+OEB_API oeb_status oeb_graph_destroy(oeb_graph* graph);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,10 +10,12 @@ The directory name is not a Python identifier; load it with ``__graft_entry__.lo
 (registered as ``oeb_gb300``).
 """
 from .abi import OebError, check, declared_functions, load_library, LIB_PATH
-from .specs import ACTIVE, KERNELS, KERNEL_NAMES, DRIVER_SCALARS
+from .specs import ACTIVE, ADJ_FIELDS, KERNELS, KERNEL_NAMES, DRIVER_SCALARS
 from .storage import Domain, Memref1d, Memref3d, Storage
 from . import kernels
 from .kernels import adjoint, call, tangent_linear, VARIANTS
+from . import chain
 
 __all__ = ["OebError", "check", "declared_functions", "load_library", "LIB_PATH", "KERNELS", "KERNEL_NAMES",
-           "DRIVER_SCALARS", "ACTIVE", "tangent_linear", "adjoint", "Domain", "Memref1d", "Memref3d", "Storage", "kernels", "call", "VARIANTS"]
+           "DRIVER_SCALARS", "ACTIVE", "ADJ_FIELDS", "tangent_linear", "adjoint", "Domain", "Memref1d", "Memref3d",
+           "Storage", "kernels", "chain", "call", "VARIANTS"]

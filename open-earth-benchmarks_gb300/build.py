@@ -31,6 +31,7 @@ UNITS = {
     "k_hdiff.cu": ["--fmad=false"],
     "k_fastwavesuv.cu": ["--fmad=false"],
     "k_fvtp2d.cu": ["--fmad=false"],
+    "chain.cu": ["--fmad=false"],
 }
 
 

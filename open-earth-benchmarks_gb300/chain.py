@@ -1,0 +1,172 @@
+"""The chained dycore step and CUDA graphs (the ``oeb_chain_*`` / ``oeb_graph_*`` C ABI).
+
+One step maps (u, v) to (uout, vout, fx1, fy1) through fastwavesuv, hadvuv5th, an explicit
+update u2 = u1 + dt_adv * (advective tendency), hdiffsmag and fvtp2d (the PPM fluxes of the
+new u); include/oeb_gb300.h states the stages and boxes.  The tangent-linear and adjoint
+steps recompute the intermediate states inside the call.
+
+    plan = ChainPlan(like=fields["u"], domain=(nx, ny, nz), modes=FORWARD | ADJOINT)
+    plan.forward(fields, scalars, outs)            # outs: uout, vout, fx1, fy1
+    plan.adjoint(fields, scalars, seeds, grads)    # seeds: uout, vout, fx1, fy1 -> grads: u, v
+    with Graph(stream) as g:                       # record library calls ...
+        plan.forward(fields, scalars, outs, stream=stream)
+    g.launch(stream)                               # ... and replay them
+
+Every 3-D field of a step shares the layout of ``like`` (sizes, strides and offset) with an
+i/j halo of at least 8 and a k halo of at least 1.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, Optional
+
+import numpy as np
+
+from .abi import check, entry, load_library
+from .storage import Domain, Memref1d, Memref3d, Storage
+
+FORWARD, TL, ADJOINT = 1, 2, 4
+HALO = 8  # i/j halo the step's inputs need
+
+FIELDS3 = ("u", "v", "utens", "vtens", "wgtfac", "ppuv", "hhl", "rho")
+ORDER = ("u", "v", "utens", "vtens", "wgtfac", "ppuv", "hhl", "rho", "fx", "acrlat0", "acrlat1", "tgrlatda0",
+         "tgrlatda1", "mask", "crlavo", "crlavu", "crlato", "crlatu", "smag_acrlat0", "crx", "cry", "ra_x", "ra_y",
+         "xfx", "yfx", "area")
+RANK1 = {"fx", "acrlat0", "acrlat1", "tgrlatda0", "tgrlatda1", "crlavo", "crlavu", "crlato", "crlatu",
+         "smag_acrlat0"}
+SCALARS = ("edadlat", "dt", "eddlat", "eddlon", "dt_adv", "tau_smag", "weight_smag", "ppm_p1", "ppm_p2")
+OUTPUTS = ("uout", "vout", "fx1", "fy1")
+
+
+class ChainFields(ctypes.Structure):
+    """oeb_chain_fields_{f64,f32}: one descriptor pointer per input, in ORDER."""
+    _fields_ = [(n, ctypes.POINTER(Memref1d if n in RANK1 else Memref3d)) for n in ORDER]
+
+
+class ChainScalars(ctypes.Structure):
+    """oeb_chain_scalars."""
+    _fields_ = [(n, ctypes.c_double) for n in SCALARS]
+
+
+def _precision(fields) -> str:
+    kinds = {f.dtype for f in fields}
+    if len(kinds) != 1:
+        raise TypeError("the fields of a step share one element type")
+    return "f64" if next(iter(kinds)) == np.float64 else "f32"
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class ChainPlan:
+    """Workspace of the chained step for one layout and domain (oeb_chain_plan_create_*)."""
+
+    def __init__(self, like: Storage, domain, modes: int = FORWARD):
+        self.precision = "f64" if like.dtype == np.float64 else "f32"
+        self.domain = Domain(*domain)
+        self._plan = ctypes.c_void_p()
+        fn = entry("oeb_chain_plan_create_%s" % self.precision)
+        check(fn(ctypes.byref(like.memref()), ctypes.byref(self.domain), ctypes.c_int(modes),
+                 ctypes.byref(self._plan)), "oeb_chain_plan_create")
+        self.modes = modes
+        self._keep = []
+
+    @property
+    def nbytes(self) -> int:
+        lib = load_library()
+        lib.oeb_chain_plan_bytes.restype = ctypes.c_size_t
+        lib.oeb_chain_plan_bytes.argtypes = [ctypes.c_void_p]
+        return int(lib.oeb_chain_plan_bytes(self._plan))
+
+    def close(self):
+        if self._plan:
+            lib = load_library()
+            lib.oeb_chain_plan_destroy.argtypes = [ctypes.c_void_p]
+            check(lib.oeb_chain_plan_destroy(self._plan), "oeb_chain_plan_destroy")
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _fields(self, fields: Dict[str, Storage]):
+        missing = [n for n in ORDER if n not in fields]
+        if missing:
+            raise ValueError("chain step: missing fields %s" % missing)
+        refs = {n: fields[n].memref() for n in ORDER}
+        cf = ChainFields(**{n: ctypes.pointer(refs[n]) for n in ORDER})
+        self._keep = [refs, cf]  # alive until the next call; a captured graph copies them at capture
+        return cf
+
+    @staticmethod
+    def _scalars(scalars: Dict[str, float]) -> ChainScalars:
+        missing = [n for n in SCALARS if n not in scalars]
+        if missing:
+            raise ValueError("chain step: missing scalars %s" % missing)
+        return ChainScalars(**{n: float(scalars[n]) for n in SCALARS})
+
+    def _call(self, what, fields, scalars, extra, stream):
+        prec = _precision([fields[n] for n in ORDER] + list(extra))
+        if prec != self.precision:
+            raise TypeError("the plan is %s, the fields are %s" % (self.precision, prec))
+        cf = self._fields(fields)
+        cs = self._scalars(scalars)
+        refs = [f.memref() for f in extra]
+        args = [self._plan, ctypes.byref(cf), ctypes.byref(cs)] + [ctypes.byref(r) for r in refs]
+        name = "oeb_chain_%s_%s" % (what, self.precision)
+        check(entry(name)(*args, ctypes.c_void_p(_stream(stream))), name)
+
+    def forward(self, fields, scalars, outs: Dict[str, Storage], stream=None):
+        self._call("forward", fields, scalars, [outs[n] for n in OUTPUTS], stream)
+
+    def tangent_linear(self, fields, scalars, dx: Dict[str, Storage], dy: Dict[str, Storage], stream=None):
+        self._call("tl", fields, scalars, [dx["u"], dx["v"]] + [dy[n] for n in OUTPUTS], stream)
+
+    def adjoint(self, fields, scalars, seeds: Dict[str, Storage], grads: Dict[str, Storage], stream=None):
+        self._call("adj", fields, scalars, [seeds[n] for n in OUTPUTS] + [grads["u"], grads["v"]], stream)
+
+
+class Graph:
+    """A CUDA graph of library calls made on `stream` inside the ``with`` block."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self._g = ctypes.c_void_p()
+
+    def __enter__(self):
+        check(entry("oeb_graph_begin")(ctypes.c_void_p(_stream(self.stream))), "oeb_graph_begin")
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        st = entry("oeb_graph_end")(ctypes.c_void_p(_stream(self.stream)), ctypes.byref(self._g))
+        if exc_type is None:
+            check(st, "oeb_graph_end")
+        return False
+
+    @property
+    def kernels(self) -> int:
+        lib = load_library()
+        lib.oeb_graph_kernel_count.restype = ctypes.c_uint64
+        lib.oeb_graph_kernel_count.argtypes = [ctypes.c_void_p]
+        return int(lib.oeb_graph_kernel_count(self._g))
+
+    def launch(self, stream=None):
+        s = self.stream if stream is None else stream
+        check(entry("oeb_graph_launch")(self._g, ctypes.c_void_p(_stream(s))), "oeb_graph_launch")
+
+    def close(self):
+        if self._g:
+            entry("oeb_graph_destroy")(self._g)
+            self._g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

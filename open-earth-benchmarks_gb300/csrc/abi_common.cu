@@ -30,7 +30,27 @@ oeb_status cuda_fail(cudaError_t err) {
   return OEB_ERR_CUDA;
 }
 
-void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+namespace {
+// Launches issued by this thread while it captures a graph: recorded, not run.
+thread_local bool t_capturing = false;
+thread_local uint64_t t_captured = 0;
+}  // namespace
+
+void count_launches(uint64_t n) {
+  if (t_capturing)
+    t_captured += n;
+  else
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+void capture_count_begin() {
+  t_capturing = true;
+  t_captured = 0;
+}
+uint64_t capture_count_end() {
+  t_capturing = false;
+  return t_captured;
+}
+bool capture_counting() { return t_capturing; }
 
 oeb_status after_launch() {
   cudaError_t e = cudaGetLastError();

@@ -7,8 +7,8 @@
 // OpenMP kernels.  Expression trees keep the reference's order and parenthesisation; a
 // subexpression that occurs twice in the reference is computed once here (same operands,
 // same value).  FP32: the same trees in float, with the sums that cancel compensated
-// (precision.cuh): the advection flux sums, the laplacian, and the paired products of the
-// pressure-gradient stencils.
+// (precision.cuh): the advection flux sums and the laplacian, and the paired products of
+// the pressure-gradient stencils in float-float.
 //
 // One CTA of 32 x 8 threads covers a 32 x 32 (i, j) tile and KB k-levels; each thread
 // computes 4 rows.  Neighbour reads go through L1.
@@ -63,19 +63,33 @@ __global__ void __launch_bounds__(kThreads) laplace_kernel(const T* __restrict__
 }
 
 // ---- uvbke: kernels/uvbke.h:61-75 ----------------------------------------------------
+// dt5 is a double in every precision (src/uvbke.cpp:11-12), so the reference compiled for
+// float multiplies by it in double and rounds once.  The FP32 kernel gets dt5 as a float
+// pair hi + lo (exact to 48 bits) and forms dt5 * t * rs with TwoProduct and fmaf, which
+// rounds about as the reference does.
+template <class T>
+__device__ __forceinline__ T uvbke_scale(T t, T rs, T dt5_hi, T dt5_lo) {
+  if constexpr (Prec<T>::kCompensated) {
+    const T p = t * rs, pe = fmaf(t, rs, -p);  // t * rs = p + pe exactly
+    return fmaf(dt5_hi, p, fmaf(dt5_hi, pe, dt5_lo * p));
+  } else {
+    return (dt5_hi * t) * rs;
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads) uvbke_kernel(T* __restrict__ ub, T* __restrict__ vb,
                                                          const T* __restrict__ uc, const T* __restrict__ vc,
                                                          const T* __restrict__ cosa, const T* __restrict__ rsina,
-                                                         T dt5, Dims d, int kb) {
+                                                         T dt5, T dt5_lo, Dims d, int kb) {
   const int64_t sj = d.sj;
   for_points(d, kb, [&](int64_t o, int) {
     const T su = ld(uc + o - sj) + ld(uc + o);
     const T sv = ld(vc + o - 1) + ld(vc + o);
     const T ca = ld(cosa + o);
     const T rs = ld(rsina + o);
-    ub[o] = ((dt5 * (su - (sv * ca))) * rs);
-    vb[o] = ((dt5 * (sv - (su * ca))) * rs);
+    ub[o] = uvbke_scale(su - (sv * ca), rs, dt5, dt5_lo);
+    vb[o] = uvbke_scale(sv - (su * ca), rs, dt5, dt5_lo);
   });
 }
 
@@ -90,14 +104,13 @@ __global__ void __launch_bounds__(kThreads) p_grad_c_kernel(T* __restrict__ uout
   for_points(d, kb, [&](int64_t o, int) {
     const T wk = ld(delpc + o);
     const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
-    // the two products nearly cancel (a small pressure-gradient residual): Acc keeps the
-    // reference's a*b + c*d in FP64 and sums them compensated in FP32
-    Acc<T> fu = Acc<T>::prod(ld(gz + o - 1 + sk) - gz0, pk1 - ld(pkc + o - 1));
-    fu.add_prod(ld(gz + o - 1) - gz1, ld(pkc + o - 1 + sk) - pk0);
-    uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) * fu.get()));
-    Acc<T> fv = Acc<T>::prod(ld(gz + o - sj + sk) - gz0, pk1 - ld(pkc + o - sj));
-    fv.add_prod(ld(gz + o - sj) - gz1, ld(pkc + o - sj + sk) - pk0);
-    vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) * fv.get()));
+    // the two products nearly cancel (a small pressure-gradient residual): diff_dot is the
+    // reference's tree in FP64 and float-float in FP32
+    const T fu = diff_dot(ld(gz + o - 1 + sk), gz0, pk1, ld(pkc + o - 1), ld(gz + o - 1), gz1, ld(pkc + o - 1 + sk), pk0);
+    uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) * fu));
+    const T fv =
+        diff_dot(ld(gz + o - sj + sk), gz0, pk1, ld(pkc + o - sj), ld(gz + o - sj), gz1, ld(pkc + o - sj + sk), pk0);
+    vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) * fv));
   });
 }
 
@@ -120,27 +133,22 @@ __global__ void __launch_bounds__(kThreads) nh_p_grad_kernel(T* __restrict__ uou
     {
       const T pkx0 = ld(pk3 + o + 1), pkx1 = ld(pk3 + o + 1 + sk);
       const T wkx = pkx1 - pkx0;
-      const T ga = gz1 - ld(gz + o + 1);
-      const T gb = gz0 - ld(gz + o + 1 + sk);
-      Acc<T> fk = Acc<T>::prod(ga, pkx1 - pk0);  // the two products nearly cancel
-      fk.add_prod(gb, pk1 - pkx0);
-      Acc<T> fp = Acc<T>::prod(ga, ld(pp + o + 1 + sk) - pp0);
-      fp.add_prod(gb, pp1 - ld(pp + o + 1));
-      const T du = ((dt / (wk + wkx)) * fk.get());
-      uout[o] = (((ld(uin + o) + du) + ((dt / (w1 + ld(wk1 + o + 1))) * fp.get())) * ld(rdx + o));
+      const T gx0 = ld(gz + o + 1), gx1 = ld(gz + o + 1 + sk);
+      // the two products of each sum nearly cancel: diff_dot (precision.cuh)
+      const T fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
+      const T fp = diff_dot(gz1, gx0, ld(pp + o + 1 + sk), pp0, gz0, gx1, pp1, ld(pp + o + 1));
+      const T du = ((dt / (wk + wkx)) * fk);
+      uout[o] = (((ld(uin + o) + du) + ((dt / (w1 + ld(wk1 + o + 1))) * fp)) * ld(rdx + o));
     }
     // v: neighbour j+1
     {
       const T pky0 = ld(pk3 + o + sj), pky1 = ld(pk3 + o + sj + sk);
       const T wky = pky1 - pky0;
-      const T ga = gz1 - ld(gz + o + sj);
-      const T gb = gz0 - ld(gz + o + sj + sk);
-      Acc<T> fk = Acc<T>::prod(ga, pky1 - pk0);
-      fk.add_prod(gb, pk1 - pky0);
-      Acc<T> fp = Acc<T>::prod(ga, ld(pp + o + sj + sk) - pp0);
-      fp.add_prod(gb, pp1 - ld(pp + o + sj));
-      const T dv = ((dt / (wk + wky)) * fk.get());
-      vout[o] = (((ld(vin + o) + dv) + ((dt / (w1 + ld(wk1 + o + sj))) * fp.get())) * ld(rdy + o));
+      const T gy0 = ld(gz + o + sj), gy1 = ld(gz + o + sj + sk);
+      const T fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
+      const T fp = diff_dot(gz1, gy0, ld(pp + o + sj + sk), pp0, gz0, gy1, pp1, ld(pp + o + sj));
+      const T dv = ((dt / (wk + wky)) * fk);
+      vout[o] = (((ld(vin + o) + dv) + ((dt / (w1 + ld(wk1 + o + sj))) * fp)) * ld(rdy + o));
     }
   });
 }
@@ -276,8 +284,10 @@ oeb_status uvbke_entry(const M3* ub, const M3* vb, const M3* uc, const M3* vc, c
   OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi},
                          {guc.lo, guc.hi, gvc.lo, gvc.hi, gca.lo, gca.hi, grs.lo, grs.hi}));
   OEB_RETURN_IF_VALIDATING();
+  const T dt5_hi = T(dt5), dt5_lo = T(dt5 - (double)dt5_hi);  // dt5_lo = 0 for FP64
   uvbke_kernel<T><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
-      gub.origin, gvb.origin, guc.origin, gvc.origin, gca.origin, grs.origin, T(dt5), make_dims(*dom, gub), kKB);
+      gub.origin, gvb.origin, guc.origin, gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo, make_dims(*dom, gub),
+      kKB);
   return after_launch();
 }
 

@@ -26,6 +26,10 @@ oeb_status cuda_fail(cudaError_t err);
 // Checks the launch just made (cudaGetLastError) and counts it.
 oeb_status after_launch();
 void count_launches(uint64_t n);
+// Launches issued while this thread captures a graph are tallied apart (recorded, not run).
+void capture_count_begin();
+uint64_t capture_count_end();
+bool capture_counting();
 // While a ValidateOnly guard is alive on this thread, entry points return after validating
 // their descriptors, before any CUDA call (used by the host-buffer path to reject bad
 // descriptors before it allocates or copies anything).

@@ -10,10 +10,11 @@
 //    cannot underflow); here without any FP64 instruction, from the operands' signs;
 //  * the sums whose large terms cancel -- the flux sums of hdiffsmag (its laplacians,
 //    hdiffsmag.h:239-241, 254-256) and of the advection drivers (hadvuv.h:10-24,
-//    hadvuv5th.h:10-36), the laplacian (laplace.h:39) and the paired products of the
-//    pressure gradients (nh_p_grad.h:126-142, p_grad_c.h:90-97) -- are accumulated with
+//    hadvuv5th.h:10-36) and the laplacian (laplace.h:39) -- are accumulated with
 //    error-free transformations (TwoSum, and TwoProduct via fmaf), i.e. compensated
-//    summation, so cancellation between their large terms does not cost FP32 digits.
+//    summation, so cancellation between their large terms does not cost FP32 digits;
+//  * the paired products of the pressure gradients (nh_p_grad.h:126-142,
+//    p_grad_c.h:90-97) are evaluated in float-float (diff_dot below).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -82,5 +83,40 @@ struct Acc<float, true> {
   }
   __device__ __forceinline__ float get() const { return s + c; }
 };
+
+namespace detail {
+// TwoSum (Knuth): a + b = s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+}  // namespace detail
+
+// (a - b) * (c - d) + (e - f) * (g - h): the paired products of the pressure-gradient
+// stencils (nh_p_grad.h:126-142, p_grad_c.h:90-97), whose two products nearly cancel.
+// FP64: exactly these operations in this order, the reference's expression tree.  FP32:
+// the four differences and the two products are error-free transformations (TwoSum,
+// TwoProduct via fmaf), and the rounding terms are summed apart and added at the end --
+// float-float evaluation -- so neither the cancellation nor the rounding of the differences
+// (of values up to several times apart) costs FP32 digits.
+template <class T>
+__device__ __forceinline__ T diff_dot(T a, T b, T c, T d, T e, T f, T g, T h) {
+  if constexpr (Prec<T>::kCompensated) {
+    float x, xl, y, yl, z, zl, w, wl;
+    detail::two_sum(a, -b, x, xl);
+    detail::two_sum(c, -d, y, yl);
+    detail::two_sum(e, -f, z, zl);
+    detail::two_sum(g, -h, w, wl);
+    const float p = x * y, pe = fmaf(x, y, -p);
+    const float q = z * w, qe = fmaf(z, w, -q);
+    float s, se;
+    detail::two_sum(p, q, s, se);
+    const float low = ((pe + qe) + se) + ((x * yl + xl * y) + (z * wl + zl * w));
+    return s + low;
+  } else {
+    return ((a - b) * (c - d)) + ((e - f) * (g - h));
+  }
+}
 
 }  // namespace oeb

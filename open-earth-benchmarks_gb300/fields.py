@@ -222,3 +222,38 @@ def make_outputs(kernel: str, nx: int, ny: int, nz: int, halo: int = HALO, dtype
 
 def points(nx, ny, nz) -> int:
     return nx * ny * nz
+
+
+# Inputs of the chained step (chain.py), from the generators of the stencils that read them:
+# (u, v) and the fastwavesuv fields from fastwavesuv, the metric terms of the advection from
+# hadvuv5th, mask and the diffusion metrics from hdiffsmag, the fluxes' geometry from fvtp2d.
+CHAIN_SOURCES = {
+    "u": ("fastwavesuv", "uin"), "v": ("fastwavesuv", "vin"), "utens": ("fastwavesuv", "utens"),
+    "vtens": ("fastwavesuv", "vtens"), "wgtfac": ("fastwavesuv", "wgtfac"), "ppuv": ("fastwavesuv", "ppuv"),
+    "hhl": ("fastwavesuv", "hhl"), "rho": ("fastwavesuv", "rho"), "fx": ("fastwavesuv", "fx"),
+    "acrlat0": ("hadvuv5th", "acrlat0"), "acrlat1": ("hadvuv5th", "acrlat1"),
+    "tgrlatda0": ("hadvuv5th", "tgrlatda0"), "tgrlatda1": ("hadvuv5th", "tgrlatda1"),
+    "mask": ("hdiffsmag", "mask"), "crlavo": ("hdiffsmag", "crlavo"), "crlavu": ("hdiffsmag", "crlavu"),
+    "crlato": ("hdiffsmag", "crlato"), "crlatu": ("hdiffsmag", "crlatu"), "smag_acrlat0": ("hdiffsmag", "acrlat0"),
+    "crx": ("fvtp2d", "crx"), "cry": ("fvtp2d", "cry"), "ra_x": ("fvtp2d", "ra_x"), "ra_y": ("fvtp2d", "ra_y"),
+    "xfx": ("fvtp2d", "xfx"), "yfx": ("fvtp2d", "yfx"), "area": ("fvtp2d", "area"),
+}
+CHAIN_HALO = 8
+CHAIN_DT_ADV = 0.01  # stage 3: the advective tendencies move u by a few per cent
+
+
+def make_chain_inputs(nx: int, ny: int, nz: int, seed: int, workload: str = "physical", halo: int = CHAIN_HALO,
+                      dtype=np.float64) -> Dict[str, np.ndarray]:
+    per_kernel = {k: make_inputs(k, nx, ny, nz, seed, workload, halo=halo, dtype=dtype)
+                  for k in {src for src, _ in CHAIN_SOURCES.values()}}
+    return {name: per_kernel[k][arg] for name, (k, arg) in CHAIN_SOURCES.items()}
+
+
+def make_chain_scalars(seed: int) -> Dict[str, float]:
+    fw = make_scalars("fastwavesuv", seed)
+    adv = make_scalars("hadvuv5th", seed)
+    smag = make_scalars("hdiffsmag", seed)
+    fv = make_scalars("fvtp2d", seed)
+    return {"edadlat": fw["edadlat"], "dt": fw["dt"], "eddlat": adv["eddlat"], "eddlon": adv["eddlon"],
+            "dt_adv": CHAIN_DT_ADV, "tau_smag": smag["tau_smag"], "weight_smag": smag["weight_smag"],
+            "ppm_p1": fv["p1"], "ppm_p2": fv["p2"]}

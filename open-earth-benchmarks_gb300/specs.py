@@ -197,3 +197,13 @@ ACTIVE = {
     "fastwavesuv": ("uin", "vin", "utens", "vtens", "ppuv"),
     "fvtp2d": ("q",),
 }
+
+# Fields an adjoint call reads or writes in full (frozen state and parameters it reads, the
+# output seeds, the input gradients), for its algorithmic bytes: x elem size per point.
+ADJ_FIELDS = {
+    "hdiffsmag": ("uin", "vin", "mask", "uoutb", "voutb", "uinb", "vinb"),
+    "hadvuv": ("uin", "vin", "uoutb", "voutb", "uinb", "vinb"),
+    "hadvuv5th": ("uin", "vin", "uoutb", "voutb", "uinb", "vinb"),
+    "fastwavesuv": ("wgtfac", "hhl", "rho", "uoutb", "voutb", "uinb", "vinb", "utensb", "vtensb", "ppuvb"),
+    "fvtp2d": ("q", "crx", "cry", "ra_x", "ra_y", "xfx", "yfx", "area", "fx1b", "fy1b", "qb"),
+}
