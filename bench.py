@@ -233,6 +233,18 @@ def run_ours(args):
                "note": "FP32 storage and arithmetic, exact limiter sign tests, compensated flux sums; "
                        "normwise error vs the FP64 oracle is stated per kernel by tests/test_gpu_fp32.py"}
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = {"workload": "forward + adjoint of each differentiated stencil, 128x128x80 + 3-cell halo, seed 3",
+                   "f64": _adjoint_leg(pkg, fields, torch, dev, args, np.float64),
+                   "f32": _adjoint_leg(pkg, fields, torch, dev, args, np.float32)}
+    chain = None
+    if not args.no_chain:
+        chain = {"workload": "chained step fastwavesuv->hadvuv5th->update->hdiffsmag->fvtp2d, forward + adjoint "
+                             "with recomputation, one CUDA graph per step, 128x128x80, i/j halo 8, seed 3",
+                 "f64": _chain_leg(pkg, fields, torch, dev, args, np.float64),
+                 "f32": _chain_leg(pkg, fields, torch, dev, args, np.float32)}
+
     e2e = None
     if not args.no_e2e:
         e2e = _e2e(pkg, fields, torch, args, names)
@@ -260,12 +272,141 @@ def run_ours(args):
         line["e2e"] = e2e
     if f32 is not None:
         line["f32"] = f32
+    if adjoint is not None:
+        line["adjoint"] = adjoint
+    if chain is not None:
+        line["chain"] = chain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_baseline(pkg, fields, budget_s=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+ADJ_KERNELS = ("hdiffsmag", "hadvuv5th", "fastwavesuv", "fvtp2d")
+
+
+def _adjoint_leg(pkg, fields, torch, dev, args, dtype):
+    """Forward + adjoint pairs of the four differentiated stencils at 128x128x80 (seed 3): per
+    kernel, the forward call and the adjoint call timed with CUDA events on the launch
+    stream, two input sets alternating."""
+    elem = 8 if dtype == np.float64 else 4
+    stream = torch.cuda.current_stream(dev)
+    dom = (NX, NY, NZ)
+    pts = NX * NY * NZ
+    peak = _measured_peak()[0]
+    lib = pkg.load_library()
+    out = {}
+    for name in ADJ_KERNELS:
+        spec = pkg.KERNELS[name]
+        sets = []
+        for r in range(2):
+            x = fields.make_inputs(name, NX, NY, NZ, seed=3 + r)
+            o = fields.make_outputs(name, NX, NY, NZ)
+            st = {k: pkg.Storage(torch.from_numpy(v.astype(dtype)).to(dev), HALO) for k, v in {**x, **o}.items()}
+            rng = np.random.default_rng([3, r])
+            shape = next(iter(o.values())).shape
+            yb = {n: pkg.Storage(torch.from_numpy(rng.normal(0.0, 1.0, size=shape).astype(dtype)).to(dev), HALO)
+                  for n in spec.semantic_outputs}
+            xb = {n: pkg.Storage(torch.zeros(shape, dtype=st[n].data.dtype, device=dev), HALO)
+                  for n in pkg.ACTIVE[name]}
+            sc = fields.make_scalars(name, seed=3)
+            if dtype == np.float32:
+                sc = {k: float(np.float32(v)) for k, v in sc.items()}
+            sets.append((st, yb, xb, sc))
+
+        def run(sv, ev=None):
+            st, yb, xb, sc = sv
+            if ev is not None:
+                ev[0].record(stream)
+            pkg.call(name, st, sc, domain=dom, stream=stream)
+            if ev is not None:
+                ev[1].record(stream)
+            pkg.adjoint(name, st, yb, xb, sc, domain=dom, stream=stream)
+            if ev is not None:
+                ev[2].record(stream)
+
+        for w in range(args.warmup):
+            run(sets[w % 2])
+        torch.cuda.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        l0 = lib.oeb_launch_count()
+        for i in range(args.steps):
+            run(sets[i % 2], evs[i])
+        torch.cuda.synchronize()
+        launches = lib.oeb_launch_count() - l0
+        fwd = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+        adj = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+        fwd_b = spec.bytes_per_point(elem) * pts
+        adj_b = len(pkg.ADJ_FIELDS[name]) * elem * pts
+        pair_gbs = (fwd_b + adj_b) / ((fwd + adj) * 1e-3) / 1e9
+        out[name] = {"forward_ms": round(fwd, 5), "adjoint_ms": round(adj, 5),
+                     "pair_gpts": round(pts / ((fwd + adj) * 1e-3) / 1e9, 4),
+                     "pair_bytes_per_point": (spec.bytes_per_point(elem) + len(pkg.ADJ_FIELDS[name]) * elem),
+                     "pair_hbm_gbs": round(pair_gbs, 1), "pair_frac": round(pair_gbs / peak, 4),
+                     "adjoint_hbm_gbs": round(adj_b / (adj * 1e-3) / 1e9, 1),
+                     "launches_per_pair": round(launches / args.steps, 2)}
+        del sets
+        torch.cuda.empty_cache()
+    return out
+
+
+def _chain_leg(pkg, fields, torch, dev, args, dtype):
+    """The chained dycore step forward + adjoint at 128x128x80 (i/j halo 8, seed 3), captured
+    once per input set in a CUDA graph; two graphs on two input sets alternate."""
+    import importlib
+    chain = importlib.import_module("oeb_gb300.chain")
+    stream = torch.cuda.Stream(device=dev)
+    H = fields.CHAIN_HALO
+    graphs, keep = [], []
+    for r in range(2):
+        x = fields.make_chain_inputs(NX, NY, NZ, 3 + r, halo=H)
+        sc = fields.make_chain_scalars(3)
+        st = {k: pkg.Storage(torch.from_numpy(v.astype(dtype)).to(dev), H, nx=NX if v.ndim == 3 else None)
+              for k, v in x.items()}
+        shape = x["u"].shape
+        tdt = torch.float64 if dtype == np.float64 else torch.float32
+        outs = {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=NX) for n in chain.OUTPUTS}
+        rng = np.random.default_rng([3, r])
+        seeds = {n: pkg.Storage(torch.from_numpy(rng.normal(0.0, 1.0, size=shape).astype(dtype)).to(dev), H, nx=NX)
+                 for n in chain.OUTPUTS}
+        grads = {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=NX) for n in ("u", "v")}
+        plan = chain.ChainPlan(st["u"], (NX, NY, NZ), chain.FORWARD | chain.ADJOINT)
+        with torch.cuda.stream(stream):
+            plan.forward(st, sc, outs, stream=stream)
+            plan.adjoint(st, sc, seeds, grads, stream=stream)
+        stream.synchronize()
+        g = chain.Graph(stream)
+        with g:
+            plan.forward(st, sc, outs, stream=stream)
+            plan.adjoint(st, sc, seeds, grads, stream=stream)
+        graphs.append(g)
+        keep.append((st, outs, seeds, grads, plan))
+    for w in range(args.warmup):
+        graphs[w % 2].launch(stream)
+    stream.synchronize()
+    lib = pkg.load_library()
+    l0 = lib.oeb_launch_count()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(args.steps):
+        graphs[i % 2].launch(stream)
+    t1.record(stream)
+    stream.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    launches = (lib.oeb_launch_count() - l0) / args.steps
+    res = {"ms_per_step": round(ms, 4), "gpts": round(NX * NY * NZ / (ms * 1e-3) / 1e9, 4),
+           "kernels_per_step": graphs[0].kernels, "launches_per_step": round(launches, 1),
+           "workspace_bytes": keep[0][4].nbytes}
+    for g in graphs:
+        g.close()
+    for k in keep:
+        k[4].close()
+    del keep
+    torch.cuda.empty_cache()
+    return res
 
 
 def _ncu_traffic(kernel):
@@ -403,6 +544,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-f32", action="store_true", help="skip the FP32-storage leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint leg")
+    ap.add_argument("--no-chain", action="store_true", help="skip the chained-step leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--kernels", nargs="*", default=None,
                     help="run only these stencils in the step (profiling); the default line uses all ten")
