@@ -245,6 +245,10 @@ def run_ours(args):
                  "f64": _chain_leg(pkg, fields, torch, dev, args, np.float64),
                  "f32": _chain_leg(pkg, fields, torch, dev, args, np.float32)}
 
+    batched = None
+    if not args.no_batch:
+        batched = _batch_leg(pkg, fields, torch, dev, args)
+
     e2e = None
     if not args.no_e2e:
         e2e = _e2e(pkg, fields, torch, args, names)
@@ -276,6 +280,8 @@ def run_ours(args):
         line["adjoint"] = adjoint
     if chain is not None:
         line["chain"] = chain
+    if batched is not None:
+        line["batched"] = batched
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_baseline(pkg, fields, budget_s=args.cpu_seconds)
     if rank == 0:
@@ -405,6 +411,93 @@ def _chain_leg(pkg, fields, torch, dev, args, dtype):
     for k in keep:
         k[4].close()
     del keep
+    torch.cuda.empty_cache()
+    return res
+
+
+def _batch_leg(pkg, fields, torch, dev, args):
+    """The uneven ensemble (48 members, nx, ny in {48..320}, nz in {40, 60, 80, 137}, FP64 or
+    FP32, seed 4): every member's chained step forward + adjoint as batched persistent
+    launches (autotuned), replayed from a CUDA graph; beside it the same work as per-member
+    launches, also from a graph."""
+    import importlib
+    chain = importlib.import_module("oeb_gb300.chain")
+    H = fields.CHAIN_HALO
+    spec = fields.ensemble_members(48, 4)
+    members = []
+    for idx, (nx, ny, nz, item) in enumerate(spec):
+        dt = np.float64 if item == 8 else np.float32
+        x = fields.make_chain_inputs_device(nx, ny, nz, 4000 + idx, dev, dt, halo=H)
+        shape = tuple(x["u"].shape)
+        tdt = x["u"].dtype
+        gen = torch.Generator(device=dev).manual_seed(idx)
+        members.append({
+            "fields": {k: pkg.Storage(v, H, nx=nx if v.dim() == 3 else None) for k, v in x.items()},
+            "scalars": fields.make_chain_scalars(4), "domain": (nx, ny, nz),
+            "outs": {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=nx) for n in chain.OUTPUTS},
+            "seeds": {n: pkg.Storage(torch.randn(shape, generator=gen, device=dev, dtype=tdt), H, nx=nx)
+                      for n in chain.OUTPUTS},
+            "grads": {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=nx) for n in ("u", "v")}})
+    stream = torch.cuda.Stream(device=dev)
+    plan = chain.BatchPlan(members, chain.FORWARD | chain.ADJOINT)
+    plan.run(stream)
+    stream.synchronize()
+    t = time.perf_counter()
+    plan.autotune(stream)
+    stream.synchronize()
+    tune_s = time.perf_counter() - t
+    plan.run(stream)
+    stream.synchronize()
+
+    def timed(graph):
+        for _ in range(args.warmup):
+            graph.launch(stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            graph.launch(stream)
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    g = chain.Graph(stream)
+    with g:
+        plan.run(stream)
+    lib = pkg.load_library()
+    l0 = lib.oeb_launch_count()
+    ms_batch = timed(g)
+    launches = (lib.oeb_launch_count() - l0) / (args.steps + args.warmup)
+    # the same work as per-member launches
+    plans = [chain.ChainPlan(m["fields"]["u"], m["domain"], chain.FORWARD | chain.ADJOINT) for m in members]
+
+    def per_member():
+        for cp, m in zip(plans, members):
+            cp.forward(m["fields"], m["scalars"], m["outs"], stream=stream)
+            cp.adjoint(m["fields"], m["scalars"], m["seeds"], m["grads"], stream=stream)
+
+    per_member()
+    stream.synchronize()
+    g2 = chain.Graph(stream)
+    with g2:
+        per_member()
+    ms_members = timed(g2)
+    pts = plan.points
+    res = {"workload": "48 members, nx, ny uniform in {48..320 step 16}, nz in {40, 60, 80, 137}, FP64 or FP32 "
+                       "(seed 4); chained step forward + adjoint with recomputation; device-generated inputs",
+           "members": len(members), "fp64_members": sum(1 for s_ in spec if s_[3] == 8),
+           "points_per_run": pts, "ms_per_run": round(ms_batch, 3), "gpts": round(pts / (ms_batch * 1e-3) / 1e9, 4),
+           "batched_launches_per_run": plan.launches, "launches_counted": round(launches, 1),
+           "per_member_launches_ms_per_run": round(ms_members, 3),
+           "per_member_launches_per_run": g2.kernels,
+           "speedup_vs_per_member_launches": round(ms_members / ms_batch, 3),
+           "autotune_s": round(tune_s, 2), "plan_bytes": plan.nbytes}
+    g.close()
+    g2.close()
+    for cp in plans:
+        cp.close()
+    plan.close()
+    del members
     torch.cuda.empty_cache()
     return res
 
@@ -546,6 +639,7 @@ def main():
     ap.add_argument("--no-f32", action="store_true", help="skip the FP32-storage leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint leg")
     ap.add_argument("--no-chain", action="store_true", help="skip the chained-step leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--kernels", nargs="*", default=None,
                     help="run only these stencils in the step (profiling); the default line uses all ten")

@@ -624,6 +624,49 @@ OEB_API oeb_status oeb_chain_adj_f32(oeb_chain_plan* plan, const oeb_chain_field
                                      const oeb_memref3d_f32* ub, const oeb_memref3d_f32* vb, void* stream);
 
 /* ------------------------------------------------------------------------- */
+/* Batched ensembles (no counterpart in the reference).  A batch plan runs    */
+/* the chained step -- forward, then adjoint -- for many ensemble members of  */
+/* uneven sizes and mixed precision.  At creation it records the step of    */
+/* every member once (the calls of oeb_chain_forward_* / oeb_chain_adj_*,   */
+/* launching nothing) and uploads, for each recorded kernel launch, the      */
+/* members' tiles and arguments; oeb_batch_run then replays each launch as   */
+/* ONE persistent kernel over all members of a precision, its CTAs walking   */
+/* the (member, tile) items.  FP64 members run on `stream`, FP32 members on  */
+/* a second stream of the plan that forks from and joins `stream`.  The     */
+/* members' descriptors are baked in: a run reads and writes the same        */
+/* buffers.  Each member has its own chain plan; the scratch of the adjoint  */
+/* stencils lives in one arena of the plan.  Results are bit-identical to    */
+/* oeb_chain_forward_* / oeb_chain_adj_* on each member.                     */
+/*                                                                           */
+/* oeb_batch_autotune times, for every batched launch, the k-levels per tile */
+/* (kb) and the CTA count (one persistent wave, or one CTA per tile) and     */
+/* keeps the fastest; oeb_batch_run uses the choices from then on.           */
+/* ------------------------------------------------------------------------- */
+typedef struct oeb_batch_plan oeb_batch_plan;
+
+typedef struct oeb_batch_member {
+  int elem_size;             /* 8: FP64 fields, 4: FP32 fields */
+  oeb_domain dom;
+  const void* fields;        /* const oeb_chain_fields_f64* or oeb_chain_fields_f32* */
+  oeb_chain_scalars scalars;
+  /* oeb_memref3d_f64 or _f32 descriptors */
+  const void *uout, *vout, *fx1, *fy1;      /* forward outputs */
+  const void *uoutb, *voutb, *fx1b, *fy1b;  /* adjoint seeds (OEB_CHAIN_ADJOINT) */
+  const void *ub, *vb;                      /* adjoint results (OEB_CHAIN_ADJOINT) */
+} oeb_batch_member;
+
+/* modes: OEB_CHAIN_FORWARD and/or OEB_CHAIN_ADJOINT. */
+OEB_API oeb_status oeb_batch_plan_create(const oeb_batch_member* members, int count, int modes, oeb_batch_plan** out);
+OEB_API oeb_status oeb_batch_run(oeb_batch_plan* plan, void* stream);
+OEB_API oeb_status oeb_batch_autotune(oeb_batch_plan* plan, void* stream);
+/* Batched launches per run, and interior points per run (all members). */
+OEB_API int oeb_batch_launches(const oeb_batch_plan* plan);
+OEB_API int64_t oeb_batch_points(const oeb_batch_plan* plan);
+/* Device bytes held by the plan (chain workspaces, scratch arena, tables). */
+OEB_API size_t oeb_batch_plan_bytes(const oeb_batch_plan* plan);
+OEB_API oeb_status oeb_batch_plan_destroy(oeb_batch_plan* plan);
+
+/* ------------------------------------------------------------------------- */
 /* CUDA graphs of library calls.  oeb_graph_begin starts capturing `stream`   */
 /* (thread-local capture mode; not the legacy NULL stream); every library call */
 /* made on it by this thread until oeb_graph_end is recorded, not run, and    */

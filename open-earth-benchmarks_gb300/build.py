@@ -32,6 +32,7 @@ UNITS = {
     "k_fastwavesuv.cu": ["--fmad=false"],
     "k_fvtp2d.cu": ["--fmad=false"],
     "chain.cu": ["--fmad=false"],
+    "batch.cu": [],
 }
 
 

@@ -170,3 +170,88 @@ class Graph:
             self.close()
         except Exception:
             pass
+
+
+class BatchMember(ctypes.Structure):
+    """oeb_batch_member."""
+    _fields_ = [("elem_size", ctypes.c_int), ("dom", Domain), ("fields", ctypes.c_void_p), ("scalars", ChainScalars),
+                ("uout", ctypes.c_void_p), ("vout", ctypes.c_void_p), ("fx1", ctypes.c_void_p),
+                ("fy1", ctypes.c_void_p), ("uoutb", ctypes.c_void_p), ("voutb", ctypes.c_void_p),
+                ("fx1b", ctypes.c_void_p), ("fy1b", ctypes.c_void_p), ("ub", ctypes.c_void_p), ("vb", ctypes.c_void_p)]
+
+
+class BatchPlan:
+    """The chained step of many ensemble members as batched persistent launches
+    (oeb_batch_plan_create / oeb_batch_run / oeb_batch_autotune).
+
+    members: a list of dicts with keys ``fields`` (the step's inputs, as for ChainPlan),
+    ``scalars``, ``domain`` (nx, ny, nz), ``outs`` (uout, vout, fx1, fy1) and, for the
+    adjoint, ``seeds`` (uout, vout, fx1, fy1) and ``grads`` (u, v).  FP64 and FP32 members
+    may be mixed.  The descriptors are copied at creation: every run reads and writes the
+    same buffers."""
+
+    def __init__(self, members, modes: int = FORWARD | ADJOINT):
+        keep = []
+        arr = (BatchMember * len(members))()
+        for i, m in enumerate(members):
+            f = m["fields"]
+            refs = {n: f[n].memref() for n in ORDER}
+            cf = ChainFields(**{n: ctypes.pointer(refs[n]) for n in ORDER})
+            keep += [refs, cf]
+            b = arr[i]
+            b.elem_size = f["u"].dtype.itemsize
+            b.dom = Domain(*m["domain"])
+            b.fields = ctypes.cast(ctypes.pointer(cf), ctypes.c_void_p)
+            b.scalars = ChainPlan._scalars(m["scalars"])
+            io = {}
+            for n in OUTPUTS:
+                io[n] = m["outs"][n] if "outs" in m else None
+                io[n + "b"] = m["seeds"][n] if "seeds" in m else None
+            io["ub"] = m["grads"]["u"] if "grads" in m else None
+            io["vb"] = m["grads"]["v"] if "grads" in m else None
+            for n, st in io.items():
+                if st is not None:
+                    r = st.memref()
+                    keep.append(r)
+                    setattr(b, n, ctypes.cast(ctypes.pointer(r), ctypes.c_void_p))
+        self._plan = ctypes.c_void_p()
+        check(entry("oeb_batch_plan_create")(arr, ctypes.c_int(len(members)), ctypes.c_int(modes),
+                                             ctypes.byref(self._plan)), "oeb_batch_plan_create")
+        del keep
+
+    def run(self, stream=None):
+        check(entry("oeb_batch_run")(self._plan, ctypes.c_void_p(_stream(stream))), "oeb_batch_run")
+
+    def autotune(self, stream=None):
+        check(entry("oeb_batch_autotune")(self._plan, ctypes.c_void_p(_stream(stream))), "oeb_batch_autotune")
+
+    @property
+    def launches(self) -> int:
+        return int(entry("oeb_batch_launches")(self._plan))
+
+    @property
+    def points(self) -> int:
+        lib = load_library()
+        lib.oeb_batch_points.restype = ctypes.c_int64
+        lib.oeb_batch_points.argtypes = [ctypes.c_void_p]
+        return int(lib.oeb_batch_points(self._plan))
+
+    @property
+    def nbytes(self) -> int:
+        lib = load_library()
+        lib.oeb_batch_plan_bytes.restype = ctypes.c_size_t
+        lib.oeb_batch_plan_bytes.argtypes = [ctypes.c_void_p]
+        return int(lib.oeb_batch_plan_bytes(self._plan))
+
+    def close(self):
+        if self._plan:
+            lib = load_library()
+            lib.oeb_batch_plan_destroy.argtypes = [ctypes.c_void_p]
+            check(lib.oeb_batch_plan_destroy(self._plan), "oeb_batch_plan_destroy")
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

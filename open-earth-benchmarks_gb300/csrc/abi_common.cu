@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "oeb_common.cuh"
+#include "launch.cuh"
 
 namespace oeb {
 
@@ -51,6 +52,51 @@ uint64_t capture_count_end() {
   return t_captured;
 }
 bool capture_counting() { return t_capturing; }
+
+namespace {
+thread_local Recorder* t_recorder = nullptr;
+}  // namespace
+
+Recorder* recorder() { return t_recorder; }
+void set_recorder(Recorder* r) { t_recorder = r; }
+
+oeb_status scratch_alloc(void** p, size_t bytes, cudaStream_t st) {
+  *p = nullptr;
+  if (Recorder* r = t_recorder) {
+    const size_t at = (r->used + 255) & ~size_t(255);
+    if (r->arena && at + bytes > r->arena_bytes) return OEB_ERR_TOO_LARGE;
+    // sizing pass: placeholder addresses, never dereferenced (nothing is launched)
+    *p = r->arena ? static_cast<void*>(r->arena + at) : reinterpret_cast<void*>(uintptr_t(4096) + at);
+    r->live.push_back({at, false});
+    r->used = at + bytes;
+    if (r->used > r->peak) r->peak = r->used;
+    return OEB_OK;
+  }
+  cudaMemPool_t pool;
+  OEB_TRY(device_pool(&pool));
+  const cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, st);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  return OEB_OK;
+}
+
+void scratch_free(void* p, cudaStream_t st) {
+  if (!p) return;
+  if (Recorder* r = t_recorder) {
+    const uintptr_t base = r->arena ? reinterpret_cast<uintptr_t>(r->arena) : uintptr_t(4096);
+    const size_t at = reinterpret_cast<uintptr_t>(p) - base;
+    for (auto& a : r->live)
+      if (a.first == at) a.second = true;
+    while (!r->live.empty() && r->live.back().second) {
+      r->used = r->live.back().first;
+      r->live.pop_back();
+    }
+    return;
+  }
+  cudaFreeAsync(p, st);
+}
 
 oeb_status after_launch() {
   cudaError_t e = cudaGetLastError();

@@ -1,0 +1,454 @@
+// batch.cu -- batched ensembles: the chained step of many uneven members as persistent launches.
+//
+// A batch plan is built in three passes over the members (each member has its own chain
+// plan, i.e. its own workspace):
+//   1. sizing: every member's forward and adjoint step is recorded with a placeholder arena,
+//      which measures the scratch the adjoint stencils take (the arena is a stack: a call's
+//      scratch is reused by the next call);
+//   2. recording: the same calls with the member's region of the real arena; every kernel
+//      launch of the step becomes a LaunchRecord (grid, dynamic shared memory, arguments);
+//   3. tables: position p of the recorded sequences is the same kernel for every member of
+//      one precision, so for each position and precision the plan uploads one table of
+//      (member, tile) items -- members largest first -- and one array of argument packs.
+// A run replays the positions in order, each as one batch_kernel launch (launch.cuh) whose
+// CTAs walk the items; FP64 members on the caller's stream, FP32 members on a second stream.
+//
+// The autotuner records the step again with other k-blockings (kb: k-levels per tile of the
+// kernels that take one) and times, for every position and precision, each kb with a single
+// persistent wave (occupancy x SMs CTAs) and with one CTA per tile, keeping the fastest.
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "launch.cuh"
+#include "oeb_common.cuh"
+
+namespace {
+
+struct Member {
+  int elem = 8;
+  oeb_domain dom{};
+  oeb_chain_scalars s{};
+  // descriptor copies, so the plan can record again (autotuning) after the caller's structs
+  // are gone; the fields structs below point into these
+  std::vector<oeb_memref3d_f64> d3;
+  std::vector<oeb_memref1d_f64> d1;
+  std::vector<oeb_memref3d_f32> f3;
+  std::vector<oeb_memref1d_f32> f1;
+  oeb_chain_fields_f64 fields64{};
+  oeb_chain_fields_f32 fields32{};
+  oeb_memref3d_f64 io64[10]{};  // uout vout fx1 fy1 uoutb voutb fx1b fy1b ub vb
+  oeb_memref3d_f32 io32[10]{};
+  oeb_chain_plan* chain = nullptr;
+  size_t arena_off = 0, arena_size = 0;
+};
+
+// One batched launch of a run.
+struct Slot {
+  oeb::BatchLaunchFn fn = nullptr;
+  int side = 0;  // 0: FP64 members on the caller's stream, 1: FP32 members on the plan's stream
+  int members = 0, total = 0;
+  size_t smem = 0;
+  int occupancy = 1;
+  size_t tiles_off = 0, args_off = 0;  // into the device table buffer
+  int ctas = 0;
+  int kb = 0;
+};
+
+}  // namespace
+
+struct oeb_batch_plan {
+  int modes = 0;
+  int device = 0;
+  int sms = 0;
+  std::vector<Member> members;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  char* tables = nullptr;
+  size_t table_bytes = 0;
+  std::vector<Slot> slots;  // forward positions, then adjoint positions
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+namespace oeb {
+namespace {
+
+constexpr int kModes[2] = {OEB_CHAIN_FORWARD, OEB_CHAIN_ADJOINT};
+
+template <class M3, class M1, class F>
+void copy_fields(const F* src, std::vector<M3>& d3, std::vector<M1>& d1, F* dst) {
+  d3.reserve(17);
+  d1.reserve(10);
+  auto c3 = [&](const M3* m) -> const M3* {
+    if (!m) return nullptr;
+    d3.push_back(*m);
+    return &d3.back();
+  };
+  auto c1 = [&](const M1* m) -> const M1* {
+    if (!m) return nullptr;
+    d1.push_back(*m);
+    return &d1.back();
+  };
+  dst->u = c3(src->u);
+  dst->v = c3(src->v);
+  dst->utens = c3(src->utens);
+  dst->vtens = c3(src->vtens);
+  dst->wgtfac = c3(src->wgtfac);
+  dst->ppuv = c3(src->ppuv);
+  dst->hhl = c3(src->hhl);
+  dst->rho = c3(src->rho);
+  dst->fx = c1(src->fx);
+  dst->acrlat0 = c1(src->acrlat0);
+  dst->acrlat1 = c1(src->acrlat1);
+  dst->tgrlatda0 = c1(src->tgrlatda0);
+  dst->tgrlatda1 = c1(src->tgrlatda1);
+  dst->mask = c3(src->mask);
+  dst->crlavo = c1(src->crlavo);
+  dst->crlavu = c1(src->crlavu);
+  dst->crlato = c1(src->crlato);
+  dst->crlatu = c1(src->crlatu);
+  dst->smag_acrlat0 = c1(src->smag_acrlat0);
+  dst->crx = c3(src->crx);
+  dst->cry = c3(src->cry);
+  dst->ra_x = c3(src->ra_x);
+  dst->ra_y = c3(src->ra_y);
+  dst->xfx = c3(src->xfx);
+  dst->yfx = c3(src->yfx);
+  dst->area = c3(src->area);
+}
+
+template <class M3>
+oeb_status copy_io(const oeb_batch_member& src, int modes, M3* io) {
+  const void* p[10] = {src.uout, src.vout, src.fx1, src.fy1, src.uoutb, src.voutb, src.fx1b, src.fy1b, src.ub, src.vb};
+  for (int q = 0; q < 10; ++q) {
+    const bool needed = q < 4 ? (modes & OEB_CHAIN_FORWARD) : (modes & OEB_CHAIN_ADJOINT);
+    if (!p[q]) {
+      if (needed) return OEB_ERR_NULL;
+      continue;
+    }
+    io[q] = *static_cast<const M3*>(p[q]);
+  }
+  return OEB_OK;
+}
+
+// Records member m's step for `mode` into rec (launches nothing).
+oeb_status record(Member& m, int mode, Recorder* rec) {
+  set_recorder(rec);
+  oeb_status st;
+  if (m.elem == 8) {
+    const oeb_memref3d_f64* io = m.io64;
+    st = mode == OEB_CHAIN_FORWARD
+             ? oeb_chain_forward_f64(m.chain, &m.fields64, &m.s, &io[0], &io[1], &io[2], &io[3], nullptr)
+             : oeb_chain_adj_f64(m.chain, &m.fields64, &m.s, &io[4], &io[5], &io[6], &io[7], &io[8], &io[9], nullptr);
+  } else {
+    const oeb_memref3d_f32* io = m.io32;
+    st = mode == OEB_CHAIN_FORWARD
+             ? oeb_chain_forward_f32(m.chain, &m.fields32, &m.s, &io[0], &io[1], &io[2], &io[3], nullptr)
+             : oeb_chain_adj_f32(m.chain, &m.fields32, &m.s, &io[4], &io[5], &io[6], &io[7], &io[8], &io[9], nullptr);
+  }
+  set_recorder(nullptr);
+  return st;
+}
+
+// Recorded sequences of every member for every mode in the plan, with k-blocking kb.
+oeb_status record_all(oeb_batch_plan* p, int kb, std::vector<std::vector<std::vector<LaunchRecord>>>* out) {
+  out->assign(2, {});
+  for (int mi = 0; mi < 2; ++mi) {
+    if (!(p->modes & kModes[mi])) continue;
+    (*out)[mi].resize(p->members.size());
+    for (size_t i = 0; i < p->members.size(); ++i) {
+      Member& m = p->members[i];
+      Recorder rec;
+      rec.kb = kb;
+      rec.arena = p->arena + m.arena_off;
+      rec.arena_bytes = m.arena_size;
+      OEB_TRY(record(m, kModes[mi], &rec));
+      (*out)[mi][i] = std::move(rec.records);
+    }
+  }
+  return OEB_OK;
+}
+
+// Slots and host tables of one recording: for every position, one slot per precision.
+oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vector<LaunchRecord>>>& seq, int kb,
+                       std::vector<Slot>* slots, std::vector<char>* host, size_t base) {
+  for (int mi = 0; mi < 2; ++mi) {
+    if (!(p->modes & kModes[mi])) continue;
+    const auto& per = seq[mi];
+    const size_t len = per[0].size();
+    for (const auto& r : per)
+      if (r.size() != len) return OEB_ERR_UNSUPPORTED;
+    for (size_t pos = 0; pos < len; ++pos) {
+      for (int side = 0; side < 2; ++side) {
+        const int elem = side ? 4 : 8;
+        std::vector<int> who;
+        for (size_t i = 0; i < p->members.size(); ++i)
+          if (p->members[i].elem == elem) who.push_back((int)i);
+        if (who.empty()) continue;
+        const LaunchRecord& r0 = per[who[0]][pos];
+        for (int i : who)
+          if (per[i][pos].launcher != r0.launcher || per[i][pos].args.size() != r0.args.size())
+            return OEB_ERR_UNSUPPORTED;
+        auto tiles_of = [&](int i) {
+          const dim3 g = per[i][pos].grid;
+          return (int64_t)g.x * g.y * g.z;
+        };
+        std::stable_sort(who.begin(), who.end(), [&](int a, int b) { return tiles_of(a) > tiles_of(b); });
+        Slot sl;
+        sl.fn = r0.launcher;
+        sl.side = side;
+        sl.members = (int)who.size();
+        sl.smem = 0;
+        sl.kb = kb;
+        int64_t total = 0;
+        std::vector<BatchTile> tiles;
+        std::vector<char> args;
+        for (int i : who) {
+          const LaunchRecord& r = per[i][pos];
+          tiles.push_back(BatchTile{(int)total, (int)r.grid.x, (int)r.grid.y, 0});
+          total += tiles_of(i);
+          args.insert(args.end(), r.args.begin(), r.args.end());
+          sl.smem = std::max(sl.smem, r.smem);
+        }
+        if (total > INT32_MAX) return OEB_ERR_TOO_LARGE;
+        sl.total = (int)total;
+        sl.occupancy = r0.occupancy(sl.smem);
+        sl.ctas = std::min<int64_t>(total, (int64_t)sl.occupancy * p->sms);
+        auto put = [&](const void* src, size_t n) {
+          const size_t at = (host->size() + 255) & ~size_t(255);
+          host->resize(at + n);
+          memcpy(host->data() + at, src, n);
+          return base + at;
+        };
+        sl.tiles_off = put(tiles.data(), tiles.size() * sizeof(BatchTile));
+        sl.args_off = put(args.data(), args.size());
+        slots->push_back(sl);
+      }
+    }
+  }
+  return OEB_OK;
+}
+
+oeb_status upload(oeb_batch_plan* p, const std::vector<char>& host) {
+  if (p->tables) cudaFree(p->tables);
+  p->tables = nullptr;
+  p->table_bytes = host.size();
+  cudaError_t e = cudaMalloc(&p->tables, std::max<size_t>(host.size(), 256));
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  OEB_CUDA_TRY(cudaMemcpy(p->tables, host.data(), host.size(), cudaMemcpyHostToDevice));
+  return OEB_OK;
+}
+
+oeb_status run_slot(oeb_batch_plan* p, const Slot& sl, int ctas, cudaStream_t main) {
+  return sl.fn(reinterpret_cast<const BatchTile*>(p->tables + sl.tiles_off), sl.members, sl.total,
+               p->tables + sl.args_off, sl.smem, ctas, sl.side ? p->side : main);
+}
+
+oeb_status run(oeb_batch_plan* p, cudaStream_t st) {
+  OEB_CUDA_TRY(cudaEventRecord(p->fork, st));
+  OEB_CUDA_TRY(cudaStreamWaitEvent(p->side, p->fork, 0));
+  for (const Slot& sl : p->slots) OEB_TRY(run_slot(p, sl, sl.ctas, st));
+  OEB_CUDA_TRY(cudaEventRecord(p->join, p->side));
+  OEB_CUDA_TRY(cudaStreamWaitEvent(st, p->join, 0));
+  return OEB_OK;
+}
+
+void destroy(oeb_batch_plan* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  cudaDeviceSynchronize();
+  for (Member& m : p->members)
+    if (m.chain) oeb_chain_plan_destroy(m.chain);
+  if (p->arena) cudaFree(p->arena);
+  if (p->tables) cudaFree(p->tables);
+  if (p->fork) cudaEventDestroy(p->fork);
+  if (p->join) cudaEventDestroy(p->join);
+  if (p->side) cudaStreamDestroy(p->side);
+  delete p;
+}
+
+oeb_status create(const oeb_batch_member* in, int count, int modes, oeb_batch_plan** out) {
+  if (!in || !out) return OEB_ERR_NULL;
+  *out = nullptr;
+  if (count < 1) return OEB_ERR_ARGUMENT;
+  modes &= OEB_CHAIN_FORWARD | OEB_CHAIN_ADJOINT;
+  if (!modes) return OEB_ERR_ARGUMENT;
+  oeb_batch_plan* p = new (std::nothrow) oeb_batch_plan();
+  if (!p) return OEB_ERR_ALLOC;
+  p->modes = modes;
+  auto fail = [&](oeb_status st) {
+    destroy(p);
+    return st;
+  };
+  if (cudaGetDevice(&p->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
+    return fail(cuda_fail(cudaGetLastError()));
+  if (cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming) != cudaSuccess)
+    return fail(cuda_fail(cudaGetLastError()));
+  p->members.resize(count);
+  for (int i = 0; i < count; ++i) {
+    const oeb_batch_member& src = in[i];
+    Member& m = p->members[i];
+    if (src.elem_size != 8 && src.elem_size != 4) return fail(OEB_ERR_ARGUMENT);
+    if (!src.fields) return fail(OEB_ERR_NULL);
+    m.elem = src.elem_size;
+    m.dom = src.dom;
+    m.s = src.scalars;
+    oeb_status st;
+    if (m.elem == 8) {
+      copy_fields(static_cast<const oeb_chain_fields_f64*>(src.fields), m.d3, m.d1, &m.fields64);
+      st = copy_io(src, modes, m.io64);
+      if (st == OEB_OK) {
+        if (!m.fields64.u) return fail(OEB_ERR_NULL);
+        st = oeb_chain_plan_create_f64(m.fields64.u, &m.dom, modes, &m.chain);
+      }
+    } else {
+      copy_fields(static_cast<const oeb_chain_fields_f32*>(src.fields), m.f3, m.f1, &m.fields32);
+      st = copy_io(src, modes, m.io32);
+      if (st == OEB_OK) {
+        if (!m.fields32.u) return fail(OEB_ERR_NULL);
+        st = oeb_chain_plan_create_f32(m.fields32.u, &m.dom, modes, &m.chain);
+      }
+    }
+    if (st != OEB_OK) return fail(st);
+  }
+  // 1. sizing: each member's scratch peak over its recorded calls
+  size_t arena = 0;
+  for (Member& m : p->members) {
+    size_t need = 0;
+    for (int mode : kModes) {
+      if (!(modes & mode)) continue;
+      Recorder rec;
+      const oeb_status st = record(m, mode, &rec);
+      if (st != OEB_OK) return fail(st);
+      need = std::max(need, rec.peak);
+    }
+    m.arena_off = arena;
+    m.arena_size = need;
+    arena += (need + 255) & ~size_t(255);
+  }
+  p->arena_bytes = arena;
+  if (arena) {
+    const cudaError_t e = cudaMalloc(&p->arena, arena);
+    if (e != cudaSuccess) {
+      cuda_fail(e);
+      return fail(OEB_ERR_ALLOC);
+    }
+  }
+  // 2. recording and 3. tables, default k-blocking
+  std::vector<std::vector<std::vector<LaunchRecord>>> seq;
+  oeb_status st = record_all(p, 0, &seq);
+  std::vector<char> host;
+  if (st == OEB_OK) st = build_slots(p, seq, 0, &p->slots, &host, 0);
+  if (st == OEB_OK) st = upload(p, host);
+  if (st != OEB_OK) return fail(st);
+  *out = p;
+  return OEB_OK;
+}
+
+oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
+  const int kbs[] = {1, 2, 4, 8};
+  constexpr int kReps = 3;
+  // every candidate's slots, in one table buffer
+  std::vector<std::vector<Slot>> cand;
+  std::vector<char> host;
+  for (int kb : kbs) {
+    std::vector<std::vector<std::vector<LaunchRecord>>> seq;
+    OEB_TRY(record_all(p, kb, &seq));
+    std::vector<Slot> slots;
+    OEB_TRY(build_slots(p, seq, kb, &slots, &host, 0));
+    if (slots.size() != p->slots.size()) return OEB_ERR_UNSUPPORTED;
+    cand.push_back(std::move(slots));
+  }
+  OEB_TRY(upload(p, host));
+  // the default choice of every slot: kb = 4, one persistent wave
+  std::vector<Slot> best = cand[2];
+  // buffers hold the data of a complete run before single launches are timed
+  for (size_t i = 0; i < best.size(); ++i) best[i].ctas = std::min(best[i].total, best[i].occupancy * p->sms);
+  p->slots = best;
+  OEB_TRY(run(p, st));
+  OEB_CUDA_TRY(cudaStreamSynchronize(st));
+  OEB_CUDA_TRY(cudaStreamSynchronize(p->side));
+  cudaEvent_t e0, e1;
+  OEB_CUDA_TRY(cudaEventCreate(&e0));
+  OEB_CUDA_TRY(cudaEventCreate(&e1));
+  oeb_status result = OEB_OK;
+  for (size_t i = 0; i < best.size() && result == OEB_OK; ++i) {
+    float best_ms = -1.f;
+    for (auto& c : cand) {
+      const Slot& sl = c[i];
+      const cudaStream_t s = sl.side ? p->side : st;
+      const int options[2] = {std::min(sl.total, sl.occupancy * p->sms), sl.total};
+      for (int ctas : options) {
+        result = run_slot(p, sl, ctas, st);  // warm-up
+        if (result != OEB_OK) break;
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < kReps && result == OEB_OK; ++r) result = run_slot(p, sl, ctas, st);
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) result = cuda_fail(cudaGetLastError());
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (result == OEB_OK && (best_ms < 0.f || ms < best_ms)) {
+          best_ms = ms;
+          best[i] = sl;
+          best[i].ctas = ctas;
+        }
+        if (options[0] == options[1]) break;
+      }
+      if (result != OEB_OK) break;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  OEB_TRY(result);
+  p->slots = best;
+  return OEB_OK;
+}
+
+}  // namespace
+}  // namespace oeb
+
+using namespace oeb;
+
+extern "C" oeb_status oeb_batch_plan_create(const oeb_batch_member* members, int count, int modes,
+                                            oeb_batch_plan** out) {
+  return create(members, count, modes, out);
+}
+
+extern "C" oeb_status oeb_batch_run(oeb_batch_plan* p, void* stream) {
+  if (!p) return OEB_ERR_NULL;
+  return run(p, (cudaStream_t)stream);
+}
+
+extern "C" oeb_status oeb_batch_autotune(oeb_batch_plan* p, void* stream) {
+  if (!p) return OEB_ERR_NULL;
+  return autotune(p, (cudaStream_t)stream);
+}
+
+extern "C" int oeb_batch_launches(const oeb_batch_plan* p) { return p ? (int)p->slots.size() : 0; }
+
+extern "C" int64_t oeb_batch_points(const oeb_batch_plan* p) {
+  int64_t n = 0;
+  if (p)
+    for (const Member& m : p->members) n += m.dom.nx * m.dom.ny * m.dom.nz;
+  return n;
+}
+
+extern "C" size_t oeb_batch_plan_bytes(const oeb_batch_plan* p) {
+  if (!p) return 0;
+  size_t n = p->arena_bytes + p->table_bytes;
+  for (const Member& m : p->members) n += oeb_chain_plan_bytes(m.chain);
+  return n;
+}
+
+extern "C" oeb_status oeb_batch_plan_destroy(oeb_batch_plan* p) {
+  if (!p) return OEB_ERR_NULL;
+  destroy(p);
+  return OEB_OK;
+}

@@ -91,14 +91,16 @@ struct Abi<float> {
 // out = alpha x + (y on the box [-ey, n+ey) in i and j, else 0) over the box widened by e;
 // x may be null (0) and may alias out.
 template <class T>
-__global__ void __launch_bounds__(kThreads) combine_kernel(T* out, const T* x, T alpha, const T* __restrict__ y,
-                                                            int ey, Dims d, int e, int kb) {
-  for_box(d, -e, -e, d.nx + 2 * e, d.ny + 2 * e, kb, [&](int64_t o, int i, int j) {
-    const bool in_y = y && i >= -ey && i < d.nx + ey && j >= -ey && j < d.ny + ey;
-    const T a = x ? alpha * x[o] : T(0);
-    out[o] = in_y ? a + y[o] : a;
-  });
-}
+struct combine_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* out, const T* x, T alpha, const T* __restrict__ y,
+                                             int ey, Dims d, int e, int kb) {
+    for_box(blk, d, -e, -e, d.nx + 2 * e, d.ny + 2 * e, kb, [&](int64_t o, int i, int j) {
+      const bool in_y = y && i >= -ey && i < d.nx + ey && j >= -ey && j < d.ny + ey;
+      const T a = x ? alpha * x[o] : T(0);
+      out[o] = in_y ? a + y[o] : a;
+    });
+  }
+};
 
 constexpr int kBoxKB = 4;
 
@@ -192,10 +194,9 @@ oeb_status launch_combine(const oeb_chain_plan* p, void* out, const void* x, T a
                           cudaStream_t st) {
   const Dims d{(int)p->dom.nx, (int)p->dom.ny, (int)p->dom.nz, p->strides[1], p->strides[0]};
   auto org = [&](const void* b) { return b ? static_cast<const T*>(b) + p->offset : nullptr; };
-  combine_kernel<T><<<tile_grid((int)p->dom.nx + 2 * e, (int)p->dom.ny + 2 * e, (int)p->dom.nz, 32, 32, kBoxKB),
-                      dim3(kTX, kTY), 0, st>>>(static_cast<T*>(out) + p->offset, org(x), alpha, org(y), ey, d, e,
-                                               kBoxKB);
-  return after_launch();
+  const int kb = tuned_kb(kBoxKB);
+  return launch<combine_kernel<T>>(tile_grid(d.nx + 2 * e, d.ny + 2 * e, d.nz, 32, 32, kb), 0, st,
+                                   static_cast<T*>(out) + p->offset, org(x), alpha, org(y), ey, d, e, kb);
 }
 
 // Stages 1-3: (u1, v1), (tu, tv), (u2, v2) into the workspace.

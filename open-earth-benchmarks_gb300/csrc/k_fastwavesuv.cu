@@ -28,89 +28,92 @@ struct FastwavesSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) fastwavesuv_kernel(
-    T* __restrict__ uout, T* __restrict__ vout, const T* __restrict__ uin, const T* __restrict__ vin,
-    const T* __restrict__ utens, const T* __restrict__ vtens, const T* __restrict__ wgtfac,
-    const T* __restrict__ ppuv, const T* __restrict__ hhl, const T* __restrict__ rho, const T* __restrict__ fx,
-    int64_t s1d, T ed2, T dt, Dims d, int kb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FastwavesSmem<T>& s = *reinterpret_cast<FastwavesSmem<T>*>(smem_raw);
-  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
-  const int sj = (int)d.sj;
-  const int64_t sk = d.sk;
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-  if (tid < kT) {
-    const int j = j0 + tid;
-    s.fx2[tid] = (j < d.ny) ? T(2.0) * ld(fx + (int64_t)j * s1d) : T(0);
-  }
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
-
-  // Region points owned by this thread, and ppgk at the current level for each.
-  int own_off[kOwned];
-  bool own_ok[kOwned];
-  T ppgk_cur[kOwned];
-#pragma unroll
-  for (int t = 0; t < kOwned; ++t) {
-    const int e = tid + t * kThreads;
-    const int b = e / kR, a = e - (e / kR) * kR;
-    const int i = i0 + a, j = j0 + b;
-    own_ok[t] = e < kR * kR && i < d.nx + 1 && j < d.ny + 1;
-    own_off[t] = i + j * sj;
-    ppgk_cur[t] = T(0);
-    if (own_ok[t]) {
-      const int64_t o = (int64_t)k0 * sk + own_off[t];
-      const T w = ld(wgtfac + o);
-      ppgk_cur[t] = w * ld(ppuv + o) + (T(1.0) - w) * ld(ppuv + o - sk);  // fastwavesuv.h:162
+struct fastwavesuv_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
+                                             const T* __restrict__ uin, const T* __restrict__ vin,
+                                             const T* __restrict__ utens, const T* __restrict__ vtens,
+                                             const T* __restrict__ wgtfac, const T* __restrict__ ppuv,
+                                             const T* __restrict__ hhl, const T* __restrict__ rho,
+                                             const T* __restrict__ fx, int64_t s1d, T ed2, T dt, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FastwavesSmem<T>& s = *reinterpret_cast<FastwavesSmem<T>*>(smem_raw);
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int sj = (int)d.sj;
+    const int64_t sk = d.sk;
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    if (tid < kT) {
+      const int j = j0 + tid;
+      s.fx2[tid] = (j < d.ny) ? T(2.0) * ld(fx + (int64_t)j * s1d) : T(0);
     }
-  }
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
 
-#pragma unroll 1
-  for (int k = k0; k < k1; ++k) {
-    const int64_t kofs = (int64_t)k * sk;
-#pragma unroll
+    // Region points owned by this thread, and ppgk at the current level for each.
+    int own_off[kOwned];
+    bool own_ok[kOwned];
+    T ppgk_cur[kOwned];
+  #pragma unroll
     for (int t = 0; t < kOwned; ++t) {
       const int e = tid + t * kThreads;
-      if (e < kR * kR) {
-        const int b = e / kR, a = e - b * kR;
-        T pc = T(0), hsum = T(0), hdif = T(0);
-        if (own_ok[t]) {
-          const int64_t o = kofs + own_off[t];
-          const T w1 = ld(wgtfac + o + sk);
-          const T next = w1 * ld(ppuv + o + sk) + (T(1.0) - w1) * ld(ppuv + o);  // ppgk at k+1
-          pc = next - ppgk_cur[t];
-          ppgk_cur[t] = next;
-          const T h1 = ld(hhl + o + sk), h0 = ld(hhl + o);
-          hsum = h1 + h0;
-          hdif = h1 - h0;
-        }
-        s.ppgc[b][a] = pc;
-        s.hs[b][a] = hsum;
-        s.hd[b][a] = hdif;
+      const int b = e / kR, a = e - (e / kR) * kR;
+      const int i = i0 + a, j = j0 + b;
+      own_ok[t] = e < kR * kR && i < d.nx + 1 && j < d.ny + 1;
+      own_off[t] = i + j * sj;
+      ppgk_cur[t] = T(0);
+      if (own_ok[t]) {
+        const int64_t o = (int64_t)k0 * sk + own_off[t];
+        const T w = ld(wgtfac + o);
+        ppgk_cur[t] = w * ld(ppuv + o) + (T(1.0) - w) * ld(ppuv + o - sk);  // fastwavesuv.h:162
       }
     }
-    __syncthreads();
-    for_region<kT, kT>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      if (i < d.nx && j < d.ny) {
-        const int64_t o = kofs + i + j * sj;
-        const T p0 = ld(ppuv + o);
-        const T r0 = ld(rho + o);
-        // fastwavesuv.h:172-175
-        const T ppgu = (ld(ppuv + o + 1) - p0) + (((s.ppgc[b][a + 1] + s.ppgc[b][a]) * T(0.5)) *
-                                                      (s.hs[b][a] - s.hs[b][a + 1])) /
-                                                         (s.hd[b][a] + s.hd[b][a + 1]);
-        // fastwavesuv.h:177-180
-        const T ppgv = (ld(ppuv + o + sj) - p0) + (((s.ppgc[b + 1][a] + s.ppgc[b][a]) * T(0.5)) *
-                                                       (s.hs[b][a] - s.hs[b + 1][a])) /
-                                                          (s.hd[b][a] + s.hd[b + 1][a]);
-        // fastwavesuv.h:182-186
-        uout[o] = ld(uin + o) + dt * (ld(utens + o) - ppgu * (s.fx2[b] / (ld(rho + o + 1) + r0)));
-        vout[o] = ld(vin + o) + dt * (ld(vtens + o) - ppgv * (ed2 / (ld(rho + o + sj) + r0)));
+
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * sk;
+  #pragma unroll
+      for (int t = 0; t < kOwned; ++t) {
+        const int e = tid + t * kThreads;
+        if (e < kR * kR) {
+          const int b = e / kR, a = e - b * kR;
+          T pc = T(0), hsum = T(0), hdif = T(0);
+          if (own_ok[t]) {
+            const int64_t o = kofs + own_off[t];
+            const T w1 = ld(wgtfac + o + sk);
+            const T next = w1 * ld(ppuv + o + sk) + (T(1.0) - w1) * ld(ppuv + o);  // ppgk at k+1
+            pc = next - ppgk_cur[t];
+            ppgk_cur[t] = next;
+            const T h1 = ld(hhl + o + sk), h0 = ld(hhl + o);
+            hsum = h1 + h0;
+            hdif = h1 - h0;
+          }
+          s.ppgc[b][a] = pc;
+          s.hs[b][a] = hsum;
+          s.hd[b][a] = hdif;
+        }
       }
-    });
-    __syncthreads();
+      __syncthreads();
+      for_region<kT, kT>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < d.nx && j < d.ny) {
+          const int64_t o = kofs + i + j * sj;
+          const T p0 = ld(ppuv + o);
+          const T r0 = ld(rho + o);
+          // fastwavesuv.h:172-175
+          const T ppgu = (ld(ppuv + o + 1) - p0) + (((s.ppgc[b][a + 1] + s.ppgc[b][a]) * T(0.5)) *
+                                                        (s.hs[b][a] - s.hs[b][a + 1])) /
+                                                           (s.hd[b][a] + s.hd[b][a + 1]);
+          // fastwavesuv.h:177-180
+          const T ppgv = (ld(ppuv + o + sj) - p0) + (((s.ppgc[b + 1][a] + s.ppgc[b][a]) * T(0.5)) *
+                                                         (s.hs[b][a] - s.hs[b + 1][a])) /
+                                                            (s.hd[b][a] + s.hd[b + 1][a]);
+          // fastwavesuv.h:182-186
+          uout[o] = ld(uin + o) + dt * (ld(utens + o) - ppgu * (s.fx2[b] / (ld(rho + o + 1) + r0)));
+          vout[o] = ld(vin + o) + dt * (ld(vtens + o) - ppgv * (ed2 / (ld(rho + o + sj) + r0)));
+        }
+      });
+      __syncthreads();
+    }
   }
-}
+};
 
 constexpr int kKB = 4;
 
@@ -139,12 +142,11 @@ oeb_status fastwavesuv_entry(const M3* uout, const M3* vout, const M3* uin, cons
   OEB_RETURN_IF_VALIDATING();
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gu.sj, gu.sk};
   const T ed2 = T(2.0) * edadlat;  // ElementType(2.0) * edadlat, fastwavesuv.h:186
-  OEB_TRY(ensure_dyn_smem((const void*)fastwavesuv_kernel<T>, (int)sizeof(FastwavesSmem<T>)));
-  fastwavesuv_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FastwavesSmem<T>),
-                          (cudaStream_t)stream>>>(
-      gu.origin, gv.origin, gui.origin, gvi.origin, gut.origin, gvt.origin, gw.origin, gp.origin, gh.origin,
-      gr.origin, lfx.origin, lfx.s, ed2, dt, d, kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<fastwavesuv_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FastwavesSmem<T>),
+                                       (cudaStream_t)stream, gu.origin, gv.origin, gui.origin, gvi.origin, gut.origin,
+                                       gvt.origin, gw.origin, gp.origin, gh.origin, gr.origin, lfx.origin, lfx.s, ed2,
+                                       dt, d, kb);
 }
 
 // Tangent-linear fastwavesuv with respect to (uin, vin, utens, vtens, ppuv); wgtfac, hhl,
@@ -179,11 +181,10 @@ oeb_status fastwavesuv_tl_entry(const M3* duout, const M3* dvout, const M3* uin,
   OEB_TRY(arr.alloc(dvout, &ov));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
   const D ed2 = D(T(2.0) * edadlat);
-  OEB_TRY(ensure_dyn_smem((const void*)fastwavesuv_kernel<D>, (int)sizeof(FastwavesSmem<D>)));
-  fastwavesuv_kernel<D><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FastwavesSmem<D>),
-                          (cudaStream_t)stream>>>(ou, ov, u, v, ut, vt, w, p, h, r, f, fx->strides[0], ed2, D(dt), d,
-                                                  kKB);
-  OEB_TRY(after_launch());
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<fastwavesuv_kernel<D>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FastwavesSmem<D>),
+                                        (cudaStream_t)stream, ou, ov, u, v, ut, vt, w, p, h, r, f, fx->strides[0], ed2,
+                                        D(dt), d, kb));
   OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
   return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
 }
@@ -210,92 +211,95 @@ struct FastwavesAdjSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) fastwavesuv_adj_kernel(
-    T* __restrict__ uinb, T* __restrict__ vinb, T* __restrict__ utensb, T* __restrict__ vtensb,
-    T* __restrict__ ppuvb, const T* __restrict__ wgtfac, const T* __restrict__ hhl, const T* __restrict__ rho,
-    const T* __restrict__ fx, int64_t s1d, const T* __restrict__ uoutb, const T* __restrict__ voutb, T ed2, T dt,
-    Dims d, int kb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FastwavesAdjSmem<T>& s = *reinterpret_cast<FastwavesAdjSmem<T>*>(smem_raw);
-  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
-  const int sj = (int)d.sj;
-  const int64_t sk = d.sk;
-  // output levels K in [Ks, Ke) of the extended range [-1, nz+1)
-  const int Ks = -1 + (int)blockIdx.z * kb, Ke = min(Ks + kb, d.nz + 1);
-  constexpr int kPts = kT * kT / kThreads;
-  T cm2[kPts], cm1[kPts], dir[kPts];  // cb(L-2), cb(L-1), direct terms of level L-1
-#pragma unroll
-  for (int t = 0; t < kPts; ++t) cm2[t] = cm1[t] = dir[t] = T(0);
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-  // adjoint of ppgu (au) and of ppgv (av) at an interior point, times g when asked
-  auto au_at = [&](int i, int j, int k, bool with_g) -> T {
-    if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
-    const int64_t o = (int64_t)k * sk + i + j * sj;
-    const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
-    const T a = -(dt * qx) * ld(uoutb + o);
-    if (!with_g) return a;
-    const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
-    const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
-    return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
-  };
-  auto av_at = [&](int i, int j, int k, bool with_g) -> T {
-    if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
-    const int64_t o = (int64_t)k * sk + i + j * sj;
-    const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
-    const T a = -(dt * qy) * ld(voutb + o);
-    if (!with_g) return a;
-    const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
-    const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
-    return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
-  };
-#pragma unroll 1
-  for (int L = Ks - 1; L <= Ke; ++L) {
-    // au, av and their g-weighted versions at level L over the tile plus the low apron
-    for_region<kR, kT>([&](int a, int b) {
-      const int i = i0 - 1 + a, j = j0 + b;
-      const T raw = au_at(i, j, L, false);
-      s.au[b][a] = raw;
-      s.ax[b][a] = (raw == T(0)) ? T(0) : au_at(i, j, L, true);
-    });
-    for_region<kT, kR>([&](int a, int b) {
-      const int i = i0 + a, j = j0 - 1 + b;
-      const T raw = av_at(i, j, L, false);
-      s.av[b][a] = raw;
-      s.ay[b][a] = (raw == T(0)) ? T(0) : av_at(i, j, L, true);
-    });
-    __syncthreads();
-#pragma unroll
-    for (int t = 0; t < kPts; ++t) {
-      const int e = tid + t * kThreads;
-      const int b = e / kT, a = e - b * kT;
-      const int i = i0 + a, j = j0 + b;
-      // cb(L) at (i, j): ppgc(i) feeds ppgu(i), ppgu(i-1), ppgv(j), ppgv(j-1)
-      const T cl = (L >= 0 && L < d.nz) ? ((s.ax[b][a + 1] + s.ax[b][a]) + (s.ay[b + 1][a] + s.ay[b][a])) : T(0);
-      const int K = L - 1;  // output level
-      if (K >= Ks && K < Ke && i <= d.nx && j <= d.ny) {
-        const int64_t o = (int64_t)K * sk + i + j * sj;
-        const T kbK = cm2[t] - cm1[t];  // kb(K)   = cb(K-1) - cb(K)
-        const T kbK1 = cm1[t] - cl;     // kb(K+1) = cb(K)   - cb(K+1)
-        T acc = dir[t];
-        if (K >= 0) acc = acc + ld(wgtfac + o) * kbK;
-        if (K + 1 <= d.nz) acc = acc + (T(1.0) - ld(wgtfac + o + sk)) * kbK1;
-        ppuvb[o] = acc;
-        if (K >= 0 && K < d.nz && i < d.nx && j < d.ny) {
-          const T ub = ld(uoutb + o), vb = ld(voutb + o);
-          uinb[o] = ub;
-          vinb[o] = vb;
-          utensb[o] = dt * ub;
-          vtensb[o] = dt * vb;
+struct fastwavesuv_adj_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
+                                             T* __restrict__ utensb, T* __restrict__ vtensb, T* __restrict__ ppuvb,
+                                             const T* __restrict__ wgtfac, const T* __restrict__ hhl,
+                                             const T* __restrict__ rho, const T* __restrict__ fx, int64_t s1d,
+                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T ed2, T dt,
+                                             Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FastwavesAdjSmem<T>& s = *reinterpret_cast<FastwavesAdjSmem<T>*>(smem_raw);
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int sj = (int)d.sj;
+    const int64_t sk = d.sk;
+    // output levels K in [Ks, Ke) of the extended range [-1, nz+1)
+    const int Ks = -1 + (int)blk.z * kb, Ke = min(Ks + kb, d.nz + 1);
+    constexpr int kPts = kT * kT / kThreads;
+    T cm2[kPts], cm1[kPts], dir[kPts];  // cb(L-2), cb(L-1), direct terms of level L-1
+  #pragma unroll
+    for (int t = 0; t < kPts; ++t) cm2[t] = cm1[t] = dir[t] = T(0);
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    // adjoint of ppgu (au) and of ppgv (av) at an interior point, times g when asked
+    auto au_at = [&](int i, int j, int k, bool with_g) -> T {
+      if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
+      const int64_t o = (int64_t)k * sk + i + j * sj;
+      const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
+      const T a = -(dt * qx) * ld(uoutb + o);
+      if (!with_g) return a;
+      const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
+      const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
+      return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+    };
+    auto av_at = [&](int i, int j, int k, bool with_g) -> T {
+      if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
+      const int64_t o = (int64_t)k * sk + i + j * sj;
+      const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
+      const T a = -(dt * qy) * ld(voutb + o);
+      if (!with_g) return a;
+      const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
+      const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
+      return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+    };
+  #pragma unroll 1
+    for (int L = Ks - 1; L <= Ke; ++L) {
+      // au, av and their g-weighted versions at level L over the tile plus the low apron
+      for_region<kR, kT>([&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 + b;
+        const T raw = au_at(i, j, L, false);
+        s.au[b][a] = raw;
+        s.ax[b][a] = (raw == T(0)) ? T(0) : au_at(i, j, L, true);
+      });
+      for_region<kT, kR>([&](int a, int b) {
+        const int i = i0 + a, j = j0 - 1 + b;
+        const T raw = av_at(i, j, L, false);
+        s.av[b][a] = raw;
+        s.ay[b][a] = (raw == T(0)) ? T(0) : av_at(i, j, L, true);
+      });
+      __syncthreads();
+  #pragma unroll
+      for (int t = 0; t < kPts; ++t) {
+        const int e = tid + t * kThreads;
+        const int b = e / kT, a = e - b * kT;
+        const int i = i0 + a, j = j0 + b;
+        // cb(L) at (i, j): ppgc(i) feeds ppgu(i), ppgu(i-1), ppgv(j), ppgv(j-1)
+        const T cl = (L >= 0 && L < d.nz) ? ((s.ax[b][a + 1] + s.ax[b][a]) + (s.ay[b + 1][a] + s.ay[b][a])) : T(0);
+        const int K = L - 1;  // output level
+        if (K >= Ks && K < Ke && i <= d.nx && j <= d.ny) {
+          const int64_t o = (int64_t)K * sk + i + j * sj;
+          const T kbK = cm2[t] - cm1[t];  // kb(K)   = cb(K-1) - cb(K)
+          const T kbK1 = cm1[t] - cl;     // kb(K+1) = cb(K)   - cb(K+1)
+          T acc = dir[t];
+          if (K >= 0) acc = acc + ld(wgtfac + o) * kbK;
+          if (K + 1 <= d.nz) acc = acc + (T(1.0) - ld(wgtfac + o + sk)) * kbK1;
+          ppuvb[o] = acc;
+          if (K >= 0 && K < d.nz && i < d.nx && j < d.ny) {
+            const T ub = ld(uoutb + o), vb = ld(voutb + o);
+            uinb[o] = ub;
+            vinb[o] = vb;
+            utensb[o] = dt * ub;
+            vtensb[o] = dt * vb;
+          }
         }
+        // direct terms of level L: au(i-1) - au(i) + av(j-1) - av(j)
+        dir[t] = (s.au[b][a] - s.au[b][a + 1]) + (s.av[b][a] - s.av[b + 1][a]);
+        cm2[t] = cm1[t];
+        cm1[t] = cl;
       }
-      // direct terms of level L: au(i-1) - au(i) + av(j-1) - av(j)
-      dir[t] = (s.au[b][a] - s.au[b][a + 1]) + (s.av[b][a] - s.av[b + 1][a]);
-      cm2[t] = cm1[t];
-      cm1[t] = cl;
+      __syncthreads();
     }
-    __syncthreads();
   }
-}
+};
 
 template <class T, class M3, class M1>
 oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utensb, const M3* vtensb,
@@ -329,13 +333,11 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   OEB_RETURN_IF_VALIDATING();
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gw.sj, gw.sk};
   const T ed2 = T(2.0) * edadlat;
-  const size_t smem = sizeof(FastwavesAdjSmem<T>);
-  OEB_TRY(ensure_dyn_smem((const void*)fastwavesuv_adj_kernel<T>, (int)smem));
-  fastwavesuv_adj_kernel<T><<<tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kKB), dim3(kTX, kTY), smem,
-                              (cudaStream_t)stream>>>(gub.origin, gvb.origin, gutb.origin, gvtb.origin, gpb.origin,
-                                                      gw.origin, gh.origin, gr.origin, lfx.origin, lfx.s, guo.origin,
-                                                      gvo.origin, ed2, dt, d, kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<fastwavesuv_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
+                                           sizeof(FastwavesAdjSmem<T>), (cudaStream_t)stream, gub.origin, gvb.origin,
+                                           gutb.origin, gvtb.origin, gpb.origin, gw.origin, gh.origin, gr.origin,
+                                           lfx.origin, lfx.s, guo.origin, gvo.origin, ed2, dt, d, kb);
 }
 
 }  // namespace

@@ -83,89 +83,90 @@ struct FvQSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) fvtp2d_q_kernel(T* __restrict__ q_i, T* __restrict__ q_j,
-                                                            T* __restrict__ fx2, T* __restrict__ fy2,
-                                                            const T* __restrict__ q, const T* __restrict__ crx,
-                                                            const T* __restrict__ cry, const T* __restrict__ ra_x,
-                                                            const T* __restrict__ ra_y, const T* __restrict__ xfx,
-                                                            const T* __restrict__ yfx, const T* __restrict__ area,
-                                                            T p1, T p2, Dims d, int kb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FvQSmem<T>& s = *reinterpret_cast<FvQSmem<T>*>(smem_raw);
-  const int i0 = -3 + (int)blockIdx.x * kT, j0 = -3 + (int)blockIdx.y * kT;
-  const int sj = (int)d.sj;
-  const int nx = d.nx, ny = d.ny;
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
-#pragma unroll 1
-  for (int k = k0; k < k1; ++k) {
-    const int64_t kofs = (int64_t)k * d.sk;
-    for_region<38, 39>([&](int a, int b) {
-      const int i = i0 - 3 + a, j = j0 - 3 + b;
-      const bool ok = i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3;
-      s.q[b][a] = ok ? ld(q + kofs + i + j * sj) : T(0);
-    });
-    __syncthreads();
-    // ---- y-PPM of q -> fy2, fyy
-    for_region<32, 35>([&](int a, int b) {
-      s.w.y.al[b][a] = ppm_al(p1, p2, s.q[b][a + 3], s.q[b + 1][a + 3], s.q[b + 2][a + 3], s.q[b + 3][a + 3]);
-    });
-    __syncthreads();
-    for_region<32, 34>([&](int a, int b) {
-      ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.q[b + 2][a + 3], &s.w.y.almq[b][a], &s.w.y.br[b][a],
-              &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
-    });
-    __syncthreads();
-    for_region<32, 33>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      T fyy = T(0);
-      if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {  // fvtp2d.h:26-27
+struct fvtp2d_q_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ q_i, T* __restrict__ q_j,
+                                             T* __restrict__ fx2, T* __restrict__ fy2, const T* __restrict__ q,
+                                             const T* __restrict__ crx, const T* __restrict__ cry,
+                                             const T* __restrict__ ra_x, const T* __restrict__ ra_y,
+                                             const T* __restrict__ xfx, const T* __restrict__ yfx,
+                                             const T* __restrict__ area, T p1, T p2, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FvQSmem<T>& s = *reinterpret_cast<FvQSmem<T>*>(smem_raw);
+    const int i0 = -3 + (int)blk.x * kT, j0 = -3 + (int)blk.y * kT;
+    const int sj = (int)d.sj;
+    const int nx = d.nx, ny = d.ny;
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region<38, 39>([&](int a, int b) {
+        const int i = i0 - 3 + a, j = j0 - 3 + b;
+        const bool ok = i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3;
+        s.q[b][a] = ok ? ld(q + kofs + i + j * sj) : T(0);
+      });
+      __syncthreads();
+      // ---- y-PPM of q -> fy2, fyy
+      for_region<32, 35>([&](int a, int b) {
+        s.w.y.al[b][a] = ppm_al(p1, p2, s.q[b][a + 3], s.q[b + 1][a + 3], s.q[b + 2][a + 3], s.q[b + 3][a + 3]);
+      });
+      __syncthreads();
+      for_region<32, 34>([&](int a, int b) {
+        ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.q[b + 2][a + 3], &s.w.y.almq[b][a], &s.w.y.br[b][a],
+                &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
+      });
+      __syncthreads();
+      for_region<32, 33>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        T fyy = T(0);
+        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {  // fvtp2d.h:26-27
+          const int64_t o = kofs + i + j * sj;
+          const T f = ppm_flux(ld(cry + o), s.q[b + 2][a + 3], s.q[b + 3][a + 3], s.w.y.br[b][a], s.w.y.b0[b][a],
+                                    s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
+          if (b < kT) fy2[o] = f;
+          fyy = ld(yfx + o) * f;  // fvtp2d.h:43
+        }
+        s.fyy[b][a] = fyy;
+      });
+      __syncthreads();
+      // ---- x-PPM of q -> fx2, fxx
+      for_region<35, 32>([&](int a, int b) {
+        s.w.x.al[b][a] = ppm_al(p1, p2, s.q[b + 3][a], s.q[b + 3][a + 1], s.q[b + 3][a + 2], s.q[b + 3][a + 3]);
+      });
+      __syncthreads();
+      for_region<34, 32>([&](int a, int b) {
+        ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.q[b + 3][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
+                &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
+      });
+      __syncthreads();
+      for_region<33, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        T fxx = T(0);
+        if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {  // fvtp2d.h:102-103
+          const int64_t o = kofs + i + j * sj;
+          const T f = ppm_flux(ld(crx + o), s.q[b + 3][a + 2], s.q[b + 3][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
+                                    s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
+          if (a < kT) fx2[o] = f;
+          fxx = ld(xfx + o) * f;  // fvtp2d.h:119
+        }
+        s.fxx[b][a] = fxx;
+      });
+      __syncthreads();
+      // ---- q_i (fvtp2d.h:48) and q_j (fvtp2d.h:124)
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
         const int64_t o = kofs + i + j * sj;
-        const T f = ppm_flux(ld(cry + o), s.q[b + 2][a + 3], s.q[b + 3][a + 3], s.w.y.br[b][a], s.w.y.b0[b][a],
-                                  s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
-        if (b < kT) fy2[o] = f;
-        fyy = ld(yfx + o) * f;  // fvtp2d.h:43
-      }
-      s.fyy[b][a] = fyy;
-    });
-    __syncthreads();
-    // ---- x-PPM of q -> fx2, fxx
-    for_region<35, 32>([&](int a, int b) {
-      s.w.x.al[b][a] = ppm_al(p1, p2, s.q[b + 3][a], s.q[b + 3][a + 1], s.q[b + 3][a + 2], s.q[b + 3][a + 3]);
-    });
-    __syncthreads();
-    for_region<34, 32>([&](int a, int b) {
-      ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.q[b + 3][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
-              &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
-    });
-    __syncthreads();
-    for_region<33, 32>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      T fxx = T(0);
-      if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {  // fvtp2d.h:102-103
-        const int64_t o = kofs + i + j * sj;
-        const T f = ppm_flux(ld(crx + o), s.q[b + 3][a + 2], s.q[b + 3][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
-                                  s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
-        if (a < kT) fx2[o] = f;
-        fxx = ld(xfx + o) * f;  // fvtp2d.h:119
-      }
-      s.fxx[b][a] = fxx;
-    });
-    __syncthreads();
-    // ---- q_i (fvtp2d.h:48) and q_j (fvtp2d.h:124)
-    for_region<32, 32>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      const int64_t o = kofs + i + j * sj;
-      const T qc = s.q[b + 3][a + 3];
-      if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
-        q_i[o] = (((qc * ld(area + o)) + s.fyy[b][a]) - s.fyy[b + 1][a]) / ld(ra_y + o);
-      }
-      if (i >= 0 && i < nx && j >= -3 && j < ny + 2) {
-        q_j[o] = (((qc * ld(area + o)) + s.fxx[b][a]) - s.fxx[b][a + 1]) / ld(ra_x + o);
-      }
-    });
-    __syncthreads();
+        const T qc = s.q[b + 3][a + 3];
+        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
+          q_i[o] = (((qc * ld(area + o)) + s.fyy[b][a]) - s.fyy[b + 1][a]) / ld(ra_y + o);
+        }
+        if (i >= 0 && i < nx && j >= -3 && j < ny + 2) {
+          q_j[o] = (((qc * ld(area + o)) + s.fxx[b][a]) - s.fxx[b][a + 1]) / ld(ra_x + o);
+        }
+      });
+      __syncthreads();
+    }
   }
-}
+};
 
 // ------------------------------ launch 2 ---------------------------------------------
 // Interior tile origin (i0, j0).  Shared layout:
@@ -191,72 +192,74 @@ struct FvFluxSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) fvtp2d_flux_kernel(T* __restrict__ fx1, T* __restrict__ fy1,
-                                                               const T* __restrict__ q_i, const T* __restrict__ q_j,
-                                                               const T* __restrict__ fx2, const T* __restrict__ fy2,
-                                                               const T* __restrict__ crx, const T* __restrict__ cry,
-                                                               const T* __restrict__ xfx, const T* __restrict__ yfx,
-                                                               T p1, T p2, Dims d, int kb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FvFluxSmem<T>& s = *reinterpret_cast<FvFluxSmem<T>*>(smem_raw);
-  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
-  const int sj = (int)d.sj;
-  const int nx = d.nx, ny = d.ny;
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
-#pragma unroll 1
-  for (int k = k0; k < k1; ++k) {
-    const int64_t kofs = (int64_t)k * d.sk;
-    for_region<37, 32>([&](int a, int b) {
-      const int i = i0 - 3 + a, j = j0 + b;
-      s.qi[b][a] = (i < nx + 2 && j < ny) ? ld(q_i + kofs + i + j * sj) : T(0);
-    });
-    for_region<32, 37>([&](int a, int b) {
-      const int i = i0 + a, j = j0 - 3 + b;
-      s.qj[b][a] = (i < nx && j < ny + 2) ? ld(q_j + kofs + i + j * sj) : T(0);
-    });
-    __syncthreads();
-    // ---- x-PPM of q_i -> fx1 and the x transport flux
-    for_region<34, 32>([&](int a, int b) {
-      s.w.x.al[b][a] = ppm_al(p1, p2, s.qi[b][a], s.qi[b][a + 1], s.qi[b][a + 2], s.qi[b][a + 3]);
-    });
-    __syncthreads();
-    for_region<33, 32>([&](int a, int b) {
-      ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.qi[b][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
-              &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
-    });
-    __syncthreads();
-    for_region<32, 32>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      if (i < nx && j < ny) {
-        const int64_t o = kofs + i + j * sj;
-        const T f = ppm_flux(ld(crx + o), s.qi[b][a + 2], s.qi[b][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
-                                  s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
-        fx1[o] = ((T(0.5) * (f + ld(fx2 + o))) * ld(xfx + o));  // fvtp2d.h:164
-      }
-    });
-    __syncthreads();
-    // ---- y-PPM of q_j -> fy1 and the y transport flux
-    for_region<32, 34>([&](int a, int b) {
-      s.w.y.al[b][a] = ppm_al(p1, p2, s.qj[b][a], s.qj[b + 1][a], s.qj[b + 2][a], s.qj[b + 3][a]);
-    });
-    __syncthreads();
-    for_region<32, 33>([&](int a, int b) {
-      ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.qj[b + 2][a], &s.w.y.almq[b][a], &s.w.y.br[b][a],
-              &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
-    });
-    __syncthreads();
-    for_region<32, 32>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      if (i < nx && j < ny) {
-        const int64_t o = kofs + i + j * sj;
-        const T f = ppm_flux(ld(cry + o), s.qj[b + 2][a], s.qj[b + 3][a], s.w.y.br[b][a], s.w.y.b0[b][a],
-                                  s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
-        fy1[o] = ((T(0.5) * (f + ld(fy2 + o))) * ld(yfx + o));  // fvtp2d.h:173
-      }
-    });
-    __syncthreads();
+struct fvtp2d_flux_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ fx1, T* __restrict__ fy1,
+                                             const T* __restrict__ q_i, const T* __restrict__ q_j,
+                                             const T* __restrict__ fx2, const T* __restrict__ fy2,
+                                             const T* __restrict__ crx, const T* __restrict__ cry,
+                                             const T* __restrict__ xfx, const T* __restrict__ yfx, T p1, T p2, Dims d,
+                                             int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FvFluxSmem<T>& s = *reinterpret_cast<FvFluxSmem<T>*>(smem_raw);
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int sj = (int)d.sj;
+    const int nx = d.nx, ny = d.ny;
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region<37, 32>([&](int a, int b) {
+        const int i = i0 - 3 + a, j = j0 + b;
+        s.qi[b][a] = (i < nx + 2 && j < ny) ? ld(q_i + kofs + i + j * sj) : T(0);
+      });
+      for_region<32, 37>([&](int a, int b) {
+        const int i = i0 + a, j = j0 - 3 + b;
+        s.qj[b][a] = (i < nx && j < ny + 2) ? ld(q_j + kofs + i + j * sj) : T(0);
+      });
+      __syncthreads();
+      // ---- x-PPM of q_i -> fx1 and the x transport flux
+      for_region<34, 32>([&](int a, int b) {
+        s.w.x.al[b][a] = ppm_al(p1, p2, s.qi[b][a], s.qi[b][a + 1], s.qi[b][a + 2], s.qi[b][a + 3]);
+      });
+      __syncthreads();
+      for_region<33, 32>([&](int a, int b) {
+        ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.qi[b][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
+                &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
+      });
+      __syncthreads();
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < nx && j < ny) {
+          const int64_t o = kofs + i + j * sj;
+          const T f = ppm_flux(ld(crx + o), s.qi[b][a + 2], s.qi[b][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
+                                    s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
+          fx1[o] = ((T(0.5) * (f + ld(fx2 + o))) * ld(xfx + o));  // fvtp2d.h:164
+        }
+      });
+      __syncthreads();
+      // ---- y-PPM of q_j -> fy1 and the y transport flux
+      for_region<32, 34>([&](int a, int b) {
+        s.w.y.al[b][a] = ppm_al(p1, p2, s.qj[b][a], s.qj[b + 1][a], s.qj[b + 2][a], s.qj[b + 3][a]);
+      });
+      __syncthreads();
+      for_region<32, 33>([&](int a, int b) {
+        ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.qj[b + 2][a], &s.w.y.almq[b][a], &s.w.y.br[b][a],
+                &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
+      });
+      __syncthreads();
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < nx && j < ny) {
+          const int64_t o = kofs + i + j * sj;
+          const T f = ppm_flux(ld(cry + o), s.qj[b + 2][a], s.qj[b + 3][a], s.w.y.br[b][a], s.w.y.b0[b][a],
+                                    s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
+          fy1[o] = ((T(0.5) * (f + ld(fy2 + o))) * ld(yfx + o));  // fvtp2d.h:173
+        }
+      });
+      __syncthreads();
+    }
   }
-}
+};
 
 constexpr int kKB = 4;
 
@@ -289,18 +292,16 @@ oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* f
                          {gq.lo, gq.hi, gcx.lo, gcx.hi, gcy.lo, gcy.hi, grx.lo, grx.hi, gry.lo, gry.hi, gxf.lo,
                           gxf.hi, gyf.lo, gyf.hi, gar.lo, gar.hi}));
   OEB_RETURN_IF_VALIDATING();
-  OEB_TRY(ensure_dyn_smem((const void*)fvtp2d_q_kernel<T>, (int)sizeof(FvQSmem<T>)));
-  OEB_TRY(ensure_dyn_smem((const void*)fvtp2d_flux_kernel<T>, (int)sizeof(FvFluxSmem<T>)));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
   cudaStream_t st = (cudaStream_t)stream;
-  fvtp2d_q_kernel<T><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvQSmem<T>), st>>>(
-      gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gq.origin, gcx.origin, gcy.origin, grx.origin, gry.origin,
-      gxf.origin, gyf.origin, gar.origin, p1, p2, d, kKB);
-  OEB_TRY(after_launch());
-  fvtp2d_flux_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvFluxSmem<T>), st>>>(
-      gfx1.origin, gfy1.origin, gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gcx.origin, gcy.origin, gxf.origin,
-      gyf.origin, p1, p2, d, kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<fvtp2d_q_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<T>), st,
+                                     gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gq.origin, gcx.origin,
+                                     gcy.origin, grx.origin, gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d,
+                                     kb));
+  return launch<fvtp2d_flux_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FvFluxSmem<T>), st,
+                                       gfx1.origin, gfy1.origin, gqi.origin, gqj.origin, gfx2.origin, gfy2.origin,
+                                       gcx.origin, gcy.origin, gxf.origin, gyf.origin, p1, p2, d, kb);
 }
 
 // Tangent-linear fvtp2d with respect to q (the PPM flags frozen at q; the Courant numbers,
@@ -337,14 +338,11 @@ oeb_status fvtp2d_tl_entry(const M3* dq_i, const M3* dq_j, const M3* dfx1, const
   OEB_TRY(arr.alloc(dfy1, &ofy1));
   OEB_TRY(arr.alloc(dfy2, &ofy2));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, q->strides[1], q->strides[0]};
-  OEB_TRY(ensure_dyn_smem((const void*)fvtp2d_q_kernel<D>, (int)sizeof(FvQSmem<D>)));
-  OEB_TRY(ensure_dyn_smem((const void*)fvtp2d_flux_kernel<D>, (int)sizeof(FvFluxSmem<D>)));
-  fvtp2d_q_kernel<D><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvQSmem<D>), st>>>(
-      oqi, oqj, ofx2, ofy2, x, cx, cy, rx, ry, xf, yf, ar, D(p1), D(p2), d, kKB);
-  OEB_TRY(after_launch());
-  fvtp2d_flux_kernel<D><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvFluxSmem<D>), st>>>(
-      ofx1, ofy1, oqi, oqj, ofx2, ofy2, cx, cy, xf, yf, D(p1), D(p2), d, kKB);
-  OEB_TRY(after_launch());
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<fvtp2d_q_kernel<D>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<D>), st, oqi,
+                                     oqj, ofx2, ofy2, x, cx, cy, rx, ry, xf, yf, ar, D(p1), D(p2), d, kb));
+  OEB_TRY(launch<fvtp2d_flux_kernel<D>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FvFluxSmem<D>), st, ofx1,
+                                        ofy1, oqi, oqj, ofx2, ofy2, cx, cy, xf, yf, D(p1), D(p2), d, kb));
   OEB_TRY(arr.unpack(dq_i->aligned + dq_i->offset, oqi, *dom, kFvQi, d.sj, d.sk));
   OEB_TRY(arr.unpack(dq_j->aligned + dq_j->offset, oqj, *dom, kFvQj, d.sj, d.sk));
   OEB_TRY(arr.unpack(dfx1->aligned + dfx1->offset, ofx1, *dom, kInterior, d.sj, d.sk));
@@ -463,116 +461,126 @@ __device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L
 
 // Pass 1: q_ib over i in [-3,N+2), j in [0,N) and q_jb over i in [0,N), j in [-3,N+2).
 template <class T>
-__global__ void __launch_bounds__(kThreads) fvtp2d_adj_qij_kernel(
-    T* __restrict__ qib, T* __restrict__ qjb, const T* __restrict__ q_i, const T* __restrict__ q_j,
-    const T* __restrict__ crx, const T* __restrict__ cry, const T* __restrict__ xfx, const T* __restrict__ yfx,
-    const T* __restrict__ fx1b, const T* __restrict__ fy1b, T p1, T p2, Dims d, int AXIS_Y) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
-  const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
-  const int64_t kofs = (int64_t)blockIdx.z * d.sk;
-  if (!AXIS_Y) {
-    // x sweep of fx1 on q_i: outputs i in [-3, nx+2), lines j in [0, ny)
-    const int A = -3 + (int)blockIdx.x * 32, L0 = (int)blockIdx.y * 32;
-    ppm_sweep_adjoint<T, 0>(
-        s, A, L0, p1, p2,
-        [&](int p, int l) { return (p >= -3 && p < nx + 2 && l < ny) ? ld(q_i + kofs + p + l * sj) : T(0); },
-        [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
-        [&](int p, int l) {
-          return (p >= 0 && p < nx && l < ny) ? (T(0.5) * ld(xfx + kofs + p + l * sj)) * ld(fx1b + kofs + p + l * sj)
-                                             : T(0);
-        },
-        [&](int a, int l, T v) {
-          if (a >= -3 && a < nx + 2 && l < ny) qib[kofs + a + l * sj] = v;
-        });
-  } else {
-    // y sweep of fy1 on q_j: outputs j in [-3, ny+2), lines i in [0, nx)
-    const int A = -3 + (int)blockIdx.x * 32, L0 = (int)blockIdx.y * 32;
-    ppm_sweep_adjoint<T, 1>(
-        s, A, L0, p1, p2,
-        [&](int p, int l) { return (p >= -3 && p < ny + 2 && l < nx) ? ld(q_j + kofs + l + p * sj) : T(0); },
-        [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
-        [&](int p, int l) {
-          return (p >= 0 && p < ny && l < nx) ? (T(0.5) * ld(yfx + kofs + l + p * sj)) * ld(fy1b + kofs + l + p * sj)
-                                             : T(0);
-        },
-        [&](int a, int l, T v) {
-          if (a >= -3 && a < ny + 2 && l < nx) qjb[kofs + l + a * sj] = v;
-        });
+struct fvtp2d_adj_qij_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ qib, T* __restrict__ qjb,
+                                             const T* __restrict__ q_i, const T* __restrict__ q_j,
+                                             const T* __restrict__ crx, const T* __restrict__ cry,
+                                             const T* __restrict__ xfx, const T* __restrict__ yfx,
+                                             const T* __restrict__ fx1b, const T* __restrict__ fy1b, T p1, T p2,
+                                             Dims d, int AXIS_Y) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
+    const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
+    const int64_t kofs = (int64_t)blk.z * d.sk;
+    if (!AXIS_Y) {
+      // x sweep of fx1 on q_i: outputs i in [-3, nx+2), lines j in [0, ny)
+      const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * 32;
+      ppm_sweep_adjoint<T, 0>(
+          s, A, L0, p1, p2,
+          [&](int p, int l) { return (p >= -3 && p < nx + 2 && l < ny) ? ld(q_i + kofs + p + l * sj) : T(0); },
+          [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
+          [&](int p, int l) {
+            return (p >= 0 && p < nx && l < ny) ? (T(0.5) * ld(xfx + kofs + p + l * sj)) * ld(fx1b + kofs + p + l * sj)
+                                               : T(0);
+          },
+          [&](int a, int l, T v) {
+            if (a >= -3 && a < nx + 2 && l < ny) qib[kofs + a + l * sj] = v;
+          });
+    } else {
+      // y sweep of fy1 on q_j: outputs j in [-3, ny+2), lines i in [0, nx)
+      const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * 32;
+      ppm_sweep_adjoint<T, 1>(
+          s, A, L0, p1, p2,
+          [&](int p, int l) { return (p >= -3 && p < ny + 2 && l < nx) ? ld(q_j + kofs + l + p * sj) : T(0); },
+          [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
+          [&](int p, int l) {
+            return (p >= 0 && p < ny && l < nx) ? (T(0.5) * ld(yfx + kofs + l + p * sj)) * ld(fy1b + kofs + l + p * sj)
+                                               : T(0);
+          },
+          [&](int a, int l, T v) {
+            if (a >= -3 && a < ny + 2 && l < nx) qjb[kofs + l + a * sj] = v;
+          });
+    }
   }
-}
+};
 
 // Pass 2: fy2b on [-3,N+2) x [0,N+1) and fx2b on [0,N+1) x [-3,N+2).
 template <class T>
-__global__ void __launch_bounds__(kThreads) fvtp2d_adj_f2_kernel(
-    T* __restrict__ fx2b, T* __restrict__ fy2b, const T* __restrict__ qib, const T* __restrict__ qjb,
-    const T* __restrict__ xfx, const T* __restrict__ yfx, const T* __restrict__ ra_x, const T* __restrict__ ra_y,
-    const T* __restrict__ fx1b, const T* __restrict__ fy1b, Dims d, int kb) {
-  const int nx = d.nx, ny = d.ny;
-  const int64_t sj = d.sj;
-  for_box(d, -3, -3, nx + 5, ny + 5, kb, [&](int64_t o, int i, int j) {
-    const bool interior = i >= 0 && i < nx && j >= 0 && j < ny;
-    if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {
-      T g = interior ? (T(0.5) * ld(yfx + o)) * ld(fy1b + o) : T(0);
-      const T a = (j < ny) ? qib[o] / ld(ra_y + o) : T(0);
-      const T b = (j >= 1) ? qib[o - sj] / ld(ra_y + o - sj) : T(0);
-      fy2b[o] = g + ld(yfx + o) * (a - b);
-    }
-    if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {
-      T g = interior ? (T(0.5) * ld(xfx + o)) * ld(fx1b + o) : T(0);
-      const T a = (i < nx) ? qjb[o] / ld(ra_x + o) : T(0);
-      const T b = (i >= 1) ? qjb[o - 1] / ld(ra_x + o - 1) : T(0);
-      fx2b[o] = g + ld(xfx + o) * (a - b);
-    }
-  });
-}
+struct fvtp2d_adj_f2_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ fx2b, T* __restrict__ fy2b,
+                                             const T* __restrict__ qib, const T* __restrict__ qjb,
+                                             const T* __restrict__ xfx, const T* __restrict__ yfx,
+                                             const T* __restrict__ ra_x, const T* __restrict__ ra_y,
+                                             const T* __restrict__ fx1b, const T* __restrict__ fy1b, Dims d, int kb) {
+    const int nx = d.nx, ny = d.ny;
+    const int64_t sj = d.sj;
+    for_box(blk, d, -3, -3, nx + 5, ny + 5, kb, [&](int64_t o, int i, int j) {
+      const bool interior = i >= 0 && i < nx && j >= 0 && j < ny;
+      if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {
+        T g = interior ? (T(0.5) * ld(yfx + o)) * ld(fy1b + o) : T(0);
+        const T a = (j < ny) ? qib[o] / ld(ra_y + o) : T(0);
+        const T b = (j >= 1) ? qib[o - sj] / ld(ra_y + o - sj) : T(0);
+        fy2b[o] = g + ld(yfx + o) * (a - b);
+      }
+      if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {
+        T g = interior ? (T(0.5) * ld(xfx + o)) * ld(fx1b + o) : T(0);
+        const T a = (i < nx) ? qjb[o] / ld(ra_x + o) : T(0);
+        const T b = (i >= 1) ? qjb[o - 1] / ld(ra_x + o - 1) : T(0);
+        fx2b[o] = g + ld(xfx + o) * (a - b);
+      }
+    });
+  }
+};
 
 // Pass 3: qb on [-3,N+3)^2: area terms + PPMx^T(fx2b) (x sweep, writes), then
 // pass 4: + PPMy^T(fy2b) (y sweep, adds).
 template <class T>
-__global__ void __launch_bounds__(kThreads) fvtp2d_adj_q_kernel(
-    T* __restrict__ qb, const T* __restrict__ q, const T* __restrict__ crx, const T* __restrict__ cry,
-    const T* __restrict__ area, const T* __restrict__ ra_x, const T* __restrict__ ra_y, const T* __restrict__ qib,
-    const T* __restrict__ qjb, const T* __restrict__ fx2b, const T* __restrict__ fy2b, T p1, T p2, Dims d,
-    int AXIS_Y) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
-  const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
-  const int64_t kofs = (int64_t)blockIdx.z * d.sk;
-  auto qval = [&](int i, int j) {
-    return (i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3) ? ld(q + kofs + i + j * sj) : T(0);
-  };
-  const int A = -3 + (int)blockIdx.x * 32, L0 = -3 + (int)blockIdx.y * 32;
-  if (!AXIS_Y) {
-    // x sweep of fx2 on q: flux points i in [0, nx+1), lines j in [-3, ny+2)
-    ppm_sweep_adjoint<T, 0>(
-        s, A, L0, p1, p2, [&](int p, int l) { return qval(p, l); },
-        [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
-        [&](int p, int l) {
-          return (p >= 0 && p < nx + 1 && l >= -3 && l < ny + 2) ? fx2b[kofs + p + l * sj] : T(0);
-        },
-        [&](int a, int l, T v) {
-          if (a >= -3 && a < nx + 3 && l >= -3 && l < ny + 3) {
-            const int64_t o = kofs + a + l * sj;
-            T acc = v;
-            if (a >= -3 && a < nx + 2 && l >= 0 && l < ny) acc = acc + (ld(area + o) / ld(ra_y + o)) * qib[o];
-            if (a >= 0 && a < nx && l >= -3 && l < ny + 2) acc = acc + (ld(area + o) / ld(ra_x + o)) * qjb[o];
-            qb[o] = acc;
-          }
-        });
-  } else {
-    // y sweep of fy2 on q: flux points j in [0, ny+1), lines i in [-3, nx+2); adds to qb
-    ppm_sweep_adjoint<T, 1>(
-        s, A, L0, p1, p2, [&](int p, int l) { return qval(l, p); },
-        [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
-        [&](int p, int l) {
-          return (p >= 0 && p < ny + 1 && l >= -3 && l < nx + 2) ? fy2b[kofs + l + p * sj] : T(0);
-        },
-        [&](int a, int l, T v) {
-          if (a >= -3 && a < ny + 3 && l >= -3 && l < nx + 3) qb[kofs + l + a * sj] = qb[kofs + l + a * sj] + v;
-        });
+struct fvtp2d_adj_q_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ qb, const T* __restrict__ q,
+                                             const T* __restrict__ crx, const T* __restrict__ cry,
+                                             const T* __restrict__ area, const T* __restrict__ ra_x,
+                                             const T* __restrict__ ra_y, const T* __restrict__ qib,
+                                             const T* __restrict__ qjb, const T* __restrict__ fx2b,
+                                             const T* __restrict__ fy2b, T p1, T p2, Dims d, int AXIS_Y) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
+    const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
+    const int64_t kofs = (int64_t)blk.z * d.sk;
+    auto qval = [&](int i, int j) {
+      return (i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3) ? ld(q + kofs + i + j * sj) : T(0);
+    };
+    const int A = -3 + (int)blk.x * 32, L0 = -3 + (int)blk.y * 32;
+    if (!AXIS_Y) {
+      // x sweep of fx2 on q: flux points i in [0, nx+1), lines j in [-3, ny+2)
+      ppm_sweep_adjoint<T, 0>(
+          s, A, L0, p1, p2, [&](int p, int l) { return qval(p, l); },
+          [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
+          [&](int p, int l) {
+            return (p >= 0 && p < nx + 1 && l >= -3 && l < ny + 2) ? fx2b[kofs + p + l * sj] : T(0);
+          },
+          [&](int a, int l, T v) {
+            if (a >= -3 && a < nx + 3 && l >= -3 && l < ny + 3) {
+              const int64_t o = kofs + a + l * sj;
+              T acc = v;
+              if (a >= -3 && a < nx + 2 && l >= 0 && l < ny) acc = acc + (ld(area + o) / ld(ra_y + o)) * qib[o];
+              if (a >= 0 && a < nx && l >= -3 && l < ny + 2) acc = acc + (ld(area + o) / ld(ra_x + o)) * qjb[o];
+              qb[o] = acc;
+            }
+          });
+    } else {
+      // y sweep of fy2 on q: flux points j in [0, ny+1), lines i in [-3, nx+2); adds to qb
+      ppm_sweep_adjoint<T, 1>(
+          s, A, L0, p1, p2, [&](int p, int l) { return qval(l, p); },
+          [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
+          [&](int p, int l) {
+            return (p >= 0 && p < ny + 1 && l >= -3 && l < nx + 2) ? fy2b[kofs + l + p * sj] : T(0);
+          },
+          [&](int a, int l, T v) {
+            if (a >= -3 && a < ny + 3 && l >= -3 && l < nx + 3) qb[kofs + l + a * sj] = qb[kofs + l + a * sj] + v;
+          });
+    }
   }
-}
+};
 
 template <class T, class M3>
 oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* cry, const M3* ra_x, const M3* ra_y,
@@ -597,8 +605,6 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
                                             gg1.lo, gg1.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
-  cudaMemPool_t pool;
-  OEB_TRY(device_pool(&pool));
   // scratch in q's layout: q_i, q_j, fx2, fy2 (forward recompute), q_ib, q_jb, fx2b, fy2b
   const T* start = (q->allocated && q->allocated <= q->aligned) ? q->allocated : q->aligned;
   const int64_t last = (q->sizes[0] - 1) * q->strides[0] + (q->sizes[1] - 1) * q->strides[1] +
@@ -606,53 +612,34 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
   const int64_t n = (int64_t)(q->aligned - start) + last + 1;
   const int64_t org = (int64_t)(q->aligned - start) + q->offset;
   void* buf = nullptr;
-  cudaError_t e = cudaMallocFromPoolAsync(&buf, (size_t)n * 8 * sizeof(T), pool, st);
-  if (e != cudaSuccess) {
-    cuda_fail(e);
-    return OEB_ERR_ALLOC;
-  }
+  OEB_TRY(scratch_alloc(&buf, (size_t)n * 8 * sizeof(T), st));
   T* base = static_cast<T*>(buf);
   T *sqi = base + org, *sqj = base + n + org, *sfx2 = base + 2 * n + org, *sfy2 = base + 3 * n + org,
     *qib = base + 4 * n + org, *qjb = base + 5 * n + org, *fx2b = base + 6 * n + org, *fy2b = base + 7 * n + org;
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
-  oeb_status stt = ensure_dyn_smem((const void*)fvtp2d_q_kernel<T>, (int)sizeof(FvQSmem<T>));
-  if (stt == OEB_OK) stt = ensure_dyn_smem((const void*)fvtp2d_adj_qij_kernel<T>, (int)sizeof(PpmAdjSmem<T>));
-  if (stt == OEB_OK) stt = ensure_dyn_smem((const void*)fvtp2d_adj_q_kernel<T>, (int)sizeof(PpmAdjSmem<T>));
-  if (stt == OEB_OK) {
-    fvtp2d_q_kernel<T><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), sizeof(FvQSmem<T>), st>>>(
-        sqi, sqj, sfx2, sfy2, gq.origin, gcx.origin, gcy.origin, grx.origin, gry.origin, gxf.origin, gyf.origin,
-        gar.origin, p1, p2, d, kKB);
-    stt = after_launch();
-  }
+  const int kb = tuned_kb(kKB);
   const size_t ps = sizeof(PpmAdjSmem<T>);
-  if (stt == OEB_OK) {
-    fvtp2d_adj_qij_kernel<T><<<dim3((d.nx + 5 + 31) / 32, (d.ny + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
-        qib, qjb, sqi, sqj, gcx.origin, gcy.origin, gxf.origin, gyf.origin, gf1.origin, gg1.origin, p1, p2, d, 0);
-    stt = after_launch();
+  oeb_status stt = launch<fvtp2d_q_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<T>), st,
+                                              sqi, sqj, sfx2, sfy2, gq.origin, gcx.origin, gcy.origin, grx.origin,
+                                              gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d, kb);
+  // the x and y sweeps of the two PPM adjoints (axis flag 0 / 1)
+  for (int axis = 0; axis < 2 && stt == OEB_OK; ++axis) {
+    const int a = axis ? d.ny : d.nx, l = axis ? d.nx : d.ny;
+    stt = launch<fvtp2d_adj_qij_kernel<T>>(dim3((a + 5 + 31) / 32, (l + 31) / 32, d.nz), ps, st, qib, qjb, sqi, sqj,
+                                           gcx.origin, gcy.origin, gxf.origin, gyf.origin, gf1.origin, gg1.origin, p1,
+                                           p2, d, axis);
   }
-  if (stt == OEB_OK) {
-    fvtp2d_adj_qij_kernel<T><<<dim3((d.ny + 5 + 31) / 32, (d.nx + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
-        qib, qjb, sqi, sqj, gcx.origin, gcy.origin, gxf.origin, gyf.origin, gf1.origin, gg1.origin, p1, p2, d, 1);
-    stt = after_launch();
+  if (stt == OEB_OK)
+    stt = launch<fvtp2d_adj_f2_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), 0, st, fx2b, fy2b, qib,
+                                          qjb, gxf.origin, gyf.origin, grx.origin, gry.origin, gf1.origin, gg1.origin, d,
+                                          kb);
+  for (int axis = 0; axis < 2 && stt == OEB_OK; ++axis) {
+    const int a = axis ? d.ny : d.nx, l = axis ? d.nx : d.ny;
+    stt = launch<fvtp2d_adj_q_kernel<T>>(dim3((a + 6 + 31) / 32, (l + 6 + 31) / 32, d.nz), ps, st, gqb.origin,
+                                         gq.origin, gcx.origin, gcy.origin, gar.origin, grx.origin, gry.origin, qib, qjb,
+                                         fx2b, fy2b, p1, p2, d, axis);
   }
-  if (stt == OEB_OK) {
-    fvtp2d_adj_f2_kernel<T><<<tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
-        fx2b, fy2b, qib, qjb, gxf.origin, gyf.origin, grx.origin, gry.origin, gf1.origin, gg1.origin, d, kKB);
-    stt = after_launch();
-  }
-  if (stt == OEB_OK) {
-    fvtp2d_adj_q_kernel<T><<<dim3((d.nx + 6 + 31) / 32, (d.ny + 6 + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
-        gqb.origin, gq.origin, gcx.origin, gcy.origin, gar.origin, grx.origin, gry.origin, qib, qjb, fx2b, fy2b, p1,
-        p2, d, 0);
-    stt = after_launch();
-  }
-  if (stt == OEB_OK) {
-    fvtp2d_adj_q_kernel<T><<<dim3((d.ny + 6 + 31) / 32, (d.nx + 6 + 31) / 32, d.nz), dim3(kTX, kTY), ps, st>>>(
-        gqb.origin, gq.origin, gcx.origin, gcy.origin, gar.origin, grx.origin, gry.origin, qib, qjb, fx2b, fy2b, p1,
-        p2, d, 1);
-    stt = after_launch();
-  }
-  cudaFreeAsync(buf, st);
+  scratch_free(buf, st);
   return stt;
 }
 

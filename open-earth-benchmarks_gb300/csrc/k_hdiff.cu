@@ -44,64 +44,65 @@ struct HdiffsaSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) hdiffsa_kernel(T* __restrict__ out, const T* __restrict__ in,
-                                                           const T* __restrict__ mask, const T* __restrict__ crlato,
-                                                           const T* __restrict__ crlatu, int64_t s1d, Dims d,
-                                                           int kb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  HdiffsaSmem<T>& s = *reinterpret_cast<HdiffsaSmem<T>*>(smem_raw);
-  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
-  const int sj = (int)d.sj;
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-  if (tid < 34) {
-    const int j = j0 - 1 + tid;
-    const bool ok = j >= -1 && j < d.ny + 1;
-    s.crlato[tid] = ok ? ld(crlato + (int64_t)j * s1d) : T(0);
-    s.crlatu[tid] = ok ? ld(crlatu + (int64_t)j * s1d) : T(0);
+struct hdiffsa_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ out, const T* __restrict__ in,
+                                             const T* __restrict__ mask, const T* __restrict__ crlato,
+                                             const T* __restrict__ crlatu, int64_t s1d, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HdiffsaSmem<T>& s = *reinterpret_cast<HdiffsaSmem<T>*>(smem_raw);
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int sj = (int)d.sj;
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    if (tid < 34) {
+      const int j = j0 - 1 + tid;
+      const bool ok = j >= -1 && j < d.ny + 1;
+      s.crlato[tid] = ok ? ld(crlato + (int64_t)j * s1d) : T(0);
+      s.crlatu[tid] = ok ? ld(crlatu + (int64_t)j * s1d) : T(0);
+    }
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      const T* pin = in + kofs;
+      for_region<36, 36>([&](int a, int b) {
+        const int i = i0 - 2 + a, j = j0 - 2 + b;
+        const bool ok = i >= -2 && i < d.nx + 2 && j >= -2 && j < d.ny + 2;
+        s.in[b][a] = ok ? ld(pin + i + j * sj) : T(0);
+      });
+      __syncthreads();
+      for_region<34, 35>([&](int a, int b) { s.dy[b][a] = s.in[b + 1][a + 1] - s.in[b][a + 1]; });
+      __syncthreads();
+      // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
+      for_region<34, 34>([&](int a, int b) {
+        const T c = s.in[b + 1][a + 1];
+        s.lap[b][a] = (((s.in[b + 1][a] + s.in[b + 1][a + 2]) - T(2.0) * c) + s.crlato[b] * s.dy[b + 1][a]) +
+                      s.crlatu[b] * (-s.dy[b][a]);
+      });
+      __syncthreads();
+      // hdiffsa.h:106-113: limited fluxes
+      for_region<33, 32>([&](int a, int b) {
+        T f = s.lap[b + 1][a + 1] - s.lap[b + 1][a];
+        if (Prec<T>::prod_gt0(f, s.in[b + 2][a + 2] - s.in[b + 2][a + 1])) f = 0;
+        s.flx[b][a] = f;
+      });
+      for_region<32, 33>([&](int a, int b) {
+        T f = s.crlato[b] * (s.lap[b + 1][a + 1] - s.lap[b][a + 1]);
+        if (Prec<T>::prod_gt0(f, s.dy[b + 1][a + 1])) f = 0;
+        s.fly[b][a] = f;
+      });
+      __syncthreads();
+      // hdiffsa.h:118-119
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < d.nx && j < d.ny) {
+          const int64_t o = kofs + i + j * sj;
+          out[o] = s.in[b + 2][a + 2] + (((s.flx[b][a] - s.flx[b][a + 1]) + s.fly[b][a]) - s.fly[b + 1][a]) * ld(mask + o);
+        }
+      });
+      __syncthreads();
+    }
   }
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
-#pragma unroll 1
-  for (int k = k0; k < k1; ++k) {
-    const int64_t kofs = (int64_t)k * d.sk;
-    const T* pin = in + kofs;
-    for_region<36, 36>([&](int a, int b) {
-      const int i = i0 - 2 + a, j = j0 - 2 + b;
-      const bool ok = i >= -2 && i < d.nx + 2 && j >= -2 && j < d.ny + 2;
-      s.in[b][a] = ok ? ld(pin + i + j * sj) : T(0);
-    });
-    __syncthreads();
-    for_region<34, 35>([&](int a, int b) { s.dy[b][a] = s.in[b + 1][a + 1] - s.in[b][a + 1]; });
-    __syncthreads();
-    // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
-    for_region<34, 34>([&](int a, int b) {
-      const T c = s.in[b + 1][a + 1];
-      s.lap[b][a] = (((s.in[b + 1][a] + s.in[b + 1][a + 2]) - T(2.0) * c) + s.crlato[b] * s.dy[b + 1][a]) +
-                    s.crlatu[b] * (-s.dy[b][a]);
-    });
-    __syncthreads();
-    // hdiffsa.h:106-113: limited fluxes
-    for_region<33, 32>([&](int a, int b) {
-      T f = s.lap[b + 1][a + 1] - s.lap[b + 1][a];
-      if (Prec<T>::prod_gt0(f, s.in[b + 2][a + 2] - s.in[b + 2][a + 1])) f = 0;
-      s.flx[b][a] = f;
-    });
-    for_region<32, 33>([&](int a, int b) {
-      T f = s.crlato[b] * (s.lap[b + 1][a + 1] - s.lap[b][a + 1]);
-      if (Prec<T>::prod_gt0(f, s.dy[b + 1][a + 1])) f = 0;
-      s.fly[b][a] = f;
-    });
-    __syncthreads();
-    // hdiffsa.h:118-119
-    for_region<32, 32>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      if (i < d.nx && j < d.ny) {
-        const int64_t o = kofs + i + j * sj;
-        out[o] = s.in[b + 2][a + 2] + (((s.flx[b][a] - s.flx[b][a + 1]) + s.fly[b][a]) - s.fly[b + 1][a]) * ld(mask + o);
-      }
-    });
-    __syncthreads();
-  }
-}
+};
 
 // ============================== hdiffsmag =========================================
 // Shared layout (per k-level), tile origin (i0, j0):
@@ -127,95 +128,97 @@ struct HdiffsmagSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) hdiffsmag_kernel(
-    T* __restrict__ uout, T* __restrict__ vout, const T* __restrict__ uin, const T* __restrict__ vin,
-    const T* __restrict__ mask, const T* __restrict__ crlavo, const T* __restrict__ crlavu,
-    const T* __restrict__ crlato, const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d, T eddlat,
-    T eddlon, T tau_smag, T weight_smag, Dims d, int kb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  HdiffsmagSmem<T>& s = *reinterpret_cast<HdiffsmagSmem<T>*>(smem_raw);
-  const int i0 = blockIdx.x * kT, j0 = blockIdx.y * kT;
-  const int sj = (int)d.sj;
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-  constexpr T rr = earth_radius_recip<T>();
-  if (tid < 34) {
-    const int j = j0 - 1 + tid;
-    s.acrlat0[tid] = (j >= -1 && j < d.ny + 1) ? ld(acrlat0 + (int64_t)j * s1d) : T(0);
-  } else if (tid >= 64 && tid < 96) {
-    const int b = tid - 64, j = j0 + b;
-    const bool ok = j < d.ny;
-    const int64_t jo = (int64_t)j * s1d;
-    s.crlato[b] = ok ? ld(crlato + jo) : T(0);
-    s.crlatu[b] = ok ? ld(crlatu + jo) : T(0);
-    s.crlavo[b] = ok ? ld(crlavo + jo) : T(0);
-    s.crlavu[b] = ok ? ld(crlavu + jo) : T(0);
-  }
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
-#pragma unroll 1
-  for (int k = k0; k < k1; ++k) {
-    const int64_t kofs = (int64_t)k * d.sk;
-    for_region<34, 34>([&](int a, int b) {
-      const int i = i0 - 1 + a, j = j0 - 1 + b;
-      const bool ok = i >= -1 && i < d.nx + 1 && j >= -1 && j < d.ny + 1;
-      const int64_t o = kofs + i + j * sj;
-      s.u[b][a] = ok ? ld(uin + o) : T(0);
-      s.v[b][a] = ok ? ld(vin + o) : T(0);
-    });
-    __syncthreads();
-    for_region<33, 33>([&](int a, int b) {
-      s.dxu[b][a] = s.u[b + 1][a + 1] - s.u[b + 1][a];
-      s.dyv[b][a] = s.v[b + 1][a + 1] - s.v[b][a + 1];
-      s.dyu[b][a] = s.u[b + 1][a] - s.u[b][a];
-      s.dxv[b][a] = s.v[b][a + 1] - s.v[b][a];
-    });
-    __syncthreads();
-    // hdiffsmag.h:213 T_s = (v(j-1)-v) eddlat R^-1 - (u(i-1)-u) acrlat0(j) eddlon
-    //              :221 S_uv = (u(j+1)-u) eddlat R^-1 + (v(i+1)-v) acrlat0(j) eddlon
-    for_region<33, 33>([&](int a, int b) {
-      const T ts = ((-s.dyv[b][a]) * eddlat) * rr - ((-s.dxu[b][a]) * s.acrlat0[b + 1]) * eddlon;
-      s.tsq[b][a] = ts * ts;
-      const T su = (s.dyu[b][a] * eddlat) * rr + (s.dxv[b][a] * s.acrlat0[b]) * eddlon;
-      s.ssq[b][a] = su * su;
-    });
-    __syncthreads();
-    for_region<32, 32>([&](int a, int b) {
-      const int i = i0 + a, j = j0 + b;
-      if (i < d.nx && j < d.ny) {
+struct hdiffsmag_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
+                                             const T* __restrict__ uin, const T* __restrict__ vin,
+                                             const T* __restrict__ mask, const T* __restrict__ crlavo,
+                                             const T* __restrict__ crlavu, const T* __restrict__ crlato,
+                                             const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d,
+                                             T eddlat, T eddlon, T tau_smag, T weight_smag, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HdiffsmagSmem<T>& s = *reinterpret_cast<HdiffsmagSmem<T>*>(smem_raw);
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int sj = (int)d.sj;
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    constexpr T rr = earth_radius_recip<T>();
+    if (tid < 34) {
+      const int j = j0 - 1 + tid;
+      s.acrlat0[tid] = (j >= -1 && j < d.ny + 1) ? ld(acrlat0 + (int64_t)j * s1d) : T(0);
+    } else if (tid >= 64 && tid < 96) {
+      const int b = tid - 64, j = j0 + b;
+      const bool ok = j < d.ny;
+      const int64_t jo = (int64_t)j * s1d;
+      s.crlato[b] = ok ? ld(crlato + jo) : T(0);
+      s.crlatu[b] = ok ? ld(crlatu + jo) : T(0);
+      s.crlavo[b] = ok ? ld(crlavo + jo) : T(0);
+      s.crlavu[b] = ok ? ld(crlavu + jo) : T(0);
+    }
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region<34, 34>([&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        const bool ok = i >= -1 && i < d.nx + 1 && j >= -1 && j < d.ny + 1;
         const int64_t o = kofs + i + j * sj;
-        const T hdweight = weight_smag * ld(mask + o);
-        // hdiffsmag.h:233-244
-        T smag_u = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b][a + 1] + s.tsq[b][a]) +
-                                             T(0.5) * (s.ssq[b][a + 1] + s.ssq[b + 1][a + 1])) -
-                   hdweight;
-        smag_u = clamp_smag(smag_u);
-        const T uc = s.u[b + 1][a + 1];
-        // u(i+1) + u(i-1) - 2u + crlato (u(j+1) - u) + crlatu (u(j-1) - u)
-        Acc<T> lu(s.u[b + 1][a + 2]);
-        lu.add(s.u[b + 1][a]);
-        lu.add(-(T(2.0) * uc));
-        lu.add_prod(s.crlato[b], s.dyu[b + 1][a + 1]);
-        lu.add_prod(s.crlatu[b], -s.dyu[b][a + 1]);
-        uout[o] = uc + smag_u * lu.get();
-        // hdiffsmag.h:248-259
-        T smag_v = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b + 1][a] + s.tsq[b][a]) +
-                                             T(0.5) * (s.ssq[b + 1][a] + s.ssq[b + 1][a + 1])) -
-                   hdweight;
-        smag_v = clamp_smag(smag_v);
-        const T vc = s.v[b + 1][a + 1];
-        Acc<T> lv(s.v[b + 1][a + 2]);
-        lv.add(s.v[b + 1][a]);
-        lv.add(-(T(2.0) * vc));
-        lv.add_prod(s.crlavo[b], s.dyv[b + 1][a]);
-        lv.add_prod(s.crlavu[b], -s.dyv[b][a]);
-        vout[o] = vc + smag_v * lv.get();
-      }
-    });
-    __syncthreads();
+        s.u[b][a] = ok ? ld(uin + o) : T(0);
+        s.v[b][a] = ok ? ld(vin + o) : T(0);
+      });
+      __syncthreads();
+      for_region<33, 33>([&](int a, int b) {
+        s.dxu[b][a] = s.u[b + 1][a + 1] - s.u[b + 1][a];
+        s.dyv[b][a] = s.v[b + 1][a + 1] - s.v[b][a + 1];
+        s.dyu[b][a] = s.u[b + 1][a] - s.u[b][a];
+        s.dxv[b][a] = s.v[b][a + 1] - s.v[b][a];
+      });
+      __syncthreads();
+      // hdiffsmag.h:213 T_s = (v(j-1)-v) eddlat R^-1 - (u(i-1)-u) acrlat0(j) eddlon
+      //              :221 S_uv = (u(j+1)-u) eddlat R^-1 + (v(i+1)-v) acrlat0(j) eddlon
+      for_region<33, 33>([&](int a, int b) {
+        const T ts = ((-s.dyv[b][a]) * eddlat) * rr - ((-s.dxu[b][a]) * s.acrlat0[b + 1]) * eddlon;
+        s.tsq[b][a] = ts * ts;
+        const T su = (s.dyu[b][a] * eddlat) * rr + (s.dxv[b][a] * s.acrlat0[b]) * eddlon;
+        s.ssq[b][a] = su * su;
+      });
+      __syncthreads();
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < d.nx && j < d.ny) {
+          const int64_t o = kofs + i + j * sj;
+          const T hdweight = weight_smag * ld(mask + o);
+          // hdiffsmag.h:233-244
+          T smag_u = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b][a + 1] + s.tsq[b][a]) +
+                                               T(0.5) * (s.ssq[b][a + 1] + s.ssq[b + 1][a + 1])) -
+                     hdweight;
+          smag_u = clamp_smag(smag_u);
+          const T uc = s.u[b + 1][a + 1];
+          // u(i+1) + u(i-1) - 2u + crlato (u(j+1) - u) + crlatu (u(j-1) - u)
+          Acc<T> lu(s.u[b + 1][a + 2]);
+          lu.add(s.u[b + 1][a]);
+          lu.add(-(T(2.0) * uc));
+          lu.add_prod(s.crlato[b], s.dyu[b + 1][a + 1]);
+          lu.add_prod(s.crlatu[b], -s.dyu[b][a + 1]);
+          uout[o] = uc + smag_u * lu.get();
+          // hdiffsmag.h:248-259
+          T smag_v = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b + 1][a] + s.tsq[b][a]) +
+                                               T(0.5) * (s.ssq[b + 1][a] + s.ssq[b + 1][a + 1])) -
+                     hdweight;
+          smag_v = clamp_smag(smag_v);
+          const T vc = s.v[b + 1][a + 1];
+          Acc<T> lv(s.v[b + 1][a + 2]);
+          lv.add(s.v[b + 1][a]);
+          lv.add(-(T(2.0) * vc));
+          lv.add_prod(s.crlavo[b], s.dyv[b + 1][a]);
+          lv.add_prod(s.crlavu[b], -s.dyv[b][a]);
+          vout[o] = vc + smag_v * lv.get();
+        }
+      });
+      __syncthreads();
+    }
   }
-}
+};
 
 constexpr int kKB = 4;
-
 
 template <class T, class M3, class M1>
 oeb_status hdiffsa_entry(const M3* out, const M3* in, const M3* mask, const M1* crlato, const M1* crlatu,
@@ -232,12 +235,10 @@ oeb_status hdiffsa_entry(const M3* out, const M3* in, const M3* mask, const M1* 
   OEB_TRY(check_same_strides<T>({&gout, &gin, &gmask}));
   OEB_TRY(check_no_alias({gout.lo, gout.hi}, {gin.lo, gin.hi, gmask.lo, gmask.hi, lo.lo, lo.hi, lu.lo, lu.hi}));
   OEB_RETURN_IF_VALIDATING();
-  const size_t smem = sizeof(HdiffsaSmem<T>);
-  OEB_TRY(ensure_dyn_smem((const void*)hdiffsa_kernel<T>, (int)smem));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gin.sj, gin.sk};
-  hdiffsa_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), smem, (cudaStream_t)stream>>>(
-      gout.origin, gin.origin, gmask.origin, lo.origin, lu.origin, lo.s, d, kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<hdiffsa_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(HdiffsaSmem<T>), (cudaStream_t)stream,
+                                   gout.origin, gin.origin, gmask.origin, lo.origin, lu.origin, lo.s, d, kb);
 }
 
 template <class T, class M3, class M1>
@@ -263,13 +264,12 @@ oeb_status hdiffsmag_entry(const M3* uout, const M3* vout, const M3* uin, const 
                          {gui.lo, gui.hi, gvi.lo, gvi.hi, gm.lo, gm.hi, lvo.lo, lvo.hi, lvu.lo, lvu.hi, lto.lo,
                           lto.hi, ltu.lo, ltu.hi, la0.lo, la0.hi}));
   OEB_RETURN_IF_VALIDATING();
-  const size_t smem = sizeof(HdiffsmagSmem<T>);
-  OEB_TRY(ensure_dyn_smem((const void*)hdiffsmag_kernel<T>, (int)smem));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
-  hdiffsmag_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), smem, (cudaStream_t)stream>>>(
-      gu.origin, gv.origin, gui.origin, gvi.origin, gm.origin, lvo.origin, lvu.origin, lto.origin, ltu.origin,
-      la0.origin, lvo.s, eddlat, eddlon, tau_smag, weight_smag, d, kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<hdiffsmag_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(HdiffsmagSmem<T>),
+                                     (cudaStream_t)stream, gu.origin, gv.origin, gui.origin, gvi.origin, gm.origin,
+                                     lvo.origin, lvu.origin, lto.origin, ltu.origin, la0.origin, lvo.s, eddlat, eddlon,
+                                     tau_smag, weight_smag, d, kb);
 }
 
 // Tangent-linear hdiffsmag: d(uout, vout) = J(uin, vin) d(uin, vin), the kernel on Dual<T>.
@@ -300,12 +300,10 @@ oeb_status hdiffsmag_tl_entry(const M3* duout, const M3* dvout, const M3* uin, c
   OEB_TRY(arr.alloc(duout, &ou));
   OEB_TRY(arr.alloc(dvout, &ov));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
-  const size_t smem = sizeof(HdiffsmagSmem<D>);
-  OEB_TRY(ensure_dyn_smem((const void*)hdiffsmag_kernel<D>, (int)smem));
-  hdiffsmag_kernel<D><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), smem, (cudaStream_t)stream>>>(
-      ou, ov, u, v, m, l0, l1, l2, l3, l4, crlavo->strides[0], D(eddlat), D(eddlon), D(tau_smag), D(weight_smag), d,
-      kKB);
-  OEB_TRY(after_launch());
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<hdiffsmag_kernel<D>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(HdiffsmagSmem<D>),
+                                      (cudaStream_t)stream, ou, ov, u, v, m, l0, l1, l2, l3, l4, crlavo->strides[0],
+                                      D(eddlat), D(eddlon), D(tau_smag), D(weight_smag), d, kb));
   OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
   return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
 }
@@ -339,113 +337,121 @@ __device__ __forceinline__ T smag_S(const T* __restrict__ u, const T* __restrict
 }
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) hdiffsmag_adj_terms_kernel(
-    SmagTerms<T> tm, const T* __restrict__ uin, const T* __restrict__ vin, const T* __restrict__ mask,
-    const T* __restrict__ crlavo, const T* __restrict__ crlavu, const T* __restrict__ crlato,
-    const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d, const T* __restrict__ uoutb,
-    const T* __restrict__ voutb, T eddlat, T eddlon, T tau_smag, T weight_smag, Dims d, int kb) {
-  constexpr T rr = earth_radius_recip<T>();
-  const T c1 = eddlat * rr;
-  const int64_t sj = d.sj;
-  for_box(d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
-    const T c2m = ld(acrlat0 + (int64_t)(j - 1) * s1d) * eddlon, c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon,
-            c2p = ld(acrlat0 + (int64_t)(j + 1) * s1d) * eddlon;
-    const T t0 = smag_T(uin, vin, o, sj, c1, c2), ti = smag_T(uin, vin, o + 1, sj, c1, c2),
-            tj = smag_T(uin, vin, o + sj, sj, c1, c2p);
-    const T s0 = smag_S(uin, vin, o, sj, c1, c2), sjm = smag_S(uin, vin, o - sj, sj, c1, c2m),
-            sim = smag_S(uin, vin, o - 1, sj, c1, c2);
-    const T hdw = weight_smag * ld(mask + o);
-    const T xu = T(0.5) * (ti * ti + t0 * t0) + T(0.5) * (sjm * sjm + s0 * s0);
-    const T xv = T(0.5) * (tj * tj + t0 * t0) + T(0.5) * (sim * sim + s0 * s0);
-    const T ru = Prec<T>::sqrt_(xu), rv = Prec<T>::sqrt_(xv);
-    const T smu = tau_smag * ru - hdw, smv = tau_smag * rv - hdw;
-    const T su = clamp_smag(smu), sv = clamp_smag(smv);
-    const int64_t jo = (int64_t)j * s1d;
-    const T u0 = ld(uin + o), v0 = ld(vin + o);
-    const T lapu = (ld(uin + o + 1) + ld(uin + o - 1) - T(2) * u0) + ld(crlato + jo) * (ld(uin + o + sj) - u0) +
-                   ld(crlatu + jo) * (ld(uin + o - sj) - u0);
-    const T lapv = (ld(vin + o + 1) + ld(vin + o - 1) - T(2) * v0) + ld(crlavo + jo) * (ld(vin + o + sj) - v0) +
-                   ld(crlavu + jo) * (ld(vin + o - sj) - v0);
-    const T yu = ld(uoutb + o), yv = ld(voutb + o);
-    tm.lu[o] = su * yu;
-    tm.lv[o] = sv * yv;
-    tm.xu[o] = (smu > T(0) && smu < T(0.5)) ? (lapu * yu) * (tau_smag / (T(2) * ru)) : T(0);
-    tm.xv[o] = (smv > T(0) && smv < T(0.5)) ? (lapv * yv) * (tau_smag / (T(2) * rv)) : T(0);
-  });
-}
+struct hdiffsmag_adj_terms_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, SmagTerms<T> tm, const T* __restrict__ uin,
+                                             const T* __restrict__ vin, const T* __restrict__ mask,
+                                             const T* __restrict__ crlavo, const T* __restrict__ crlavu,
+                                             const T* __restrict__ crlato, const T* __restrict__ crlatu,
+                                             const T* __restrict__ acrlat0, int64_t s1d, const T* __restrict__ uoutb,
+                                             const T* __restrict__ voutb, T eddlat, T eddlon, T tau_smag,
+                                             T weight_smag, Dims d, int kb) {
+    constexpr T rr = earth_radius_recip<T>();
+    const T c1 = eddlat * rr;
+    const int64_t sj = d.sj;
+    for_box(blk, d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
+      const T c2m = ld(acrlat0 + (int64_t)(j - 1) * s1d) * eddlon, c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon,
+              c2p = ld(acrlat0 + (int64_t)(j + 1) * s1d) * eddlon;
+      const T t0 = smag_T(uin, vin, o, sj, c1, c2), ti = smag_T(uin, vin, o + 1, sj, c1, c2),
+              tj = smag_T(uin, vin, o + sj, sj, c1, c2p);
+      const T s0 = smag_S(uin, vin, o, sj, c1, c2), sjm = smag_S(uin, vin, o - sj, sj, c1, c2m),
+              sim = smag_S(uin, vin, o - 1, sj, c1, c2);
+      const T hdw = weight_smag * ld(mask + o);
+      const T xu = T(0.5) * (ti * ti + t0 * t0) + T(0.5) * (sjm * sjm + s0 * s0);
+      const T xv = T(0.5) * (tj * tj + t0 * t0) + T(0.5) * (sim * sim + s0 * s0);
+      const T ru = Prec<T>::sqrt_(xu), rv = Prec<T>::sqrt_(xv);
+      const T smu = tau_smag * ru - hdw, smv = tau_smag * rv - hdw;
+      const T su = clamp_smag(smu), sv = clamp_smag(smv);
+      const int64_t jo = (int64_t)j * s1d;
+      const T u0 = ld(uin + o), v0 = ld(vin + o);
+      const T lapu = (ld(uin + o + 1) + ld(uin + o - 1) - T(2) * u0) + ld(crlato + jo) * (ld(uin + o + sj) - u0) +
+                     ld(crlatu + jo) * (ld(uin + o - sj) - u0);
+      const T lapv = (ld(vin + o + 1) + ld(vin + o - 1) - T(2) * v0) + ld(crlavo + jo) * (ld(vin + o + sj) - v0) +
+                     ld(crlavu + jo) * (ld(vin + o - sj) - v0);
+      const T yu = ld(uoutb + o), yv = ld(voutb + o);
+      tm.lu[o] = su * yu;
+      tm.lv[o] = sv * yv;
+      tm.xu[o] = (smu > T(0) && smu < T(0.5)) ? (lapu * yu) * (tau_smag / (T(2) * ru)) : T(0);
+      tm.xv[o] = (smv > T(0) && smv < T(0.5)) ? (lapv * yv) * (tau_smag / (T(2) * rv)) : T(0);
+    });
+  }
+};
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) hdiffsmag_adj_ts_kernel(SmagTerms<T> tm, const T* __restrict__ uin,
-                                                                    const T* __restrict__ vin,
-                                                                    const T* __restrict__ acrlat0, int64_t s1d,
-                                                                    T eddlat, T eddlon, Dims d, int kb) {
-  constexpr T rr = earth_radius_recip<T>();
-  const T c1 = eddlat * rr;
-  const int64_t sj = d.sj;
-  auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
-  for_box(d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int i, int j) {
-    const T c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon;
-    if (i >= 0 && i <= d.nx && j >= 0 && j <= d.ny) {
-      T w = T(0);
-      if (in(i - 1, j)) w = w + tm.xu[o - 1];
-      if (in(i, j)) w = w + tm.xu[o] + tm.xv[o];
-      if (in(i, j - 1)) w = w + tm.xv[o - sj];
-      tm.tb[o] = (w == T(0)) ? T(0) : smag_T(uin, vin, o, sj, c1, c2) * w;
-    }
-    if (i >= -1 && i < d.nx && j >= -1 && j < d.ny) {
-      T w = T(0);
-      if (in(i, j + 1)) w = w + tm.xu[o + sj];
-      if (in(i, j)) w = w + tm.xu[o] + tm.xv[o];
-      if (in(i + 1, j)) w = w + tm.xv[o + 1];
-      tm.sb[o] = (w == T(0)) ? T(0) : smag_S(uin, vin, o, sj, c1, c2) * w;
-    }
-  });
-}
+struct hdiffsmag_adj_ts_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, SmagTerms<T> tm, const T* __restrict__ uin,
+                                             const T* __restrict__ vin, const T* __restrict__ acrlat0, int64_t s1d,
+                                             T eddlat, T eddlon, Dims d, int kb) {
+    constexpr T rr = earth_radius_recip<T>();
+    const T c1 = eddlat * rr;
+    const int64_t sj = d.sj;
+    auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+    for_box(blk, d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int i, int j) {
+      const T c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon;
+      if (i >= 0 && i <= d.nx && j >= 0 && j <= d.ny) {
+        T w = T(0);
+        if (in(i - 1, j)) w = w + tm.xu[o - 1];
+        if (in(i, j)) w = w + tm.xu[o] + tm.xv[o];
+        if (in(i, j - 1)) w = w + tm.xv[o - sj];
+        tm.tb[o] = (w == T(0)) ? T(0) : smag_T(uin, vin, o, sj, c1, c2) * w;
+      }
+      if (i >= -1 && i < d.nx && j >= -1 && j < d.ny) {
+        T w = T(0);
+        if (in(i, j + 1)) w = w + tm.xu[o + sj];
+        if (in(i, j)) w = w + tm.xu[o] + tm.xv[o];
+        if (in(i + 1, j)) w = w + tm.xv[o + 1];
+        tm.sb[o] = (w == T(0)) ? T(0) : smag_S(uin, vin, o, sj, c1, c2) * w;
+      }
+    });
+  }
+};
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) hdiffsmag_adj_gather_kernel(
-    T* __restrict__ uinb, T* __restrict__ vinb, SmagTerms<T> tm, const T* __restrict__ uoutb,
-    const T* __restrict__ voutb, const T* __restrict__ crlavo, const T* __restrict__ crlavu,
-    const T* __restrict__ crlato, const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d, T eddlat,
-    T eddlon, Dims d, int kb) {
-  constexpr T rr = earth_radius_recip<T>();
-  const T c1 = eddlat * rr;
-  const int64_t sj = d.sj;
-  auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
-  auto inT = [&](int i, int j) { return i >= 0 && i <= d.nx && j >= 0 && j <= d.ny; };
-  auto inS = [&](int i, int j) { return i >= -1 && i < d.nx && j >= -1 && j < d.ny; };
-  for_box(d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int a, int b) {
-    const T c2 = ld(acrlat0 + (int64_t)b * s1d) * eddlon;
-    T ub = T(0), vb = T(0);
-    if (in(a, b)) {
-      const int64_t bo = (int64_t)b * s1d;
-      ub = ld(uoutb + o) - (T(2) + ld(crlato + bo) + ld(crlatu + bo)) * tm.lu[o];
-      vb = ld(voutb + o) - (T(2) + ld(crlavo + bo) + ld(crlavu + bo)) * tm.lv[o];
-    }
-    if (in(a - 1, b)) ub = ub + tm.lu[o - 1], vb = vb + tm.lv[o - 1];
-    if (in(a + 1, b)) ub = ub + tm.lu[o + 1], vb = vb + tm.lv[o + 1];
-    if (in(a, b - 1)) {
-      const int64_t bo = (int64_t)(b - 1) * s1d;
-      ub = ub + ld(crlato + bo) * tm.lu[o - sj];
-      vb = vb + ld(crlavo + bo) * tm.lv[o - sj];
-    }
-    if (in(a, b + 1)) {
-      const int64_t bo = (int64_t)(b + 1) * s1d;
-      ub = ub + ld(crlatu + bo) * tm.lu[o + sj];
-      vb = vb + ld(crlavu + bo) * tm.lv[o + sj];
-    }
-    const T tb0 = inT(a, b) ? tm.tb[o] : T(0);
-    const T sb0 = inS(a, b) ? tm.sb[o] : T(0);
-    if (inT(a + 1, b)) ub = ub - c2 * tm.tb[o + 1];
-    ub = ub + c2 * tb0 - c1 * sb0;
-    if (inS(a, b - 1)) ub = ub + c1 * tm.sb[o - sj];
-    if (inT(a, b + 1)) vb = vb + c1 * tm.tb[o + sj];
-    vb = vb - c1 * tb0 - c2 * sb0;
-    if (inS(a - 1, b)) vb = vb + c2 * tm.sb[o - 1];
-    uinb[o] = ub;
-    vinb[o] = vb;
-  });
-}
+struct hdiffsmag_adj_gather_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
+                                             SmagTerms<T> tm, const T* __restrict__ uoutb,
+                                             const T* __restrict__ voutb, const T* __restrict__ crlavo,
+                                             const T* __restrict__ crlavu, const T* __restrict__ crlato,
+                                             const T* __restrict__ crlatu, const T* __restrict__ acrlat0, int64_t s1d,
+                                             T eddlat, T eddlon, Dims d, int kb) {
+    constexpr T rr = earth_radius_recip<T>();
+    const T c1 = eddlat * rr;
+    const int64_t sj = d.sj;
+    auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+    auto inT = [&](int i, int j) { return i >= 0 && i <= d.nx && j >= 0 && j <= d.ny; };
+    auto inS = [&](int i, int j) { return i >= -1 && i < d.nx && j >= -1 && j < d.ny; };
+    for_box(blk, d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int a, int b) {
+      const T c2 = ld(acrlat0 + (int64_t)b * s1d) * eddlon;
+      T ub = T(0), vb = T(0);
+      if (in(a, b)) {
+        const int64_t bo = (int64_t)b * s1d;
+        ub = ld(uoutb + o) - (T(2) + ld(crlato + bo) + ld(crlatu + bo)) * tm.lu[o];
+        vb = ld(voutb + o) - (T(2) + ld(crlavo + bo) + ld(crlavu + bo)) * tm.lv[o];
+      }
+      if (in(a - 1, b)) ub = ub + tm.lu[o - 1], vb = vb + tm.lv[o - 1];
+      if (in(a + 1, b)) ub = ub + tm.lu[o + 1], vb = vb + tm.lv[o + 1];
+      if (in(a, b - 1)) {
+        const int64_t bo = (int64_t)(b - 1) * s1d;
+        ub = ub + ld(crlato + bo) * tm.lu[o - sj];
+        vb = vb + ld(crlavo + bo) * tm.lv[o - sj];
+      }
+      if (in(a, b + 1)) {
+        const int64_t bo = (int64_t)(b + 1) * s1d;
+        ub = ub + ld(crlatu + bo) * tm.lu[o + sj];
+        vb = vb + ld(crlavu + bo) * tm.lv[o + sj];
+      }
+      const T tb0 = inT(a, b) ? tm.tb[o] : T(0);
+      const T sb0 = inS(a, b) ? tm.sb[o] : T(0);
+      if (inT(a + 1, b)) ub = ub - c2 * tm.tb[o + 1];
+      ub = ub + c2 * tb0 - c1 * sb0;
+      if (inS(a, b - 1)) ub = ub + c1 * tm.sb[o - sj];
+      if (inT(a, b + 1)) vb = vb + c1 * tm.tb[o + sj];
+      vb = vb - c1 * tb0 - c2 * sb0;
+      if (inS(a - 1, b)) vb = vb + c2 * tm.sb[o - 1];
+      uinb[o] = ub;
+      vinb[o] = vb;
+    });
+  }
+};
 
 template <class T, class M3, class M1>
 oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M3* mask,
@@ -466,43 +472,34 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
   OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi}, {gui.lo, gui.hi, guo.lo, guo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
-  cudaMemPool_t pool;
-  OEB_TRY(device_pool(&pool));
   const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
   const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +
                        (uin->sizes[2] - 1) * uin->strides[2];
   const int64_t n = (int64_t)(uin->aligned - start) + last + 1;
   const int64_t org = (int64_t)(uin->aligned - start) + uin->offset;
   void* buf = nullptr;
-  cudaError_t e = cudaMallocFromPoolAsync(&buf, (size_t)n * 6 * sizeof(T), pool, st);
-  if (e != cudaSuccess) {
-    cuda_fail(e);
-    return OEB_ERR_ALLOC;
-  }
+  OEB_TRY(scratch_alloc(&buf, (size_t)n * 6 * sizeof(T), st));
   T* base = static_cast<T*>(buf);
   SmagTerms<T> tm{base + org, base + n + org, base + 2 * n + org, base + 3 * n + org, base + 4 * n + org,
                   base + 5 * n + org};
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
   auto org1 = [](const M1* m) { return (const T*)m->aligned + m->offset; };
   const int64_t s1d = acrlat0->strides[0];
-  cudaStream_t s0 = st;
-  hdiffsmag_adj_terms_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, s0>>>(
-      tm, gui.origin, (const T*)vin->aligned + vin->offset, (const T*)mask->aligned + mask->offset, org1(crlavo),
-      org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d, guo.origin,
-      (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kKB);
-  oeb_status stt = after_launch();
-  if (stt == OEB_OK) {
-    hdiffsmag_adj_ts_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, s0>>>(
-        tm, gui.origin, (const T*)vin->aligned + vin->offset, org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
-    stt = after_launch();
-  }
-  if (stt == OEB_OK) {
-    hdiffsmag_adj_gather_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, s0>>>(
-        gub.origin, gvb.origin, tm, guo.origin, (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu),
-        org1(crlato), org1(crlatu), org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
-    stt = after_launch();
-  }
-  cudaFreeAsync(buf, st);
+  const int kb = tuned_kb(kKB);
+  oeb_status stt = launch<hdiffsmag_adj_terms_kernel<T>>(
+      tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), 0, st, tm, gui.origin, (const T*)vin->aligned + vin->offset,
+      (const T*)mask->aligned + mask->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d,
+      guo.origin, (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kb);
+  if (stt == OEB_OK)
+    stt = launch<hdiffsmag_adj_ts_kernel<T>>(tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kb), 0, st, tm, gui.origin,
+                                             (const T*)vin->aligned + vin->offset, org1(acrlat0), s1d, eddlat, eddlon,
+                                             d, kb);
+  if (stt == OEB_OK)
+    stt = launch<hdiffsmag_adj_gather_kernel<T>>(
+        tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kb), 0, st, gub.origin, gvb.origin, tm, guo.origin,
+        (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0),
+        s1d, eddlat, eddlon, d, kb);
+  scratch_free(buf, st);
   return stt;
 }
 
@@ -580,18 +577,17 @@ oeb_status hdiffsmag_adj_noalloc_entry(const oeb_memref3d_f64* uinb, const oeb_m
   auto org1 = [](const oeb_memref1d_f64* m) { return (const T*)m->aligned + m->offset; };
   const int64_t s1d = acrlat0->strides[0];
   cudaStream_t st = (cudaStream_t)stream;
-  hdiffsmag_adj_terms_kernel<T><<<tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
-      tm, gui.origin, (const T*)vin->aligned + vin->offset, (const T*)mask->aligned + mask->offset, org1(crlavo),
-      org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d, guo.origin,
-      (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kKB);
-  OEB_TRY(after_launch());
-  hdiffsmag_adj_ts_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
-      tm, gui.origin, (const T*)vin->aligned + vin->offset, org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
-  OEB_TRY(after_launch());
-  hdiffsmag_adj_gather_kernel<T><<<tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), dim3(kTX, kTY), 0, st>>>(
-      gub.origin, gvb.origin, tm, guo.origin, (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu),
-      org1(crlato), org1(crlatu), org1(acrlat0), s1d, eddlat, eddlon, d, kKB);
-  return after_launch();
+  OEB_TRY(launch<hdiffsmag_adj_terms_kernel<T>>(
+      tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), 0, st, tm, gui.origin, (const T*)vin->aligned + vin->offset,
+      (const T*)mask->aligned + mask->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d,
+      guo.origin, (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kKB));
+  OEB_TRY(launch<hdiffsmag_adj_ts_kernel<T>>(tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), 0, st, tm, gui.origin,
+                                             (const T*)vin->aligned + vin->offset, org1(acrlat0), s1d, eddlat, eddlon,
+                                             d, kKB));
+  return launch<hdiffsmag_adj_gather_kernel<T>>(
+      tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), 0, st, gub.origin, gvb.origin, tm, guo.origin,
+      (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0),
+      s1d, eddlat, eddlon, d, kKB);
 }
 
 }  // namespace

@@ -24,10 +24,10 @@ constexpr int kTI = 32, kTJ = 32, kRows = kTJ / kTY;
 // Visits the points of this thread: f(o, j) with o the in-plane offset of (i, j) plus the
 // plane offset of k.
 template <class F>
-__device__ __forceinline__ void for_points(const Dims& d, int kb, F&& f) {
-  const int i = blockIdx.x * kTI + threadIdx.x;
+__device__ __forceinline__ void for_points(const uint3& blk, const Dims& d, int kb, F&& f) {
+  const int i = blk.x * kTI + threadIdx.x;
   if (i >= d.nx) return;
-  const int k0 = blockIdx.z * kb;
+  const int k0 = blk.z * kb;
   const int k1 = min(k0 + kb, d.nz);
   const int sj = (int)d.sj;
 #pragma unroll 1
@@ -35,7 +35,7 @@ __device__ __forceinline__ void for_points(const Dims& d, int kb, F&& f) {
     const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll
     for (int r = 0; r < kRows; ++r) {
-      const int j = blockIdx.y * kTJ + threadIdx.y + kTY * r;
+      const int j = blk.y * kTJ + threadIdx.y + kTY * r;
       if (j < d.ny) f(kofs + i + j * sj, j);
     }
   }
@@ -43,24 +43,26 @@ __device__ __forceinline__ void for_points(const Dims& d, int kb, F&& f) {
 
 // ---- laplace: kernels/laplace.h:34-43 ----------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(kThreads) laplace_kernel(const T* __restrict__ in, T* __restrict__ out, Dims d,
-                                                           int kb) {
-  const int64_t sj = d.sj;
-  for_points(d, kb, [&](int64_t o, int) {
-    if constexpr (Prec<T>::kCompensated) {
-      // -4 in nearly cancels the neighbour sum on smooth fields: sum all five terms
-      // compensated (-4 in is exact)
-      Acc<T> acc(ld(in + o - 1));
-      acc.add(ld(in + o + 1));
-      acc.add(ld(in + o + sj));
-      acc.add(ld(in + o - sj));
-      acc.add(T(-4.0) * ld(in + o));
-      out[o] = acc.get();
-    } else {
-      out[o] = T(-4.0) * ld(in + o) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
-    }
-  });
-}
+struct laplace_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, const T* __restrict__ in, T* __restrict__ out, Dims d,
+                                             int kb) {
+    const int64_t sj = d.sj;
+    for_points(blk, d, kb, [&](int64_t o, int) {
+      if constexpr (Prec<T>::kCompensated) {
+        // -4 in nearly cancels the neighbour sum on smooth fields: sum all five terms
+        // compensated (-4 in is exact)
+        Acc<T> acc(ld(in + o - 1));
+        acc.add(ld(in + o + 1));
+        acc.add(ld(in + o + sj));
+        acc.add(ld(in + o - sj));
+        acc.add(T(-4.0) * ld(in + o));
+        out[o] = acc.get();
+      } else {
+        out[o] = T(-4.0) * ld(in + o) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
+      }
+    });
+  }
+};
 
 // ---- uvbke: kernels/uvbke.h:61-75 ----------------------------------------------------
 // dt5 is a double in every precision (src/uvbke.cpp:11-12), so the reference compiled for
@@ -78,80 +80,86 @@ __device__ __forceinline__ T uvbke_scale(T t, T rs, T dt5_hi, T dt5_lo) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) uvbke_kernel(T* __restrict__ ub, T* __restrict__ vb,
-                                                         const T* __restrict__ uc, const T* __restrict__ vc,
-                                                         const T* __restrict__ cosa, const T* __restrict__ rsina,
-                                                         T dt5, T dt5_lo, Dims d, int kb) {
-  const int64_t sj = d.sj;
-  for_points(d, kb, [&](int64_t o, int) {
-    const T su = ld(uc + o - sj) + ld(uc + o);
-    const T sv = ld(vc + o - 1) + ld(vc + o);
-    const T ca = ld(cosa + o);
-    const T rs = ld(rsina + o);
-    ub[o] = uvbke_scale(su - (sv * ca), rs, dt5, dt5_lo);
-    vb[o] = uvbke_scale(sv - (su * ca), rs, dt5, dt5_lo);
-  });
-}
+struct uvbke_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ ub, T* __restrict__ vb,
+                                             const T* __restrict__ uc, const T* __restrict__ vc,
+                                             const T* __restrict__ cosa, const T* __restrict__ rsina, T dt5, T dt5_lo,
+                                             Dims d, int kb) {
+    const int64_t sj = d.sj;
+    for_points(blk, d, kb, [&](int64_t o, int) {
+      const T su = ld(uc + o - sj) + ld(uc + o);
+      const T sv = ld(vc + o - 1) + ld(vc + o);
+      const T ca = ld(cosa + o);
+      const T rs = ld(rsina + o);
+      ub[o] = uvbke_scale(su - (sv * ca), rs, dt5, dt5_lo);
+      vb[o] = uvbke_scale(sv - (su * ca), rs, dt5, dt5_lo);
+    });
+  }
+};
 
 // ---- p_grad_c: kernels/p_grad_c.h:80-101 ---------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(kThreads) p_grad_c_kernel(T* __restrict__ uout, T* __restrict__ vout,
-                                                            const T* __restrict__ uin, const T* __restrict__ vin,
-                                                            const T* __restrict__ rdxc, const T* __restrict__ rdyc,
-                                                            const T* __restrict__ delpc, const T* __restrict__ gz,
-                                                            const T* __restrict__ pkc, T dt2, Dims d, int kb) {
-  const int64_t sj = d.sj, sk = d.sk;
-  for_points(d, kb, [&](int64_t o, int) {
-    const T wk = ld(delpc + o);
-    const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
-    // the two products nearly cancel (a small pressure-gradient residual): diff_dot is the
-    // reference's tree in FP64 and float-float in FP32
-    const T fu = diff_dot(ld(gz + o - 1 + sk), gz0, pk1, ld(pkc + o - 1), ld(gz + o - 1), gz1, ld(pkc + o - 1 + sk), pk0);
-    uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) * fu));
-    const T fv =
-        diff_dot(ld(gz + o - sj + sk), gz0, pk1, ld(pkc + o - sj), ld(gz + o - sj), gz1, ld(pkc + o - sj + sk), pk0);
-    vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) * fv));
-  });
-}
+struct p_grad_c_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
+                                             const T* __restrict__ uin, const T* __restrict__ vin,
+                                             const T* __restrict__ rdxc, const T* __restrict__ rdyc,
+                                             const T* __restrict__ delpc, const T* __restrict__ gz,
+                                             const T* __restrict__ pkc, T dt2, Dims d, int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    for_points(blk, d, kb, [&](int64_t o, int) {
+      const T wk = ld(delpc + o);
+      const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
+      // the two products nearly cancel (a small pressure-gradient residual): diff_dot is the
+      // reference's tree in FP64 and float-float in FP32
+      const T fu = diff_dot(ld(gz + o - 1 + sk), gz0, pk1, ld(pkc + o - 1), ld(gz + o - 1), gz1, ld(pkc + o - 1 + sk), pk0);
+      uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) * fu));
+      const T fv =
+          diff_dot(ld(gz + o - sj + sk), gz0, pk1, ld(pkc + o - sj), ld(gz + o - sj), gz1, ld(pkc + o - sj + sk), pk0);
+      vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) * fv));
+    });
+  }
+};
 
 // ---- nh_p_grad: kernels/nh_p_grad.h:116-146 --------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(kThreads) nh_p_grad_kernel(T* __restrict__ uout, T* __restrict__ vout,
-                                                             const T* __restrict__ uin, const T* __restrict__ vin,
-                                                             const T* __restrict__ rdx, const T* __restrict__ rdy,
-                                                             const T* __restrict__ gz, const T* __restrict__ pp,
-                                                             const T* __restrict__ pk3, const T* __restrict__ wk1,
-                                                             T dt, Dims d, int kb) {
-  const int64_t sj = d.sj, sk = d.sk;
-  for_points(d, kb, [&](int64_t o, int) {
-    const T pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
-    const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk);
-    const T pp0 = ld(pp + o), pp1 = ld(pp + o + sk);
-    const T w1 = ld(wk1 + o);
-    const T wk = pk1 - pk0;
-    // u: neighbour i+1
-    {
-      const T pkx0 = ld(pk3 + o + 1), pkx1 = ld(pk3 + o + 1 + sk);
-      const T wkx = pkx1 - pkx0;
-      const T gx0 = ld(gz + o + 1), gx1 = ld(gz + o + 1 + sk);
-      // the two products of each sum nearly cancel: diff_dot (precision.cuh)
-      const T fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
-      const T fp = diff_dot(gz1, gx0, ld(pp + o + 1 + sk), pp0, gz0, gx1, pp1, ld(pp + o + 1));
-      const T du = ((dt / (wk + wkx)) * fk);
-      uout[o] = (((ld(uin + o) + du) + ((dt / (w1 + ld(wk1 + o + 1))) * fp)) * ld(rdx + o));
-    }
-    // v: neighbour j+1
-    {
-      const T pky0 = ld(pk3 + o + sj), pky1 = ld(pk3 + o + sj + sk);
-      const T wky = pky1 - pky0;
-      const T gy0 = ld(gz + o + sj), gy1 = ld(gz + o + sj + sk);
-      const T fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
-      const T fp = diff_dot(gz1, gy0, ld(pp + o + sj + sk), pp0, gz0, gy1, pp1, ld(pp + o + sj));
-      const T dv = ((dt / (wk + wky)) * fk);
-      vout[o] = (((ld(vin + o) + dv) + ((dt / (w1 + ld(wk1 + o + sj))) * fp)) * ld(rdy + o));
-    }
-  });
-}
+struct nh_p_grad_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
+                                             const T* __restrict__ uin, const T* __restrict__ vin,
+                                             const T* __restrict__ rdx, const T* __restrict__ rdy,
+                                             const T* __restrict__ gz, const T* __restrict__ pp,
+                                             const T* __restrict__ pk3, const T* __restrict__ wk1, T dt, Dims d,
+                                             int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    for_points(blk, d, kb, [&](int64_t o, int) {
+      const T pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
+      const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk);
+      const T pp0 = ld(pp + o), pp1 = ld(pp + o + sk);
+      const T w1 = ld(wk1 + o);
+      const T wk = pk1 - pk0;
+      // u: neighbour i+1
+      {
+        const T pkx0 = ld(pk3 + o + 1), pkx1 = ld(pk3 + o + 1 + sk);
+        const T wkx = pkx1 - pkx0;
+        const T gx0 = ld(gz + o + 1), gx1 = ld(gz + o + 1 + sk);
+        // the two products of each sum nearly cancel: diff_dot (precision.cuh)
+        const T fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
+        const T fp = diff_dot(gz1, gx0, ld(pp + o + 1 + sk), pp0, gz0, gx1, pp1, ld(pp + o + 1));
+        const T du = ((dt / (wk + wkx)) * fk);
+        uout[o] = (((ld(uin + o) + du) + ((dt / (w1 + ld(wk1 + o + 1))) * fp)) * ld(rdx + o));
+      }
+      // v: neighbour j+1
+      {
+        const T pky0 = ld(pk3 + o + sj), pky1 = ld(pk3 + o + sj + sk);
+        const T wky = pky1 - pky0;
+        const T gy0 = ld(gz + o + sj), gy1 = ld(gz + o + sj + sk);
+        const T fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
+        const T fp = diff_dot(gz1, gy0, ld(pp + o + sj + sk), pp0, gz0, gy1, pp1, ld(pp + o + sj));
+        const T dv = ((dt / (wk + wky)) * fk);
+        vout[o] = (((ld(vin + o) + dv) + ((dt / (w1 + ld(wk1 + o + sj))) * fp)) * ld(rdy + o));
+      }
+    });
+  }
+};
 
 // ---- hadvuv / hadvuv5th: kernels/hadvuv.h:4-27,178-210 and kernels/hadvuv5th.h:4-39,177-201
 
@@ -199,50 +207,51 @@ __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64
 }
 
 template <class T, int ORDER>
-__global__ void __launch_bounds__(kThreads) hadv_kernel(T* __restrict__ uout, T* __restrict__ vout,
-                                                        const T* __restrict__ uin, const T* __restrict__ vin,
-                                                        const T* __restrict__ acrlat0, const T* __restrict__ acrlat1,
-                                                        const T* __restrict__ tgrlatda0,
-                                                        const T* __restrict__ tgrlatda1, int64_t s1d, T eddlat,
-                                                        T eddlon, Dims d, int kb) {
-  const int64_t sj = d.sj;
-  constexpr T third = T(1.0) / T(3.0);
-  constexpr T rr = earth_radius_recip<T>();
-  for_points(d, kb, [&](int64_t o, int j) {
-    const int64_t jo = (int64_t)j * s1d;
-    const T u0 = ld(uin + o), v0 = ld(vin + o);
-    const T um = ld(uin + o - 1) + u0;  // uin(i-1)+uin(i), first pair of both averages
-    // u at the u-position and v at the u-position (hadvuv.h:186-189)
-    const T u_atupos = third * (um + ld(uin + o + 1));
-    const T v_atupos = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
-    T ua = ld(acrlat0 + jo) * u_atupos;
-    T va = rr * v_atupos;
-    T rx, ry;
-    if (ORDER == 3) {
-      rx = adv3_axis(uin, o, 1, ua);
-      ry = adv3_axis(uin, o, sj, va);
-    } else {
-      rx = adv5_axis(uin, o, 1, ua);
-      ry = adv5_axis(uin, o, sj, va);
-    }
-    const T ures = eddlat * rx + eddlon * ry;
-    uout[o] = ures + (ld(tgrlatda0 + jo) * u0) * v_atupos;
-    // u and v at the v-position (hadvuv.h:197-206)
-    const T u_atvpos = T(0.25) * (((um) + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
-    const T v_atvpos = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
-    ua = ld(acrlat1 + jo) * u_atvpos;
-    va = rr * v_atvpos;
-    if (ORDER == 3) {
-      rx = adv3_axis(vin, o, 1, ua);
-      ry = adv3_axis(vin, o, sj, va);
-    } else {
-      rx = adv5_axis(vin, o, 1, ua);
-      ry = adv5_axis(vin, o, sj, va);
-    }
-    const T vres = eddlat * rx + eddlon * ry;
-    vout[o] = vres - (ld(tgrlatda1 + jo) * u_atvpos) * u_atvpos;
-  });
-}
+struct hadv_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
+                                             const T* __restrict__ uin, const T* __restrict__ vin,
+                                             const T* __restrict__ acrlat0, const T* __restrict__ acrlat1,
+                                             const T* __restrict__ tgrlatda0, const T* __restrict__ tgrlatda1,
+                                             int64_t s1d, T eddlat, T eddlon, Dims d, int kb) {
+    const int64_t sj = d.sj;
+    constexpr T third = T(1.0) / T(3.0);
+    constexpr T rr = earth_radius_recip<T>();
+    for_points(blk, d, kb, [&](int64_t o, int j) {
+      const int64_t jo = (int64_t)j * s1d;
+      const T u0 = ld(uin + o), v0 = ld(vin + o);
+      const T um = ld(uin + o - 1) + u0;  // uin(i-1)+uin(i), first pair of both averages
+      // u at the u-position and v at the u-position (hadvuv.h:186-189)
+      const T u_atupos = third * (um + ld(uin + o + 1));
+      const T v_atupos = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
+      T ua = ld(acrlat0 + jo) * u_atupos;
+      T va = rr * v_atupos;
+      T rx, ry;
+      if (ORDER == 3) {
+        rx = adv3_axis(uin, o, 1, ua);
+        ry = adv3_axis(uin, o, sj, va);
+      } else {
+        rx = adv5_axis(uin, o, 1, ua);
+        ry = adv5_axis(uin, o, sj, va);
+      }
+      const T ures = eddlat * rx + eddlon * ry;
+      uout[o] = ures + (ld(tgrlatda0 + jo) * u0) * v_atupos;
+      // u and v at the v-position (hadvuv.h:197-206)
+      const T u_atvpos = T(0.25) * (((um) + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
+      const T v_atvpos = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
+      ua = ld(acrlat1 + jo) * u_atvpos;
+      va = rr * v_atvpos;
+      if (ORDER == 3) {
+        rx = adv3_axis(vin, o, 1, ua);
+        ry = adv3_axis(vin, o, sj, va);
+      } else {
+        rx = adv5_axis(vin, o, 1, ua);
+        ry = adv5_axis(vin, o, sj, va);
+      }
+      const T vres = eddlat * rx + eddlon * ry;
+      vout[o] = vres - (ld(tgrlatda1 + jo) * u_atvpos) * u_atvpos;
+    });
+  }
+};
 
 constexpr int kKB = 4;  // k-levels per CTA
 
@@ -251,7 +260,7 @@ Dims make_dims(const oeb_domain& dom, const Grid<T>& g) {
   return Dims{(int)dom.nx, (int)dom.ny, (int)dom.nz, g.sj, g.sk};
 }
 
-dim3 grid_for(const oeb_domain& dom) { return tile_grid((int)dom.nx, (int)dom.ny, (int)dom.nz, kTI, kTJ, kKB); }
+dim3 grid_for(const oeb_domain& dom, int kb) { return tile_grid((int)dom.nx, (int)dom.ny, (int)dom.nz, kTI, kTJ, kb); }
 
 // ------------------------------ entry points -----------------------------------------
 
@@ -264,9 +273,9 @@ oeb_status laplace_entry(const M3* in, const M3* out, const oeb_domain* dom, voi
   OEB_TRY(check_same_strides<T>({&gin, &gout}));
   OEB_TRY(check_no_alias({gout.lo, gout.hi}, {gin.lo, gin.hi}));
   OEB_RETURN_IF_VALIDATING();
-  laplace_kernel<T><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(gin.origin, gout.origin,
-                                                                                make_dims(*dom, gin), kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<laplace_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gin.origin, gout.origin,
+                                   make_dims(*dom, gin), kb);
 }
 
 template <class T, class M3>
@@ -285,10 +294,9 @@ oeb_status uvbke_entry(const M3* ub, const M3* vb, const M3* uc, const M3* vc, c
                          {guc.lo, guc.hi, gvc.lo, gvc.hi, gca.lo, gca.hi, grs.lo, grs.hi}));
   OEB_RETURN_IF_VALIDATING();
   const T dt5_hi = T(dt5), dt5_lo = T(dt5 - (double)dt5_hi);  // dt5_lo = 0 for FP64
-  uvbke_kernel<T><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
-      gub.origin, gvb.origin, guc.origin, gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo, make_dims(*dom, gub),
-      kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<uvbke_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gub.origin, gvb.origin, guc.origin,
+                                 gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo, make_dims(*dom, gub), kb);
 }
 
 template <class T, class M3>
@@ -310,10 +318,10 @@ oeb_status p_grad_c_entry(const M3* uout, const M3* vout, const M3* uin, const M
   OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi}, {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo,
                                                         gry.hi, gdp.lo, gdp.hi, ggz.lo, ggz.hi, gpk.lo, gpk.hi}));
   OEB_RETURN_IF_VALIDATING();
-  p_grad_c_kernel<T><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
-      gu.origin, gv.origin, gui.origin, gvi.origin, grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin, dt2,
-      make_dims(*dom, gu), kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<p_grad_c_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
+                                    gvi.origin, grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin, dt2,
+                                    make_dims(*dom, gu), kb);
 }
 
 template <class T, class M3>
@@ -338,10 +346,10 @@ oeb_status nh_p_grad_entry(const M3* uout, const M3* vout, const M3* uin, const 
                          {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo, gry.hi, ggz.lo, ggz.hi, gpp.lo,
                           gpp.hi, gpk.lo, gpk.hi, gw1.lo, gw1.hi}));
   OEB_RETURN_IF_VALIDATING();
-  nh_p_grad_kernel<T><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
-      gu.origin, gv.origin, gui.origin, gvi.origin, grx.origin, gry.origin, ggz.origin, gpp.origin, gpk.origin,
-      gw1.origin, dt, make_dims(*dom, gu), kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<nh_p_grad_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
+                                     gvi.origin, grx.origin, gry.origin, ggz.origin, gpp.origin, gpk.origin,
+                                     gw1.origin, dt, make_dims(*dom, gu), kb);
 }
 
 template <class T, int ORDER, class M3, class M1>
@@ -366,10 +374,10 @@ oeb_status hadv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* v
   OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi}, {gui.lo, gui.hi, gvi.lo, gvi.hi, a0.lo, a0.hi, a1.lo, a1.hi,
                                                         t0.lo, t0.hi, t1.lo, t1.hi}));
   OEB_RETURN_IF_VALIDATING();
-  hadv_kernel<T, ORDER><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
-      gu.origin, gv.origin, gui.origin, gvi.origin, a0.origin, a1.origin, t0.origin, t1.origin, a0.s, eddlat, eddlon,
-      make_dims(*dom, gu), kKB);
-  return after_launch();
+  const int kb = tuned_kb(kKB);
+  return launch<hadv_kernel<T, ORDER>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
+                                       gvi.origin, a0.origin, a1.origin, t0.origin, t1.origin, a0.s, eddlat, eddlon,
+                                       make_dims(*dom, gu), kb);
 }
 
 // Tangent-linear hadvuv / hadvuv5th: d(uout, vout) = J(uin, vin) d(uin, vin), on Dual<T>.
@@ -397,9 +405,9 @@ oeb_status hadv_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const 
   OEB_TRY(arr.alloc(duout, &ou));
   OEB_TRY(arr.alloc(dvout, &ov));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
-  hadv_kernel<D, ORDER><<<grid_for(*dom), dim3(kTX, kTY), 0, (cudaStream_t)stream>>>(
-      ou, ov, u, v, a0, a1, t0, t1, acrlat0->strides[0], D(eddlat), D(eddlon), d, kKB);
-  OEB_TRY(after_launch());
+  const int kb = tuned_kb(kKB);
+  OEB_TRY((launch<hadv_kernel<D, ORDER>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, ou, ov, u, v, a0, a1, t0, t1,
+                                         acrlat0->strides[0], D(eddlat), D(eddlon), d, kb)));
   OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
   return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
 }
@@ -458,98 +466,104 @@ __device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t
 }
 
 template <class T, int ORDER>
-__global__ void __launch_bounds__(kThreads) hadv_adj_terms_kernel(
-    HadvTerms<T> tm, const T* __restrict__ uin, const T* __restrict__ vin, const T* __restrict__ acrlat0,
-    const T* __restrict__ acrlat1, const T* __restrict__ tgrlatda0, const T* __restrict__ tgrlatda1, int64_t s1d,
-    const T* __restrict__ uoutb, const T* __restrict__ voutb, T eddlat, T eddlon, Dims d, int kb) {
-  const int64_t sj = d.sj;
-  constexpr T third = T(1.0) / T(3.0);
-  constexpr T rr = earth_radius_recip<T>();
-  for_points(d, kb, [&](int64_t o, int j) {
-    const int64_t jo = (int64_t)j * s1d;
-    const T u0 = ld(uin + o), v0 = ld(vin + o);
-    const T um = ld(uin + o - 1) + u0;
-    const T ua = third * (um + ld(uin + o + 1));
-    const T va = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
-    const T ub = T(0.25) * ((um + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
-    const T vb = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
-    const T a0 = ld(acrlat0 + jo), a1 = ld(acrlat1 + jo), t0 = ld(tgrlatda0 + jo), t1 = ld(tgrlatda1 + jo);
-    const T Ax = a0 * ua, Ay = rr * va, Bx = a1 * ub, By = rr * vb;
-    const bool px = Ax > 0, py = Ay > 0, qx = Bx > 0, qy = By > 0;
-    const T Px = adv_sum<T, ORDER>(uin, o, 1, px), Py = adv_sum<T, ORDER>(uin, o, sj, py);
-    const T Qx = adv_sum<T, ORDER>(vin, o, 1, qx), Qy = adv_sum<T, ORDER>(vin, o, sj, qy);
-    const T yu = ld(uoutb + o), yv = ld(voutb + o);
-    tm.ax[o] = (eddlat * Ax) * yu;
-    tm.ay[o] = (eddlon * Ay) * yu;
-    tm.bx[o] = ((eddlat * Px) * a0) * (third * yu);
-    tm.by[o] = ((eddlon * Py) * rr + t0 * u0) * (T(0.25) * yu);
-    tm.dd[o] = (t0 * va) * yu;
-    tm.gx[o] = (eddlat * Bx) * yv;
-    tm.gy[o] = (eddlon * By) * yv;
-    tm.ex[o] = ((eddlat * Qx) * a1 - (T(2) * t1) * ub) * (T(0.25) * yv);
-    tm.ey[o] = ((eddlon * Qy) * rr) * (third * yv);
-    tm.fl[o] = (unsigned char)((px ? 1 : 0) | (py ? 2 : 0) | (qx ? 4 : 0) | (qy ? 8 : 0));
-  });
-}
+struct hadv_adj_terms_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, HadvTerms<T> tm, const T* __restrict__ uin,
+                                             const T* __restrict__ vin, const T* __restrict__ acrlat0,
+                                             const T* __restrict__ acrlat1, const T* __restrict__ tgrlatda0,
+                                             const T* __restrict__ tgrlatda1, int64_t s1d,
+                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T eddlat,
+                                             T eddlon, Dims d, int kb) {
+    const int64_t sj = d.sj;
+    constexpr T third = T(1.0) / T(3.0);
+    constexpr T rr = earth_radius_recip<T>();
+    for_points(blk, d, kb, [&](int64_t o, int j) {
+      const int64_t jo = (int64_t)j * s1d;
+      const T u0 = ld(uin + o), v0 = ld(vin + o);
+      const T um = ld(uin + o - 1) + u0;
+      const T ua = third * (um + ld(uin + o + 1));
+      const T va = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
+      const T ub = T(0.25) * ((um + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
+      const T vb = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
+      const T a0 = ld(acrlat0 + jo), a1 = ld(acrlat1 + jo), t0 = ld(tgrlatda0 + jo), t1 = ld(tgrlatda1 + jo);
+      const T Ax = a0 * ua, Ay = rr * va, Bx = a1 * ub, By = rr * vb;
+      const bool px = Ax > 0, py = Ay > 0, qx = Bx > 0, qy = By > 0;
+      const T Px = adv_sum<T, ORDER>(uin, o, 1, px), Py = adv_sum<T, ORDER>(uin, o, sj, py);
+      const T Qx = adv_sum<T, ORDER>(vin, o, 1, qx), Qy = adv_sum<T, ORDER>(vin, o, sj, qy);
+      const T yu = ld(uoutb + o), yv = ld(voutb + o);
+      tm.ax[o] = (eddlat * Ax) * yu;
+      tm.ay[o] = (eddlon * Ay) * yu;
+      tm.bx[o] = ((eddlat * Px) * a0) * (third * yu);
+      tm.by[o] = ((eddlon * Py) * rr + t0 * u0) * (T(0.25) * yu);
+      tm.dd[o] = (t0 * va) * yu;
+      tm.gx[o] = (eddlat * Bx) * yv;
+      tm.gy[o] = (eddlon * By) * yv;
+      tm.ex[o] = ((eddlat * Qx) * a1 - (T(2) * t1) * ub) * (T(0.25) * yv);
+      tm.ey[o] = ((eddlon * Qy) * rr) * (third * yv);
+      tm.fl[o] = (unsigned char)((px ? 1 : 0) | (py ? 2 : 0) | (qx ? 4 : 0) | (qy ? 8 : 0));
+    });
+  }
+};
 
 // Visits every cell of the box [-h, nx+h) x [-h, ny+h) x [0, nz) owned by this thread.
 template <class F>
-__device__ __forceinline__ void for_box_points(const Dims& d, int h, int kb, F&& f) {
-  const int i = -h + (int)(blockIdx.x * kTI + threadIdx.x);
+__device__ __forceinline__ void for_box_points(const uint3& blk, const Dims& d, int h, int kb, F&& f) {
+  const int i = -h + (int)(blk.x * kTI + threadIdx.x);
   if (i >= d.nx + h) return;
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
+  const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
   const int sj = (int)d.sj;
 #pragma unroll 1
   for (int k = k0; k < k1; ++k) {
     const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll
     for (int r = 0; r < kRows; ++r) {
-      const int j = -h + (int)(blockIdx.y * kTJ + threadIdx.y) + kTY * r;
+      const int j = -h + (int)(blk.y * kTJ + threadIdx.y) + kTY * r;
       if (j < d.ny + h) f(kofs + i + j * sj, i, j);
     }
   }
 }
 
 template <class T, int ORDER>
-__global__ void __launch_bounds__(kThreads) hadv_adj_gather_kernel(T* __restrict__ uinb, T* __restrict__ vinb,
-                                                                   HadvTerms<T> tm, Dims d, int kb) {
-  constexpr int h = ORDER == 3 ? 2 : 3;
-  const int64_t sj = d.sj;
-  for_box_points(d, h, kb, [&](int64_t o, int a, int b) {
-    auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
-    T ub = T(0), vb = T(0);
-    // upwind stencils: point (a - m, b) reads (a, b) with offset m, and likewise in j
-#pragma unroll
-    for (int m = -h; m <= h; ++m) {
-      if (in(a - m, b)) {
-        const int64_t q = o - m;
-        const unsigned char f = tm.fl[q];
-        ub = ub + upwind_weight<T, ORDER>(f & 1, m) * tm.ax[q];
-        vb = vb + upwind_weight<T, ORDER>(f & 4, m) * tm.gx[q];
+struct hadv_adj_gather_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
+                                             HadvTerms<T> tm, Dims d, int kb) {
+    constexpr int h = ORDER == 3 ? 2 : 3;
+    const int64_t sj = d.sj;
+    for_box_points(blk, d, h, kb, [&](int64_t o, int a, int b) {
+      auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+      T ub = T(0), vb = T(0);
+      // upwind stencils: point (a - m, b) reads (a, b) with offset m, and likewise in j
+  #pragma unroll
+      for (int m = -h; m <= h; ++m) {
+        if (in(a - m, b)) {
+          const int64_t q = o - m;
+          const unsigned char f = tm.fl[q];
+          ub = ub + upwind_weight<T, ORDER>(f & 1, m) * tm.ax[q];
+          vb = vb + upwind_weight<T, ORDER>(f & 4, m) * tm.gx[q];
+        }
+        if (in(a, b - m)) {
+          const int64_t q = o - m * sj;
+          const unsigned char f = tm.fl[q];
+          ub = ub + upwind_weight<T, ORDER>(f & 2, m) * tm.ay[q];
+          vb = vb + upwind_weight<T, ORDER>(f & 8, m) * tm.gy[q];
+        }
       }
-      if (in(a, b - m)) {
-        const int64_t q = o - m * sj;
-        const unsigned char f = tm.fl[q];
-        ub = ub + upwind_weight<T, ORDER>(f & 2, m) * tm.ay[q];
-        vb = vb + upwind_weight<T, ORDER>(f & 8, m) * tm.gy[q];
-      }
-    }
-    // u average of point i (i-1, i, i+1) and the ub average (i-1..i, j..j+1)
-    if (in(a - 1, b)) ub = ub + tm.bx[o - 1];
-    if (in(a, b)) ub = (ub + tm.bx[o]) + (tm.dd[o] + tm.ex[o]);
-    if (in(a + 1, b)) ub = (ub + tm.bx[o + 1]) + tm.ex[o + 1];
-    if (in(a, b - 1)) ub = ub + tm.ex[o - sj];
-    if (in(a + 1, b - 1)) ub = ub + tm.ex[o + 1 - sj];
-    // v average va of point (i, j): (i+1, j), (i+1, j-1), (i, j), (i, j-1); vb: (i, j-1..j+1)
-    if (in(a - 1, b)) vb = vb + tm.by[o - 1];
-    if (in(a - 1, b + 1)) vb = vb + tm.by[o - 1 + sj];
-    if (in(a, b)) vb = (vb + tm.by[o]) + tm.ey[o];
-    if (in(a, b + 1)) vb = (vb + tm.by[o + sj]) + tm.ey[o + sj];
-    if (in(a, b - 1)) vb = vb + tm.ey[o - sj];
-    uinb[o] = ub;
-    vinb[o] = vb;
-  });
-}
+      // u average of point i (i-1, i, i+1) and the ub average (i-1..i, j..j+1)
+      if (in(a - 1, b)) ub = ub + tm.bx[o - 1];
+      if (in(a, b)) ub = (ub + tm.bx[o]) + (tm.dd[o] + tm.ex[o]);
+      if (in(a + 1, b)) ub = (ub + tm.bx[o + 1]) + tm.ex[o + 1];
+      if (in(a, b - 1)) ub = ub + tm.ex[o - sj];
+      if (in(a + 1, b - 1)) ub = ub + tm.ex[o + 1 - sj];
+      // v average va of point (i, j): (i+1, j), (i+1, j-1), (i, j), (i, j-1); vb: (i, j-1..j+1)
+      if (in(a - 1, b)) vb = vb + tm.by[o - 1];
+      if (in(a - 1, b + 1)) vb = vb + tm.by[o - 1 + sj];
+      if (in(a, b)) vb = (vb + tm.by[o]) + tm.ey[o];
+      if (in(a, b + 1)) vb = (vb + tm.by[o + sj]) + tm.ey[o + sj];
+      if (in(a, b - 1)) vb = vb + tm.ey[o - sj];
+      uinb[o] = ub;
+      vinb[o] = vb;
+    });
+  }
+};
 
 template <class T, int ORDER, class M3, class M1>
 oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M1* acrlat0,
@@ -573,8 +587,6 @@ oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M
                          {gui.lo, gui.hi, gvi.lo, gvi.hi, guo.lo, guo.hi, gvo.lo, gvo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
-  cudaMemPool_t pool;
-  OEB_TRY(device_pool(&pool));
   // scratch: nine term fields and the flags, in uin's layout (terms are read at interior points only)
   const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
   const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +
@@ -582,32 +594,23 @@ oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M
   const int64_t n = (int64_t)(uin->aligned - start) + last + 1;
   const int64_t org = (int64_t)(uin->aligned - start) + uin->offset;
   void* buf = nullptr;
-  const size_t bytes = (size_t)n * (9 * sizeof(T) + 1);
-  cudaError_t e = cudaMallocFromPoolAsync(&buf, bytes, pool, st);
-  if (e != cudaSuccess) {
-    cuda_fail(e);
-    return OEB_ERR_ALLOC;
-  }
+  OEB_TRY(scratch_alloc(&buf, (size_t)n * (9 * sizeof(T) + 1), st));
   HadvTerms<T> tm;
   T* base = static_cast<T*>(buf);
   T** fields[9] = {&tm.ax, &tm.ay, &tm.bx, &tm.by, &tm.dd, &tm.gx, &tm.gy, &tm.ex, &tm.ey};
   for (int q = 0; q < 9; ++q) *fields[q] = base + q * n + org;
   tm.fl = reinterpret_cast<unsigned char*>(base + 9 * n) + org;
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
-  oeb_status stt = OEB_OK;
-  hadv_adj_terms_kernel<T, ORDER><<<grid_for(*dom), dim3(kTX, kTY), 0, st>>>(
-      tm, gui.origin, gvi.origin, (const T*)acrlat0->aligned + acrlat0->offset,
+  const int kb = tuned_kb(kKB);
+  oeb_status stt = launch<hadv_adj_terms_kernel<T, ORDER>>(
+      grid_for(*dom, kb), 0, st, tm, gui.origin, gvi.origin, (const T*)acrlat0->aligned + acrlat0->offset,
       (const T*)acrlat1->aligned + acrlat1->offset, (const T*)tgrlatda0->aligned + tgrlatda0->offset,
       (const T*)tgrlatda1->aligned + tgrlatda1->offset, acrlat0->strides[0], guo.origin, gvo.origin, eddlat, eddlon, d,
-      kKB);
-  stt = after_launch();
-  if (stt == OEB_OK) {
-    hadv_adj_gather_kernel<T, ORDER>
-        <<<tile_grid(d.nx + 2 * h, d.ny + 2 * h, d.nz, kTI, kTJ, kKB), dim3(kTX, kTY), 0, st>>>(gub.origin, gvb.origin,
-                                                                                              tm, d, kKB);
-    stt = after_launch();
-  }
-  cudaFreeAsync(buf, st);
+      kb);
+  if (stt == OEB_OK)
+    stt = launch<hadv_adj_gather_kernel<T, ORDER>>(tile_grid(d.nx + 2 * h, d.ny + 2 * h, d.nz, kTI, kTJ, kb), 0, st,
+                                                   gub.origin, gvb.origin, tm, d, kb);
+  scratch_free(buf, st);
   return stt;
 }
 

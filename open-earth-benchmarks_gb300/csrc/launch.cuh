@@ -1,0 +1,166 @@
+// launch.cuh -- the one way this library launches a kernel, and the batched persistent form.
+//
+// Every kernel is a Body: a struct with `static __device__ void run(uint3 blk, A... a)` that
+// does the work of the CTA `blk` of its grid (the code that would read blockIdx).  launch<Body>
+// either runs it as an ordinary grid (grid_kernel, blk = blockIdx), or -- while a Recorder is
+// installed on the calling thread -- records the grid and the arguments instead.  A batch plan
+// (batch.cu) records the same sequence of calls for many ensemble members and then replays
+// each recorded position as ONE persistent launch over all members: batch_kernel, whose CTAs
+// walk a list of (member, tile) items.  The bodies never read blockIdx or gridDim, so a tile
+// computes the same results in either form.
+//
+// Scratch memory of a call (adjoint terms, dual-number arrays) comes from scratch_alloc: the
+// library's stream-ordered pool normally, the plan's arena while recording (so that it lives
+// as long as the plan).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <utility>
+#include <vector>
+
+#include "oeb_common.cuh"
+
+namespace oeb {
+
+constexpr int kLaunchTX = 32, kLaunchTY = 8;  // every CTA is 32 x 8 threads
+
+// ---- argument packs (trivially copyable, identical layout on host and device) -------
+template <class... A>
+struct Pack;
+template <>
+struct Pack<> {};
+template <class H, class... R>
+struct Pack<H, R...> {
+  H h;
+  Pack<R...> r;
+};
+
+inline Pack<> make_pack() { return {}; }
+template <class H, class... R>
+Pack<H, R...> make_pack(H h, R... r) {
+  return Pack<H, R...>{h, make_pack(r...)};
+}
+
+template <class Body, class... Done>
+__device__ __forceinline__ void call_pack(const uint3& blk, const Pack<>&, const Done&... d) {
+  Body::run(blk, d...);
+}
+template <class Body, class H, class... R, class... Done>
+__device__ __forceinline__ void call_pack(const uint3& blk, const Pack<H, R...>& p, const Done&... d) {
+  call_pack<Body>(blk, p.r, d..., p.h);
+}
+
+// ---- kernels ----------------------------------------------------------------------------
+template <class Body, class... A>
+__global__ void __launch_bounds__(kLaunchTX* kLaunchTY) grid_kernel(A... a) {
+  Body::run(blockIdx, a...);
+}
+
+// One item per (member, tile); tiles[m] = {first item of member m, tiles along x, along y}.
+struct BatchTile {
+  int first, gx, gy, pad;
+};
+
+template <class Body, class... A>
+__global__ void __launch_bounds__(kLaunchTX* kLaunchTY)
+    batch_kernel(const BatchTile* __restrict__ tiles, int members, int total, const Pack<A...>* __restrict__ args) {
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int lo = 0, hi = members - 1;  // last member whose first item is <= item
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tiles[mid].first <= item) lo = mid; else hi = mid - 1;
+    }
+    const BatchTile t = tiles[lo];
+    const int local = item - t.first;
+    const int plane = t.gx * t.gy;
+    const uint3 blk = make_uint3((unsigned)(local % t.gx), (unsigned)((local % plane) / t.gx),
+                                 (unsigned)(local / plane));
+    const Pack<A...> a = args[lo];
+    call_pack<Body>(blk, a);
+    __syncthreads();  // the next item reuses the shared memory
+  }
+}
+
+// ---- recording ----------------------------------------------------------------------------
+// Launches one recorded position for `members` members: tiles and args are device arrays.
+using BatchLaunchFn = oeb_status (*)(const BatchTile* tiles, int members, int total, const void* args, size_t smem,
+                                     int ctas, cudaStream_t st);
+// CTAs of batch_kernel that fit on one SM with `smem` dynamic shared memory.
+using BatchOccupancyFn = int (*)(size_t smem);
+
+struct LaunchRecord {
+  BatchLaunchFn launcher;  // also identifies the kernel (Body and argument types)
+  BatchOccupancyFn occupancy;
+  dim3 grid;
+  size_t smem;
+  std::vector<unsigned char> args;  // Pack<A...>
+};
+
+struct Recorder {
+  std::vector<LaunchRecord> records;
+  char* arena = nullptr;  // scratch arena (nullptr: sizing pass, addresses are placeholders)
+  size_t arena_bytes = 0;
+  size_t used = 0;  // top of the arena stack
+  size_t peak = 0;  // the most it held
+  // live allocations, oldest first: {offset, freed}.  A call's scratch is freed when the call
+  // returns; the stack pops every freed allocation on its top, so later calls reuse the space
+  // (safe: a batch runs each recorded launch for all members before the next one).
+  std::vector<std::pair<size_t, bool>> live;
+  int kb = 0;  // k-levels per CTA for the kernels that take one (0: their default)
+};
+
+Recorder* recorder();             // the calling thread's recorder, or nullptr
+void set_recorder(Recorder* r);  // installs (or with nullptr removes) it
+// k-levels per CTA: the recorder's choice while recording, else `def`.
+inline int tuned_kb(int def) {
+  const Recorder* r = recorder();
+  return (r && r->kb > 0) ? r->kb : def;
+}
+
+oeb_status scratch_alloc(void** p, size_t bytes, cudaStream_t st);
+void scratch_free(void* p, cudaStream_t st);
+
+template <class Body, class... A>
+oeb_status batch_launch(const BatchTile* tiles, int members, int total, const void* args, size_t smem, int ctas,
+                        cudaStream_t st) {
+  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)batch_kernel<Body, A...>, (int)smem));
+  batch_kernel<Body, A...><<<ctas, dim3(kLaunchTX, kLaunchTY), smem, st>>>(
+      tiles, members, total, static_cast<const Pack<A...>*>(args));
+  return after_launch();
+}
+
+template <class Body, class... A>
+int batch_occupancy(size_t smem) {
+  if (smem > 48 * 1024 && ensure_dyn_smem((const void*)batch_kernel<Body, A...>, (int)smem) != OEB_OK) return 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<Body, A...>, kLaunchTX * kLaunchTY, smem) !=
+          cudaSuccess ||
+      n < 1)
+    n = 1;
+  return n;
+}
+
+template <class Body, class... A>
+oeb_status launch(dim3 grid, size_t smem, cudaStream_t st, A... a) {
+  if (grid.x == 0 || grid.y == 0 || grid.z == 0) return OEB_OK;
+  if (Recorder* r = recorder()) {
+    LaunchRecord rec;
+    rec.launcher = &batch_launch<Body, A...>;
+    rec.occupancy = &batch_occupancy<Body, A...>;
+    rec.grid = grid;
+    rec.smem = smem;
+    const Pack<A...> p = make_pack(a...);
+    rec.args.resize(sizeof(p));
+    memcpy(rec.args.data(), &p, sizeof(p));
+    r->records.push_back(std::move(rec));
+    return OEB_OK;
+  }
+  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_kernel<Body, A...>, (int)smem));
+  grid_kernel<Body, A...><<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(a...);
+  return after_launch();
+}
+
+}  // namespace oeb

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "launch.cuh"
 #include "oeb_common.cuh"
 
 namespace oeb {
@@ -47,21 +48,22 @@ __host__ __device__ constexpr T earth_radius_recip() {
 }
 
 // Visits, for this thread, the cells (i, j, k) of the box [ilo, ilo+ni) x [jlo, jlo+nj) x
-// [k0, k0+kb) of its CTA: blockIdx.x/y pick a 32 x 32 tile, each thread takes 4 rows.
+// [k0, k0+kb) of its CTA: blk.x/y pick a 32 x 32 tile, each thread takes 4 rows.
 // f(o, i, j) gets the plane-plus-in-plane offset o of (i, j, k) from the interior origin.
 template <class F>
-__device__ __forceinline__ void for_box(const Dims& d, int ilo, int jlo, int ni, int nj, int kb, F&& f) {
-  const int a = (int)(blockIdx.x * 32 + threadIdx.x);
+__device__ __forceinline__ void for_box(const uint3& blk, const Dims& d, int ilo, int jlo, int ni, int nj, int kb,
+                                        F&& f) {
+  const int a = (int)(blk.x * 32 + threadIdx.x);
   if (a >= ni) return;
   const int i = ilo + a;
-  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, d.nz);
+  const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
   const int sj = (int)d.sj;
 #pragma unroll 1
   for (int k = k0; k < k1; ++k) {
     const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll
     for (int r = 0; r < 32 / kTY; ++r) {
-      const int b = (int)(blockIdx.y * 32 + threadIdx.y) + kTY * r;
+      const int b = (int)(blk.y * 32 + threadIdx.y) + kTY * r;
       if (b < nj) f(kofs + i + (jlo + b) * sj, i, jlo + b);
     }
   }

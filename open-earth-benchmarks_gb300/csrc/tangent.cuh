@@ -4,8 +4,8 @@
 // Jacobian at the state x applied to the perturbation dx of its active inputs, with every
 // branch frozen at x.  The kernel is the forward kernel instantiated with Dual<T>:
 //   1. each input field is packed into a Dual array in the field's own layout (value from x,
-//      derivative from dx for active inputs, 0 for parameters), in device scratch from the
-//      stream-ordered pool;
+//      derivative from dx for active inputs, 0 for parameters), in device scratch
+//      (scratch_alloc: the stream-ordered pool, or a batch plan's arena);
 //   2. the forward kernel runs on the Dual arrays;
 //   3. the derivative part of each output is copied to dy over the output's written box.
 // Scratch is returned to the pool on every exit path.
@@ -16,27 +16,36 @@
 
 #include "dual.cuh"
 #include "oeb_common.cuh"
+#include "stencil_util.cuh"
 
 namespace oeb {
 
+constexpr int kFlatThreads = kTX * kTY;
+
 template <class T>
-__global__ void pack_dual_kernel(Dual<T>* __restrict__ out, const T* __restrict__ v, const T* __restrict__ d,
-                                 int64_t n) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    out[e] = Dual<T>(v[e], d ? d[e] : T(0));
-}
+struct pack_dual_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, Dual<T>* __restrict__ out, const T* __restrict__ v,
+                                             const T* __restrict__ d, int64_t n) {
+    const int64_t e = (int64_t)blk.x * kFlatThreads + threadIdx.y * kTX + threadIdx.x;
+    if (e < n) out[e] = Dual<T>(v[e], d ? d[e] : T(0));
+  }
+};
 
 // dy(box) = derivative part of y(box); box = [-ilo, nx+ihi) x [-jlo, ny+jhi) x [-klo, nz+khi)
 template <class T>
-__global__ void unpack_deriv_kernel(T* __restrict__ dy, const Dual<T>* __restrict__ y, int ni, int nj, int nk,
-                                    int64_t sj, int64_t sk) {
-  const int64_t n = (int64_t)ni * nj * nk;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+struct unpack_deriv_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ dy, const Dual<T>* __restrict__ y,
+                                             int ni, int nj, int nk, int64_t sj, int64_t sk) {
+    const int64_t n = (int64_t)ni * nj * nk;
+    const int64_t e = (int64_t)blk.x * kFlatThreads + threadIdx.y * kTX + threadIdx.x;
+    if (e >= n) return;
     const int64_t i = e % ni, r = e / ni, j = r % nj, k = r / nj;
     const int64_t o = i + j * sj + k * sk;
     dy[o] = y[o].d;
   }
-}
+};
+
+inline dim3 flat_grid(int64_t n) { return dim3((unsigned)((n + kFlatThreads - 1) / kFlatThreads)); }
 
 // Device scratch of one tangent-linear call.
 template <class T>
@@ -44,7 +53,7 @@ class DualArrays {
  public:
   explicit DualArrays(cudaStream_t s) : s_(s) {}
   ~DualArrays() {
-    for (void* p : bufs_) cudaFreeAsync(p, s_);
+    for (void* p : bufs_) scratch_free(p, s_);
   }
 
   // Dual copy of the field described by `x` (derivative from `dx` if given, else 0), in
@@ -61,20 +70,12 @@ class DualArrays {
       if (dx->offset != x->offset || (dx->aligned - dx->allocated) != (x->aligned - x->allocated))
         return OEB_ERR_LAYOUT;
     }
-    cudaMemPool_t pool;
-    OEB_TRY(device_pool(&pool));
     void* buf = nullptr;
-    cudaError_t e = cudaMallocFromPoolAsync(&buf, (size_t)n * sizeof(Dual<T>), pool, s_);
-    if (e != cudaSuccess) {
-      cuda_fail(e);
-      return OEB_ERR_ALLOC;
-    }
+    OEB_TRY(scratch_alloc(&buf, (size_t)n * sizeof(Dual<T>), s_));
     bufs_.push_back(buf);
     Dual<T>* base = static_cast<Dual<T>*>(buf);
     const T* dstart = dx ? ((dx->allocated && dx->allocated <= dx->aligned) ? dx->allocated : dx->aligned) : nullptr;
-    pack_dual_kernel<T><<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s_>>>(base, start, dstart,
-                                                                                                n);
-    OEB_TRY(after_launch());
+    OEB_TRY(launch<pack_dual_kernel<T>>(flat_grid(n), 0, s_, base, start, dstart, n));
     *origin = base + (x->aligned - start) + x->offset;
     return OEB_OK;
   }
@@ -91,9 +92,7 @@ class DualArrays {
     const int ni = (int)(d.nx + r.ilo + r.ihi), nj = (int)(d.ny + r.jlo + r.jhi), nk = (int)(d.nz + r.klo + r.khi);
     const int64_t first = -(int64_t)r.ilo - (int64_t)r.jlo * sj - (int64_t)r.klo * sk;
     const int64_t n = (int64_t)ni * nj * nk;
-    unpack_deriv_kernel<T><<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s_>>>(
-        dy_origin + first, origin + first, ni, nj, nk, sj, sk);
-    return after_launch();
+    return launch<unpack_deriv_kernel<T>>(flat_grid(n), 0, s_, dy_origin + first, origin + first, ni, nj, nk, sj, sk);
   }
 
  private:
@@ -103,14 +102,8 @@ class DualArrays {
     int64_t last = 0;
     for (size_t r = 0; r < 3; ++r) last += (y->sizes[r] - 1) * y->strides[r];
     const int64_t n = (int64_t)(y->aligned - start) + last + 1;
-    cudaMemPool_t pool;
-    OEB_TRY(device_pool(&pool));
     void* buf = nullptr;
-    cudaError_t e = cudaMallocFromPoolAsync(&buf, (size_t)n * sizeof(Dual<T>), pool, s_);
-    if (e != cudaSuccess) {
-      cuda_fail(e);
-      return OEB_ERR_ALLOC;
-    }
+    OEB_TRY(scratch_alloc(&buf, (size_t)n * sizeof(Dual<T>), s_));
     bufs_.push_back(buf);
     *origin = static_cast<Dual<T>*>(buf) + (y->aligned - start) + y->offset;
     return OEB_OK;

@@ -257,3 +257,93 @@ def make_chain_scalars(seed: int) -> Dict[str, float]:
     return {"edadlat": fw["edadlat"], "dt": fw["dt"], "eddlat": adv["eddlat"], "eddlon": adv["eddlon"],
             "dt_adv": CHAIN_DT_ADV, "tau_smag": smag["tau_smag"], "weight_smag": smag["weight_smag"],
             "ppm_p1": fv["p1"], "ppm_p2": fv["p2"]}
+
+
+# ---- the same generators on the device (torch), for workloads too large for numpy -------
+# Same formulas and distributions as above; the random streams are torch's, so values differ
+# from the numpy generators for the same seed.
+def _t_grid(nx, ny, nz, halo, device, torch):
+    i = torch.arange(-halo, nx + halo, dtype=torch.float64, device=device)[None, None, :]
+    j = torch.arange(-halo, ny + halo, dtype=torch.float64, device=device)[None, :, None]
+    k = torch.arange(-halo, nz + halo, dtype=torch.float64, device=device)[:, None, None]
+    return i, j, k
+
+
+def _t_modes(g, nx, ny, nz, gen, torch, vertical=True, nmodes=3, kmax=4):
+    i, j, k = g
+    shape = (k.shape[0], j.shape[1], i.shape[2])
+    out = torch.zeros(shape, dtype=torch.float64, device=i.device)
+    for _ in range(nmodes):
+        kx, ky = (int(v) for v in torch.randint(1, kmax + 1, (2,), generator=gen))
+        phi, psi, chi = (float(v) * 2 * np.pi for v in torch.rand(3, generator=gen, dtype=torch.float64))
+        mode = torch.sin(2 * np.pi * kx * i / nx + phi) * torch.cos(2 * np.pi * ky * j / ny + psi)
+        if vertical:
+            kz = int(torch.randint(1, 3, (1,), generator=gen))
+            mode = mode * (1.0 + 0.5 * torch.sin(2 * np.pi * kz * k / max(nz, 1) + chi))
+        out += mode.expand(shape)
+    return out
+
+
+def make_chain_inputs_device(nx: int, ny: int, nz: int, seed: int, device, dtype=np.float64,
+                             halo: int = CHAIN_HALO):
+    """Inputs of the chained step (CHAIN_SOURCES) made on `device` with the "physical"
+    generators; returns torch tensors, whole allocations with the halo."""
+    import torch
+    g = _t_grid(nx, ny, nz, halo, device, torch)
+    i, j, k = g
+    shape = (k.shape[0], j.shape[1], i.shape[2])
+    tdt = torch.float64 if np.dtype(dtype) == np.float64 else torch.float32
+    out = {}
+    for idx, (name, (kernel, arg)) in enumerate(CHAIN_SOURCES.items()):
+        gen = torch.Generator(device="cpu").manual_seed(int(seed) * 1000003 + idx * 7919)
+        dgen = torch.Generator(device=device).manual_seed(int(seed) * 1000003 + idx * 7919 + 1)
+        cls = _CLASSES[kernel][arg]
+        rank1 = name in ("fx", "acrlat0", "acrlat1", "tgrlatda0", "tgrlatda1", "crlavo", "crlavu", "crlato", "crlatu",
+                         "smag_acrlat0")
+        if rank1:
+            a = 1.0 + 0.1 * torch.rand(ny + 2 * halo, generator=dgen, device=device, dtype=torch.float64)
+        elif cls == "vel":
+            a = 10.0 * _t_modes(g, nx, ny, nz, gen, torch) + 0.1 * torch.randn(shape, generator=dgen, device=device,
+                                                                                dtype=torch.float64)
+        elif cls == "tend":
+            a = 1e-3 * (10.0 * _t_modes(g, nx, ny, nz, gen, torch) +
+                        0.1 * torch.randn(shape, generator=dgen, device=device, dtype=torch.float64))
+        elif cls == "unit":
+            a = torch.rand(shape, generator=dgen, device=device, dtype=torch.float64)
+        elif cls == "weight":
+            a = 0.4 + 0.2 * torch.rand(shape, generator=dgen, device=device, dtype=torch.float64)
+        elif cls == "ppert":
+            a = 100.0 * _t_modes(g, nx, ny, nz, gen, torch) + torch.randn(shape, generator=dgen, device=device,
+                                                                          dtype=torch.float64)
+        elif cls == "height":
+            frac = k / max(nz, 1)
+            a = 20000.0 * (1.0 - frac) * (1.0 + 0.01 * _t_modes(g, nx, ny, nz, gen, torch, vertical=False) / 3.0)
+        elif cls == "density":
+            a = 1.2 * (1.0 + 0.01 * _t_modes(g, nx, ny, nz, gen, torch))
+        elif cls == "tracer":
+            a = _t_modes(g, nx, ny, nz, gen, torch) + 0.05 * torch.randn(shape, generator=dgen, device=device,
+                                                                         dtype=torch.float64)
+            a -= a.mean()
+        elif cls == "courant":
+            a = _t_modes(g, nx, ny, nz, gen, torch) + 0.05 * torch.randn(shape, generator=dgen, device=device,
+                                                                         dtype=torch.float64)
+            a = 0.8 * a / a.abs().max()
+        elif cls == "area":
+            a = 1.0 + 0.1 * _t_modes(g, nx, ny, nz, gen, torch) / 3.0
+        else:
+            raise KeyError(cls)
+        out[name] = a.expand(shape).to(tdt).contiguous() if a.dim() == 3 else a.to(tdt).contiguous()
+    return out
+
+
+def ensemble_members(count: int = 48, seed: int = 4):
+    """The uneven ensemble: nx, ny uniform in {48, 64, ..., 320}, nz in {40, 60, 80, 137},
+    FP64 or FP32 with equal odds.  Returns [(nx, ny, nz, itemsize)]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.arange(48, 321, 16)
+    out = []
+    for _ in range(count):
+        nx, ny = (int(v) for v in rng.choice(sizes, size=2))
+        nz = int(rng.choice([40, 60, 80, 137]))
+        out.append((nx, ny, nz, 8 if rng.random() < 0.5 else 4))
+    return out

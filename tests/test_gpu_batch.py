@@ -1,0 +1,126 @@
+"""Batched ensembles: the chained step of uneven, mixed-precision members as persistent launches.
+
+Every member's forward outputs and adjoint gradients from oeb_batch_run must be
+bit-identical to the same member run alone through oeb_chain_forward_* / oeb_chain_adj_*
+(the same kernels on the same tiles), after the autotuner has changed the k-blocking and
+CTA counts, and when the run is replayed from a CUDA graph after the inputs change in place.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import assert_bitwise_equal
+
+pytestmark = pytest.mark.gpu
+
+H = 8
+SENTINEL = -7.0e5
+# (nx, ny, nz, dtype): uneven, ragged tiles, both precisions
+MEMBERS = [(48, 64, 7, np.float64), (80, 48, 5, np.float32), (64, 96, 9, np.float64), (33, 41, 3, np.float32),
+           (17, 17, 2, np.float64), (128, 112, 12, np.float32), (1, 1, 1, np.float64)]
+
+
+def _member(pkg, fields, chain, cuda, nx, ny, nz, dtype, seed):
+    import torch
+    x = fields.make_chain_inputs(nx, ny, nz, seed, halo=H)
+    s = fields.make_chain_scalars(seed)
+    shape = x["u"].shape
+
+    def dev(a):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        return pkg.Storage(torch.from_numpy(a).to(cuda), H, nx=nx if a.ndim == 3 else None)
+
+    rng = np.random.default_rng([seed, 9])
+    seeds = {}
+    for n in chain.OUTPUTS:
+        y = np.zeros(shape)
+        y[H:H + nz, H:H + ny, H:H + nx] = rng.normal(0.0, 1.0, size=(nz, ny, nx))
+        seeds[n] = dev(y)
+    return {"fields": {k: dev(v) for k, v in x.items()}, "scalars": s, "domain": (nx, ny, nz),
+            "outs": {n: dev(np.full(shape, SENTINEL)) for n in chain.OUTPUTS},
+            "seeds": seeds, "grads": {n: dev(np.full(shape, SENTINEL)) for n in ("u", "v")},
+            "dev": dev, "shape": shape}
+
+
+def _alone(chain, m):
+    """The member through its own chain plan, into fresh buffers."""
+    import torch
+    plan = chain.ChainPlan(m["fields"]["u"], m["domain"], chain.FORWARD | chain.ADJOINT)
+    outs = {n: m["dev"](np.full(m["shape"], SENTINEL)) for n in chain.OUTPUTS}
+    grads = {n: m["dev"](np.full(m["shape"], SENTINEL)) for n in ("u", "v")}
+    plan.forward(m["fields"], m["scalars"], outs)
+    plan.adjoint(m["fields"], m["scalars"], m["seeds"], grads)
+    torch.cuda.synchronize()
+    plan.close()
+    return {n: v.numpy() for n, v in outs.items()}, {n: v.numpy() for n, v in grads.items()}
+
+
+def _check(chain, members, what):
+    for i, m in enumerate(members):
+        outs, grads = _alone(chain, m)
+        for n in chain.OUTPUTS:
+            assert_bitwise_equal(m["outs"][n].numpy(), outs[n], "%s member %d %s" % (what, i, n))
+        for n in ("u", "v"):
+            assert_bitwise_equal(m["grads"][n].numpy(), grads[n], "%s member %d grad %s" % (what, i, n))
+
+
+@pytest.fixture(scope="module")
+def chain(pkg):
+    import importlib
+    return importlib.import_module("oeb_gb300.chain")
+
+
+def test_batch_matches_members_run_alone(pkg, fields, chain, cuda):
+    import torch
+    members = [_member(pkg, fields, chain, cuda, nx, ny, nz, dt, 40 + i) for i, (nx, ny, nz, dt) in enumerate(MEMBERS)]
+    plan = chain.BatchPlan(members, chain.FORWARD | chain.ADJOINT)
+    assert plan.points == sum(nx * ny * nz for nx, ny, nz, _ in MEMBERS)
+    lib = pkg.load_library()
+    before = lib.oeb_launch_count()
+    plan.run()
+    torch.cuda.synchronize()
+    assert lib.oeb_launch_count() - before == plan.launches
+    _check(chain, members, "batch")
+    # the autotuner changes k-blocking and CTA counts, not results
+    plan.autotune()
+    for m in members:
+        for st in list(m["outs"].values()) + list(m["grads"].values()):
+            st.data.fill_(SENTINEL)
+    plan.run()
+    torch.cuda.synchronize()
+    _check(chain, members, "autotuned batch")
+    plan.close()
+
+
+def test_batch_graph_replay(pkg, fields, chain, cuda):
+    import torch
+    members = [_member(pkg, fields, chain, cuda, nx, ny, nz, dt, 60 + i)
+               for i, (nx, ny, nz, dt) in enumerate(MEMBERS[:4])]
+    plan = chain.BatchPlan(members, chain.FORWARD | chain.ADJOINT)
+    stream = torch.cuda.Stream()
+    plan.run(stream)  # one-time set-up outside the capture
+    stream.synchronize()
+    g = chain.Graph(stream)
+    with g:
+        plan.run(stream)
+    for i, m in enumerate(members):  # new inputs in place
+        nx, ny, nz = m["domain"]
+        x2 = fields.make_chain_inputs(nx, ny, nz, 90 + i, halo=H)
+        for k in ("u", "v", "utens", "mask", "crx"):
+            m["fields"][k].data.copy_(torch.from_numpy(x2[k].astype(MEMBERS[i][3])).to(cuda))
+        for st in list(m["outs"].values()) + list(m["grads"].values()):
+            st.data.fill_(SENTINEL)
+    torch.cuda.synchronize()
+    g.launch(stream)
+    stream.synchronize()
+    _check(chain, members, "graph")
+    g.close()
+    plan.close()
+
+
+def test_batch_rejects_a_member_without_outputs(pkg, fields, chain, cuda):
+    m = _member(pkg, fields, chain, cuda, 16, 16, 2, np.float64, 7)
+    del m["outs"]
+    with pytest.raises(pkg.OebError):
+        chain.BatchPlan([m], chain.FORWARD)
