@@ -83,5 +83,35 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     return LIB
 
 
+DRIVER_DIR = PKG / "driver"
+DRIVER = PKG / "oeb_driver"
+DRIVER_UNITS = ("oeb_driver_main.cpp", "oeb_driver_f64.cpp", "oeb_driver_f32.cpp")
+
+
+def _cuda_home() -> Path:
+    return Path(nvcc()).resolve().parent.parent if Path(nvcc()).exists() else Path("/usr/local/cuda")
+
+
+def build_driver(force: bool = False) -> Path:
+    """The GPU driver (driver/): a reference-style C++ program over the drop-in headers,
+    linked against liboeb_gb300.so; returns its path."""
+    lib = build()
+    deps = [*(DRIVER_DIR / u for u in DRIVER_UNITS), *DRIVER_DIR.glob("*.h"), *DRIVER_DIR.glob("*.inc"),
+            *(REPO / "include" / "oeb").glob("*"), REPO / "include" / "oeb_gb300.h", lib]
+    if not force and not _stale(DRIVER, deps):
+        return DRIVER
+    cuda = _cuda_home()
+    cxx = os.environ.get("CXX", "g++")
+    tmp = DRIVER.with_suffix(".tmp")
+    cmd = [cxx, "-std=c++17", "-O2", "-I", str(REPO / "include" / "oeb"), "-I", str(REPO / "include"), "-I",
+           str(DRIVER_DIR), "-I", str(cuda / "include"), *(str(DRIVER_DIR / u) for u in DRIVER_UNITS), "-L", str(PKG),
+           "-loeb_gb300", "-L", str(cuda / "lib64"), "-lcudart", "-Wl,-rpath," + str(PKG), "-o", str(tmp)]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("driver build failed: %s\n%s" % (" ".join(cmd), proc.stderr))
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))

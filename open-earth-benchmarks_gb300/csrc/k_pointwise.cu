@@ -163,46 +163,59 @@ struct nh_p_grad_kernel {
 
 // ---- hadvuv / hadvuv5th: kernels/hadvuv.h:4-27,178-210 and kernels/hadvuv5th.h:4-39,177-201
 
+// The upwind sums without a branch.  Both branches of the reference's drivers are one
+// left-to-right sum of the same shape -- products, one plain term, products -- and differ
+// only in which coefficients and neighbours fill the slots.  Each lane selects its operands
+// (integer selects, no FP64 work) and then performs exactly the operation sequence of its
+// branch: the FP64 results are bit-identical to the branchy form, and a warp whose lanes
+// disagree on the upwind direction no longer runs both branches.  (a > 0 ? a : -a) * sum
+// is the reference's `-uavg * (...)`, the negation being exact.
+
 // 3rd-order upwind advection along one axis (stride s): hadvuv.h:10-16 (x) and :18-24 (y).
+//   a > 0:  ((c6 f[-2] + f[-1]) + ch f[0]) + c3 f[1]
+//   else :  ((c3 f[-1] + ch f[0]) + f[1]) + c6 f[2]
 template <class T>
 __device__ __forceinline__ T adv3_axis(const T* __restrict__ f, int64_t o, int64_t s, T a) {
   constexpr T c6 = T(-1.0) / T(6.0), c3 = T(-1.0) / T(3.0), ch = T(-0.5);
-  if (a > 0) {
-    Acc<T> acc = Acc<T>::prod(c6, ld(f + o - 2 * s));
-    acc.add(ld(f + o - s));
-    acc.add_prod(ch, ld(f + o));
-    acc.add_prod(c3, ld(f + o + s));
-    return a * acc.get();
+  const bool pos = a > 0;
+  const T fa = ld(f + o + (pos ? -2 : -1) * s), fb = ld(f + o - s), f0 = ld(f + o), fc = ld(f + o + s),
+          fd = ld(f + o + (pos ? 1 : 2) * s);
+  if constexpr (Prec<T>::kCompensated) {
+    // FP32: every term through TwoProduct (a plain term is a product by 1, exactly)
+    Acc<T> acc = Acc<T>::prod(pos ? c6 : c3, fa);
+    acc.add_prod(pos ? T(1.0) : ch, pos ? fb : f0);
+    acc.add_prod(pos ? ch : T(1.0), pos ? f0 : fc);
+    acc.add_prod(pos ? c3 : c6, fd);
+    return (pos ? a : -a) * acc.get();
   } else {
-    Acc<T> acc = Acc<T>::prod(c3, ld(f + o - s));
-    acc.add_prod(ch, ld(f + o));
-    acc.add(ld(f + o + s));
-    acc.add_prod(c6, ld(f + o + 2 * s));
-    return -a * acc.get();
+    const T p0 = (pos ? c6 : c3) * fa, ph = ch * f0, p3 = (pos ? c3 : c6) * fd;
+    return (pos ? a : -a) * (((p0 + (pos ? fb : ph)) + (pos ? ph : fc)) + p3);
   }
 }
 
 // 5th-order upwind advection along one axis: hadvuv5th.h:10-22 (x) and :24-36 (y).
+//   a > 0:  ((((c30 f[-3] + c4 f[-2]) + f[-1]) + c3 f[0]) + c2 f[1]) + c20 f[2]
+//   else :  ((((c20 f[-2] + c2 f[-1]) + c3 f[0]) + f[1]) + c4 f[2]) + c30 f[3]
 template <class T>
 __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64_t s, T a) {
   constexpr T c30 = T(1.0) / T(30.0), c4 = T(-1.0) / T(4.0), c3 = T(-1.0) / T(3.0), c2 = T(-1.0) / T(2.0),
               c20 = T(1.0) / T(20.0);
-  if (a > 0) {
-    Acc<T> acc = Acc<T>::prod(c30, ld(f + o - 3 * s));
-    acc.add_prod(c4, ld(f + o - 2 * s));
-    acc.add(ld(f + o - s));
-    acc.add_prod(c3, ld(f + o));
-    acc.add_prod(c2, ld(f + o + s));
-    acc.add_prod(c20, ld(f + o + 2 * s));
-    return a * acc.get();
+  const bool pos = a > 0;
+  const int64_t sh = pos ? 0 : s;  // the negative branch reads one cell further along the axis
+  const T x0 = ld(f + o - 3 * s + sh), x1 = ld(f + o - 2 * s + sh), fm1 = ld(f + o - s), f0 = ld(f + o),
+          fp1 = ld(f + o + s), x4 = ld(f + o + s + sh), x5 = ld(f + o + 2 * s + sh);
+  if constexpr (Prec<T>::kCompensated) {
+    Acc<T> acc = Acc<T>::prod(pos ? c30 : c20, x0);
+    acc.add_prod(pos ? c4 : c2, x1);
+    acc.add_prod(pos ? T(1.0) : c3, pos ? fm1 : f0);
+    acc.add_prod(pos ? c3 : T(1.0), pos ? f0 : fp1);
+    acc.add_prod(pos ? c2 : c4, x4);
+    acc.add_prod(pos ? c20 : c30, x5);
+    return (pos ? a : -a) * acc.get();
   } else {
-    Acc<T> acc = Acc<T>::prod(c20, ld(f + o - 2 * s));
-    acc.add_prod(c2, ld(f + o - s));
-    acc.add_prod(c3, ld(f + o));
-    acc.add(ld(f + o + s));
-    acc.add_prod(c4, ld(f + o + 2 * s));
-    acc.add_prod(c30, ld(f + o + 3 * s));
-    return -a * acc.get();
+    const T p0 = (pos ? c30 : c20) * x0, p1 = (pos ? c4 : c2) * x1, pm = c3 * f0, p4 = (pos ? c2 : c4) * x4,
+            p5 = (pos ? c20 : c30) * x5;
+    return (pos ? a : -a) * (((((p0 + p1) + (pos ? fm1 : pm)) + (pos ? pm : fp1)) + p4) + p5);
   }
 }
 

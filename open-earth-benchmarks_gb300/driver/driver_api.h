@@ -1,0 +1,19 @@
+// driver_api.h -- what the GPU driver's main() needs from its two precision translation units.
+#ifndef OEB_DRIVER_API_H
+#define OEB_DRIVER_API_H
+
+#include <cstdint>
+
+// the globals every reference driver defines (src/<k>.cpp:4-7); set by main() from the CLI
+extern int64_t domain_size;
+extern int64_t domain_height;
+extern int64_t halo_width;
+
+namespace oeb_driver {
+struct Result;
+}
+
+bool oeb_driver_run_f64(const char* kernel, int algo, int count, oeb_driver::Result* r);
+bool oeb_driver_run_f32(const char* kernel, int algo, int count, oeb_driver::Result* r);
+
+#endif  // OEB_DRIVER_API_H
