@@ -114,6 +114,10 @@ OEB_API uint64_t oeb_launch_count(void);
 OEB_API int oeb_is_device_pointer(const void* p);
 /* Blocks until all work on `stream` has finished (NULL = legacy default stream). */
 OEB_API oeb_status oeb_stream_synchronize(void* stream);
+/* k-levels each CTA of the tiled stencils covers (1..1024), for every later call on every
+ * thread; 0 (the default) restores each kernel's own choice.  A tuning knob: results do not
+ * depend on it.  Batch plans record and tune their own. */
+OEB_API oeb_status oeb_set_kblock(int kb);
 
 /* ------------------------------------------------------------------------- */
 /* Device storage (the device twin of allocateStorage/freeStorage,           */

@@ -55,7 +55,10 @@ bool capture_counting() { return t_capturing; }
 
 namespace {
 thread_local Recorder* t_recorder = nullptr;
+std::atomic<int> g_kb_override{0};
 }  // namespace
+
+int kb_override() { return g_kb_override.load(std::memory_order_relaxed); }
 
 Recorder* recorder() { return t_recorder; }
 void set_recorder(Recorder* r) { t_recorder = r; }
@@ -368,3 +371,9 @@ static int64_t span_bytes(const M* m) {
 
 extern "C" int64_t oeb_memref3d_span_bytes_f64(const oeb_memref3d_f64* m) { return span_bytes<oeb_memref3d_f64, double>(m); }
 extern "C" int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m) { return span_bytes<oeb_memref3d_f32, float>(m); }
+
+extern "C" oeb_status oeb_set_kblock(int kb) {
+  if (kb < 0 || kb > 1024) return OEB_ERR_ARGUMENT;
+  oeb::g_kb_override.store(kb, std::memory_order_relaxed);
+  return OEB_OK;
+}

@@ -102,7 +102,7 @@ struct combine_kernel {
   }
 };
 
-constexpr int kBoxKB = 4;
+constexpr int kBoxKB = 1;
 
 // A 3-D descriptor whose origin is shifted by -e in i and j (the same memory).
 template <class M>

@@ -1,7 +1,7 @@
 // k_fastwavesuv.cu -- fastwavesuv (kernels/fastwavesuv.h:154-191) in FP64 and FP32.
 //
 // The OpenMP variant evaluates ppgk = wgtfac*ppuv + (1-wgtfac)*ppuv(k-1) six times per point
-// ((i,j),(i+1,j),(i,j+1) at k and k+1).  Here each CTA marches upward through KB k-levels
+// ((i,j),(i+1,j),(i,j+1) at k and k+1).  Here each CTA marches upward through kb k-levels
 // of a 32 x 32 tile: at level k every point of the tile plus a one-cell apron in i and j
 // computes ppgk(k+1) once, keeps it in a register for level k+1, and publishes
 // ppgc = ppgk(k+1) - ppgk(k) and the hhl sum and difference of its column through shared
@@ -115,7 +115,8 @@ struct fastwavesuv_kernel {
   }
 };
 
-constexpr int kKB = 4;
+constexpr int kKB = 1;     // k-levels per CTA by default (the most CTAs hide latency best)
+constexpr int kAdjKB = 4;  // the adjoint's k-levels per CTA
 
 template <class T, class M3, class M1>
 oeb_status fastwavesuv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* utens,
@@ -333,7 +334,9 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   OEB_RETURN_IF_VALIDATING();
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gw.sj, gw.sk};
   const T ed2 = T(2.0) * edadlat;
-  const int kb = tuned_kb(kKB);
+  // the adjoint carries a three-level window of ppgc/hhl terms up the column: longer
+  // k-blocks reuse it (4 levels: 0.68 ms against 0.89 ms for 1 at 128 x 128 x 80, FP64)
+  const int kb = tuned_kb(kAdjKB);
   return launch<fastwavesuv_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
                                            sizeof(FastwavesAdjSmem<T>), (cudaStream_t)stream, gub.origin, gvb.origin,
                                            gutb.origin, gvtb.origin, gpb.origin, gw.origin, gh.origin, gr.origin,

@@ -261,7 +261,7 @@ struct fvtp2d_flux_kernel {
   }
 };
 
-constexpr int kKB = 4;
+constexpr int kKB = 1;  // k-levels per CTA by default (the most CTAs hide latency best)
 
 template <class T, class M3>
 oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* fx2, const M3* fy1, const M3* fy2,

@@ -12,7 +12,7 @@
 // subtracts in the other order (x - y == -(y - x) exactly in IEEE round-to-nearest).
 //
 // Compiled with --fmad=false (see k_pointwise.cu).  One CTA of 32 x 8 threads per
-// 32 x 32 tile and KB k-levels.
+// 32 x 32 tile and kb k-levels.
 #include <mutex>
 #include <vector>
 
@@ -218,7 +218,7 @@ struct hdiffsmag_kernel {
   }
 };
 
-constexpr int kKB = 4;
+constexpr int kKB = 1;  // k-levels per CTA by default (the most CTAs hide latency best)
 
 template <class T, class M3, class M1>
 oeb_status hdiffsa_entry(const M3* out, const M3* in, const M3* mask, const M1* crlato, const M1* crlatu,

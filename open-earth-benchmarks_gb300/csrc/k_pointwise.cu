@@ -10,7 +10,7 @@
 // (precision.cuh): the advection flux sums and the laplacian, and the paired products of
 // the pressure-gradient stencils in float-float.
 //
-// One CTA of 32 x 8 threads covers a 32 x 32 (i, j) tile and KB k-levels; each thread
+// One CTA of 32 x 8 threads covers a 32 x 32 (i, j) tile and kb k-levels; each thread
 // computes 4 rows.  Neighbour reads go through L1.
 #include "precision.cuh"
 #include "stencil_util.cuh"
@@ -266,7 +266,7 @@ struct hadv_kernel {
   }
 };
 
-constexpr int kKB = 4;  // k-levels per CTA
+constexpr int kKB = 1;  // k-levels per CTA (one: the most CTAs, which hides FP64 and load latency best)
 
 template <class T>
 Dims make_dims(const oeb_domain& dom, const Grid<T>& g) {

@@ -114,10 +114,14 @@ struct Recorder {
 
 Recorder* recorder();             // the calling thread's recorder, or nullptr
 void set_recorder(Recorder* r);  // installs (or with nullptr removes) it
-// k-levels per CTA: the recorder's choice while recording, else `def`.
+// k-levels per CTA set by oeb_set_kblock (0: none).
+int kb_override();
+// k-levels per CTA: the recorder's choice while recording, else oeb_set_kblock's, else `def`.
 inline int tuned_kb(int def) {
   const Recorder* r = recorder();
-  return (r && r->kb > 0) ? r->kb : def;
+  if (r && r->kb > 0) return r->kb;
+  const int o = kb_override();
+  return o > 0 ? o : def;
 }
 
 oeb_status scratch_alloc(void** p, size_t bytes, cudaStream_t st);
