@@ -283,7 +283,10 @@ def run_ours(args):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": _algorithmic_bytes(pkg, dom_k),
-                     "launch_ms": round(per_kernel[dom_k], 5)},
+                     "launch_ms": round(per_kernel[dom_k], 5),
+                     "fp64_pipe_active_pct": _ncu_summary(dom_k, "fp64_pipe_active_pct"),
+                     "note": "FP64 stencils are bound by the FP64 pipe (1.6 op/clk/SM on GB300), not HBM; "
+                             "fp64_pipe_active_pct is ncu's sm__pipe_fp64_cycles_active for this kernel"},
         "per_kernel_ms": {k: round(v, 5) for k, v in per_kernel.items()},
         "per_kernel_gbs": {k: round(_algorithmic_bytes(pkg, k) / (v * 1e-3) / 1e9, 1) for k, v in per_kernel.items()},
         "kernel_share": {k: round(v / total_k, 4) for k, v in per_kernel.items()},
@@ -520,18 +523,24 @@ def _batch_leg(pkg, fields, torch, dev, args):
     return res
 
 
-def _ncu_traffic(kernel):
-    """dram bytes per launch of `kernel` from the committed ncu summary, if there is one."""
+def _ncu_summary(kernel, key):
+    """A figure of `kernel`'s committed ncu summary (profiles/ncu_<kernel>_128x128x80.md)."""
     p = ROOT / "profiles" / ("ncu_%s_128x128x80.md" % kernel)
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
-        if ln.startswith("dram_bytes_per_launch:"):
+        if ln.startswith(key + ":"):
             try:
-                return int(float(ln.split(":", 1)[1].strip()))
+                return float(ln.split(":", 1)[1].strip())
             except ValueError:
                 return None
     return None
+
+
+def _ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if there is one."""
+    v = _ncu_summary(kernel, "dram_bytes_per_launch")
+    return int(v) if v is not None else None
 
 
 def _e2e(pkg, fields, torch, args, names):

@@ -118,6 +118,10 @@ OEB_API oeb_status oeb_stream_synchronize(void* stream);
  * thread; 0 (the default) restores each kernel's own choice.  A tuning knob: results do not
  * depend on it.  Batch plans record and tune their own. */
 OEB_API oeb_status oeb_set_kblock(int kb);
+/* k-slabs of the host entry points' copy/compute/copy pipeline (1..8), for every later call;
+ * 0 (the default) picks 8 for calls that move 8 MB or more and 1 below.  A tuning knob:
+ * results do not depend on it. */
+OEB_API oeb_status oeb_set_host_slabs(int slabs);
 
 /* ------------------------------------------------------------------------- */
 /* Device storage (the device twin of allocateStorage/freeStorage,           */

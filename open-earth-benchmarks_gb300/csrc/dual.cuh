@@ -84,6 +84,15 @@ struct Prec<Dual<T>> {
     const T s = Prec<T>::sqrt_(x.v);
     return Dual<T>(s, x.d / (T(2) * s));
   }
+  __device__ static __forceinline__ bool gt0(Dual<T> x) { return Prec<T>::gt0(x.v); }
+  __device__ static __forceinline__ bool lt_nonneg(Dual<T> a, Dual<T> b) { return Prec<T>::lt_nonneg(a.v, b.v); }
+  template <int K>
+  __device__ static __forceinline__ Dual<T> scale2(Dual<T> x) {
+    return Dual<T>(Prec<T>::template scale2<K>(x.v), Prec<T>::template scale2<K>(x.d));
+  }
+  __device__ static __forceinline__ Dual<T> add_flag(Dual<T> q, Dual<T> t, bool flag) {
+    return q + t * (flag ? T(1) : T(0));
+  }
 };
 
 template <class T>

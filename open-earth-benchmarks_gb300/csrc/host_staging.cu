@@ -2,12 +2,24 @@
 //
 // These take the same descriptors as the device entry points, but pointing to HOST memory
 // (for instance fields made by the reference's allocateStorage, include/util.h:126-141).
-// Each call copies every input descriptor's whole span (allocatedPtr to its last element)
-// to device memory from a library-owned stream-ordered pool, rebases the descriptors, runs
-// the device entry point, copies back exactly the box each output is written over (one
-// cudaMemcpy3DAsync per output), returns the device memory to the pool and synchronises
-// the stream.  Cells outside the written boxes are never written, as in the reference.
-// Pinned host memory makes the copies DMA transfers; pageable memory also works.
+// Each call stages every field through device memory from a library-owned stream-ordered
+// pool and returns when the outputs are back in host memory.  Cells outside the written
+// boxes are never written, as in the reference.
+//
+// The call is a three-stage pipeline over k-slabs of the domain, on two copy streams of the
+// library and the caller's stream:
+//   copy-in   the inputs in k order: slab s needs every level up to its top + 1 (no stencil
+//             reads further in k), which in the k-major layout is a prefix of each field's
+//             span, so the inputs go up in prefix chunks, each byte once;
+//   compute   the device entry point on descriptors shifted to the slab (origin + k0 planes,
+//             nz = the slab's levels), as soon as its chunk is in;
+//   copy-out  each output's written box for the slab (cudaMemcpy3DAsync), as soon as the
+//             slab is computed.
+// Host-to-device and device-to-host copies run on separate copy engines and overlap the
+// kernels, so a call costs about its largest stage instead of their sum.  Pinned host memory
+// makes the copies DMA transfers; pageable memory also works.
+#include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -60,8 +72,9 @@ class Stager {
     for (void* p : bufs_) cudaFreeAsync(p, s_);
   }
 
+  // A device buffer for the span of `host`; `dev` is `host` rebased onto it.
   template <class M>
-  oeb_status in(const M* host, int64_t elems, M* dev, bool copy) {
+  oeb_status alloc(const M* host, int64_t elems, M* dev) {
     void* buf = nullptr;
     const size_t bytes = (size_t)elems * sizeof(T);
     cudaError_t e = cudaMallocFromPoolAsync(&buf, bytes, pool_, s_);
@@ -71,7 +84,6 @@ class Stager {
     }
     bufs_.push_back(buf);
     const T* start = span_start(host->allocated, host->aligned);
-    if (copy) OEB_CUDA_TRY(cudaMemcpyAsync(buf, start, bytes, cudaMemcpyHostToDevice, s_));
     *dev = *host;
     T* base = static_cast<T*>(buf);
     dev->aligned = base + (host->aligned - start);
@@ -111,9 +123,49 @@ oeb_status copy_box_back(const M3* host, const M3* dev, const oeb_domain& d, con
 }
 
 constexpr int kMaxFields = 16;
+constexpr int kMaxSlabs = 8;
+constexpr int64_t kMinPipelinedBytes = int64_t(8) << 20;  // smaller calls run as one slab
+std::atomic<int> g_host_slabs{0};                          // oeb_set_host_slabs (0: automatic)
 
-// Stages the inputs (3-D and 1-D) and outputs of one call, runs `launch` on the device
-// descriptors and copies the outputs back.
+// The copy streams and events of the staged calls on one device, created once.  Calls on a
+// device are serialised by `mu` (each is synchronous anyway).
+struct StageStreams {
+  std::mutex mu;
+  cudaStream_t in = nullptr, out = nullptr;
+  cudaEvent_t ev_in[kMaxSlabs], ev_comp[kMaxSlabs];
+};
+
+oeb_status stage_streams(StageStreams** out) {
+  static std::mutex mu;
+  static std::vector<StageStreams*> per_device;
+  int dev = 0;
+  OEB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)per_device.size() <= dev) per_device.resize(dev + 1, nullptr);
+  if (!per_device[dev]) {
+    StageStreams* ss = new StageStreams();
+    cudaError_t e = cudaStreamCreateWithFlags(&ss->in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ss->out, cudaStreamNonBlocking);
+    for (int q = 0; q < kMaxSlabs && e == cudaSuccess; ++q) {
+      e = cudaEventCreateWithFlags(&ss->ev_in[q], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ss->ev_comp[q], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return cuda_fail(e);  // the partial set is kept out of use
+    per_device[dev] = ss;
+  }
+  *out = per_device[dev];
+  return OEB_OK;
+}
+
+template <class M>
+M shift_k(const M& m, int64_t k0) {
+  M r = m;
+  r.offset += k0 * m.strides[0];
+  return r;
+}
+
+// Stages the inputs (3-D and 1-D) and outputs of one call and runs `launch(d3, d1, o3, dom,
+// stream)` on the device descriptors, slab by slab, with the copies overlapped.
 template <class T, class M3, class M1, class Launch>
 oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<const M3*> in3,
                     std::initializer_list<const M1*> in1, std::initializer_list<OutSpec<M3>> out3, Launch&& launch) {
@@ -129,50 +181,98 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
   M3 d3[kMaxFields];
   M1 d1[kMaxFields];
   M3 o3[kMaxFields];
+  const M3* h3[kMaxFields];
+  int n3 = 0, n1 = 0, no = 0;
+  for (const M3* m : in3) h3[n3] = m, d3[n3++] = *m;
+  for (const M1* m : in1) d1[n1++] = *m;
+  for (const OutSpec<M3>& o : out3) o3[no++] = *o.host;
   {
     // Validate the host descriptors with the device entry point's own checks, before any
     // allocation or copy (the descriptors are identical up to the base pointers).
-    int n = 0;
-    for (const M3* m : in3) d3[n++] = *m;
-    n = 0;
-    for (const M1* m : in1) d1[n++] = *m;
-    n = 0;
-    for (const OutSpec<M3>& o : out3) o3[n++] = *o.host;
     ValidateOnly guard;
-    OEB_TRY(launch(d3, d1, o3));
+    OEB_TRY(launch(d3, d1, o3, dom, stream));
   }
-  cudaStream_t s = (cudaStream_t)stream;
+  StageStreams* ss = nullptr;
+  OEB_TRY(stage_streams(&ss));
+  std::lock_guard<std::mutex> lock(ss->mu);
+  cudaStream_t sc = (cudaStream_t)stream;
   cudaMemPool_t pool = nullptr;
   OEB_TRY(device_pool(&pool));
+  int64_t span[kMaxFields];
+  int64_t bytes = 0;
+  for (int n = 0; n < n3; ++n) bytes += (span[n] = span_elems3(h3[n])) * (int64_t)sizeof(T);
+  const int want = g_host_slabs.load(std::memory_order_relaxed);
+  const int slabs = (int)std::min<int64_t>(want > 0 ? want : (bytes < kMinPipelinedBytes ? 1 : kMaxSlabs), dom->nz);
   oeb_status st = OEB_OK;
   {
-    Stager<T> stage(s, pool);
+    Stager<T> stage(ss->in, pool);  // buffers go back to the pool on ss->in, after the final sync
+    for (int n = 0; n < n3 && st == OEB_OK; ++n) st = stage.alloc(h3[n], span[n], &d3[n]);
     int n = 0;
-    for (const M3* m : in3) {
-      st = stage.in(m, span_elems3(m), &d3[n++], true);
-      if (st != OEB_OK) break;
-    }
-    n = 0;
     for (const M1* m : in1) {
       if (st != OEB_OK) break;
-      st = stage.in(m, span_elems1(m), &d1[n++], true);
+      st = stage.alloc(m, span_elems1(m), &d1[n]);
+      if (st == OEB_OK)
+        st = cudaMemcpyAsync(d1[n].allocated, span_start(m->allocated, m->aligned), span_elems1(m) * sizeof(T),
+                             cudaMemcpyHostToDevice, ss->in) == cudaSuccess
+                 ? OEB_OK
+                 : cuda_fail(cudaGetLastError());
+      ++n;
     }
     n = 0;
     for (const OutSpec<M3>& o : out3) {
       if (st != OEB_OK) break;
-      st = stage.in(o.host, span_elems3(o.host), &o3[n++], false);
+      st = stage.alloc(o.host, span_elems3(o.host), &o3[n++]);
     }
-    if (st == OEB_OK) st = launch(d3, d1, o3);
-    if (st == OEB_OK) {
-      n = 0;
+    int64_t copied[kMaxFields] = {0};
+    for (int s = 0; s < slabs && st == OEB_OK; ++s) {
+      const int64_t k0 = dom->nz * s / slabs, k1 = dom->nz * (s + 1) / slabs;
+      // copy-in: every input's prefix up to level k1 (the slab's top + 1), whole on the last slab
+      for (int q = 0; q < n3 && st == OEB_OK; ++q) {
+        const M3* h = h3[q];
+        const T* hstart = span_start(h->allocated, h->aligned);
+        const int64_t end = s == slabs - 1 ? span[q]
+                                           : std::min(span[q], (int64_t)(h->aligned - hstart) + h->offset +
+                                                                   (k1 + 1) * h->strides[0]);
+        if (end > copied[q]) {
+          if (cudaMemcpyAsync(d3[q].allocated + copied[q], hstart + copied[q], (size_t)(end - copied[q]) * sizeof(T),
+                              cudaMemcpyHostToDevice, ss->in) != cudaSuccess)
+            st = cuda_fail(cudaGetLastError());
+          copied[q] = end;
+        }
+      }
+      if (st != OEB_OK) break;
+      // (errors end the loop through `st`: the synchronisation below always runs before the
+      // buffers go back to the pool)
+      if (cudaEventRecord(ss->ev_in[s], ss->in) != cudaSuccess || cudaStreamWaitEvent(sc, ss->ev_in[s], 0) != cudaSuccess) {
+        st = cuda_fail(cudaGetLastError());
+        break;
+      }
+      // compute the slab
+      M3 s3[kMaxFields], so[kMaxFields];
+      for (int q = 0; q < n3; ++q) s3[q] = shift_k(d3[q], k0);
+      for (int q = 0; q < no; ++q) so[q] = shift_k(o3[q], k0);
+      const oeb_domain ds{dom->nx, dom->ny, k1 - k0};
+      st = launch(s3, d1, so, &ds, stream);
+      if (st != OEB_OK) break;
+      if (cudaEventRecord(ss->ev_comp[s], sc) != cudaSuccess ||
+          cudaStreamWaitEvent(ss->out, ss->ev_comp[s], 0) != cudaSuccess) {
+        st = cuda_fail(cudaGetLastError());
+        break;
+      }
+      // copy-out: the slab's part of every output's written box
+      int q = 0;
       for (const OutSpec<M3>& o : out3) {
-        st = copy_box_back<T>(o.host, &o3[n++], *dom, o.box, s);
+        const M3 hs = shift_k(*o.host, k0);
+        st = copy_box_back<T>(&hs, &so[q++], ds, o.box, ss->out);
         if (st != OEB_OK) break;
       }
     }
-  }  // device buffers returned to the pool here (stream-ordered)
-  cudaError_t e = cudaStreamSynchronize(s);
-  if (st == OEB_OK && e != cudaSuccess) st = cuda_fail(e);
+    const cudaError_t e1 = cudaStreamSynchronize(ss->out);
+    const cudaError_t e2 = cudaStreamSynchronize(sc);
+    const cudaError_t e3 = cudaStreamSynchronize(ss->in);
+    if (st == OEB_OK && (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess))
+      st = cuda_fail(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3);
+  }  // device buffers returned to the pool here (stream-ordered on ss->in)
   return st;
 }
 
@@ -187,16 +287,16 @@ using namespace oeb;
 #define OEB_HOST_ENTRIES(S, T) \
 extern "C" oeb_status oeb_laplace_##S##_host(const OEB_HM3(S)* in, const OEB_HM3(S)* out, const oeb_domain* dom, void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {in}, {}, {{out, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
-                                    return oeb_laplace_##S(&i3[0], &o3[0], dom, stream); \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
+                                    return oeb_laplace_##S(&i3[0], &o3[0], dm, sm); \
                                   }); \
 } \
  \
 extern "C" oeb_status oeb_hdiffsa_##S##_host(const OEB_HM3(S)* out, const OEB_HM3(S)* in, const OEB_HM3(S)* mask, const OEB_HM1(S)* crlato, \
                                            const OEB_HM1(S)* crlatu, const oeb_domain* dom, void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {in, mask}, {crlato, crlatu}, {{out, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
-                                    return oeb_hdiffsa_##S(&o3[0], &i3[0], &i3[1], &i1[0], &i1[1], dom, stream); \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
+                                    return oeb_hdiffsa_##S(&o3[0], &i3[0], &i3[1], &i1[0], &i1[1], dm, sm); \
                                   }); \
 } \
  \
@@ -207,9 +307,9 @@ extern "C" oeb_status oeb_hdiffsmag_##S##_host(const OEB_HM3(S)* uout, const OEB
                                              void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>( \
       dom, stream, {uin, vin, mask}, {crlavo, crlavu, crlato, crlatu, acrlat0}, {{uout, kInterior}, {vout, kInterior}}, \
-      [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+      [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
         return oeb_hdiffsmag_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i1[0], &i1[1], &i1[2], &i1[3], &i1[4], \
-                                 eddlat, eddlon, tau_smag, weight_smag, dom, stream); \
+                                 eddlat, eddlon, tau_smag, weight_smag, dm, sm); \
       }); \
 } \
  \
@@ -219,9 +319,9 @@ extern "C" oeb_status oeb_hadvuv_##S##_host(const OEB_HM3(S)* uout, const OEB_HM
                                           void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1}, \
                                   {{uout, kInterior}, {vout, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
                                     return oeb_hadvuv_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2], \
-                                                          &i1[3], eddlat, eddlon, dom, stream); \
+                                                          &i1[3], eddlat, eddlon, dm, sm); \
                                   }); \
 } \
  \
@@ -231,9 +331,9 @@ extern "C" oeb_status oeb_hadvuv5th_##S##_host(const OEB_HM3(S)* uout, const OEB
                                              void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin}, {acrlat0, acrlat1, tgrlatda0, tgrlatda1}, \
                                   {{uout, kInterior}, {vout, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
                                     return oeb_hadvuv5th_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i1[0], &i1[1], &i1[2], \
-                                                             &i1[3], eddlat, eddlon, dom, stream); \
+                                                             &i1[3], eddlat, eddlon, dm, sm); \
                                   }); \
 } \
  \
@@ -243,19 +343,19 @@ extern "C" oeb_status oeb_fastwavesuv_##S##_host(const OEB_HM3(S)* uout, const O
                                                const oeb_domain* dom, void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin, utens, vtens, wgtfac, ppuv, hhl, rho}, {fx}, \
                                   {{uout, kInterior}, {vout, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3) { \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)* i1, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
                                     return oeb_fastwavesuv_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
-                                                               &i3[5], &i3[6], &i3[7], &i1[0], edadlat, dt, dom, \
-                                                               stream); \
+                                                               &i3[5], &i3[6], &i3[7], &i1[0], edadlat, dt, dm, \
+                                                               sm); \
                                   }); \
 } \
  \
 extern "C" oeb_status oeb_uvbke_##S##_host(const OEB_HM3(S)* ub, const OEB_HM3(S)* vb, const OEB_HM3(S)* uc, const OEB_HM3(S)* vc, const OEB_HM3(S)* cosa, \
                                          const OEB_HM3(S)* rsina, double dt5, const oeb_domain* dom, void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uc, vc, cosa, rsina}, {}, {{ub, kInterior}, {vb, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
-                                    return oeb_uvbke_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], dt5, dom, \
-                                                         stream); \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
+                                    return oeb_uvbke_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], dt5, dm, \
+                                                         sm); \
                                   }); \
 } \
  \
@@ -264,9 +364,9 @@ extern "C" oeb_status oeb_nh_p_grad_##S##_host(const OEB_HM3(S)* uout, const OEB
                                              const OEB_HM3(S)* wk1, T dt, const oeb_domain* dom, void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin, rdx, rdy, gz, pp, pk3, wk1}, {}, \
                                   {{uout, kInterior}, {vout, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
                                     return oeb_nh_p_grad_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
-                                                             &i3[5], &i3[6], &i3[7], dt, dom, stream); \
+                                                             &i3[5], &i3[6], &i3[7], dt, dm, sm); \
                                   }); \
 } \
  \
@@ -275,9 +375,9 @@ extern "C" oeb_status oeb_p_grad_c_##S##_host(const OEB_HM3(S)* uout, const OEB_
                                             const OEB_HM3(S)* pkc, T dt2, const oeb_domain* dom, void* stream) { \
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>(dom, stream, {uin, vin, rdxc, rdyc, delpc, gz, pkc}, {}, \
                                   {{uout, kInterior}, {vout, kInterior}}, \
-                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+                                  [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
                                     return oeb_p_grad_c_##S(&o3[0], &o3[1], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
-                                                            &i3[5], &i3[6], dt2, dom, stream); \
+                                                            &i3[5], &i3[6], dt2, dm, sm); \
                                   }); \
 } \
  \
@@ -288,11 +388,17 @@ extern "C" oeb_status oeb_fvtp2d_##S##_host(const OEB_HM3(S)* q_i, const OEB_HM3
   return run_host<T, OEB_HM3(S), OEB_HM1(S)>( \
       dom, stream, {q, crx, cry, ra_x, ra_y, xfx, yfx, area}, {}, \
       {{q_i, kFvQi}, {q_j, kFvQj}, {fx1, kInterior}, {fx2, kFvFx2}, {fy1, kInterior}, {fy2, kFvFy2}}, \
-      [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3) { \
+      [&](const OEB_HM3(S)* i3, const OEB_HM1(S)*, const OEB_HM3(S)* o3, const oeb_domain* dm, void* sm) { \
         return oeb_fvtp2d_##S(&o3[0], &o3[1], &o3[2], &o3[3], &o3[4], &o3[5], &i3[0], &i3[1], &i3[2], &i3[3], &i3[4], \
-                              &i3[5], &i3[6], &i3[7], p1, p2, dom, stream); \
+                              &i3[5], &i3[6], &i3[7], p1, p2, dm, sm); \
       }); \
 }
 
 OEB_HOST_ENTRIES(f64, double)
 OEB_HOST_ENTRIES(f32, float)
+
+extern "C" oeb_status oeb_set_host_slabs(int slabs) {
+  if (slabs < 0 || slabs > oeb::kMaxSlabs) return OEB_ERR_ARGUMENT;
+  oeb::g_host_slabs.store(slabs, std::memory_order_relaxed);
+  return OEB_OK;
+}

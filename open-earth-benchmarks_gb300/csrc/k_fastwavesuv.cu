@@ -98,11 +98,11 @@ struct fastwavesuv_kernel {
           const T p0 = ld(ppuv + o);
           const T r0 = ld(rho + o);
           // fastwavesuv.h:172-175
-          const T ppgu = (ld(ppuv + o + 1) - p0) + (((s.ppgc[b][a + 1] + s.ppgc[b][a]) * T(0.5)) *
+          const T ppgu = (ld(ppuv + o + 1) - p0) + (scale2<-1>(s.ppgc[b][a + 1] + s.ppgc[b][a]) *
                                                         (s.hs[b][a] - s.hs[b][a + 1])) /
                                                            (s.hd[b][a] + s.hd[b][a + 1]);
           // fastwavesuv.h:177-180
-          const T ppgv = (ld(ppuv + o + sj) - p0) + (((s.ppgc[b + 1][a] + s.ppgc[b][a]) * T(0.5)) *
+          const T ppgv = (ld(ppuv + o + sj) - p0) + (scale2<-1>(s.ppgc[b + 1][a] + s.ppgc[b][a]) *
                                                          (s.hs[b][a] - s.hs[b + 1][a])) /
                                                             (s.hd[b][a] + s.hd[b + 1][a]);
           // fastwavesuv.h:182-186

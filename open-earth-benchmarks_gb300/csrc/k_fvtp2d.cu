@@ -43,17 +43,17 @@ __device__ __forceinline__ void ppm_aux(T al0, T al1, T q0, T* almq, T* br, T* b
 
 // fvtp2d.h:28-34: upwind flux at point j from the aux values at j-1 and j.  The flag sum
 // smt5(j-1) + smt5(j)*(smt5(j-1)==0) is exactly 1.0 when either flag is set, else 0.0.
+// Branch-free: each lane selects the operands of its upwind side and performs that side's
+// FP64 operations, (1 - c)(br - c b0) as 1 + (-c) and br + (-(c b0)) -- the same values, an
+// IEEE subtraction being the addition of the negation -- so no warp runs both sides.
 template <class T>
 __device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T br_m1, T b0_m1, T almq_0, T b0_0, unsigned char smt_m1,
                                       unsigned char smt_0) {
-  const T smt = (smt_m1 | smt_0) ? T(1.0) : T(0.0);
-  if (c > T(0.)) {
-    const T t = (T(1.) - c) * (br_m1 - (c * b0_m1));
-    return q_m1 + (t * smt);
-  } else {
-    const T t = (T(1.) + c) * (almq_0 + (c * b0_0));
-    return q_0 + (t * smt);
-  }
+  const bool pos = gt0(c);
+  const T u = T(1.) + (pos ? -c : c);
+  const T p = c * (pos ? b0_m1 : b0_0);
+  const T v = (pos ? br_m1 : almq_0) + (pos ? -p : p);
+  return Prec<T>::add_flag(pos ? q_m1 : q_0, u * v, (smt_m1 | smt_0) != 0);
 }
 
 // ------------------------------ launch 1 ---------------------------------------------
@@ -233,7 +233,7 @@ struct fvtp2d_flux_kernel {
           const int64_t o = kofs + i + j * sj;
           const T f = ppm_flux(ld(crx + o), s.qi[b][a + 2], s.qi[b][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
                                     s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
-          fx1[o] = ((T(0.5) * (f + ld(fx2 + o))) * ld(xfx + o));  // fvtp2d.h:164
+          fx1[o] = (scale2<-1>(f + ld(fx2 + o)) * ld(xfx + o));  // fvtp2d.h:164
         }
       });
       __syncthreads();
@@ -253,7 +253,7 @@ struct fvtp2d_flux_kernel {
           const int64_t o = kofs + i + j * sj;
           const T f = ppm_flux(ld(cry + o), s.qj[b + 2][a], s.qj[b + 3][a], s.w.y.br[b][a], s.w.y.b0[b][a],
                                     s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
-          fy1[o] = ((T(0.5) * (f + ld(fy2 + o))) * ld(yfx + o));  // fvtp2d.h:173
+          fy1[o] = (scale2<-1>(f + ld(fy2 + o)) * ld(yfx + o));  // fvtp2d.h:173
         }
       });
       __syncthreads();

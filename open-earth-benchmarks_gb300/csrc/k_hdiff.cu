@@ -187,8 +187,8 @@ struct hdiffsmag_kernel {
           const int64_t o = kofs + i + j * sj;
           const T hdweight = weight_smag * ld(mask + o);
           // hdiffsmag.h:233-244
-          T smag_u = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b][a + 1] + s.tsq[b][a]) +
-                                               T(0.5) * (s.ssq[b][a + 1] + s.ssq[b + 1][a + 1])) -
+          T smag_u = tau_smag * Prec<T>::sqrt_(scale2<-1>(s.tsq[b][a + 1] + s.tsq[b][a]) +
+                                               scale2<-1>(s.ssq[b][a + 1] + s.ssq[b + 1][a + 1])) -
                      hdweight;
           smag_u = clamp_smag(smag_u);
           const T uc = s.u[b + 1][a + 1];
@@ -200,8 +200,8 @@ struct hdiffsmag_kernel {
           lu.add_prod(s.crlatu[b], -s.dyu[b][a + 1]);
           uout[o] = uc + smag_u * lu.get();
           // hdiffsmag.h:248-259
-          T smag_v = tau_smag * Prec<T>::sqrt_(T(0.5) * (s.tsq[b + 1][a] + s.tsq[b][a]) +
-                                               T(0.5) * (s.ssq[b + 1][a] + s.ssq[b + 1][a + 1])) -
+          T smag_v = tau_smag * Prec<T>::sqrt_(scale2<-1>(s.tsq[b + 1][a] + s.tsq[b][a]) +
+                                               scale2<-1>(s.ssq[b + 1][a] + s.ssq[b + 1][a + 1])) -
                      hdweight;
           smag_v = clamp_smag(smag_v);
           const T vc = s.v[b + 1][a + 1];

@@ -177,7 +177,7 @@ struct nh_p_grad_kernel {
 template <class T>
 __device__ __forceinline__ T adv3_axis(const T* __restrict__ f, int64_t o, int64_t s, T a) {
   constexpr T c6 = T(-1.0) / T(6.0), c3 = T(-1.0) / T(3.0), ch = T(-0.5);
-  const bool pos = a > 0;
+  const bool pos = gt0(a);
   const T fa = ld(f + o + (pos ? -2 : -1) * s), fb = ld(f + o - s), f0 = ld(f + o), fc = ld(f + o + s),
           fd = ld(f + o + (pos ? 1 : 2) * s);
   if constexpr (Prec<T>::kCompensated) {
@@ -200,7 +200,7 @@ template <class T>
 __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64_t s, T a) {
   constexpr T c30 = T(1.0) / T(30.0), c4 = T(-1.0) / T(4.0), c3 = T(-1.0) / T(3.0), c2 = T(-1.0) / T(2.0),
               c20 = T(1.0) / T(20.0);
-  const bool pos = a > 0;
+  const bool pos = gt0(a);
   const int64_t sh = pos ? 0 : s;  // the negative branch reads one cell further along the axis
   const T x0 = ld(f + o - 3 * s + sh), x1 = ld(f + o - 2 * s + sh), fm1 = ld(f + o - s), f0 = ld(f + o),
           fp1 = ld(f + o + s), x4 = ld(f + o + s + sh), x5 = ld(f + o + 2 * s + sh);
@@ -235,7 +235,7 @@ struct hadv_kernel {
       const T um = ld(uin + o - 1) + u0;  // uin(i-1)+uin(i), first pair of both averages
       // u at the u-position and v at the u-position (hadvuv.h:186-189)
       const T u_atupos = third * (um + ld(uin + o + 1));
-      const T v_atupos = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
+      const T v_atupos = scale2<-2>(((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
       T ua = ld(acrlat0 + jo) * u_atupos;
       T va = rr * v_atupos;
       T rx, ry;
@@ -249,7 +249,7 @@ struct hadv_kernel {
       const T ures = eddlat * rx + eddlon * ry;
       uout[o] = ures + (ld(tgrlatda0 + jo) * u0) * v_atupos;
       // u and v at the v-position (hadvuv.h:197-206)
-      const T u_atvpos = T(0.25) * (((um) + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
+      const T u_atvpos = scale2<-2>(((um) + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
       const T v_atvpos = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
       ua = ld(acrlat1 + jo) * u_atvpos;
       va = rr * v_atvpos;

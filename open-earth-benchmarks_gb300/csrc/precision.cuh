@@ -24,13 +24,60 @@ namespace oeb {
 template <class T>
 struct Prec;
 
+// FP64 operations done exactly on the integer pipe.  The GB300 issues 1.6 FP64 operations
+// per clock per SM and about 100 integer ones, and the FP64 stencils are bound by the FP64
+// pipe; so sign tests, comparisons of non-negative values, multiplications by powers of two
+// and the multiply by a 0/1 flag of fvtp2d are done on the bit patterns.  Each gives the
+// result of the FP64 operation it replaces, bit for bit, and falls back to that operation
+// for every input where the shortcut could differ (zeros, subnormals, infinities, NaN, a
+// product that could underflow, a scaling that could leave the normal range).
+namespace fp64 {
+__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ int exponent(long long b) { return (int)((b >> 52) & 0x7FF); }
+// both operands normal and |a b| >= 2^(ea + eb - 2046) >= 2^-1074: the rounded product is
+// nonzero and carries the sign of the exact one
+__device__ __forceinline__ bool product_sign_known(long long ua, long long ub) {
+  const int ea = exponent(ua), eb = exponent(ub);
+  return ea > 0 && eb > 0 && ea < 2047 && eb < 2047 && ea + eb >= 972;
+}
+}  // namespace fp64
+
 template <>
 struct Prec<double> {
   static constexpr bool kCompensated = false;
   // reference semantics: the rounded FP64 product compared with 0 (hdiffsa.h:106, fvtp2d.h:23)
-  __device__ static __forceinline__ bool prod_gt0(double a, double b) { return a * b > 0; }
-  __device__ static __forceinline__ bool prod_lt0(double a, double b) { return (a * b) < 0.0; }
+  __device__ static __forceinline__ bool prod_gt0(double a, double b) {
+    const long long ua = fp64::bits(a), ub = fp64::bits(b);
+    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) >= 0 : a * b > 0;
+  }
+  __device__ static __forceinline__ bool prod_lt0(double a, double b) {
+    const long long ua = fp64::bits(a), ub = fp64::bits(b);
+    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) < 0 : (a * b) < 0.0;
+  }
   __device__ static __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  // x > 0 (false for NaN and -0)
+  __device__ static __forceinline__ bool gt0(double x) {
+    const long long b = fp64::bits(x);
+    return b > 0 && b <= 0x7FF0000000000000LL;
+  }
+  // a < b for a, b >= +0 and not NaN: the bit patterns order as the values
+  __device__ static __forceinline__ bool lt_nonneg(double a, double b) { return fp64::bits(a) < fp64::bits(b); }
+  // x * 2^K
+  template <int K>
+  __device__ static __forceinline__ double scale2(double x) {
+    const long long b = fp64::bits(x);
+    const int e = fp64::exponent(b);
+    if (e > 0 && e < 2047 && e + K > 0 && e + K < 2047) return __longlong_as_double(b + ((long long)K << 52));
+    return x * (K >= 0 ? double(1LL << (K >= 0 ? K : 0)) : 1.0 / double(1LL << (K < 0 ? -K : 0)));
+  }
+  // q + t * (flag ? 1.0 : 0.0): t * 1 is t; t * 0 is a zero with t's sign (t finite), and
+  // q + (+-0) is q except -0 + +0 = +0
+  __device__ static __forceinline__ double add_flag(double q, double t, bool flag) {
+    if (flag) return q + t;
+    const long long bt = fp64::bits(t);
+    if (fp64::exponent(bt) == 0x7FF) return q + t * 0.0;  // t infinite or NaN
+    return (fp64::bits(q) == (long long)0x8000000000000000ULL && bt >= 0) ? 0.0 : q;
+  }
 };
 
 template <>
@@ -44,7 +91,24 @@ struct Prec<float> {
     return (a > 0.f && b < 0.f) || (a < 0.f && b > 0.f);
   }
   __device__ static __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  __device__ static __forceinline__ bool gt0(float x) { return x > 0.f; }
+  __device__ static __forceinline__ bool lt_nonneg(float a, float b) { return a < b; }
+  template <int K>
+  __device__ static __forceinline__ float scale2(float x) {
+    return x * (K >= 0 ? float(1LL << (K >= 0 ? K : 0)) : 1.0f / float(1LL << (K < 0 ? -K : 0)));
+  }
+  __device__ static __forceinline__ float add_flag(float q, float t, bool flag) { return q + t * (flag ? 1.f : 0.f); }
 };
+
+// the same operations by element type
+template <class T>
+__device__ __forceinline__ bool gt0(T x) {
+  return Prec<T>::gt0(x);
+}
+template <int K, class T>
+__device__ __forceinline__ T scale2(T x) {
+  return Prec<T>::template scale2<K>(x);
+}
 
 // Left-to-right sum of terms.  Plain for FP64 (the reference's order and rounding); for FP32
 // a compensated sum: every addition is a TwoSum and every product a TwoProduct, the

@@ -6,6 +6,7 @@
 
 #include "launch.cuh"
 #include "oeb_common.cuh"
+#include "precision.cuh"
 
 namespace oeb {
 
@@ -34,11 +35,12 @@ __device__ __forceinline__ T ld(const T* p) {
 }
 
 // std::min(0.5, std::max(0.0, x)) with libstdc++'s comparisons (hdiffsmag.h:236, :251):
-// max(a,b) = (a < b) ? b : a, min(a,b) = (b < a) ? b : a.
+// max(a,b) = (a < b) ? b : a, min(a,b) = (b < a) ? b : a.  lo is >= +0 and not NaN, so its
+// comparison with 0.5 may use the non-negative ordering.
 template <class T>
 __device__ __forceinline__ T clamp_smag(T x) {
-  const T lo = (T(0.0) < x) ? x : T(0.0);
-  return (lo < T(0.5)) ? lo : T(0.5);
+  const T lo = Prec<T>::gt0(x) ? x : T(0.0);
+  return Prec<T>::lt_nonneg(lo, T(0.5)) ? lo : T(0.5);
 }
 
 // 1 / EARTH_RADIUS folded at compile time in the element type (include/util.h:17-18).
