@@ -16,9 +16,9 @@
  *
  * Device entry points (oeb_<k>_f64 / _f32) take DEVICE pointers and are
  * asynchronous on the given cudaStream_t (passed as void*, NULL = legacy default
- * stream).  Host entry points (oeb_<k>_f64_host) take HOST pointers, stage the
- * fields through device memory and return after the outputs are back in host
- * memory.  No entry point writes the scratch fields of the reference signatures
+ * stream).  Host entry points (oeb_<k>_f64_host) take HOST pointers -- run on them
+ * in place where the device can address host memory, else staged through device
+ * memory -- and return after the outputs are in host memory.  No entry point writes the scratch fields of the reference signatures
  * (lap/flx/fly, T_sqr_s, uatupos..., ppgk..., wk, du, dv, fxx, al, ...): they are
  * not parameters of this ABI.  Cells outside each output's written box are left
  * untouched, as in the reference.
@@ -122,6 +122,11 @@ OEB_API oeb_status oeb_set_kblock(int kb);
  * 0 (the default) picks 8 for calls that move 8 MB or more and 1 below.  A tuning knob:
  * results do not depend on it. */
 OEB_API oeb_status oeb_set_host_slabs(int slabs);
+/* 1 (the default): host entry points run the kernels on the host fields in place when the
+ * device can address all of them (pageable memory on systems whose GPU uses the host page
+ * tables, such as Grace-Blackwell; page-locked memory mapped at the same address elsewhere);
+ * 0: always stage through device memory.  Results do not depend on it. */
+OEB_API oeb_status oeb_set_host_direct(int enable);
 
 /* ------------------------------------------------------------------------- */
 /* Device storage (the device twin of allocateStorage/freeStorage,           */

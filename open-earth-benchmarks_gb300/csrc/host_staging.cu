@@ -1,12 +1,19 @@
 // host_staging.cu -- host-buffer entry points oeb_<k>_f64_host.
 //
 // These take the same descriptors as the device entry points, but pointing to HOST memory
-// (for instance fields made by the reference's allocateStorage, include/util.h:126-141).
-// Each call stages every field through device memory from a library-owned stream-ordered
-// pool and returns when the outputs are back in host memory.  Cells outside the written
-// boxes are never written, as in the reference.
+// (for instance fields made by the reference's allocateStorage, include/util.h:126-141),
+// and return when the outputs are in host memory.  Cells outside the written boxes are
+// never written, as in the reference.
 //
-// The call is a three-stage pipeline over k-slabs of the domain, on two copy streams of the
+// Direct mode (the default where it applies): when the device can address every field in
+// place -- a GB300 with its Grace host reads and writes pageable host memory over NVLink-C2C
+// through the host's page tables; elsewhere page-locked memory mapped at the same address --
+// the call runs the device entry point on the host descriptors themselves.  The stencils'
+// loads and stores cross the link as the kernel runs: no staging copies, and the transfers
+// overlap the arithmetic.
+//
+// Staged mode (other memory, or oeb_set_host_direct(0)): every field goes through device
+// memory from a library-owned stream-ordered pool, in a three-stage pipeline over k-slabs of the domain, on two copy streams of the
 // library and the caller's stream:
 //   copy-in   the inputs in k order: slab s needs every level up to its top + 1 (no stencil
 //             reads further in k), which in the k-major layout is a prefix of each field's
@@ -157,6 +164,33 @@ oeb_status stage_streams(StageStreams** out) {
   return OEB_OK;
 }
 
+std::atomic<int> g_host_direct{1};  // oeb_set_host_direct
+
+// Whether the current device can address host memory at `p` in place: it reads pageable
+// memory through the host's page tables (cudaDevAttrPageableMemoryAccess, the NVLink-C2C
+// systems), or `p` is page-locked memory mapped at the same address.
+bool device_addressable(const void* p) {
+  static std::mutex mu;
+  static std::vector<int> pageable;  // per device: -1 unknown, 0 / 1
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)pageable.size() <= dev) pageable.resize(dev + 1, -1);
+    if (pageable[dev] < 0) {
+      int v = 0;
+      pageable[dev] = cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && v == 1;
+    }
+    if (pageable[dev]) return true;
+  }
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+}
+
 template <class M>
 M shift_k(const M& m, int64_t k0) {
   M r = m;
@@ -191,6 +225,18 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
     // allocation or copy (the descriptors are identical up to the base pointers).
     ValidateOnly guard;
     OEB_TRY(launch(d3, d1, o3, dom, stream));
+  }
+  // Direct: the kernels read and write the host fields in place over the host link -- no
+  // staging copies, and the transfers overlap the arithmetic by construction.
+  bool direct = g_host_direct.load(std::memory_order_relaxed) != 0;
+  for (int q = 0; q < n3 && direct; ++q) direct = device_addressable(d3[q].aligned);
+  for (int q = 0; q < n1 && direct; ++q) direct = device_addressable(d1[q].aligned);
+  for (int q = 0; q < no && direct; ++q) direct = device_addressable(o3[q].aligned);
+  if (direct) {
+    oeb_status st = launch(d3, d1, o3, dom, stream);
+    const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (st == OEB_OK && e != cudaSuccess) st = cuda_fail(e);
+    return st;
   }
   StageStreams* ss = nullptr;
   OEB_TRY(stage_streams(&ss));
@@ -400,5 +446,11 @@ OEB_HOST_ENTRIES(f32, float)
 extern "C" oeb_status oeb_set_host_slabs(int slabs) {
   if (slabs < 0 || slabs > oeb::kMaxSlabs) return OEB_ERR_ARGUMENT;
   oeb::g_host_slabs.store(slabs, std::memory_order_relaxed);
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_set_host_direct(int enable) {
+  if (enable != 0 && enable != 1) return OEB_ERR_ARGUMENT;
+  oeb::g_host_direct.store(enable, std::memory_order_relaxed);
   return OEB_OK;
 }

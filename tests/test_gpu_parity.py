@@ -81,22 +81,39 @@ def test_driver_scalars(pkg, fields, orc, cuda, name):
     _run_both(pkg, fields, orc, cuda, name, 48, 48, 6, seed=7, scalars=fields.make_scalars(name, 7, "driver"))
 
 
+@pytest.fixture(params=["direct", "staged"])
+def host_mode(request, pkg):
+    """The host entry points in place on the host fields (where the device can address
+    them) and staged through device memory."""
+    lib = pkg.load_library()
+    assert lib.oeb_set_host_direct(1 if request.param == "direct" else 0) == 0
+    yield request.param
+    lib.oeb_set_host_direct(1)
+
+
 @pytest.mark.parametrize("name", KERNELS)
-def test_host_entry_points(pkg, fields, orc, name):
-    """oeb_<k>_f64_host with host buffers: same bits, untouched cells preserved."""
+@pytest.mark.parametrize("size", [(37, 29, 4), (128, 96, 24)], ids=["37x29x4", "128x96x24"])
+@pytest.mark.parametrize("memory", ["pageable", "pinned"])
+def test_host_entry_points(pkg, fields, orc, host_mode, name, size, memory):
+    """oeb_<k>_f64_host with host buffers: same bits, untouched cells preserved.  The larger
+    case runs the staged copy / compute / copy pipeline over several k-slabs."""
+    import torch
     spec = pkg.KERNELS[name]
-    nx, ny, nz = 37, 29, 4
+    nx, ny, nz = size
     inputs = fields.make_inputs(name, nx, ny, nz, seed=8)
     sc = fields.make_scalars(name, seed=8)
     outs = fields.make_outputs(name, nx, ny, nz)
     want = {k: v.copy() for k, v in {**inputs, **outs}.items()}
     orc.run_oracle(spec, want, sc, nx, ny, nz, H)
-    host = {k: pkg.Storage(v.copy(), H) for k, v in {**inputs, **outs}.items()}
+    if memory == "pinned":
+        host = {k: pkg.Storage(torch.from_numpy(v.copy()).pin_memory(), H) for k, v in {**inputs, **outs}.items()}
+    else:
+        host = {k: pkg.Storage(v.copy(), H) for k, v in {**inputs, **outs}.items()}
     pkg.call(name, host, sc, domain=(nx, ny, nz))
     for a in spec.by_role("out3"):
-        assert_bitwise_equal(host[a.name].data, want[a.name], "%s.%s (host path)" % (name, a.name))
+        assert_bitwise_equal(host[a.name].numpy(), want[a.name], "%s.%s (host path)" % (name, a.name))
     for a in spec.by_role("in3"):
-        assert_bitwise_equal(host[a.name].data, inputs[a.name], "%s.%s input unchanged" % (name, a.name))
+        assert_bitwise_equal(host[a.name].numpy(), inputs[a.name], "%s.%s input unchanged" % (name, a.name))
 
 
 def test_reference_named_api(pkg, fields, orc, cuda):
