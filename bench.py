@@ -63,19 +63,87 @@ def _dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """SM clocks and clock-event reasons sampled over the timed region.
+
+    NVML (libnvidia-ml, read-only queries) is polled every 2 ms from a thread between
+    start() and stop(), so even a timed region of a few tens of ms gets a record; where
+    NVML cannot be loaded, nvidia-smi samples every 200 ms instead.
+    """
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason bits (nvml.h)
+    REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                   "hw_thermal_slowdown": 0x40}
+    PERIOD_S = 0.002
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.samples = []  # (sm_mhz, max_mhz, reason bits) from NVML
+        self.source = None
+        self._nvml = None
+        self._stop = threading.Event()
+        self._t = None
 
-    def __enter__(self):
+    def _open_nvml(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        handle = ctypes.c_void_p()
+        rc = 1
         try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.gpu)
+            bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+            rc = lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(handle))
+        except Exception:
+            rc = 1
+        if rc != 0:
+            rc = lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.gpu), ctypes.byref(handle))
+        if rc != 0:
+            raise RuntimeError("no NVML handle")
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        clk, mx, bits = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+
+        def read():
+            if lib.nvmlDeviceGetClockInfo(handle, 1, ctypes.byref(clk)) != 0:  # NVML_CLOCK_SM
+                return None
+            lib.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(mx))
+            if reasons(handle, ctypes.byref(bits)) != 0:
+                bits.value = 0
+            return float(clk.value), float(mx.value), int(bits.value)
+
+        if read() is None:
+            raise RuntimeError("NVML clock query failed")
+        return read
+
+    def _poll(self):
+        while True:
+            r = self._nvml()
+            if r is not None:
+                self.samples.append(r)
+            if self._stop.wait(self.PERIOD_S):
+                break
+
+    def start(self):
+        """Begins sampling (call just before the timed region)."""
+        try:
+            if self._nvml is None:
+                self._nvml = self._open_nvml()
+            self.source = "nvml"
+            self._stop.clear()
+            self._t = threading.Thread(target=self._poll, daemon=True)
+            self._t.start()
+            return
+        except Exception:
+            self._nvml = None
+        try:
+            self.source = "nvidia-smi"
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
@@ -83,22 +151,38 @@ class ClockSampler:
             self._t.start()
         except Exception:
             self.proc = None
-        return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def __exit__(self, *exc):
+    def stop(self):
+        """Ends sampling (call right after the timed region's synchronize)."""
+        if self.source == "nvml" and self._t is not None:
+            self._stop.set()
+            self._t.join(timeout=5)
+            self._t = None
         if self.proc is not None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.proc = None
+
+    def __enter__(self):
+        self.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
 
     def summary(self):
         sm, mx, reasons = [], [], set()
+        for c, m, b in self.samples:
+            sm.append(c)
+            mx.append(m)
+            reasons.update(n for n, bit in self.REASON_BITS.items() if b & bit)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -113,9 +197,10 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock query unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "sm_min_mhz": min(sm),
+                "reasons": sorted(reasons), "samples": len(sm), "source": self.source,
+                "window": "timed region only"}
 
 
 def _make_set(pkg, fields, torch, dev, seed, names, pinned=False, dtype=np.float64, shape=None, workload="physical"):
@@ -162,11 +247,15 @@ def _time_steps(pkg, torch, sets, names, steps, warmup, stream, dom, clocks=None
     t1 = torch.cuda.Event(enable_timing=True)
     launches0 = lib.oeb_launch_count()
     torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.start()
     t0.record(stream)
     for s in range(steps):
         step(sets[s % len(sets)], evs[s])
     t1.record(stream)
     torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.stop()
     launches = lib.oeb_launch_count() - launches0
     per_kernel = {name: statistics.mean(evs[s][idx][0].elapsed_time(evs[s][idx][1]) for s in range(steps))
                   for idx, name in enumerate(names)}
@@ -195,8 +284,9 @@ def run_ours(args):
     dom = (NX, NY, NZ)
     if world > 1:
         torch.distributed.barrier()
-    with ClockSampler(local) as clocks:
-        ms_total, per_kernel, launches = _time_steps(pkg, torch, sets, names, args.steps, args.warmup, stream, dom)
+    clocks = ClockSampler(local)
+    ms_total, per_kernel, launches = _time_steps(pkg, torch, sets, names, args.steps, args.warmup, stream, dom,
+                                                 clocks=clocks)
     if world > 1:
         t = torch.tensor([ms_total], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -667,6 +757,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_one(args):
+    """`--profile-one K`: K alone, `--calls` times, for an ncu capture (prints nothing timed)."""
+    import torch
+    pkg = graft.load_package()
+    import importlib
+    fields = importlib.import_module("oeb_gb300.fields")
+    dtype = np.float64 if args.precision == "f64" else np.float32
+    shape = tuple(args.shape)
+    st, sc = _make_set(pkg, fields, torch, torch.device("cuda", 0), 2, [args.profile_one], dtype=dtype, shape=shape,
+                       workload=args.workload)[args.profile_one]
+    for _ in range(args.calls):
+        pkg.call(args.profile_one, st, sc, domain=shape)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_one": args.profile_one, "precision": args.precision, "shape": list(shape),
+                      "calls": args.calls}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -682,7 +789,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--kernels", nargs="*", default=None,
                     help="run only these stencils in the step (profiling); the default line uses all ten")
+    ap.add_argument("--profile-one", default=None, help="run only this stencil --calls times (for ncu captures)")
+    ap.add_argument("--precision", choices=["f64", "f32"], default="f64")
+    ap.add_argument("--shape", type=int, nargs=3, default=[NX, NY, NZ])
+    ap.add_argument("--workload", choices=["physical", "fronts", "smooth"], default="physical")
+    ap.add_argument("--calls", type=int, default=4)
     args = ap.parse_args()
+    if args.profile_one:
+        profile_one(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         sys.stderr.write("warning: fewer than 3 warm-up steps\n")
     if args.impl == "reference":

@@ -231,41 +231,44 @@ struct fastwavesuv_adj_kernel {
   #pragma unroll
     for (int t = 0; t < kPts; ++t) cm2[t] = cm1[t] = dir[t] = T(0);
     const int tid = threadIdx.y * kTX + threadIdx.x;
-    // adjoint of ppgu (au) and of ppgv (av) at an interior point, times g when asked
-    auto au_at = [&](int i, int j, int k, bool with_g) -> T {
+    // adjoint of ppgu (au) and of ppgv (av) at an interior point, and the same times g
+    // (each division once: a = -dt q ybar, then a g)
+    auto au_at = [&](int i, int j, int k, T* ag) -> T {
+      *ag = T(0);
       if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
       const int64_t o = (int64_t)k * sk + i + j * sj;
       const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
       const T a = -(dt * qx) * ld(uoutb + o);
-      if (!with_g) return a;
-      const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
-      const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
-      return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+      if (a != T(0)) {
+        const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
+        const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
+        *ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+      }
+      return a;
     };
-    auto av_at = [&](int i, int j, int k, bool with_g) -> T {
+    auto av_at = [&](int i, int j, int k, T* ag) -> T {
+      *ag = T(0);
       if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
       const int64_t o = (int64_t)k * sk + i + j * sj;
       const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
       const T a = -(dt * qy) * ld(voutb + o);
-      if (!with_g) return a;
-      const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
-      const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
-      return a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+      if (a != T(0)) {
+        const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
+        const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
+        *ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+      }
+      return a;
     };
   #pragma unroll 1
     for (int L = Ks - 1; L <= Ke; ++L) {
       // au, av and their g-weighted versions at level L over the tile plus the low apron
       for_region<kR, kT>([&](int a, int b) {
         const int i = i0 - 1 + a, j = j0 + b;
-        const T raw = au_at(i, j, L, false);
-        s.au[b][a] = raw;
-        s.ax[b][a] = (raw == T(0)) ? T(0) : au_at(i, j, L, true);
+        s.au[b][a] = au_at(i, j, L, &s.ax[b][a]);
       });
       for_region<kT, kR>([&](int a, int b) {
         const int i = i0 + a, j = j0 - 1 + b;
-        const T raw = av_at(i, j, L, false);
-        s.av[b][a] = raw;
-        s.ay[b][a] = (raw == T(0)) ? T(0) : av_at(i, j, L, true);
+        s.av[b][a] = av_at(i, j, L, &s.ay[b][a]);
       });
       __syncthreads();
   #pragma unroll

@@ -449,7 +449,7 @@ __device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L
   __syncthreads();
   region(5, 5 + 32, [&](int w, int l) {
     const int a = A - 5 + w;
-    T g = (p1 * (s.al[l][w + 1] + s.al[l][w])) + (p2 * (s.al[l][w + 2] + s.al[l][w - 1])) - s.alm[l][w] - s.br[l][w];
+    T g = fma(p1, s.al[l][w + 1] + s.al[l][w], fma(p2, s.al[l][w + 2] + s.al[l][w - 1], -s.alm[l][w])) - s.br[l][w];
     const T f1 = fb(a + 1, L0 + l);
     if (f1 != T(0) && cv(a + 1, L0 + l) > T(0)) g = g + f1;
     const T f0 = fb(a, L0 + l);

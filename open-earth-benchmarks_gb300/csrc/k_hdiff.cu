@@ -431,22 +431,22 @@ struct hdiffsmag_adj_gather_kernel {
       if (in(a + 1, b)) ub = ub + tm.lu[o + 1], vb = vb + tm.lv[o + 1];
       if (in(a, b - 1)) {
         const int64_t bo = (int64_t)(b - 1) * s1d;
-        ub = ub + ld(crlato + bo) * tm.lu[o - sj];
-        vb = vb + ld(crlavo + bo) * tm.lv[o - sj];
+        ub = fma(ld(crlato + bo), tm.lu[o - sj], ub);
+        vb = fma(ld(crlavo + bo), tm.lv[o - sj], vb);
       }
       if (in(a, b + 1)) {
         const int64_t bo = (int64_t)(b + 1) * s1d;
-        ub = ub + ld(crlatu + bo) * tm.lu[o + sj];
-        vb = vb + ld(crlavu + bo) * tm.lv[o + sj];
+        ub = fma(ld(crlatu + bo), tm.lu[o + sj], ub);
+        vb = fma(ld(crlavu + bo), tm.lv[o + sj], vb);
       }
       const T tb0 = inT(a, b) ? tm.tb[o] : T(0);
       const T sb0 = inS(a, b) ? tm.sb[o] : T(0);
-      if (inT(a + 1, b)) ub = ub - c2 * tm.tb[o + 1];
-      ub = ub + c2 * tb0 - c1 * sb0;
-      if (inS(a, b - 1)) ub = ub + c1 * tm.sb[o - sj];
-      if (inT(a, b + 1)) vb = vb + c1 * tm.tb[o + sj];
-      vb = vb - c1 * tb0 - c2 * sb0;
-      if (inS(a - 1, b)) vb = vb + c2 * tm.sb[o - 1];
+      if (inT(a + 1, b)) ub = fma(-c2, tm.tb[o + 1], ub);
+      ub = fma(-c1, sb0, fma(c2, tb0, ub));
+      if (inS(a, b - 1)) ub = fma(c1, tm.sb[o - sj], ub);
+      if (inT(a, b + 1)) vb = fma(c1, tm.tb[o + sj], vb);
+      vb = fma(-c2, sb0, fma(-c1, tb0, vb));
+      if (inS(a - 1, b)) vb = fma(c2, tm.sb[o - 1], vb);
       uinb[o] = ub;
       vinb[o] = vb;
     });

@@ -10,6 +10,10 @@
 // (precision.cuh): the advection flux sums and the laplacian, and the paired products of
 // the pressure-gradient stencils in float-float.
 //
+// The adjoint kernels reproduce no reference arithmetic: their accumulations use explicit
+// fma() (one rounding, half the FP64 instructions), which --fmad=false does not affect.  The
+// state values that decide their branches are recomputed exactly as the forward computes them.
+//
 // One CTA of 32 x 8 threads covers a 32 x 32 (i, j) tile and kb k-levels; each thread
 // computes 4 rows.  Neighbour reads go through L1.
 #include "precision.cuh"
@@ -473,7 +477,7 @@ __device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t
 #pragma unroll
   for (int m = lo; m <= -lo; ++m) {
     const T w = upwind_weight<T, ORDER>(pos, m);
-    if (w != T(0)) acc = acc + w * ld(f + o + m * s);
+    if (w != T(0)) acc = fma(w, ld(f + o + m * s), acc);  // adjoint coefficients: one rounding
   }
   return acc;
 }
@@ -550,14 +554,14 @@ struct hadv_adj_gather_kernel {
         if (in(a - m, b)) {
           const int64_t q = o - m;
           const unsigned char f = tm.fl[q];
-          ub = ub + upwind_weight<T, ORDER>(f & 1, m) * tm.ax[q];
-          vb = vb + upwind_weight<T, ORDER>(f & 4, m) * tm.gx[q];
+          ub = fma(upwind_weight<T, ORDER>(f & 1, m), tm.ax[q], ub);
+          vb = fma(upwind_weight<T, ORDER>(f & 4, m), tm.gx[q], vb);
         }
         if (in(a, b - m)) {
           const int64_t q = o - m * sj;
           const unsigned char f = tm.fl[q];
-          ub = ub + upwind_weight<T, ORDER>(f & 2, m) * tm.ay[q];
-          vb = vb + upwind_weight<T, ORDER>(f & 8, m) * tm.gy[q];
+          ub = fma(upwind_weight<T, ORDER>(f & 2, m), tm.ay[q], ub);
+          vb = fma(upwind_weight<T, ORDER>(f & 8, m), tm.gy[q], vb);
         }
       }
       // u average of point i (i-1, i, i+1) and the ub average (i-1..i, j..j+1)

@@ -146,3 +146,38 @@ def test_launches_are_counted(pkg, fields, cuda):
     pkg.call("laplace", d, {}, domain=(16, 16, 2))
     torch.cuda.synchronize()
     assert lib.oeb_launch_count() == before + 1
+
+
+@pytest.mark.parametrize("kb", [2, 3, 8])
+def test_kblock_does_not_change_results(pkg, fields, orc, cuda, kb):
+    # oeb_set_kblock changes how the k-levels are split among CTAs, never a result
+    lib = pkg.load_library()
+    assert lib.oeb_set_kblock(kb) == 0
+    try:
+        for name in KERNELS:
+            _run_both(pkg, fields, orc, cuda, name, 40, 36, 7, seed=13)
+    finally:
+        lib.oeb_set_kblock(0)
+
+
+@pytest.mark.parametrize("slabs", [2, 3, 8])
+def test_host_slabs_do_not_change_results(pkg, fields, orc, slabs):
+    # the staged host path over 2, 3 and 8 k-slabs (7 levels: uneven slabs)
+    lib = pkg.load_library()
+    assert lib.oeb_set_host_direct(0) == 0 and lib.oeb_set_host_slabs(slabs) == 0
+    try:
+        for name in KERNELS:
+            spec = pkg.KERNELS[name]
+            nx, ny, nz = 33, 30, 7
+            inputs = fields.make_inputs(name, nx, ny, nz, seed=14)
+            sc = fields.make_scalars(name, seed=14)
+            outs = fields.make_outputs(name, nx, ny, nz)
+            want = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+            orc.run_oracle(spec, want, sc, nx, ny, nz, H)
+            host = {k: pkg.Storage(v.copy(), H) for k, v in {**inputs, **outs}.items()}
+            pkg.call(name, host, sc, domain=(nx, ny, nz))
+            for a in spec.by_role("out3"):
+                assert_bitwise_equal(host[a.name].numpy(), want[a.name], "%s.%s slabs %d" % (name, a.name, slabs))
+    finally:
+        lib.oeb_set_host_slabs(0)
+        lib.oeb_set_host_direct(1)
