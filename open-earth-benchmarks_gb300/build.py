@@ -33,6 +33,7 @@ UNITS = {
     "k_fvtp2d.cu": ["--fmad=false"],
     "chain.cu": ["--fmad=false"],
     "batch.cu": [],
+    "selftest.cu": [],
 }
 
 

@@ -9,6 +9,12 @@
 // walk a list of (member, tile) items.  The bodies never read blockIdx or gridDim, so a tile
 // computes the same results in either form.
 //
+// Every kernel instantiated for double runs as the same kernel instantiated for F64i
+// (precision.cuh): double arithmetic with the multiplications on the integer pipe, bit for
+// bit the same results.  launch() rebinds the Body and reinterprets its arguments (double,
+// double*, and structs or pointers of a template over double) as their F64i twins, which
+// have the same layout.
+//
 // Scratch memory of a call (adjoint terms, dual-number arrays) comes from scratch_alloc: the
 // library's stream-ordered pool normally, the plan's arena while recording (so that it lives
 // as long as the plan).
@@ -22,6 +28,7 @@
 #include <vector>
 
 #include "oeb_common.cuh"
+#include "precision.cuh"
 
 namespace oeb {
 
@@ -147,8 +154,66 @@ int batch_occupancy(size_t smem) {
   return n;
 }
 
+// ---- double -> F64i ----------------------------------------------------------------------
+template <class B>
+struct Rebind {
+  using type = B;
+  static constexpr bool on = false;
+};
+template <template <class> class K>
+struct Rebind<K<double>> {
+  using type = K<F64i>;
+  static constexpr bool on = true;
+};
+template <template <class, int> class K, int N>
+struct Rebind<K<double, N>> {
+  using type = K<F64i, N>;
+  static constexpr bool on = true;
+};
+
+template <class A>
+struct ArgMap {
+  using type = A;
+  static A conv(A a) { return a; }
+};
+template <>
+struct ArgMap<double> {
+  using type = F64i;
+  static F64i conv(double a) { return F64i(a); }
+};
+template <>
+struct ArgMap<double*> {
+  using type = F64i*;
+  static F64i* conv(double* a) { return reinterpret_cast<F64i*>(a); }
+};
+template <>
+struct ArgMap<const double*> {
+  using type = const F64i*;
+  static const F64i* conv(const double* a) { return reinterpret_cast<const F64i*>(a); }
+};
+template <template <class> class X>
+struct ArgMap<X<double>> {
+  using type = X<F64i>;
+  static X<F64i> conv(const X<double>& a) {
+    static_assert(sizeof(X<F64i>) == sizeof(X<double>), "F64i twin must have the same layout");
+    X<F64i> r;
+    memcpy(static_cast<void*>(&r), &a, sizeof(r));
+    return r;
+  }
+};
+template <template <class> class X>
+struct ArgMap<X<double>*> {
+  using type = X<F64i>*;
+  static X<F64i>* conv(X<double>* a) { return reinterpret_cast<X<F64i>*>(a); }
+};
+template <template <class> class X>
+struct ArgMap<const X<double>*> {
+  using type = const X<F64i>*;
+  static const X<F64i>* conv(const X<double>* a) { return reinterpret_cast<const X<F64i>*>(a); }
+};
+
 template <class Body, class... A>
-oeb_status launch(dim3 grid, size_t smem, cudaStream_t st, A... a) {
+oeb_status launch_as(dim3 grid, size_t smem, cudaStream_t st, A... a) {
   if (grid.x == 0 || grid.y == 0 || grid.z == 0) return OEB_OK;
   if (Recorder* r = recorder()) {
     LaunchRecord rec;
@@ -165,6 +230,15 @@ oeb_status launch(dim3 grid, size_t smem, cudaStream_t st, A... a) {
   if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_kernel<Body, A...>, (int)smem));
   grid_kernel<Body, A...><<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(a...);
   return after_launch();
+}
+
+template <class Body, class... A>
+oeb_status launch(dim3 grid, size_t smem, cudaStream_t st, A... a) {
+  if constexpr (Rebind<Body>::on) {
+    return launch_as<typename Rebind<Body>::type, typename ArgMap<A>::type...>(grid, smem, st, ArgMap<A>::conv(a)...);
+  } else {
+    return launch_as<Body, A...>(grid, smem, st, a...);
+  }
 }
 
 }  // namespace oeb

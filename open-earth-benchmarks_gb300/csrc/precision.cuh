@@ -26,11 +26,15 @@ struct Prec;
 
 // FP64 operations done exactly on the integer pipe.  The GB300 issues 1.6 FP64 operations
 // per clock per SM and about 100 integer ones, and the FP64 stencils are bound by the FP64
-// pipe; so sign tests, comparisons of non-negative values, multiplications by powers of two
-// and the multiply by a 0/1 flag of fvtp2d are done on the bit patterns.  Each gives the
-// result of the FP64 operation it replaces, bit for bit, and falls back to that operation
-// for every input where the shortcut could differ (zeros, subnormals, infinities, NaN, a
-// product that could underflow, a scaling that could leave the normal range).
+// pipe; so multiplications, sign tests, comparisons of non-negative values, multiplications
+// by powers of two and the multiply by a 0/1 flag of fvtp2d are done on the bit patterns.
+// Each gives the result of the FP64 operation it replaces, bit for bit, and falls back to
+// that operation for every input where the shortcut could differ (zeros, subnormals,
+// infinities, NaN, a result that could underflow or overflow).
+//
+// The fallbacks are calls, not inline operations: an inline FP64 operation on a branch is
+// if-converted into a predicated instruction that takes its slot in the FP64 pipe on every
+// pass, taken or not, and the integer path would then save nothing.
 namespace fp64 {
 __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
 __device__ __forceinline__ int exponent(long long b) { return (int)((b >> 52) & 0x7FF); }
@@ -40,6 +44,108 @@ __device__ __forceinline__ bool product_sign_known(long long ua, long long ub) {
   const int ea = exponent(ua), eb = exponent(ub);
   return ea > 0 && eb > 0 && ea < 2047 && eb < 2047 && ea + eb >= 972;
 }
+
+static __device__ __noinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+static __device__ __noinline__ double add_mul0_rn(double q, double t) { return __dadd_rn(q, __dmul_rn(t, 0.0)); }
+
+// a * b rounded to nearest even, on the integer pipe.  For normal a, b whose product is
+// normal: the exact product of the two 53-bit significands (1.f, hidden bit set) has 105 or
+// 106 bits; its top 53 bits are the significand of the result, the next bit is the round
+// bit and the OR of the rest the sticky bit, and IEEE 754 round-to-nearest-even adds one
+// ulp when round and (sticky or the last kept bit) are set.  A carry out of the significand
+// moves into the exponent field by itself, which is the correct rounding up to the next
+// power of two.  The 106-bit product comes from four 32 x 32 -> 64-bit multiplies of the
+// significands split into a high part of 21 bits and a low part of 32.  Any other input --
+// a zero, subnormal, infinite or NaN operand, or an exponent sum outside [1, 2045] where the
+// result could be subnormal or overflow -- takes the FP64 multiply.
+__device__ __forceinline__ double mul(double a, double b) {
+  const unsigned long long ua = (unsigned long long)bits(a), ub = (unsigned long long)bits(b);
+  const unsigned ha = (unsigned)(ua >> 32), hb = (unsigned)(ub >> 32);
+  const unsigned la = (unsigned)ua, lb = (unsigned)ub;
+  const unsigned ea = (ha >> 20) & 0x7FFu, eb = (hb >> 20) & 0x7FFu;
+  const unsigned a1 = (ha & 0xFFFFFu) | 0x100000u, b1 = (hb & 0xFFFFFu) | 0x100000u;
+  // (a1 2^32 + la)(b1 2^32 + lb) = w3:w2:w1:w0 (32-bit words), in [2^104, 2^106)
+  const unsigned long long p00 = (unsigned long long)la * lb;
+  const unsigned long long p01 = (unsigned long long)la * b1 + (p00 >> 32);
+  const unsigned long long p10 = (unsigned long long)a1 * lb + (unsigned)p01;
+  const unsigned long long p11 = (unsigned long long)a1 * b1 + (p01 >> 32) + (p10 >> 32);
+  const unsigned w0 = (unsigned)p00, w1 = (unsigned)p10, w2 = (unsigned)p11, w3 = (unsigned)(p11 >> 32);
+  const unsigned top = w3 >> 9;  // 1 if the product has 106 bits
+  const unsigned sh = 20u + top;  // significand = (w3:w2:w1) >> sh, hidden bit at bit 52
+  const unsigned mlo = __funnelshift_r(w1, w2, sh);
+  const unsigned mhi = __funnelshift_r(w2, w3, sh);
+  // the bits below the significand, left-aligned: bit 31 is the round bit; w0 joins the
+  // sticky bits at bit 0 (the shift leaves at least 11 zero bits there)
+  const unsigned rest = (w1 << (12u - top)) | (w0 != 0u ? 1u : 0u);
+  const unsigned up = (rest + (mlo & 1u)) > 0x80000000u ? 1u : 0u;
+  const int e = (int)(ea + eb) - 1023 + (int)top;  // biased exponent before rounding
+  unsigned long long r = ((((unsigned long long)mhi) << 32) | mlo) + up;
+  r += (unsigned long long)(unsigned)(e - 1) << 52;  // the hidden bit adds the last 1
+  r |= ((unsigned long long)((ha ^ hb) & 0x80000000u)) << 32;
+  const bool fast = (ea - 1u < 2046u) & (eb - 1u < 2046u) & ((unsigned)(e - 1) < 2045u);
+  if (__builtin_expect(!fast, 0)) return mul_rn(a, b);
+  return __longlong_as_double((long long)r);
+}
+
+static __device__ __noinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+// FP32 reciprocal estimate (PTX rcp.approx: relative error within a few 2^-23)
+__device__ __forceinline__ float rcp_estimate(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// a / b rounded to nearest even, on the integer pipe, by digit recurrence.  For normal a,
+// b whose quotient is normal: with the significands ma, mb in [2^52, 2^53) and X = ma (or
+// 2 ma when ma < mb, the exponent one lower) so that X / mb is in [1, 2), the result's
+// significand and round bit are Q = floor(X 2^53 / mb), in [2^53, 2^54), and its sticky bit
+// is (X 2^53 - Q mb != 0).  Q is found as three digits of 20, 20 and 13 bits: each digit q
+// estimates P 2^s / mb for the current remainder P with a 30-bit fixed-point reciprocal R
+// of mb (from the FP32 reciprocal of mb's top 24 bits), rounded to nearest, and the next
+// remainder P 2^s - q mb is computed exactly in 64-bit two's complement (it is below 2 mb in
+// magnitude, so the arithmetic modulo 2^64 is exact).  A digit may be off by one; the
+// remainders stay signed and the last one, within (-mb, 2 mb), is brought into [0, mb) by
+// one correction of Q.  Round-to-nearest-even then adds one ulp when the round bit is set
+// and the remainder or the last kept bit is nonzero.  Inputs outside that case -- zeros,
+// subnormals, infinities, NaN, a quotient that could be subnormal or overflow -- and any
+// remainder still outside [0, mb) take the FP64 division.
+__device__ __forceinline__ double div(double a, double b) {
+  typedef unsigned long long u64;
+  typedef long long i64;
+  const u64 ua = (u64)bits(a), ub = (u64)bits(b);
+  const unsigned ha = (unsigned)(ua >> 32), hb = (unsigned)(ub >> 32);
+  const unsigned ea = (ha >> 20) & 0x7FFu, eb = (hb >> 20) & 0x7FFu;
+  const u64 ma = (ua & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const u64 mb = (ub & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const bool lt = ma < mb;
+  const u64 X = lt ? ma << 1 : ma;
+  const int e = (int)ea - (int)eb + 1023 - (lt ? 1 : 0);  // biased exponent before rounding
+  // R ~ 2^82 / mb, in (2^29, 2^30]: 2^29 / (mb >> 29) scaled by 2^53
+  const int R = (int)(rcp_estimate((float)(int)(mb >> 29)) * 9007199254740992.0f);
+  // digit q ~ P 2^s / mb = (P >> 24) R 2^(s - 58), rounded to nearest
+  const int qa = (int)(((i64)(int)(X >> 24) * R + (1ll << 37)) >> 38);
+  const u64 P1 = (X << 20) - (u64)((i64)qa * (i64)mb);
+  const int qb = (int)(((i64)(int)((i64)P1 >> 24) * R + (1ll << 37)) >> 38);
+  const u64 P2 = (P1 << 20) - (u64)((i64)qb * (i64)mb);
+  const int qc = (int)(((i64)(int)((i64)P2 >> 24) * R + (1ll << 44)) >> 45);
+  i64 P = (i64)((P2 << 13) - (u64)((i64)qc * (i64)mb));
+  i64 Q = ((i64)qa << 33) + ((i64)qb << 13) + qc;
+  if (P < 0) {
+    Q -= 1;
+    P += (i64)mb;
+  } else if (P >= (i64)mb) {
+    Q += 1;
+    P -= (i64)mb;
+  }
+  const u64 sig = (u64)Q >> 1;  // hidden bit at bit 52
+  const unsigned up = (unsigned)(Q & 1) & ((P != 0 ? 1u : 0u) | (unsigned)(sig & 1));
+  u64 r = sig + up + ((u64)(unsigned)(e - 1) << 52);
+  r |= ((u64)((ha ^ hb) & 0x80000000u)) << 32;
+  const bool fast = (ea - 1u < 2046u) & (eb - 1u < 2046u) & ((unsigned)(e - 1) < 2045u) & (P >= 0) & (P < (i64)mb);
+  if (__builtin_expect(!fast, 0)) return div_rn(a, b);
+  return __longlong_as_double((long long)r);
+}
 }  // namespace fp64
 
 template <>
@@ -48,11 +154,11 @@ struct Prec<double> {
   // reference semantics: the rounded FP64 product compared with 0 (hdiffsa.h:106, fvtp2d.h:23)
   __device__ static __forceinline__ bool prod_gt0(double a, double b) {
     const long long ua = fp64::bits(a), ub = fp64::bits(b);
-    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) >= 0 : a * b > 0;
+    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) >= 0 : fp64::mul_rn(a, b) > 0;
   }
   __device__ static __forceinline__ bool prod_lt0(double a, double b) {
     const long long ua = fp64::bits(a), ub = fp64::bits(b);
-    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) < 0 : (a * b) < 0.0;
+    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) < 0 : fp64::mul_rn(a, b) < 0.0;
   }
   __device__ static __forceinline__ double sqrt_(double x) { return sqrt(x); }
   // x > 0 (false for NaN and -0)
@@ -68,14 +174,14 @@ struct Prec<double> {
     const long long b = fp64::bits(x);
     const int e = fp64::exponent(b);
     if (e > 0 && e < 2047 && e + K > 0 && e + K < 2047) return __longlong_as_double(b + ((long long)K << 52));
-    return x * (K >= 0 ? double(1LL << (K >= 0 ? K : 0)) : 1.0 / double(1LL << (K < 0 ? -K : 0)));
+    return fp64::mul_rn(x, K >= 0 ? double(1LL << (K >= 0 ? K : 0)) : 1.0 / double(1LL << (K < 0 ? -K : 0)));
   }
   // q + t * (flag ? 1.0 : 0.0): t * 1 is t; t * 0 is a zero with t's sign (t finite), and
   // q + (+-0) is q except -0 + +0 = +0
   __device__ static __forceinline__ double add_flag(double q, double t, bool flag) {
     if (flag) return q + t;
     const long long bt = fp64::bits(t);
-    if (fp64::exponent(bt) == 0x7FF) return q + t * 0.0;  // t infinite or NaN
+    if (fp64::exponent(bt) == 0x7FF) return fp64::add_mul0_rn(q, t);  // t infinite or NaN
     return (fp64::bits(q) == (long long)0x8000000000000000ULL && bt >= 0) ? 0.0 : q;
   }
 };
@@ -98,6 +204,65 @@ struct Prec<float> {
     return x * (K >= 0 ? float(1LL << (K >= 0 ? K : 0)) : 1.0f / float(1LL << (K < 0 ? -K : 0)));
   }
   __device__ static __forceinline__ float add_flag(float q, float t, bool flag) { return q + t * (flag ? 1.f : 0.f); }
+};
+
+// FP64 in the stencil kernels: a double whose multiplications and divisions run on the
+// integer pipe (fp64::mul, fp64::div) and whose additions, subtractions and square roots
+// are the FP64 instructions.  Every operation rounds exactly as the double operation does,
+// so a kernel gives the same bits with F64i as with double; the FP64 pipe, which bounds
+// these kernels, then carries only the additions and square roots, while the integer pipe
+// does the multiplications and divisions beside it.  Same size and alignment as double:
+// double fields are read and written as F64i in place.  launch() (launch.cuh) runs every
+// kernel instantiated for double with F64i.
+struct F64i {
+  double v;
+  F64i() = default;
+  __host__ __device__ constexpr F64i(double x) : v(x) {}
+};
+static_assert(sizeof(F64i) == sizeof(double) && alignof(F64i) == alignof(double), "F64i must alias double");
+
+__host__ __device__ constexpr F64i operator+(F64i a, F64i b) { return F64i(a.v + b.v); }
+__host__ __device__ constexpr F64i operator-(F64i a, F64i b) { return F64i(a.v - b.v); }
+// constant expressions (the kernels' folded coefficients) divide at compile time
+__host__ __device__ constexpr F64i operator/(F64i a, F64i b) {
+#if defined(__CUDA_ARCH__)
+  if (!__builtin_is_constant_evaluated()) return F64i(fp64::div(a.v, b.v));
+#endif
+  return F64i(a.v / b.v);
+}
+__host__ __device__ constexpr F64i operator-(F64i a) { return F64i(-a.v); }
+__device__ __forceinline__ F64i operator*(F64i a, F64i b) { return F64i(fp64::mul(a.v, b.v)); }
+__device__ __forceinline__ F64i& operator+=(F64i& a, F64i b) { return a = a + b; }
+__device__ __forceinline__ F64i& operator-=(F64i& a, F64i b) { return a = a - b; }
+__device__ __forceinline__ F64i& operator*=(F64i& a, F64i b) { return a = a * b; }
+__device__ __forceinline__ F64i& operator/=(F64i& a, F64i b) { return a = a / b; }
+__host__ __device__ constexpr bool operator<(F64i a, F64i b) { return a.v < b.v; }
+__host__ __device__ constexpr bool operator>(F64i a, F64i b) { return a.v > b.v; }
+__host__ __device__ constexpr bool operator<=(F64i a, F64i b) { return a.v <= b.v; }
+__host__ __device__ constexpr bool operator>=(F64i a, F64i b) { return a.v >= b.v; }
+__host__ __device__ constexpr bool operator==(F64i a, F64i b) { return a.v == b.v; }
+__host__ __device__ constexpr bool operator!=(F64i a, F64i b) { return a.v != b.v; }
+// fused multiply-add of the adjoint accumulations: the FP64 instruction (one rounding); the
+// float and double overloads stay visible beside it
+using ::fma;
+__device__ __forceinline__ F64i fma(F64i a, F64i b, F64i c) { return F64i(::fma(a.v, b.v, c.v)); }
+__device__ __forceinline__ F64i ld(const F64i* p) { return F64i(__ldg(reinterpret_cast<const double*>(p))); }
+
+template <>
+struct Prec<F64i> {
+  static constexpr bool kCompensated = false;
+  __device__ static __forceinline__ bool prod_gt0(F64i a, F64i b) { return Prec<double>::prod_gt0(a.v, b.v); }
+  __device__ static __forceinline__ bool prod_lt0(F64i a, F64i b) { return Prec<double>::prod_lt0(a.v, b.v); }
+  __device__ static __forceinline__ F64i sqrt_(F64i x) { return F64i(sqrt(x.v)); }
+  __device__ static __forceinline__ bool gt0(F64i x) { return Prec<double>::gt0(x.v); }
+  __device__ static __forceinline__ bool lt_nonneg(F64i a, F64i b) { return Prec<double>::lt_nonneg(a.v, b.v); }
+  template <int K>
+  __device__ static __forceinline__ F64i scale2(F64i x) {
+    return F64i(Prec<double>::template scale2<K>(x.v));
+  }
+  __device__ static __forceinline__ F64i add_flag(F64i q, F64i t, bool flag) {
+    return F64i(Prec<double>::add_flag(q.v, t.v, flag));
+  }
 };
 
 // the same operations by element type

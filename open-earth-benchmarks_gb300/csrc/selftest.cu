@@ -1,0 +1,101 @@
+// selftest.cu -- oeb_selftest_fp64: the integer-pipe FP64 multiply and division
+// (precision.cuh, fp64::mul and fp64::div) against the FP64 instructions on seeded random
+// operands, on the device.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "oeb_common.cuh"
+#include "precision.cuh"
+
+namespace oeb {
+namespace {
+
+__device__ __forceinline__ uint64_t splitmix(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// One operand of distribution `mode` from the hash h.
+__device__ double operand(uint64_t h, int mode) {
+  uint64_t m = h & 0xFFFFFFFFFFFFFull;
+  const uint64_t sign = h & 0x8000000000000000ull;
+  const uint64_t g = splitmix(h);
+  uint64_t e;
+  switch (mode) {
+    case 0:
+      return __longlong_as_double((long long)h);
+    case 1:
+      e = 1023 - 40 + g % 81;
+      break;
+    case 2:
+      e = (g & 1) ? 1 + (g >> 1) % 60 : 2046 - (g >> 1) % 60;
+      break;
+    case 3:
+      e = 1 + g % 2046;
+      m &= ~((1ull << ((g >> 40) % 52)) - 1);
+      break;
+    default:
+      e = 1023 - 5 + g % 11;
+      m = (g & 4) ? (m | 0xFFFFF00000000ull) : (m & 0xFF);
+      break;
+  }
+  return __longlong_as_double((long long)(sign | (e << 52) | m));
+}
+
+__global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsigned long long* bad,
+                                unsigned long long* first) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const uint64_t h = splitmix(seed ^ (uint64_t)t);
+    double a, b;
+    if (mode == 5) {  // b times a small integer over b: exact quotients and quotients near 1
+      b = operand(splitmix(h + 17), 1);
+      a = __dmul_rn(b, (double)(1 + h % 1000));
+    } else {
+      a = operand(h, mode);
+      b = operand(splitmix(h + 17), mode);
+    }
+    const double want = op == 0 ? __dmul_rn(a, b) : __ddiv_rn(a, b);
+    const double got = op == 0 ? fp64::mul(a, b) : fp64::div(a, b);
+    const unsigned long long bw = (unsigned long long)__double_as_longlong(want);
+    const unsigned long long bg = (unsigned long long)__double_as_longlong(got);
+    if (bw != bg && !(want != want && got != got)) {
+      if (atomicAdd(bad, 1ull) == 0ull) {
+        first[0] = (unsigned long long)__double_as_longlong(a);
+        first[1] = (unsigned long long)__double_as_longlong(b);
+        first[2] = bw;
+        first[3] = bg;
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace oeb
+
+extern "C" oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int mode, uint64_t* mismatches,
+                                        uint64_t* first) {
+  if (!mismatches) return OEB_ERR_NULL;
+  if (op < 0 || op > 1 || pairs < 0 || mode < 0 || mode > 5) return OEB_ERR_ARGUMENT;
+  unsigned long long* d = nullptr;
+  OEB_CUDA_TRY(cudaMalloc(&d, 5 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
+  if (e == cudaSuccess && pairs > 0) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    oeb::selftest_kernel<<<sms * 8, 256>>>(op, seed, pairs, mode, d, d + 1);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) oeb::count_launches(1);
+  }
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return oeb::cuda_fail(e);
+  *mismatches = h[0];
+  if (first)
+    for (int i = 0; i < 4; ++i) first[i] = h[1 + i];
+  return OEB_OK;
+}

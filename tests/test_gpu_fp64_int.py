@@ -1,0 +1,41 @@
+"""The FP64 multiply and division of the FP64 kernels, done on the integer pipe, against the
+FP64 instructions.
+
+oeb_selftest_fp64 computes seeded random operand pairs both ways on the GPU and counts
+results that differ in any bit.  Six distributions: any bit pattern (NaN, infinities, zeros
+and subnormals take the fallback), ordinary magnitudes, exponents near both ends of the
+normal range (results that underflow or overflow), short significands (rounding ties),
+significands near all-ones and near zero (carries out of the significand), and exact
+quotients (b times a small integer, over b).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PAIRS = 1 << 27
+
+
+@pytest.mark.parametrize("mode", range(6), ids=["any-bits", "ordinary", "range-ends", "ties", "carries", "exact"])
+@pytest.mark.parametrize("op", [0, 1], ids=["mul", "div"])
+def test_integer_pipe_operation_is_the_fp64_operation(pkg, cuda, op, mode):
+    lib = pkg.load_library()
+    bad = ctypes.c_uint64(0)
+    first = (ctypes.c_uint64 * 4)()
+    st = lib.oeb_selftest_fp64(ctypes.c_int(op), ctypes.c_int64(PAIRS), ctypes.c_uint64(0xC0FFEE + 7919 * mode + op),
+                               ctypes.c_int(mode), ctypes.byref(bad), first)
+    assert st == 0, st
+    assert bad.value == 0, "%d of %d results differ; first a=%016x b=%016x fp64=%016x int=%016x" % (
+        bad.value, PAIRS, first[0], first[1], first[2], first[3])
+
+
+def test_selftest_rejects_bad_arguments(pkg, cuda):
+    lib = pkg.load_library()
+    bad = ctypes.c_uint64(0)
+    args = (ctypes.c_int64(16), ctypes.c_uint64(1))
+    assert lib.oeb_selftest_fp64(ctypes.c_int(0), *args, ctypes.c_int(9), ctypes.byref(bad), None) != 0
+    assert lib.oeb_selftest_fp64(ctypes.c_int(2), *args, ctypes.c_int(0), ctypes.byref(bad), None) != 0
+    assert lib.oeb_selftest_fp64(ctypes.c_int(0), *args, ctypes.c_int(0), None, None) != 0
