@@ -45,8 +45,23 @@ __device__ __forceinline__ bool product_sign_known(long long ua, long long ub) {
   return ea > 0 && eb > 0 && ea < 2047 && eb < 2047 && ea + eb >= 972;
 }
 
-static __device__ __noinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
-static __device__ __noinline__ double add_mul0_rn(double q, double t) { return __dadd_rn(q, __dmul_rn(t, 0.0)); }
+// The fallbacks of the integer-pipe operations below take and return bit patterns: their
+// result then merges with the fast path's as an integer, where a merge of two doubles has
+// been seen to cost an FP64 instruction on every pass.
+static __device__ __noinline__ unsigned long long mul_bits(unsigned long long a, unsigned long long b) {
+  return (unsigned long long)bits(__dmul_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b)));
+}
+static __device__ __noinline__ unsigned long long div_bits(unsigned long long a, unsigned long long b) {
+  return (unsigned long long)bits(__ddiv_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b)));
+}
+static __device__ __noinline__ unsigned long long add_bits(unsigned long long a, unsigned long long b) {
+  return (unsigned long long)bits(__dadd_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b)));
+}
+// q + t * 0.0, both roundings (t infinite or NaN: a NaN)
+static __device__ __noinline__ unsigned long long add_mul0_bits(unsigned long long q, unsigned long long t) {
+  return (unsigned long long)bits(
+      __dadd_rn(__longlong_as_double((long long)q), __dmul_rn(__longlong_as_double((long long)t), 0.0)));
+}
 
 // a * b rounded to nearest even, on the integer pipe.  For normal a, b whose product is
 // normal: the exact product of the two 53-bit significands (1.f, hidden bit set) has 105 or
@@ -83,11 +98,9 @@ __device__ __forceinline__ double mul(double a, double b) {
   r += (unsigned long long)(unsigned)(e - 1) << 52;  // the hidden bit adds the last 1
   r |= ((unsigned long long)((ha ^ hb) & 0x80000000u)) << 32;
   const bool fast = (ea - 1u < 2046u) & (eb - 1u < 2046u) & ((unsigned)(e - 1) < 2045u);
-  if (__builtin_expect(!fast, 0)) return mul_rn(a, b);
+  if (__builtin_expect(!fast, 0)) r = mul_bits(ua, ub);
   return __longlong_as_double((long long)r);
 }
-
-static __device__ __noinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 
 // FP32 reciprocal estimate (PTX rcp.approx: relative error within a few 2^-23)
 __device__ __forceinline__ float rcp_estimate(float x) {
@@ -143,8 +156,86 @@ __device__ __forceinline__ double div(double a, double b) {
   u64 r = sig + up + ((u64)(unsigned)(e - 1) << 52);
   r |= ((u64)((ha ^ hb) & 0x80000000u)) << 32;
   const bool fast = (ea - 1u < 2046u) & (eb - 1u < 2046u) & ((unsigned)(e - 1) < 2045u) & (P >= 0) & (P < (i64)mb);
-  if (__builtin_expect(!fast, 0)) return div_rn(a, b);
+  if (__builtin_expect(!fast, 0)) r = div_bits(ua, ub);
   return __longlong_as_double((long long)r);
+}
+
+// a + b rounded to nearest even, on the integer pipe.  With |x| >= |y| the operands ordered
+// by magnitude (their bit patterns without the sign order as the magnitudes), the 53-bit
+// significands are placed at bits 62..10 of 64-bit words, so ten guard bits sit below
+// them; y's is shifted right by the exponent difference with every bit shifted out ORed
+// into bit 0 (the sticky bit).  The significands are added or, for opposite signs,
+// subtracted (the difference is >= 0), the sum is normalised so that its leading bit is
+// bit 63 (at most one place right for a sum, any number left for a difference -- a left
+// shift of more than two places happens only when no bit was shifted out), and
+// round-to-nearest-even on bits 10..0 gives the result, the exponent following the
+// normalisation.  Exact cancellation gives +0 and y = +-0 gives x, as IEEE addition does.
+// Zeros for x, subnormals, infinities, NaN and a result that could be subnormal or
+// overflow take the FP64 addition.
+__device__ __forceinline__ double add(double a, double b) {
+  typedef unsigned long long u64;
+  const u64 M = 0x7FFFFFFFFFFFFFFFull;
+  const u64 ua = (u64)bits(a), ub = (u64)bits(b);
+  const u64 aa = ua & M, ab = ub & M;
+  const bool sw = ab > aa;
+  const u64 x = sw ? ub : ua, y = sw ? ua : ub;
+  const u64 ax = sw ? ab : aa, ay = sw ? aa : ab;
+  const unsigned ex = (unsigned)(ax >> 52), ey = (unsigned)(ay >> 52);
+  const u64 mx = ((ax & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) << 10;
+  const u64 my = ((ay & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) << 10;
+  const unsigned d = ex - ey;
+  const unsigned dc = d < 63u ? d : 63u;
+  const u64 ya = (my >> dc) | ((my & ((1ull << dc) - 1ull)) != 0ull ? 1ull : 0ull);
+  const bool sub = (long long)(x ^ y) < 0;
+  const u64 S = sub ? mx - ya : mx + ya;
+  const int lz = __clzll((long long)S);
+  const u64 N = S << (lz & 63);
+  const u64 sig = N >> 11;
+  const unsigned rest = (unsigned)N & 0x7FFu;
+  const unsigned up = (rest + (unsigned)(sig & 1ull)) > 0x400u ? 1u : 0u;
+  const int e = (int)ex + 1 - lz;  // biased exponent before rounding
+  u64 r = (((u64)(unsigned)(e - 1)) << 52) + sig + up;
+  r |= x & 0x8000000000000000ull;
+  const bool xok = ex - 1u < 2046u;
+  bool fast = xok & (ey - 1u < 2046u) & ((unsigned)(e - 1) < 2045u);
+  if (S == 0ull) {
+    r = 0ull;
+    fast = xok;
+  }
+  if (ay == 0ull) {
+    r = x;
+    fast = xok;
+  }
+  if (__builtin_expect(!fast, 0)) r = add_bits(ua, ub);
+  return __longlong_as_double((long long)r);
+}
+
+// -x: the sign bit flipped (IEEE negation)
+__device__ __forceinline__ double neg(double x) {
+  return __longlong_as_double(bits(x) ^ (long long)0x8000000000000000ull);
+}
+
+// Ordered comparisons on the bit patterns: a pattern mapped to its magnitude, negated for a
+// negative sign, orders as the values do (+0 and -0 both map to 0); any comparison with a
+// NaN is false.
+__device__ __forceinline__ long long order_key(long long b) {
+  const long long m = b & 0x7FFFFFFFFFFFFFFFll;
+  return b < 0 ? -m : m;
+}
+__device__ __forceinline__ bool unordered(long long a, long long b) {
+  return ((a & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll) | ((b & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll);
+}
+__device__ __forceinline__ bool lt(double a, double b) {
+  const long long ia = bits(a), ib = bits(b);
+  return !unordered(ia, ib) && order_key(ia) < order_key(ib);
+}
+__device__ __forceinline__ bool le(double a, double b) {
+  const long long ia = bits(a), ib = bits(b);
+  return !unordered(ia, ib) && order_key(ia) <= order_key(ib);
+}
+__device__ __forceinline__ bool eq(double a, double b) {
+  const long long ia = bits(a), ib = bits(b);
+  return !unordered(ia, ib) && order_key(ia) == order_key(ib);
 }
 }  // namespace fp64
 
@@ -154,11 +245,16 @@ struct Prec<double> {
   // reference semantics: the rounded FP64 product compared with 0 (hdiffsa.h:106, fvtp2d.h:23)
   __device__ static __forceinline__ bool prod_gt0(double a, double b) {
     const long long ua = fp64::bits(a), ub = fp64::bits(b);
-    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) >= 0 : fp64::mul_rn(a, b) > 0;
+    if (fp64::product_sign_known(ua, ub)) return (ua ^ ub) >= 0;
+    const long long p = (long long)fp64::mul_bits((unsigned long long)ua, (unsigned long long)ub);
+    return p > 0 && p <= 0x7FF0000000000000LL;  // positive, not NaN
   }
   __device__ static __forceinline__ bool prod_lt0(double a, double b) {
     const long long ua = fp64::bits(a), ub = fp64::bits(b);
-    return fp64::product_sign_known(ua, ub) ? (ua ^ ub) < 0 : fp64::mul_rn(a, b) < 0.0;
+    if (fp64::product_sign_known(ua, ub)) return (ua ^ ub) < 0;
+    const long long p = (long long)fp64::mul_bits((unsigned long long)ua, (unsigned long long)ub);
+    const long long m = p & 0x7FFFFFFFFFFFFFFFLL;
+    return p < 0 && m != 0 && m <= 0x7FF0000000000000LL;  // negative, not -0, not NaN
   }
   __device__ static __forceinline__ double sqrt_(double x) { return sqrt(x); }
   // x > 0 (false for NaN and -0)
@@ -173,16 +269,26 @@ struct Prec<double> {
   __device__ static __forceinline__ double scale2(double x) {
     const long long b = fp64::bits(x);
     const int e = fp64::exponent(b);
-    if (e > 0 && e < 2047 && e + K > 0 && e + K < 2047) return __longlong_as_double(b + ((long long)K << 52));
-    return fp64::mul_rn(x, K >= 0 ? double(1LL << (K >= 0 ? K : 0)) : 1.0 / double(1LL << (K < 0 ? -K : 0)));
+    long long r = b + ((long long)K << 52);
+    if (!(e > 0 && e < 2047 && e + K > 0 && e + K < 2047)) {
+      const double f = K >= 0 ? double(1LL << (K >= 0 ? K : 0)) : 1.0 / double(1LL << (K < 0 ? -K : 0));
+      r = (long long)fp64::mul_bits((unsigned long long)b, (unsigned long long)fp64::bits(f));
+    }
+    return __longlong_as_double(r);
   }
   // q + t * (flag ? 1.0 : 0.0): t * 1 is t; t * 0 is a zero with t's sign (t finite), and
   // q + (+-0) is q except -0 + +0 = +0
   __device__ static __forceinline__ double add_flag(double q, double t, bool flag) {
-    if (flag) return q + t;
-    const long long bt = fp64::bits(t);
-    if (fp64::exponent(bt) == 0x7FF) return fp64::add_mul0_rn(q, t);  // t infinite or NaN
-    return (fp64::bits(q) == (long long)0x8000000000000000ULL && bt >= 0) ? 0.0 : q;
+    const long long bq = fp64::bits(q), bt = fp64::bits(t);
+    long long r;
+    if (flag) {
+      r = fp64::bits(q + t);
+    } else if (fp64::exponent(bt) == 0x7FF) {  // t infinite or NaN
+      r = (long long)fp64::add_mul0_bits((unsigned long long)bq, (unsigned long long)bt);
+    } else {
+      r = (bq == (long long)0x8000000000000000ULL && bt >= 0) ? 0 : bq;
+    }
+    return __longlong_as_double(r);
   }
 };
 
@@ -230,18 +336,23 @@ __host__ __device__ constexpr F64i operator/(F64i a, F64i b) {
 #endif
   return F64i(a.v / b.v);
 }
-__host__ __device__ constexpr F64i operator-(F64i a) { return F64i(-a.v); }
+__host__ __device__ constexpr F64i operator-(F64i a) {
+#if defined(__CUDA_ARCH__)
+  if (!__builtin_is_constant_evaluated()) return F64i(fp64::neg(a.v));
+#endif
+  return F64i(-a.v);
+}
 __device__ __forceinline__ F64i operator*(F64i a, F64i b) { return F64i(fp64::mul(a.v, b.v)); }
 __device__ __forceinline__ F64i& operator+=(F64i& a, F64i b) { return a = a + b; }
 __device__ __forceinline__ F64i& operator-=(F64i& a, F64i b) { return a = a - b; }
 __device__ __forceinline__ F64i& operator*=(F64i& a, F64i b) { return a = a * b; }
 __device__ __forceinline__ F64i& operator/=(F64i& a, F64i b) { return a = a / b; }
-__host__ __device__ constexpr bool operator<(F64i a, F64i b) { return a.v < b.v; }
-__host__ __device__ constexpr bool operator>(F64i a, F64i b) { return a.v > b.v; }
-__host__ __device__ constexpr bool operator<=(F64i a, F64i b) { return a.v <= b.v; }
-__host__ __device__ constexpr bool operator>=(F64i a, F64i b) { return a.v >= b.v; }
-__host__ __device__ constexpr bool operator==(F64i a, F64i b) { return a.v == b.v; }
-__host__ __device__ constexpr bool operator!=(F64i a, F64i b) { return a.v != b.v; }
+__device__ __forceinline__ bool operator<(F64i a, F64i b) { return fp64::lt(a.v, b.v); }
+__device__ __forceinline__ bool operator>(F64i a, F64i b) { return fp64::lt(b.v, a.v); }
+__device__ __forceinline__ bool operator<=(F64i a, F64i b) { return fp64::le(a.v, b.v); }
+__device__ __forceinline__ bool operator>=(F64i a, F64i b) { return fp64::le(b.v, a.v); }
+__device__ __forceinline__ bool operator==(F64i a, F64i b) { return fp64::eq(a.v, b.v); }
+__device__ __forceinline__ bool operator!=(F64i a, F64i b) { return !fp64::eq(a.v, b.v); }
 // fused multiply-add of the adjoint accumulations: the FP64 instruction (one rounding); the
 // float and double overloads stay visible beside it
 using ::fma;
@@ -264,6 +375,26 @@ struct Prec<F64i> {
     return F64i(Prec<double>::add_flag(q.v, t.v, flag));
   }
 };
+
+// An addition or subtraction that the FP64 kernels do on the integer pipe (fp64::add) to
+// balance it against the FP64 pipe; every other element type adds as usual.  The results
+// are those of + and -.
+template <class T>
+__device__ __forceinline__ T iadd(T a, T b) {
+  return a + b;
+}
+template <class T>
+__device__ __forceinline__ T isub(T a, T b) {
+  return a - b;
+}
+template <>
+__device__ __forceinline__ F64i iadd<F64i>(F64i a, F64i b) {
+  return F64i(fp64::add(a.v, b.v));
+}
+template <>
+__device__ __forceinline__ F64i isub<F64i>(F64i a, F64i b) {
+  return F64i(fp64::add(a.v, fp64::neg(b.v)));
+}
 
 // the same operations by element type
 template <class T>

@@ -1,6 +1,6 @@
-// selftest.cu -- oeb_selftest_fp64: the integer-pipe FP64 multiply and division
-// (precision.cuh, fp64::mul and fp64::div) against the FP64 instructions on seeded random
-// operands, on the device.
+// selftest.cu -- oeb_selftest_fp64: the integer-pipe FP64 multiply, division, addition and
+// subtraction (precision.cuh: fp64::mul, fp64::div, fp64::add, isub) against the FP64
+// instructions on seeded random operands, on the device.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -53,12 +53,24 @@ __global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsi
     if (mode == 5) {  // b times a small integer over b: exact quotients and quotients near 1
       b = operand(splitmix(h + 17), 1);
       a = __dmul_rn(b, (double)(1 + h % 1000));
+    } else if (mode == 6) {  // a + (-a (1 + small)): cancellation of all but a few bits
+      a = operand(h, 1);
+      b = -__dmul_rn(a, 1.0 + ldexp((double)(h % 1024), -52 + (int)(h % 7)));
+    } else if (mode == 7) {  // b = a 2^-k with its low bits changed: every alignment shift
+      a = operand(h, 1);
+      const double s2 = ldexp(a, -(int)(splitmix(h) % 70));
+      b = __longlong_as_double(__double_as_longlong((h & 1) ? -s2 : s2) ^ (long long)(splitmix(h + 3) & 0xFF));
     } else {
       a = operand(h, mode);
       b = operand(splitmix(h + 17), mode);
     }
-    const double want = op == 0 ? __dmul_rn(a, b) : __ddiv_rn(a, b);
-    const double got = op == 0 ? fp64::mul(a, b) : fp64::div(a, b);
+    double want, got;
+    switch (op) {
+      case 0: want = __dmul_rn(a, b); got = fp64::mul(a, b); break;
+      case 1: want = __ddiv_rn(a, b); got = fp64::div(a, b); break;
+      case 2: want = __dadd_rn(a, b); got = fp64::add(a, b); break;
+      default: want = __dsub_rn(a, b); got = isub(F64i(a), F64i(b)).v; break;
+    }
     const unsigned long long bw = (unsigned long long)__double_as_longlong(want);
     const unsigned long long bg = (unsigned long long)__double_as_longlong(got);
     if (bw != bg && !(want != want && got != got)) {
@@ -78,7 +90,7 @@ __global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsi
 extern "C" oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int mode, uint64_t* mismatches,
                                         uint64_t* first) {
   if (!mismatches) return OEB_ERR_NULL;
-  if (op < 0 || op > 1 || pairs < 0 || mode < 0 || mode > 5) return OEB_ERR_ARGUMENT;
+  if (op < 0 || op > 3 || pairs < 0 || mode < 0 || mode > 7) return OEB_ERR_ARGUMENT;
   unsigned long long* d = nullptr;
   OEB_CUDA_TRY(cudaMalloc(&d, 5 * sizeof(unsigned long long)));
   cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
