@@ -129,14 +129,15 @@ OEB_API oeb_status oeb_set_host_slabs(int slabs);
 OEB_API oeb_status oeb_set_host_direct(int enable);
 
 /* Self-check of the FP64 operations that the FP64 kernels run on the integer pipe: op 0
- * multiply, 1 divide, 2 add, 3 subtract.  `pairs` seeded random operand pairs of
- * distribution `mode` (0: any bit pattern; 1: magnitudes 2^-40..2^40; 2: exponents within
- * 60 of the normal range's ends; 3: short significands, which make rounding ties; 4:
- * significands near all-ones and near zero; 5: b times a small integer, and b; 6: a and
- * -a (1 + small), cancellation; 7: a and a 2^-k with changed low bits, every alignment)
- * are computed both ways on the current device; `mismatches` receives how many results
- * differ in any bit (NaNs compare equal), `first` (4 words, may be NULL) the first
- * differing a, b, FP64-instruction result and integer-pipe result.  Synchronous. */
+ * multiply, 1 divide, 2 add, 3 subtract, 4 square root of a.  `pairs` seeded random
+ * operand pairs of distribution `mode` (0: any bit pattern; 1: magnitudes 2^-40..2^40;
+ * 2: exponents within 60 of the normal range's ends; 3: short significands, which make
+ * rounding ties; 4: significands near all-ones and near zero; 5: b times a small integer,
+ * and b (for the square root: exact squares); 6: a and -a (1 + small), cancellation; 7: a
+ * and a 2^-k with changed low bits, every alignment) are computed both ways on the current
+ * device; `mismatches` receives how many results differ in any bit (NaNs compare equal),
+ * `first` (4 words, may be NULL) the first differing a, b, FP64-instruction result and
+ * integer-pipe result.  Synchronous. */
 OEB_API oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int mode, uint64_t* mismatches,
                                      uint64_t* first);
 

@@ -70,12 +70,12 @@ struct hdiffsa_kernel {
         s.in[b][a] = ok ? ld(pin + i + j * sj) : T(0);
       });
       __syncthreads();
-      for_region<34, 35>([&](int a, int b) { s.dy[b][a] = s.in[b + 1][a + 1] - s.in[b][a + 1]; });
+      for_region<34, 35>([&](int a, int b) { s.dy[b][a] = isub(s.in[b + 1][a + 1], s.in[b][a + 1]); });
       __syncthreads();
       // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
       for_region<34, 34>([&](int a, int b) {
         const T c = s.in[b + 1][a + 1];
-        s.lap[b][a] = (((s.in[b + 1][a] + s.in[b + 1][a + 2]) - T(2.0) * c) + s.crlato[b] * s.dy[b + 1][a]) +
+        s.lap[b][a] = ((iadd(s.in[b + 1][a], s.in[b + 1][a + 2]) - T(2.0) * c) + s.crlato[b] * s.dy[b + 1][a]) +
                       s.crlatu[b] * (-s.dy[b][a]);
       });
       __syncthreads();

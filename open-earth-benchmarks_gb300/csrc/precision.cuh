@@ -57,6 +57,9 @@ static __device__ __noinline__ unsigned long long div_bits(unsigned long long a,
 static __device__ __noinline__ unsigned long long add_bits(unsigned long long a, unsigned long long b) {
   return (unsigned long long)bits(__dadd_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b)));
 }
+static __device__ __noinline__ unsigned long long sqrt_bits(unsigned long long x) {
+  return (unsigned long long)bits(__dsqrt_rn(__longlong_as_double((long long)x)));
+}
 // q + t * 0.0, both roundings (t infinite or NaN: a NaN)
 static __device__ __noinline__ unsigned long long add_mul0_bits(unsigned long long q, unsigned long long t) {
   return (unsigned long long)bits(
@@ -210,6 +213,70 @@ __device__ __forceinline__ double add(double a, double b) {
   return __longlong_as_double((long long)r);
 }
 
+// FP32 reciprocal square root estimate (PTX rsqrt.approx: relative error within a few 2^-23)
+__device__ __forceinline__ float rsqrt_estimate(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// sqrt(x) rounded to nearest even, on the integer pipe.  For positive normal x with
+// significand m in [2^52, 2^53) and M = m (or 2 m, making the exponent even), the result's
+// significand and round bit are S = floor(sqrt(M 2^54)), in [2^53, 2^54), and its sticky
+// bit is (M 2^54 - S^2 != 0).  S is found in two halves of 27 bits, S = s1 2^27 + s0:
+//  * s1 = floor(sqrt(M)): an estimate from the FP32 reciprocal square root y of M's top 24
+//    bits, one Newton step s1 + (M - s1^2) / (2 s1) with the exact integer residual, and
+//    one correction that brings r = M - s1^2 into [0, 2 s1];
+//  * s0 ~ r 2^54 / (2 s1 2^27) from y, one Newton step on the residual
+//    R = r 2^54 - s0 (2 s1 2^27 + s0), computed exactly in 64-bit two's complement (it stays
+//    within a few multiples of 2 S), and one correction that brings R into [0, 2 S].
+// Round-to-nearest-even then adds one ulp when the round bit is set and R or the last kept
+// bit is nonzero (an exact tie cannot occur).  Zero, negative, subnormal, infinite and NaN
+// inputs, and any residual still outside [0, 2 S], take the FP64 square root.
+__device__ __forceinline__ double sqrt(double x) {
+  typedef unsigned long long u64;
+  typedef long long i64;
+  const u64 ux = (u64)bits(x);
+  const unsigned ex = (unsigned)(ux >> 52);  // with the sign: a negative x gives ex >= 2048
+  const u64 m = (ux & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const unsigned odd = (ex & 1u) ^ 1u;  // the unbiased exponent of m is odd
+  const u64 M = m << odd;               // [2^52, 2^54)
+  const float mf = (float)(unsigned)(M >> 30);  // [2^22, 2^24), exact
+  const float y = rsqrt_estimate(mf);
+  unsigned s1 = (unsigned)(mf * y * 32768.0f + 0.5f);
+  i64 r = (i64)(M - (u64)s1 * s1);
+  s1 = (unsigned)((int)s1 + (int)rintf((float)r * (y * (1.0f / 65536.0f))));
+  r = (i64)(M - (u64)s1 * s1);
+  if (r < 0) {
+    s1 -= 1;
+    r += 2 * (i64)s1 + 1;
+  } else if (r > 2 * (i64)s1) {
+    r -= 2 * (i64)s1 + 1;
+    s1 += 1;
+  }
+  int s0 = (int)rintf((float)r * (y * 2048.0f));
+  const u64 t = (u64)s1 << 28;
+  u64 rem = ((u64)r << 54) - (u64)(i64)s0 * (t + (u64)(i64)s0);
+  s0 += (int)rintf((float)(int)((i64)rem >> 32) * (y * (1.0f / 2048.0f)));
+  rem = ((u64)r << 54) - (u64)(i64)s0 * (t + (u64)(i64)s0);
+  u64 S = ((u64)s1 << 27) + (u64)(i64)s0;
+  i64 R = (i64)rem;
+  if (R < 0) {
+    R += 2 * (i64)S - 1;
+    S -= 1;
+  } else if (R > 2 * (i64)S) {
+    R -= 2 * (i64)S + 1;
+    S += 1;
+  }
+  const u64 sig = S >> 1;  // hidden bit at bit 52
+  const unsigned up = (unsigned)(S & 1ull) & ((R != 0 ? 1u : 0u) | (unsigned)(sig & 1ull));
+  const unsigned be = ((ex - odd - 1u) >> 1) + 512u;  // biased exponent of the root
+  u64 res = (((u64)(be - 1u)) << 52) + sig + up;
+  const bool fast = (ex - 1u < 2046u) & (R >= 0) & (R <= 2 * (i64)S);
+  if (__builtin_expect(!fast, 0)) res = sqrt_bits(ux);
+  return __longlong_as_double((long long)res);
+}
+
 // -x: the sign bit flipped (IEEE negation)
 __device__ __forceinline__ double neg(double x) {
   return __longlong_as_double(bits(x) ^ (long long)0x8000000000000000ull);
@@ -312,12 +379,13 @@ struct Prec<float> {
   __device__ static __forceinline__ float add_flag(float q, float t, bool flag) { return q + t * (flag ? 1.f : 0.f); }
 };
 
-// FP64 in the stencil kernels: a double whose multiplications and divisions run on the
-// integer pipe (fp64::mul, fp64::div) and whose additions, subtractions and square roots
-// are the FP64 instructions.  Every operation rounds exactly as the double operation does,
-// so a kernel gives the same bits with F64i as with double; the FP64 pipe, which bounds
-// these kernels, then carries only the additions and square roots, while the integer pipe
-// does the multiplications and divisions beside it.  Same size and alignment as double:
+// FP64 in the stencil kernels: a double whose multiplications, divisions, square roots
+// (Prec<F64i>::sqrt_), negations and comparisons run on the integer pipe (fp64::mul, div,
+// sqrt, neg, lt/le/eq) and whose additions and subtractions are the FP64 instruction, or
+// fp64::add where a kernel asks for it with iadd/isub.  Every operation rounds exactly as
+// the double operation does, so a kernel gives the same bits with F64i as with double; the
+// FP64 pipe, which bounds these kernels, then carries only the additions, while the
+// integer pipe does the rest beside it.  Same size and alignment as double:
 // double fields are read and written as F64i in place.  launch() (launch.cuh) runs every
 // kernel instantiated for double with F64i.
 struct F64i {
@@ -364,7 +432,7 @@ struct Prec<F64i> {
   static constexpr bool kCompensated = false;
   __device__ static __forceinline__ bool prod_gt0(F64i a, F64i b) { return Prec<double>::prod_gt0(a.v, b.v); }
   __device__ static __forceinline__ bool prod_lt0(F64i a, F64i b) { return Prec<double>::prod_lt0(a.v, b.v); }
-  __device__ static __forceinline__ F64i sqrt_(F64i x) { return F64i(sqrt(x.v)); }
+  __device__ static __forceinline__ F64i sqrt_(F64i x) { return F64i(fp64::sqrt(x.v)); }
   __device__ static __forceinline__ bool gt0(F64i x) { return Prec<double>::gt0(x.v); }
   __device__ static __forceinline__ bool lt_nonneg(F64i a, F64i b) { return Prec<double>::lt_nonneg(a.v, b.v); }
   template <int K>

@@ -1,6 +1,6 @@
-// selftest.cu -- oeb_selftest_fp64: the integer-pipe FP64 multiply, division, addition and
-// subtraction (precision.cuh: fp64::mul, fp64::div, fp64::add, isub) against the FP64
-// instructions on seeded random operands, on the device.
+// selftest.cu -- oeb_selftest_fp64: the integer-pipe FP64 multiply, division, addition,
+// subtraction and square root (precision.cuh: fp64::mul, div, add, isub, sqrt) against the
+// FP64 instructions on seeded random operands, on the device.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -50,7 +50,11 @@ __global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsi
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
     const uint64_t h = splitmix(seed ^ (uint64_t)t);
     double a, b;
-    if (mode == 5) {  // b times a small integer over b: exact quotients and quotients near 1
+    if (mode == 5 && op == 4) {  // exact squares
+      const double q = (double)(1 + h % 100000000);
+      a = __dmul_rn(q, q);
+      b = 0.0;
+    } else if (mode == 5) {  // b times a small integer over b: exact quotients and quotients near 1
       b = operand(splitmix(h + 17), 1);
       a = __dmul_rn(b, (double)(1 + h % 1000));
     } else if (mode == 6) {  // a + (-a (1 + small)): cancellation of all but a few bits
@@ -69,7 +73,8 @@ __global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsi
       case 0: want = __dmul_rn(a, b); got = fp64::mul(a, b); break;
       case 1: want = __ddiv_rn(a, b); got = fp64::div(a, b); break;
       case 2: want = __dadd_rn(a, b); got = fp64::add(a, b); break;
-      default: want = __dsub_rn(a, b); got = isub(F64i(a), F64i(b)).v; break;
+      case 3: want = __dsub_rn(a, b); got = isub(F64i(a), F64i(b)).v; break;
+      default: want = __dsqrt_rn(a); got = fp64::sqrt(a); break;
     }
     const unsigned long long bw = (unsigned long long)__double_as_longlong(want);
     const unsigned long long bg = (unsigned long long)__double_as_longlong(got);
@@ -90,7 +95,7 @@ __global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsi
 extern "C" oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int mode, uint64_t* mismatches,
                                         uint64_t* first) {
   if (!mismatches) return OEB_ERR_NULL;
-  if (op < 0 || op > 3 || pairs < 0 || mode < 0 || mode > 7) return OEB_ERR_ARGUMENT;
+  if (op < 0 || op > 4 || pairs < 0 || mode < 0 || mode > 7) return OEB_ERR_ARGUMENT;
   unsigned long long* d = nullptr;
   OEB_CUDA_TRY(cudaMalloc(&d, 5 * sizeof(unsigned long long)));
   cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));

@@ -1,12 +1,12 @@
-"""The FP64 multiply, division, addition and subtraction of the FP64 kernels, done on the
-integer pipe, against the FP64 instructions.
+"""The FP64 multiply, division, addition, subtraction and square root of the FP64 kernels,
+done on the integer pipe, against the FP64 instructions.
 
 oeb_selftest_fp64 computes seeded random operand pairs both ways on the GPU and counts
 results that differ in any bit.  Eight distributions: any bit pattern (NaN, infinities,
 zeros and subnormals take the fallback), ordinary magnitudes, exponents near both ends of
 the normal range (results that underflow or overflow), short significands (rounding ties),
 significands near all-ones and near zero (carries out of the significand), exact quotients
-(b times a small integer, over b), cancellation (a and -a (1 + small)) and every alignment
+(b times a small integer, over b) and exact squares, cancellation (a and -a (1 + small)) and every alignment
 shift of an addition (a and a 2^-k with changed low bits).
 """
 from __future__ import annotations
@@ -22,7 +22,7 @@ PAIRS = 1 << 26
 
 @pytest.mark.parametrize("mode", range(8), ids=["any-bits", "ordinary", "range-ends", "ties", "carries", "exact",
                                                  "cancel", "align"])
-@pytest.mark.parametrize("op", [0, 1, 2, 3], ids=["mul", "div", "add", "sub"])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4], ids=["mul", "div", "add", "sub", "sqrt"])
 def test_integer_pipe_operation_is_the_fp64_operation(pkg, cuda, op, mode):
     lib = pkg.load_library()
     bad = ctypes.c_uint64(0)
@@ -39,5 +39,5 @@ def test_selftest_rejects_bad_arguments(pkg, cuda):
     bad = ctypes.c_uint64(0)
     args = (ctypes.c_int64(16), ctypes.c_uint64(1))
     assert lib.oeb_selftest_fp64(ctypes.c_int(0), *args, ctypes.c_int(9), ctypes.byref(bad), None) != 0
-    assert lib.oeb_selftest_fp64(ctypes.c_int(4), *args, ctypes.c_int(0), ctypes.byref(bad), None) != 0
+    assert lib.oeb_selftest_fp64(ctypes.c_int(5), *args, ctypes.c_int(0), ctypes.byref(bad), None) != 0
     assert lib.oeb_selftest_fp64(ctypes.c_int(0), *args, ctypes.c_int(0), None, None) != 0
