@@ -685,7 +685,9 @@ typedef struct oeb_batch_member {
 OEB_API oeb_status oeb_batch_plan_create(const oeb_batch_member* members, int count, int modes, oeb_batch_plan** out);
 OEB_API oeb_status oeb_batch_run(oeb_batch_plan* plan, void* stream);
 OEB_API oeb_status oeb_batch_autotune(oeb_batch_plan* plan, void* stream);
-/* Batched launches per run, and interior points per run (all members). */
+/* Kernel launches per run (one batched launch per recorded position and precision, or one
+ * launch per member where the autotuner chose per-member launches), and interior points
+ * per run (all members). */
 OEB_API int oeb_batch_launches(const oeb_batch_plan* plan);
 OEB_API int64_t oeb_batch_points(const oeb_batch_plan* plan);
 /* Device bytes held by the plan (chain workspaces, scratch arena, tables). */

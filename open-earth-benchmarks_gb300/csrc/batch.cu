@@ -14,8 +14,12 @@
 // CTAs walk the items; FP64 members on the caller's stream, FP32 members on a second stream.
 //
 // The autotuner records the step again with other k-blockings (kb: k-levels per tile of the
-// kernels that take one) and times, for every position and precision, each kb with a single
-// persistent wave (occupancy x SMs CTAs) and with one CTA per tile, keeping the fastest.
+// kernels that take one) and times, for every position and precision, each kb in three forms:
+// the batched launch as a single persistent wave (occupancy x SMs CTAs), the batched launch
+// with one CTA per tile, and plain per-member launches of the recorded grids (the same tiles,
+// one ordinary launch per member: no item search, arguments in the kernel's parameter space).
+// It keeps the fastest, so a tuned plan is never slower, position by position, than launching
+// the members one by one.
 #include <algorithm>
 #include <new>
 #include <vector>
@@ -46,6 +50,7 @@ struct Member {
 // One batched launch of a run.
 struct Slot {
   oeb::BatchLaunchFn fn = nullptr;
+  oeb::GridLaunchFn gfn = nullptr;
   int side = 0;  // 0: FP64 members on the caller's stream, 1: FP32 members on the plan's stream
   int members = 0, total = 0;
   size_t smem = 0;
@@ -53,6 +58,11 @@ struct Slot {
   size_t tiles_off = 0, args_off = 0;  // into the device table buffer
   int ctas = 0;
   int kb = 0;
+  bool per_member = false;  // run as one ordinary launch per member
+  // per member, in slot order: grid, dynamic shared memory and argument pack (host copy)
+  std::vector<dim3> grids;
+  std::vector<size_t> smems, arg_offs;
+  std::vector<unsigned char> host_args;
 };
 
 }  // namespace
@@ -197,6 +207,7 @@ oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vec
         std::stable_sort(who.begin(), who.end(), [&](int a, int b) { return tiles_of(a) > tiles_of(b); });
         Slot sl;
         sl.fn = r0.launcher;
+        sl.gfn = r0.grid_launcher;
         sl.side = side;
         sl.members = (int)who.size();
         sl.smem = 0;
@@ -210,6 +221,12 @@ oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vec
           total += tiles_of(i);
           args.insert(args.end(), r.args.begin(), r.args.end());
           sl.smem = std::max(sl.smem, r.smem);
+          sl.grids.push_back(r.grid);
+          sl.smems.push_back(r.smem);
+          const size_t at = (sl.host_args.size() + 15) & ~size_t(15);  // packs 16-byte aligned
+          sl.host_args.resize(at + r.args.size());
+          memcpy(sl.host_args.data() + at, r.args.data(), r.args.size());
+          sl.arg_offs.push_back(at);
         }
         if (total > INT32_MAX) return OEB_ERR_TOO_LARGE;
         sl.total = (int)total;
@@ -243,15 +260,21 @@ oeb_status upload(oeb_batch_plan* p, const std::vector<char>& host) {
   return OEB_OK;
 }
 
-oeb_status run_slot(oeb_batch_plan* p, const Slot& sl, int ctas, cudaStream_t main) {
+oeb_status run_slot(oeb_batch_plan* p, const Slot& sl, int ctas, bool per_member, cudaStream_t main) {
+  const cudaStream_t s = sl.side ? p->side : main;
+  if (per_member) {
+    for (size_t i = 0; i < sl.grids.size(); ++i)
+      OEB_TRY(sl.gfn(sl.host_args.data() + sl.arg_offs[i], sl.grids[i], sl.smems[i], s));
+    return OEB_OK;
+  }
   return sl.fn(reinterpret_cast<const BatchTile*>(p->tables + sl.tiles_off), sl.members, sl.total,
-               p->tables + sl.args_off, sl.smem, ctas, sl.side ? p->side : main);
+               p->tables + sl.args_off, sl.smem, ctas, s);
 }
 
 oeb_status run(oeb_batch_plan* p, cudaStream_t st) {
   OEB_CUDA_TRY(cudaEventRecord(p->fork, st));
   OEB_CUDA_TRY(cudaStreamWaitEvent(p->side, p->fork, 0));
-  for (const Slot& sl : p->slots) OEB_TRY(run_slot(p, sl, sl.ctas, st));
+  for (const Slot& sl : p->slots) OEB_TRY(run_slot(p, sl, sl.ctas, sl.per_member, st));
   OEB_CUDA_TRY(cudaEventRecord(p->join, p->side));
   OEB_CUDA_TRY(cudaStreamWaitEvent(st, p->join, 0));
   return OEB_OK;
@@ -384,12 +407,16 @@ oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
     for (auto& c : cand) {
       const Slot& sl = c[i];
       const cudaStream_t s = sl.side ? p->side : st;
-      const int options[2] = {std::min(sl.total, sl.occupancy * p->sms), sl.total};
-      for (int ctas : options) {
-        result = run_slot(p, sl, ctas, st);  // warm-up
+      // persistent wave, one CTA per tile (batched launches), then per-member launches
+      const int wave = std::min(sl.total, sl.occupancy * p->sms);
+      const int options[3] = {wave, sl.total, 0};
+      for (int o = 0; o < 3 && result == OEB_OK; ++o) {
+        if (o == 1 && options[1] == options[0]) continue;
+        const bool per_member = o == 2;
+        result = run_slot(p, sl, options[o], per_member, st);  // warm-up
         if (result != OEB_OK) break;
         cudaEventRecord(e0, s);
-        for (int r = 0; r < kReps && result == OEB_OK; ++r) result = run_slot(p, sl, ctas, st);
+        for (int r = 0; r < kReps && result == OEB_OK; ++r) result = run_slot(p, sl, options[o], per_member, st);
         cudaEventRecord(e1, s);
         if (cudaEventSynchronize(e1) != cudaSuccess) result = cuda_fail(cudaGetLastError());
         float ms = 0.f;
@@ -397,9 +424,9 @@ oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
         if (result == OEB_OK && (best_ms < 0.f || ms < best_ms)) {
           best_ms = ms;
           best[i] = sl;
-          best[i].ctas = ctas;
+          best[i].ctas = per_member ? wave : options[o];
+          best[i].per_member = per_member;
         }
-        if (options[0] == options[1]) break;
       }
       if (result != OEB_OK) break;
     }
@@ -431,7 +458,12 @@ extern "C" oeb_status oeb_batch_autotune(oeb_batch_plan* p, void* stream) {
   return autotune(p, (cudaStream_t)stream);
 }
 
-extern "C" int oeb_batch_launches(const oeb_batch_plan* p) { return p ? (int)p->slots.size() : 0; }
+extern "C" int oeb_batch_launches(const oeb_batch_plan* p) {
+  int n = 0;
+  if (p)
+    for (const Slot& sl : p->slots) n += sl.per_member ? (int)sl.grids.size() : 1;
+  return n;
+}
 
 extern "C" int64_t oeb_batch_points(const oeb_batch_plan* p) {
   int64_t n = 0;

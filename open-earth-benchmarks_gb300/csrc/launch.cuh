@@ -98,8 +98,12 @@ using BatchLaunchFn = oeb_status (*)(const BatchTile* tiles, int members, int to
 // CTAs of batch_kernel that fit on one SM with `smem` dynamic shared memory.
 using BatchOccupancyFn = int (*)(size_t smem);
 
+// Launches one recorded call as an ordinary grid from its argument pack (host memory).
+using GridLaunchFn = oeb_status (*)(const void* args, dim3 grid, size_t smem, cudaStream_t st);
+
 struct LaunchRecord {
   BatchLaunchFn launcher;  // also identifies the kernel (Body and argument types)
+  GridLaunchFn grid_launcher;
   BatchOccupancyFn occupancy;
   dim3 grid;
   size_t smem;
@@ -140,6 +144,22 @@ oeb_status batch_launch(const BatchTile* tiles, int members, int total, const vo
   if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)batch_kernel<Body, A...>, (int)smem));
   batch_kernel<Body, A...><<<ctas, dim3(kLaunchTX, kLaunchTY), smem, st>>>(
       tiles, members, total, static_cast<const Pack<A...>*>(args));
+  return after_launch();
+}
+
+template <class Body, class... Done>
+void launch_unpacked(dim3 grid, size_t smem, cudaStream_t st, const Pack<>&, const Done&... d) {
+  grid_kernel<Body, Done...><<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(d...);
+}
+template <class Body, class H, class... R, class... Done>
+void launch_unpacked(dim3 grid, size_t smem, cudaStream_t st, const Pack<H, R...>& p, const Done&... d) {
+  launch_unpacked<Body>(grid, smem, st, p.r, d..., p.h);
+}
+
+template <class Body, class... A>
+oeb_status grid_launch_packed(const void* args, dim3 grid, size_t smem, cudaStream_t st) {
+  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_kernel<Body, A...>, (int)smem));
+  launch_unpacked<Body>(grid, smem, st, *static_cast<const Pack<A...>*>(args));
   return after_launch();
 }
 
@@ -218,6 +238,7 @@ oeb_status launch_as(dim3 grid, size_t smem, cudaStream_t st, A... a) {
   if (Recorder* r = recorder()) {
     LaunchRecord rec;
     rec.launcher = &batch_launch<Body, A...>;
+    rec.grid_launcher = &grid_launch_packed<Body, A...>;
     rec.occupancy = &batch_occupancy<Body, A...>;
     rec.grid = grid;
     rec.smem = smem;
