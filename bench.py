@@ -375,8 +375,11 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": _algorithmic_bytes(pkg, dom_k),
                      "launch_ms": round(per_kernel[dom_k], 5),
                      "fp64_pipe_active_pct": _ncu_summary(dom_k, "fp64_pipe_active_pct"),
-                     "note": "FP64 stencils are bound by the FP64 pipe (1.6 op/clk/SM on GB300), not HBM; "
-                             "fp64_pipe_active_pct is ncu's sm__pipe_fp64_cycles_active for this kernel"},
+                     "alu_pipe_active_pct": _ncu_summary(dom_k, "alu_pipe_active_pct"),
+                     "note": "the FP64 stencils are compute-bound, not HBM-bound: GB300 issues 1.6 FP64 "
+                             "op/clk/SM, so the kernels run as F64i (exact integer-pipe multiply, divide, "
+                             "sqrt, compare beside FP64-pipe adds); the pipe figures are ncu's "
+                             "sm__pipe_fp64_cycles_active and sm__inst_executed_pipe_alu for this kernel"},
         "per_kernel_ms": {k: round(v, 5) for k, v in per_kernel.items()},
         "per_kernel_gbs": {k: round(_algorithmic_bytes(pkg, k) / (v * 1e-3) / 1e9, 1) for k, v in per_kernel.items()},
         "kernel_share": {k: round(v / total_k, 4) for k, v in per_kernel.items()},

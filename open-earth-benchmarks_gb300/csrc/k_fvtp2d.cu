@@ -514,7 +514,7 @@ struct fvtp2d_adj_f2_kernel {
                                              const T* __restrict__ fx1b, const T* __restrict__ fy1b, Dims d, int kb) {
     const int nx = d.nx, ny = d.ny;
     const int64_t sj = d.sj;
-    for_box(blk, d, -3, -3, nx + 5, ny + 5, kb, [&](int64_t o, int i, int j) {
+    for_box<RowUnroll<T>::value>(blk, d, -3, -3, nx + 5, ny + 5, kb, [&](int64_t o, int i, int j) {
       const bool interior = i >= 0 && i < nx && j >= 0 && j < ny;
       if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {
         T g = interior ? (T(0.5) * ld(yfx + o)) * ld(fy1b + o) : T(0);

@@ -348,7 +348,7 @@ struct hdiffsmag_adj_terms_kernel {
     constexpr T rr = earth_radius_recip<T>();
     const T c1 = eddlat * rr;
     const int64_t sj = d.sj;
-    for_box(blk, d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
+    for_box<RowUnroll<T>::value>(blk, d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
       const T c2m = ld(acrlat0 + (int64_t)(j - 1) * s1d) * eddlon, c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon,
               c2p = ld(acrlat0 + (int64_t)(j + 1) * s1d) * eddlon;
       const T t0 = smag_T(uin, vin, o, sj, c1, c2), ti = smag_T(uin, vin, o + 1, sj, c1, c2),
@@ -385,7 +385,7 @@ struct hdiffsmag_adj_ts_kernel {
     const T c1 = eddlat * rr;
     const int64_t sj = d.sj;
     auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
-    for_box(blk, d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int i, int j) {
+    for_box<RowUnroll<T>::value>(blk, d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int i, int j) {
       const T c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon;
       if (i >= 0 && i <= d.nx && j >= 0 && j <= d.ny) {
         T w = T(0);
@@ -419,7 +419,7 @@ struct hdiffsmag_adj_gather_kernel {
     auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
     auto inT = [&](int i, int j) { return i >= 0 && i <= d.nx && j >= 0 && j <= d.ny; };
     auto inS = [&](int i, int j) { return i >= -1 && i < d.nx && j >= -1 && j < d.ny; };
-    for_box(blk, d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int a, int b) {
+    for_box<RowUnroll<T>::value>(blk, d, -1, -1, d.nx + 2, d.ny + 2, kb, [&](int64_t o, int a, int b) {
       const T c2 = ld(acrlat0 + (int64_t)b * s1d) * eddlon;
       T ub = T(0), vb = T(0);
       if (in(a, b)) {

@@ -27,7 +27,7 @@ constexpr int kTI = 32, kTJ = 32, kRows = kTJ / kTY;
 
 // Visits the points of this thread: f(o, j) with o the in-plane offset of (i, j) plus the
 // plane offset of k.
-template <class F>
+template <int U = kRows, class F>
 __device__ __forceinline__ void for_points(const uint3& blk, const Dims& d, int kb, F&& f) {
   const int i = blk.x * kTI + threadIdx.x;
   if (i >= d.nx) return;
@@ -37,7 +37,7 @@ __device__ __forceinline__ void for_points(const uint3& blk, const Dims& d, int 
 #pragma unroll 1
   for (int k = k0; k < k1; ++k) {
     const int64_t kofs = (int64_t)k * d.sk;
-#pragma unroll
+#pragma unroll U
     for (int r = 0; r < kRows; ++r) {
       const int j = blk.y * kTJ + threadIdx.y + kTY * r;
       if (j < d.ny) f(kofs + i + j * sj, j);
@@ -51,7 +51,7 @@ struct laplace_kernel {
   static __device__ __forceinline__ void run(const uint3& blk, const T* __restrict__ in, T* __restrict__ out, Dims d,
                                              int kb) {
     const int64_t sj = d.sj;
-    for_points(blk, d, kb, [&](int64_t o, int) {
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
       if constexpr (Prec<T>::kCompensated) {
         // -4 in nearly cancels the neighbour sum on smooth fields: sum all five terms
         // compensated (-4 in is exact)
@@ -90,7 +90,7 @@ struct uvbke_kernel {
                                              const T* __restrict__ cosa, const T* __restrict__ rsina, T dt5, T dt5_lo,
                                              Dims d, int kb) {
     const int64_t sj = d.sj;
-    for_points(blk, d, kb, [&](int64_t o, int) {
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
       const T su = ld(uc + o - sj) + ld(uc + o);
       const T sv = ld(vc + o - 1) + ld(vc + o);
       const T ca = ld(cosa + o);
@@ -110,7 +110,7 @@ struct p_grad_c_kernel {
                                              const T* __restrict__ delpc, const T* __restrict__ gz,
                                              const T* __restrict__ pkc, T dt2, Dims d, int kb) {
     const int64_t sj = d.sj, sk = d.sk;
-    for_points(blk, d, kb, [&](int64_t o, int) {
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
       const T wk = ld(delpc + o);
       const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
       // the two products nearly cancel (a small pressure-gradient residual): diff_dot is the
@@ -134,7 +134,7 @@ struct nh_p_grad_kernel {
                                              const T* __restrict__ pk3, const T* __restrict__ wk1, T dt, Dims d,
                                              int kb) {
     const int64_t sj = d.sj, sk = d.sk;
-    for_points(blk, d, kb, [&](int64_t o, int) {
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
       const T pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
       const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk);
       const T pp0 = ld(pp + o), pp1 = ld(pp + o + sk);
@@ -233,7 +233,7 @@ struct hadv_kernel {
     const int64_t sj = d.sj;
     constexpr T third = T(1.0) / T(3.0);
     constexpr T rr = earth_radius_recip<T>();
-    for_points(blk, d, kb, [&](int64_t o, int j) {
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
       const int64_t jo = (int64_t)j * s1d;
       const T u0 = ld(uin + o), v0 = ld(vin + o);
       const T um = ld(uin + o - 1) + u0;  // uin(i-1)+uin(i), first pair of both averages
@@ -493,7 +493,7 @@ struct hadv_adj_terms_kernel {
     const int64_t sj = d.sj;
     constexpr T third = T(1.0) / T(3.0);
     constexpr T rr = earth_radius_recip<T>();
-    for_points(blk, d, kb, [&](int64_t o, int j) {
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
       const int64_t jo = (int64_t)j * s1d;
       const T u0 = ld(uin + o), v0 = ld(vin + o);
       const T um = ld(uin + o - 1) + u0;

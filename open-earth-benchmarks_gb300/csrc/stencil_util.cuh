@@ -49,10 +49,23 @@ __host__ __device__ constexpr T earth_radius_recip() {
   return T(1.0) / T(6371.229e3);
 }
 
+// Rows of a thread's 4 (32 x 32 tile, 8 thread rows) that a kernel unrolls.  The FP64
+// kernels' F64i arithmetic is long integer code, and four unrolled copies of a point's work
+// overflow the instruction cache (measured: the advection stencils 16-20 % faster rolled).
+template <class T>
+struct RowUnroll {
+  static constexpr int value = 32 / kTY;
+};
+template <>
+struct RowUnroll<F64i> {
+  static constexpr int value = 1;
+};
+
 // Visits, for this thread, the cells (i, j, k) of the box [ilo, ilo+ni) x [jlo, jlo+nj) x
-// [k0, k0+kb) of its CTA: blk.x/y pick a 32 x 32 tile, each thread takes 4 rows.
-// f(o, i, j) gets the plane-plus-in-plane offset o of (i, j, k) from the interior origin.
-template <class F>
+// [k0, k0+kb) of its CTA: blk.x/y pick a 32 x 32 tile, each thread takes 4 rows (U of them
+// unrolled).  f(o, i, j) gets the plane-plus-in-plane offset o of (i, j, k) from the
+// interior origin.
+template <int U = 32 / kTY, class F>
 __device__ __forceinline__ void for_box(const uint3& blk, const Dims& d, int ilo, int jlo, int ni, int nj, int kb,
                                         F&& f) {
   const int a = (int)(blk.x * 32 + threadIdx.x);
@@ -63,7 +76,7 @@ __device__ __forceinline__ void for_box(const uint3& blk, const Dims& d, int ilo
 #pragma unroll 1
   for (int k = k0; k < k1; ++k) {
     const int64_t kofs = (int64_t)k * d.sk;
-#pragma unroll
+#pragma unroll U
     for (int r = 0; r < 32 / kTY; ++r) {
       const int b = (int)(blk.y * 32 + threadIdx.y) + kTY * r;
       if (b < nj) f(kofs + i + (jlo + b) * sj, i, jlo + b);
