@@ -119,14 +119,22 @@ OEB_API oeb_status oeb_stream_synchronize(void* stream);
  * depend on it.  Batch plans record and tune their own. */
 OEB_API oeb_status oeb_set_kblock(int kb);
 /* k-slabs of the host entry points' copy/compute/copy pipeline (1..8), for every later call;
- * 0 (the default) picks 8 for calls that move 8 MB or more and 1 below.  A tuning knob:
- * results do not depend on it. */
+ * 0 (the default) picks 8 for synchronous calls that move 8 MB or more, and 1 for smaller
+ * and for asynchronous calls.  A tuning knob: results do not depend on it. */
 OEB_API oeb_status oeb_set_host_slabs(int slabs);
 /* 1 (the default): host entry points run the kernels on the host fields in place when the
  * device can address all of them (pageable memory on systems whose GPU uses the host page
  * tables, such as Grace-Blackwell; page-locked memory mapped at the same address elsewhere);
  * 0: always stage through device memory.  Results do not depend on it. */
 OEB_API oeb_status oeb_set_host_direct(int enable);
+/* 0 (the default): host entry points return once their outputs are in host memory.
+ * 1: they return once their work is enqueued; the outputs are in host memory when `stream`
+ * has completed (synchronise it), and the host fields must stay valid and unchanged until
+ * then.  Asynchronous calls always stage through device memory, one slab a call, and
+ * pipeline across calls on one device: a call's copy-in overlaps the previous calls'
+ * compute and copy-out.  Host memory should be page-locked (pageable source memory makes
+ * the driver's copies synchronous).  Results do not depend on it. */
+OEB_API oeb_status oeb_set_host_async(int enable);
 
 /* Self-check of the FP64 operations that the FP64 kernels run on the integer pipe: op 0
  * multiply, 1 divide, 2 add, 3 subtract, 4 square root of a.  `pairs` seeded random
@@ -238,11 +246,12 @@ OEB_API oeb_status oeb_fvtp2d_f64(const oeb_memref3d_f64* q_i, const oeb_memref3
                           const oeb_domain* dom, void* stream);
 
 /* ------------------------------------------------------------------------- */
-/* FP64 forward stencils, HOST pointers, synchronous.  Same arguments as the  */
-/* device entry points; each call stages its fields through device memory    */
-/* (inputs: the whole descriptor span; outputs: exactly the written box) and  */
-/* returns once the outputs are in host memory.  Any host memory works;       */
-/* pinned memory makes the copies DMA transfers.                              */
+/* FP64 forward stencils, HOST pointers, synchronous (see oeb_set_host_async). */
+/* Same arguments as the device entry points; each call runs the kernels on    */
+/* the host fields in place where the device can address them, else stages   */
+/* its fields through device memory (inputs: the whole descriptor span;       */
+/* outputs: exactly the written box), and returns once the outputs are in     */
+/* host memory.  Any host memory works; pinned memory makes the copies DMA.   */
 /* ------------------------------------------------------------------------- */
 
 OEB_API oeb_status oeb_laplace_f64_host(const oeb_memref3d_f64* in, const oeb_memref3d_f64* out,

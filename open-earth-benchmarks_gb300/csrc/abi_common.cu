@@ -141,6 +141,11 @@ oeb_status device_pool(cudaMemPool_t* out) {
     OEB_CUDA_TRY(cudaMemPoolCreate(&p, &props));
     uint64_t threshold = ~0ull;
     OEB_CUDA_TRY(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &threshold));
+    // memory freed on one stream is never reused by an allocation on another through an
+    // inserted dependency (the pool grows instead): asynchronous host calls allocate on the
+    // copy-in stream and free on the caller's, and must not serialise the two
+    int no = 0;
+    OEB_CUDA_TRY(cudaMemPoolSetAttribute(p, cudaMemPoolReuseAllowInternalDependencies, &no));
     pools[dev] = p;
   }
   *out = pools[dev];

@@ -81,14 +81,17 @@ def test_driver_scalars(pkg, fields, orc, cuda, name):
     _run_both(pkg, fields, orc, cuda, name, 48, 48, 6, seed=7, scalars=fields.make_scalars(name, 7, "driver"))
 
 
-@pytest.fixture(params=["direct", "staged"])
+@pytest.fixture(params=["direct", "staged", "async"])
 def host_mode(request, pkg):
     """The host entry points in place on the host fields (where the device can address
-    them) and staged through device memory."""
+    them), staged through device memory, and asynchronous (staged, returning once enqueued:
+    the test synchronises before it reads the outputs)."""
     lib = pkg.load_library()
     assert lib.oeb_set_host_direct(1 if request.param == "direct" else 0) == 0
+    assert lib.oeb_set_host_async(1 if request.param == "async" else 0) == 0
     yield request.param
     lib.oeb_set_host_direct(1)
+    lib.oeb_set_host_async(0)
 
 
 @pytest.mark.parametrize("name", KERNELS)
@@ -110,6 +113,7 @@ def test_host_entry_points(pkg, fields, orc, host_mode, name, size, memory):
     else:
         host = {k: pkg.Storage(v.copy(), H) for k, v in {**inputs, **outs}.items()}
     pkg.call(name, host, sc, domain=(nx, ny, nz))
+    torch.cuda.synchronize()  # an asynchronous call completes with its stream
     for a in spec.by_role("out3"):
         assert_bitwise_equal(host[a.name].numpy(), want[a.name], "%s.%s (host path)" % (name, a.name))
     for a in spec.by_role("in3"):
@@ -181,3 +185,35 @@ def test_host_slabs_do_not_change_results(pkg, fields, orc, slabs):
     finally:
         lib.oeb_set_host_slabs(0)
         lib.oeb_set_host_direct(1)
+
+
+def test_async_host_calls_pipeline(pkg, fields, orc, cuda):
+    """All ten host entry points enqueued asynchronously on one stream, back to back (each
+    call's copy-in overlaps the previous calls' compute and copy-out), one synchronisation at
+    the end: every output as the oracle's, every input unchanged."""
+    import torch
+    lib = pkg.load_library()
+    nx, ny, nz = 70, 53, 9
+    stream = torch.cuda.Stream()
+    cases = {}
+    for name in KERNELS:
+        spec = pkg.KERNELS[name]
+        inputs = fields.make_inputs(name, nx, ny, nz, seed=21)
+        sc = fields.make_scalars(name, seed=21)
+        outs = fields.make_outputs(name, nx, ny, nz)
+        want = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+        orc.run_oracle(spec, want, sc, nx, ny, nz, H)
+        host = {k: pkg.Storage(torch.from_numpy(v.copy()).pin_memory(), H) for k, v in {**inputs, **outs}.items()}
+        cases[name] = (spec, inputs, sc, want, host)
+    assert lib.oeb_set_host_async(1) == 0
+    try:
+        for name, (spec, inputs, sc, want, host) in cases.items():
+            pkg.call(name, host, sc, domain=(nx, ny, nz), stream=stream)
+        stream.synchronize()
+    finally:
+        lib.oeb_set_host_async(0)
+    for name, (spec, inputs, sc, want, host) in cases.items():
+        for a in spec.by_role("out3"):
+            assert_bitwise_equal(host[a.name].numpy(), want[a.name], "%s.%s (asynchronous host path)" % (name, a.name))
+        for a in spec.by_role("in3"):
+            assert_bitwise_equal(host[a.name].numpy(), inputs[a.name], "%s.%s input unchanged" % (name, a.name))
