@@ -62,7 +62,9 @@ __device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T br_m1, T b0_m1, T al
 //   y pass: al 32 x 35 (i0+a, j0-1+b); almq/br/b0/smt 32 x 34 (i0+a, j0-1+b)
 //   x pass: al 35 x 32 (i0-1+a, j0+b); almq/br/b0/smt 34 x 32 (i0-1+a, j0+b)
 //   fyy  : 32 x 33 (i0+a, j0+b) = yfx * fy2, 0 outside fy2's range
-//   fxx  : 33 x 32 (i0+a, j0+b) = xfx * fx2, 0 outside fx2's range
+//   fxx  : 33 x 32 (i0+a, j0+b) = xfx * fx2, 0 outside fx2's range, in fyy's place: q_i, the
+//          only reader of fyy, is computed before the x pass writes fxx (56 KB a tile: four
+//          CTAs per SM)
 template <class T>
 struct FvQSmem {
   T q[39][38];
@@ -78,8 +80,10 @@ struct FvQSmem {
       unsigned char smt[32][34];
     } x;
   } w;
-  T fyy[33][32];
-  T fxx[32][33];
+  union {
+    T fyy[33][32];
+    T fxx[32][33];
+  } f;
 };
 
 template <class T>
@@ -125,9 +129,17 @@ struct fvtp2d_q_kernel {
           if (b < kT) fy2[o] = f;
           fyy = ld(yfx + o) * f;  // fvtp2d.h:43
         }
-        s.fyy[b][a] = fyy;
+        s.f.fyy[b][a] = fyy;
       });
       __syncthreads();
+      // ---- q_i (fvtp2d.h:48), the last reader of fyy, beside the x-PPM edge values
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
+          const int64_t o = kofs + i + j * sj;
+          q_i[o] = (((s.q[b + 3][a + 3] * ld(area + o)) + s.f.fyy[b][a]) - s.f.fyy[b + 1][a]) / ld(ra_y + o);
+        }
+      });
       // ---- x-PPM of q -> fx2, fxx
       for_region<35, 32>([&](int a, int b) {
         s.w.x.al[b][a] = ppm_al(p1, p2, s.q[b + 3][a], s.q[b + 3][a + 1], s.q[b + 3][a + 2], s.q[b + 3][a + 3]);
@@ -148,19 +160,16 @@ struct fvtp2d_q_kernel {
           if (a < kT) fx2[o] = f;
           fxx = ld(xfx + o) * f;  // fvtp2d.h:119
         }
-        s.fxx[b][a] = fxx;
+        s.f.fxx[b][a] = fxx;
       });
       __syncthreads();
-      // ---- q_i (fvtp2d.h:48) and q_j (fvtp2d.h:124)
+      // ---- q_j (fvtp2d.h:124)
       for_region<32, 32>([&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         const int64_t o = kofs + i + j * sj;
         const T qc = s.q[b + 3][a + 3];
-        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
-          q_i[o] = (((qc * ld(area + o)) + s.fyy[b][a]) - s.fyy[b + 1][a]) / ld(ra_y + o);
-        }
         if (i >= 0 && i < nx && j >= -3 && j < ny + 2) {
-          q_j[o] = (((qc * ld(area + o)) + s.fxx[b][a]) - s.fxx[b][a + 1]) / ld(ra_x + o);
+          q_j[o] = (((qc * ld(area + o)) + s.f.fxx[b][a]) - s.f.fxx[b][a + 1]) / ld(ra_x + o);
         }
       });
       __syncthreads();

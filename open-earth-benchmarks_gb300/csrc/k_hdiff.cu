@@ -107,20 +107,19 @@ struct hdiffsa_kernel {
 // ============================== hdiffsmag =========================================
 // Shared layout (per k-level), tile origin (i0, j0):
 //   u, v : 34 x 34, (i0-1+a, j0-1+b)
-//   dxu  : 33 x 33, (i0-1+a, j0+b)     u(i+1,j) - u(i,j)
 //   dyv  : 33 x 33, (i0+a,   j0-1+b)   v(i,j+1) - v(i,j)
 //   dyu  : 33 x 33, (i0-1+a, j0-1+b)   u(i,j+1) - u(i,j)
-//   dxv  : 33 x 33, (i0-1+a, j0-1+b)   v(i+1,j) - v(i,j)
+// (the x differences dxu = u(i+1,j) - u(i,j) at (i0-1+a, j0+b) and dxv = v(i+1,j) - v(i,j)
+// at (i0-1+a, j0-1+b) are each read once, by the deformations of the same cell: they live in
+// registers, which keeps the tile at 53 KB, four CTAs per SM)
 //   tsq  : 33 x 33, (i0+a,   j0+b)     T_s^2
 //   ssq  : 33 x 33, (i0-1+a, j0-1+b)   S_uv^2
 template <class T>
 struct HdiffsmagSmem {
   T u[34][34];
   T v[34][34];
-  T dxu[33][33];
   T dyv[33][33];
   T dyu[33][33];
-  T dxv[33][33];
   T tsq[33][33];
   T ssq[33][33];
   T acrlat0[34];  // j0-1+b
@@ -165,19 +164,18 @@ struct hdiffsmag_kernel {
         s.v[b][a] = ok ? ld(vin + o) : T(0);
       });
       __syncthreads();
-      for_region<33, 33>([&](int a, int b) {
-        s.dxu[b][a] = s.u[b + 1][a + 1] - s.u[b + 1][a];
-        s.dyv[b][a] = s.v[b + 1][a + 1] - s.v[b][a + 1];
-        s.dyu[b][a] = s.u[b + 1][a] - s.u[b][a];
-        s.dxv[b][a] = s.v[b][a + 1] - s.v[b][a];
-      });
-      __syncthreads();
       // hdiffsmag.h:213 T_s = (v(j-1)-v) eddlat R^-1 - (u(i-1)-u) acrlat0(j) eddlon
       //              :221 S_uv = (u(j+1)-u) eddlat R^-1 + (v(i+1)-v) acrlat0(j) eddlon
       for_region<33, 33>([&](int a, int b) {
-        const T ts = ((-s.dyv[b][a]) * eddlat) * rr - ((-s.dxu[b][a]) * s.acrlat0[b + 1]) * eddlon;
+        const T dxu = s.u[b + 1][a + 1] - s.u[b + 1][a];
+        const T dyv = s.v[b + 1][a + 1] - s.v[b][a + 1];
+        const T dyu = s.u[b + 1][a] - s.u[b][a];
+        const T dxv = s.v[b][a + 1] - s.v[b][a];
+        s.dyv[b][a] = dyv;
+        s.dyu[b][a] = dyu;
+        const T ts = ((-dyv) * eddlat) * rr - ((-dxu) * s.acrlat0[b + 1]) * eddlon;
         s.tsq[b][a] = ts * ts;
-        const T su = (s.dyu[b][a] * eddlat) * rr + (s.dxv[b][a] * s.acrlat0[b]) * eddlon;
+        const T su = (dyu * eddlat) * rr + (dxv * s.acrlat0[b]) * eddlon;
         s.ssq[b][a] = su * su;
       });
       __syncthreads();
