@@ -90,6 +90,9 @@ struct Prec<Dual<T>> {
   __device__ static __forceinline__ Dual<T> scale2(Dual<T> x) {
     return Dual<T>(Prec<T>::template scale2<K>(x.v), Prec<T>::template scale2<K>(x.d));
   }
+  __device__ static __forceinline__ Dual<T> scale2v(Dual<T> x, int k) {
+    return Dual<T>(Prec<T>::scale2v(x.v, k), Prec<T>::scale2v(x.d, k));
+  }
   __device__ static __forceinline__ Dual<T> add_flag(Dual<T> q, Dual<T> t, bool flag) {
     return q + t * (flag ? T(1) : T(0));
   }

@@ -75,7 +75,7 @@ struct hdiffsa_kernel {
       // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
       for_region<34, 34>([&](int a, int b) {
         const T c = s.in[b + 1][a + 1];
-        s.lap[b][a] = ((iadd(s.in[b + 1][a], s.in[b + 1][a + 2]) - T(2.0) * c) + s.crlato[b] * s.dy[b + 1][a]) +
+        s.lap[b][a] = ((iadd(s.in[b + 1][a], s.in[b + 1][a + 2]) - scale2<1>(c)) + s.crlato[b] * s.dy[b + 1][a]) +
                       s.crlatu[b] * (-s.dy[b][a]);
       });
       __syncthreads();
@@ -193,7 +193,7 @@ struct hdiffsmag_kernel {
           // u(i+1) + u(i-1) - 2u + crlato (u(j+1) - u) + crlatu (u(j-1) - u)
           Acc<T> lu(s.u[b + 1][a + 2]);
           lu.add(s.u[b + 1][a]);
-          lu.add(-(T(2.0) * uc));
+          lu.add(-scale2<1>(uc));
           lu.add_prod(s.crlato[b], s.dyu[b + 1][a + 1]);
           lu.add_prod(s.crlatu[b], -s.dyu[b][a + 1]);
           uout[o] = uc + smag_u * lu.get();
@@ -205,7 +205,7 @@ struct hdiffsmag_kernel {
           const T vc = s.v[b + 1][a + 1];
           Acc<T> lv(s.v[b + 1][a + 2]);
           lv.add(s.v[b + 1][a]);
-          lv.add(-(T(2.0) * vc));
+          lv.add(-scale2<1>(vc));
           lv.add_prod(s.crlavo[b], s.dyv[b + 1][a]);
           lv.add_prod(s.crlavu[b], -s.dyv[b][a]);
           vout[o] = vc + smag_v * lv.get();

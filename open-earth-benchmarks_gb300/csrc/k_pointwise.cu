@@ -62,7 +62,7 @@ struct laplace_kernel {
         acc.add(T(-4.0) * ld(in + o));
         out[o] = acc.get();
       } else {
-        out[o] = T(-4.0) * ld(in + o) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
+        out[o] = -scale2<2>(ld(in + o)) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
       }
     });
   }
@@ -192,7 +192,7 @@ __device__ __forceinline__ T adv3_axis(const T* __restrict__ f, int64_t o, int64
     acc.add_prod(pos ? c3 : c6, fd);
     return (pos ? a : -a) * acc.get();
   } else {
-    const T p0 = (pos ? c6 : c3) * fa, ph = ch * f0, p3 = (pos ? c3 : c6) * fd;
+    const T p0 = (pos ? c6 : c3) * fa, ph = -scale2<-1>(f0), p3 = (pos ? c3 : c6) * fd;  // ch = -1/2
     return (pos ? a : -a) * (((p0 + (pos ? fb : ph)) + (pos ? ph : fc)) + p3);
   }
 }
@@ -217,7 +217,8 @@ __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64
     acc.add_prod(pos ? c20 : c30, x5);
     return (pos ? a : -a) * acc.get();
   } else {
-    const T p0 = (pos ? c30 : c20) * x0, p1 = (pos ? c4 : c2) * x1, pm = c3 * f0, p4 = (pos ? c2 : c4) * x4,
+    // c4 = -1/4 and c2 = -1/2: the products by them are exact power-of-two scalings
+    const T p0 = (pos ? c30 : c20) * x0, p1 = -scale2v(x1, pos ? -2 : -1), pm = c3 * f0, p4 = -scale2v(x4, pos ? -1 : -2),
             p5 = (pos ? c20 : c30) * x5;
     return (pos ? a : -a) * (((((p0 + p1) + (pos ? fm1 : pm)) + (pos ? pm : fp1)) + p4) + p5);
   }

@@ -343,6 +343,15 @@ struct Prec<double> {
     }
     return __longlong_as_double(r);
   }
+  // x * 2^k for a k chosen at run time (|k| small)
+  __device__ static __forceinline__ double scale2v(double x, int k) {
+    const long long b = fp64::bits(x);
+    const int e = fp64::exponent(b);
+    long long r = b + ((long long)k << 52);
+    if (!(e > 0 && e < 2047 && e + k > 0 && e + k < 2047))
+      r = (long long)fp64::mul_bits((unsigned long long)b, (unsigned long long)(1023 + k) << 52);
+    return __longlong_as_double(r);
+  }
   // q + t * (flag ? 1.0 : 0.0): t * 1 is t; t * 0 is a zero with t's sign (t finite), and
   // q + (+-0) is q except -0 + +0 = +0
   __device__ static __forceinline__ double add_flag(double q, double t, bool flag) {
@@ -376,6 +385,7 @@ struct Prec<float> {
   __device__ static __forceinline__ float scale2(float x) {
     return x * (K >= 0 ? float(1LL << (K >= 0 ? K : 0)) : 1.0f / float(1LL << (K < 0 ? -K : 0)));
   }
+  __device__ static __forceinline__ float scale2v(float x, int k) { return x * __int_as_float((127 + k) << 23); }
   __device__ static __forceinline__ float add_flag(float q, float t, bool flag) { return q + t * (flag ? 1.f : 0.f); }
 };
 
@@ -439,6 +449,7 @@ struct Prec<F64i> {
   __device__ static __forceinline__ F64i scale2(F64i x) {
     return F64i(Prec<double>::template scale2<K>(x.v));
   }
+  __device__ static __forceinline__ F64i scale2v(F64i x, int k) { return F64i(Prec<double>::scale2v(x.v, k)); }
   __device__ static __forceinline__ F64i add_flag(F64i q, F64i t, bool flag) {
     return F64i(Prec<double>::add_flag(q.v, t.v, flag));
   }
@@ -472,6 +483,11 @@ __device__ __forceinline__ bool gt0(T x) {
 template <int K, class T>
 __device__ __forceinline__ T scale2(T x) {
   return Prec<T>::template scale2<K>(x);
+}
+// x * 2^k, k chosen at run time (|k| small)
+template <class T>
+__device__ __forceinline__ T scale2v(T x, int k) {
+  return Prec<T>::scale2v(x, k);
 }
 
 // Left-to-right sum of terms.  Plain for FP64 (the reference's order and rounding); for FP32
