@@ -103,6 +103,9 @@ struct fvtp2d_q_kernel {
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
+      // the inputs of the flux and q_i / q_j phases, read only after the PPM phases
+      const T* const late[7] = {cry, yfx, area, ra_y, crx, xfx, ra_x};
+      prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
       for_region<38, 39>([&](int a, int b) {
         const int i = i0 - 3 + a, j = j0 - 3 + b;
         const bool ok = i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3;
@@ -217,6 +220,9 @@ struct fvtp2d_flux_kernel {
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
+      // the flux phases' own inputs, read only after the PPM phases: on their way to L2 now
+      const T* const late[6] = {crx, fx2, xfx, cry, fy2, yfx};
+      prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
       for_region<37, 32>([&](int a, int b) {
         const int i = i0 - 3 + a, j = j0 + b;
         s.qi[b][a] = (i < nx + 2 && j < ny) ? ld(q_i + kofs + i + j * sj) : T(0);

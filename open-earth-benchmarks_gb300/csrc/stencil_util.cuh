@@ -28,6 +28,26 @@ __device__ __forceinline__ void for_region(F&& f) {
   }
 }
 
+// Brings the 128-byte line holding `p` into L2 (PTX prefetch.global.L2); `p` must lie in a
+// field the kernel reads.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Prefetches into L2, for the 32 x 32 tile at (i0, j0) of plane offset kofs, every line that
+// the tile's interior cells (0 <= i < nx, 0 <= j < ny: inside every field's reach) of each of
+// the N fields cover (two 128-byte lines a row of 32 doubles, one of 32 floats), spread over
+// the CTA's threads.
+template <class T, int N>
+__device__ __forceinline__ void prefetch_tile(const T* const (&fields)[N], int64_t kofs, int i0, int j0, int nx,
+                                              int ny, int sj) {
+  constexpr int kLines = 32 * (int)sizeof(T) / 128;  // lines a row
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  for (int e = tid; e < N * 32 * kLines; e += kThreads) {
+    const int f = e / (32 * kLines), r = (e / kLines) % 32, l = e % kLines;
+    const int i = i0 + l * (128 / (int)sizeof(T)), j = j0 + r;
+    if (i >= 0 && j >= 0 && i < nx && j < ny) prefetch_l2(fields[f] + kofs + i + (int64_t)j * sj);
+  }
+}
+
 // Read-only global load through the non-coherent path.
 template <class T>
 __device__ __forceinline__ T ld(const T* p) {
