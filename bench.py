@@ -361,10 +361,15 @@ def run_ours(args):
 
     del sets
     torch.cuda.empty_cache()
+    # end to end, measured before the other legs fill device memory (the 27 GB batch plan)
+    e2e = None
+    if not args.no_e2e:
+        e2e = _e2e(pkg, fields, torch, args, names)
     f32 = None
     if not args.no_f32:
         sets32 = [_make_set(pkg, fields, torch, dev, SEED + r, names, dtype=np.float32) for r in range(2)]
         ms32, pk32, l32 = _time_steps(pkg, torch, sets32, names, args.steps, args.warmup, stream, dom)
+        ms32c, l32c, _ = _time_concurrent(pkg, torch, sets32, names, args.steps, args.warmup, dom, dev)
         del sets32
         torch.cuda.empty_cache()
         # configuration 3: FP32 at 256 x 256 x 80 with steep fronts (seed 2)
@@ -372,6 +377,7 @@ def run_ours(args):
         sets3 = [_make_set(pkg, fields, torch, dev, 2 + r, names, dtype=np.float32, shape=big, workload="fronts")
                  for r in range(2)]
         ms3, pk3, _ = _time_steps(pkg, torch, sets3, names, args.steps, args.warmup, stream, big)
+        ms3c, _, _ = _time_concurrent(pkg, torch, sets3, names, args.steps, args.warmup, big, dev)
         del sets3
         torch.cuda.empty_cache()
         pts3 = big[0] * big[1] * big[2]
@@ -379,19 +385,27 @@ def run_ours(args):
         d32 = max(pk32, key=pk32.get)
         ach32 = _algorithmic_bytes(pkg, d32, 4) / (pk32[d32] * 1e-3) / 1e9
         step_bytes32 = sum(_algorithmic_bytes(pkg, k, 4) for k in names)
-        f32 = {"value": round(pts_step * args.steps / (ms32 * 1e-3) / 1e9, 4), "unit": "GPts/s",
-               "ms_per_step": round(ms32 / args.steps, 4), "speedup_vs_f64": round(ms_seq / ms32, 3),
-               "step_hbm_gbs": round(step_bytes32 / (ms32 / args.steps * 1e-3) / 1e9, 1),
+        f32 = {"value": round(pts_step * args.steps / (ms32c * 1e-3) / 1e9, 4), "unit": "GPts/s",
+               "ms_per_step": round(ms32c / args.steps, 4), "speedup_vs_f64": round(ms_total / ms32c, 3),
+               "step_hbm_gbs": round(step_bytes32 / (ms32c / args.steps * 1e-3) / 1e9, 1),
+               "issue": "as the FP64 step: the ten stencils on ten streams, one CUDA graph per input set",
+               "sequential": {"value": round(pts_step * args.steps / (ms32 * 1e-3) / 1e9, 4),
+                              "ms_per_step": round(ms32 / args.steps, 4),
+                              "speedup_vs_f64_sequential": round(ms_seq / ms32, 3),
+                              "step_hbm_gbs": round(step_bytes32 / (ms32 / args.steps * 1e-3) / 1e9, 1)},
                "roofline": {"bound": "hbm", "kernel": d32, "achieved": round(ach32, 2), "peak": _measured_peak()[0],
                             "unit": "GB/s", "frac": round(ach32 / _measured_peak()[0], 4)},
                "per_kernel_ms": {k: round(v, 5) for k, v in pk32.items()},
                "per_kernel_gbs": {k: round(_algorithmic_bytes(pkg, k, 4) / (v * 1e-3) / 1e9, 1)
                                   for k, v in pk32.items()},
-               "gpu_launches": int(l32),
+               "gpu_launches": int(l32c),
                "config3_256x256x80_fronts": {
-                   "value": round(len(names) * pts3 * args.steps / (ms3 * 1e-3) / 1e9, 4), "unit": "GPts/s",
-                   "ms_per_step": round(ms3 / args.steps, 4),
-                   "step_hbm_gbs": round(sum(by3.values()) / (ms3 / args.steps * 1e-3) / 1e9, 1),
+                   "value": round(len(names) * pts3 * args.steps / (ms3c * 1e-3) / 1e9, 4), "unit": "GPts/s",
+                   "ms_per_step": round(ms3c / args.steps, 4),
+                   "step_hbm_gbs": round(sum(by3.values()) / (ms3c / args.steps * 1e-3) / 1e9, 1),
+                   "sequential": {"value": round(len(names) * pts3 * args.steps / (ms3 * 1e-3) / 1e9, 4),
+                                  "ms_per_step": round(ms3 / args.steps, 4),
+                                  "step_hbm_gbs": round(sum(by3.values()) / (ms3 / args.steps * 1e-3) / 1e9, 1)},
                    "per_kernel_ms": {k: round(v, 5) for k, v in pk3.items()},
                    "per_kernel_gbs": {k: round(by3[k] / (v * 1e-3) / 1e9, 1) for k, v in pk3.items()},
                    "per_kernel_frac": {k: round(by3[k] / (v * 1e-3) / 1e9 / _measured_peak()[0], 4)
@@ -415,9 +429,6 @@ def run_ours(args):
     if not args.no_batch:
         batched = _batch_leg(pkg, fields, torch, dev, args)
 
-    e2e = None
-    if not args.no_e2e:
-        e2e = _e2e(pkg, fields, torch, args, names)
 
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "GPts/s", "n_gpus": world, "steps": args.steps,
