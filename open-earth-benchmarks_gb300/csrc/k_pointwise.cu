@@ -134,7 +134,7 @@ struct nh_p_grad_kernel {
                                              const T* __restrict__ pk3, const T* __restrict__ wk1, T dt, Dims d,
                                              int kb) {
     const int64_t sj = d.sj, sk = d.sk;
-    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
+    for_points<HeavyRowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
       const T pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
       const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk);
       const T pp0 = ld(pp + o), pp1 = ld(pp + o + sk);
@@ -234,7 +234,7 @@ struct hadv_kernel {
     const int64_t sj = d.sj;
     constexpr T third = T(1.0) / T(3.0);
     constexpr T rr = earth_radius_recip<T>();
-    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
+    for_points<HeavyRowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
       const int64_t jo = (int64_t)j * s1d;
       const T u0 = ld(uin + o), v0 = ld(vin + o);
       const T um = ld(uin + o - 1) + u0;  // uin(i-1)+uin(i), first pair of both averages

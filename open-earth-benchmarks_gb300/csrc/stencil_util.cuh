@@ -80,6 +80,17 @@ template <>
 struct RowUnroll<F64i> {
   static constexpr int value = 1;
 };
+// The same for the stencils whose per-point work is longest (advection, pressure gradient):
+// FP32 unrolls two rows (measured at 256 x 256 x 80: hadvuv 89 -> 62 us, hadvuv5th 107 ->
+// 77 us, nh_p_grad 101 -> 94 us against four), FP64 one.
+template <class T>
+struct HeavyRowUnroll {
+  static constexpr int value = 2;
+};
+template <>
+struct HeavyRowUnroll<F64i> {
+  static constexpr int value = 1;
+};
 
 // Visits, for this thread, the cells (i, j, k) of the box [ilo, ilo+ni) x [jlo, jlo+nj) x
 // [k0, k0+kb) of its CTA: blk.x/y pick a 32 x 32 tile, each thread takes 4 rows (U of them
