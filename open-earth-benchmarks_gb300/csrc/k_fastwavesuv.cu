@@ -69,6 +69,8 @@ struct fastwavesuv_kernel {
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * sk;
+      const T* const late[6] = {ppuv, rho, uin, utens, vin, vtens};  // read in the last phase
+      prefetch_tile(late, kofs, i0, j0, d.nx, d.ny, sj);
   #pragma unroll
       for (int t = 0; t < kOwned; ++t) {
         const int e = tid + t * kThreads;
