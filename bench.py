@@ -721,7 +721,15 @@ def _e2e(pkg, fields, torch, args, names):
         spec = pkg.KERNELS[name]
         st, _ = hs[name]
         for a in spec.args:
-            if a.role in ("in3", "in1"):
+            if a.role == "in3":
+                # the k-planes the kernel reads (-klo .. nz+khi-1, every row of them), rounded out
+                # to 64 KB of the field's span as the host entry points copy them
+                data = st[a.name].data
+                plane, align = data.shape[1] * data.shape[2], 65536 // 8
+                lo = (HALO - a.reach[4]) * plane // align * align
+                hi = min(data.numel(), -(-(HALO + NZ + a.reach[5]) * plane // align) * align)
+                h2d += (hi - lo) * 8
+            elif a.role == "in1":
                 h2d += st[a.name].data.numel() * 8
             elif a.role == "out3":
                 ilo, ihi, jlo, jhi, klo, khi = a.reach
@@ -767,7 +775,8 @@ def _e2e(pkg, fields, torch, args, names):
                                    "path": "the same calls, each returning when its outputs are in host memory, "
                                            "copy-in / compute / copy-out pipelined over k-slabs within the call"},
             "link_ceiling": "pinned host-to-device copies reach 211 GB/s (189 GB/s beside a device-to-host copy) "
-                            "on this GB300: the step's 556 MB of input span alone take 2.6 ms"}
+                            "on this GB300: the step's %d MB of input planes alone take %.1f ms"
+                            % (h2d // 1000000, h2d / 211e9 * 1e3)}
 
 
 def _cpu_baseline(pkg, fields, budget_s=15.0, threads=None):

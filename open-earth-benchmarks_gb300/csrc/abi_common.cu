@@ -19,10 +19,29 @@ namespace oeb {
 namespace {
 thread_local char g_last_cuda_error[256] = "";
 thread_local int g_validate_only = 0;
+thread_local ReachLog* t_reach_log = nullptr;
 std::atomic<uint64_t> g_launches{0};
 }  // namespace
 
 bool validating() { return g_validate_only > 0; }
+void set_reach_log(ReachLog* log) { t_reach_log = log; }
+
+bool ReachLog::find(const void* m, Reach* out) const {
+  bool found = false;
+  for (int q = 0; q < n; ++q) {
+    if (desc[q] != m) continue;
+    const Reach& r = reach[q];
+    if (!found) {
+      *out = r;
+    } else {
+      out->ilo = std::max(out->ilo, r.ilo), out->ihi = std::max(out->ihi, r.ihi);
+      out->jlo = std::max(out->jlo, r.jlo), out->jhi = std::max(out->jhi, r.jhi);
+      out->klo = std::max(out->klo, r.klo), out->khi = std::max(out->khi, r.khi);
+    }
+    found = true;
+  }
+  return found;
+}
 ValidateOnly::ValidateOnly() { ++g_validate_only; }
 ValidateOnly::~ValidateOnly() { --g_validate_only; }
 
@@ -185,6 +204,12 @@ oeb_status check_field3(const M* m, const oeb_domain& d, const Reach& r, Grid<T>
   // box [-lo, n-1+hi] on each axis must fit in [-h, size-h-1]
   if (r.ilo > hi || r.jlo > hj || r.klo > hk) return OEB_ERR_HALO;
   if (d.nx + r.ihi > szi - hi || d.ny + r.jhi > szj - hj || d.nz + r.khi > szk - hk) return OEB_ERR_HALO;
+  if (ReachLog* log = t_reach_log) {
+    if (log->n < ReachLog::kMax) {
+      log->desc[log->n] = m;
+      log->reach[log->n++] = r;
+    }
+  }
   g->origin = m->aligned + m->offset;
   g->sj = sj;
   g->sk = sk;

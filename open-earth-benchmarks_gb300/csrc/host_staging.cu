@@ -223,11 +223,16 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
   for (const M3* m : in3) h3[n3] = m, d3[n3++] = *m;
   for (const M1* m : in1) d1[n1++] = *m;
   for (const OutSpec<M3>& o : out3) o3[no++] = *o.host;
+  ReachLog reach;
   {
     // Validate the host descriptors with the device entry point's own checks, before any
-    // allocation or copy (the descriptors are identical up to the base pointers).
+    // allocation or copy (the descriptors are identical up to the base pointers); the checks
+    // record each input's reach
     ValidateOnly guard;
-    OEB_TRY(launch(d3, d1, o3, dom, stream));
+    set_reach_log(&reach);
+    const oeb_status vst = launch(d3, d1, o3, dom, stream);
+    set_reach_log(nullptr);
+    OEB_TRY(vst);
   }
   // Direct: the kernels read and write the host fields in place over the host link -- no
   // staging copies, and the transfers overlap the arithmetic by construction.  Asynchronous
@@ -279,16 +284,31 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
       if (st != OEB_OK) break;
       st = stage.alloc(o.host, span_elems3(o.host), &o3[n++]);
     }
-    int64_t copied[kMaxFields] = {0};
+    // each input's copy range (elements from its span start): the k-planes its kernel reads,
+    // -klo .. nz+khi-1 of its validated reach (every row of them), else the whole span
+    int64_t copied[kMaxFields] = {0}, need_end[kMaxFields];
+    for (int q = 0; q < n3; ++q) {
+      const M3* h = h3[q];
+      need_end[q] = span[q];
+      Reach r;
+      if (reach.find(&d3[q], &r)) {
+        // rounded out to 64 KB of the span (the copy engines move whole pages faster)
+        constexpr int64_t kAlign = 65536 / (int64_t)sizeof(T);
+        const int64_t sk = h->strides[0], hk = h->offset / sk;
+        const int64_t base = (int64_t)(h->aligned - span_start(h->allocated, h->aligned));
+        copied[q] = std::max<int64_t>(0, (base + (hk - r.klo) * sk) / kAlign * kAlign);
+        need_end[q] = std::min<int64_t>(span[q], (base + (hk + dom->nz + r.khi) * sk + kAlign - 1) / kAlign * kAlign);
+      }
+    }
     for (int s = 0; s < slabs && st == OEB_OK; ++s) {
       const int64_t k0 = dom->nz * s / slabs, k1 = dom->nz * (s + 1) / slabs;
       // copy-in: every input's prefix up to level k1 (the slab's top + 1), whole on the last slab
       for (int q = 0; q < n3 && st == OEB_OK; ++q) {
         const M3* h = h3[q];
         const T* hstart = span_start(h->allocated, h->aligned);
-        const int64_t end = s == slabs - 1 ? span[q]
-                                           : std::min(span[q], (int64_t)(h->aligned - hstart) + h->offset +
-                                                                   (k1 + 1) * h->strides[0]);
+        const int64_t end = s == slabs - 1 ? need_end[q]
+                                           : std::min(need_end[q], (int64_t)(h->aligned - hstart) + h->offset +
+                                                                       (k1 + 1) * h->strides[0]);
         if (end > copied[q]) {
           if (cudaMemcpyAsync(d3[q].allocated + copied[q], hstart + copied[q], (size_t)(end - copied[q]) * sizeof(T),
                               cudaMemcpyHostToDevice, ss->in) != cudaSuccess)

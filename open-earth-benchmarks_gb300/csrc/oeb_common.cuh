@@ -95,6 +95,19 @@ oeb_status check_domain(const oeb_domain* dom);
 
 template <class T, class M>
 oeb_status check_field3(const M* m, const oeb_domain& d, const Reach& r, Grid<T>* g);
+
+// While a ReachLog is installed on the calling thread, check_field3 records the reach each
+// 3-D descriptor is validated against (the host entry points learn from it which k-planes of
+// an input the kernel reads, and copy only those).
+struct ReachLog {
+  static constexpr int kMax = 32;
+  const void* desc[kMax];
+  Reach reach[kMax];
+  int n = 0;
+  // the reach recorded for `m` (the union if it was validated more than once), or false
+  bool find(const void* m, Reach* out) const;
+};
+void set_reach_log(ReachLog* log);
 template <class T, class M>
 oeb_status check_field1(const M* m, const oeb_domain& d, int jlo, int jhi, Line<T>* l);
 
