@@ -766,8 +766,9 @@ def _e2e(pkg, fields, torch, args, names):
     return {"value": round(pts / dt / 1e9, 4), "unit": "GPts/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(dt * 1e3, 3),
             "path": "oeb_<k>_f64_host on pinned host buffers with oeb_set_host_async(1): the ten calls are enqueued on "
-                    "one stream and the step ends with its synchronisation; each call stages its fields through "
-                    "device memory, and the copy-in of one call overlaps the compute and copy-out of the previous",
+                    "one stream and the step ends with its synchronisation; "
+                    "each call stages the k-planes its kernel reads through device memory, and the copy-in of one "
+                    "call overlaps the compute and copy-out of the previous",
             "synchronous_direct": {"value": round(pts / dt_direct / 1e9, 4), "ms_per_step": round(dt_direct * 1e3, 3),
                                    "path": "the same calls, each returning when its outputs are in host memory; the "
                                            "kernels read and write the host fields in place over NVLink-C2C"},
