@@ -384,14 +384,20 @@ oeb_status fvtp2d_tl_entry(const M3* dq_i, const M3* dq_j, const M3* dfx1, const
 
 constexpr int kW = 44;  // window along the sweep axis: outputs A..A+31 need A-5 .. A+38
 
+// gs and als are dead once the flags smt are set; tb and al take their places (46 KB a CTA
+// in FP64: four CTAs per SM)
 template <class T>
 struct PpmAdjSmem {
-  T gs[32][kW];   // state values of the swept field
-  T als[32][kW];  // state edge values al
-  T tb[32][kW];
+  union {
+    T gs[32][kW];  // state values of the swept field
+    T al[32][kW];
+  } u0;
+  union {
+    T als[32][kW];  // state edge values al
+    T tb[32][kW];
+  } u1;
   T alm[32][kW];
   T br[32][kW];
-  T al[32][kW];
   unsigned char smt[32][kW];
 };
 
@@ -417,14 +423,14 @@ __device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L
       f(w, l);
     }
   };
-  region(0, kW, [&](int w, int l) { s.gs[l][w] = gst(A - 5 + w, L0 + l); });
+  region(0, kW, [&](int w, int l) { s.u0.gs[l][w] = gst(A - 5 + w, L0 + l); });
   __syncthreads();
   region(2, kW - 1, [&](int w, int l) {
-    s.als[l][w] = (p1 * (s.gs[l][w - 1] + s.gs[l][w])) + (p2 * (s.gs[l][w - 2] + s.gs[l][w + 1]));
+    s.u1.als[l][w] = (p1 * (s.u0.gs[l][w - 1] + s.u0.gs[l][w])) + (p2 * (s.u0.gs[l][w - 2] + s.u0.gs[l][w + 1]));
   });
   __syncthreads();
   region(2, kW - 2, [&](int w, int l) {
-    s.smt[l][w] = Prec<T>::prod_lt0(s.als[l][w] - s.gs[l][w], s.als[l][w + 1] - s.gs[l][w]);
+    s.smt[l][w] = Prec<T>::prod_lt0(s.u1.als[l][w] - s.u0.gs[l][w], s.u1.als[l][w + 1] - s.u0.gs[l][w]);
   });
   __syncthreads();
   region(3, kW - 2, [&](int w, int l) {
@@ -435,12 +441,12 @@ __device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L
       const T c = cv(p, L0 + l);
       t = f * ((c > T(0)) ? (T(1) - c) : (T(1) + c));
     }
-    s.tb[l][w] = t;
+    s.u1.tb[l][w] = t;
   });
   __syncthreads();
   region(3, kW - 3, [&](int w, int l) {
     const int p = A - 5 + w;
-    const T t0 = s.tb[l][w], t1 = s.tb[l][w + 1];
+    const T t0 = s.u1.tb[l][w], t1 = s.u1.tb[l][w + 1];
     T b0 = T(0), am = T(0), bb = T(0);
     if (t1 != T(0)) {
       const T c1 = cv(p + 1, L0 + l);
@@ -460,11 +466,11 @@ __device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L
     s.br[l][w] = bb + b0;
   });
   __syncthreads();
-  region(4, kW - 3, [&](int w, int l) { s.al[l][w] = s.alm[l][w] + s.br[l][w - 1]; });
+  region(4, kW - 3, [&](int w, int l) { s.u0.al[l][w] = s.alm[l][w] + s.br[l][w - 1]; });
   __syncthreads();
   region(5, 5 + 32, [&](int w, int l) {
     const int a = A - 5 + w;
-    T g = fma(p1, s.al[l][w + 1] + s.al[l][w], fma(p2, s.al[l][w + 2] + s.al[l][w - 1], -s.alm[l][w])) - s.br[l][w];
+    T g = fma(p1, s.u0.al[l][w + 1] + s.u0.al[l][w], fma(p2, s.u0.al[l][w + 2] + s.u0.al[l][w - 1], -s.alm[l][w])) - s.br[l][w];
     const T f1 = fb(a + 1, L0 + l);
     if (f1 != T(0) && cv(a + 1, L0 + l) > T(0)) g = g + f1;
     const T f0 = fb(a, L0 + l);
