@@ -118,7 +118,11 @@ struct fastwavesuv_kernel {
 };
 
 constexpr int kKB = 1;     // k-levels per CTA by default (the most CTAs hide latency best)
-constexpr int kAdjKB = 4;  // the adjoint's k-levels per CTA
+// the adjoint's k-levels per CTA (measured at 128 x 128 x 80: FP64 best at 4, FP32 at 2)
+template <class T>
+constexpr int adj_kb() {
+  return sizeof(T) == 4 ? 2 : 4;
+}
 
 template <class T, class M3, class M1>
 oeb_status fastwavesuv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* utens,
@@ -341,7 +345,7 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   const T ed2 = T(2.0) * edadlat;
   // the adjoint carries a three-level window of ppgc/hhl terms up the column: longer
   // k-blocks reuse it (4 levels: 0.68 ms against 0.89 ms for 1 at 128 x 128 x 80, FP64)
-  const int kb = tuned_kb(kAdjKB);
+  const int kb = tuned_kb(adj_kb<T>());
   return launch<fastwavesuv_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
                                            sizeof(FastwavesAdjSmem<T>), (cudaStream_t)stream, gub.origin, gvb.origin,
                                            gutb.origin, gvtb.origin, gpb.origin, gw.origin, gh.origin, gr.origin,
