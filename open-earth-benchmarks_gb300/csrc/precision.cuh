@@ -72,8 +72,8 @@ static __device__ __noinline__ unsigned long long add_mul0_bits(unsigned long lo
 // bit and the OR of the rest the sticky bit, and IEEE 754 round-to-nearest-even adds one
 // ulp when round and (sticky or the last kept bit) are set.  A carry out of the significand
 // moves into the exponent field by itself, which is the correct rounding up to the next
-// power of two.  The 106-bit product comes from four 32 x 32 -> 64-bit multiplies of the
-// significands split into a high part of 21 bits and a low part of 32.  Any other input --
+// power of two.  The 106-bit product comes from four independent 32 x 32 -> 64-bit multiplies
+// of the significands split into a high part of 21 bits and a low part of 32.  Any other input --
 // a zero, subnormal, infinite or NaN operand, or an exponent sum outside [1, 2045] where the
 // result could be subnormal or overflow -- takes the FP64 multiply.
 __device__ __forceinline__ double mul(double a, double b) {
@@ -82,12 +82,16 @@ __device__ __forceinline__ double mul(double a, double b) {
   const unsigned la = (unsigned)ua, lb = (unsigned)ub;
   const unsigned ea = (ha >> 20) & 0x7FFu, eb = (hb >> 20) & 0x7FFu;
   const unsigned a1 = (ha & 0xFFFFFu) | 0x100000u, b1 = (hb & 0xFFFFFu) | 0x100000u;
-  // (a1 2^32 + la)(b1 2^32 + lb) = w3:w2:w1:w0 (32-bit words), in [2^104, 2^106)
+  // (a1 2^32 + la)(b1 2^32 + lb) = w3:w2:w1:w0 (32-bit words), in [2^104, 2^106); the four
+  // partial products are independent (a short dependency chain), the middle ones summed
+  // with the carry of the lowest (below 2^55: no overflow)
   const unsigned long long p00 = (unsigned long long)la * lb;
-  const unsigned long long p01 = (unsigned long long)la * b1 + (p00 >> 32);
-  const unsigned long long p10 = (unsigned long long)a1 * lb + (unsigned)p01;
-  const unsigned long long p11 = (unsigned long long)a1 * b1 + (p01 >> 32) + (p10 >> 32);
-  const unsigned w0 = (unsigned)p00, w1 = (unsigned)p10, w2 = (unsigned)p11, w3 = (unsigned)(p11 >> 32);
+  const unsigned long long p01 = (unsigned long long)la * b1;
+  const unsigned long long p10 = (unsigned long long)a1 * lb;
+  const unsigned long long p11 = (unsigned long long)a1 * b1;
+  const unsigned long long mid = p01 + p10 + (p00 >> 32);
+  const unsigned long long top64 = p11 + (mid >> 32);
+  const unsigned w0 = (unsigned)p00, w1 = (unsigned)mid, w2 = (unsigned)top64, w3 = (unsigned)(top64 >> 32);
   const unsigned top = w3 >> 9;  // 1 if the product has 106 bits
   const unsigned sh = 20u + top;  // significand = (w3:w2:w1) >> sh, hidden bit at bit 52
   const unsigned mlo = __funnelshift_r(w1, w2, sh);
