@@ -100,29 +100,40 @@ struct fvtp2d_q_kernel {
     const int sj = (int)d.sj;
     const int nx = d.nx, ny = d.ny;
     const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    // the cells each phase needs for this tile's outputs (fewer at the output box's far
+    // edge: the box is nx+5 wide, so the last tile column holds a few useful columns only)
+    auto lim = [](int v, int hi) { return max(0, min(v, hi)); };
+    const int ax = lim(nx + 2 - i0, 32);        // columns of fy2 and q_i
+    const int yfb = lim(ny + 1 - j0, 33);       // rows of fy2 / fyy
+    const int qib = lim(ny - j0, 32);           // rows of q_i
+    const int xfa = lim(nx + 1 - i0, 33);       // columns of fx2 / fxx
+    const int by = lim(ny + 2 - j0, 32);        // rows of fx2 and q_j
+    const int qja = lim(nx - i0, 32);           // columns of q_j
+    const int qcols = min(38, max(ax + 3, xfa + 5));          // q read by the phases above
+    const int qrows = min(39, max(yfb + 5, max(by, qib) + 3));
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
       // the inputs of the flux and q_i / q_j phases, read only after the PPM phases
       const T* const late[7] = {cry, yfx, area, ra_y, crx, xfx, ra_x};
       prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
-      for_region<38, 39>([&](int a, int b) {
+      for_region_lim<38, 39>(qcols, qrows, [&](int a, int b) {
         const int i = i0 - 3 + a, j = j0 - 3 + b;
         const bool ok = i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3;
         s.q[b][a] = ok ? ld(q + kofs + i + j * sj) : T(0);
       });
       __syncthreads();
       // ---- y-PPM of q -> fy2, fyy
-      for_region<32, 35>([&](int a, int b) {
+      for_region_lim<32, 35>(ax, yfb + 2, [&](int a, int b) {
         s.w.y.al[b][a] = ppm_al(p1, p2, s.q[b][a + 3], s.q[b + 1][a + 3], s.q[b + 2][a + 3], s.q[b + 3][a + 3]);
       });
       __syncthreads();
-      for_region<32, 34>([&](int a, int b) {
+      for_region_lim<32, 34>(ax, yfb + 1, [&](int a, int b) {
         ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.q[b + 2][a + 3], &s.w.y.almq[b][a], &s.w.y.br[b][a],
                 &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
       });
       __syncthreads();
-      for_region<32, 33>([&](int a, int b) {
+      for_region_lim<32, 33>(ax, yfb, [&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         T fyy = T(0);
         if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {  // fvtp2d.h:26-27
@@ -136,7 +147,7 @@ struct fvtp2d_q_kernel {
       });
       __syncthreads();
       // ---- q_i (fvtp2d.h:48), the last reader of fyy, beside the x-PPM edge values
-      for_region<32, 32>([&](int a, int b) {
+      for_region_lim<32, 32>(ax, qib, [&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
           const int64_t o = kofs + i + j * sj;
@@ -144,16 +155,16 @@ struct fvtp2d_q_kernel {
         }
       });
       // ---- x-PPM of q -> fx2, fxx
-      for_region<35, 32>([&](int a, int b) {
+      for_region_lim<35, 32>(xfa + 2, by, [&](int a, int b) {
         s.w.x.al[b][a] = ppm_al(p1, p2, s.q[b + 3][a], s.q[b + 3][a + 1], s.q[b + 3][a + 2], s.q[b + 3][a + 3]);
       });
       __syncthreads();
-      for_region<34, 32>([&](int a, int b) {
+      for_region_lim<34, 32>(xfa + 1, by, [&](int a, int b) {
         ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.q[b + 3][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
                 &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
       });
       __syncthreads();
-      for_region<33, 32>([&](int a, int b) {
+      for_region_lim<33, 32>(xfa, by, [&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         T fxx = T(0);
         if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {  // fvtp2d.h:102-103
@@ -167,7 +178,7 @@ struct fvtp2d_q_kernel {
       });
       __syncthreads();
       // ---- q_j (fvtp2d.h:124)
-      for_region<32, 32>([&](int a, int b) {
+      for_region_lim<32, 32>(qja, by, [&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         const int64_t o = kofs + i + j * sj;
         const T qc = s.q[b + 3][a + 3];

@@ -28,6 +28,25 @@ __device__ __forceinline__ void for_region(F&& f) {
   }
 }
 
+// for_region over the first w x h cells of the W x H region only (a < w, b < h): a tile at
+// the edge of its output box skips the cells no output needs.  Full tiles take the
+// compile-time loop.
+template <int W, int H, class F>
+__device__ __forceinline__ void for_region_lim(int w, int h, F&& f) {
+  if (w >= W && h >= H) {
+    for_region<W, H>(f);
+    return;
+  }
+  if (w <= 0 || h <= 0) return;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+#pragma unroll 1
+  for (int e = tid; e < w * h; e += kThreads) {
+    const int b = e / w;
+    const int a = e - b * w;
+    f(a, b);
+  }
+}
+
 // Brings the 128-byte line holding `p` into L2 (PTX prefetch.global.L2); `p` must lie in a
 // field the kernel reads.
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
