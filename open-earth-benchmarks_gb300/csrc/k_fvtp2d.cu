@@ -412,24 +412,44 @@ struct PpmAdjSmem {
   unsigned char smt[32][kW];
 };
 
-// One transposed PPM sweep along AXIS (0: i, 1: j) for outputs A..A+31 on lines L0..L0+31.
+// One transposed PPM sweep along AXIS (0: i, 1: j) for outputs A..A+nout-1 on lines
+// L0..L0+nl-1 (nout, nl <= 32: a tile at the edge of its output box works on its own part of
+// the window and lines only; every phase's window shrinks by the 32 - nout missing outputs).
 // gst(p, l): state value at axis position p of line l (0 where the field is not defined);
 // cv(p, l): Courant number at flux point p (any value elsewhere);
 // fb(p, l): flux adjoint at p (0 off the flux points);  put(a, l, v): receives gbar(a).
 template <class T, int AXIS, class GS, class CV, class FB, class PUT>
-__device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L0, T p1, T p2, GS&& gst, CV&& cv,
-                                                  FB&& fb, PUT&& put) {
+__device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L0, int nout, int nl, T p1, T p2,
+                                                  GS&& gst, CV&& cv, FB&& fb, PUT&& put) {
+  const int cut = 32 - nout;
+  const bool full = cut == 0 && nl == 32;
   auto region = [&](int w0, int w1, auto&& f) {
     const int tid = threadIdx.y * kTX + threadIdx.x;
-    const int W = w1 - w0;
-    for (int e = tid; e < W * 32; e += kThreads) {
+    if (full) {  // compile-time extents
+      const int W = w1 - w0;
+      for (int e = tid; e < W * 32; e += kThreads) {
+        int w, l;
+        if (AXIS == 0) {
+          l = e / W;
+          w = w0 + (e - l * W);
+        } else {
+          w = w0 + e / 32;
+          l = e - (e / 32) * 32;
+        }
+        f(w, l);
+      }
+      return;
+    }
+    const int W = w1 - cut - w0;
+    if (W <= 0 || nl <= 0) return;
+    for (int e = tid; e < W * nl; e += kThreads) {
       int w, l;
       if (AXIS == 0) {
         l = e / W;
         w = w0 + (e - l * W);
       } else {
-        w = w0 + e / 32;
-        l = e - (e / 32) * 32;
+        w = w0 + e / nl;
+        l = e - (e / nl) * nl;
       }
       f(w, l);
     }
@@ -508,7 +528,7 @@ struct fvtp2d_adj_qij_kernel {
       // x sweep of fx1 on q_i: outputs i in [-3, nx+2), lines j in [0, ny)
       const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * 32;
       ppm_sweep_adjoint<T, 0>(
-          s, A, L0, p1, p2,
+          s, A, L0, max(0, min(32, nx + 2 - A)), max(0, min(32, ny - L0)), p1, p2,
           [&](int p, int l) { return (p >= -3 && p < nx + 2 && l < ny) ? ld(q_i + kofs + p + l * sj) : T(0); },
           [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
           [&](int p, int l) {
@@ -522,7 +542,7 @@ struct fvtp2d_adj_qij_kernel {
       // y sweep of fy1 on q_j: outputs j in [-3, ny+2), lines i in [0, nx)
       const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * 32;
       ppm_sweep_adjoint<T, 1>(
-          s, A, L0, p1, p2,
+          s, A, L0, max(0, min(32, ny + 2 - A)), max(0, min(32, nx - L0)), p1, p2,
           [&](int p, int l) { return (p >= -3 && p < ny + 2 && l < nx) ? ld(q_j + kofs + l + p * sj) : T(0); },
           [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
           [&](int p, int l) {
@@ -585,7 +605,8 @@ struct fvtp2d_adj_q_kernel {
     if (!AXIS_Y) {
       // x sweep of fx2 on q: flux points i in [0, nx+1), lines j in [-3, ny+2)
       ppm_sweep_adjoint<T, 0>(
-          s, A, L0, p1, p2, [&](int p, int l) { return qval(p, l); },
+          s, A, L0, max(0, min(32, nx + 3 - A)), max(0, min(32, ny + 3 - L0)), p1, p2,
+          [&](int p, int l) { return qval(p, l); },
           [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
           [&](int p, int l) {
             return (p >= 0 && p < nx + 1 && l >= -3 && l < ny + 2) ? fx2b[kofs + p + l * sj] : T(0);
@@ -602,7 +623,8 @@ struct fvtp2d_adj_q_kernel {
     } else {
       // y sweep of fy2 on q: flux points j in [0, ny+1), lines i in [-3, nx+2); adds to qb
       ppm_sweep_adjoint<T, 1>(
-          s, A, L0, p1, p2, [&](int p, int l) { return qval(l, p); },
+          s, A, L0, max(0, min(32, ny + 3 - A)), max(0, min(32, nx + 3 - L0)), p1, p2,
+          [&](int p, int l) { return qval(l, p); },
           [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
           [&](int p, int l) {
             return (p >= 0 && p < ny + 1 && l >= -3 && l < nx + 2) ? fy2b[kofs + l + p * sj] : T(0);
