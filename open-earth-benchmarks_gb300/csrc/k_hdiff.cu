@@ -60,32 +60,34 @@ struct hdiffsa_kernel {
       s.crlatu[tid] = ok ? ld(crlatu + (int64_t)j * s1d) : T(0);
     }
     const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    // outputs of this tile (fewer at the domain's far edge) and what each phase needs for them
+    const int vx = max(0, min(kT, d.nx - i0)), vy = max(0, min(kT, d.ny - j0));
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
       const T* pin = in + kofs;
-      for_region<36, 36>([&](int a, int b) {
+      for_region_lim<36, 36>(vx + 4, vy + 4, [&](int a, int b) {
         const int i = i0 - 2 + a, j = j0 - 2 + b;
         const bool ok = i >= -2 && i < d.nx + 2 && j >= -2 && j < d.ny + 2;
         s.in[b][a] = ok ? ld(pin + i + j * sj) : T(0);
       });
       __syncthreads();
-      for_region<34, 35>([&](int a, int b) { s.dy[b][a] = isub(s.in[b + 1][a + 1], s.in[b][a + 1]); });
+      for_region_lim<34, 35>(vx + 2, vy + 3, [&](int a, int b) { s.dy[b][a] = isub(s.in[b + 1][a + 1], s.in[b][a + 1]); });
       __syncthreads();
       // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
-      for_region<34, 34>([&](int a, int b) {
+      for_region_lim<34, 34>(vx + 2, vy + 2, [&](int a, int b) {
         const T c = s.in[b + 1][a + 1];
         s.lap[b][a] = ((iadd(s.in[b + 1][a], s.in[b + 1][a + 2]) - scale2<1>(c)) + s.crlato[b] * s.dy[b + 1][a]) +
                       s.crlatu[b] * (-s.dy[b][a]);
       });
       __syncthreads();
       // hdiffsa.h:106-113: limited fluxes
-      for_region<33, 32>([&](int a, int b) {
+      for_region_lim<33, 32>(vx + 1, vy, [&](int a, int b) {
         T f = s.lap[b + 1][a + 1] - s.lap[b + 1][a];
         if (Prec<T>::prod_gt0(f, s.in[b + 2][a + 2] - s.in[b + 2][a + 1])) f = 0;
         s.flx[b][a] = f;
       });
-      for_region<32, 33>([&](int a, int b) {
+      for_region_lim<32, 33>(vx, vy + 1, [&](int a, int b) {
         T f = s.crlato[b] * (s.lap[b + 1][a + 1] - s.lap[b][a + 1]);
         if (Prec<T>::prod_gt0(f, s.dy[b + 1][a + 1])) f = 0;
         s.fly[b][a] = f;
@@ -153,10 +155,12 @@ struct hdiffsmag_kernel {
       s.crlavu[b] = ok ? ld(crlavu + jo) : T(0);
     }
     const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    // outputs of this tile (fewer at the domain's far edge) and what each phase needs for them
+    const int vx = max(0, min(kT, d.nx - i0)), vy = max(0, min(kT, d.ny - j0));
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
-      for_region<34, 34>([&](int a, int b) {
+      for_region_lim<34, 34>(vx + 2, vy + 2, [&](int a, int b) {
         const int i = i0 - 1 + a, j = j0 - 1 + b;
         const bool ok = i >= -1 && i < d.nx + 1 && j >= -1 && j < d.ny + 1;
         const int64_t o = kofs + i + j * sj;
@@ -166,7 +170,7 @@ struct hdiffsmag_kernel {
       __syncthreads();
       // hdiffsmag.h:213 T_s = (v(j-1)-v) eddlat R^-1 - (u(i-1)-u) acrlat0(j) eddlon
       //              :221 S_uv = (u(j+1)-u) eddlat R^-1 + (v(i+1)-v) acrlat0(j) eddlon
-      for_region<33, 33>([&](int a, int b) {
+      for_region_lim<33, 33>(vx + 1, vy + 1, [&](int a, int b) {
         const T dxu = s.u[b + 1][a + 1] - s.u[b + 1][a];
         const T dyv = s.v[b + 1][a + 1] - s.v[b][a + 1];
         const T dyu = s.u[b + 1][a] - s.u[b][a];
