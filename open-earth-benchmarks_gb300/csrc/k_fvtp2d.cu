@@ -228,32 +228,34 @@ struct fvtp2d_flux_kernel {
     const int sj = (int)d.sj;
     const int nx = d.nx, ny = d.ny;
     const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    // outputs of this tile (fewer at the domain's far edge) and what each phase needs for them
+    const int vx = max(0, min(kT, nx - i0)), vy = max(0, min(kT, ny - j0));
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
       // the flux phases' own inputs, read only after the PPM phases: on their way to L2 now
       const T* const late[6] = {crx, fx2, xfx, cry, fy2, yfx};
       prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
-      for_region<37, 32>([&](int a, int b) {
+      for_region_lim<37, 32>(vx + 5, vy, [&](int a, int b) {
         const int i = i0 - 3 + a, j = j0 + b;
         s.qi[b][a] = (i < nx + 2 && j < ny) ? ld(q_i + kofs + i + j * sj) : T(0);
       });
-      for_region<32, 37>([&](int a, int b) {
+      for_region_lim<32, 37>(vx, vy + 5, [&](int a, int b) {
         const int i = i0 + a, j = j0 - 3 + b;
         s.qj[b][a] = (i < nx && j < ny + 2) ? ld(q_j + kofs + i + j * sj) : T(0);
       });
       __syncthreads();
       // ---- x-PPM of q_i -> fx1 and the x transport flux
-      for_region<34, 32>([&](int a, int b) {
+      for_region_lim<34, 32>(vx + 2, vy, [&](int a, int b) {
         s.w.x.al[b][a] = ppm_al(p1, p2, s.qi[b][a], s.qi[b][a + 1], s.qi[b][a + 2], s.qi[b][a + 3]);
       });
       __syncthreads();
-      for_region<33, 32>([&](int a, int b) {
+      for_region_lim<33, 32>(vx + 1, vy, [&](int a, int b) {
         ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.qi[b][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
                 &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
       });
       __syncthreads();
-      for_region<32, 32>([&](int a, int b) {
+      for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         if (i < nx && j < ny) {
           const int64_t o = kofs + i + j * sj;
@@ -264,16 +266,16 @@ struct fvtp2d_flux_kernel {
       });
       __syncthreads();
       // ---- y-PPM of q_j -> fy1 and the y transport flux
-      for_region<32, 34>([&](int a, int b) {
+      for_region_lim<32, 34>(vx, vy + 2, [&](int a, int b) {
         s.w.y.al[b][a] = ppm_al(p1, p2, s.qj[b][a], s.qj[b + 1][a], s.qj[b + 2][a], s.qj[b + 3][a]);
       });
       __syncthreads();
-      for_region<32, 33>([&](int a, int b) {
+      for_region_lim<32, 33>(vx, vy + 1, [&](int a, int b) {
         ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.qj[b + 2][a], &s.w.y.almq[b][a], &s.w.y.br[b][a],
                 &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
       });
       __syncthreads();
-      for_region<32, 32>([&](int a, int b) {
+      for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
         const int i = i0 + a, j = j0 + b;
         if (i < nx && j < ny) {
           const int64_t o = kofs + i + j * sj;
