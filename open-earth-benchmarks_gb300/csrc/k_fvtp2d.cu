@@ -192,21 +192,23 @@ struct fvtp2d_q_kernel {
 };
 
 // ------------------------------ launch 2 ---------------------------------------------
+// The x sweep (fx1 from q_i) and the y sweep (fy1 from q_j) are independent: each CTA does
+// one of them (blk.z's low bit picks the axis), so a CTA holds one field and one set of PPM
+// intermediates (45 KB in FP64: five CTAs per SM) and half the dependent phases.
 // Interior tile origin (i0, j0).  Shared layout:
-//   qi : 37 x 32, (i0-3+a, j0+b)      qj : 32 x 37, (i0+a, j0-3+b)
-//   x pass: al 34 x 32 (i0-1+a, j0+b); almq/br/b0/smt 33 x 32 (i0-1+a, j0+b)
-//   y pass: al 32 x 34 (i0+a, j0-1+b); almq/br/b0/smt 32 x 33 (i0+a, j0-1+b)
+//   x sweep: qi 37 x 32 (i0-3+a, j0+b); al 34 x 32 (i0-1+a, j0+b); almq/br/b0/smt 33 x 32 (i0-1+a, j0+b)
+//   y sweep: qj 32 x 37 (i0+a, j0-3+b); al 32 x 34 (i0+a, j0-1+b); almq/br/b0/smt 32 x 33 (i0+a, j0-1+b)
 template <class T>
 struct FvFluxSmem {
-  T qi[32][37];
-  T qj[37][32];
   union {
     struct {
+      T qi[32][37];
       T al[32][34];
       T almq[32][33], br[32][33], b0[32][33];
       unsigned char smt[32][33];
     } x;
     struct {
+      T qj[37][32];
       T al[34][32];
       T almq[33][32], br[33][32], b0[33][32];
       unsigned char smt[33][32];
@@ -227,67 +229,80 @@ struct fvtp2d_flux_kernel {
     const int i0 = blk.x * kT, j0 = blk.y * kT;
     const int sj = (int)d.sj;
     const int nx = d.nx, ny = d.ny;
-    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const bool ysweep = (blk.z & 1u) != 0;
+    const int k0 = (int)(blk.z >> 1) * kb, k1 = min(k0 + kb, d.nz);
     // outputs of this tile (fewer at the domain's far edge) and what each phase needs for them
     const int vx = max(0, min(kT, nx - i0)), vy = max(0, min(kT, ny - j0));
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
-      // the flux phases' own inputs, read only after the PPM phases: on their way to L2 now
-      const T* const late[6] = {crx, fx2, xfx, cry, fy2, yfx};
-      prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
-      for_region_lim<37, 32>(vx + 5, vy, [&](int a, int b) {
-        const int i = i0 - 3 + a, j = j0 + b;
-        s.qi[b][a] = (i < nx + 2 && j < ny) ? ld(q_i + kofs + i + j * sj) : T(0);
-      });
-      for_region_lim<32, 37>(vx, vy + 5, [&](int a, int b) {
-        const int i = i0 + a, j = j0 - 3 + b;
-        s.qj[b][a] = (i < nx && j < ny + 2) ? ld(q_j + kofs + i + j * sj) : T(0);
-      });
-      __syncthreads();
-      // ---- x-PPM of q_i -> fx1 and the x transport flux
-      for_region_lim<34, 32>(vx + 2, vy, [&](int a, int b) {
-        s.w.x.al[b][a] = ppm_al(p1, p2, s.qi[b][a], s.qi[b][a + 1], s.qi[b][a + 2], s.qi[b][a + 3]);
-      });
-      __syncthreads();
-      for_region_lim<33, 32>(vx + 1, vy, [&](int a, int b) {
-        ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.qi[b][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
-                &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
-      });
-      __syncthreads();
-      for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
-        const int i = i0 + a, j = j0 + b;
-        if (i < nx && j < ny) {
-          const int64_t o = kofs + i + j * sj;
-          const T f = ppm_flux(ld(crx + o), s.qi[b][a + 2], s.qi[b][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
-                                    s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
-          fx1[o] = (scale2<-1>(f + ld(fx2 + o)) * ld(xfx + o));  // fvtp2d.h:164
-        }
-      });
-      __syncthreads();
-      // ---- y-PPM of q_j -> fy1 and the y transport flux
-      for_region_lim<32, 34>(vx, vy + 2, [&](int a, int b) {
-        s.w.y.al[b][a] = ppm_al(p1, p2, s.qj[b][a], s.qj[b + 1][a], s.qj[b + 2][a], s.qj[b + 3][a]);
-      });
-      __syncthreads();
-      for_region_lim<32, 33>(vx, vy + 1, [&](int a, int b) {
-        ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.qj[b + 2][a], &s.w.y.almq[b][a], &s.w.y.br[b][a],
-                &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
-      });
-      __syncthreads();
-      for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
-        const int i = i0 + a, j = j0 + b;
-        if (i < nx && j < ny) {
-          const int64_t o = kofs + i + j * sj;
-          const T f = ppm_flux(ld(cry + o), s.qj[b + 2][a], s.qj[b + 3][a], s.w.y.br[b][a], s.w.y.b0[b][a],
-                                    s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
-          fy1[o] = (scale2<-1>(f + ld(fy2 + o)) * ld(yfx + o));  // fvtp2d.h:173
-        }
-      });
-      __syncthreads();
+      if (!ysweep) {
+        // ---- x-PPM of q_i -> fx1 and the x transport flux
+        const T* const late[3] = {crx, fx2, xfx};  // read in the last phase only
+        prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
+        for_region_lim<37, 32>(vx + 5, vy, [&](int a, int b) {
+          const int i = i0 - 3 + a, j = j0 + b;
+          s.w.x.qi[b][a] = (i < nx + 2 && j < ny) ? ld(q_i + kofs + i + j * sj) : T(0);
+        });
+        __syncthreads();
+        for_region_lim<34, 32>(vx + 2, vy, [&](int a, int b) {
+          s.w.x.al[b][a] = ppm_al(p1, p2, s.w.x.qi[b][a], s.w.x.qi[b][a + 1], s.w.x.qi[b][a + 2], s.w.x.qi[b][a + 3]);
+        });
+        __syncthreads();
+        for_region_lim<33, 32>(vx + 1, vy, [&](int a, int b) {
+          ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.w.x.qi[b][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
+                  &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
+        });
+        __syncthreads();
+        for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
+          const int i = i0 + a, j = j0 + b;
+          if (i < nx && j < ny) {
+            const int64_t o = kofs + i + j * sj;
+            const T f = ppm_flux(ld(crx + o), s.w.x.qi[b][a + 2], s.w.x.qi[b][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
+                                 s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
+            fx1[o] = (scale2<-1>(f + ld(fx2 + o)) * ld(xfx + o));  // fvtp2d.h:164
+          }
+        });
+        __syncthreads();
+      } else {
+        // ---- y-PPM of q_j -> fy1 and the y transport flux
+        const T* const late[3] = {cry, fy2, yfx};
+        prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
+        for_region_lim<32, 37>(vx, vy + 5, [&](int a, int b) {
+          const int i = i0 + a, j = j0 - 3 + b;
+          s.w.y.qj[b][a] = (i < nx && j < ny + 2) ? ld(q_j + kofs + i + j * sj) : T(0);
+        });
+        __syncthreads();
+        for_region_lim<32, 34>(vx, vy + 2, [&](int a, int b) {
+          s.w.y.al[b][a] = ppm_al(p1, p2, s.w.y.qj[b][a], s.w.y.qj[b + 1][a], s.w.y.qj[b + 2][a], s.w.y.qj[b + 3][a]);
+        });
+        __syncthreads();
+        for_region_lim<32, 33>(vx, vy + 1, [&](int a, int b) {
+          ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.w.y.qj[b + 2][a], &s.w.y.almq[b][a], &s.w.y.br[b][a],
+                  &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
+        });
+        __syncthreads();
+        for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
+          const int i = i0 + a, j = j0 + b;
+          if (i < nx && j < ny) {
+            const int64_t o = kofs + i + j * sj;
+            const T f = ppm_flux(ld(cry + o), s.w.y.qj[b + 2][a], s.w.y.qj[b + 3][a], s.w.y.br[b][a], s.w.y.b0[b][a],
+                                 s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
+            fy1[o] = (scale2<-1>(f + ld(fy2 + o)) * ld(yfx + o));  // fvtp2d.h:173
+          }
+        });
+        __syncthreads();
+      }
     }
   }
 };
+
+// Grid of launch 2: the tiles of the interior, twice along z (one CTA per axis).
+inline dim3 flux_grid(const Dims& d, int kb) {
+  dim3 g = tile_grid(d.nx, d.ny, d.nz, kT, kT, kb);
+  g.z *= 2;
+  return g;
+}
 
 constexpr int kKB = 1;  // k-levels per CTA by default (the most CTAs hide latency best)
 
@@ -327,7 +342,7 @@ oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* f
                                      gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gq.origin, gcx.origin,
                                      gcy.origin, grx.origin, gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d,
                                      kb));
-  return launch<fvtp2d_flux_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FvFluxSmem<T>), st,
+  return launch<fvtp2d_flux_kernel<T>>(flux_grid(d, kb), sizeof(FvFluxSmem<T>), st,
                                        gfx1.origin, gfy1.origin, gqi.origin, gqj.origin, gfx2.origin, gfy2.origin,
                                        gcx.origin, gcy.origin, gxf.origin, gyf.origin, p1, p2, d, kb);
 }
@@ -369,7 +384,7 @@ oeb_status fvtp2d_tl_entry(const M3* dq_i, const M3* dq_j, const M3* dfx1, const
   const int kb = tuned_kb(kKB);
   OEB_TRY(launch<fvtp2d_q_kernel<D>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<D>), st, oqi,
                                      oqj, ofx2, ofy2, x, cx, cy, rx, ry, xf, yf, ar, D(p1), D(p2), d, kb));
-  OEB_TRY(launch<fvtp2d_flux_kernel<D>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FvFluxSmem<D>), st, ofx1,
+  OEB_TRY(launch<fvtp2d_flux_kernel<D>>(flux_grid(d, kb), sizeof(FvFluxSmem<D>), st, ofx1,
                                         ofy1, oqi, oqj, ofx2, ofy2, cx, cy, xf, yf, D(p1), D(p2), d, kb));
   OEB_TRY(arr.unpack(dq_i->aligned + dq_i->offset, oqi, *dom, kFvQi, d.sj, d.sk));
   OEB_TRY(arr.unpack(dq_j->aligned + dq_j->offset, oqj, *dom, kFvQj, d.sj, d.sk));
