@@ -30,14 +30,15 @@ __device__ __forceinline__ T ppm_al(T p1, T p2, T qm2, T qm1, T q0, T qp1) {
   return (p1 * (qm1 + q0)) + (p2 * (qm2 + qp1));
 }
 
-// fvtp2d.h:20-23: almq = al - q, br = al(+1) - q, b0 = almq + br, smt5 = almq*br < 0
+// fvtp2d.h:20-23: almq = al - q, br = al(+1) - q, smt5 = almq*br < 0 (b0 = almq + br is formed
+// where it is used: ppm_flux uses one of its two b0 operands, so forming it there is one
+// addition a flux point, as storing it was one an aux point, of the same operands)
 template <class T>
-__device__ __forceinline__ void ppm_aux(T al0, T al1, T q0, T* almq, T* br, T* b0, unsigned char* smt) {
+__device__ __forceinline__ void ppm_aux(T al0, T al1, T q0, T* almq, T* br, unsigned char* smt) {
   const T m = al0 - q0;
   const T r = al1 - q0;
   *almq = m;
   *br = r;
-  *b0 = m + r;
   *smt = Prec<T>::prod_lt0(m, r);
 }
 
@@ -47,11 +48,12 @@ __device__ __forceinline__ void ppm_aux(T al0, T al1, T q0, T* almq, T* br, T* b
 // FP64 operations, (1 - c)(br - c b0) as 1 + (-c) and br + (-(c b0)) -- the same values, an
 // IEEE subtraction being the addition of the negation -- so no warp runs both sides.
 template <class T>
-__device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T br_m1, T b0_m1, T almq_0, T b0_0, unsigned char smt_m1,
+__device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T almq_m1, T br_m1, T almq_0, T br_0, unsigned char smt_m1,
                                       unsigned char smt_0) {
   const bool pos = gt0(c);
   const T u = T(1.) + (pos ? -c : c);
-  const T p = c * (pos ? b0_m1 : b0_0);
+  const T b0 = (pos ? almq_m1 : almq_0) + (pos ? br_m1 : br_0);  // fvtp2d.h:22 at the upwind side
+  const T p = c * b0;
   const T v = (pos ? br_m1 : almq_0) + (pos ? -p : p);
   return Prec<T>::add_flag(pos ? q_m1 : q_0, u * v, (smt_m1 | smt_0) != 0);
 }
@@ -59,8 +61,8 @@ __device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T br_m1, T b0_m1, T al
 // ------------------------------ launch 1 ---------------------------------------------
 // Tile origin (i0, j0) = (-3 + 32 bx, -3 + 32 by).  Shared layout:
 //   q    : 38 x 39, (i0-3+a, j0-3+b)
-//   y pass: al 32 x 35 (i0+a, j0-1+b); almq/br/b0/smt 32 x 34 (i0+a, j0-1+b)
-//   x pass: al 35 x 32 (i0-1+a, j0+b); almq/br/b0/smt 34 x 32 (i0-1+a, j0+b)
+//   y pass: al 32 x 35 (i0+a, j0-1+b); almq/br/smt 32 x 34 (i0+a, j0-1+b)
+//   x pass: al 35 x 32 (i0-1+a, j0+b); almq/br/smt 34 x 32 (i0-1+a, j0+b)
 //   fyy  : 32 x 33 (i0+a, j0+b) = yfx * fy2, 0 outside fy2's range
 //   fxx  : 33 x 32 (i0+a, j0+b) = xfx * fx2, 0 outside fx2's range, in fyy's place: q_i, the
 //          only reader of fyy, is computed before the x pass writes fxx (56 KB a tile: four
@@ -71,12 +73,12 @@ struct FvQSmem {
   union {
     struct {
       T al[35][32];
-      T almq[34][32], br[34][32], b0[34][32];
+      T almq[34][32], br[34][32];
       unsigned char smt[34][32];
     } y;
     struct {
       T al[32][35];
-      T almq[32][34], br[32][34], b0[32][34];
+      T almq[32][34], br[32][34];
       unsigned char smt[32][34];
     } x;
   } w;
@@ -130,7 +132,7 @@ struct fvtp2d_q_kernel {
       __syncthreads();
       for_region_lim<32, 34>(ax, yfb + 1, [&](int a, int b) {
         ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.q[b + 2][a + 3], &s.w.y.almq[b][a], &s.w.y.br[b][a],
-                &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
+                &s.w.y.smt[b][a]);
       });
       __syncthreads();
       for_region_lim<32, 33>(ax, yfb, [&](int a, int b) {
@@ -138,8 +140,8 @@ struct fvtp2d_q_kernel {
         T fyy = T(0);
         if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {  // fvtp2d.h:26-27
           const int64_t o = kofs + i + j * sj;
-          const T f = ppm_flux(ld(cry + o), s.q[b + 2][a + 3], s.q[b + 3][a + 3], s.w.y.br[b][a], s.w.y.b0[b][a],
-                                    s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
+          const T f = ppm_flux(ld(cry + o), s.q[b + 2][a + 3], s.q[b + 3][a + 3], s.w.y.almq[b][a], s.w.y.br[b][a],
+                                 s.w.y.almq[b + 1][a], s.w.y.br[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
           if (b < kT) fy2[o] = f;
           fyy = ld(yfx + o) * f;  // fvtp2d.h:43
         }
@@ -161,7 +163,7 @@ struct fvtp2d_q_kernel {
       __syncthreads();
       for_region_lim<34, 32>(xfa + 1, by, [&](int a, int b) {
         ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.q[b + 3][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
-                &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
+                &s.w.x.smt[b][a]);
       });
       __syncthreads();
       for_region_lim<33, 32>(xfa, by, [&](int a, int b) {
@@ -169,8 +171,8 @@ struct fvtp2d_q_kernel {
         T fxx = T(0);
         if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {  // fvtp2d.h:102-103
           const int64_t o = kofs + i + j * sj;
-          const T f = ppm_flux(ld(crx + o), s.q[b + 3][a + 2], s.q[b + 3][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
-                                    s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
+          const T f = ppm_flux(ld(crx + o), s.q[b + 3][a + 2], s.q[b + 3][a + 3], s.w.x.almq[b][a], s.w.x.br[b][a],
+                                 s.w.x.almq[b][a + 1], s.w.x.br[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
           if (a < kT) fx2[o] = f;
           fxx = ld(xfx + o) * f;  // fvtp2d.h:119
         }
@@ -196,21 +198,21 @@ struct fvtp2d_q_kernel {
 // one of them (blk.z's low bit picks the axis), so a CTA holds one field and one set of PPM
 // intermediates (45 KB in FP64: five CTAs per SM) and half the dependent phases.
 // Interior tile origin (i0, j0).  Shared layout:
-//   x sweep: qi 37 x 32 (i0-3+a, j0+b); al 34 x 32 (i0-1+a, j0+b); almq/br/b0/smt 33 x 32 (i0-1+a, j0+b)
-//   y sweep: qj 32 x 37 (i0+a, j0-3+b); al 32 x 34 (i0+a, j0-1+b); almq/br/b0/smt 32 x 33 (i0+a, j0-1+b)
+//   x sweep: qi 37 x 32 (i0-3+a, j0+b); al 34 x 32 (i0-1+a, j0+b); almq/br/smt 33 x 32 (i0-1+a, j0+b)
+//   y sweep: qj 32 x 37 (i0+a, j0-3+b); al 32 x 34 (i0+a, j0-1+b); almq/br/smt 32 x 33 (i0+a, j0-1+b)
 template <class T>
 struct FvFluxSmem {
   union {
     struct {
       T qi[32][37];
       T al[32][34];
-      T almq[32][33], br[32][33], b0[32][33];
+      T almq[32][33], br[32][33];
       unsigned char smt[32][33];
     } x;
     struct {
       T qj[37][32];
       T al[34][32];
-      T almq[33][32], br[33][32], b0[33][32];
+      T almq[33][32], br[33][32];
       unsigned char smt[33][32];
     } y;
   } w;
@@ -251,15 +253,15 @@ struct fvtp2d_flux_kernel {
         __syncthreads();
         for_region_lim<33, 32>(vx + 1, vy, [&](int a, int b) {
           ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.w.x.qi[b][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
-                  &s.w.x.b0[b][a], &s.w.x.smt[b][a]);
+                &s.w.x.smt[b][a]);
         });
         __syncthreads();
         for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
           const int i = i0 + a, j = j0 + b;
           if (i < nx && j < ny) {
             const int64_t o = kofs + i + j * sj;
-            const T f = ppm_flux(ld(crx + o), s.w.x.qi[b][a + 2], s.w.x.qi[b][a + 3], s.w.x.br[b][a], s.w.x.b0[b][a],
-                                 s.w.x.almq[b][a + 1], s.w.x.b0[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
+            const T f = ppm_flux(ld(crx + o), s.w.x.qi[b][a + 2], s.w.x.qi[b][a + 3], s.w.x.almq[b][a], s.w.x.br[b][a],
+                                 s.w.x.almq[b][a + 1], s.w.x.br[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
             fx1[o] = (scale2<-1>(f + ld(fx2 + o)) * ld(xfx + o));  // fvtp2d.h:164
           }
         });
@@ -279,15 +281,15 @@ struct fvtp2d_flux_kernel {
         __syncthreads();
         for_region_lim<32, 33>(vx, vy + 1, [&](int a, int b) {
           ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.w.y.qj[b + 2][a], &s.w.y.almq[b][a], &s.w.y.br[b][a],
-                  &s.w.y.b0[b][a], &s.w.y.smt[b][a]);
+                &s.w.y.smt[b][a]);
         });
         __syncthreads();
         for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
           const int i = i0 + a, j = j0 + b;
           if (i < nx && j < ny) {
             const int64_t o = kofs + i + j * sj;
-            const T f = ppm_flux(ld(cry + o), s.w.y.qj[b + 2][a], s.w.y.qj[b + 3][a], s.w.y.br[b][a], s.w.y.b0[b][a],
-                                 s.w.y.almq[b + 1][a], s.w.y.b0[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
+            const T f = ppm_flux(ld(cry + o), s.w.y.qj[b + 2][a], s.w.y.qj[b + 3][a], s.w.y.almq[b][a], s.w.y.br[b][a],
+                                 s.w.y.almq[b + 1][a], s.w.y.br[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
             fy1[o] = (scale2<-1>(f + ld(fy2 + o)) * ld(yfx + o));  // fvtp2d.h:173
           }
         });
