@@ -59,33 +59,37 @@ __device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T almq_m1, T br_m1, T 
 }
 
 // ------------------------------ launch 1 ---------------------------------------------
+// The y pass (fy2, fyy, then q_i) and the x pass (fx2, fxx, then q_j) are independent given
+// q: each CTA does one of them (blk.z's low bit picks the axis) and holds only the part of
+// the q tile and the PPM intermediates that pass reads, with fyy / fxx in the place of al,
+// which is dead once the aux values are set (37 KB a CTA in FP64: six CTAs per SM).
 // Tile origin (i0, j0) = (-3 + 32 bx, -3 + 32 by).  Shared layout:
-//   q    : 38 x 39, (i0-3+a, j0-3+b)
-//   y pass: al 32 x 35 (i0+a, j0-1+b); almq/br/smt 32 x 34 (i0+a, j0-1+b)
-//   x pass: al 35 x 32 (i0-1+a, j0+b); almq/br/smt 34 x 32 (i0-1+a, j0+b)
-//   fyy  : 32 x 33 (i0+a, j0+b) = yfx * fy2, 0 outside fy2's range
-//   fxx  : 33 x 32 (i0+a, j0+b) = xfx * fx2, 0 outside fx2's range, in fyy's place: q_i, the
-//          only reader of fyy, is computed before the x pass writes fxx (56 KB a tile: four
-//          CTAs per SM)
+//   y pass: q 32 x 39 (i0+a, j0-3+b); al 32 x 35 (i0+a, j0-1+b), then fyy 32 x 33 (i0+a, j0+b)
+//           = yfy * fy2, 0 outside fy2's range; almq/br/smt 32 x 34 (i0+a, j0-1+b)
+//   x pass: q 38 x 32 (i0-3+a, j0+b); al 35 x 32 (i0-1+a, j0+b), then fxx 33 x 32 (i0+a, j0+b)
+//           = xfx * fx2, 0 outside fx2's range; almq/br/smt 34 x 32 (i0-1+a, j0+b)
 template <class T>
 struct FvQSmem {
-  T q[39][38];
   union {
     struct {
-      T al[35][32];
+      T q[39][32];
+      union {
+        T al[35][32];
+        T fyy[33][32];
+      } e;
       T almq[34][32], br[34][32];
       unsigned char smt[34][32];
     } y;
     struct {
-      T al[32][35];
+      T q[32][38];
+      union {
+        T al[32][35];
+        T fxx[32][33];
+      } e;
       T almq[32][34], br[32][34];
       unsigned char smt[32][34];
     } x;
   } w;
-  union {
-    T fyy[33][32];
-    T fxx[32][33];
-  } f;
 };
 
 template <class T>
@@ -101,97 +105,111 @@ struct fvtp2d_q_kernel {
     const int i0 = -3 + (int)blk.x * kT, j0 = -3 + (int)blk.y * kT;
     const int sj = (int)d.sj;
     const int nx = d.nx, ny = d.ny;
-    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const bool ypass = (blk.z & 1u) == 0;
+    const int k0 = (int)(blk.z >> 1) * kb, k1 = min(k0 + kb, d.nz);
     // the cells each phase needs for this tile's outputs (fewer at the output box's far
     // edge: the box is nx+5 wide, so the last tile column holds a few useful columns only)
     auto lim = [](int v, int hi) { return max(0, min(v, hi)); };
-    const int ax = lim(nx + 2 - i0, 32);        // columns of fy2 and q_i
-    const int yfb = lim(ny + 1 - j0, 33);       // rows of fy2 / fyy
-    const int qib = lim(ny - j0, 32);           // rows of q_i
-    const int xfa = lim(nx + 1 - i0, 33);       // columns of fx2 / fxx
-    const int by = lim(ny + 2 - j0, 32);        // rows of fx2 and q_j
-    const int qja = lim(nx - i0, 32);           // columns of q_j
-    const int qcols = min(38, max(ax + 3, xfa + 5));          // q read by the phases above
-    const int qrows = min(39, max(yfb + 5, max(by, qib) + 3));
+    auto qok = [&](int i, int j) { return i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3; };
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
-      // the inputs of the flux and q_i / q_j phases, read only after the PPM phases
-      const T* const late[7] = {cry, yfx, area, ra_y, crx, xfx, ra_x};
-      prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
-      for_region_lim<38, 39>(qcols, qrows, [&](int a, int b) {
-        const int i = i0 - 3 + a, j = j0 - 3 + b;
-        const bool ok = i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3;
-        s.q[b][a] = ok ? ld(q + kofs + i + j * sj) : T(0);
-      });
-      __syncthreads();
-      // ---- y-PPM of q -> fy2, fyy
-      for_region_lim<32, 35>(ax, yfb + 2, [&](int a, int b) {
-        s.w.y.al[b][a] = ppm_al(p1, p2, s.q[b][a + 3], s.q[b + 1][a + 3], s.q[b + 2][a + 3], s.q[b + 3][a + 3]);
-      });
-      __syncthreads();
-      for_region_lim<32, 34>(ax, yfb + 1, [&](int a, int b) {
-        ppm_aux(s.w.y.al[b][a], s.w.y.al[b + 1][a], s.q[b + 2][a + 3], &s.w.y.almq[b][a], &s.w.y.br[b][a],
-                &s.w.y.smt[b][a]);
-      });
-      __syncthreads();
-      for_region_lim<32, 33>(ax, yfb, [&](int a, int b) {
-        const int i = i0 + a, j = j0 + b;
-        T fyy = T(0);
-        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {  // fvtp2d.h:26-27
-          const int64_t o = kofs + i + j * sj;
-          const T f = ppm_flux(ld(cry + o), s.q[b + 2][a + 3], s.q[b + 3][a + 3], s.w.y.almq[b][a], s.w.y.br[b][a],
-                                 s.w.y.almq[b + 1][a], s.w.y.br[b + 1][a], s.w.y.smt[b][a], s.w.y.smt[b + 1][a]);
-          if (b < kT) fy2[o] = f;
-          fyy = ld(yfx + o) * f;  // fvtp2d.h:43
-        }
-        s.f.fyy[b][a] = fyy;
-      });
-      __syncthreads();
-      // ---- q_i (fvtp2d.h:48), the last reader of fyy, beside the x-PPM edge values
-      for_region_lim<32, 32>(ax, qib, [&](int a, int b) {
-        const int i = i0 + a, j = j0 + b;
-        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
-          const int64_t o = kofs + i + j * sj;
-          q_i[o] = (((s.q[b + 3][a + 3] * ld(area + o)) + s.f.fyy[b][a]) - s.f.fyy[b + 1][a]) / ld(ra_y + o);
-        }
-      });
-      // ---- x-PPM of q -> fx2, fxx
-      for_region_lim<35, 32>(xfa + 2, by, [&](int a, int b) {
-        s.w.x.al[b][a] = ppm_al(p1, p2, s.q[b + 3][a], s.q[b + 3][a + 1], s.q[b + 3][a + 2], s.q[b + 3][a + 3]);
-      });
-      __syncthreads();
-      for_region_lim<34, 32>(xfa + 1, by, [&](int a, int b) {
-        ppm_aux(s.w.x.al[b][a], s.w.x.al[b][a + 1], s.q[b + 3][a + 2], &s.w.x.almq[b][a], &s.w.x.br[b][a],
-                &s.w.x.smt[b][a]);
-      });
-      __syncthreads();
-      for_region_lim<33, 32>(xfa, by, [&](int a, int b) {
-        const int i = i0 + a, j = j0 + b;
-        T fxx = T(0);
-        if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {  // fvtp2d.h:102-103
-          const int64_t o = kofs + i + j * sj;
-          const T f = ppm_flux(ld(crx + o), s.q[b + 3][a + 2], s.q[b + 3][a + 3], s.w.x.almq[b][a], s.w.x.br[b][a],
-                                 s.w.x.almq[b][a + 1], s.w.x.br[b][a + 1], s.w.x.smt[b][a], s.w.x.smt[b][a + 1]);
-          if (a < kT) fx2[o] = f;
-          fxx = ld(xfx + o) * f;  // fvtp2d.h:119
-        }
-        s.f.fxx[b][a] = fxx;
-      });
-      __syncthreads();
-      // ---- q_j (fvtp2d.h:124)
-      for_region_lim<32, 32>(qja, by, [&](int a, int b) {
-        const int i = i0 + a, j = j0 + b;
-        const int64_t o = kofs + i + j * sj;
-        const T qc = s.q[b + 3][a + 3];
-        if (i >= 0 && i < nx && j >= -3 && j < ny + 2) {
-          q_j[o] = (((qc * ld(area + o)) + s.f.fxx[b][a]) - s.f.fxx[b][a + 1]) / ld(ra_x + o);
-        }
-      });
-      __syncthreads();
+      if (ypass) {
+        auto& w = s.w.y;
+        const int ax = lim(nx + 2 - i0, 32);   // columns of fy2 and q_i
+        const int yfb = lim(ny + 1 - j0, 33);  // rows of fy2 / fyy
+        const int qib = lim(ny - j0, 32);      // rows of q_i
+        const T* const late[4] = {cry, yfx, area, ra_y};  // read after the PPM phases
+        prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
+        // (one row more than the phases read, so that full tiles take the compile-time loop)
+        for_region_lim<32, 39>(ax, min(39, max(yfb + 6, qib + 3)), [&](int a, int b) {
+          const int i = i0 + a, j = j0 - 3 + b;
+          w.q[b][a] = qok(i, j) ? ld(q + kofs + i + j * sj) : T(0);
+        });
+        __syncthreads();
+        for_region_lim<32, 35>(ax, yfb + 2, [&](int a, int b) {
+          w.e.al[b][a] = ppm_al(p1, p2, w.q[b][a], w.q[b + 1][a], w.q[b + 2][a], w.q[b + 3][a]);
+        });
+        __syncthreads();
+        for_region_lim<32, 34>(ax, yfb + 1, [&](int a, int b) {
+          ppm_aux(w.e.al[b][a], w.e.al[b + 1][a], w.q[b + 2][a], &w.almq[b][a], &w.br[b][a], &w.smt[b][a]);
+        });
+        __syncthreads();
+        for_region_lim<32, 33>(ax, yfb, [&](int a, int b) {
+          const int i = i0 + a, j = j0 + b;
+          T fyy = T(0);
+          if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {  // fvtp2d.h:26-27
+            const int64_t o = kofs + i + j * sj;
+            const T f = ppm_flux(ld(cry + o), w.q[b + 2][a], w.q[b + 3][a], w.almq[b][a], w.br[b][a],
+                                 w.almq[b + 1][a], w.br[b + 1][a], w.smt[b][a], w.smt[b + 1][a]);
+            if (b < kT) fy2[o] = f;
+            fyy = ld(yfx + o) * f;  // fvtp2d.h:43
+          }
+          w.e.fyy[b][a] = fyy;  // al is dead: the aux values are set
+        });
+        __syncthreads();
+        // q_i (fvtp2d.h:48)
+        for_region_lim<32, 32>(ax, qib, [&](int a, int b) {
+          const int i = i0 + a, j = j0 + b;
+          if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
+            const int64_t o = kofs + i + j * sj;
+            q_i[o] = (((w.q[b + 3][a] * ld(area + o)) + w.e.fyy[b][a]) - w.e.fyy[b + 1][a]) / ld(ra_y + o);
+          }
+        });
+        __syncthreads();
+      } else {
+        auto& w = s.w.x;
+        const int xfa = lim(nx + 1 - i0, 33);  // columns of fx2 / fxx
+        const int by = lim(ny + 2 - j0, 32);   // rows of fx2 and q_j
+        const int qja = lim(nx - i0, 32);      // columns of q_j
+        const T* const late[4] = {crx, xfx, area, ra_x};
+        prefetch_tile(late, kofs, i0, j0, nx, ny, sj);
+        for_region_lim<38, 32>(min(38, max(xfa + 5, qja + 3)), by, [&](int a, int b) {
+          const int i = i0 - 3 + a, j = j0 + b;
+          w.q[b][a] = qok(i, j) ? ld(q + kofs + i + j * sj) : T(0);
+        });
+        __syncthreads();
+        for_region_lim<35, 32>(xfa + 2, by, [&](int a, int b) {
+          w.e.al[b][a] = ppm_al(p1, p2, w.q[b][a], w.q[b][a + 1], w.q[b][a + 2], w.q[b][a + 3]);
+        });
+        __syncthreads();
+        for_region_lim<34, 32>(xfa + 1, by, [&](int a, int b) {
+          ppm_aux(w.e.al[b][a], w.e.al[b][a + 1], w.q[b][a + 2], &w.almq[b][a], &w.br[b][a], &w.smt[b][a]);
+        });
+        __syncthreads();
+        for_region_lim<33, 32>(xfa, by, [&](int a, int b) {
+          const int i = i0 + a, j = j0 + b;
+          T fxx = T(0);
+          if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {  // fvtp2d.h:102-103
+            const int64_t o = kofs + i + j * sj;
+            const T f = ppm_flux(ld(crx + o), w.q[b][a + 2], w.q[b][a + 3], w.almq[b][a], w.br[b][a],
+                                 w.almq[b][a + 1], w.br[b][a + 1], w.smt[b][a], w.smt[b][a + 1]);
+            if (a < kT) fx2[o] = f;
+            fxx = ld(xfx + o) * f;  // fvtp2d.h:119
+          }
+          w.e.fxx[b][a] = fxx;  // al is dead: the aux values are set
+        });
+        __syncthreads();
+        // q_j (fvtp2d.h:124)
+        for_region_lim<32, 32>(qja, by, [&](int a, int b) {
+          const int i = i0 + a, j = j0 + b;
+          if (i >= 0 && i < nx && j >= -3 && j < ny + 2) {
+            const int64_t o = kofs + i + j * sj;
+            q_j[o] = (((w.q[b][a + 3] * ld(area + o)) + w.e.fxx[b][a]) - w.e.fxx[b][a + 1]) / ld(ra_x + o);
+          }
+        });
+        __syncthreads();
+      }
     }
   }
 };
+
+// Grid of launch 1: the tiles of the output box [-3, n+2)^2, twice along z (one CTA per axis).
+inline dim3 q_grid(const Dims& d, int kb) {
+  dim3 g = tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb);
+  g.z *= 2;
+  return g;
+}
 
 // ------------------------------ launch 2 ---------------------------------------------
 // The x sweep (fx1 from q_i) and the y sweep (fy1 from q_j) are independent: each CTA does
@@ -340,7 +358,7 @@ oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* f
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
   cudaStream_t st = (cudaStream_t)stream;
   const int kb = tuned_kb(kKB);
-  OEB_TRY(launch<fvtp2d_q_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<T>), st,
+  OEB_TRY(launch<fvtp2d_q_kernel<T>>(q_grid(d, kb), sizeof(FvQSmem<T>), st,
                                      gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gq.origin, gcx.origin,
                                      gcy.origin, grx.origin, gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d,
                                      kb));
@@ -384,7 +402,7 @@ oeb_status fvtp2d_tl_entry(const M3* dq_i, const M3* dq_j, const M3* dfx1, const
   OEB_TRY(arr.alloc(dfy2, &ofy2));
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, q->strides[1], q->strides[0]};
   const int kb = tuned_kb(kKB);
-  OEB_TRY(launch<fvtp2d_q_kernel<D>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<D>), st, oqi,
+  OEB_TRY(launch<fvtp2d_q_kernel<D>>(q_grid(d, kb), sizeof(FvQSmem<D>), st, oqi,
                                      oqj, ofx2, ofy2, x, cx, cy, rx, ry, xf, yf, ar, D(p1), D(p2), d, kb));
   OEB_TRY(launch<fvtp2d_flux_kernel<D>>(flux_grid(d, kb), sizeof(FvFluxSmem<D>), st, ofx1,
                                         ofy1, oqi, oqj, ofx2, ofy2, cx, cy, xf, yf, D(p1), D(p2), d, kb));
@@ -692,7 +710,7 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
   const int kb = tuned_kb(kKB);
   const size_t ps = sizeof(PpmAdjSmem<T>);
-  oeb_status stt = launch<fvtp2d_q_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(FvQSmem<T>), st,
+  oeb_status stt = launch<fvtp2d_q_kernel<T>>(q_grid(d, kb), sizeof(FvQSmem<T>), st,
                                               sqi, sqj, sfx2, sfy2, gq.origin, gcx.origin, gcy.origin, grx.origin,
                                               gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d, kb);
   // the x and y sweeps of the two PPM adjoints (axis flag 0 / 1)
