@@ -736,9 +736,13 @@ def _e2e(pkg, fields, torch, args, names):
                 d2h += (NX + ilo + ihi) * (NY + jlo + jhi) * (NZ + klo + khi) * 8
 
     stream = torch.cuda.Stream()
+    # The calls are independent.  They are issued with the most output fields first, so the
+    # part of the step after the last copy-in (that call's compute and copy-out) is a
+    # one-output call's and not fvtp2d's six outputs.
+    order = sorted(names, key=lambda n: -len(pkg.KERNELS[n].by_role("out3")))
 
     def step():
-        for name in names:
+        for name in order:
             st, sc = hs[name]
             pkg.call(name, st, sc, domain=dom, stream=stream)
         stream.synchronize()  # every output of the step is in host memory
@@ -766,7 +770,7 @@ def _e2e(pkg, fields, torch, args, names):
     return {"value": round(pts / dt / 1e9, 4), "unit": "GPts/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(dt * 1e3, 3),
             "path": "oeb_<k>_f64_host on pinned host buffers with oeb_set_host_async(1): the ten calls are enqueued on "
-                    "one stream and the step ends with its synchronisation; "
+                    "one stream, most output fields first, and the step ends with its synchronisation; "
                     "each call stages the k-planes its kernel reads through device memory, and the copy-in of one "
                     "call overlaps the compute and copy-out of the previous",
             "synchronous_direct": {"value": round(pts / dt_direct / 1e9, 4), "ms_per_step": round(dt_direct * 1e3, 3),
