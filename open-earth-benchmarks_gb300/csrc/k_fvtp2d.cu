@@ -62,7 +62,8 @@ __device__ __forceinline__ T ppm_flux(T c, T q_m1, T q_0, T almq_m1, T br_m1, T 
 // The y pass (fy2, fyy, then q_i) and the x pass (fx2, fxx, then q_j) are independent given
 // q: each CTA does one of them (blk.z's low bit picks the axis) and holds only the part of
 // the q tile and the PPM intermediates that pass reads, with fyy / fxx in the place of al,
-// which is dead once the aux values are set (37 KB a CTA in FP64: six CTAs per SM).
+// which is dead once the aux values are set (37 KB a CTA in FP64; its 42 registers a thread
+// allow five CTAs per SM).
 // Tile origin (i0, j0) = (-3 + 32 bx, -3 + 32 by).  Shared layout:
 //   y pass: q 32 x 39 (i0+a, j0-3+b); al 32 x 35 (i0+a, j0-1+b), then fyy 32 x 33 (i0+a, j0+b)
 //           = yfy * fy2, 0 outside fy2's range; almq/br/smt 32 x 34 (i0+a, j0-1+b)
@@ -214,7 +215,7 @@ inline dim3 q_grid(const Dims& d, int kb) {
 // ------------------------------ launch 2 ---------------------------------------------
 // The x sweep (fx1 from q_i) and the y sweep (fy1 from q_j) are independent: each CTA does
 // one of them (blk.z's low bit picks the axis), so a CTA holds one field and one set of PPM
-// intermediates (45 KB in FP64: five CTAs per SM) and half the dependent phases.
+// intermediates (36 KB in FP64: six CTAs per SM) and half the dependent phases.
 // Interior tile origin (i0, j0).  Shared layout:
 //   x sweep: qi 37 x 32 (i0-3+a, j0+b); al 34 x 32 (i0-1+a, j0+b); almq/br/smt 33 x 32 (i0-1+a, j0+b)
 //   y sweep: qj 32 x 37 (i0+a, j0-3+b); al 32 x 34 (i0+a, j0-1+b); almq/br/smt 32 x 33 (i0+a, j0-1+b)
