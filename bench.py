@@ -355,6 +355,7 @@ def run_ours(args):
         ms_total = float(t.item())
         torch.distributed.barrier()
     ms_step = ms_total / args.steps
+    clock_summary = clocks.summary()
     pts_step = len(names) * NX * NY * NZ
     value = world * pts_step * args.steps / (ms_total * 1e-3) / 1e9
     total_k = sum(per_kernel.values())
@@ -452,6 +453,8 @@ def run_ours(args):
                      "launch_ms": round(per_kernel[dom_k], 5),
                      "fp64_pipe_active_pct": _ncu_summary(dom_k, "fp64_pipe_active_pct"),
                      "alu_pipe_active_pct": _ncu_summary(dom_k, "alu_pipe_active_pct"),
+                     "fp64_pipe_roof": _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clock_summary,
+                                                           torch.cuda.get_device_properties(dev).multi_processor_count),
                      "note": "the FP64 stencils are compute-bound, not HBM-bound: GB300 issues 1.6 FP64 "
                              "op/clk/SM, so the kernels run as F64i (exact integer-pipe multiply, divide, "
                              "sqrt, compare beside FP64-pipe adds); the pipe figures are ncu's "
@@ -459,7 +462,7 @@ def run_ours(args):
         "per_kernel_ms": {k: round(v, 5) for k, v in per_kernel.items()},
         "per_kernel_gbs": {k: round(_algorithmic_bytes(pkg, k) / (v * 1e-3) / 1e9, 1) for k, v in per_kernel.items()},
         "kernel_share": {k: round(v / total_k, 4) for k, v in per_kernel.items()},
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
         "gpu_launches": int(launches),
         "sequential": {"value": round(world * pts_step * args.steps / (ms_seq * 1e-3) / 1e9, 4),
                        "ms_per_step": round(ms_seq / args.steps, 4), "gpu_launches": int(launches_seq),
@@ -708,6 +711,35 @@ def _ncu_summary(kernel, key):
             except ValueError:
                 return None
     return None
+
+
+# FP64-pipe thread instructions (DADD / DMUL / DFMA) per clock per SM on the GB300, measured
+# by a dependent-free DADD throughput loop: 505 G/s at 2070 MHz on 152 SMs.
+FP64_PIPE_PER_CLK_SM = 1.6
+PIPE_MIX_PROFILE = "pipe_mix_ten_stencils_f64"
+
+
+def _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clocks_summary, sms):
+    """The FP64 pipe as the roof: each kernel's FP64-pipe instructions per interior point
+    (committed ncu counts) x points, over the pipe's rate at the SM clock sampled during the
+    timed region.  For the dominant kernel (sequential pass) and for the whole concurrent
+    step.  None without the counts or a clock sample."""
+    mhz = (clocks_summary or {}).get("sm_mhz")
+    per_pt = {k: _ncu_summary(PIPE_MIX_PROFILE, "fp64_instr_per_point_" + k) for k in names}
+    if not mhz or any(v is None for v in per_pt.values()):
+        return None
+    rate = FP64_PIPE_PER_CLK_SM * sms * mhz * 1e6  # thread instructions / s
+    pts = NX * NY * NZ
+    k_bound_ms = per_pt[dom_k] * pts / rate * 1e3
+    step_bound_ms = sum(per_pt.values()) * pts / rate * 1e3
+    return {"unit": "FP64-pipe instructions", "rate_per_clk_per_sm": FP64_PIPE_PER_CLK_SM, "sms": sms,
+            "sm_mhz": mhz, "kernel": dom_k, "kernel_instr_per_point": per_pt[dom_k],
+            "kernel_bound_ms": round(k_bound_ms, 5), "kernel_frac": round(k_bound_ms / per_kernel[dom_k], 4),
+            "step_instr_per_point": round(sum(per_pt.values()), 2), "step_bound_ms": round(step_bound_ms, 5),
+            "step_frac": round(step_bound_ms / ms_step, 4),
+            "source": "instructions per point: profiles/ncu_%s_128x128x80.md (ncu "
+                      "sm__inst_executed_pipe_fp64); frac = bound / measured (kernel: sequential pass; step: "
+                      "the concurrent graph)" % PIPE_MIX_PROFILE}
 
 
 def _ncu_traffic(kernel):

@@ -1,0 +1,62 @@
+"""bench.py's figures that come from committed ncu summaries, checked on the CPU.
+
+The bench line's `roofline.traffic`, its pipe percentages and its FP64-pipe roof read
+profiles/*.md; a summary that lost a key would silently turn them into null.
+"""
+from __future__ import annotations
+
+import importlib.util
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def bench():
+    spec = importlib.util.spec_from_file_location("oeb_bench_cpu", ROOT / "bench.py")
+    mod = importlib.util.module_from_spec(spec)
+    argv = sys.argv
+    sys.argv = ["bench.py"]
+    try:
+        spec.loader.exec_module(mod)
+    finally:
+        sys.argv = argv
+    return mod
+
+
+NAMES = ["laplace", "hdiffsa", "hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "uvbke", "nh_p_grad", "p_grad_c",
+         "fvtp2d"]
+
+
+def test_dominant_kernel_summary_keys(bench):
+    traffic = bench._ncu_traffic("fvtp2d")
+    # DRAM bytes per call: at least the algorithmic 80 B/pt (the q_i, q_j, fx2, fy2 round
+    # trip between the two launches comes on top), at most a few times it
+    assert traffic is not None and 80 * 128 * 128 * 80 <= traffic <= 4 * 80 * 128 * 128 * 80
+    for key in ("fp64_pipe_active_pct", "alu_pipe_active_pct"):
+        v = bench._ncu_summary("fvtp2d", key)
+        assert v is not None and 0 < v <= 100
+
+
+def test_fp64_pipe_counts_present(bench):
+    for k in NAMES:
+        v = bench._ncu_summary(bench.PIPE_MIX_PROFILE, "fp64_instr_per_point_" + k)
+        assert v is not None and 1 <= v <= 200, k
+
+
+def test_fp64_pipe_roofline_arithmetic(bench):
+    per_kernel = {k: 0.1 for k in NAMES}
+    r = bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {"sm_mhz": 2000.0}, 100)
+    rate = bench.FP64_PIPE_PER_CLK_SM * 100 * 2000e6
+    pts = bench.NX * bench.NY * bench.NZ
+    want_k = r["kernel_instr_per_point"] * pts / rate * 1e3
+    assert r["kernel_bound_ms"] == pytest.approx(want_k, rel=1e-4)
+    assert r["kernel_frac"] == pytest.approx(want_k / 0.1, rel=1e-3)
+    want_s = sum(bench._ncu_summary(bench.PIPE_MIX_PROFILE, "fp64_instr_per_point_" + k) for k in NAMES) * pts / rate * 1e3
+    assert r["step_bound_ms"] == pytest.approx(want_s, rel=1e-4)
+    assert r["step_frac"] == pytest.approx(want_s / 1.0, rel=1e-3)
+    # no clock sample: no roof
+    assert bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {}, 100) is None
