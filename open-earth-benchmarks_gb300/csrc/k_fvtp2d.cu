@@ -433,46 +433,53 @@ oeb_status fvtp2d_tl_entry(const M3* dq_i, const M3* dq_j, const M3* dfx1, const
 
 constexpr int kW = 44;  // window along the sweep axis: outputs A..A+31 need A-5 .. A+38
 
-// gs and als are dead once the flags smt are set; tb and al take their places (46 KB a CTA
-// in FP64: four CTAs per SM)
+// Lines a CTA sweeps: 16 in FP64 (23 KB a CTA: the registers, not shared memory, then bound
+// the CTAs per SM, at five or six against four with 32 lines), 32 in FP32 (eight CTAs per SM
+// either way).
 template <class T>
+constexpr int adj_lines() {
+  return sizeof(T) == 8 ? 16 : 32;
+}
+
+// gs and als are dead once the flags smt are set; tb and al take their places
+template <class T, int LN>
 struct PpmAdjSmem {
   union {
-    T gs[32][kW];  // state values of the swept field
-    T al[32][kW];
+    T gs[LN][kW];  // state values of the swept field
+    T al[LN][kW];
   } u0;
   union {
-    T als[32][kW];  // state edge values al
-    T tb[32][kW];
+    T als[LN][kW];  // state edge values al
+    T tb[LN][kW];
   } u1;
-  T alm[32][kW];
-  T br[32][kW];
-  unsigned char smt[32][kW];
+  T alm[LN][kW];
+  T br[LN][kW];
+  unsigned char smt[LN][kW];
 };
 
 // One transposed PPM sweep along AXIS (0: i, 1: j) for outputs A..A+nout-1 on lines
-// L0..L0+nl-1 (nout, nl <= 32: a tile at the edge of its output box works on its own part of
+// L0..L0+nl-1 (nout <= 32, nl <= LN: a tile at the edge of its output box works on its own part of
 // the window and lines only; every phase's window shrinks by the 32 - nout missing outputs).
 // gst(p, l): state value at axis position p of line l (0 where the field is not defined);
 // cv(p, l): Courant number at flux point p (any value elsewhere);
 // fb(p, l): flux adjoint at p (0 off the flux points);  put(a, l, v): receives gbar(a).
-template <class T, int AXIS, class GS, class CV, class FB, class PUT>
-__device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T>& s, int A, int L0, int nout, int nl, T p1, T p2,
+template <class T, int AXIS, int LN, class GS, class CV, class FB, class PUT>
+__device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T, LN>& s, int A, int L0, int nout, int nl, T p1, T p2,
                                                   GS&& gst, CV&& cv, FB&& fb, PUT&& put) {
   const int cut = 32 - nout;
-  const bool full = cut == 0 && nl == 32;
+  const bool full = cut == 0 && nl == LN;
   auto region = [&](int w0, int w1, auto&& f) {
     const int tid = threadIdx.y * kTX + threadIdx.x;
     if (full) {  // compile-time extents
       const int W = w1 - w0;
-      for (int e = tid; e < W * 32; e += kThreads) {
+      for (int e = tid; e < W * LN; e += kThreads) {
         int w, l;
         if (AXIS == 0) {
           l = e / W;
           w = w0 + (e - l * W);
         } else {
-          w = w0 + e / 32;
-          l = e - (e / 32) * 32;
+          w = w0 + e / LN;
+          l = e - (e / LN) * LN;
         }
         f(w, l);
       }
@@ -559,14 +566,15 @@ struct fvtp2d_adj_qij_kernel {
                                              const T* __restrict__ fx1b, const T* __restrict__ fy1b, T p1, T p2,
                                              Dims d, int AXIS_Y) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
+    constexpr int LN = adj_lines<T>();
+    PpmAdjSmem<T, LN>& s = *reinterpret_cast<PpmAdjSmem<T, LN>*>(smem_raw);
     const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
     const int64_t kofs = (int64_t)blk.z * d.sk;
     if (!AXIS_Y) {
       // x sweep of fx1 on q_i: outputs i in [-3, nx+2), lines j in [0, ny)
-      const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * 32;
-      ppm_sweep_adjoint<T, 0>(
-          s, A, L0, max(0, min(32, nx + 2 - A)), max(0, min(32, ny - L0)), p1, p2,
+      const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * LN;
+      ppm_sweep_adjoint<T, 0, LN>(
+          s, A, L0, max(0, min(32, nx + 2 - A)), max(0, min(LN, ny - L0)), p1, p2,
           [&](int p, int l) { return (p >= -3 && p < nx + 2 && l < ny) ? ld(q_i + kofs + p + l * sj) : T(0); },
           [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
           [&](int p, int l) {
@@ -578,9 +586,9 @@ struct fvtp2d_adj_qij_kernel {
           });
     } else {
       // y sweep of fy1 on q_j: outputs j in [-3, ny+2), lines i in [0, nx)
-      const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * 32;
-      ppm_sweep_adjoint<T, 1>(
-          s, A, L0, max(0, min(32, ny + 2 - A)), max(0, min(32, nx - L0)), p1, p2,
+      const int A = -3 + (int)blk.x * 32, L0 = (int)blk.y * LN;
+      ppm_sweep_adjoint<T, 1, LN>(
+          s, A, L0, max(0, min(32, ny + 2 - A)), max(0, min(LN, nx - L0)), p1, p2,
           [&](int p, int l) { return (p >= -3 && p < ny + 2 && l < nx) ? ld(q_j + kofs + l + p * sj) : T(0); },
           [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
           [&](int p, int l) {
@@ -633,17 +641,18 @@ struct fvtp2d_adj_q_kernel {
                                              const T* __restrict__ qjb, const T* __restrict__ fx2b,
                                              const T* __restrict__ fy2b, T p1, T p2, Dims d, int AXIS_Y) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PpmAdjSmem<T>& s = *reinterpret_cast<PpmAdjSmem<T>*>(smem_raw);
+    constexpr int LN = adj_lines<T>();
+    PpmAdjSmem<T, LN>& s = *reinterpret_cast<PpmAdjSmem<T, LN>*>(smem_raw);
     const int nx = d.nx, ny = d.ny, sj = (int)d.sj;
     const int64_t kofs = (int64_t)blk.z * d.sk;
     auto qval = [&](int i, int j) {
       return (i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3) ? ld(q + kofs + i + j * sj) : T(0);
     };
-    const int A = -3 + (int)blk.x * 32, L0 = -3 + (int)blk.y * 32;
+    const int A = -3 + (int)blk.x * 32, L0 = -3 + (int)blk.y * LN;
     if (!AXIS_Y) {
       // x sweep of fx2 on q: flux points i in [0, nx+1), lines j in [-3, ny+2)
-      ppm_sweep_adjoint<T, 0>(
-          s, A, L0, max(0, min(32, nx + 3 - A)), max(0, min(32, ny + 3 - L0)), p1, p2,
+      ppm_sweep_adjoint<T, 0, LN>(
+          s, A, L0, max(0, min(32, nx + 3 - A)), max(0, min(LN, ny + 3 - L0)), p1, p2,
           [&](int p, int l) { return qval(p, l); },
           [&](int p, int l) { return ld(crx + kofs + p + l * sj); },
           [&](int p, int l) {
@@ -660,8 +669,8 @@ struct fvtp2d_adj_q_kernel {
           });
     } else {
       // y sweep of fy2 on q: flux points j in [0, ny+1), lines i in [-3, nx+2); adds to qb
-      ppm_sweep_adjoint<T, 1>(
-          s, A, L0, max(0, min(32, ny + 3 - A)), max(0, min(32, nx + 3 - L0)), p1, p2,
+      ppm_sweep_adjoint<T, 1, LN>(
+          s, A, L0, max(0, min(32, ny + 3 - A)), max(0, min(LN, nx + 3 - L0)), p1, p2,
           [&](int p, int l) { return qval(l, p); },
           [&](int p, int l) { return ld(cry + kofs + l + p * sj); },
           [&](int p, int l) {
@@ -710,14 +719,15 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
     *qib = base + 4 * n + org, *qjb = base + 5 * n + org, *fx2b = base + 6 * n + org, *fy2b = base + 7 * n + org;
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
   const int kb = tuned_kb(kKB);
-  const size_t ps = sizeof(PpmAdjSmem<T>);
+  constexpr int LN = adj_lines<T>();
+  const size_t ps = sizeof(PpmAdjSmem<T, LN>);
   oeb_status stt = launch<fvtp2d_q_kernel<T>>(q_grid(d, kb), sizeof(FvQSmem<T>), st,
                                               sqi, sqj, sfx2, sfy2, gq.origin, gcx.origin, gcy.origin, grx.origin,
                                               gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d, kb);
   // the x and y sweeps of the two PPM adjoints (axis flag 0 / 1)
   for (int axis = 0; axis < 2 && stt == OEB_OK; ++axis) {
     const int a = axis ? d.ny : d.nx, l = axis ? d.nx : d.ny;
-    stt = launch<fvtp2d_adj_qij_kernel<T>>(dim3((a + 5 + 31) / 32, (l + 31) / 32, d.nz), ps, st, qib, qjb, sqi, sqj,
+    stt = launch<fvtp2d_adj_qij_kernel<T>>(dim3((a + 5 + 31) / 32, (l + LN - 1) / LN, d.nz), ps, st, qib, qjb, sqi, sqj,
                                            gcx.origin, gcy.origin, gxf.origin, gyf.origin, gf1.origin, gg1.origin, p1,
                                            p2, d, axis);
   }
@@ -727,7 +737,7 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
                                           kb);
   for (int axis = 0; axis < 2 && stt == OEB_OK; ++axis) {
     const int a = axis ? d.ny : d.nx, l = axis ? d.nx : d.ny;
-    stt = launch<fvtp2d_adj_q_kernel<T>>(dim3((a + 6 + 31) / 32, (l + 6 + 31) / 32, d.nz), ps, st, gqb.origin,
+    stt = launch<fvtp2d_adj_q_kernel<T>>(dim3((a + 6 + 31) / 32, (l + 6 + LN - 1) / LN, d.nz), ps, st, gqb.origin,
                                          gq.origin, gcx.origin, gcy.origin, gar.origin, grx.origin, gry.origin, qib, qjb,
                                          fx2b, fy2b, p1, p2, d, axis);
   }
