@@ -508,6 +508,9 @@ __device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t
 
 template <class T, int ORDER>
 struct hadv_adj_terms_kernel {
+  // FP64: 80 registers instead of 94, three CTAs per SM instead of two (the hadvuv5th
+  // adjoint 4 % faster; the same bound on the hdiffsmag and fastwavesuv adjoints was slower)
+  static constexpr int kMinCtas = sizeof(T) == 8 ? 3 : 0;
   static __device__ __forceinline__ void run(const uint3& blk, HadvTerms<T> tm, const T* __restrict__ uin,
                                              const T* __restrict__ vin, const T* __restrict__ acrlat0,
                                              const T* __restrict__ acrlat1, const T* __restrict__ tgrlatda0,

@@ -66,6 +66,31 @@ __global__ void __launch_bounds__(kLaunchTX* kLaunchTY) grid_kernel(A... a) {
   Body::run(blockIdx, a...);
 }
 
+// The same for a body that declares kMinCtas > 0: the compiler keeps its registers low
+// enough for that many CTAs per SM.
+template <class Body, int N, class... A>
+__global__ void __launch_bounds__(kLaunchTX* kLaunchTY, N) grid_kernel_bound(A... a) {
+  Body::run(blockIdx, a...);
+}
+
+template <class Body, class = void>
+struct MinCtas {
+  static constexpr int value = 0;
+};
+template <class Body>
+struct MinCtas<Body, std::void_t<decltype(Body::kMinCtas)>> {
+  static constexpr int value = Body::kMinCtas;
+};
+
+// The grid kernel of Body over arguments A...
+template <class Body, class... A>
+constexpr auto grid_entry() {
+  if constexpr (MinCtas<Body>::value > 0)
+    return &grid_kernel_bound<Body, MinCtas<Body>::value, A...>;
+  else
+    return &grid_kernel<Body, A...>;
+}
+
 // One item per (member, tile); tiles[m] = {first item of member m, tiles along x, along y}.
 struct BatchTile {
   int first, gx, gy, pad;
@@ -149,7 +174,7 @@ oeb_status batch_launch(const BatchTile* tiles, int members, int total, const vo
 
 template <class Body, class... Done>
 void launch_unpacked(dim3 grid, size_t smem, cudaStream_t st, const Pack<>&, const Done&... d) {
-  grid_kernel<Body, Done...><<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(d...);
+  grid_entry<Body, Done...>()<<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(d...);
 }
 template <class Body, class H, class... R, class... Done>
 void launch_unpacked(dim3 grid, size_t smem, cudaStream_t st, const Pack<H, R...>& p, const Done&... d) {
@@ -158,7 +183,7 @@ void launch_unpacked(dim3 grid, size_t smem, cudaStream_t st, const Pack<H, R...
 
 template <class Body, class... A>
 oeb_status grid_launch_packed(const void* args, dim3 grid, size_t smem, cudaStream_t st) {
-  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_kernel<Body, A...>, (int)smem));
+  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_entry<Body, A...>(), (int)smem));
   launch_unpacked<Body>(grid, smem, st, *static_cast<const Pack<A...>*>(args));
   return after_launch();
 }
@@ -248,8 +273,8 @@ oeb_status launch_as(dim3 grid, size_t smem, cudaStream_t st, A... a) {
     r->records.push_back(std::move(rec));
     return OEB_OK;
   }
-  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_kernel<Body, A...>, (int)smem));
-  grid_kernel<Body, A...><<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(a...);
+  if (smem > 48 * 1024) OEB_TRY(ensure_dyn_smem((const void*)grid_entry<Body, A...>(), (int)smem));
+  grid_entry<Body, A...>()<<<grid, dim3(kLaunchTX, kLaunchTY), smem, st>>>(a...);
   return after_launch();
 }
 
