@@ -603,6 +603,17 @@ struct fvtp2d_adj_qij_kernel {
 };
 
 // Pass 2: fy2b on [-3,N+2) x [0,N+1) and fx2b on [0,N+1) x [-3,N+2).
+// fy2b(i,j) = g + yfx (ry(i,j) - ry(i,j-1)) with ry = q_ib / ra_y on rows [0, N) (0 elsewhere),
+// fx2b(i,j) = g + xfx (rx(i,j) - rx(i-1,j)) with rx = q_jb / ra_x on columns [0, N): each
+// quotient is read by two neighbouring points, so a CTA divides once per cell into shared
+// memory (ry over its 33 rows j0-1.., rx over its 33 columns i0-1..) and forms both fluxes
+// from there.  Tile origin (i0, j0) = (-3 + 32 bx, -3 + 32 by).
+template <class T>
+struct AdjF2Smem {
+  T ry[33][32];  // (i0+a, j0-1+b)
+  T rx[32][33];  // (i0-1+a, j0+b)
+};
+
 template <class T>
 struct fvtp2d_adj_f2_kernel {
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ fx2b, T* __restrict__ fy2b,
@@ -610,23 +621,43 @@ struct fvtp2d_adj_f2_kernel {
                                              const T* __restrict__ xfx, const T* __restrict__ yfx,
                                              const T* __restrict__ ra_x, const T* __restrict__ ra_y,
                                              const T* __restrict__ fx1b, const T* __restrict__ fy1b, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    AdjF2Smem<T>& s = *reinterpret_cast<AdjF2Smem<T>*>(smem_raw);
     const int nx = d.nx, ny = d.ny;
     const int64_t sj = d.sj;
-    for_box<RowUnroll<T>::value>(blk, d, -3, -3, nx + 5, ny + 5, kb, [&](int64_t o, int i, int j) {
-      const bool interior = i >= 0 && i < nx && j >= 0 && j < ny;
-      if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {
-        T g = interior ? (T(0.5) * ld(yfx + o)) * ld(fy1b + o) : T(0);
-        const T a = (j < ny) ? qib[o] / ld(ra_y + o) : T(0);
-        const T b = (j >= 1) ? qib[o - sj] / ld(ra_y + o - sj) : T(0);
-        fy2b[o] = g + ld(yfx + o) * (a - b);
-      }
-      if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {
-        T g = interior ? (T(0.5) * ld(xfx + o)) * ld(fx1b + o) : T(0);
-        const T a = (i < nx) ? qjb[o] / ld(ra_x + o) : T(0);
-        const T b = (i >= 1) ? qjb[o - 1] / ld(ra_x + o - 1) : T(0);
-        fx2b[o] = g + ld(xfx + o) * (a - b);
-      }
-    });
+    const int i0 = -3 + (int)blk.x * kT, j0 = -3 + (int)blk.y * kT;
+    // outputs of this tile in the box [-3, nx+2) x [-3, ny+2)
+    const int vx = max(0, min(kT, nx + 2 - i0)), vy = max(0, min(kT, ny + 2 - j0));
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region_lim<32, 33>(vx, vy + 1, [&](int a, int b) {
+        const int i = i0 + a, r = j0 - 1 + b;
+        const int64_t o = kofs + i + r * sj;
+        s.ry[b][a] = (r >= 0 && r < ny && i < nx + 2) ? qib[o] / ld(ra_y + o) : T(0);
+      });
+      for_region_lim<33, 32>(vx + 1, vy, [&](int a, int b) {
+        const int c = i0 - 1 + a, j = j0 + b;
+        const int64_t o = kofs + c + j * sj;
+        s.rx[b][a] = (c >= 0 && c < nx && j < ny + 2) ? qjb[o] / ld(ra_x + o) : T(0);
+      });
+      __syncthreads();
+      for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        const int64_t o = kofs + i + j * sj;
+        const bool interior = i >= 0 && i < nx && j >= 0 && j < ny;
+        if (j >= 0 && j < ny + 1) {
+          T g = interior ? (T(0.5) * ld(yfx + o)) * ld(fy1b + o) : T(0);
+          fy2b[o] = g + ld(yfx + o) * (s.ry[b + 1][a] - s.ry[b][a]);
+        }
+        if (i >= 0 && i < nx + 1) {
+          T g = interior ? (T(0.5) * ld(xfx + o)) * ld(fx1b + o) : T(0);
+          fx2b[o] = g + ld(xfx + o) * (s.rx[b][a + 1] - s.rx[b][a]);
+        }
+      });
+      __syncthreads();
+    }
   }
 };
 
@@ -732,7 +763,8 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
                                            p2, d, axis);
   }
   if (stt == OEB_OK)
-    stt = launch<fvtp2d_adj_f2_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), 0, st, fx2b, fy2b, qib,
+    stt = launch<fvtp2d_adj_f2_kernel<T>>(tile_grid(d.nx + 5, d.ny + 5, d.nz, kT, kT, kb), sizeof(AdjF2Smem<T>), st,
+                                          fx2b, fy2b, qib,
                                           qjb, gxf.origin, gyf.origin, grx.origin, gry.origin, gf1.origin, gg1.origin, d,
                                           kb);
   for (int axis = 0; axis < 2 && stt == OEB_OK; ++axis) {
