@@ -209,6 +209,51 @@ oeb_status fastwavesuv_tl_entry(const M3* duout, const M3* dvout, const M3* uin,
 // with every coefficient zero off the interior.  ppuvb covers i in [0,N], j in [0,N],
 // k in [-1,N_z] (the reach of ppuv).  One CTA marches a 32 x 32 tile of that box through a
 // chunk of k-levels, keeping cb at three levels in registers.
+// The adjoint's coefficients at every interior point, once (pass 1): au = -dt qx uoutb and
+// au gx, av = -dt qy voutb and av gy (each division once; the g-weighted term is 0 where a
+// is).  The march (pass 2) reads them at the kb + 2 levels of its k-block instead of
+// recomputing them there.
+template <class T>
+struct FastwavesAdjTerms {
+  T *au, *ax, *av, *ay;  // in the layout of the state fields, 0 outside the interior unread
+};
+
+template <class T>
+struct fastwavesuv_adj_terms_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, FastwavesAdjTerms<T> tm, const T* __restrict__ hhl,
+                                             const T* __restrict__ rho, const T* __restrict__ fx, int64_t s1d,
+                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T ed2, T dt,
+                                             Dims d, int kb) {
+    const int64_t sk = d.sk, sj = d.sj;
+    for_box<RowUnroll<T>::value>(blk, d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
+      {
+        const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
+        const T a = -(dt * qx) * ld(uoutb + o);
+        T ag = T(0);
+        if (a != T(0)) {
+          const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
+          const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
+          ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+        }
+        tm.au[o] = a;
+        tm.ax[o] = ag;
+      }
+      {
+        const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
+        const T a = -(dt * qy) * ld(voutb + o);
+        T ag = T(0);
+        if (a != T(0)) {
+          const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
+          const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
+          ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+        }
+        tm.av[o] = a;
+        tm.ay[o] = ag;
+      }
+    });
+  }
+};
+
 template <class T>
 struct FastwavesAdjSmem {
   T ax[kT][kR];  // au(i0-1+a, j0+b) gx, then au itself in the second half
@@ -221,10 +266,9 @@ template <class T>
 struct fastwavesuv_adj_kernel {
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
                                              T* __restrict__ utensb, T* __restrict__ vtensb, T* __restrict__ ppuvb,
-                                             const T* __restrict__ wgtfac, const T* __restrict__ hhl,
-                                             const T* __restrict__ rho, const T* __restrict__ fx, int64_t s1d,
-                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T ed2, T dt,
-                                             Dims d, int kb) {
+                                             const T* __restrict__ wgtfac, FastwavesAdjTerms<T> tm,
+                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T dt, Dims d,
+                                             int kb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FastwavesAdjSmem<T>& s = *reinterpret_cast<FastwavesAdjSmem<T>*>(smem_raw);
     const int i0 = blk.x * kT, j0 = blk.y * kT;
@@ -234,45 +278,40 @@ struct fastwavesuv_adj_kernel {
     const int Ks = -1 + (int)blk.z * kb, Ke = min(Ks + kb, d.nz + 1);
     constexpr int kPts = kT * kT / kThreads;
     T cm2[kPts], cm1[kPts], dir[kPts];  // cb(L-2), cb(L-1), direct terms of level L-1
+    // outputs of this tile in the box [0, nx] x [0, ny]: a tile at its far edge holds one
+    // column or row of them, and computes au / av only where those outputs read them (the
+    // march below reads no other cell for an output it writes)
+    const int vx = min(kT, d.nx + 1 - i0), vy = min(kT, d.ny + 1 - j0);
   #pragma unroll
     for (int t = 0; t < kPts; ++t) cm2[t] = cm1[t] = dir[t] = T(0);
     const int tid = threadIdx.y * kTX + threadIdx.x;
-    // adjoint of ppgu (au) and of ppgv (av) at an interior point, and the same times g
-    // (each division once: a = -dt q ybar, then a g)
+    // adjoint of ppgu (au) and of ppgv (av) at an interior point, and the same times g (pass 1)
     auto au_at = [&](int i, int j, int k, T* ag) -> T {
-      *ag = T(0);
-      if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
-      const int64_t o = (int64_t)k * sk + i + j * sj;
-      const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
-      const T a = -(dt * qx) * ld(uoutb + o);
-      if (a != T(0)) {
-        const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
-        const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
-        *ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+      if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) {
+        *ag = T(0);
+        return T(0);
       }
-      return a;
+      const int64_t o = (int64_t)k * sk + i + j * sj;
+      *ag = ld(tm.ax + o);
+      return ld(tm.au + o);
     };
     auto av_at = [&](int i, int j, int k, T* ag) -> T {
-      *ag = T(0);
-      if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) return T(0);
-      const int64_t o = (int64_t)k * sk + i + j * sj;
-      const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
-      const T a = -(dt * qy) * ld(voutb + o);
-      if (a != T(0)) {
-        const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
-        const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
-        *ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+      if (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) {
+        *ag = T(0);
+        return T(0);
       }
-      return a;
+      const int64_t o = (int64_t)k * sk + i + j * sj;
+      *ag = ld(tm.ay + o);
+      return ld(tm.av + o);
     };
   #pragma unroll 1
     for (int L = Ks - 1; L <= Ke; ++L) {
       // au, av and their g-weighted versions at level L over the tile plus the low apron
-      for_region<kR, kT>([&](int a, int b) {
+      for_region_lim<kR, kT>(vx + 1, vy, [&](int a, int b) {
         const int i = i0 - 1 + a, j = j0 + b;
         s.au[b][a] = au_at(i, j, L, &s.ax[b][a]);
       });
-      for_region<kT, kR>([&](int a, int b) {
+      for_region_lim<kT, kR>(vx, vy + 1, [&](int a, int b) {
         const int i = i0 + a, j = j0 - 1 + b;
         s.av[b][a] = av_at(i, j, L, &s.ay[b][a]);
       });
@@ -343,13 +382,29 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   OEB_RETURN_IF_VALIDATING();
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gw.sj, gw.sk};
   const T ed2 = T(2.0) * edadlat;
-  // the adjoint carries a three-level window of ppgc/hhl terms up the column: longer
-  // k-blocks reuse it (4 levels: 0.68 ms against 0.89 ms for 1 at 128 x 128 x 80, FP64)
+  cudaStream_t st = (cudaStream_t)stream;
+  // scratch for the four coefficient fields, in uoutb's layout
+  const T* start = (uoutb->allocated && uoutb->allocated <= uoutb->aligned) ? uoutb->allocated : uoutb->aligned;
+  const int64_t last = (uoutb->sizes[0] - 1) * uoutb->strides[0] + (uoutb->sizes[1] - 1) * uoutb->strides[1] +
+                       (uoutb->sizes[2] - 1) * uoutb->strides[2];
+  const int64_t n = (int64_t)(uoutb->aligned - start) + last + 1;
+  const int64_t org = (int64_t)(uoutb->aligned - start) + uoutb->offset;
+  void* buf = nullptr;
+  OEB_TRY(scratch_alloc(&buf, (size_t)n * 4 * sizeof(T), st));
+  T* base = static_cast<T*>(buf);
+  const FastwavesAdjTerms<T> tm{base + org, base + n + org, base + 2 * n + org, base + 3 * n + org};
+  oeb_status stt = launch<fastwavesuv_adj_terms_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, 1), 0, st, tm,
+                                                           gh.origin, gr.origin, lfx.origin, lfx.s, guo.origin,
+                                                           gvo.origin, ed2, dt, d, 1);
+  // the march carries a three-level window of ppgc terms up the column; a k-block of kb
+  // levels reads the coefficients at kb + 2
   const int kb = tuned_kb(adj_kb<T>());
-  return launch<fastwavesuv_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
-                                           sizeof(FastwavesAdjSmem<T>), (cudaStream_t)stream, gub.origin, gvb.origin,
-                                           gutb.origin, gvtb.origin, gpb.origin, gw.origin, gh.origin, gr.origin,
-                                           lfx.origin, lfx.s, guo.origin, gvo.origin, ed2, dt, d, kb);
+  if (stt == OEB_OK)
+    stt = launch<fastwavesuv_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
+                                            sizeof(FastwavesAdjSmem<T>), st, gub.origin, gvb.origin, gutb.origin,
+                                            gvtb.origin, gpb.origin, gw.origin, tm, guo.origin, gvo.origin, dt, d, kb);
+  scratch_free(buf, st);
+  return stt;
 }
 
 }  // namespace
