@@ -118,10 +118,11 @@ struct fastwavesuv_kernel {
 };
 
 constexpr int kKB = 1;     // k-levels per CTA by default (the most CTAs hide latency best)
-// the adjoint's k-levels per CTA (measured at 128 x 128 x 80: FP64 best at 4, FP32 at 2)
+// the adjoint march's k-levels per CTA (measured at 128 x 128 x 80: FP64 best at 3, FP32 at
+// 2; a block of kb levels reads the coefficients of kb + 2)
 template <class T>
 constexpr int adj_kb() {
-  return sizeof(T) == 4 ? 2 : 4;
+  return sizeof(T) == 4 ? 2 : 3;
 }
 
 template <class T, class M3, class M1>
