@@ -339,6 +339,15 @@ __device__ __forceinline__ T smag_S(const T* __restrict__ u, const T* __restrict
   return c1 * (ld(u + o + sj) - ld(u + o)) + c2 * (ld(v + o + 1) - ld(v + o));
 }
 
+// T^2 and S^2 of a tile's cells, each computed once (every point reads three of each):
+//   tsq : 33 x 33, (i0+a,   j0+b)     T_s^2
+//   ssq : 33 x 33, (i0-1+a, j0-1+b)   S_uv^2
+template <class T>
+struct SmagAdjSmem {
+  T tsq[33][33];
+  T ssq[33][33];
+};
+
 template <class T>
 struct hdiffsmag_adj_terms_kernel {
   static __device__ __forceinline__ void run(const uint3& blk, SmagTerms<T> tm, const T* __restrict__ uin,
@@ -348,34 +357,54 @@ struct hdiffsmag_adj_terms_kernel {
                                              const T* __restrict__ acrlat0, int64_t s1d, const T* __restrict__ uoutb,
                                              const T* __restrict__ voutb, T eddlat, T eddlon, T tau_smag,
                                              T weight_smag, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmagAdjSmem<T>& s = *reinterpret_cast<SmagAdjSmem<T>*>(smem_raw);
     constexpr T rr = earth_radius_recip<T>();
     const T c1 = eddlat * rr;
     const int64_t sj = d.sj;
-    for_box<RowUnroll<T>::value>(blk, d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
-      const T c2m = ld(acrlat0 + (int64_t)(j - 1) * s1d) * eddlon, c2 = ld(acrlat0 + (int64_t)j * s1d) * eddlon,
-              c2p = ld(acrlat0 + (int64_t)(j + 1) * s1d) * eddlon;
-      const T t0 = smag_T(uin, vin, o, sj, c1, c2), ti = smag_T(uin, vin, o + 1, sj, c1, c2),
-              tj = smag_T(uin, vin, o + sj, sj, c1, c2p);
-      const T s0 = smag_S(uin, vin, o, sj, c1, c2), sjm = smag_S(uin, vin, o - sj, sj, c1, c2m),
-              sim = smag_S(uin, vin, o - 1, sj, c1, c2);
-      const T hdw = weight_smag * ld(mask + o);
-      const T xu = T(0.5) * (ti * ti + t0 * t0) + T(0.5) * (sjm * sjm + s0 * s0);
-      const T xv = T(0.5) * (tj * tj + t0 * t0) + T(0.5) * (sim * sim + s0 * s0);
-      const T ru = Prec<T>::sqrt_(xu), rv = Prec<T>::sqrt_(xv);
-      const T smu = tau_smag * ru - hdw, smv = tau_smag * rv - hdw;
-      const T su = clamp_smag(smu), sv = clamp_smag(smv);
-      const int64_t jo = (int64_t)j * s1d;
-      const T u0 = ld(uin + o), v0 = ld(vin + o);
-      const T lapu = (ld(uin + o + 1) + ld(uin + o - 1) - T(2) * u0) + ld(crlato + jo) * (ld(uin + o + sj) - u0) +
-                     ld(crlatu + jo) * (ld(uin + o - sj) - u0);
-      const T lapv = (ld(vin + o + 1) + ld(vin + o - 1) - T(2) * v0) + ld(crlavo + jo) * (ld(vin + o + sj) - v0) +
-                     ld(crlavu + jo) * (ld(vin + o - sj) - v0);
-      const T yu = ld(uoutb + o), yv = ld(voutb + o);
-      tm.lu[o] = su * yu;
-      tm.lv[o] = sv * yv;
-      tm.xu[o] = (smu > T(0) && smu < T(0.5)) ? (lapu * yu) * (tau_smag / (T(2) * ru)) : T(0);
-      tm.xv[o] = (smv > T(0) && smv < T(0.5)) ? (lapv * yv) * (tau_smag / (T(2) * rv)) : T(0);
-    });
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int vx = max(0, min(kT, d.nx - i0)), vy = max(0, min(kT, d.ny - j0));
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      // T at (i, j) for i in [i0, i0+vx], j in [j0, j0+vy]; S at (i, j) for i in [i0-1, i0+vx),
+      // j in [j0-1, j0+vy): every cell the tile's points read
+      for_region_lim<33, 33>(vx + 1, vy + 1, [&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        const T t = smag_T(uin, vin, kofs + i + j * sj, sj, c1, ld(acrlat0 + (int64_t)j * s1d) * eddlon);
+        s.tsq[b][a] = t * t;
+      });
+      for_region_lim<33, 33>(vx + 1, vy + 1, [&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        const T v = smag_S(uin, vin, kofs + i + j * sj, sj, c1, ld(acrlat0 + (int64_t)j * s1d) * eddlon);
+        s.ssq[b][a] = v * v;
+      });
+      __syncthreads();
+      for_region_lim<32, 32>(vx, vy, [&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        const int64_t o = kofs + i + j * sj;
+        const T hdw = weight_smag * ld(mask + o);
+        // T(i+1,j)^2 + T(i,j)^2, S(i,j-1)^2 + S(i,j)^2; T(i,j+1)^2 + T(i,j)^2, S(i-1,j)^2 + S(i,j)^2
+        const T xu = T(0.5) * (s.tsq[b][a + 1] + s.tsq[b][a]) + T(0.5) * (s.ssq[b][a + 1] + s.ssq[b + 1][a + 1]);
+        const T xv = T(0.5) * (s.tsq[b + 1][a] + s.tsq[b][a]) + T(0.5) * (s.ssq[b + 1][a] + s.ssq[b + 1][a + 1]);
+        const T ru = Prec<T>::sqrt_(xu), rv = Prec<T>::sqrt_(xv);
+        const T smu = tau_smag * ru - hdw, smv = tau_smag * rv - hdw;
+        const T su = clamp_smag(smu), sv = clamp_smag(smv);
+        const int64_t jo = (int64_t)j * s1d;
+        const T u0 = ld(uin + o), v0 = ld(vin + o);
+        const T lapu = (ld(uin + o + 1) + ld(uin + o - 1) - T(2) * u0) + ld(crlato + jo) * (ld(uin + o + sj) - u0) +
+                       ld(crlatu + jo) * (ld(uin + o - sj) - u0);
+        const T lapv = (ld(vin + o + 1) + ld(vin + o - 1) - T(2) * v0) + ld(crlavo + jo) * (ld(vin + o + sj) - v0) +
+                       ld(crlavu + jo) * (ld(vin + o - sj) - v0);
+        const T yu = ld(uoutb + o), yv = ld(voutb + o);
+        tm.lu[o] = su * yu;
+        tm.lv[o] = sv * yv;
+        tm.xu[o] = (smu > T(0) && smu < T(0.5)) ? (lapu * yu) * (tau_smag / (T(2) * ru)) : T(0);
+        tm.xv[o] = (smv > T(0) && smv < T(0.5)) ? (lapv * yv) * (tau_smag / (T(2) * rv)) : T(0);
+      });
+      __syncthreads();
+    }
   }
 };
 
@@ -490,7 +519,7 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
   const int64_t s1d = acrlat0->strides[0];
   const int kb = tuned_kb(kKB);
   oeb_status stt = launch<hdiffsmag_adj_terms_kernel<T>>(
-      tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), 0, st, tm, gui.origin, (const T*)vin->aligned + vin->offset,
+      tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(SmagAdjSmem<T>), st, tm, gui.origin, (const T*)vin->aligned + vin->offset,
       (const T*)mask->aligned + mask->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d,
       guo.origin, (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kb);
   if (stt == OEB_OK)
@@ -581,7 +610,7 @@ oeb_status hdiffsmag_adj_noalloc_entry(const oeb_memref3d_f64* uinb, const oeb_m
   const int64_t s1d = acrlat0->strides[0];
   cudaStream_t st = (cudaStream_t)stream;
   OEB_TRY(launch<hdiffsmag_adj_terms_kernel<T>>(
-      tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), 0, st, tm, gui.origin, (const T*)vin->aligned + vin->offset,
+      tile_grid(d.nx, d.ny, d.nz, kT, kT, kKB), sizeof(SmagAdjSmem<T>), st, tm, gui.origin, (const T*)vin->aligned + vin->offset,
       (const T*)mask->aligned + mask->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0), s1d,
       guo.origin, (const T*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag, weight_smag, d, kKB));
   OEB_TRY(launch<hdiffsmag_adj_ts_kernel<T>>(tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kKB), 0, st, tm, gui.origin,
