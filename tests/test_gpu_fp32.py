@@ -33,7 +33,8 @@ FLIP_KERNELS = {"hdiffsa"}          # limiter flips at input-resolution ties
 FLIP_FRACTION = 1e-4                # at most 1 point in 10^4 above the bound
 KERNELS = ("laplace", "hdiffsa", "hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "uvbke", "nh_p_grad",
            "p_grad_c", "fvtp2d")
-REPORT = Path(os.environ.get("OEB_FP32_REPORT", "gpurun_out/fp32_errors.json"))
+# the measured errors are also written, as JSON, to the file OEB_FP32_REPORT names (if set)
+REPORT = Path(os.environ["OEB_FP32_REPORT"]) if os.environ.get("OEB_FP32_REPORT") else None
 _results = {}
 
 
@@ -91,8 +92,9 @@ def test_fp32_error_vs_fp64_oracle(pkg, fields, orc, cuda, name, case):
     workload, nx, ny, nz, seed = case
     res = _run(pkg, fields, orc, cuda, name, nx, ny, nz, seed, workload)
     _results["%s/%s_%dx%dx%d" % (name, workload, nx, ny, nz)] = res
-    REPORT.parent.mkdir(parents=True, exist_ok=True)
-    REPORT.write_text(json.dumps(_results, indent=1, sort_keys=True))
+    if REPORT is not None:
+        REPORT.parent.mkdir(parents=True, exist_ok=True)
+        REPORT.write_text(json.dumps(_results, indent=1, sort_keys=True))
     for out, r in res.items():
         what = "%s.%s %s" % (name, out, case)
         if name in FLIP_KERNELS:
