@@ -67,6 +67,23 @@ def _dist_env():
     return rank, world, local
 
 
+def _max_over_ranks(torch, ms, dev):
+    """The largest of every rank's `ms` (every rank calls it; without a process group, `ms`)."""
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([float(ms)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _replica_gpts(world, points_per_step, steps, ms_total):
+    """Whole-job GPts/s: each rank runs the step on its own GPU and its own inputs (replicas,
+    no collective in the data path), so the job updates world x points_per_step a step, over
+    the slowest rank's time."""
+    return world * points_per_step * steps / (ms_total * 1e-3) / 1e9
+
+
 class ClockSampler:
     """SM clocks and clock-event reasons sampled over the timed region.
 
@@ -349,15 +366,14 @@ def run_ours(args):
     clocks = ClockSampler(local)
     ms_total, launches, graph_kernels = _time_concurrent(pkg, torch, sets, names, args.steps, args.warmup, dom, dev,
                                                          clocks, ms_each=per_kernel)
+    ms_total = _max_over_ranks(torch, ms_total, dev)
+    ms_seq = _max_over_ranks(torch, ms_seq, dev)
     if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
         torch.distributed.barrier()
     ms_step = ms_total / args.steps
     clock_summary = clocks.summary()
     pts_step = len(names) * NX * NY * NZ
-    value = world * pts_step * args.steps / (ms_total * 1e-3) / 1e9
+    value = _replica_gpts(world, pts_step, args.steps, ms_total)
     total_k = sum(per_kernel.values())
     dom_k = max(per_kernel, key=per_kernel.get)
     peak, peak_src = _measured_peak()
@@ -464,7 +480,7 @@ def run_ours(args):
         "kernel_share": {k: round(v / total_k, 4) for k, v in per_kernel.items()},
         "clocks": clock_summary,
         "gpu_launches": int(launches),
-        "sequential": {"value": round(world * pts_step * args.steps / (ms_seq * 1e-3) / 1e9, 4),
+        "sequential": {"value": round(_replica_gpts(world, pts_step, args.steps, ms_seq), 4),
                        "ms_per_step": round(ms_seq / args.steps, 4), "gpu_launches": int(launches_seq),
                        "issue": "the ten stencils one after another on one stream, a CUDA event pair around each "
                                 "(per_kernel_ms, kernel_share and roofline come from this pass)"},
