@@ -694,6 +694,25 @@ typedef struct oeb_batch_member {
 OEB_API oeb_status oeb_batch_plan_create(const oeb_batch_member* members, int count, int modes, oeb_batch_plan** out);
 OEB_API oeb_status oeb_batch_run(oeb_batch_plan* plan, void* stream);
 OEB_API oeb_status oeb_batch_autotune(oeb_batch_plan* plan, void* stream);
+/* Tuning records (no counterpart in the reference: its drivers take no tuning).  A record
+ * keeps the autotuner's choices, so that a later process can apply them to a plan over the
+ * same ensemble without timing anything again.  It holds two ints per batched launch, in
+ * run order: kb (0 = each kernel's default, or 1, 2, 4, 8) and the launch form (0: one
+ * persistent wave, sized on the device it is applied on; 1: one CTA per tile; 2: one
+ * ordinary launch per member).
+ * oeb_batch_tuning_get: *count = the plan's launches; with record != NULL it also writes
+ *   2 * count ints there (OEB_ERR_TOO_LARGE if capacity, in launches, is below count).
+ * oeb_batch_tuning_apply: OEB_ERR_ARGUMENT if count differs from the plan's launches or a
+ *   kb or form is not one of the values above.  It records the step again for each kb
+ *   named, waits for the device to go idle, then swaps in the new tables.  On any error the
+ *   plan is unchanged.  Results do not depend on the record.  Do not call it during a
+ *   stream capture.
+ * oeb_batch_signature: a 64-bit hash of the modes, each member's element size and domain
+ *   (in order) and the launch count.  A record saved with one signature fits any plan
+ *   with the same signature. */
+OEB_API oeb_status oeb_batch_tuning_get(const oeb_batch_plan* plan, int* record, int capacity, int* count);
+OEB_API oeb_status oeb_batch_tuning_apply(oeb_batch_plan* plan, const int* record, int count);
+OEB_API oeb_status oeb_batch_signature(const oeb_batch_plan* plan, uint64_t* out);
 /* Kernel launches per run (one batched launch per recorded position and precision, or one
  * launch per member where the autotuner chose per-member launches), and interior points
  * per run (all members). */

@@ -18,11 +18,12 @@ i/j halo of at least 8 and a k halo of at least 1.
 from __future__ import annotations
 
 import ctypes
-from typing import Dict, Optional
+import json
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
-from .abi import check, entry, load_library
+from .abi import OebError, check, entry, load_library
 from .storage import Domain, Memref1d, Memref3d, Storage
 
 FORWARD, TL, ADJOINT = 1, 2, 4
@@ -224,6 +225,54 @@ class BatchPlan:
 
     def autotune(self, stream=None):
         check(entry("oeb_batch_autotune")(self._plan, ctypes.c_void_p(_stream(stream))), "oeb_batch_autotune")
+
+    TUNING_FORMAT = "oeb-batch-tuning/1"
+
+    @property
+    def signature(self) -> int:
+        """64-bit hash of the modes, the members' element sizes and domains, and the launch
+        count (oeb_batch_signature): a tuning record fits every plan with the same one."""
+        out = ctypes.c_uint64()
+        check(entry("oeb_batch_signature")(self._plan, ctypes.byref(out)), "oeb_batch_signature")
+        return int(out.value)
+
+    def tuning(self) -> List[Tuple[int, int]]:
+        """The plan's launch choices, (kb, form) per batched launch in run order
+        (oeb_batch_tuning_get); form 0 is one persistent wave, 1 one CTA per tile, 2 one
+        ordinary launch per member."""
+        n = ctypes.c_int()
+        check(entry("oeb_batch_tuning_get")(self._plan, None, ctypes.c_int(0), ctypes.byref(n)),
+              "oeb_batch_tuning_get")
+        rec = (ctypes.c_int * (2 * max(n.value, 1)))()
+        check(entry("oeb_batch_tuning_get")(self._plan, rec, n, ctypes.byref(n)), "oeb_batch_tuning_get")
+        return [(rec[2 * i], rec[2 * i + 1]) for i in range(n.value)]
+
+    def apply_tuning(self, choices) -> None:
+        """Makes the plan launch as `choices` says (oeb_batch_tuning_apply): as tuning()
+        returns them, here or in another process, for a plan with the same signature."""
+        flat = [int(v) for kb_form in choices for v in kb_form]
+        rec = (ctypes.c_int * max(len(flat), 1))(*flat)
+        check(entry("oeb_batch_tuning_apply")(self._plan, rec, ctypes.c_int(len(flat) // 2)),
+              "oeb_batch_tuning_apply")
+
+    def save_tuning(self, path) -> None:
+        """Writes the plan's choices as a JSON tuning record, keyed by its signature."""
+        with open(path, "w") as f:
+            json.dump({"format": self.TUNING_FORMAT, "signature": "%016x" % self.signature,
+                       "choices": [list(c) for c in self.tuning()]}, f)
+
+    def load_tuning(self, path) -> None:
+        """Applies a record written by save_tuning.  Raises OebError, leaving the plan as it
+        was, if the record is of another format or was saved for a plan with another
+        signature (other members, domains, precisions or modes)."""
+        with open(path) as f:
+            rec = json.load(f)
+        if rec.get("format") != self.TUNING_FORMAT:
+            raise OebError("%s: not a batch tuning record (format %r)" % (path, rec.get("format")))
+        if rec.get("signature") != "%016x" % self.signature:
+            raise OebError("%s: saved for another ensemble (signature %s, this plan %016x)"
+                           % (path, rec.get("signature"), self.signature))
+        self.apply_tuning(rec["choices"])
 
     @property
     def launches(self) -> int:

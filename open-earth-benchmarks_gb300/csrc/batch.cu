@@ -438,6 +438,105 @@ oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
   return OEB_OK;
 }
 
+// ---- tuning records ------------------------------------------------------------------
+// A record keeps the autotuner's choices so that a later process can reuse them without
+// timing anything: two ints a slot, in run order -- the slot's kb, and its launch form
+// (kFormWave: one persistent wave; kFormPerTile: one CTA per tile; kFormPerMember: one
+// ordinary launch per member).  The wave's CTA count is taken from the device the record is
+// applied on.  kb is one of the values a plan records with: 0 (every kernel's own default,
+// as at creation) or 1, 2, 4, 8 (the autotuner's candidates).
+constexpr int kFormWave = 0, kFormPerTile = 1, kFormPerMember = 2;
+
+int wave_ctas(const oeb_batch_plan* p, const Slot& sl) { return std::min(sl.total, sl.occupancy * p->sms); }
+
+bool recorded_kb(int kb) { return kb == 0 || kb == 1 || kb == 2 || kb == 4 || kb == 8; }
+
+// FNV-1a over what fixes the plan's launch sequence: modes, then every member's element
+// size and domain in order, then the slot count.
+uint64_t signature(const oeb_batch_plan* p) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](int64_t v) {
+    for (int b = 0; b < 8; ++b) {
+      h ^= (uint64_t)((v >> (8 * b)) & 0xff);
+      h *= 1099511628211ull;
+    }
+  };
+  mix(p->modes);
+  mix((int64_t)p->members.size());
+  for (const Member& m : p->members) {
+    mix(m.elem);
+    mix(m.dom.nx);
+    mix(m.dom.ny);
+    mix(m.dom.nz);
+  }
+  mix((int64_t)p->slots.size());
+  return h;
+}
+
+oeb_status tuning_get(const oeb_batch_plan* p, int* rec, int capacity, int* count) {
+  if (!count) return OEB_ERR_NULL;
+  *count = (int)p->slots.size();
+  if (!rec) return OEB_OK;
+  if (capacity < *count) return OEB_ERR_TOO_LARGE;
+  for (size_t i = 0; i < p->slots.size(); ++i) {
+    const Slot& sl = p->slots[i];
+    rec[2 * i] = sl.kb;
+    rec[2 * i + 1] = sl.per_member ? kFormPerMember : (sl.ctas == wave_ctas(p, sl) ? kFormWave : kFormPerTile);
+  }
+  return OEB_OK;
+}
+
+// Records the step with every kb the record names, builds their slots into one new table
+// buffer, and only then replaces the plan's tables and slots: on any error the plan is left
+// as it was.
+oeb_status tuning_apply(oeb_batch_plan* p, const int* rec, int count) {
+  if (!rec) return OEB_ERR_NULL;
+  if (count != (int)p->slots.size()) return OEB_ERR_ARGUMENT;
+  std::vector<int> kbs;
+  for (int i = 0; i < count; ++i) {
+    const int kb = rec[2 * i], form = rec[2 * i + 1];
+    if (!recorded_kb(kb) || form < kFormWave || form > kFormPerMember) return OEB_ERR_ARGUMENT;
+    if (std::find(kbs.begin(), kbs.end(), kb) == kbs.end()) kbs.push_back(kb);
+  }
+  std::vector<std::vector<Slot>> cand;
+  std::vector<char> host;
+  for (int kb : kbs) {
+    std::vector<std::vector<std::vector<LaunchRecord>>> seq;
+    OEB_TRY(record_all(p, kb, &seq));
+    std::vector<Slot> slots;
+    OEB_TRY(build_slots(p, seq, kb, &slots, &host, 0));
+    if (slots.size() != p->slots.size()) return OEB_ERR_UNSUPPORTED;
+    cand.push_back(std::move(slots));
+  }
+  std::vector<Slot> next(count);
+  for (int i = 0; i < count; ++i) {
+    const size_t c = (size_t)(std::find(kbs.begin(), kbs.end(), rec[2 * i]) - kbs.begin());
+    Slot sl = cand[c][i];
+    const int form = rec[2 * i + 1];
+    sl.per_member = form == kFormPerMember;
+    sl.ctas = form == kFormPerTile ? sl.total : wave_ctas(p, sl);
+    next[i] = std::move(sl);
+  }
+  char* tables = nullptr;
+  const cudaError_t e = cudaMalloc(&tables, std::max<size_t>(host.size(), 256));
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  const cudaError_t c = cudaMemcpy(tables, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (c != cudaSuccess) {
+    cudaFree(tables);
+    return cuda_fail(c);
+  }
+  // the old tables may still be read by a run in flight on the plan's streams
+  OEB_CUDA_TRY(cudaDeviceSynchronize());
+  if (p->tables) cudaFree(p->tables);
+  p->tables = tables;
+  p->table_bytes = host.size();
+  p->slots = std::move(next);
+  return OEB_OK;
+}
+
 }  // namespace
 }  // namespace oeb
 
@@ -456,6 +555,22 @@ extern "C" oeb_status oeb_batch_run(oeb_batch_plan* p, void* stream) {
 extern "C" oeb_status oeb_batch_autotune(oeb_batch_plan* p, void* stream) {
   if (!p) return OEB_ERR_NULL;
   return autotune(p, (cudaStream_t)stream);
+}
+
+extern "C" oeb_status oeb_batch_signature(const oeb_batch_plan* p, uint64_t* out) {
+  if (!p || !out) return OEB_ERR_NULL;
+  *out = signature(p);
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_batch_tuning_get(const oeb_batch_plan* p, int* record, int capacity, int* count) {
+  if (!p) return OEB_ERR_NULL;
+  return tuning_get(p, record, capacity, count);
+}
+
+extern "C" oeb_status oeb_batch_tuning_apply(oeb_batch_plan* p, const int* record, int count) {
+  if (!p) return OEB_ERR_NULL;
+  return tuning_apply(p, record, count);
 }
 
 extern "C" int oeb_batch_launches(const oeb_batch_plan* p) {

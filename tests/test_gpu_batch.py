@@ -124,3 +124,77 @@ def test_batch_rejects_a_member_without_outputs(pkg, fields, chain, cuda):
     del m["outs"]
     with pytest.raises(pkg.OebError):
         chain.BatchPlan([m], chain.FORWARD)
+
+
+def _reset(members):
+    for m in members:
+        for st in list(m["outs"].values()) + list(m["grads"].values()):
+            st.data.fill_(SENTINEL)
+
+
+def test_tuning_record_applies_to_a_new_plan(pkg, fields, chain, cuda, tmp_path):
+    # the autotuner's choices, saved by one plan and loaded by another over the same
+    # ensemble, give the same launches and bit-identical results without timing anything
+    import torch
+    spec = MEMBERS[:5]
+
+    def members():
+        return [_member(pkg, fields, chain, cuda, nx, ny, nz, dt, 70 + i) for i, (nx, ny, nz, dt) in enumerate(spec)]
+
+    a = chain.BatchPlan(members(), chain.FORWARD | chain.ADJOINT)
+    default = a.tuning()
+    assert default and all(c == (0, 0) for c in default)
+    a.autotune()
+    tuned = a.tuning()
+    assert len(tuned) == len(default)
+    assert all(kb in (1, 2, 4, 8) and form in (0, 1, 2) for kb, form in tuned)
+    path = tmp_path / "tuning.json"
+    a.save_tuning(path)
+    b_members = members()
+    b = chain.BatchPlan(b_members, chain.FORWARD | chain.ADJOINT)
+    assert b.signature == a.signature
+    b.load_tuning(path)
+    assert b.tuning() == tuned
+    assert b.launches == a.launches
+    lib = pkg.load_library()
+    before = lib.oeb_launch_count()
+    b.run()
+    torch.cuda.synchronize()
+    assert lib.oeb_launch_count() - before == b.launches
+    _check(chain, b_members, "tuning record applied")
+    # the default choices as a record put the plan back
+    b.apply_tuning(default)
+    assert b.tuning() == default
+    _reset(b_members)
+    b.run()
+    torch.cuda.synchronize()
+    _check(chain, b_members, "default record applied")
+    a.close()
+    b.close()
+
+
+def test_tuning_record_rejected_for_another_plan(pkg, fields, chain, cuda, tmp_path):
+    # a record of another ensemble, of another format, or with a count, kb or form outside
+    # the documented values is refused, and the plan keeps its choices
+    a = chain.BatchPlan([_member(pkg, fields, chain, cuda, nx, ny, nz, dt, 80 + i)
+                         for i, (nx, ny, nz, dt) in enumerate(MEMBERS[:2])], chain.FORWARD)
+    path = tmp_path / "a.json"
+    a.save_tuning(path)
+    c = chain.BatchPlan([_member(pkg, fields, chain, cuda, nx, ny, nz, dt, 85 + i)
+                         for i, (nx, ny, nz, dt) in enumerate(MEMBERS[1:3])], chain.FORWARD)
+    assert c.signature != a.signature
+    before = c.tuning()
+    with pytest.raises(pkg.OebError):
+        c.load_tuning(path)
+    other = tmp_path / "other.json"
+    other.write_text('{"format": "something-else", "signature": "%016x", "choices": []}' % c.signature)
+    with pytest.raises(pkg.OebError):
+        c.load_tuning(other)
+    n = len(before)
+    for bad in ([(0, 0)] * (n + 1), [(3, 0)] + before[1:], [(1, 3)] + before[1:], [(-1, 0)] + before[1:]):
+        with pytest.raises(pkg.OebError) as err:
+            c.apply_tuning(bad)
+        assert err.value.status == 12  # OEB_ERR_ARGUMENT
+    assert c.tuning() == before
+    a.close()
+    c.close()
