@@ -13,7 +13,9 @@ namespace oeb_driver {
 struct Result;
 }
 
-bool oeb_driver_run_f64(const char* kernel, int algo, int count, oeb_driver::Result* r);
-bool oeb_driver_run_f32(const char* kernel, int algo, int count, oeb_driver::Result* r);
+// adjoint: each timed call is the forward variant followed by oeb_<kernel>_adj_<precision>,
+// seeded with the forward outputs (kernels with an adjoint only: see kAdjoint in main())
+bool oeb_driver_run_f64(const char* kernel, int algo, int count, bool adjoint, oeb_driver::Result* r);
+bool oeb_driver_run_f32(const char* kernel, int algo, int count, bool adjoint, oeb_driver::Result* r);
 
 #endif  // OEB_DRIVER_API_H

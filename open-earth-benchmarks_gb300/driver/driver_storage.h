@@ -130,6 +130,7 @@ struct Result {
   double total_ms;
   int64_t points;
   int fields;  // 3-D inputs + semantic outputs: the algorithmic bytes are fields x points x sizeof(T)
+  bool adjoint;  // each timed call was the forward variant followed by the kernel's adjoint
 };
 
 }  // namespace oeb_driver

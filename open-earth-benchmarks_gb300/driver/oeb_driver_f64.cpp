@@ -29,8 +29,10 @@ static const double dt5 = 0.5 * 225.0;
 #include "p_grad_c.h"
 #include "uvbke.h"
 
+// the adjoint entry points of this precision (include/oeb_gb300.h)
+#define OEB_DRIVER_ADJ(k) oeb_##k##_adj_f64
 #include "driver_kernels.inc"
 
-bool oeb_driver_run_f64(const char* kernel, int algo, int count, oeb_driver::Result* r) {
-  return run_kernel(kernel, algo, count, r);
+bool oeb_driver_run_f64(const char* kernel, int algo, int count, bool adjoint, oeb_driver::Result* r) {
+  return run_kernel(kernel, algo, count, adjoint, r);
 }

@@ -41,6 +41,40 @@ def test_unknown_algo_and_kernel(driver):
     assert proc.returncode == 1 and "unknown kernel" in proc.stderr
 
 
+ADJOINT_KERNELS = {"hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "fvtp2d"}
+
+
+def test_adjoint_flag_skips_kernels_without_one(driver):
+    # --adjoint on a kernel without an adjoint entry point says so and runs nothing (no CUDA
+    # call: this runs on the CPU)
+    for name in sorted(KERNELS - ADJOINT_KERNELS):
+        proc = _run(driver, name, "0", "--adjoint", "--json")
+        assert proc.returncode == 0, (name, proc.stdout, proc.stderr)
+        assert "%s: no adjoint" % name in proc.stdout.splitlines()
+        assert not [ln for ln in proc.stdout.splitlines() if ln.startswith("{")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["", "--f32"])
+def test_sweep_all_kernels_with_adjoint(driver, precision):
+    args = ["all", "0", "48", "10", "--count", "3", "--json", "--adjoint"] + ([precision] if precision else [])
+    proc = _run(driver, *args)
+    assert proc.returncode == 0, proc.stdout + proc.stderr
+    lines = proc.stdout.splitlines()
+    recs = [json.loads(ln) for ln in lines if ln.startswith("{")]
+    assert {r["kernel"] for r in recs} == ADJOINT_KERNELS
+    for name in KERNELS - ADJOINT_KERNELS:
+        assert "%s: no adjoint" % name in lines
+    for r in recs:
+        assert r["mode"] == "forward+adjoint" and r["count"] == 3
+        assert r["precision"] == ("f32" if precision else "f64")
+        assert r["ms_per_call"] > 0 and r["gpts"] > 0
+    # the reference's timer line, labelled with the adjoint
+    for name in ADJOINT_KERNELS:
+        assert [ln for ln in lines if ln.startswith("%s + adjoint: " % name) and ln.endswith(" ms")], name
+    assert sum(1 for ln in lines if " + adjoint: " in ln) == len(ADJOINT_KERNELS)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["", "--f32"])
 @pytest.mark.parametrize("algo", ["0", "3"])
