@@ -1,5 +1,9 @@
 """oeb_hdiffsmag_adj_noalloc_f64: the hdiffsmag adjoint on the library's fixed scratch array.
 
+The entry point exists for callers that cannot allocate device memory while they run. One
+example is a host whose own allocator reserved the GPU's memory at start-up, where a pool
+allocation could fail mid-run; another is a time-step loop that must not allocate in its step.
+
 It must give the same results as the pool-backed oeb_hdiffsmag_adj_f64 (bit for bit: the
 same kernels on the same arguments), on consecutive calls that reuse the array with
 different sizes, and reject fields whose allocation exceeds the array (2^21 cells) before
