@@ -247,16 +247,25 @@ oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vec
   return OEB_OK;
 }
 
+// Replaces the plan's device tables by `host`.  The new buffer is allocated and filled
+// first, and the old one freed only after the device is idle (a run in flight may still read
+// it): on any error the plan keeps its tables, which still match its slots.
 oeb_status upload(oeb_batch_plan* p, const std::vector<char>& host) {
-  if (p->tables) cudaFree(p->tables);
-  p->tables = nullptr;
-  p->table_bytes = host.size();
-  cudaError_t e = cudaMalloc(&p->tables, std::max<size_t>(host.size(), 256));
+  char* tables = nullptr;
+  cudaError_t e = cudaMalloc(&tables, std::max<size_t>(host.size(), 256));
   if (e != cudaSuccess) {
     cuda_fail(e);
     return OEB_ERR_ALLOC;
   }
-  OEB_CUDA_TRY(cudaMemcpy(p->tables, host.data(), host.size(), cudaMemcpyHostToDevice));
+  e = cudaMemcpy(tables, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && p->tables) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    cudaFree(tables);
+    return cuda_fail(e);
+  }
+  if (p->tables) cudaFree(p->tables);
+  p->tables = tables;
+  p->table_bytes = host.size();
   return OEB_OK;
 }
 
@@ -517,22 +526,7 @@ oeb_status tuning_apply(oeb_batch_plan* p, const int* rec, int count) {
     sl.ctas = form == kFormPerTile ? sl.total : wave_ctas(p, sl);
     next[i] = std::move(sl);
   }
-  char* tables = nullptr;
-  const cudaError_t e = cudaMalloc(&tables, std::max<size_t>(host.size(), 256));
-  if (e != cudaSuccess) {
-    cuda_fail(e);
-    return OEB_ERR_ALLOC;
-  }
-  const cudaError_t c = cudaMemcpy(tables, host.data(), host.size(), cudaMemcpyHostToDevice);
-  if (c != cudaSuccess) {
-    cudaFree(tables);
-    return cuda_fail(c);
-  }
-  // the old tables may still be read by a run in flight on the plan's streams
-  OEB_CUDA_TRY(cudaDeviceSynchronize());
-  if (p->tables) cudaFree(p->tables);
-  p->tables = tables;
-  p->table_bytes = host.size();
+  OEB_TRY(upload(p, host));
   p->slots = std::move(next);
   return OEB_OK;
 }
