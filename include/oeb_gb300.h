@@ -163,6 +163,23 @@ OEB_API oeb_status oeb_storage3d_alloc_f32(int64_t nx, int64_t ny, int64_t nz, i
 OEB_API oeb_status oeb_storage1d_alloc_f32(int64_t n, int64_t halo, oeb_memref1d_f32* out);
 /* Frees a descriptor returned by oeb_storage*_alloc_* and clears its pointers. */
 OEB_API oeb_status oeb_storage_free(void* memref);
+/* Whole-field transfers (the device side of include/util.h:99-148, which has no device
+ * fields): oeb_upload* copies a host field to its device twin, oeb_download* back.  The
+ * descriptors must have the same sizes, strides and offset, and the same distance from
+ * allocated to aligned.  The whole span is copied, from allocated (or aligned, where
+ * allocated is NULL or above it) to one past the last element, halo and padding included.
+ * The copy uses cudaMemcpyDefault, so either side may be host memory (pageable or pinned) or
+ * device memory.  Asynchronous on `stream`: synchronise it before reading a downloaded field
+ * or changing an uploaded host field.  OEB_ERR_NULL, OEB_ERR_LAYOUT, or OEB_ERR_ALIAS (the
+ * spans overlap) are returned before any CUDA call. */
+OEB_API oeb_status oeb_upload3d_f64(const oeb_memref3d_f64* dev, const oeb_memref3d_f64* host, void* stream);
+OEB_API oeb_status oeb_download3d_f64(const oeb_memref3d_f64* host, const oeb_memref3d_f64* dev, void* stream);
+OEB_API oeb_status oeb_upload1d_f64(const oeb_memref1d_f64* dev, const oeb_memref1d_f64* host, void* stream);
+OEB_API oeb_status oeb_download1d_f64(const oeb_memref1d_f64* host, const oeb_memref1d_f64* dev, void* stream);
+OEB_API oeb_status oeb_upload3d_f32(const oeb_memref3d_f32* dev, const oeb_memref3d_f32* host, void* stream);
+OEB_API oeb_status oeb_download3d_f32(const oeb_memref3d_f32* host, const oeb_memref3d_f32* dev, void* stream);
+OEB_API oeb_status oeb_upload1d_f32(const oeb_memref1d_f32* dev, const oeb_memref1d_f32* host, void* stream);
+OEB_API oeb_status oeb_download1d_f32(const oeb_memref1d_f32* host, const oeb_memref1d_f32* dev, void* stream);
 /* Bytes spanned by a descriptor: from allocated to one past the last element. */
 OEB_API int64_t oeb_memref3d_span_bytes_f64(const oeb_memref3d_f64* m);
 OEB_API int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m);

@@ -407,3 +407,58 @@ extern "C" oeb_status oeb_set_kblock(int kb) {
   oeb::g_kb_override.store(kb, std::memory_order_relaxed);
   return OEB_OK;
 }
+
+// ---- whole-field transfers (oeb_upload* / oeb_download*) ------------------------------
+// A field made by allocateStorage (include/util.h:99-148) moves to or from its device twin as
+// one copy of its span: from the span start (allocated, or aligned where allocated is unset
+// or above it) to one past the last element, halo and padding included.  Both descriptors
+// must describe the same layout; cudaMemcpyDefault lets either side be host (pageable or
+// pinned) or device memory.
+namespace {
+
+template <class T, int R, class M>
+oeb_status transfer(const M* dst, const M* src, void* stream) {
+  if (!dst || !src || !dst->aligned || !src->aligned) return OEB_ERR_NULL;
+  const T* ds = (dst->allocated && dst->allocated <= dst->aligned) ? dst->allocated : dst->aligned;
+  const T* ss = (src->allocated && src->allocated <= src->aligned) ? src->allocated : src->aligned;
+  if (dst->offset != src->offset || (dst->aligned - ds) != (src->aligned - ss)) return OEB_ERR_LAYOUT;
+  int64_t last = 0;
+  for (int r = 0; r < R; ++r) {
+    if (dst->sizes[r] != src->sizes[r] || dst->strides[r] != src->strides[r]) return OEB_ERR_LAYOUT;
+    if (dst->sizes[r] < 1 || dst->strides[r] < 1) return OEB_ERR_LAYOUT;
+    last += (dst->sizes[r] - 1) * dst->strides[r];
+  }
+  const int64_t elems = (int64_t)(dst->aligned - ds) + last + 1;
+  const uintptr_t a = (uintptr_t)ds, b = (uintptr_t)ss, n = (uintptr_t)elems * sizeof(T);
+  if (a < b + n && b < a + n) return OEB_ERR_ALIAS;
+  const cudaError_t e =
+      cudaMemcpyAsync((void*)ds, ss, (size_t)elems * sizeof(T), cudaMemcpyDefault, (cudaStream_t)stream);
+  return e == cudaSuccess ? OEB_OK : oeb::cuda_fail(e);
+}
+
+}  // namespace
+
+extern "C" oeb_status oeb_upload3d_f64(const oeb_memref3d_f64* dev, const oeb_memref3d_f64* host, void* stream) {
+  return transfer<double, 3>(dev, host, stream);
+}
+extern "C" oeb_status oeb_download3d_f64(const oeb_memref3d_f64* host, const oeb_memref3d_f64* dev, void* stream) {
+  return transfer<double, 3>(host, dev, stream);
+}
+extern "C" oeb_status oeb_upload1d_f64(const oeb_memref1d_f64* dev, const oeb_memref1d_f64* host, void* stream) {
+  return transfer<double, 1>(dev, host, stream);
+}
+extern "C" oeb_status oeb_download1d_f64(const oeb_memref1d_f64* host, const oeb_memref1d_f64* dev, void* stream) {
+  return transfer<double, 1>(host, dev, stream);
+}
+extern "C" oeb_status oeb_upload3d_f32(const oeb_memref3d_f32* dev, const oeb_memref3d_f32* host, void* stream) {
+  return transfer<float, 3>(dev, host, stream);
+}
+extern "C" oeb_status oeb_download3d_f32(const oeb_memref3d_f32* host, const oeb_memref3d_f32* dev, void* stream) {
+  return transfer<float, 3>(host, dev, stream);
+}
+extern "C" oeb_status oeb_upload1d_f32(const oeb_memref1d_f32* dev, const oeb_memref1d_f32* host, void* stream) {
+  return transfer<float, 1>(dev, host, stream);
+}
+extern "C" oeb_status oeb_download1d_f32(const oeb_memref1d_f32* host, const oeb_memref1d_f32* dev, void* stream) {
+  return transfer<float, 1>(host, dev, stream);
+}
