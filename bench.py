@@ -339,6 +339,15 @@ def _algorithmic_bytes(pkg, name, elem=8):
     return pkg.KERNELS[name].bytes_per_point(elem) * NX * NY * NZ
 
 
+def _config(names, world):
+    """The workload description both arms print (ours and --impl reference), so that the two
+    lines name the same configuration."""
+    return {"workload": WORKLOAD, "kernels": list(names), "interior": [NX, NY, NZ], "halo": HALO,
+            "points_per_step": len(names) * NX * NY * NZ,
+            "l2": "inputs larger than L2: two 827 MB input sets alternate between steps",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_ours(args):
     import torch
     rank, world, local = _dist_env()
@@ -455,13 +464,9 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 4), "unit": "GPts/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; fields.py 'physical')",
-        "config": {"workload": WORKLOAD, "kernels": names, "interior": [NX, NY, NZ], "halo": HALO,
-                   "points_per_step": pts_step,
-                   "l2": "inputs larger than L2: two 827 MB input sets alternate between steps",
-                   "issue": "the ten stencils are independent: each step forks them onto ten streams and joins "
-                            "them (events), captured once per input set as a CUDA graph of %d kernels and "
-                            "replayed" % graph_kernels,
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": _config(names, world),
+        "issue": "the ten stencils are independent: each step forks them onto ten streams and joins them "
+                 "(events), captured once per input set as a CUDA graph of %d kernels and replayed" % graph_kernels,
         "roofline": {"bound": "hbm", "kernel": dom_k, "achieved": round(achieved, 2), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_source": peak_src,
@@ -903,7 +908,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "GPts/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; fields.py 'physical')",
-            "config": {"workload": WORKLOAD, "interior": [NX, NY, NZ], "halo": HALO},
+            "config": _config(list(pkg.KERNELS), world),
             "cpu_baseline": {"value": round(value, 5), "unit": "GPts/s", "cores": threads, "kind": kind,
                              "sample": "each step = the ten reference kernels once at 128x128x80 (_openmp "
                                        "variants, serial fvtp2d), %s, OMP_NUM_THREADS=%s" %

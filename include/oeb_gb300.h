@@ -165,13 +165,16 @@ OEB_API oeb_status oeb_storage1d_alloc_f32(int64_t n, int64_t halo, oeb_memref1d
 OEB_API oeb_status oeb_storage_free(void* memref);
 /* Whole-field transfers (the device side of include/util.h:99-148, which has no device
  * fields): oeb_upload* copies a host field to its device twin, oeb_download* back.  The
- * descriptors must have the same sizes, strides and offset, and the same distance from
- * allocated to aligned.  The whole span is copied, from allocated (or aligned, where
- * allocated is NULL or above it) to one past the last element, halo and padding included.
- * The copy uses cudaMemcpyDefault, so either side may be host memory (pageable or pinned) or
- * device memory.  Asynchronous on `stream`: synchronise it before reading a downloaded field
- * or changing an uploaded host field.  OEB_ERR_NULL, OEB_ERR_LAYOUT, or OEB_ERR_ALIAS (the
- * spans overlap) are returned before any CUDA call. */
+ * descriptors must have the same offset, sizes and strides.  Accepted pairs: a host field
+ * made by the reference's allocateStorage (aligned = allocated + 32 - halo) or by any other
+ * allocator of that layout, with a device field from oeb_storage*_alloc_* of the same sizes,
+ * halo and pitch_multiple 1 (aligned = allocated), in either direction; the allocated
+ * pointers take no part.  The elements from aligned[0] to the last one are copied, halo and
+ * row padding included.  The copy uses cudaMemcpyDefault, so either side may be host memory
+ * (pageable or pinned) or device memory.  Asynchronous on `stream`: synchronise it before
+ * reading a downloaded field or changing an uploaded host field.  OEB_ERR_NULL,
+ * OEB_ERR_LAYOUT, or OEB_ERR_ALIAS (the element ranges overlap) are returned before any CUDA
+ * call. */
 OEB_API oeb_status oeb_upload3d_f64(const oeb_memref3d_f64* dev, const oeb_memref3d_f64* host, void* stream);
 OEB_API oeb_status oeb_download3d_f64(const oeb_memref3d_f64* host, const oeb_memref3d_f64* dev, void* stream);
 OEB_API oeb_status oeb_upload1d_f64(const oeb_memref1d_f64* dev, const oeb_memref1d_f64* host, void* stream);
@@ -538,7 +541,8 @@ OEB_API oeb_status oeb_hdiffsmag_adj_f64(const oeb_memref3d_f64* uinb, const oeb
 /* the process exits.  All calls share it and it keeps the last call's contents (nothing in   */
 /* it needs to start at zero); calls that overlap on the GPU race.  The first call on a       */
 /* device looks up the array's device address with that device current: make that first call */
-/* before any stream capture.                                                                 */
+/* before any stream capture.  The address is kept for the life of the process, so do not     */
+/* call this entry point on a device after cudaDeviceReset of that device.                    */
 OEB_API oeb_status oeb_hdiffsmag_adj_noalloc_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask,
                                                 const oeb_memref1d_f64* crlavo, const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu,
                                                 const oeb_memref1d_f64* acrlat0, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double eddlat, double eddlon,

@@ -410,29 +410,29 @@ extern "C" oeb_status oeb_set_kblock(int kb) {
 
 // ---- whole-field transfers (oeb_upload* / oeb_download*) ------------------------------
 // A field made by allocateStorage (include/util.h:99-148) moves to or from its device twin as
-// one copy of its span: from the span start (allocated, or aligned where allocated is unset
-// or above it) to one past the last element, halo and padding included.  Both descriptors
-// must describe the same layout; cudaMemcpyDefault lets either side be host (pageable or
-// pinned) or device memory.
+// one copy of its elements: from aligned[0] (element (0,0,0) of the box, halo included) to one
+// past the last element, row padding included.  What lies between allocated and aligned is
+// unused padding in allocateStorage (aligned = allocated + 32 - halo, util.h:139) and none in
+// oeb_storage*_alloc (aligned = allocated), so it is neither compared nor copied.  Both
+// descriptors must have the same offset, sizes and strides; cudaMemcpyDefault lets either
+// side be host (pageable or pinned) or device memory.
 namespace {
 
 template <class T, int R, class M>
 oeb_status transfer(const M* dst, const M* src, void* stream) {
   if (!dst || !src || !dst->aligned || !src->aligned) return OEB_ERR_NULL;
-  const T* ds = (dst->allocated && dst->allocated <= dst->aligned) ? dst->allocated : dst->aligned;
-  const T* ss = (src->allocated && src->allocated <= src->aligned) ? src->allocated : src->aligned;
-  if (dst->offset != src->offset || (dst->aligned - ds) != (src->aligned - ss)) return OEB_ERR_LAYOUT;
+  if (dst->offset != src->offset) return OEB_ERR_LAYOUT;
   int64_t last = 0;
   for (int r = 0; r < R; ++r) {
     if (dst->sizes[r] != src->sizes[r] || dst->strides[r] != src->strides[r]) return OEB_ERR_LAYOUT;
     if (dst->sizes[r] < 1 || dst->strides[r] < 1) return OEB_ERR_LAYOUT;
     last += (dst->sizes[r] - 1) * dst->strides[r];
   }
-  const int64_t elems = (int64_t)(dst->aligned - ds) + last + 1;
-  const uintptr_t a = (uintptr_t)ds, b = (uintptr_t)ss, n = (uintptr_t)elems * sizeof(T);
+  const int64_t elems = last + 1;
+  const uintptr_t a = (uintptr_t)dst->aligned, b = (uintptr_t)src->aligned, n = (uintptr_t)elems * sizeof(T);
   if (a < b + n && b < a + n) return OEB_ERR_ALIAS;
-  const cudaError_t e =
-      cudaMemcpyAsync((void*)ds, ss, (size_t)elems * sizeof(T), cudaMemcpyDefault, (cudaStream_t)stream);
+  const cudaError_t e = cudaMemcpyAsync((void*)dst->aligned, src->aligned, (size_t)elems * sizeof(T),
+                                        cudaMemcpyDefault, (cudaStream_t)stream);
   return e == cudaSuccess ? OEB_OK : oeb::cuda_fail(e);
 }
 

@@ -531,6 +531,25 @@ oeb_status tuning_apply(oeb_batch_plan* p, const int* rec, int count) {
   return OEB_OK;
 }
 
+// Makes the plan's device current for the lifetime of the guard and restores the caller's
+// device afterwards: the entry points that allocate, copy or launch run on the device the plan
+// was created on, whichever device the calling thread has current.
+class PlanDevice {
+ public:
+  explicit PlanDevice(const oeb_batch_plan* p) {
+    ok_ = cudaGetDevice(&prev_) == cudaSuccess && (prev_ == p->device || cudaSetDevice(p->device) == cudaSuccess);
+    switched_ = ok_ && prev_ != p->device;
+  }
+  ~PlanDevice() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  bool ok() const { return ok_; }
+
+ private:
+  int prev_ = 0;
+  bool ok_ = false, switched_ = false;
+};
+
 }  // namespace
 }  // namespace oeb
 
@@ -543,11 +562,15 @@ extern "C" oeb_status oeb_batch_plan_create(const oeb_batch_member* members, int
 
 extern "C" oeb_status oeb_batch_run(oeb_batch_plan* p, void* stream) {
   if (!p) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
   return run(p, (cudaStream_t)stream);
 }
 
 extern "C" oeb_status oeb_batch_autotune(oeb_batch_plan* p, void* stream) {
   if (!p) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
   return autotune(p, (cudaStream_t)stream);
 }
 
@@ -564,6 +587,8 @@ extern "C" oeb_status oeb_batch_tuning_get(const oeb_batch_plan* p, int* record,
 
 extern "C" oeb_status oeb_batch_tuning_apply(oeb_batch_plan* p, const int* record, int count) {
   if (!p) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
   return tuning_apply(p, record, count);
 }
 

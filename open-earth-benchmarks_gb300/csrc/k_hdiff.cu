@@ -554,6 +554,8 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
 //  * Set-up: the array's name is only a host-side stand-in for the device variable.  The first
 //    call on a device looks up its device address with cudaGetSymbolAddress, with that device
 //    current, and keeps it for later calls; make that first call before any stream capture.
+//    The kept address outlives a cudaDeviceReset of that device, after which it is stale: the
+//    entry point is not for use on a device after such a reset.
 constexpr int64_t kNoAllocCells = int64_t(1) << 21;
 static __device__ __align__(256) double g_hdiffsmag_adj_scratch[6 * kNoAllocCells];
 

@@ -8,7 +8,8 @@ recipe runs the same way on an x86 host and on an aarch64 GPU host:
 * ``oracle/_ref/liboeb_ref.so`` -- the reference's own ``include/util.h`` and
   ``kernels/*.h``, compiled from where they lie in the reference source tree through
   the harness TUs in ``oracle/ref/`` (nothing is copied).  Built only when that
-  source tree is present (``OEB_REFERENCE_DIR``, default ``/root/reference``).
+  source tree is present (``OEB_REFERENCE_DIR``, else a ``reference`` directory beside
+  this repository's root).
 
 Both use ``-O3 -fopenmp`` (the reference's CMakeLists.txt:12 flags plus its OpenMP
 link) and ``-ffp-contract=off``: x86-64 gcc emits no FMA by default, but aarch64 gcc
@@ -35,7 +36,9 @@ COMMON_FLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
 def reference_dir() -> Path:
-    return Path(os.environ.get("OEB_REFERENCE_DIR", "/root/reference"))
+    """The reference source tree: $OEB_REFERENCE_DIR, else ``reference`` beside the repository."""
+    env = os.environ.get("OEB_REFERENCE_DIR")
+    return Path(env) if env else REPO.parent / "reference"
 
 
 def _newer(target: Path, sources) -> bool:
