@@ -477,6 +477,12 @@ OEB_API oeb_status oeb_fvtp2d_f32_host(const oeb_memref3d_f32* q_i, const oeb_me
 /*   hdiffsmag, hadvuv, hadvuv5th : active (uin, vin)                          */
 /*   fastwavesuv                  : active (uin, vin, utens, vtens, ppuv)      */
 /*   fvtp2d                       : active q; dy = all six outputs            */
+/*   laplace, hdiffsa             : active in                                 */
+/*   uvbke                        : active (uc, vc)                           */
+/*   nh_p_grad                    : active (uin, vin, gz, pp, pk3, wk1)       */
+/*   p_grad_c                     : active (uin, vin, delpc, gz, pkc)         */
+/* Argument order: dy for every output, the forward inputs in the reference    */
+/* signature's order, dx for every active input, the scalars.                 */
 /* ------------------------------------------------------------------------- */
 
 OEB_API oeb_status oeb_hdiffsmag_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask,
@@ -497,6 +503,18 @@ OEB_API oeb_status oeb_fvtp2d_tl_f64(const oeb_memref3d_f64* dq_i, const oeb_mem
                                     const oeb_memref3d_f64* crx, const oeb_memref3d_f64* cry, const oeb_memref3d_f64* ra_x, const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx, const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area,
                                     const oeb_memref3d_f64* dq, double ppm_p1, double ppm_p2, const oeb_domain* dom, void* stream);
 
+/* kernels/laplace.h:34-43, hdiffsa.h:95-123, uvbke.h:61-75, nh_p_grad.h:116-146, p_grad_c.h:80-101 */
+OEB_API oeb_status oeb_laplace_tl_f64(const oeb_memref3d_f64* dout, const oeb_memref3d_f64* in, const oeb_memref3d_f64* din,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsa_tl_f64(const oeb_memref3d_f64* dout, const oeb_memref3d_f64* in, const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_memref3d_f64* din,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_uvbke_tl_f64(const oeb_memref3d_f64* dub, const oeb_memref3d_f64* dvb, const oeb_memref3d_f64* uc, const oeb_memref3d_f64* vc, const oeb_memref3d_f64* cosa, const oeb_memref3d_f64* rsina, const oeb_memref3d_f64* duc, const oeb_memref3d_f64* dvc, double dt5,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_nh_p_grad_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* rdx, const oeb_memref3d_f64* rdy, const oeb_memref3d_f64* gz, const oeb_memref3d_f64* pp, const oeb_memref3d_f64* pk3, const oeb_memref3d_f64* wk1, const oeb_memref3d_f64* duin, const oeb_memref3d_f64* dvin, const oeb_memref3d_f64* dgz, const oeb_memref3d_f64* dpp, const oeb_memref3d_f64* dpk3, const oeb_memref3d_f64* dwk1, double dt,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_p_grad_c_tl_f64(const oeb_memref3d_f64* duout, const oeb_memref3d_f64* dvout, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* rdxc, const oeb_memref3d_f64* rdyc, const oeb_memref3d_f64* delpc, const oeb_memref3d_f64* gz, const oeb_memref3d_f64* pkc, const oeb_memref3d_f64* duin, const oeb_memref3d_f64* dvin, const oeb_memref3d_f64* ddelpc, const oeb_memref3d_f64* dgz, const oeb_memref3d_f64* dpkc, double dt2,
+                                    const oeb_domain* dom, void* stream);
+
 OEB_API oeb_status oeb_hdiffsmag_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* mask,
                                        const oeb_memref1d_f32* crlavo, const oeb_memref1d_f32* crlavu, const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_memref1d_f32* acrlat0,
                                        const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin, float eddlat, float eddlon, float tau_smag, float weight_smag,
@@ -515,6 +533,18 @@ OEB_API oeb_status oeb_fvtp2d_tl_f32(const oeb_memref3d_f32* dq_i, const oeb_mem
                                     const oeb_memref3d_f32* crx, const oeb_memref3d_f32* cry, const oeb_memref3d_f32* ra_x, const oeb_memref3d_f32* ra_y, const oeb_memref3d_f32* xfx, const oeb_memref3d_f32* yfx, const oeb_memref3d_f32* area,
                                     const oeb_memref3d_f32* dq, float ppm_p1, float ppm_p2, const oeb_domain* dom, void* stream);
 
+/* kernels/laplace.h:34-43, hdiffsa.h:95-123, uvbke.h:61-75, nh_p_grad.h:116-146, p_grad_c.h:80-101 */
+OEB_API oeb_status oeb_laplace_tl_f32(const oeb_memref3d_f32* dout, const oeb_memref3d_f32* in, const oeb_memref3d_f32* din,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsa_tl_f32(const oeb_memref3d_f32* dout, const oeb_memref3d_f32* in, const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_memref3d_f32* din,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_uvbke_tl_f32(const oeb_memref3d_f32* dub, const oeb_memref3d_f32* dvb, const oeb_memref3d_f32* uc, const oeb_memref3d_f32* vc, const oeb_memref3d_f32* cosa, const oeb_memref3d_f32* rsina, const oeb_memref3d_f32* duc, const oeb_memref3d_f32* dvc, double dt5,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_nh_p_grad_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* rdx, const oeb_memref3d_f32* rdy, const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp, const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1, const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin, const oeb_memref3d_f32* dgz, const oeb_memref3d_f32* dpp, const oeb_memref3d_f32* dpk3, const oeb_memref3d_f32* dwk1, float dt,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_p_grad_c_tl_f32(const oeb_memref3d_f32* duout, const oeb_memref3d_f32* dvout, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* rdxc, const oeb_memref3d_f32* rdyc, const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pkc, const oeb_memref3d_f32* duin, const oeb_memref3d_f32* dvin, const oeb_memref3d_f32* ddelpc, const oeb_memref3d_f32* dgz, const oeb_memref3d_f32* dpkc, float dt2,
+                                    const oeb_domain* dom, void* stream);
+
 
 /* ------------------------------------------------------------------------- */
 /* Adjoint (transpose) stencils: xb = J(x)^T yb, the transpose of the         */
@@ -526,7 +556,27 @@ OEB_API oeb_status oeb_fvtp2d_tl_f32(const oeb_memref3d_f32* dq_i, const oeb_mem
 /*   hdiffsmag: xb = (uinb, vinb) on halo 1;  hadvuv / hadvuv5th: halo 2 / 3  */
 /*   fastwavesuv: uinb, vinb, utensb, vtensb on the interior, ppuvb on        */
 /*     i,j in [0,N], k in [-1,N_z];  fvtp2d: qb on halo 3 from (fx1b, fy1b)   */
+/*   laplace: inb on halo 1;  hdiffsa: inb on halo 2 (limiters frozen)       */
+/*   uvbke: ucb on i in [0,N), j in [-1,N); vcb on i in [-1,N), j in [0,N)   */
+/*   nh_p_grad: uinb, vinb on the interior; gzb, ppb, pk3b on i,j in [0,N],  */
+/*     k in [0,N_z]; wk1b on i,j in [0,N]                                     */
+/*   p_grad_c: uinb, vinb on the interior; delpcb on i,j in [-1,N); gzb,     */
+/*     pkcb on i,j in [-1,N), k in [0,N_z]                                    */
+/* Argument order: xb for every active input, the forward inputs in the       */
+/* reference signature's order, yb for every semantic output, the scalars.    */
 /* ------------------------------------------------------------------------- */
+
+/* kernels/laplace.h:34-43, hdiffsa.h:95-123, uvbke.h:61-75, nh_p_grad.h:116-146, p_grad_c.h:80-101 */
+OEB_API oeb_status oeb_laplace_adj_f64(const oeb_memref3d_f64* inb, const oeb_memref3d_f64* in, const oeb_memref3d_f64* outb,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsa_adj_f64(const oeb_memref3d_f64* inb, const oeb_memref3d_f64* in, const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_memref3d_f64* outb,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_uvbke_adj_f64(const oeb_memref3d_f64* ucb, const oeb_memref3d_f64* vcb, const oeb_memref3d_f64* uc, const oeb_memref3d_f64* vc, const oeb_memref3d_f64* cosa, const oeb_memref3d_f64* rsina, const oeb_memref3d_f64* ubb, const oeb_memref3d_f64* vbb, double dt5,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_nh_p_grad_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* gzb, const oeb_memref3d_f64* ppb, const oeb_memref3d_f64* pk3b, const oeb_memref3d_f64* wk1b, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* rdx, const oeb_memref3d_f64* rdy, const oeb_memref3d_f64* gz, const oeb_memref3d_f64* pp, const oeb_memref3d_f64* pk3, const oeb_memref3d_f64* wk1, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double dt,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_p_grad_c_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* delpcb, const oeb_memref3d_f64* gzb, const oeb_memref3d_f64* pkcb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* rdxc, const oeb_memref3d_f64* rdyc, const oeb_memref3d_f64* delpc, const oeb_memref3d_f64* gz, const oeb_memref3d_f64* pkc, const oeb_memref3d_f64* uoutb, const oeb_memref3d_f64* voutb, double dt2,
+                                    const oeb_domain* dom, void* stream);
 
 OEB_API oeb_status oeb_hdiffsmag_adj_f64(const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin, const oeb_memref3d_f64* vin, const oeb_memref3d_f64* mask, const oeb_memref1d_f64* crlavo,
                                         const oeb_memref1d_f64* crlavu, const oeb_memref1d_f64* crlato, const oeb_memref1d_f64* crlatu, const oeb_memref1d_f64* acrlat0, const oeb_memref3d_f64* uoutb,
@@ -560,6 +610,18 @@ OEB_API oeb_status oeb_fastwavesuv_adj_f64(const oeb_memref3d_f64* uinb, const o
 OEB_API oeb_status oeb_fvtp2d_adj_f64(const oeb_memref3d_f64* qb, const oeb_memref3d_f64* q, const oeb_memref3d_f64* crx, const oeb_memref3d_f64* cry, const oeb_memref3d_f64* ra_x, const oeb_memref3d_f64* ra_y, const oeb_memref3d_f64* xfx,
                                      const oeb_memref3d_f64* yfx, const oeb_memref3d_f64* area, const oeb_memref3d_f64* fx1b, const oeb_memref3d_f64* fy1b, double ppm_p1, double ppm_p2,
                                      const oeb_domain* dom, void* stream);
+
+/* kernels/laplace.h:34-43, hdiffsa.h:95-123, uvbke.h:61-75, nh_p_grad.h:116-146, p_grad_c.h:80-101 */
+OEB_API oeb_status oeb_laplace_adj_f32(const oeb_memref3d_f32* inb, const oeb_memref3d_f32* in, const oeb_memref3d_f32* outb,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_hdiffsa_adj_f32(const oeb_memref3d_f32* inb, const oeb_memref3d_f32* in, const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_memref3d_f32* outb,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_uvbke_adj_f32(const oeb_memref3d_f32* ucb, const oeb_memref3d_f32* vcb, const oeb_memref3d_f32* uc, const oeb_memref3d_f32* vc, const oeb_memref3d_f32* cosa, const oeb_memref3d_f32* rsina, const oeb_memref3d_f32* ubb, const oeb_memref3d_f32* vbb, double dt5,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_nh_p_grad_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* gzb, const oeb_memref3d_f32* ppb, const oeb_memref3d_f32* pk3b, const oeb_memref3d_f32* wk1b, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* rdx, const oeb_memref3d_f32* rdy, const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp, const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1, const oeb_memref3d_f32* uoutb, const oeb_memref3d_f32* voutb, float dt,
+                                    const oeb_domain* dom, void* stream);
+OEB_API oeb_status oeb_p_grad_c_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* delpcb, const oeb_memref3d_f32* gzb, const oeb_memref3d_f32* pkcb, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* rdxc, const oeb_memref3d_f32* rdyc, const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pkc, const oeb_memref3d_f32* uoutb, const oeb_memref3d_f32* voutb, float dt2,
+                                    const oeb_domain* dom, void* stream);
 
 OEB_API oeb_status oeb_hdiffsmag_adj_f32(const oeb_memref3d_f32* uinb, const oeb_memref3d_f32* vinb, const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin, const oeb_memref3d_f32* mask, const oeb_memref1d_f32* crlavo,
                                         const oeb_memref1d_f32* crlavu, const oeb_memref1d_f32* crlato, const oeb_memref1d_f32* crlatu, const oeb_memref1d_f32* acrlat0, const oeb_memref3d_f32* uoutb,

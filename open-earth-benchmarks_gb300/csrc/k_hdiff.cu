@@ -311,6 +311,174 @@ oeb_status hdiffsmag_tl_entry(const M3* duout, const M3* dvout, const M3* uin, c
   return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
 }
 
+// ============================== hdiffsa: tangent-linear and adjoint ===============
+// Linearised at `in` with the flux limiters of hdiffsa.h:106-113 frozen:
+//   out = in + mask (flx(i-1) - flx + fly(j-1) - fly),
+//   flx = fx (lap(i+1) - lap),  fly = fy crlato(j) (lap(j+1) - lap),
+//   fx = 0 where flx (in(i+1) - in) > 0 at the state, else 1 (fy likewise with j),
+//   lap = in(i-1) + in(i+1) - 2 in + crlato(j) (in(j+1) - in) + crlatu(j) (in(j-1) - in).
+// Active input: in (mask, crlato, crlatu are parameters).  The transpose for outb, with
+// G = mask outb on the interior and 0 elsewhere:
+//   Fx = fx (G(i+1) - G) on [-1,N) x [0,N),  Fy = fy crlato(j) (G(j+1) - G) on [0,N) x [-1,N),
+//   lapb = Fx(i-1) - Fx + Fy(j-1) - Fy,
+//   inb = outb (interior) + lapb(i-1) + lapb(i+1) - (2 + crlato(j) + crlatu(j)) lapb
+//         + crlato(j-1) lapb(j-1) + crlatu(j+1) lapb(j+1)    on in's reach box [-2, N+2)^2.
+// One kernel: a CTA stages its tile's in and G in shared memory, recomputes lap and the limiter
+// flags exactly as the forward kernel does (the same operations on the same operands), then
+// forms Fx, Fy, lapb and inb in shared memory.  Shared layout (per k-level), inb tile origin
+// (i0, j0):
+//   in   : 38 x 38, (i0-3+a, j0-3+b)
+//   lap  : 36 x 36, (i0-2+a, j0-2+b)
+//   gl   : 36 x 36, G at (i0-2+a, j0-2+b); then lapb, 34 x 34 at (i0-1+a, j0-1+b)
+//   fx   : 35 x 34, (i0-2+a, j0-1+b);   fy : 34 x 35, (i0-1+a, j0-2+b)
+template <class T>
+struct HdiffsaAdjSmem {
+  T in[38][38];
+  T lap[36][36];
+  T gl[36][36];
+  T fx[34][35];
+  T fy[35][34];
+  T crlato[38], crlatu[38];  // j0-3+b
+};
+
+template <class T>
+struct hdiffsa_adj_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ inb, const T* __restrict__ in,
+                                             const T* __restrict__ mask, const T* __restrict__ crlato,
+                                             const T* __restrict__ crlatu, int64_t s1d, const T* __restrict__ outb,
+                                             Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HdiffsaAdjSmem<T>& s = *reinterpret_cast<HdiffsaAdjSmem<T>*>(smem_raw);
+    T(*lapb)[34] = reinterpret_cast<T(*)[34]>(&s.gl[0][0]);
+    const int i0 = -2 + (int)blk.x * kT, j0 = -2 + (int)blk.y * kT;
+    const int64_t sj = d.sj;
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    if (tid < 38) {
+      const int j = j0 - 3 + tid;
+      const bool ok = j >= -1 && j < d.ny + 1;
+      s.crlato[tid] = ok ? ld(crlato + (int64_t)j * s1d) : T(0);
+      s.crlatu[tid] = ok ? ld(crlatu + (int64_t)j * s1d) : T(0);
+    }
+    auto interior = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region<38, 38>([&](int a, int b) {
+        const int i = i0 - 3 + a, j = j0 - 3 + b;
+        const bool ok = i >= -2 && i < d.nx + 2 && j >= -2 && j < d.ny + 2;
+        s.in[b][a] = ok ? ld(in + kofs + i + j * sj) : T(0);
+      });
+      for_region<36, 36>([&](int a, int b) {
+        const int i = i0 - 2 + a, j = j0 - 2 + b;
+        const int64_t o = kofs + i + j * sj;
+        s.gl[b][a] = interior(i, j) ? ld(outb + o) * ld(mask + o) : T(0);
+      });
+      __syncthreads();
+      // hdiffsa.h:101 where the forward forms lap (i, j in [-1, N+1)), its operations in its order
+      for_region<36, 36>([&](int a, int b) {
+        const int i = i0 - 2 + a, j = j0 - 2 + b;
+        T v = T(0);
+        if (i >= -1 && i < d.nx + 1 && j >= -1 && j < d.ny + 1) {
+          const T c = s.in[b + 1][a + 1];
+          v = (((s.in[b + 1][a] + s.in[b + 1][a + 2]) - scale2<1>(c)) + s.crlato[b + 1] * (s.in[b + 2][a + 1] - c)) +
+              s.crlatu[b + 1] * (s.in[b][a + 1] - c);
+        }
+        s.lap[b][a] = v;
+      });
+      __syncthreads();
+      // hdiffsa.h:106-109: Fx at (i, j), kept where the forward keeps flx
+      for_region<35, 34>([&](int a, int b) {
+        const int i = i0 - 2 + a, j = j0 - 1 + b;
+        T v = T(0);
+        if (i >= -1 && i < d.nx && j >= 0 && j < d.ny) {
+          const T f = s.lap[b + 1][a + 1] - s.lap[b + 1][a];
+          if (!Prec<T>::prod_gt0(f, s.in[b + 2][a + 2] - s.in[b + 2][a + 1])) v = s.gl[b + 1][a + 1] - s.gl[b + 1][a];
+        }
+        s.fx[b][a] = v;
+      });
+      // hdiffsa.h:110-113: Fy at (i, j), crlato(j) folded in
+      for_region<34, 35>([&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 - 2 + b;
+        T v = T(0);
+        if (i >= 0 && i < d.nx && j >= -1 && j < d.ny) {
+          const T co = s.crlato[b + 1];
+          const T f = co * (s.lap[b + 1][a + 1] - s.lap[b][a + 1]);
+          if (!Prec<T>::prod_gt0(f, s.in[b + 2][a + 2] - s.in[b + 1][a + 2])) v = co * (s.gl[b + 1][a + 1] - s.gl[b][a + 1]);
+        }
+        s.fy[b][a] = v;
+      });
+      __syncthreads();
+      // lapb over the dead G
+      for_region<34, 34>([&](int a, int b) { lapb[b][a] = (s.fx[b][a] - s.fx[b][a + 1]) + (s.fy[b][a] - s.fy[b + 1][a]); });
+      __syncthreads();
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < d.nx + 2 && j < d.ny + 2) {
+          const int64_t o = kofs + i + j * sj;
+          const T c = lapb[b + 1][a + 1];
+          T v = (lapb[b + 1][a] + lapb[b + 1][a + 2]) - ((T(2) + s.crlato[b + 3]) + s.crlatu[b + 3]) * c;
+          v = fma(s.crlato[b + 2], lapb[b][a + 1], v);
+          v = fma(s.crlatu[b + 4], lapb[b + 2][a + 1], v);
+          if (interior(i, j)) v = v + ld(outb + o);
+          inb[o] = v;
+        }
+      });
+      __syncthreads();
+    }
+  }
+};
+
+template <class T, class M3, class M1>
+oeb_status hdiffsa_tl_entry(const M3* dout, const M3* in, const M3* mask, const M1* crlato, const M1* crlatu,
+                            const M3* din, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(hdiffsa_entry<T>(dout, in, mask, crlato, crlatu, dom, stream));
+    OEB_TRY(hdiffsa_entry<T>(dout, din, mask, crlato, crlatu, dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *x, *m, *lo, *lu, *y;
+  OEB_TRY(arr.pack(in, din, &x));
+  OEB_TRY(arr.pack(mask, (const M3*)nullptr, &m));
+  OEB_TRY(arr.pack(crlato, (const M1*)nullptr, &lo));
+  OEB_TRY(arr.pack(crlatu, (const M1*)nullptr, &lu));
+  OEB_TRY(arr.alloc(dout, &y));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, in->strides[1], in->strides[0]};
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<hdiffsa_kernel<D>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(HdiffsaSmem<D>),
+                                    (cudaStream_t)stream, y, x, m, lo, lu, crlato->strides[0], d, kb));
+  return arr.unpack(dout->aligned + dout->offset, y, *dom, kInterior, d.sj, d.sk);
+}
+
+template <class T, class M3, class M1>
+oeb_status hdiffsa_adj_entry(const M3* inb, const M3* in, const M3* mask, const M1* crlato, const M1* crlatu,
+                             const M3* outb, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(hdiffsa_entry<T>(outb, in, mask, crlato, crlatu, dom, stream));
+  }
+  Grid<T> gib, gin, gm, gob;
+  Line<T> lo, lu;
+  OEB_TRY((check_field3<T>(inb, *dom, Reach{2, 2, 2, 2, 0, 0}, &gib)));
+  OEB_TRY((check_field3<T>(in, *dom, Reach{2, 2, 2, 2, 0, 0}, &gin)));
+  OEB_TRY((check_field3<T>(mask, *dom, kInterior, &gm)));
+  OEB_TRY((check_field3<T>(outb, *dom, kInterior, &gob)));
+  OEB_TRY((check_field1<T>(crlato, *dom, 1, 1, &lo)));
+  OEB_TRY((check_field1<T>(crlatu, *dom, 1, 1, &lu)));
+  OEB_TRY(check_same_strides<T>({&gib, &gin, &gm, &gob}));
+  OEB_TRY(check_no_alias({gib.lo, gib.hi},
+                         {gin.lo, gin.hi, gm.lo, gm.hi, gob.lo, gob.hi, lo.lo, lo.hi, lu.lo, lu.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gin.sj, gin.sk};
+  const int kb = tuned_kb(kKB);
+  return launch<hdiffsa_adj_kernel<T>>(tile_grid(d.nx + 4, d.ny + 4, d.nz, kT, kT, kb), sizeof(HdiffsaAdjSmem<T>),
+                                       (cudaStream_t)stream, gib.origin, gin.origin, gm.origin, lo.origin, lu.origin,
+                                       lo.s, gob.origin, d, kb);
+}
+
 // ============================== hdiffsmag adjoint ================================
 // Linearised at (uin, vin) with the clamp of hdiffsmag.h:236/251 frozen:
 //   uout = u + su Lu,  su = clamp(tau sqrt(Xu) - w mask),  Xu = (T(i+1)^2 + T^2)/2 + (S(j-1)^2 + S^2)/2
@@ -663,8 +831,24 @@ using namespace oeb;
                                   voutb, eddlat, eddlon, tau_smag, weight_smag, dom, stream);                     \
   }
 
+#define OEB_HDIFFSA_DIFF_ENTRIES(S, T)                                                                              \
+  extern "C" oeb_status oeb_hdiffsa_tl_##S(const oeb_memref3d_##S* dout, const oeb_memref3d_##S* in,               \
+                                           const oeb_memref3d_##S* mask, const oeb_memref1d_##S* crlato,          \
+                                           const oeb_memref1d_##S* crlatu, const oeb_memref3d_##S* din,           \
+                                           const oeb_domain* dom, void* stream) {                                  \
+    return hdiffsa_tl_entry<T>(dout, in, mask, crlato, crlatu, din, dom, stream);                                  \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_hdiffsa_adj_##S(const oeb_memref3d_##S* inb, const oeb_memref3d_##S* in,              \
+                                            const oeb_memref3d_##S* mask, const oeb_memref1d_##S* crlato,         \
+                                            const oeb_memref1d_##S* crlatu, const oeb_memref3d_##S* outb,         \
+                                            const oeb_domain* dom, void* stream) {                                 \
+    return hdiffsa_adj_entry<T>(inb, in, mask, crlato, crlatu, outb, dom, stream);                                 \
+  }
+
 OEB_HDIFF_ENTRIES(f64, double)
 OEB_HDIFF_ENTRIES(f32, float)
+OEB_HDIFFSA_DIFF_ENTRIES(f64, double)
+OEB_HDIFFSA_DIFF_ENTRIES(f32, float)
 
 extern "C" oeb_status oeb_hdiffsmag_adj_noalloc_f64(
     const oeb_memref3d_f64* uinb, const oeb_memref3d_f64* vinb, const oeb_memref3d_f64* uin,

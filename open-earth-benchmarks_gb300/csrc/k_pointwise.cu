@@ -658,6 +658,537 @@ oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M
   return stt;
 }
 
+
+// ============================== shared pieces of the adjoints below ==================
+// Scratch term fields of an adjoint, each laid out like `like` (the terms are written and read
+// at interior points only): cells per field and the offset of the interior origin.
+struct TermLayout {
+  int64_t n, org;
+};
+template <class M3>
+TermLayout term_layout(const M3* like) {
+  const auto* start = (like->allocated && like->allocated <= like->aligned) ? like->allocated : like->aligned;
+  const int64_t last = (like->sizes[0] - 1) * like->strides[0] + (like->sizes[1] - 1) * like->strides[1] +
+                       (like->sizes[2] - 1) * like->strides[2];
+  return TermLayout{(int64_t)(like->aligned - start) + last + 1, (int64_t)(like->aligned - start) + like->offset};
+}
+
+__device__ __forceinline__ bool inside(const Dims& d, int i, int j, int k) {
+  return i >= 0 && i < d.nx && j >= 0 && j < d.ny && k >= 0 && k < d.nz;
+}
+
+// ============================== laplace: tangent-linear and adjoint ==================
+// laplace.h:39 is linear: out = -4 in + (in(i-1) + in(i+1)) + (in(j+1) + in(j-1)).  Its
+// transpose for outb gathers, at every cell c of in's reach box [-1, N+1)^2 x [0, Nz):
+//   inb(c) = -4 outb(c) + outb(c-i) + outb(c+i) + outb(c-j) + outb(c+j)   (interior terms only)
+template <class T>
+struct laplace_adj_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ inb, const T* __restrict__ outb,
+                                             Dims d, int kb) {
+    const int64_t sj = d.sj;
+    for_box_k<RowUnroll<T>::value>(blk, d.sj, d.sk, -1, -1, d.nx + 2, d.ny + 2, d.nz, kb,
+                                   [&](int64_t o, int i, int j, int k) {
+      T v = inside(d, i, j, k) ? T(-4.0) * ld(outb + o) : T(0);
+      if (inside(d, i - 1, j, k)) v = v + ld(outb + o - 1);
+      if (inside(d, i + 1, j, k)) v = v + ld(outb + o + 1);
+      if (inside(d, i, j - 1, k)) v = v + ld(outb + o - sj);
+      if (inside(d, i, j + 1, k)) v = v + ld(outb + o + sj);
+      inb[o] = v;
+    });
+  }
+};
+
+template <class T, class M3>
+oeb_status laplace_tl_entry(const M3* dout, const M3* in, const M3* din, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(laplace_entry<T>(in, dout, dom, stream));
+    OEB_TRY(laplace_entry<T>(din, dout, dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *x, *y;
+  OEB_TRY(arr.pack(in, din, &x));
+  OEB_TRY(arr.alloc(dout, &y));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, in->strides[1], in->strides[0]};
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<laplace_kernel<D>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, x, y, d, kb));
+  return arr.unpack(dout->aligned + dout->offset, y, *dom, kInterior, d.sj, d.sk);
+}
+
+template <class T, class M3>
+oeb_status laplace_adj_entry(const M3* inb, const M3* in, const M3* outb, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(laplace_entry<T>(in, outb, dom, stream));
+  }
+  Grid<T> gib, gin, gob;
+  OEB_TRY((check_field3<T>(inb, *dom, Reach{1, 1, 1, 1, 0, 0}, &gib)));
+  OEB_TRY((check_field3<T>(in, *dom, Reach{1, 1, 1, 1, 0, 0}, &gin)));
+  OEB_TRY((check_field3<T>(outb, *dom, kInterior, &gob)));
+  OEB_TRY(check_same_strides<T>({&gib, &gin, &gob}));
+  OEB_TRY(check_no_alias({gib.lo, gib.hi}, {gin.lo, gin.hi, gob.lo, gob.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gob.sj, gob.sk};
+  const int kb = tuned_kb(kKB);
+  return launch<laplace_adj_kernel<T>>(tile_grid(d.nx + 2, d.ny + 2, d.nz, kTI, kTJ, kb), 0, (cudaStream_t)stream,
+                                       gib.origin, gob.origin, d, kb);
+}
+
+// ============================== uvbke: tangent-linear and adjoint =====================
+// uvbke.h:66-71 is linear in (uc, vc) with su = uc(j-1) + uc and sv = vc(i-1) + vc:
+//   ub = dt5 (su - sv cosa) rsina,  vb = dt5 (sv - su cosa) rsina.
+// Its transpose for (ubb, vbb): at each interior point
+//   sub = dt5 rsina (ubb - cosa vbb),  svb = dt5 rsina (vbb - cosa ubb),
+// and each cell gathers ucb(c) = sub(c) + sub(c+j) (on [0,N) x [-1,N)) and
+// vcb(c) = svb(c) + svb(c+i) (on [-1,N) x [0,N)), interior points only.
+template <class T>
+__device__ __forceinline__ T uvbke_sub(const T* ubb, const T* vbb, const T* cosa, const T* rsina, int64_t o, T dt5) {
+  return (dt5 * ld(rsina + o)) * (ld(ubb + o) - ld(cosa + o) * ld(vbb + o));
+}
+template <class T>
+__device__ __forceinline__ T uvbke_svb(const T* ubb, const T* vbb, const T* cosa, const T* rsina, int64_t o, T dt5) {
+  return (dt5 * ld(rsina + o)) * (ld(vbb + o) - ld(cosa + o) * ld(ubb + o));
+}
+
+template <class T>
+struct uvbke_adj_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ ucb, T* __restrict__ vcb,
+                                             const T* __restrict__ cosa, const T* __restrict__ rsina,
+                                             const T* __restrict__ ubb, const T* __restrict__ vbb, T dt5, Dims d,
+                                             int kb) {
+    const int64_t sj = d.sj;
+    for_box_k<RowUnroll<T>::value>(blk, d.sj, d.sk, -1, -1, d.nx + 1, d.ny + 1, d.nz, kb,
+                                   [&](int64_t o, int i, int j, int k) {
+      const bool here = inside(d, i, j, k);
+      const T su = here ? uvbke_sub(ubb, vbb, cosa, rsina, o, dt5) : T(0);
+      const T sv = here ? uvbke_svb(ubb, vbb, cosa, rsina, o, dt5) : T(0);
+      if (i >= 0) ucb[o] = inside(d, i, j + 1, k) ? su + uvbke_sub(ubb, vbb, cosa, rsina, o + sj, dt5) : su;
+      if (j >= 0) vcb[o] = inside(d, i + 1, j, k) ? sv + uvbke_svb(ubb, vbb, cosa, rsina, o + 1, dt5) : sv;
+    });
+  }
+};
+
+template <class T, class M3>
+oeb_status uvbke_tl_entry(const M3* dub, const M3* dvb, const M3* uc, const M3* vc, const M3* cosa, const M3* rsina,
+                          const M3* duc, const M3* dvc, double dt5, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(uvbke_entry<T>(dub, dvb, uc, vc, cosa, rsina, dt5, dom, stream));
+    OEB_TRY(uvbke_entry<T>(dub, dvb, duc, dvc, cosa, rsina, dt5, dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *u, *v, *ca, *rs, *ou, *ov;
+  OEB_TRY(arr.pack(uc, duc, &u));
+  OEB_TRY(arr.pack(vc, dvc, &v));
+  OEB_TRY(arr.pack(cosa, (const M3*)nullptr, &ca));
+  OEB_TRY(arr.pack(rsina, (const M3*)nullptr, &rs));
+  OEB_TRY(arr.alloc(dub, &ou));
+  OEB_TRY(arr.alloc(dvb, &ov));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uc->strides[1], uc->strides[0]};
+  const T dt5_hi = T(dt5), dt5_lo = T(dt5 - (double)dt5_hi);
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<uvbke_kernel<D>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, ou, ov, u, v, ca, rs, D(dt5_hi),
+                                  D(dt5_lo), d, kb));
+  OEB_TRY(arr.unpack(dub->aligned + dub->offset, ou, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dvb->aligned + dvb->offset, ov, *dom, kInterior, d.sj, d.sk);
+}
+
+template <class T, class M3>
+oeb_status uvbke_adj_entry(const M3* ucb, const M3* vcb, const M3* uc, const M3* vc, const M3* cosa, const M3* rsina,
+                           const M3* ubb, const M3* vbb, double dt5, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(uvbke_entry<T>(ubb, vbb, uc, vc, cosa, rsina, dt5, dom, stream));
+  }
+  Grid<T> gucb, gvcb, gca, grs, gub, gvb;
+  OEB_TRY((check_field3<T>(ucb, *dom, Reach{0, 0, 1, 0, 0, 0}, &gucb)));
+  OEB_TRY((check_field3<T>(vcb, *dom, Reach{1, 0, 0, 0, 0, 0}, &gvcb)));
+  OEB_TRY((check_field3<T>(cosa, *dom, kInterior, &gca)));
+  OEB_TRY((check_field3<T>(rsina, *dom, kInterior, &grs)));
+  OEB_TRY((check_field3<T>(ubb, *dom, kInterior, &gub)));
+  OEB_TRY((check_field3<T>(vbb, *dom, kInterior, &gvb)));
+  OEB_TRY(check_same_strides<T>({&gucb, &gvcb, &gca, &grs, &gub, &gvb}));
+  OEB_TRY(check_no_alias({gucb.lo, gucb.hi, gvcb.lo, gvcb.hi},
+                         {gca.lo, gca.hi, grs.lo, grs.hi, gub.lo, gub.hi, gvb.lo, gvb.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gub.sj, gub.sk};
+  const int kb = tuned_kb(kKB);
+  return launch<uvbke_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz, kTI, kTJ, kb), 0, (cudaStream_t)stream,
+                                     gucb.origin, gvcb.origin, gca.origin, grs.origin, gub.origin, gvb.origin, T(dt5),
+                                     d, kb);
+}
+
+// ============================== p_grad_c: tangent-linear and adjoint ==================
+// p_grad_c.h:90-97 at point p, along the axis of stride s (i for uout, j for vout):
+//   out = in + c f,  c = dt2 rd / (delpc(p-s) + delpc(p)),
+//   f = A1 B1 + A2 B2,  A1 = gz(p-s,k+1) - gz(p),  B1 = pkc(p,k+1) - pkc(p-s),
+//                       A2 = gz(p-s) - gz(p,k+1),  B2 = pkc(p-s,k+1) - pkc(p).
+// Active inputs: uin, vin, delpc, gz, pkc (rdxc, rdyc, dt2 are parameters).  The transpose
+// for outb, with fb = outb c and sb = -fb f / (delpc(p-s) + delpc(p)):
+//   inb += outb;  delpcb(p-s), delpcb(p) += sb;
+//   gzb(p-s,k+1) += fb B1, gzb(p) -= fb B1, gzb(p-s) += fb B2, gzb(p,k+1) -= fb B2;
+//   pkcb(p,k+1) += fb A1, pkcb(p-s) -= fb A1, pkcb(p-s,k+1) += fb A2, pkcb(p) -= fb A2.
+// Pass 1 writes uinb, vinb and the five terms (sb, fb B1, fb B2, fb A1, fb A2) of each axis at
+// every interior point; pass 2 makes every cell of the reach boxes gather them.
+template <class T>
+struct PgcTerms {
+  T* t[10];  // per axis (u: 0-4, v: 5-9): sb, fb B1, fb B2, fb A1, fb A2
+};
+
+template <class T>
+__device__ __forceinline__ void pgc_adj_axis(T* const* t, const T* __restrict__ gz, const T* __restrict__ pkc,
+                                             const T* __restrict__ delpc, int64_t o, int64_t s, int64_t sk, T gz0,
+                                             T gz1, T pk0, T pk1, T wk, T coef, T y) {
+  const T A1 = ld(gz + o - s + sk) - gz0, B1 = pk1 - ld(pkc + o - s);
+  const T A2 = ld(gz + o - s) - gz1, B2 = ld(pkc + o - s + sk) - pk0;
+  const T f = A1 * B1 + A2 * B2;
+  const T r = T(1) / (ld(delpc + o - s) + wk);
+  const T fb = (y * coef) * r;
+  t[0][o] = -(fb * f) * r;
+  t[1][o] = fb * B1;
+  t[2][o] = fb * B2;
+  t[3][o] = fb * A1;
+  t[4][o] = fb * A2;
+}
+
+template <class T>
+struct p_grad_c_adj_terms_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, PgcTerms<T> tm, T* __restrict__ uinb,
+                                             T* __restrict__ vinb, const T* __restrict__ rdxc,
+                                             const T* __restrict__ rdyc, const T* __restrict__ delpc,
+                                             const T* __restrict__ gz, const T* __restrict__ pkc,
+                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T dt2, Dims d,
+                                             int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
+      const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
+      const T wk = ld(delpc + o);
+      const T yu = ld(uoutb + o), yv = ld(voutb + o);
+      uinb[o] = yu;
+      vinb[o] = yv;
+      pgc_adj_axis(tm.t, gz, pkc, delpc, o, 1, sk, gz0, gz1, pk0, pk1, wk, dt2 * ld(rdxc + o), yu);
+      pgc_adj_axis(tm.t + 5, gz, pkc, delpc, o, sj, sk, gz0, gz1, pk0, pk1, wk, dt2 * ld(rdyc + o), yv);
+    });
+  }
+};
+
+// Every cell c of [-1, N) x [-1, N) x [0, Nz] (delpcb only below Nz) gathers the terms of the
+// interior points that read it: along axis s, the points c, c+s, c-k and c+s-k.
+template <class T>
+struct p_grad_c_adj_gather_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ delpcb, T* __restrict__ gzb,
+                                             T* __restrict__ pkcb, PgcTerms<T> tm, Dims d, int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    for_box_k<RowUnroll<T>::value>(blk, sj, sk, -1, -1, d.nx + 1, d.ny + 1, d.nz + 1, kb,
+                                   [&](int64_t o, int i, int j, int k) {
+      T db = T(0), gb = T(0), pb = T(0);
+  #pragma unroll
+      for (int ax = 0; ax < 2; ++ax) {
+        T* const* t = tm.t + 5 * ax;
+        const int di = ax == 0 ? 1 : 0, dj = 1 - di;
+        const int64_t s = ax == 0 ? 1 : sj;
+        if (inside(d, i, j, k)) {  // p = c
+          db = db + t[0][o];
+          gb = gb - t[1][o];
+          pb = pb - t[4][o];
+        }
+        if (inside(d, i + di, j + dj, k)) {  // p = c + s
+          db = db + t[0][o + s];
+          gb = gb + t[2][o + s];
+          pb = pb - t[3][o + s];
+        }
+        if (inside(d, i, j, k - 1)) {  // p = c - k
+          gb = gb - t[2][o - sk];
+          pb = pb + t[3][o - sk];
+        }
+        if (inside(d, i + di, j + dj, k - 1)) {  // p = c + s - k
+          gb = gb + t[1][o + s - sk];
+          pb = pb + t[4][o + s - sk];
+        }
+      }
+      if (k < d.nz) delpcb[o] = db;
+      gzb[o] = gb;
+      pkcb[o] = pb;
+    });
+  }
+};
+
+template <class T, class M3>
+oeb_status p_grad_c_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M3* rdxc,
+                             const M3* rdyc, const M3* delpc, const M3* gz, const M3* pkc, const M3* duin,
+                             const M3* dvin, const M3* ddelpc, const M3* dgz, const M3* dpkc, T dt2,
+                             const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(p_grad_c_entry<T>(duout, dvout, uin, vin, rdxc, rdyc, delpc, gz, pkc, dt2, dom, stream));
+    OEB_TRY(p_grad_c_entry<T>(duout, dvout, duin, dvin, rdxc, rdyc, ddelpc, dgz, dpkc, dt2, dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *u, *v, *rx, *ry, *dp, *g, *pk, *ou, *ov;
+  OEB_TRY(arr.pack(uin, duin, &u));
+  OEB_TRY(arr.pack(vin, dvin, &v));
+  OEB_TRY(arr.pack(rdxc, (const M3*)nullptr, &rx));
+  OEB_TRY(arr.pack(rdyc, (const M3*)nullptr, &ry));
+  OEB_TRY(arr.pack(delpc, ddelpc, &dp));
+  OEB_TRY(arr.pack(gz, dgz, &g));
+  OEB_TRY(arr.pack(pkc, dpkc, &pk));
+  OEB_TRY(arr.alloc(duout, &ou));
+  OEB_TRY(arr.alloc(dvout, &ov));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<p_grad_c_kernel<D>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, ou, ov, u, v, rx, ry, dp, g, pk,
+                                     D(dt2), d, kb));
+  OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
+}
+
+template <class T, class M3>
+oeb_status p_grad_c_adj_entry(const M3* uinb, const M3* vinb, const M3* delpcb, const M3* gzb, const M3* pkcb,
+                              const M3* uin, const M3* vin, const M3* rdxc, const M3* rdyc, const M3* delpc,
+                              const M3* gz, const M3* pkc, const M3* uoutb, const M3* voutb, T dt2,
+                              const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(p_grad_c_entry<T>(uoutb, voutb, uin, vin, rdxc, rdyc, delpc, gz, pkc, dt2, dom, stream));
+  }
+  Grid<T> gub, gvb, gdb, ggb, gpb, grx, gry, gdp, ggz, gpk, guo, gvo;
+  const Reach rk{1, 0, 1, 0, 0, 1};
+  OEB_TRY((check_field3<T>(uinb, *dom, kInterior, &gub)));
+  OEB_TRY((check_field3<T>(vinb, *dom, kInterior, &gvb)));
+  OEB_TRY((check_field3<T>(delpcb, *dom, Reach{1, 0, 1, 0, 0, 0}, &gdb)));
+  OEB_TRY((check_field3<T>(gzb, *dom, rk, &ggb)));
+  OEB_TRY((check_field3<T>(pkcb, *dom, rk, &gpb)));
+  OEB_TRY((check_field3<T>(rdxc, *dom, kInterior, &grx)));
+  OEB_TRY((check_field3<T>(rdyc, *dom, kInterior, &gry)));
+  OEB_TRY((check_field3<T>(delpc, *dom, Reach{1, 0, 1, 0, 0, 0}, &gdp)));
+  OEB_TRY((check_field3<T>(gz, *dom, rk, &ggz)));
+  OEB_TRY((check_field3<T>(pkc, *dom, rk, &gpk)));
+  OEB_TRY((check_field3<T>(uoutb, *dom, kInterior, &guo)));
+  OEB_TRY((check_field3<T>(voutb, *dom, kInterior, &gvo)));
+  OEB_TRY(check_same_strides<T>({&gub, &gvb, &gdb, &ggb, &gpb, &grx, &gry, &gdp, &ggz, &gpk, &guo, &gvo}));
+  OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi, gdb.lo, gdb.hi, ggb.lo, ggb.hi, gpb.lo, gpb.hi},
+                         {grx.lo, grx.hi, gry.lo, gry.hi, gdp.lo, gdp.hi, ggz.lo, ggz.hi, gpk.lo, gpk.hi, guo.lo,
+                          guo.hi, gvo.lo, gvo.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  cudaStream_t st = (cudaStream_t)stream;
+  const TermLayout lay = term_layout(uoutb);
+  void* buf = nullptr;
+  OEB_TRY(scratch_alloc(&buf, (size_t)lay.n * 10 * sizeof(T), st));
+  PgcTerms<T> tm;
+  for (int q = 0; q < 10; ++q) tm.t[q] = static_cast<T*>(buf) + q * lay.n + lay.org;
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, guo.sj, guo.sk};
+  const int kb = tuned_kb(kKB);
+  oeb_status stt = launch<p_grad_c_adj_terms_kernel<T>>(grid_for(*dom, kb), 0, st, tm, gub.origin, gvb.origin,
+                                                        grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin,
+                                                        guo.origin, gvo.origin, dt2, d, kb);
+  if (stt == OEB_OK)
+    stt = launch<p_grad_c_adj_gather_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 1, kTI, kTJ, kb), 0, st,
+                                                gdb.origin, ggb.origin, gpb.origin, tm, d, kb);
+  scratch_free(buf, st);
+  return stt;
+}
+
+// ============================== nh_p_grad: tangent-linear and adjoint =================
+// nh_p_grad.h:121-141 at point p along the axis of stride s (i+1 for uout, j+1 for vout),
+// with X0 = X(p), X1 = X(p,k+1) and x0, x1 the same at p+s:
+//   out = (in + c1 fk + c2 fp) rd,  c1 = dt / ((pk1 - pk0) + (pkx1 - pkx0)),  c2 = dt / (w1 + w1x),
+//   fk = A1 B1 + A2 B2,  fp = A1 P1 + A2 P2,
+//   A1 = gz1 - gx0, A2 = gz0 - gx1, B1 = pkx1 - pk0, B2 = pk1 - pkx0, P1 = ppx1 - pp0, P2 = pp1 - ppx0.
+// Active inputs: uin, vin, gz, pp, pk3, wk1 (rdx, rdy, dt are parameters).  With U = outb rd,
+// fkb = U c1, fpb = U c2, sb = -fkb fk / (wk + wkx) and wb = -fpb fp / (w1 + w1x), the
+// transpose is: inb += U;
+//   gz:  a1 = fkb B1 + fpb P1 -> gz1 += a1, gx0 -= a1;  a2 = fkb B2 + fpb P2 -> gz0 += a2, gx1 -= a2
+//   pk3: c1 = fkb A1 + sb -> pkx1 += c1, pk0 -= c1;     c2 = fkb A2 + sb -> pk1 += c2, pkx0 -= c2
+//   pp:  e1 = fpb A1 -> ppx1 += e1, pp0 -= e1;          e2 = fpb A2 -> pp1 += e2, ppx0 -= e2
+//   wk1: w1 += wb, w1x += wb.
+// Pass 1 writes uinb, vinb and the seven terms of each axis; pass 2 gathers them.
+template <class T>
+struct NhpTerms {
+  T* t[14];  // per axis (u: 0-6, v: 7-13): a1, a2, c1, c2, e1, e2, wb
+};
+
+template <class T>
+__device__ __forceinline__ void nhp_adj_axis(T* const* t, const T* __restrict__ gz, const T* __restrict__ pp,
+                                             const T* __restrict__ pk3, const T* __restrict__ wk1, int64_t o,
+                                             int64_t s, int64_t sk, T gz0, T gz1, T pk0, T pk1, T pp0, T pp1, T w1,
+                                             T dt, T U) {
+  const T gx0 = ld(gz + o + s), gx1 = ld(gz + o + s + sk);
+  const T pkx0 = ld(pk3 + o + s), pkx1 = ld(pk3 + o + s + sk);
+  const T ppx0 = ld(pp + o + s), ppx1 = ld(pp + o + s + sk);
+  const T A1 = gz1 - gx0, A2 = gz0 - gx1;
+  const T B1 = pkx1 - pk0, B2 = pk1 - pkx0;
+  const T P1 = ppx1 - pp0, P2 = pp1 - ppx0;
+  const T fk = A1 * B1 + A2 * B2, fp = A1 * P1 + A2 * P2;
+  const T rs = T(1) / ((pk1 - pk0) + (pkx1 - pkx0));
+  const T rw = T(1) / (w1 + ld(wk1 + o + s));
+  const T Ud = U * dt;
+  const T fkb = Ud * rs, fpb = Ud * rw;
+  const T sb = -(fkb * fk) * rs;
+  t[0][o] = fkb * B1 + fpb * P1;
+  t[1][o] = fkb * B2 + fpb * P2;
+  t[2][o] = fkb * A1 + sb;
+  t[3][o] = fkb * A2 + sb;
+  t[4][o] = fpb * A1;
+  t[5][o] = fpb * A2;
+  t[6][o] = -(fpb * fp) * rw;
+}
+
+template <class T>
+struct nh_p_grad_adj_terms_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, NhpTerms<T> tm, T* __restrict__ uinb,
+                                             T* __restrict__ vinb, const T* __restrict__ rdx,
+                                             const T* __restrict__ rdy, const T* __restrict__ gz,
+                                             const T* __restrict__ pp, const T* __restrict__ pk3,
+                                             const T* __restrict__ wk1, const T* __restrict__ uoutb,
+                                             const T* __restrict__ voutb, T dt, Dims d, int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
+      const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
+      const T pp0 = ld(pp + o), pp1 = ld(pp + o + sk), w1 = ld(wk1 + o);
+      const T U = ld(uoutb + o) * ld(rdx + o), V = ld(voutb + o) * ld(rdy + o);
+      uinb[o] = U;
+      vinb[o] = V;
+      nhp_adj_axis(tm.t, gz, pp, pk3, wk1, o, 1, sk, gz0, gz1, pk0, pk1, pp0, pp1, w1, dt, U);
+      nhp_adj_axis(tm.t + 7, gz, pp, pk3, wk1, o, sj, sk, gz0, gz1, pk0, pk1, pp0, pp1, w1, dt, V);
+    });
+  }
+};
+
+// Every cell c of [0, N] x [0, N] x [0, Nz] (wk1b only below Nz) gathers, along axis s, the
+// terms of the interior points c, c-s, c-k and c-s-k.
+template <class T>
+struct nh_p_grad_adj_gather_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ gzb, T* __restrict__ ppb,
+                                             T* __restrict__ pk3b, T* __restrict__ wk1b, NhpTerms<T> tm, Dims d,
+                                             int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    for_box_k<RowUnroll<T>::value>(blk, sj, sk, 0, 0, d.nx + 1, d.ny + 1, d.nz + 1, kb,
+                                   [&](int64_t o, int i, int j, int k) {
+      T gb = T(0), pb = T(0), kb3 = T(0), wb = T(0);
+  #pragma unroll
+      for (int ax = 0; ax < 2; ++ax) {
+        T* const* t = tm.t + 7 * ax;
+        const int di = ax == 0 ? 1 : 0, dj = 1 - di;
+        const int64_t s = ax == 0 ? 1 : sj;
+        if (inside(d, i, j, k)) {  // p = c
+          gb = gb + t[1][o];
+          kb3 = kb3 - t[2][o];
+          pb = pb - t[4][o];
+          wb = wb + t[6][o];
+        }
+        if (inside(d, i - di, j - dj, k)) {  // p = c - s
+          gb = gb - t[0][o - s];
+          kb3 = kb3 - t[3][o - s];
+          pb = pb - t[5][o - s];
+          wb = wb + t[6][o - s];
+        }
+        if (inside(d, i, j, k - 1)) {  // p = c - k
+          gb = gb + t[0][o - sk];
+          kb3 = kb3 + t[3][o - sk];
+          pb = pb + t[5][o - sk];
+        }
+        if (inside(d, i - di, j - dj, k - 1)) {  // p = c - s - k
+          gb = gb - t[1][o - s - sk];
+          kb3 = kb3 + t[2][o - s - sk];
+          pb = pb + t[4][o - s - sk];
+        }
+      }
+      gzb[o] = gb;
+      ppb[o] = pb;
+      pk3b[o] = kb3;
+      if (k < d.nz) wk1b[o] = wb;
+    });
+  }
+};
+
+template <class T, class M3>
+oeb_status nh_p_grad_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M3* rdx,
+                              const M3* rdy, const M3* gz, const M3* pp, const M3* pk3, const M3* wk1,
+                              const M3* duin, const M3* dvin, const M3* dgz, const M3* dpp, const M3* dpk3,
+                              const M3* dwk1, T dt, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(nh_p_grad_entry<T>(duout, dvout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, dt, dom, stream));
+    OEB_TRY(nh_p_grad_entry<T>(duout, dvout, duin, dvin, rdx, rdy, dgz, dpp, dpk3, dwk1, dt, dom, stream));
+  }
+  OEB_RETURN_IF_VALIDATING();
+  using D = Dual<T>;
+  DualArrays<T> arr((cudaStream_t)stream);
+  D *u, *v, *rx, *ry, *g, *p, *pk, *w, *ou, *ov;
+  OEB_TRY(arr.pack(uin, duin, &u));
+  OEB_TRY(arr.pack(vin, dvin, &v));
+  OEB_TRY(arr.pack(rdx, (const M3*)nullptr, &rx));
+  OEB_TRY(arr.pack(rdy, (const M3*)nullptr, &ry));
+  OEB_TRY(arr.pack(gz, dgz, &g));
+  OEB_TRY(arr.pack(pp, dpp, &p));
+  OEB_TRY(arr.pack(pk3, dpk3, &pk));
+  OEB_TRY(arr.pack(wk1, dwk1, &w));
+  OEB_TRY(arr.alloc(duout, &ou));
+  OEB_TRY(arr.alloc(dvout, &ov));
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
+  const int kb = tuned_kb(kKB);
+  OEB_TRY(launch<nh_p_grad_kernel<D>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, ou, ov, u, v, rx, ry, g, p, pk, w,
+                                      D(dt), d, kb));
+  OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
+  return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
+}
+
+template <class T, class M3>
+oeb_status nh_p_grad_adj_entry(const M3* uinb, const M3* vinb, const M3* gzb, const M3* ppb, const M3* pk3b,
+                               const M3* wk1b, const M3* uin, const M3* vin, const M3* rdx, const M3* rdy,
+                               const M3* gz, const M3* pp, const M3* pk3, const M3* wk1, const M3* uoutb,
+                               const M3* voutb, T dt, const oeb_domain* dom, void* stream) {
+  {
+    ValidateOnly guard;
+    OEB_TRY(nh_p_grad_entry<T>(uoutb, voutb, uin, vin, rdx, rdy, gz, pp, pk3, wk1, dt, dom, stream));
+  }
+  Grid<T> gub, gvb, ggb, gpb, gkb, gwb, grx, gry, ggz, gpp, gpk, gw1, guo, gvo;
+  const Reach r11{0, 1, 0, 1, 0, 1}, r10{0, 1, 0, 1, 0, 0};
+  OEB_TRY((check_field3<T>(uinb, *dom, kInterior, &gub)));
+  OEB_TRY((check_field3<T>(vinb, *dom, kInterior, &gvb)));
+  OEB_TRY((check_field3<T>(gzb, *dom, r11, &ggb)));
+  OEB_TRY((check_field3<T>(ppb, *dom, r11, &gpb)));
+  OEB_TRY((check_field3<T>(pk3b, *dom, r11, &gkb)));
+  OEB_TRY((check_field3<T>(wk1b, *dom, r10, &gwb)));
+  OEB_TRY((check_field3<T>(rdx, *dom, kInterior, &grx)));
+  OEB_TRY((check_field3<T>(rdy, *dom, kInterior, &gry)));
+  OEB_TRY((check_field3<T>(gz, *dom, r11, &ggz)));
+  OEB_TRY((check_field3<T>(pp, *dom, r11, &gpp)));
+  OEB_TRY((check_field3<T>(pk3, *dom, r11, &gpk)));
+  OEB_TRY((check_field3<T>(wk1, *dom, r10, &gw1)));
+  OEB_TRY((check_field3<T>(uoutb, *dom, kInterior, &guo)));
+  OEB_TRY((check_field3<T>(voutb, *dom, kInterior, &gvo)));
+  OEB_TRY(check_same_strides<T>(
+      {&gub, &gvb, &ggb, &gpb, &gkb, &gwb, &grx, &gry, &ggz, &gpp, &gpk, &gw1, &guo, &gvo}));
+  OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi, ggb.lo, ggb.hi, gpb.lo, gpb.hi, gkb.lo, gkb.hi, gwb.lo,
+                          gwb.hi},
+                         {grx.lo, grx.hi, gry.lo, gry.hi, ggz.lo, ggz.hi, gpp.lo, gpp.hi, gpk.lo, gpk.hi, gw1.lo,
+                          gw1.hi, guo.lo, guo.hi, gvo.lo, gvo.hi}));
+  OEB_RETURN_IF_VALIDATING();
+  cudaStream_t st = (cudaStream_t)stream;
+  const TermLayout lay = term_layout(uoutb);
+  void* buf = nullptr;
+  OEB_TRY(scratch_alloc(&buf, (size_t)lay.n * 14 * sizeof(T), st));
+  NhpTerms<T> tm;
+  for (int q = 0; q < 14; ++q) tm.t[q] = static_cast<T*>(buf) + q * lay.n + lay.org;
+  const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, guo.sj, guo.sk};
+  const int kb = tuned_kb(kKB);
+  oeb_status stt = launch<nh_p_grad_adj_terms_kernel<T>>(grid_for(*dom, kb), 0, st, tm, gub.origin, gvb.origin,
+                                                         grx.origin, gry.origin, ggz.origin, gpp.origin, gpk.origin,
+                                                         gw1.origin, guo.origin, gvo.origin, dt, d, kb);
+  if (stt == OEB_OK)
+    stt = launch<nh_p_grad_adj_gather_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 1, kTI, kTJ, kb), 0, st,
+                                                 ggb.origin, gpb.origin, gkb.origin, gwb.origin, tm, d, kb);
+  scratch_free(buf, st);
+  return stt;
+}
+
 }  // namespace
 }  // namespace oeb
 
@@ -737,5 +1268,63 @@ using namespace oeb;
                                 eddlat, eddlon, dom, stream);                                                      \
   }
 
+#define OEB_POINTWISE_DIFF_ENTRIES(S, T)                                                                           \
+  extern "C" oeb_status oeb_laplace_tl_##S(const OEB_M3(S) * dout, const OEB_M3(S) * in, const OEB_M3(S) * din,     \
+                                           const oeb_domain* dom, void* stream) {                                  \
+    return laplace_tl_entry<T>(dout, in, din, dom, stream);                                                        \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_laplace_adj_##S(const OEB_M3(S) * inb, const OEB_M3(S) * in, const OEB_M3(S) * outb,    \
+                                            const oeb_domain* dom, void* stream) {                                 \
+    return laplace_adj_entry<T>(inb, in, outb, dom, stream);                                                       \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_uvbke_tl_##S(const OEB_M3(S) * dub, const OEB_M3(S) * dvb, const OEB_M3(S) * uc,        \
+                                         const OEB_M3(S) * vc, const OEB_M3(S) * cosa, const OEB_M3(S) * rsina,     \
+                                         const OEB_M3(S) * duc, const OEB_M3(S) * dvc, double dt5,                 \
+                                         const oeb_domain* dom, void* stream) {                                    \
+    return uvbke_tl_entry<T>(dub, dvb, uc, vc, cosa, rsina, duc, dvc, dt5, dom, stream);                           \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_uvbke_adj_##S(const OEB_M3(S) * ucb, const OEB_M3(S) * vcb, const OEB_M3(S) * uc,       \
+                                          const OEB_M3(S) * vc, const OEB_M3(S) * cosa, const OEB_M3(S) * rsina,    \
+                                          const OEB_M3(S) * ubb, const OEB_M3(S) * vbb, double dt5,                \
+                                          const oeb_domain* dom, void* stream) {                                   \
+    return uvbke_adj_entry<T>(ucb, vcb, uc, vc, cosa, rsina, ubb, vbb, dt5, dom, stream);                          \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_p_grad_c_tl_##S(                                                                       \
+      const OEB_M3(S) * duout, const OEB_M3(S) * dvout, const OEB_M3(S) * uin, const OEB_M3(S) * vin,               \
+      const OEB_M3(S) * rdxc, const OEB_M3(S) * rdyc, const OEB_M3(S) * delpc, const OEB_M3(S) * gz,                \
+      const OEB_M3(S) * pkc, const OEB_M3(S) * duin, const OEB_M3(S) * dvin, const OEB_M3(S) * ddelpc,             \
+      const OEB_M3(S) * dgz, const OEB_M3(S) * dpkc, T dt2, const oeb_domain* dom, void* stream) {                 \
+    return p_grad_c_tl_entry<T>(duout, dvout, uin, vin, rdxc, rdyc, delpc, gz, pkc, duin, dvin, ddelpc, dgz, dpkc, \
+                                dt2, dom, stream);                                                                 \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_p_grad_c_adj_##S(                                                                      \
+      const OEB_M3(S) * uinb, const OEB_M3(S) * vinb, const OEB_M3(S) * delpcb, const OEB_M3(S) * gzb,              \
+      const OEB_M3(S) * pkcb, const OEB_M3(S) * uin, const OEB_M3(S) * vin, const OEB_M3(S) * rdxc,                 \
+      const OEB_M3(S) * rdyc, const OEB_M3(S) * delpc, const OEB_M3(S) * gz, const OEB_M3(S) * pkc,                 \
+      const OEB_M3(S) * uoutb, const OEB_M3(S) * voutb, T dt2, const oeb_domain* dom, void* stream) {              \
+    return p_grad_c_adj_entry<T>(uinb, vinb, delpcb, gzb, pkcb, uin, vin, rdxc, rdyc, delpc, gz, pkc, uoutb,       \
+                                 voutb, dt2, dom, stream);                                                         \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_nh_p_grad_tl_##S(                                                                      \
+      const OEB_M3(S) * duout, const OEB_M3(S) * dvout, const OEB_M3(S) * uin, const OEB_M3(S) * vin,               \
+      const OEB_M3(S) * rdx, const OEB_M3(S) * rdy, const OEB_M3(S) * gz, const OEB_M3(S) * pp,                     \
+      const OEB_M3(S) * pk3, const OEB_M3(S) * wk1, const OEB_M3(S) * duin, const OEB_M3(S) * dvin,                 \
+      const OEB_M3(S) * dgz, const OEB_M3(S) * dpp, const OEB_M3(S) * dpk3, const OEB_M3(S) * dwk1, T dt,           \
+      const oeb_domain* dom, void* stream) {                                                                       \
+    return nh_p_grad_tl_entry<T>(duout, dvout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, duin, dvin, dgz, dpp, dpk3,   \
+                                 dwk1, dt, dom, stream);                                                           \
+  }                                                                                                                \
+  extern "C" oeb_status oeb_nh_p_grad_adj_##S(                                                                     \
+      const OEB_M3(S) * uinb, const OEB_M3(S) * vinb, const OEB_M3(S) * gzb, const OEB_M3(S) * ppb,                 \
+      const OEB_M3(S) * pk3b, const OEB_M3(S) * wk1b, const OEB_M3(S) * uin, const OEB_M3(S) * vin,                 \
+      const OEB_M3(S) * rdx, const OEB_M3(S) * rdy, const OEB_M3(S) * gz, const OEB_M3(S) * pp,                     \
+      const OEB_M3(S) * pk3, const OEB_M3(S) * wk1, const OEB_M3(S) * uoutb, const OEB_M3(S) * voutb, T dt,         \
+      const oeb_domain* dom, void* stream) {                                                                       \
+    return nh_p_grad_adj_entry<T>(uinb, vinb, gzb, ppb, pk3b, wk1b, uin, vin, rdx, rdy, gz, pp, pk3, wk1, uoutb,   \
+                                  voutb, dt, dom, stream);                                                         \
+  }
+
 OEB_POINTWISE_ENTRIES(f64, double)
 OEB_POINTWISE_ENTRIES(f32, float)
+OEB_POINTWISE_DIFF_ENTRIES(f64, double)
+OEB_POINTWISE_DIFF_ENTRIES(f32, float)

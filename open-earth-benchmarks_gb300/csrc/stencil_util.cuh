@@ -134,6 +134,26 @@ __device__ __forceinline__ void for_box(const uint3& blk, const Dims& d, int ilo
   }
 }
 
+// for_box over the k-levels [k0, k0+kb) of [0, nk) (nk may exceed the interior's nz: the
+// boxes of fields read at k+1), handing f the level as well: f(o, i, j, k).
+template <int U = 32 / kTY, class F>
+__device__ __forceinline__ void for_box_k(const uint3& blk, int64_t sj, int64_t sk, int ilo, int jlo, int ni, int nj,
+                                          int nk, int kb, F&& f) {
+  const int a = (int)(blk.x * 32 + threadIdx.x);
+  if (a >= ni) return;
+  const int i = ilo + a;
+  const int k0 = blk.z * kb, k1 = min(k0 + kb, nk);
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    const int64_t kofs = (int64_t)k * sk;
+#pragma unroll U
+    for (int r = 0; r < 32 / kTY; ++r) {
+      const int b = (int)(blk.y * 32 + threadIdx.y) + kTY * r;
+      if (b < nj) f(kofs + i + (int64_t)(jlo + b) * sj, i, jlo + b, k);
+    }
+  }
+}
+
 // Grid of a tiled kernel: one CTA per TI x TJ tile of the (i, j) region
 // [ilo, ilo+ni) x [jlo, jlo+nj) and per kb k-levels.
 inline dim3 tile_grid(int ni, int nj, int nz, int ti, int tj, int kb) {

@@ -196,6 +196,11 @@ ACTIVE = {
     "hadvuv5th": ("uin", "vin"),
     "fastwavesuv": ("uin", "vin", "utens", "vtens", "ppuv"),
     "fvtp2d": ("q",),
+    "laplace": ("in",),
+    "hdiffsa": ("in",),
+    "uvbke": ("uc", "vc"),
+    "nh_p_grad": ("uin", "vin", "gz", "pp", "pk3", "wk1"),
+    "p_grad_c": ("uin", "vin", "delpc", "gz", "pkc"),
 }
 
 # Fields an adjoint call reads or writes in full (frozen state and parameters it reads, the
@@ -206,4 +211,10 @@ ADJ_FIELDS = {
     "hadvuv5th": ("uin", "vin", "uoutb", "voutb", "uinb", "vinb"),
     "fastwavesuv": ("wgtfac", "hhl", "rho", "uoutb", "voutb", "uinb", "vinb", "utensb", "vtensb", "ppuvb"),
     "fvtp2d": ("q", "crx", "cry", "ra_x", "ra_y", "xfx", "yfx", "area", "fx1b", "fy1b", "qb"),
+    "laplace": ("outb", "inb"),
+    "hdiffsa": ("in", "mask", "outb", "inb"),
+    "uvbke": ("cosa", "rsina", "ubb", "vbb", "ucb", "vcb"),
+    "nh_p_grad": ("rdx", "rdy", "gz", "pp", "pk3", "wk1", "uoutb", "voutb", "uinb", "vinb", "gzb", "ppb", "pk3b",
+                  "wk1b"),
+    "p_grad_c": ("rdxc", "rdyc", "delpc", "gz", "pkc", "uoutb", "voutb", "uinb", "vinb", "delpcb", "gzb", "pkcb"),
 }

@@ -1,8 +1,8 @@
 """Tangent-linear and adjoint stencils on the GPU.
 
-For hdiffsmag, hadvuv, hadvuv5th, fastwavesuv and fvtp2d the library exports
-``oeb_<k>_tl_<p>`` (dy = J(x) dx, branches frozen at x) and ``oeb_<k>_adj_<p>``
-(xbar = J(x)^T ybar, a gather with no atomics).  Checked here:
+For every one of the ten stencils the library exports ``oeb_<k>_tl_<p>`` (dy = J(x) dx,
+branches frozen at x) and ``oeb_<k>_adj_<p>`` (xbar = J(x)^T ybar, a gather with no
+atomics).  Checked here:
 
 * the dot-product test <J dx, J dx> = <dx, J^T (J dx)> over the written boxes, to 1e-13
   relative in FP64 and 1e-5 in FP32;
@@ -20,7 +20,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 H = 3
-ADJ = ("hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "fvtp2d")
+ADJ = ("hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "fvtp2d", "laplace", "hdiffsa", "uvbke", "nh_p_grad",
+       "p_grad_c")
 SENTINEL = -7.0e5
 
 

@@ -198,3 +198,57 @@ def test_tuning_record_rejected_for_another_plan(pkg, fields, chain, cuda, tmp_p
     assert c.tuning() == before
     a.close()
     c.close()
+
+
+# Members of benchmark configuration 5's sizes: nx, ny from {48..320} step 16, nz from
+# {40, 60, 80, 137}, mixed precision; two of them 256 or more wide with 137 levels.
+ORACLE_MEMBERS = [(272, 48, 137, np.float64), (48, 256, 137, np.float32), (64, 80, 40, np.float64),
+                  (96, 48, 60, np.float32), (320, 64, 80, np.float64)]
+
+
+def test_batch_members_match_the_oracle_step(pkg, fields, chain, cuda):
+    # every FP64 member's forward outputs bit for bit against the step composed from the
+    # oracle's stencils (oracle/chain.py); every FP32 member's normwise against that FP64 step,
+    # both the total error and the error of the FP32 arithmetic alone (the FP64 step on the
+    # FP32-rounded inputs)
+    import torch
+    from oracle import chain as ochain
+    members = [_member(pkg, fields, chain, cuda, nx, ny, nz, dt, 140 + i)
+               for i, (nx, ny, nz, dt) in enumerate(ORACLE_MEMBERS)]
+    plan = chain.BatchPlan(members, chain.FORWARD | chain.ADJOINT)
+    plan.autotune()
+    for m in members:
+        for st in list(m["outs"].values()) + list(m["grads"].values()):
+            st.data.fill_(SENTINEL)
+    plan.run()
+    torch.cuda.synchronize()
+    boxes = {"uout": 3, "vout": 3, "fx1": 0, "fy1": 0}
+    for i, (m, (nx, ny, nz, dt)) in enumerate(zip(members, ORACLE_MEMBERS)):
+        x = fields.make_chain_inputs(nx, ny, nz, 140 + i, halo=H)
+        s = m["scalars"]
+
+        def box(a, e):
+            return a[H:H + nz, H - e:H + ny + e, H - e:H + nx + e]
+
+        if dt == np.float64:
+            want = ochain.run_chain(x, s, nx, ny, nz, H)
+            for n in chain.OUTPUTS:
+                assert_bitwise_equal(m["outs"][n].numpy(), want[n], "batched FP64 member %d (%dx%dx%d) %s" %
+                                     (i, nx, ny, nz, n))
+        else:
+            want = ochain.run_chain(x, s, nx, ny, nz, H)
+            xq = {k: v.astype(np.float32).astype(np.float64) for k, v in x.items()}
+            sq = {k: float(np.float32(v)) for k, v in s.items()}
+            want_q = ochain.run_chain(xq, sq, nx, ny, nz, H)
+            for n, e in boxes.items():
+                got = box(m["outs"][n].numpy().astype(np.float64), e)
+                scale = float(np.max(np.abs(box(want[n], e))))
+                tot = np.abs(got - box(want[n], e)) / scale
+                ar = np.abs(got - box(want_q[n], e)) / scale
+                what = "batched FP32 member %d (%dx%dx%d) %s" % (i, nx, ny, nz, n)
+                # as the chained step alone: an fvtp2d limiter may flip where FP32 cannot
+                # resolve the deciding difference
+                assert int((ar > 1e-5).sum()) <= 1e-4 * ar.size + 2, what
+                assert float(np.sqrt(np.mean(ar ** 2))) <= 1e-6, what
+                assert float(np.sqrt(np.mean(tot ** 2))) <= 1e-5, what
+    plan.close()

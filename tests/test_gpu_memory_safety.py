@@ -25,7 +25,8 @@ SENTINEL = -7.0e5
 NX, NY, NZ = 37, 45, 5
 KERNELS = ("laplace", "hdiffsa", "hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "uvbke", "nh_p_grad",
            "p_grad_c", "fvtp2d")
-ADJ = ("hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "fvtp2d")
+ADJ = ("hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "fvtp2d", "laplace", "hdiffsa", "uvbke", "nh_p_grad",
+       "p_grad_c")
 
 
 class Guarded:
