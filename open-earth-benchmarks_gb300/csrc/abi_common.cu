@@ -13,6 +13,7 @@
 
 #include "oeb_common.cuh"
 #include "launch.cuh"
+#include "stage.cuh"
 
 namespace oeb {
 
@@ -78,6 +79,36 @@ std::atomic<int> g_kb_override{0};
 }  // namespace
 
 int kb_override() { return g_kb_override.load(std::memory_order_relaxed); }
+
+namespace {
+thread_local int t_host_in_place = 0;
+}  // namespace
+bool fields_in_host_memory() { return t_host_in_place > 0; }
+HostInPlace::HostInPlace() { ++t_host_in_place; }
+HostInPlace::~HostInPlace() { --t_host_in_place; }
+
+// SMs of each device, read once (cudaDevAttrMultiProcessorCount); 0 until read.
+namespace {
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_sms[kMaxDevices];
+}  // namespace
+
+int staged_kb(int tiles, int nz, int ctas_per_sm) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+  int sms = dev < kMaxDevices ? g_sms[dev].load(std::memory_order_relaxed) : 0;
+  if (sms < 1) {
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    if (dev < kMaxDevices) g_sms[dev].store(sms, std::memory_order_relaxed);
+  }
+  // the most k-chunks per tile that still fit every CTA into one wave, then levels per chunk
+  const long slots = (long)sms * (ctas_per_sm > 0 ? ctas_per_sm : 1);
+  long chunks = tiles > 0 ? slots / tiles : 1;
+  if (chunks < 1) chunks = 1;
+  if (chunks > nz) chunks = nz;
+  const long kb = (nz + chunks - 1) / (chunks > 0 ? chunks : 1);
+  return (int)(kb < 1 ? 1 : kb);
+}
 
 Recorder* recorder() { return t_recorder; }
 void set_recorder(Recorder* r) { t_recorder = r; }

@@ -245,7 +245,11 @@ oeb_status run_host(const oeb_domain* dom, void* stream, std::initializer_list<c
   for (int q = 0; q < n1 && direct; ++q) direct = device_addressable(d1[q].aligned);
   for (int q = 0; q < no && direct; ++q) direct = device_addressable(o3[q].aligned);
   if (direct) {
-    oeb_status st = launch(d3, d1, o3, dom, stream);
+    oeb_status st;
+    {
+      HostInPlace in_place;
+      st = launch(d3, d1, o3, dom, stream);
+    }
     const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (st == OEB_OK && e != cudaSuccess) st = cuda_fail(e);
     return st;

@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "precision.cuh"
+#include "stage.cuh"
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
@@ -296,6 +297,268 @@ struct hadv_kernel {
 
 constexpr int kKB = 1;  // k-levels per CTA (one: the most CTAs, which hides FP64 and load latency best)
 
+// ---- FP32 forms staged through shared memory (stage.cuh) -----------------------------
+// A CTA owns a 32 x 32 tile and the k-levels [k0, k0+kb); each level's input boxes are copied
+// into a ring of NB shared-memory buffers by cp.async, ahead of the level being computed.  The
+// arithmetic is the FP32 kernels' above, in the same order; only where the operands come from
+// changes.  Stencils that read level k+1 (p_grad_c, nh_p_grad) compute level k once levels k
+// and k+1 are resident, with one more level in flight; laplace and uvbke keep two in flight.
+
+// Marches the levels of a staged CTA: issue(k) copies level k (or commits an empty group),
+// compute(k) reads the resident levels k .. k+LEAD.
+// NB - 1 - LEAD levels are in flight while level k is computed.
+template <int NB, int LEAD, class Issue, class Compute>
+__device__ __forceinline__ void staged_march(int k0, int k1, Issue&& issue, Compute&& compute) {
+  static_assert(NB >= LEAD + 2, "at least one level in flight beyond those a level reads");
+#pragma unroll 1
+  for (int t = 0; t < NB - 1; ++t) issue(k0 + t);
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    issue(k + NB - 1);  // into the buffer level k-1 left
+    cp_async_wait<NB - 1 - LEAD>();  // every level up to k + LEAD has landed
+    __syncthreads();
+    compute(k);
+    __syncthreads();  // the buffer of level k is refilled next
+  }
+}
+
+// laplace.h:39, FP32: one 34 x 34 box of `in` a level.
+struct laplace_staged_f32 {
+  static constexpr int NB = 3;
+  static constexpr int kCtasPerSm = 8;
+  struct Smem {
+    float in[NB][34 * 34];
+  };
+  static __device__ __forceinline__ void run(const uint3& blk, const float* __restrict__ in, float* __restrict__ out,
+                                             Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
+    auto issue = [&](int k) {
+      if (k < k1) stage_box<34, 34>(s.in[k % NB], in, (int64_t)k * d.sk, i0 - 1, j0 - 1, d.sj, i0 - 1, ie + 1, j0 - 1, je + 1);
+      cp_async_commit();
+    };
+    staged_march<NB, 0>(k0, k1, issue, [&](int k) {
+      const float* t = s.in[k % NB];
+      const int a = threadIdx.x, i = i0 + a;
+      if (i >= ie) return;
+      const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const int b = threadIdx.y + kTY * r, j = j0 + b;
+        if (j < je) {
+          const float* c = t + (b + 1) * 34 + (a + 1);
+          Acc<float> acc(c[-1]);
+          acc.add(c[1]);
+          acc.add(c[34]);
+          acc.add(c[-34]);
+          acc.add(-4.0f * c[0]);
+          out[kofs + i + (int64_t)j * d.sj] = acc.get();
+        }
+      }
+    });
+  }
+};
+
+// uvbke.h:66-71, FP32: uc on 32 x 33 (j0-1 ..), vc on 33 x 32 (i0-1 ..), cosa and rsina on the tile.
+struct uvbke_staged_f32 {
+  static constexpr int NB = 3;
+  static constexpr int kCtasPerSm = 4;
+  struct Smem {
+    float uc[NB][33 * 32], vc[NB][32 * 33], ca[NB][32 * 32], rs[NB][32 * 32];
+  };
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ ub, float* __restrict__ vb,
+                                             const float* __restrict__ uc, const float* __restrict__ vc,
+                                             const float* __restrict__ cosa, const float* __restrict__ rsina,
+                                             float dt5, float dt5_lo, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
+    auto issue = [&](int k) {
+      if (k < k1) {
+        const int64_t ko = (int64_t)k * d.sk;
+        const int q = k % NB;
+        stage_box<32, 33>(s.uc[q], uc, ko, i0, j0 - 1, d.sj, i0, ie, j0 - 1, je);
+        stage_box<33, 32>(s.vc[q], vc, ko, i0 - 1, j0, d.sj, i0 - 1, ie, j0, je);
+        stage_box<32, 32>(s.ca[q], cosa, ko, i0, j0, d.sj, i0, ie, j0, je);
+        stage_box<32, 32>(s.rs[q], rsina, ko, i0, j0, d.sj, i0, ie, j0, je);
+      }
+      cp_async_commit();
+    };
+    staged_march<NB, 0>(k0, k1, issue, [&](int k) {
+      const int q = k % NB;
+      const int a = threadIdx.x, i = i0 + a;
+      if (i >= ie) return;
+      const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const int b = threadIdx.y + kTY * r, j = j0 + b;
+        if (j < je) {
+          const float su = s.uc[q][b * 32 + a] + s.uc[q][(b + 1) * 32 + a];
+          const float sv = s.vc[q][b * 33 + a] + s.vc[q][b * 33 + a + 1];
+          const float ca = s.ca[q][b * 32 + a], rs = s.rs[q][b * 32 + a];
+          const int64_t o = kofs + i + (int64_t)j * d.sj;
+          ub[o] = uvbke_scale(su - (sv * ca), rs, dt5, dt5_lo);
+          vb[o] = uvbke_scale(sv - (su * ca), rs, dt5, dt5_lo);
+        }
+      }
+    });
+  }
+};
+
+// p_grad_c.h:90-97, FP32: uin, vin, rdxc, rdyc on the tile; delpc, gz, pkc on 33 x 33 from
+// (i0-1, j0-1); gz and pkc also at k+1 (the next level's buffer).
+struct p_grad_c_staged_f32 {
+  static constexpr int NB = 3;
+  static constexpr int kCtasPerSm = 2;
+  struct Level {
+    float uin[32 * 32], vin[32 * 32], rx[32 * 32], ry[32 * 32], dp[33 * 33], gz[33 * 33], pk[33 * 33];
+  };
+  struct Smem {
+    Level l[NB];
+  };
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uout, float* __restrict__ vout,
+                                             const float* __restrict__ uin, const float* __restrict__ vin,
+                                             const float* __restrict__ rdxc, const float* __restrict__ rdyc,
+                                             const float* __restrict__ delpc, const float* __restrict__ gz,
+                                             const float* __restrict__ pkc, float dt2, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
+    auto issue = [&](int k) {
+      if (k <= k1) {  // level k1 only for the fields read at k+1
+        const int64_t ko = (int64_t)k * d.sk;
+        Level& L = s.l[k % NB];
+        if (k < k1) {
+          stage_box<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<32, 32>(L.rx, rdxc, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<32, 32>(L.ry, rdyc, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<33, 33>(L.dp, delpc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
+        }
+        stage_box<33, 33>(L.gz, gz, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
+        stage_box<33, 33>(L.pk, pkc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
+      }
+      cp_async_commit();
+    };
+    staged_march<NB, 1>(k0, k1, issue, [&](int k) {
+      const Level& C = s.l[k % NB];
+      const Level& N = s.l[(k + 1) % NB];
+      const int a = threadIdx.x, i = i0 + a;
+      if (i >= ie) return;
+      const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const int b = threadIdx.y + kTY * r, j = j0 + b;
+        if (j < je) {
+          const int c = (b + 1) * 33 + (a + 1);  // (i, j) in the 33 x 33 boxes
+          const int p = b * 32 + a;              // (i, j) in the tile
+          const float wk = C.dp[c];
+          const float gz0 = C.gz[c], gz1 = N.gz[c], pk0 = C.pk[c], pk1 = N.pk[c];
+          const float fu = diff_dot(N.gz[c - 1], gz0, pk1, C.pk[c - 1], C.gz[c - 1], gz1, N.pk[c - 1], pk0);
+          const int64_t o = kofs + i + (int64_t)j * d.sj;
+          uout[o] = (C.uin[p] + (((dt2 * C.rx[p]) / (C.dp[c - 1] + wk)) * fu));
+          const float fv = diff_dot(N.gz[c - 33], gz0, pk1, C.pk[c - 33], C.gz[c - 33], gz1, N.pk[c - 33], pk0);
+          vout[o] = (C.vin[p] + (((dt2 * C.ry[p]) / (C.dp[c - 33] + wk)) * fv));
+        }
+      }
+    });
+  }
+};
+
+// nh_p_grad.h:121-141, FP32: uin, vin, rdx, rdy on the tile; gz, pp, pk3 on 33 x 33 from
+// (i0, j0) at k and k+1; wk1 on 33 x 33 at k.
+struct nh_p_grad_staged_f32 {
+  static constexpr int NB = 3;
+  static constexpr int kCtasPerSm = 2;
+  struct Level {
+    float uin[32 * 32], vin[32 * 32], rx[32 * 32], ry[32 * 32], gz[33 * 33], pp[33 * 33], pk[33 * 33], w1[33 * 33];
+  };
+  struct Smem {
+    Level l[NB];
+  };
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uout, float* __restrict__ vout,
+                                             const float* __restrict__ uin, const float* __restrict__ vin,
+                                             const float* __restrict__ rdx, const float* __restrict__ rdy,
+                                             const float* __restrict__ gz, const float* __restrict__ pp,
+                                             const float* __restrict__ pk3, const float* __restrict__ wk1, float dt,
+                                             Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
+    auto issue = [&](int k) {
+      if (k <= k1) {  // level k1 only for the fields read at k+1
+        const int64_t ko = (int64_t)k * d.sk;
+        Level& L = s.l[k % NB];
+        if (k < k1) {
+          stage_box<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<32, 32>(L.rx, rdx, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<32, 32>(L.ry, rdy, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_box<33, 33>(L.w1, wk1, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+        }
+        stage_box<33, 33>(L.gz, gz, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+        stage_box<33, 33>(L.pp, pp, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+        stage_box<33, 33>(L.pk, pk3, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+      }
+      cp_async_commit();
+    };
+    staged_march<NB, 1>(k0, k1, issue, [&](int k) {
+      const Level& C = s.l[k % NB];
+      const Level& N = s.l[(k + 1) % NB];
+      const int a = threadIdx.x, i = i0 + a;
+      if (i >= ie) return;
+      const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll 2
+      for (int r = 0; r < kRows; ++r) {
+        const int b = threadIdx.y + kTY * r, j = j0 + b;
+        if (j < je) {
+          const int c = b * 33 + a;  // (i, j) in the 33 x 33 boxes
+          const int p = b * 32 + a;  // (i, j) in the tile
+          const float pk0 = C.pk[c], pk1 = N.pk[c], gz0 = C.gz[c], gz1 = N.gz[c], pp0 = C.pp[c], pp1 = N.pp[c];
+          const float w1 = C.w1[c];
+          const float wk = pk1 - pk0;
+          const int64_t o = kofs + i + (int64_t)j * d.sj;
+          {  // u: neighbour i+1
+            const float pkx0 = C.pk[c + 1], pkx1 = N.pk[c + 1];
+            const float wkx = pkx1 - pkx0;
+            const float gx0 = C.gz[c + 1], gx1 = N.gz[c + 1];
+            const float fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
+            const float fp = diff_dot(gz1, gx0, N.pp[c + 1], pp0, gz0, gx1, pp1, C.pp[c + 1]);
+            const float du = ((dt / (wk + wkx)) * fk);
+            uout[o] = (((C.uin[p] + du) + ((dt / (w1 + C.w1[c + 1])) * fp)) * C.rx[p]);
+          }
+          {  // v: neighbour j+1
+            const float pky0 = C.pk[c + 33], pky1 = N.pk[c + 33];
+            const float wky = pky1 - pky0;
+            const float gy0 = C.gz[c + 33], gy1 = N.gz[c + 33];
+            const float fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
+            const float fp = diff_dot(gz1, gy0, N.pp[c + 33], pp0, gz0, gy1, pp1, C.pp[c + 33]);
+            const float dv = ((dt / (wk + wky)) * fk);
+            vout[o] = (((C.vin[p] + dv) + ((dt / (w1 + C.w1[c + 33])) * fp)) * C.ry[p]);
+          }
+        }
+      }
+    });
+  }
+};
+
+// Grid and k-levels a CTA of a staged body: about one wave of CTAs (stage.cuh).
+template <class S>
+void staged_launch_shape(const oeb_domain& dom, dim3* grid, int* kb) {
+  const int tiles = (int)(((dom.nx + kTI - 1) / kTI) * ((dom.ny + kTJ - 1) / kTJ));
+  *kb = tuned_kb(staged_kb(tiles, (int)dom.nz, S::kCtasPerSm));
+  *grid = tile_grid((int)dom.nx, (int)dom.ny, (int)dom.nz, kTI, kTJ, *kb);
+}
+
 template <class T>
 Dims make_dims(const oeb_domain& dom, const Grid<T>& g) {
   return Dims{(int)dom.nx, (int)dom.ny, (int)dom.nz, g.sj, g.sk};
@@ -314,6 +577,13 @@ oeb_status laplace_entry(const M3* in, const M3* out, const oeb_domain* dom, voi
   OEB_TRY(check_same_strides<T>({&gin, &gout}));
   OEB_TRY(check_no_alias({gout.lo, gout.hi}, {gin.lo, gin.hi}));
   OEB_RETURN_IF_VALIDATING();
+  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
+    dim3 grid;
+    int kb;
+    staged_launch_shape<laplace_staged_f32>(*dom, &grid, &kb);
+    return launch<laplace_staged_f32>(grid, sizeof(laplace_staged_f32::Smem), (cudaStream_t)stream, gin.origin,
+                                      gout.origin, make_dims(*dom, gin), kb);
+  }
   const int kb = tuned_kb(kKB);
   return launch<laplace_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gin.origin, gout.origin,
                                    make_dims(*dom, gin), kb);
@@ -335,6 +605,14 @@ oeb_status uvbke_entry(const M3* ub, const M3* vb, const M3* uc, const M3* vc, c
                          {guc.lo, guc.hi, gvc.lo, gvc.hi, gca.lo, gca.hi, grs.lo, grs.hi}));
   OEB_RETURN_IF_VALIDATING();
   const T dt5_hi = T(dt5), dt5_lo = T(dt5 - (double)dt5_hi);  // dt5_lo = 0 for FP64
+  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
+    dim3 grid;
+    int kb;
+    staged_launch_shape<uvbke_staged_f32>(*dom, &grid, &kb);
+    return launch<uvbke_staged_f32>(grid, sizeof(uvbke_staged_f32::Smem), (cudaStream_t)stream, gub.origin,
+                                    gvb.origin, guc.origin, gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo,
+                                    make_dims(*dom, gub), kb);
+  }
   const int kb = tuned_kb(kKB);
   return launch<uvbke_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gub.origin, gvb.origin, guc.origin,
                                  gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo, make_dims(*dom, gub), kb);
@@ -359,6 +637,14 @@ oeb_status p_grad_c_entry(const M3* uout, const M3* vout, const M3* uin, const M
   OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi}, {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo,
                                                         gry.hi, gdp.lo, gdp.hi, ggz.lo, ggz.hi, gpk.lo, gpk.hi}));
   OEB_RETURN_IF_VALIDATING();
+  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
+    dim3 grid;
+    int kb;
+    staged_launch_shape<p_grad_c_staged_f32>(*dom, &grid, &kb);
+    return launch<p_grad_c_staged_f32>(grid, sizeof(p_grad_c_staged_f32::Smem), (cudaStream_t)stream, gu.origin,
+                                       gv.origin, gui.origin, gvi.origin, grx.origin, gry.origin, gdp.origin,
+                                       ggz.origin, gpk.origin, dt2, make_dims(*dom, gu), kb);
+  }
   const int kb = tuned_kb(kKB);
   return launch<p_grad_c_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
                                     gvi.origin, grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin, dt2,
@@ -387,6 +673,14 @@ oeb_status nh_p_grad_entry(const M3* uout, const M3* vout, const M3* uin, const 
                          {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo, gry.hi, ggz.lo, ggz.hi, gpp.lo,
                           gpp.hi, gpk.lo, gpk.hi, gw1.lo, gw1.hi}));
   OEB_RETURN_IF_VALIDATING();
+  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
+    dim3 grid;
+    int kb;
+    staged_launch_shape<nh_p_grad_staged_f32>(*dom, &grid, &kb);
+    return launch<nh_p_grad_staged_f32>(grid, sizeof(nh_p_grad_staged_f32::Smem), (cudaStream_t)stream, gu.origin,
+                                        gv.origin, gui.origin, gvi.origin, grx.origin, gry.origin, ggz.origin,
+                                        gpp.origin, gpk.origin, gw1.origin, dt, make_dims(*dom, gu), kb);
+  }
   const int kb = tuned_kb(kKB);
   return launch<nh_p_grad_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
                                      gvi.origin, grx.origin, gry.origin, ggz.origin, gpp.origin, gpk.origin,

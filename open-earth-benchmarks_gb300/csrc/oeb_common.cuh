@@ -43,6 +43,16 @@ struct ValidateOnly {
     if (oeb::validating()) return OEB_OK; \
   } while (0)
 
+// While a HostInPlace guard is alive on this thread, the fields the entry points receive are
+// host memory the device reads in place (the host entry points' direct mode); the kernels that
+// stage their tiles with cp.async then keep to ordinary loads, which are what that mode was
+// measured and tested with.
+bool fields_in_host_memory();
+struct HostInPlace {
+  HostInPlace();
+  ~HostInPlace();
+};
+
 // Raises a kernel's dynamic shared-memory limit to `bytes` on the current device, once per
 // (kernel, device); thread-safe.
 oeb_status ensure_dyn_smem(const void* kernel, int bytes);

@@ -17,6 +17,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+import branch_flips
+
 pytestmark = pytest.mark.gpu
 
 H = 3
@@ -138,14 +140,31 @@ def test_dot_product_f32(pkg, fields, cuda, name):
     _dot_test(Case(pkg, fields, cuda, name, 128, 128, 80, seed=3, dtype=np.float32), 1e-5)
 
 
-def _compare_fd(case: Case, fd: dict, dy: dict, tol=1e-6, max_flip_fraction=1e-4):
+def _flip_cells(case: Case, xp: dict, xm: dict):
+    """hdiffsa: the output cells whose limiter flags differ between the two ends of the step
+    (tests/branch_flips.py); None for the other stencils, whose flips are counted."""
+    if case.name != "hdiffsa":
+        return None
+    ks = slice(H, H + case.nz)
+    fp = branch_flips.hdiffsa_flags(xp["in"][ks], case.x["crlato"], case.x["crlatu"], case.nx, case.ny, H)
+    fm = branch_flips.hdiffsa_flags(xm["in"][ks], case.x["crlato"], case.x["crlatu"], case.nx, case.ny, H)
+    return branch_flips.hdiffsa_affected(fp, fm, case.nx, case.ny)
+
+
+def _compare_fd(case: Case, fd: dict, dy: dict, tol=1e-6, max_flip_fraction=1e-4, flips=None):
     """|FD - TL| <= tol * max|TL| on every cell of every output box, except cells where a
-    branch flips within the step (at most max_flip_fraction of the box, plus 2)."""
+    branch flips within the step: those in `flips` where they are known (hdiffsa's
+    discontinuous limiter), else at most max_flip_fraction of the box, plus 2."""
     for a in case.spec.by_role("out3"):
         t = case.sem_box(a.name, dy[a.name])
         f = case.sem_box(a.name, fd[a.name])
         scale = max(float(np.max(np.abs(t))), 1e-300)
         bad = np.abs(f - t) > tol * scale
+        if flips is not None:
+            outside = int(np.count_nonzero(bad & ~flips))
+            assert outside == 0, "%s.%s: TL differs from central differences on %d cells where no branch flips" % (
+                case.name, a.name, outside)
+            continue
         allowed = int(max_flip_fraction * t.size) + 2
         assert np.count_nonzero(bad) <= allowed, (
             "%s.%s: TL differs from central differences on %d of %d cells (max rel %.3g)" %
@@ -160,7 +179,7 @@ def test_tl_vs_central_differences_gpu(pkg, fields, cuda, name):
     xm = {k: (v - eps * case.dx[k] if k in case.dx else v) for k, v in case.x.items()}
     fp, fm = case.forward(xp), case.forward(xm)
     fd = {k: (fp[k] - fm[k]) / (2 * eps) for k in fp}
-    _compare_fd(case, fd, case.tl())
+    _compare_fd(case, fd, case.tl(), flips=_flip_cells(case, xp, xm))
 
 
 @pytest.mark.parametrize("name", ADJ)
@@ -179,7 +198,7 @@ def test_tl_vs_central_differences_oracle(pkg, fields, orc, cuda, name):
     xm = {k: (v - eps * case.dx[k] if k in case.dx else v) for k, v in case.x.items()}
     fp, fm = oracle_forward(xp), oracle_forward(xm)
     fd = {k: (fp[k] - fm[k]) / (2 * eps) for k in fp}
-    _compare_fd(case, fd, case.tl())
+    _compare_fd(case, fd, case.tl(), flips=_flip_cells(case, xp, xm))
 
 
 @pytest.mark.parametrize("name", ADJ)
