@@ -326,8 +326,9 @@ __device__ __forceinline__ void staged_march(int k0, int k1, Issue&& issue, Comp
 struct laplace_staged_f32 {
   static constexpr int NB = 3;
   static constexpr int kCtasPerSm = 8;
+  using B = RowBox<34, 34>;
   struct Smem {
-    float in[NB][34 * 34];
+    float in[NB][B::N];
   };
   static __device__ __forceinline__ void run(const uint3& blk, const float* __restrict__ in, float* __restrict__ out,
                                              Dims d, int kb) {
@@ -337,24 +338,24 @@ struct laplace_staged_f32 {
     const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
     const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
     auto issue = [&](int k) {
-      if (k < k1) stage_box<34, 34>(s.in[k % NB], in, (int64_t)k * d.sk, i0 - 1, j0 - 1, d.sj, i0 - 1, ie + 1, j0 - 1, je + 1);
+      if (k < k1)
+        stage_rows<34, 34>(s.in[k % NB], in, (int64_t)k * d.sk, i0 - 1, j0 - 1, d.sj, i0 - 1, ie + 1, j0 - 1, je + 1);
       cp_async_commit();
     };
     staged_march<NB, 0>(k0, k1, issue, [&](int k) {
-      const float* t = s.in[k % NB];
+      const int64_t kofs = (int64_t)k * d.sk;
+      const auto t = row_view<34, 34>(s.in[k % NB], in, kofs, i0 - 1, j0 - 1, d.sj);
       const int a = threadIdx.x, i = i0 + a;
       if (i >= ie) return;
-      const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         const int b = threadIdx.y + kTY * r, j = j0 + b;
         if (j < je) {
-          const float* c = t + (b + 1) * 34 + (a + 1);
-          Acc<float> acc(c[-1]);
-          acc.add(c[1]);
-          acc.add(c[34]);
-          acc.add(c[-34]);
-          acc.add(-4.0f * c[0]);
+          Acc<float> acc(t(a, b + 1));
+          acc.add(t(a + 2, b + 1));
+          acc.add(t(a + 1, b + 2));
+          acc.add(t(a + 1, b));
+          acc.add(-4.0f * t(a + 1, b + 1));
           out[kofs + i + (int64_t)j * d.sj] = acc.get();
         }
       }
@@ -362,12 +363,16 @@ struct laplace_staged_f32 {
   }
 };
 
-// uvbke.h:66-71, FP32: uc on 32 x 33 (j0-1 ..), vc on 33 x 32 (i0-1 ..), cosa and rsina on the tile.
+// uvbke.h:66-71, FP32: uc on 32 x 33 (from j0-1), vc on 33 x 32 (from i0-1), cosa and rsina on
+// the tile.
 struct uvbke_staged_f32 {
   static constexpr int NB = 3;
   static constexpr int kCtasPerSm = 4;
+  struct Level {
+    float uc[RowBox<32, 33>::N], vc[RowBox<33, 32>::N], ca[RowBox<32, 32>::N], rs[RowBox<32, 32>::N];
+  };
   struct Smem {
-    float uc[NB][33 * 32], vc[NB][32 * 33], ca[NB][32 * 32], rs[NB][32 * 32];
+    Level l[NB];
   };
   static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ ub, float* __restrict__ vb,
                                              const float* __restrict__ uc, const float* __restrict__ vc,
@@ -381,26 +386,30 @@ struct uvbke_staged_f32 {
     auto issue = [&](int k) {
       if (k < k1) {
         const int64_t ko = (int64_t)k * d.sk;
-        const int q = k % NB;
-        stage_box<32, 33>(s.uc[q], uc, ko, i0, j0 - 1, d.sj, i0, ie, j0 - 1, je);
-        stage_box<33, 32>(s.vc[q], vc, ko, i0 - 1, j0, d.sj, i0 - 1, ie, j0, je);
-        stage_box<32, 32>(s.ca[q], cosa, ko, i0, j0, d.sj, i0, ie, j0, je);
-        stage_box<32, 32>(s.rs[q], rsina, ko, i0, j0, d.sj, i0, ie, j0, je);
+        Level& L = s.l[k % NB];
+        stage_rows<32, 33>(L.uc, uc, ko, i0, j0 - 1, d.sj, i0, ie, j0 - 1, je);
+        stage_rows<33, 32>(L.vc, vc, ko, i0 - 1, j0, d.sj, i0 - 1, ie, j0, je);
+        stage_rows<32, 32>(L.ca, cosa, ko, i0, j0, d.sj, i0, ie, j0, je);
+        stage_rows<32, 32>(L.rs, rsina, ko, i0, j0, d.sj, i0, ie, j0, je);
       }
       cp_async_commit();
     };
     staged_march<NB, 0>(k0, k1, issue, [&](int k) {
-      const int q = k % NB;
+      const int64_t kofs = (int64_t)k * d.sk;
+      const Level& L = s.l[k % NB];
+      const auto tu = row_view<32, 33>(L.uc, uc, kofs, i0, j0 - 1, d.sj);
+      const auto tv = row_view<33, 32>(L.vc, vc, kofs, i0 - 1, j0, d.sj);
+      const auto tc = row_view<32, 32>(L.ca, cosa, kofs, i0, j0, d.sj);
+      const auto tr = row_view<32, 32>(L.rs, rsina, kofs, i0, j0, d.sj);
       const int a = threadIdx.x, i = i0 + a;
       if (i >= ie) return;
-      const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         const int b = threadIdx.y + kTY * r, j = j0 + b;
         if (j < je) {
-          const float su = s.uc[q][b * 32 + a] + s.uc[q][(b + 1) * 32 + a];
-          const float sv = s.vc[q][b * 33 + a] + s.vc[q][b * 33 + a + 1];
-          const float ca = s.ca[q][b * 32 + a], rs = s.rs[q][b * 32 + a];
+          const float su = tu(a, b) + tu(a, b + 1);
+          const float sv = tv(a, b) + tv(a + 1, b);
+          const float ca = tc(a, b), rs = tr(a, b);
           const int64_t o = kofs + i + (int64_t)j * d.sj;
           ub[o] = uvbke_scale(su - (sv * ca), rs, dt5, dt5_lo);
           vb[o] = uvbke_scale(sv - (su * ca), rs, dt5, dt5_lo);
@@ -415,8 +424,10 @@ struct uvbke_staged_f32 {
 struct p_grad_c_staged_f32 {
   static constexpr int NB = 3;
   static constexpr int kCtasPerSm = 2;
+  using P = RowBox<32, 32>;
+  using Q = RowBox<33, 33>;
   struct Level {
-    float uin[32 * 32], vin[32 * 32], rx[32 * 32], ry[32 * 32], dp[33 * 33], gz[33 * 33], pk[33 * 33];
+    float uin[P::N], vin[P::N], rx[P::N], ry[P::N], dp[Q::N], gz[Q::N], pk[Q::N];
   };
   struct Smem {
     Level l[NB];
@@ -436,36 +447,44 @@ struct p_grad_c_staged_f32 {
         const int64_t ko = (int64_t)k * d.sk;
         Level& L = s.l[k % NB];
         if (k < k1) {
-          stage_box<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<32, 32>(L.rx, rdxc, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<32, 32>(L.ry, rdyc, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<33, 33>(L.dp, delpc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
+          stage_rows<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<32, 32>(L.rx, rdxc, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<32, 32>(L.ry, rdyc, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<33, 33>(L.dp, delpc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
         }
-        stage_box<33, 33>(L.gz, gz, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
-        stage_box<33, 33>(L.pk, pkc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
+        stage_rows<33, 33>(L.gz, gz, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
+        stage_rows<33, 33>(L.pk, pkc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
       }
       cp_async_commit();
     };
     staged_march<NB, 1>(k0, k1, issue, [&](int k) {
+      const int64_t kofs = (int64_t)k * d.sk, kofs1 = kofs + d.sk;
       const Level& C = s.l[k % NB];
       const Level& N = s.l[(k + 1) % NB];
+      const auto uin_ = row_view<32, 32>(C.uin, uin, kofs, i0, j0, d.sj);
+      const auto vin_ = row_view<32, 32>(C.vin, vin, kofs, i0, j0, d.sj);
+      const auto rx = row_view<32, 32>(C.rx, rdxc, kofs, i0, j0, d.sj);
+      const auto ry = row_view<32, 32>(C.ry, rdyc, kofs, i0, j0, d.sj);
+      const auto dp = row_view<33, 33>(C.dp, delpc, kofs, i0 - 1, j0 - 1, d.sj);
+      const auto g0 = row_view<33, 33>(C.gz, gz, kofs, i0 - 1, j0 - 1, d.sj);
+      const auto g1 = row_view<33, 33>(N.gz, gz, kofs1, i0 - 1, j0 - 1, d.sj);
+      const auto p0 = row_view<33, 33>(C.pk, pkc, kofs, i0 - 1, j0 - 1, d.sj);
+      const auto p1 = row_view<33, 33>(N.pk, pkc, kofs1, i0 - 1, j0 - 1, d.sj);
       const int a = threadIdx.x, i = i0 + a;
       if (i >= ie) return;
-      const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         const int b = threadIdx.y + kTY * r, j = j0 + b;
         if (j < je) {
-          const int c = (b + 1) * 33 + (a + 1);  // (i, j) in the 33 x 33 boxes
-          const int p = b * 32 + a;              // (i, j) in the tile
-          const float wk = C.dp[c];
-          const float gz0 = C.gz[c], gz1 = N.gz[c], pk0 = C.pk[c], pk1 = N.pk[c];
-          const float fu = diff_dot(N.gz[c - 1], gz0, pk1, C.pk[c - 1], C.gz[c - 1], gz1, N.pk[c - 1], pk0);
+          // (i, j) is (a+1, b+1) in the 33 x 33 boxes and (a, b) in the tile's
+          const float wk = dp(a + 1, b + 1);
+          const float gz0 = g0(a + 1, b + 1), gz1 = g1(a + 1, b + 1), pk0 = p0(a + 1, b + 1), pk1 = p1(a + 1, b + 1);
+          const float fu = diff_dot(g1(a, b + 1), gz0, pk1, p0(a, b + 1), g0(a, b + 1), gz1, p1(a, b + 1), pk0);
           const int64_t o = kofs + i + (int64_t)j * d.sj;
-          uout[o] = (C.uin[p] + (((dt2 * C.rx[p]) / (C.dp[c - 1] + wk)) * fu));
-          const float fv = diff_dot(N.gz[c - 33], gz0, pk1, C.pk[c - 33], C.gz[c - 33], gz1, N.pk[c - 33], pk0);
-          vout[o] = (C.vin[p] + (((dt2 * C.ry[p]) / (C.dp[c - 33] + wk)) * fv));
+          uout[o] = (uin_(a, b) + (((dt2 * rx(a, b)) / (dp(a, b + 1) + wk)) * fu));
+          const float fv = diff_dot(g1(a + 1, b), gz0, pk1, p0(a + 1, b), g0(a + 1, b), gz1, p1(a + 1, b), pk0);
+          vout[o] = (vin_(a, b) + (((dt2 * ry(a, b)) / (dp(a + 1, b) + wk)) * fv));
         }
       }
     });
@@ -477,8 +496,10 @@ struct p_grad_c_staged_f32 {
 struct nh_p_grad_staged_f32 {
   static constexpr int NB = 3;
   static constexpr int kCtasPerSm = 2;
+  using P = RowBox<32, 32>;
+  using Q = RowBox<33, 33>;
   struct Level {
-    float uin[32 * 32], vin[32 * 32], rx[32 * 32], ry[32 * 32], gz[33 * 33], pp[33 * 33], pk[33 * 33], w1[33 * 33];
+    float uin[P::N], vin[P::N], rx[P::N], ry[P::N], gz[Q::N], pp[Q::N], pk[Q::N], w1[Q::N];
   };
   struct Smem {
     Level l[NB];
@@ -499,51 +520,60 @@ struct nh_p_grad_staged_f32 {
         const int64_t ko = (int64_t)k * d.sk;
         Level& L = s.l[k % NB];
         if (k < k1) {
-          stage_box<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<32, 32>(L.rx, rdx, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<32, 32>(L.ry, rdy, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_box<33, 33>(L.w1, wk1, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+          stage_rows<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<32, 32>(L.rx, rdx, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<32, 32>(L.ry, rdy, ko, i0, j0, d.sj, i0, ie, j0, je);
+          stage_rows<33, 33>(L.w1, wk1, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
         }
-        stage_box<33, 33>(L.gz, gz, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
-        stage_box<33, 33>(L.pp, pp, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
-        stage_box<33, 33>(L.pk, pk3, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+        stage_rows<33, 33>(L.gz, gz, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+        stage_rows<33, 33>(L.pp, pp, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
+        stage_rows<33, 33>(L.pk, pk3, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
       }
       cp_async_commit();
     };
     staged_march<NB, 1>(k0, k1, issue, [&](int k) {
+      const int64_t kofs = (int64_t)k * d.sk, kofs1 = kofs + d.sk;
       const Level& C = s.l[k % NB];
       const Level& N = s.l[(k + 1) % NB];
+      const auto uin_ = row_view<32, 32>(C.uin, uin, kofs, i0, j0, d.sj);
+      const auto vin_ = row_view<32, 32>(C.vin, vin, kofs, i0, j0, d.sj);
+      const auto rx = row_view<32, 32>(C.rx, rdx, kofs, i0, j0, d.sj);
+      const auto ry = row_view<32, 32>(C.ry, rdy, kofs, i0, j0, d.sj);
+      const auto w = row_view<33, 33>(C.w1, wk1, kofs, i0, j0, d.sj);
+      const auto g0 = row_view<33, 33>(C.gz, gz, kofs, i0, j0, d.sj);
+      const auto g1 = row_view<33, 33>(N.gz, gz, kofs1, i0, j0, d.sj);
+      const auto q0 = row_view<33, 33>(C.pp, pp, kofs, i0, j0, d.sj);
+      const auto q1 = row_view<33, 33>(N.pp, pp, kofs1, i0, j0, d.sj);
+      const auto p0 = row_view<33, 33>(C.pk, pk3, kofs, i0, j0, d.sj);
+      const auto p1 = row_view<33, 33>(N.pk, pk3, kofs1, i0, j0, d.sj);
       const int a = threadIdx.x, i = i0 + a;
       if (i >= ie) return;
-      const int64_t kofs = (int64_t)k * d.sk;
 #pragma unroll 2
       for (int r = 0; r < kRows; ++r) {
         const int b = threadIdx.y + kTY * r, j = j0 + b;
         if (j < je) {
-          const int c = b * 33 + a;  // (i, j) in the 33 x 33 boxes
-          const int p = b * 32 + a;  // (i, j) in the tile
-          const float pk0 = C.pk[c], pk1 = N.pk[c], gz0 = C.gz[c], gz1 = N.gz[c], pp0 = C.pp[c], pp1 = N.pp[c];
-          const float w1 = C.w1[c];
+          const float pk0 = p0(a, b), pk1 = p1(a, b), gz0 = g0(a, b), gz1 = g1(a, b), pp0 = q0(a, b), pp1 = q1(a, b);
+          const float w1 = w(a, b);
           const float wk = pk1 - pk0;
           const int64_t o = kofs + i + (int64_t)j * d.sj;
           {  // u: neighbour i+1
-            const float pkx0 = C.pk[c + 1], pkx1 = N.pk[c + 1];
+            const float pkx0 = p0(a + 1, b), pkx1 = p1(a + 1, b);
             const float wkx = pkx1 - pkx0;
-            const float gx0 = C.gz[c + 1], gx1 = N.gz[c + 1];
+            const float gx0 = g0(a + 1, b), gx1 = g1(a + 1, b);
             const float fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
-            const float fp = diff_dot(gz1, gx0, N.pp[c + 1], pp0, gz0, gx1, pp1, C.pp[c + 1]);
+            const float fp = diff_dot(gz1, gx0, q1(a + 1, b), pp0, gz0, gx1, pp1, q0(a + 1, b));
             const float du = ((dt / (wk + wkx)) * fk);
-            uout[o] = (((C.uin[p] + du) + ((dt / (w1 + C.w1[c + 1])) * fp)) * C.rx[p]);
+            uout[o] = (((uin_(a, b) + du) + ((dt / (w1 + w(a + 1, b))) * fp)) * rx(a, b));
           }
           {  // v: neighbour j+1
-            const float pky0 = C.pk[c + 33], pky1 = N.pk[c + 33];
+            const float pky0 = p0(a, b + 1), pky1 = p1(a, b + 1);
             const float wky = pky1 - pky0;
-            const float gy0 = C.gz[c + 33], gy1 = N.gz[c + 33];
+            const float gy0 = g0(a, b + 1), gy1 = g1(a, b + 1);
             const float fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
-            const float fp = diff_dot(gz1, gy0, N.pp[c + 33], pp0, gz0, gy1, pp1, C.pp[c + 33]);
+            const float fp = diff_dot(gz1, gy0, q1(a, b + 1), pp0, gz0, gy1, pp1, q0(a, b + 1));
             const float dv = ((dt / (wk + wky)) * fk);
-            vout[o] = (((C.vin[p] + dv) + ((dt / (w1 + C.w1[c + 33])) * fp)) * C.ry[p]);
+            vout[o] = (((vin_(a, b) + dv) + ((dt / (w1 + w(a, b + 1))) * fp)) * ry(a, b));
           }
         }
       }
