@@ -74,14 +74,12 @@ struct laplace_kernel {
     const int64_t sj = d.sj;
     for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int) {
       if constexpr (Prec<T>::kCompensated) {
-        // -4 in nearly cancels the neighbour sum on smooth fields: sum all five terms
-        // compensated (-4 in is exact)
-        Acc<T> acc(ld(in + o - 1));
-        acc.add(ld(in + o + 1));
-        acc.add(ld(in + o + sj));
-        acc.add(ld(in + o - sj));
-        acc.add(T(-4.0) * ld(in + o));
-        out[o] = acc.get();
+        // -4 in nearly cancels the neighbour sum on smooth fields.  FP32 sums the four
+        // neighbour differences instead: each is exact where the neighbours lie within a factor
+        // 2 (Sterbenz), and the sum then cancels no more than the differences themselves --
+        // about the accuracy of a compensated five-term sum, in 7 operations instead of 30.
+        const T c = ld(in + o);
+        out[o] = ((ld(in + o - 1) - c) + (ld(in + o + 1) - c)) + ((ld(in + o + sj) - c) + (ld(in + o - sj) - c));
       } else {
         out[o] = -scale2<2>(ld(in + o)) + ((ld(in + o - 1) + ld(in + o + 1)) + (ld(in + o + sj) + ld(in + o - sj)));
       }
@@ -298,15 +296,19 @@ struct hadv_kernel {
 constexpr int kKB = 1;  // k-levels per CTA (one: the most CTAs, which hides FP64 and load latency best)
 
 // ---- FP32 forms staged through shared memory (stage.cuh) -----------------------------
-// A CTA owns a 32 x 32 tile and the k-levels [k0, k0+kb); each level's input boxes are copied
-// into a ring of NB shared-memory buffers by cp.async, ahead of the level being computed.  The
-// arithmetic is the FP32 kernels' above, in the same order; only where the operands come from
-// changes.  Stencils that read level k+1 (p_grad_c, nh_p_grad) compute level k once levels k
-// and k+1 are resident, with one more level in flight; laplace and uvbke keep two in flight.
+// laplace and nh_p_grad: a CTA owns a 32 x 32 tile and the k-levels [k0, k0+kb); the input
+// boxes read at neighbouring points are copied level by level into a ring of NB shared-memory
+// buffers by cp.async, ahead of the level being computed.  nh_p_grad reads level k+1 as well,
+// so it computes level k once levels k and k+1 are resident, with one more level in flight;
+// laplace keeps two levels in flight.  Measured at 256 x 256 x 80 (each stencil alone, average
+// over back-to-back launches): laplace 0.38 -> 0.49 of the HBM copy rate, nh_p_grad 0.32 ->
+// 0.42.  uvbke and p_grad_c measured faster as the plain kernels above (0.69 and 0.60 against
+// 0.62 and 0.48 staged) and keep them: their loads are all independent, and eight CTAs an SM
+// of plain loads keep more bytes in flight than the two or four CTAs their staged rings allowed.
 
 // Marches the levels of a staged CTA: issue(k) copies level k (or commits an empty group),
-// compute(k) reads the resident levels k .. k+LEAD.
-// NB - 1 - LEAD levels are in flight while level k is computed.
+// compute(k) reads the resident levels k .. k+LEAD; NB - 1 - LEAD levels are in flight while
+// level k is computed.
 template <int NB, int LEAD, class Issue, class Compute>
 __device__ __forceinline__ void staged_march(int k0, int k1, Issue&& issue, Compute&& compute) {
   static_assert(NB >= LEAD + 2, "at least one level in flight beyond those a level reads");
@@ -322,7 +324,8 @@ __device__ __forceinline__ void staged_march(int k0, int k1, Issue&& issue, Comp
   }
 }
 
-// laplace.h:39, FP32: one 34 x 34 box of `in` a level.
+// laplace.h:39, FP32: one 34 x 34 box of `in` a level, summed in the difference form of
+// laplace_kernel above.
 struct laplace_staged_f32 {
   static constexpr int NB = 3;
   static constexpr int kCtasPerSm = 8;
@@ -344,162 +347,55 @@ struct laplace_staged_f32 {
     };
     staged_march<NB, 0>(k0, k1, issue, [&](int k) {
       const int64_t kofs = (int64_t)k * d.sk;
-      const auto t = row_view<34, 34>(s.in[k % NB], in, kofs, i0 - 1, j0 - 1, d.sj);
+      const RowMis mis = row_mis(in, kofs, i0 - 1, j0 - 1, d.sj);
+      const float* t = s.in[k % NB];
       const int a = threadIdx.x, i = i0 + a;
       if (i >= ie) return;
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         const int b = threadIdx.y + kTY * r, j = j0 + b;
         if (j < je) {
-          Acc<float> acc(t(a, b + 1));
-          acc.add(t(a + 2, b + 1));
-          acc.add(t(a + 1, b + 2));
-          acc.add(t(a + 1, b));
-          acc.add(-4.0f * t(a + 1, b + 1));
-          out[kofs + i + (int64_t)j * d.sj] = acc.get();
+          const float* up = t + b * B::SW + mis(b) + a;  // row j-1 from cell i-1
+          const float* mid = t + (b + 1) * B::SW + mis(b + 1) + a;
+          const float* dn = t + (b + 2) * B::SW + mis(b + 2) + a;
+          const float c = mid[1];
+          out[kofs + i + (int64_t)j * d.sj] = ((mid[0] - c) + (mid[2] - c)) + ((dn[1] - c) + (up[1] - c));
         }
       }
     });
   }
 };
 
-// uvbke.h:66-71, FP32: uc on 32 x 33 (from j0-1), vc on 33 x 32 (from i0-1), cosa and rsina on
-// the tile.
-struct uvbke_staged_f32 {
-  static constexpr int NB = 3;
-  static constexpr int kCtasPerSm = 4;
-  struct Level {
-    float uc[RowBox<32, 33>::N], vc[RowBox<33, 32>::N], ca[RowBox<32, 32>::N], rs[RowBox<32, 32>::N];
-  };
-  struct Smem {
-    Level l[NB];
-  };
-  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ ub, float* __restrict__ vb,
-                                             const float* __restrict__ uc, const float* __restrict__ vc,
-                                             const float* __restrict__ cosa, const float* __restrict__ rsina,
-                                             float dt5, float dt5_lo, Dims d, int kb) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
-    const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
-    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
-    const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
-    auto issue = [&](int k) {
-      if (k < k1) {
-        const int64_t ko = (int64_t)k * d.sk;
-        Level& L = s.l[k % NB];
-        stage_rows<32, 33>(L.uc, uc, ko, i0, j0 - 1, d.sj, i0, ie, j0 - 1, je);
-        stage_rows<33, 32>(L.vc, vc, ko, i0 - 1, j0, d.sj, i0 - 1, ie, j0, je);
-        stage_rows<32, 32>(L.ca, cosa, ko, i0, j0, d.sj, i0, ie, j0, je);
-        stage_rows<32, 32>(L.rs, rsina, ko, i0, j0, d.sj, i0, ie, j0, je);
-      }
-      cp_async_commit();
-    };
-    staged_march<NB, 0>(k0, k1, issue, [&](int k) {
-      const int64_t kofs = (int64_t)k * d.sk;
-      const Level& L = s.l[k % NB];
-      const auto tu = row_view<32, 33>(L.uc, uc, kofs, i0, j0 - 1, d.sj);
-      const auto tv = row_view<33, 32>(L.vc, vc, kofs, i0 - 1, j0, d.sj);
-      const auto tc = row_view<32, 32>(L.ca, cosa, kofs, i0, j0, d.sj);
-      const auto tr = row_view<32, 32>(L.rs, rsina, kofs, i0, j0, d.sj);
-      const int a = threadIdx.x, i = i0 + a;
-      if (i >= ie) return;
+// The four fields a staged nh_p_grad thread reads at its own points only, loaded into registers
+// one level ahead of the level it computes (the loads of level k+1 are in flight while level k
+// is computed).
+struct PointRegs {
+  float v[4][kRows];
+  __device__ __forceinline__ void fetch(const float* __restrict__ f0, const float* __restrict__ f1,
+                                        const float* __restrict__ f2, const float* __restrict__ f3, int64_t kofs,
+                                        int i, int j0, int je, int64_t sj) {
 #pragma unroll
-      for (int r = 0; r < kRows; ++r) {
-        const int b = threadIdx.y + kTY * r, j = j0 + b;
-        if (j < je) {
-          const float su = tu(a, b) + tu(a, b + 1);
-          const float sv = tv(a, b) + tv(a + 1, b);
-          const float ca = tc(a, b), rs = tr(a, b);
-          const int64_t o = kofs + i + (int64_t)j * d.sj;
-          ub[o] = uvbke_scale(su - (sv * ca), rs, dt5, dt5_lo);
-          vb[o] = uvbke_scale(sv - (su * ca), rs, dt5, dt5_lo);
-        }
-      }
-    });
+    for (int r = 0; r < kRows; ++r) {
+      const int j = j0 + (int)threadIdx.y + kTY * r;
+      const bool ok = j < je;
+      const int64_t o = kofs + i + (int64_t)(ok ? j : j0) * sj;
+      v[0][r] = ok ? ld(f0 + o) : 0.f;
+      v[1][r] = ok ? ld(f1 + o) : 0.f;
+      v[2][r] = ok ? ld(f2 + o) : 0.f;
+      v[3][r] = ok ? ld(f3 + o) : 0.f;
+    }
   }
 };
 
-// p_grad_c.h:90-97, FP32: uin, vin, rdxc, rdyc on the tile; delpc, gz, pkc on 33 x 33 from
-// (i0-1, j0-1); gz and pkc also at k+1 (the next level's buffer).
-struct p_grad_c_staged_f32 {
-  static constexpr int NB = 3;
-  static constexpr int kCtasPerSm = 2;
-  using P = RowBox<32, 32>;
-  using Q = RowBox<33, 33>;
-  struct Level {
-    float uin[P::N], vin[P::N], rx[P::N], ry[P::N], dp[Q::N], gz[Q::N], pk[Q::N];
-  };
-  struct Smem {
-    Level l[NB];
-  };
-  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uout, float* __restrict__ vout,
-                                             const float* __restrict__ uin, const float* __restrict__ vin,
-                                             const float* __restrict__ rdxc, const float* __restrict__ rdyc,
-                                             const float* __restrict__ delpc, const float* __restrict__ gz,
-                                             const float* __restrict__ pkc, float dt2, Dims d, int kb) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
-    const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
-    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
-    const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
-    auto issue = [&](int k) {
-      if (k <= k1) {  // level k1 only for the fields read at k+1
-        const int64_t ko = (int64_t)k * d.sk;
-        Level& L = s.l[k % NB];
-        if (k < k1) {
-          stage_rows<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<32, 32>(L.rx, rdxc, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<32, 32>(L.ry, rdyc, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<33, 33>(L.dp, delpc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
-        }
-        stage_rows<33, 33>(L.gz, gz, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
-        stage_rows<33, 33>(L.pk, pkc, ko, i0 - 1, j0 - 1, d.sj, i0 - 1, ie, j0 - 1, je);
-      }
-      cp_async_commit();
-    };
-    staged_march<NB, 1>(k0, k1, issue, [&](int k) {
-      const int64_t kofs = (int64_t)k * d.sk, kofs1 = kofs + d.sk;
-      const Level& C = s.l[k % NB];
-      const Level& N = s.l[(k + 1) % NB];
-      const auto uin_ = row_view<32, 32>(C.uin, uin, kofs, i0, j0, d.sj);
-      const auto vin_ = row_view<32, 32>(C.vin, vin, kofs, i0, j0, d.sj);
-      const auto rx = row_view<32, 32>(C.rx, rdxc, kofs, i0, j0, d.sj);
-      const auto ry = row_view<32, 32>(C.ry, rdyc, kofs, i0, j0, d.sj);
-      const auto dp = row_view<33, 33>(C.dp, delpc, kofs, i0 - 1, j0 - 1, d.sj);
-      const auto g0 = row_view<33, 33>(C.gz, gz, kofs, i0 - 1, j0 - 1, d.sj);
-      const auto g1 = row_view<33, 33>(N.gz, gz, kofs1, i0 - 1, j0 - 1, d.sj);
-      const auto p0 = row_view<33, 33>(C.pk, pkc, kofs, i0 - 1, j0 - 1, d.sj);
-      const auto p1 = row_view<33, 33>(N.pk, pkc, kofs1, i0 - 1, j0 - 1, d.sj);
-      const int a = threadIdx.x, i = i0 + a;
-      if (i >= ie) return;
-#pragma unroll
-      for (int r = 0; r < kRows; ++r) {
-        const int b = threadIdx.y + kTY * r, j = j0 + b;
-        if (j < je) {
-          // (i, j) is (a+1, b+1) in the 33 x 33 boxes and (a, b) in the tile's
-          const float wk = dp(a + 1, b + 1);
-          const float gz0 = g0(a + 1, b + 1), gz1 = g1(a + 1, b + 1), pk0 = p0(a + 1, b + 1), pk1 = p1(a + 1, b + 1);
-          const float fu = diff_dot(g1(a, b + 1), gz0, pk1, p0(a, b + 1), g0(a, b + 1), gz1, p1(a, b + 1), pk0);
-          const int64_t o = kofs + i + (int64_t)j * d.sj;
-          uout[o] = (uin_(a, b) + (((dt2 * rx(a, b)) / (dp(a, b + 1) + wk)) * fu));
-          const float fv = diff_dot(g1(a + 1, b), gz0, pk1, p0(a + 1, b), g0(a + 1, b), gz1, p1(a + 1, b), pk0);
-          vout[o] = (vin_(a, b) + (((dt2 * ry(a, b)) / (dp(a + 1, b) + wk)) * fv));
-        }
-      }
-    });
-  }
-};
-
-// nh_p_grad.h:121-141, FP32: uin, vin, rdx, rdy on the tile; gz, pp, pk3 on 33 x 33 from
-// (i0, j0) at k and k+1; wk1 on 33 x 33 at k.
+// nh_p_grad.h:121-141, FP32: gz, pp, pk3 staged on 33 x 33 from (i0, j0) at k and k+1, wk1 at
+// k; uin, vin, rdx, rdy in registers a level ahead.
 struct nh_p_grad_staged_f32 {
   static constexpr int NB = 3;
-  static constexpr int kCtasPerSm = 2;
-  using P = RowBox<32, 32>;
+  static constexpr int kCtasPerSm = 3;
+  static constexpr int kMinCtas = 3;  // registers for three CTAs an SM
   using Q = RowBox<33, 33>;
   struct Level {
-    float uin[P::N], vin[P::N], rx[P::N], ry[P::N], gz[Q::N], pp[Q::N], pk[Q::N], w1[Q::N];
+    float gz[Q::N], pp[Q::N], pk[Q::N], w1[Q::N];
   };
   struct Smem {
     Level l[NB];
@@ -515,68 +411,77 @@ struct nh_p_grad_staged_f32 {
     const int i0 = blk.x * kTI, j0 = blk.y * kTJ;
     const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
     const int ie = min(i0 + kTI, d.nx), je = min(j0 + kTJ, d.ny);
+    const int a = threadIdx.x, i = i0 + a;
+    const int ic = i < ie ? i : i0;  // a column of the tile for the register loads
     auto issue = [&](int k) {
       if (k <= k1) {  // level k1 only for the fields read at k+1
         const int64_t ko = (int64_t)k * d.sk;
         Level& L = s.l[k % NB];
-        if (k < k1) {
-          stage_rows<32, 32>(L.uin, uin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<32, 32>(L.vin, vin, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<32, 32>(L.rx, rdx, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<32, 32>(L.ry, rdy, ko, i0, j0, d.sj, i0, ie, j0, je);
-          stage_rows<33, 33>(L.w1, wk1, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
-        }
+        if (k < k1) stage_rows<33, 33>(L.w1, wk1, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
         stage_rows<33, 33>(L.gz, gz, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
         stage_rows<33, 33>(L.pp, pp, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
         stage_rows<33, 33>(L.pk, pk3, ko, i0, j0, d.sj, i0, ie + 1, j0, je + 1);
       }
       cp_async_commit();
     };
+    PointRegs cur;
+    cur.fetch(uin, vin, rdx, rdy, (int64_t)k0 * d.sk, ic, j0, je, d.sj);
     staged_march<NB, 1>(k0, k1, issue, [&](int k) {
+      PointRegs nxt;
+      if (k + 1 < k1) nxt.fetch(uin, vin, rdx, rdy, (int64_t)(k + 1) * d.sk, ic, j0, je, d.sj);
       const int64_t kofs = (int64_t)k * d.sk, kofs1 = kofs + d.sk;
       const Level& C = s.l[k % NB];
       const Level& N = s.l[(k + 1) % NB];
-      const auto uin_ = row_view<32, 32>(C.uin, uin, kofs, i0, j0, d.sj);
-      const auto vin_ = row_view<32, 32>(C.vin, vin, kofs, i0, j0, d.sj);
-      const auto rx = row_view<32, 32>(C.rx, rdx, kofs, i0, j0, d.sj);
-      const auto ry = row_view<32, 32>(C.ry, rdy, kofs, i0, j0, d.sj);
-      const auto w = row_view<33, 33>(C.w1, wk1, kofs, i0, j0, d.sj);
-      const auto g0 = row_view<33, 33>(C.gz, gz, kofs, i0, j0, d.sj);
-      const auto g1 = row_view<33, 33>(N.gz, gz, kofs1, i0, j0, d.sj);
-      const auto q0 = row_view<33, 33>(C.pp, pp, kofs, i0, j0, d.sj);
-      const auto q1 = row_view<33, 33>(N.pp, pp, kofs1, i0, j0, d.sj);
-      const auto p0 = row_view<33, 33>(C.pk, pk3, kofs, i0, j0, d.sj);
-      const auto p1 = row_view<33, 33>(N.pk, pk3, kofs1, i0, j0, d.sj);
-      const int a = threadIdx.x, i = i0 + a;
-      if (i >= ie) return;
-#pragma unroll 2
-      for (int r = 0; r < kRows; ++r) {
-        const int b = threadIdx.y + kTY * r, j = j0 + b;
-        if (j < je) {
-          const float pk0 = p0(a, b), pk1 = p1(a, b), gz0 = g0(a, b), gz1 = g1(a, b), pp0 = q0(a, b), pp1 = q1(a, b);
-          const float w1 = w(a, b);
-          const float wk = pk1 - pk0;
-          const int64_t o = kofs + i + (int64_t)j * d.sj;
-          {  // u: neighbour i+1
-            const float pkx0 = p0(a + 1, b), pkx1 = p1(a + 1, b);
-            const float wkx = pkx1 - pkx0;
-            const float gx0 = g0(a + 1, b), gx1 = g1(a + 1, b);
-            const float fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
-            const float fp = diff_dot(gz1, gx0, q1(a + 1, b), pp0, gz0, gx1, pp1, q0(a + 1, b));
-            const float du = ((dt / (wk + wkx)) * fk);
-            uout[o] = (((uin_(a, b) + du) + ((dt / (w1 + w(a + 1, b))) * fp)) * rx(a, b));
-          }
-          {  // v: neighbour j+1
-            const float pky0 = p0(a, b + 1), pky1 = p1(a, b + 1);
-            const float wky = pky1 - pky0;
-            const float gy0 = g0(a, b + 1), gy1 = g1(a, b + 1);
-            const float fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
-            const float fp = diff_dot(gz1, gy0, q1(a, b + 1), pp0, gz0, gy1, pp1, q0(a, b + 1));
-            const float dv = ((dt / (wk + wky)) * fk);
-            vout[o] = (((vin_(a, b) + dv) + ((dt / (w1 + w(a, b + 1))) * fp)) * ry(a, b));
+      const RowMis mw = row_mis(wk1, kofs, i0, j0, d.sj);
+      const RowMis mg0 = row_mis(gz, kofs, i0, j0, d.sj), mg1 = row_mis(gz, kofs1, i0, j0, d.sj);
+      const RowMis mq0 = row_mis(pp, kofs, i0, j0, d.sj), mq1 = row_mis(pp, kofs1, i0, j0, d.sj);
+      const RowMis mp0 = row_mis(pk3, kofs, i0, j0, d.sj), mp1 = row_mis(pk3, kofs1, i0, j0, d.sj);
+      if (i < ie) {
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+          const int b = threadIdx.y + kTY * r, j = j0 + b;
+          if (j < je) {
+            // rows j (box row b) and j+1 (box row b+1); cell i is a in them
+            const float* wc = C.w1 + b * Q::SW + mw(b) + a;
+            const float* wn = C.w1 + (b + 1) * Q::SW + mw(b + 1) + a;
+            const float* g0c = C.gz + b * Q::SW + mg0(b) + a;
+            const float* g0n = C.gz + (b + 1) * Q::SW + mg0(b + 1) + a;
+            const float* g1c = N.gz + b * Q::SW + mg1(b) + a;
+            const float* g1n = N.gz + (b + 1) * Q::SW + mg1(b + 1) + a;
+            const float* q0c = C.pp + b * Q::SW + mq0(b) + a;
+            const float* q0n = C.pp + (b + 1) * Q::SW + mq0(b + 1) + a;
+            const float* q1c = N.pp + b * Q::SW + mq1(b) + a;
+            const float* q1n = N.pp + (b + 1) * Q::SW + mq1(b + 1) + a;
+            const float* p0c = C.pk + b * Q::SW + mp0(b) + a;
+            const float* p0n = C.pk + (b + 1) * Q::SW + mp0(b + 1) + a;
+            const float* p1c = N.pk + b * Q::SW + mp1(b) + a;
+            const float* p1n = N.pk + (b + 1) * Q::SW + mp1(b + 1) + a;
+            const float pk0 = p0c[0], pk1 = p1c[0], gz0 = g0c[0], gz1 = g1c[0], pp0 = q0c[0], pp1 = q1c[0];
+            const float w1 = wc[0];
+            const float wk = pk1 - pk0;
+            const int64_t o = kofs + i + (int64_t)j * d.sj;
+            {  // u: neighbour i+1
+              const float pkx0 = p0c[1], pkx1 = p1c[1];
+              const float wkx = pkx1 - pkx0;
+              const float gx0 = g0c[1], gx1 = g1c[1];
+              const float fk = diff_dot(gz1, gx0, pkx1, pk0, gz0, gx1, pk1, pkx0);
+              const float fp = diff_dot(gz1, gx0, q1c[1], pp0, gz0, gx1, pp1, q0c[1]);
+              const float du = ((dt / (wk + wkx)) * fk);
+              uout[o] = (((cur.v[0][r] + du) + ((dt / (w1 + wc[1])) * fp)) * cur.v[2][r]);
+            }
+            {  // v: neighbour j+1
+              const float pky0 = p0n[0], pky1 = p1n[0];
+              const float wky = pky1 - pky0;
+              const float gy0 = g0n[0], gy1 = g1n[0];
+              const float fk = diff_dot(gz1, gy0, pky1, pk0, gz0, gy1, pk1, pky0);
+              const float fp = diff_dot(gz1, gy0, q1n[0], pp0, gz0, gy1, pp1, q0n[0]);
+              const float dv = ((dt / (wk + wky)) * fk);
+              vout[o] = (((cur.v[1][r] + dv) + ((dt / (w1 + wn[0])) * fp)) * cur.v[3][r]);
+            }
           }
         }
       }
+      cur = nxt;
     });
   }
 };
@@ -635,14 +540,6 @@ oeb_status uvbke_entry(const M3* ub, const M3* vb, const M3* uc, const M3* vc, c
                          {guc.lo, guc.hi, gvc.lo, gvc.hi, gca.lo, gca.hi, grs.lo, grs.hi}));
   OEB_RETURN_IF_VALIDATING();
   const T dt5_hi = T(dt5), dt5_lo = T(dt5 - (double)dt5_hi);  // dt5_lo = 0 for FP64
-  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
-    dim3 grid;
-    int kb;
-    staged_launch_shape<uvbke_staged_f32>(*dom, &grid, &kb);
-    return launch<uvbke_staged_f32>(grid, sizeof(uvbke_staged_f32::Smem), (cudaStream_t)stream, gub.origin,
-                                    gvb.origin, guc.origin, gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo,
-                                    make_dims(*dom, gub), kb);
-  }
   const int kb = tuned_kb(kKB);
   return launch<uvbke_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gub.origin, gvb.origin, guc.origin,
                                  gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo, make_dims(*dom, gub), kb);
@@ -667,14 +564,6 @@ oeb_status p_grad_c_entry(const M3* uout, const M3* vout, const M3* uin, const M
   OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi}, {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo,
                                                         gry.hi, gdp.lo, gdp.hi, ggz.lo, ggz.hi, gpk.lo, gpk.hi}));
   OEB_RETURN_IF_VALIDATING();
-  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
-    dim3 grid;
-    int kb;
-    staged_launch_shape<p_grad_c_staged_f32>(*dom, &grid, &kb);
-    return launch<p_grad_c_staged_f32>(grid, sizeof(p_grad_c_staged_f32::Smem), (cudaStream_t)stream, gu.origin,
-                                       gv.origin, gui.origin, gvi.origin, grx.origin, gry.origin, gdp.origin,
-                                       ggz.origin, gpk.origin, dt2, make_dims(*dom, gu), kb);
-  }
   const int kb = tuned_kb(kKB);
   return launch<p_grad_c_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
                                     gvi.origin, grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin, dt2,
