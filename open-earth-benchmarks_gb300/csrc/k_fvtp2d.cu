@@ -1,6 +1,6 @@
 // k_fvtp2d.cu -- fvtp2d (kernels/fvtp2d.h:4-177, the serial variant) in FP64 and FP32.
 //
-// Two launches per call, per k-level tiles of 32 x 32 with every PPM intermediate computed
+// FP64: two launches per call, per k-level tiles of 32 x 32 with every PPM intermediate computed
 // once per point into shared memory:
 //   1. fvtp2d_q:    y-PPM of q -> fy2 (fvtp2d.h:8-37), x-PPM of q -> fx2 (:84-113), then
 //                   q_i (:39-51) and q_j (:115-127).  Tiles cover the extended index range
@@ -10,10 +10,13 @@
 //                   transport fluxes fx1 = (fx1+fx2)/2 * xfx, fy1 = (fy1+fy2)/2 * yfx (:160-176).
 // q_i, q_j, fx2 and fy2 are outputs of the reference signature; launch 2 reads them back
 // from global memory (the FP64 pipe, not HBM, bounds this kernel, so storing them costs
-// less than recomputing their aprons).
+// less than recomputing their aprons).  FP32, bound by memory instead, runs one launch that
+// recomputes the aprons (fvtp2d_fused_kernel).
 //
 // Compiled with --fmad=false (see k_pointwise.cu).  In FP32 the monotonicity flag smt5 is decided
 // on the exact product (precision.cuh).
+#include <type_traits>
+
 #include "oeb_reach.cuh"
 #include "precision.cuh"
 #include "stencil_util.cuh"
@@ -325,6 +328,179 @@ inline dim3 flux_grid(const Dims& d, int kb) {
   return g;
 }
 
+// ------------------------------ FP32: one launch -------------------------------------
+// The FP32 call is bound by memory, and the two launches above move 2.1x its algorithmic
+// bytes: launch 2 reads back q_i, q_j, fx2 and fy2, which launch 1 has just written.  Here one
+// CTA per interior 32 x 32 tile and k-level does both sweeps of q over a 3-cell apron, in
+// shared memory, and then the sweeps of q_i and q_j: nothing it writes is read back.
+//   y pass of q on the columns [i0-3, i0+34): fy2 on rows [j0, j0+33), q_i on [j0, j0+32);
+//   x pass of q on the rows [j0-3, j0+34): fx2 on columns [i0, i0+33), q_j on [i0, i0+32);
+//   x-PPM of q_i and y-PPM of q_j on the tile: fx1 and fy1.
+// The apron costs about 16 % more PPM arithmetic than the two launches.  Each value of q_i,
+// q_j, fx2 and fy2 is written by the one tile that owns it: its own columns (rows), plus the
+// three before the first tile and the extra ones after the last (those arrays' boxes reach
+// 3 cells before the interior and 1 or 2 after it).  The arithmetic is launch 1's and launch
+// 2's, operation for operation, so the results are the same bits.
+// Shared layout (per k-level), tile origin (i0, j0), 37 = the apron width:
+//   q    : 39 x 39, (i0-3+a, j0-3+b)
+//   y pass (columns i0-3+a, a < 37): ya = al on rows j0-1+b (35), then fyy on rows j0+b (33);
+//          ym, yr, ys = almq, br, smt5 on rows j0-1+b (34); qi on rows j0+b (32)
+//   x pass (rows j0-3+b, b < 37): xa = al on columns i0-1+a (35), then fxx on i0+a (33);
+//          xm, xr, xs on columns i0-1+a (34); qj on columns i0+a (32)
+//   fx2c, fy2c: fx2 and fy2 on the tile (32 x 32)
+//   second stage, over the dead aux arrays: x-PPM of qi (al on i0-1+a, 34; aux 33) and
+//   y-PPM of qj (al on j0-1+b, 34; aux 33)
+template <class T>
+struct FvFusedSmem {
+  T q[39][39];
+  T ya[35][37];
+  T ym[34][37], yr[34][37];
+  unsigned char ys[34][37];
+  T qi[32][37];
+  T xa[37][35];
+  T xm[37][34], xr[37][34];
+  unsigned char xs[37][34];
+  T qj[37][32];
+  T fx2c[32][32], fy2c[32][32];
+};
+
+template <class T>
+struct fvtp2d_fused_kernel {
+  static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ q_i, T* __restrict__ q_j,
+                                             T* __restrict__ fx1, T* __restrict__ fx2, T* __restrict__ fy1,
+                                             T* __restrict__ fy2, const T* __restrict__ q, const T* __restrict__ crx,
+                                             const T* __restrict__ cry, const T* __restrict__ ra_x,
+                                             const T* __restrict__ ra_y, const T* __restrict__ xfx,
+                                             const T* __restrict__ yfx, const T* __restrict__ area, T p1, T p2, Dims d,
+                                             int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FvFusedSmem<T>& s = *reinterpret_cast<FvFusedSmem<T>*>(smem_raw);
+    // second-stage arrays over the dead aux arrays of the first
+    T(*xa2)[34] = reinterpret_cast<T(*)[34]>(&s.ym[0][0]);  // x-PPM of qi: al, 32 rows x 34
+    T(*xm2)[33] = reinterpret_cast<T(*)[33]>(&s.yr[0][0]);  // almq, 32 x 33
+    T(*xr2)[33] = reinterpret_cast<T(*)[33]>(&s.ya[0][0]);  // br, 32 x 33
+    unsigned char(*xs2)[33] = reinterpret_cast<unsigned char(*)[33]>(&s.ys[0][0]);
+    T(*ya3)[32] = reinterpret_cast<T(*)[32]>(&s.xm[0][0]);  // y-PPM of qj: al, 34 rows x 32
+    T(*ym3)[32] = reinterpret_cast<T(*)[32]>(&s.xr[0][0]);  // almq, 33 x 32
+    T(*yr3)[32] = reinterpret_cast<T(*)[32]>(&s.xa[0][0]);  // br, 33 x 32
+    unsigned char(*ys3)[32] = reinterpret_cast<unsigned char(*)[32]>(&s.xs[0][0]);
+    const int i0 = (int)blk.x * kT, j0 = (int)blk.y * kT;
+    const int sj = (int)d.sj;
+    const int nx = d.nx, ny = d.ny;
+    const int k0 = (int)blk.z * kb, k1 = min(k0 + kb, d.nz);
+    // cells this tile owns in the extended boxes of fy2 / q_i (columns) and fx2 / q_j (rows)
+    const int ci0 = i0 == 0 ? -3 : i0, ci1 = i0 + kT >= nx ? nx + 2 : i0 + kT;
+    const int rj0 = j0 == 0 ? -3 : j0, rj1 = j0 + kT >= ny ? ny + 2 : j0 + kT;
+    const int fyr1 = j0 + kT >= ny ? ny + 1 : j0 + kT;  // rows of fy2 owned
+    const int fxc1 = i0 + kT >= nx ? nx + 1 : i0 + kT;  // columns of fx2 owned
+    auto qok = [&](int i, int j) { return i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3; };
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region<39, 39>([&](int a, int b) {
+        const int i = i0 - 3 + a, j = j0 - 3 + b;
+        s.q[b][a] = qok(i, j) ? ld(q + kofs + i + j * sj) : T(0);
+      });
+      __syncthreads();
+      // edge values (fvtp2d.h:12, :57, :88, :133)
+      for_region<37, 35>([&](int a, int b) {
+        s.ya[b][a] = ppm_al(p1, p2, s.q[b][a], s.q[b + 1][a], s.q[b + 2][a], s.q[b + 3][a]);
+      });
+      for_region<35, 37>([&](int a, int b) {
+        s.xa[b][a] = ppm_al(p1, p2, s.q[b][a], s.q[b][a + 1], s.q[b][a + 2], s.q[b][a + 3]);
+      });
+      __syncthreads();
+      for_region<37, 34>([&](int a, int b) {
+        ppm_aux(s.ya[b][a], s.ya[b + 1][a], s.q[b + 2][a], &s.ym[b][a], &s.yr[b][a], &s.ys[b][a]);
+      });
+      for_region<34, 37>([&](int a, int b) {
+        ppm_aux(s.xa[b][a], s.xa[b][a + 1], s.q[b][a + 2], &s.xm[b][a], &s.xr[b][a], &s.xs[b][a]);
+      });
+      __syncthreads();
+      // fy2 (fvtp2d.h:26-34) on (i0-3+a, j0+b) and fyy = yfx fy2 (:43), over the dead al
+      for_region<37, 33>([&](int a, int b) {
+        const int i = i0 - 3 + a, j = j0 + b;
+        T fyy = T(0);
+        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny + 1) {
+          const int64_t o = kofs + i + j * sj;
+          const T f = ppm_flux(ld(cry + o), s.q[b + 2][a], s.q[b + 3][a], s.ym[b][a], s.yr[b][a], s.ym[b + 1][a],
+                               s.yr[b + 1][a], s.ys[b][a], s.ys[b + 1][a]);
+          if (i >= ci0 && i < ci1 && j < fyr1) fy2[o] = f;
+          if (a >= 3 && a < 3 + kT && b < kT) s.fy2c[b][a - 3] = f;
+          fyy = ld(yfx + o) * f;
+        }
+        s.ya[b][a] = fyy;
+      });
+      // fx2 (fvtp2d.h:102-110) on (i0+a, j0-3+b) and fxx = xfx fx2 (:119)
+      for_region<33, 37>([&](int a, int b) {
+        const int i = i0 + a, j = j0 - 3 + b;
+        T fxx = T(0);
+        if (i >= 0 && i < nx + 1 && j >= -3 && j < ny + 2) {
+          const int64_t o = kofs + i + j * sj;
+          const T f = ppm_flux(ld(crx + o), s.q[b][a + 2], s.q[b][a + 3], s.xm[b][a], s.xr[b][a], s.xm[b][a + 1],
+                               s.xr[b][a + 1], s.xs[b][a], s.xs[b][a + 1]);
+          if (j >= rj0 && j < rj1 && i < fxc1) fx2[o] = f;
+          if (b >= 3 && b < 3 + kT && a < kT) s.fx2c[b - 3][a] = f;
+          fxx = ld(xfx + o) * f;
+        }
+        s.xa[b][a] = fxx;
+      });
+      __syncthreads();
+      // q_i (fvtp2d.h:48) on (i0-3+a, j0+b) and q_j (:124) on (i0+a, j0-3+b)
+      for_region<37, 32>([&](int a, int b) {
+        const int i = i0 - 3 + a, j = j0 + b;
+        T v = T(0);
+        if (i >= -3 && i < nx + 2 && j >= 0 && j < ny) {
+          const int64_t o = kofs + i + j * sj;
+          v = (((s.q[b + 3][a] * ld(area + o)) + s.ya[b][a]) - s.ya[b + 1][a]) / ld(ra_y + o);
+          if (i >= ci0 && i < ci1) q_i[o] = v;
+        }
+        s.qi[b][a] = v;
+      });
+      for_region<32, 37>([&](int a, int b) {
+        const int i = i0 + a, j = j0 - 3 + b;
+        T v = T(0);
+        if (i >= 0 && i < nx && j >= -3 && j < ny + 2) {
+          const int64_t o = kofs + i + j * sj;
+          v = (((s.q[b][a + 3] * ld(area + o)) + s.xa[b][a]) - s.xa[b][a + 1]) / ld(ra_x + o);
+          if (j >= rj0 && j < rj1) q_j[o] = v;
+        }
+        s.qj[b][a] = v;
+      });
+      __syncthreads();
+      // x-PPM of q_i (fvtp2d.h:53-82) and y-PPM of q_j (:129-158): edge values
+      for_region<34, 32>([&](int a, int b) {
+        xa2[b][a] = ppm_al(p1, p2, s.qi[b][a], s.qi[b][a + 1], s.qi[b][a + 2], s.qi[b][a + 3]);
+      });
+      for_region<32, 34>([&](int a, int b) {
+        ya3[b][a] = ppm_al(p1, p2, s.qj[b][a], s.qj[b + 1][a], s.qj[b + 2][a], s.qj[b + 3][a]);
+      });
+      __syncthreads();
+      for_region<33, 32>([&](int a, int b) {
+        ppm_aux(xa2[b][a], xa2[b][a + 1], s.qi[b][a + 2], &xm2[b][a], &xr2[b][a], &xs2[b][a]);
+      });
+      for_region<32, 33>([&](int a, int b) {
+        ppm_aux(ya3[b][a], ya3[b + 1][a], s.qj[b + 2][a], &ym3[b][a], &yr3[b][a], &ys3[b][a]);
+      });
+      __syncthreads();
+      // fx1, fy1 (fvtp2d.h:164, :173)
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i < nx && j < ny) {
+          const int64_t o = kofs + i + j * sj;
+          const T fx = ppm_flux(ld(crx + o), s.qi[b][a + 2], s.qi[b][a + 3], xm2[b][a], xr2[b][a], xm2[b][a + 1],
+                                xr2[b][a + 1], xs2[b][a], xs2[b][a + 1]);
+          fx1[o] = (scale2<-1>(fx + s.fx2c[b][a]) * ld(xfx + o));
+          const T fy = ppm_flux(ld(cry + o), s.qj[b + 2][a], s.qj[b + 3][a], ym3[b][a], yr3[b][a], ym3[b + 1][a],
+                                yr3[b + 1][a], ys3[b][a], ys3[b + 1][a]);
+          fy1[o] = (scale2<-1>(fy + s.fy2c[b][a]) * ld(yfx + o));
+        }
+      });
+      __syncthreads();
+    }
+  }
+};
+
 constexpr int kKB = 1;  // k-levels per CTA by default (the most CTAs hide latency best)
 
 template <class T, class M3>
@@ -359,6 +535,13 @@ oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* f
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gq.sj, gq.sk};
   cudaStream_t st = (cudaStream_t)stream;
   const int kb = tuned_kb(kKB);
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 is bound by memory: one launch, nothing read back
+    return launch<fvtp2d_fused_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FvFusedSmem<T>), st,
+                                          gqi.origin, gqj.origin, gfx1.origin, gfx2.origin, gfy1.origin, gfy2.origin,
+                                          gq.origin, gcx.origin, gcy.origin, grx.origin, gry.origin, gxf.origin,
+                                          gyf.origin, gar.origin, p1, p2, d, kb);
+  }
   OEB_TRY(launch<fvtp2d_q_kernel<T>>(q_grid(d, kb), sizeof(FvQSmem<T>), st,
                                      gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gq.origin, gcx.origin,
                                      gcy.origin, grx.origin, gry.origin, gxf.origin, gyf.origin, gar.origin, p1, p2, d,
