@@ -180,22 +180,29 @@ oeb_status record_all(oeb_batch_plan* p, int kb, std::vector<std::vector<std::ve
   return OEB_OK;
 }
 
-// Slots and host tables of one recording: for every position, one slot per precision.
+// Slots and host tables of one recording: for every position, one slot per precision.  The
+// members of one precision record the same launches; the two precisions may record different
+// numbers of them (FP32 fvtp2d is one launch, FP64 two), so positions count per precision.
 oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vector<LaunchRecord>>>& seq, int kb,
                        std::vector<Slot>* slots, std::vector<char>* host, size_t base) {
   for (int mi = 0; mi < 2; ++mi) {
     if (!(p->modes & kModes[mi])) continue;
     const auto& per = seq[mi];
-    const size_t len = per[0].size();
-    for (const auto& r : per)
-      if (r.size() != len) return OEB_ERR_UNSUPPORTED;
+    std::vector<int> members_of[2];
+    size_t len_of[2] = {0, 0};
+    for (int side = 0; side < 2; ++side) {
+      for (size_t i = 0; i < p->members.size(); ++i)
+        if (p->members[i].elem == (side ? 4 : 8)) members_of[side].push_back((int)i);
+      if (members_of[side].empty()) continue;
+      len_of[side] = per[members_of[side][0]].size();
+      for (int i : members_of[side])
+        if (per[i].size() != len_of[side]) return OEB_ERR_UNSUPPORTED;
+    }
+    const size_t len = std::max(len_of[0], len_of[1]);
     for (size_t pos = 0; pos < len; ++pos) {
       for (int side = 0; side < 2; ++side) {
-        const int elem = side ? 4 : 8;
-        std::vector<int> who;
-        for (size_t i = 0; i < p->members.size(); ++i)
-          if (p->members[i].elem == elem) who.push_back((int)i);
-        if (who.empty()) continue;
+        if (pos >= len_of[side]) continue;
+        std::vector<int> who = members_of[side];
         const LaunchRecord& r0 = per[who[0]][pos];
         for (int i : who)
           if (per[i][pos].launcher != r0.launcher || per[i][pos].args.size() != r0.args.size())
