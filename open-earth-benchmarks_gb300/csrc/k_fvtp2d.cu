@@ -19,6 +19,7 @@
 
 #include "oeb_reach.cuh"
 #include "precision.cuh"
+#include "stage.cuh"
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
@@ -364,8 +365,28 @@ struct FvFusedSmem {
   T fx2c[32][32], fy2c[32][32];
 };
 
+// Asks L2 for the lines of field f (level offset kofs) that hold the cells [ilo, ihi) x
+// [jlo, jhi) (empty ranges ask nothing), spread over the CTA's threads; the ranges lie in the
+// field's reach.
+template <class T>
+__device__ __forceinline__ void prefetch_box(const T* f, int64_t kofs, int ilo, int ihi, int jlo, int jhi, int sj) {
+  if (ihi <= ilo || jhi <= jlo) return;
+  const uintptr_t first = reinterpret_cast<uintptr_t>(f + kofs + ilo) / 128;
+  const int lines = (int)((reinterpret_cast<uintptr_t>(f + kofs + ihi - 1) / 128) - first) + 1;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  for (int e = tid; e < lines * (jhi - jlo); e += kThreads) {
+    const int r = e / lines, l = e - r * lines;
+    const T* row = f + kofs + (int64_t)(jlo + r) * sj;
+    const uintptr_t a = (reinterpret_cast<uintptr_t>(row + ilo) / 128 + l) * 128;
+    // the line's first cell of the range (clamped into it), so the address lies in the field
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(row + ilo), hi = reinterpret_cast<uintptr_t>(row + ihi - 1);
+    prefetch_l2(reinterpret_cast<const void*>(a < lo ? lo : (a > hi ? hi : a)));
+  }
+}
+
 template <class T>
 struct fvtp2d_fused_kernel {
+  static constexpr int kCtasPerSm = 4;
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ q_i, T* __restrict__ q_j,
                                              T* __restrict__ fx1, T* __restrict__ fx2, T* __restrict__ fy1,
                                              T* __restrict__ fy2, const T* __restrict__ q, const T* __restrict__ crx,
@@ -394,13 +415,27 @@ struct fvtp2d_fused_kernel {
     const int fyr1 = j0 + kT >= ny ? ny + 1 : j0 + kT;  // rows of fy2 owned
     const int fxc1 = i0 + kT >= nx ? nx + 1 : i0 + kT;  // columns of fx2 owned
     auto qok = [&](int i, int j) { return i >= -3 && i < nx + 3 && j >= -3 && j < ny + 3; };
+    // L2 prefetches: at each level, the inputs its later phases read, and the next level's q
+    // (the loads of the late phases and of the next q tile then find their lines in L2)
+    auto late_prefetch = [&](int64_t kofs) {
+      prefetch_box(cry, kofs, max(i0 - 3, -3), min(i0 + 34, nx + 2), max(j0, 0), min(j0 + 33, ny + 1), sj);
+      prefetch_box(yfx, kofs, max(i0 - 3, -3), min(i0 + 34, nx + 2), max(j0, 0), min(j0 + 33, ny + 1), sj);
+      prefetch_box(crx, kofs, max(i0, 0), min(i0 + 33, nx + 1), max(j0 - 3, -3), min(j0 + 34, ny + 2), sj);
+      prefetch_box(xfx, kofs, max(i0, 0), min(i0 + 33, nx + 1), max(j0 - 3, -3), min(j0 + 34, ny + 2), sj);
+      prefetch_box(area, kofs, max(i0 - 3, -3), min(i0 + 34, nx + 2), max(j0 - 3, -3), min(j0 + 34, ny + 2), sj);
+      prefetch_box(ra_y, kofs, max(i0 - 3, -3), min(i0 + 34, nx + 2), max(j0, 0), min(j0 + 32, ny), sj);
+      prefetch_box(ra_x, kofs, max(i0, 0), min(i0 + 32, nx), max(j0 - 3, -3), min(j0 + 34, ny + 2), sj);
+    };
   #pragma unroll 1
     for (int k = k0; k < k1; ++k) {
       const int64_t kofs = (int64_t)k * d.sk;
+      late_prefetch(kofs);
       for_region<39, 39>([&](int a, int b) {
         const int i = i0 - 3 + a, j = j0 - 3 + b;
         s.q[b][a] = qok(i, j) ? ld(q + kofs + i + j * sj) : T(0);
       });
+      if (k + 1 < k1)
+        prefetch_box(q, kofs + d.sk, max(i0 - 3, -3), min(i0 + 36, nx + 3), max(j0 - 3, -3), min(j0 + 36, ny + 3), sj);
       __syncthreads();
       // edge values (fvtp2d.h:12, :57, :88, :133)
       for_region<37, 35>([&](int a, int b) {
@@ -537,10 +572,12 @@ oeb_status fvtp2d_entry(const M3* q_i, const M3* q_j, const M3* fx1, const M3* f
   const int kb = tuned_kb(kKB);
   if constexpr (std::is_same<T, float>::value) {
     // FP32 is bound by memory: one launch, nothing read back
-    return launch<fvtp2d_fused_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(FvFusedSmem<T>), st,
+    const int tiles = ((d.nx + kT - 1) / kT) * ((d.ny + kT - 1) / kT);
+    const int kbf = tuned_kb(staged_kb(tiles, d.nz, fvtp2d_fused_kernel<T>::kCtasPerSm));
+    return launch<fvtp2d_fused_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kbf), sizeof(FvFusedSmem<T>), st,
                                           gqi.origin, gqj.origin, gfx1.origin, gfx2.origin, gfy1.origin, gfy2.origin,
                                           gq.origin, gcx.origin, gcy.origin, grx.origin, gry.origin, gxf.origin,
-                                          gyf.origin, gar.origin, p1, p2, d, kb);
+                                          gyf.origin, gar.origin, p1, p2, d, kbf);
   }
   OEB_TRY(launch<fvtp2d_q_kernel<T>>(q_grid(d, kb), sizeof(FvQSmem<T>), st,
                                      gqi.origin, gqj.origin, gfx2.origin, gfy2.origin, gq.origin, gcx.origin,
