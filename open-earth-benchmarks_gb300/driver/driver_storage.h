@@ -122,6 +122,21 @@ void release(S& s) {
   s.allocatedPtr = s.alignedPtr = nullptr;
 }
 
+// The interior cells [0, n)^2 x [0, nz) of a device field, as doubles in host memory.
+template <class T>
+std::vector<double> interior(const Storage<T, 3>& s, int64_t n, int64_t nz) {
+  const int64_t span = (s.sizes[0] - 1) * s.strides[0] + (s.sizes[1] - 1) * s.strides[1] + s.sizes[2];
+  std::vector<T> host((size_t)span);
+  cuda_check(cudaMemcpy(host.data(), s.alignedPtr, host.size() * sizeof(T), cudaMemcpyDeviceToHost), "download");
+  std::vector<double> out;
+  out.reserve((size_t)(n * n * nz));
+  for (int64_t k = 0; k < nz; ++k)
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t i = 0; i < n; ++i)
+        out.push_back((double)host[(size_t)(s.offset + k * s.strides[0] + j * s.strides[1] + i)]);
+  return out;
+}
+
 // One timed kernel run, as the reference's timer prints it plus a JSON line.
 struct Result {
   const char* kernel;
@@ -131,6 +146,8 @@ struct Result {
   int64_t points;
   int fields;  // 3-D inputs + semantic outputs: the algorithmic bytes are fields x points x sizeof(T)
   bool adjoint;  // each timed call was the forward variant followed by the kernel's adjoint
+  // the semantic outputs' interiors after the timed calls (when asked for), for error columns
+  std::vector<std::vector<double>> outputs;
 };
 
 }  // namespace oeb_driver

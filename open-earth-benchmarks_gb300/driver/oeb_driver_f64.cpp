@@ -33,6 +33,6 @@ static const double dt5 = 0.5 * 225.0;
 #define OEB_DRIVER_ADJ(k) oeb_##k##_adj_f64
 #include "driver_kernels.inc"
 
-bool oeb_driver_run_f64(const char* kernel, int algo, int count, bool adjoint, oeb_driver::Result* r) {
-  return run_kernel(kernel, algo, count, adjoint, r);
+bool oeb_driver_run_f64(const char* kernel, int algo, int count, bool adjoint, bool keep, oeb_driver::Result* r) {
+  return run_kernel(kernel, algo, count, adjoint, keep, r);
 }

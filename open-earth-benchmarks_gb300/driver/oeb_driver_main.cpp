@@ -10,17 +10,21 @@
 // through the drop-in headers on device-resident fields.  Output: the reference's lines
 // (ALGO, domain_size, domain_height, then "<name>: T ms / C count, avg A ms" per kernel, or
 // "Unknown ALGO" for a variant the kernel lacks, as the reference prints it) and, with --json,
-// one JSON line per kernel with GPts/s and algorithmic HBM GB/s.  --adjoint (not in the
-// reference, which has no adjoints) times each call as the forward variant followed by the
-// kernel's adjoint, for hdiffsmag, hadvuv, hadvuv5th, fastwavesuv and fvtp2d; any other
-// kernel prints "<kernel>: no adjoint" and is skipped.  Exit status 1 for a usage error or an
-// unknown kernel name.
+// one JSON line per kernel with GPts/s, algorithmic HBM GB/s and their fraction of this GPU's
+// device-to-device copy rate (measured by the driver, once); FP32 lines add the normwise
+// max and rms error of the semantic outputs against the FP64 run of the same variant on the
+// same fills (the FP64 stencils give the reference's results bit for bit).  --adjoint (not in
+// the reference, which has no adjoints) times each call as the forward variant followed by the
+// kernel's adjoint.  Exit status 1 for a usage error or an unknown kernel name.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "driver_api.h"
 #include "driver_storage.h"
@@ -33,12 +37,67 @@ namespace {
 
 const char* kAll[] = {"fastwavesuv", "fvtp2d", "hadvuv", "hadvuv5th", "hdiffsa", "hdiffsmag",
                       "laplace",     "nh_p_grad", "p_grad_c", "uvbke"};
-// the kernels with an adjoint entry point (include/oeb_gb300.h)
-const char* kAdjoint[] = {"fastwavesuv", "fvtp2d", "hadvuv", "hadvuv5th", "hdiffsmag"};
+
+// Normwise errors of `got` against `ref` over all outputs: max |e| / max |ref| and
+// rms(e) / max |ref|, the worst output's.
+void errors(const std::vector<std::vector<double>>& got, const std::vector<std::vector<double>>& ref, double* mx,
+            double* rms) {
+  *mx = *rms = 0.0;
+  for (size_t o = 0; o < got.size() && o < ref.size(); ++o) {
+    double scale = 0.0, emax = 0.0, esq = 0.0;
+    for (double v : ref[o]) scale = std::max(scale, std::fabs(v));
+    for (size_t c = 0; c < got[o].size(); ++c) {
+      const double e = std::fabs(got[o][c] - ref[o][c]);
+      emax = std::max(emax, e);
+      esq += e * e;
+    }
+    if (scale > 0.0 && !got[o].empty()) {
+      *mx = std::max(*mx, emax / scale);
+      *rms = std::max(*rms, std::sqrt(esq / (double)got[o].size()) / scale);
+    }
+  }
+}
 
 bool listed(const char* const* b, const char* const* e, const std::string& name) {
   return std::find_if(b, e, [&](const char* k) { return name == k; }) != e;
 }
+
+}  // namespace
+
+double oeb_driver_copy_gbs() {
+  static double gbs = -1.0;
+  if (gbs >= 0.0) return gbs;
+  gbs = 0.0;
+  const size_t bytes = size_t(1) << 30;  // 1 GiB each way, far above the L2
+  void *a = nullptr, *b = nullptr;
+  if (cudaMalloc(&a, bytes) != cudaSuccess || cudaMalloc(&b, bytes) != cudaSuccess) {
+    cudaFree(a);
+    cudaGetLastError();
+    return gbs;
+  }
+  cudaMemset(a, 0, bytes);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 6; ++rep) {
+    cudaEventRecord(e0, 0);
+    cudaMemcpyAsync(b, a, bytes, cudaMemcpyDeviceToDevice, 0);
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // the first copy is the warm-up
+  }
+  if (best > 0.f) gbs = 2.0 * (double)bytes / (best * 1e-3) / 1e9;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(a);
+  cudaFree(b);
+  return gbs;
+}
+
+namespace {
 
 int usage() {
   std::fprintf(stderr,
@@ -86,14 +145,10 @@ int main(int argc, char** argv) {
     names.push_back(kernel);
   int status = 0;
   for (const std::string& name : names) {
-    if (adjoint && listed(std::begin(kAll), std::end(kAll), name) &&
-        !listed(std::begin(kAdjoint), std::end(kAdjoint), name)) {
-      std::printf("%s: no adjoint\n", name.c_str());
-      continue;
-    }
     oeb_driver::Result r{};
-    const bool ok = f32 ? oeb_driver_run_f32(name.c_str(), algo, count, adjoint, &r)
-                        : oeb_driver_run_f64(name.c_str(), algo, count, adjoint, &r);
+    const bool errs = json && f32;
+    const bool ok = f32 ? oeb_driver_run_f32(name.c_str(), algo, count, adjoint, errs, &r)
+                        : oeb_driver_run_f64(name.c_str(), algo, count, adjoint, false, &r);
     if (!ok) {
       if (!listed(std::begin(kAll), std::end(kAll), name)) {
         std::fprintf(stderr, "oeb_driver: unknown kernel %s\n", name.c_str());
@@ -109,14 +164,25 @@ int main(int argc, char** argv) {
     if (json) {
       const double s = r.total_ms * 1e-3 / r.count;
       const double bytes = (double)r.fields * (double)r.points * (f32 ? 4.0 : 8.0);
+      const double copy = oeb_driver_copy_gbs();
+      std::string err;
+      if (errs) {
+        oeb_driver::Result ref{};
+        oeb_driver_run_f64(name.c_str(), algo, 1, false, true, &ref);
+        double mx = 0.0, rms = 0.0;
+        errors(r.outputs, ref.outputs, &mx, &rms);
+        char buf[160];
+        std::snprintf(buf, sizeof buf, ", \"max_rel_err_vs_f64\": %.3e, \"rms_rel_err_vs_f64\": %.3e", mx, rms);
+        err = buf;
+      }
       std::printf(
           "{\"kernel\": \"%s\", \"variant\": \"%s\", \"mode\": \"%s\", \"precision\": \"%s\", "
           "\"domain\": [%lld, %lld, %lld], \"halo\": %lld, \"count\": %d, \"ms_per_call\": %.6f, \"gpts\": %.4f, "
-          "\"hbm_gbs\": %.1f}\n",
+          "\"hbm_gbs\": %.1f, \"copy_gbs\": %.1f, \"hbm_frac_of_copy\": %.4f%s}\n",
           name.c_str(), r.variant[0] ? r.variant : "default", r.adjoint ? "forward+adjoint" : "forward",
           f32 ? "f32" : "f64", (long long)domain_size,
           (long long)domain_size, (long long)domain_height, (long long)halo_width, r.count, s * 1e3,
-          (double)r.points / s / 1e9, bytes / s / 1e9);
+          (double)r.points / s / 1e9, bytes / s / 1e9, copy, copy > 0.0 ? bytes / s / 1e9 / copy : 0.0, err.c_str());
     }
     std::fflush(stdout);
   }

@@ -41,19 +41,6 @@ def test_unknown_algo_and_kernel(driver):
     assert proc.returncode == 1 and "unknown kernel" in proc.stderr
 
 
-ADJOINT_KERNELS = {"hdiffsmag", "hadvuv", "hadvuv5th", "fastwavesuv", "fvtp2d"}
-
-
-def test_adjoint_flag_skips_kernels_without_one(driver):
-    # --adjoint on a kernel without an adjoint entry point says so and runs nothing (no CUDA
-    # call: this runs on the CPU)
-    for name in sorted(KERNELS - ADJOINT_KERNELS):
-        proc = _run(driver, name, "0", "--adjoint", "--json")
-        assert proc.returncode == 0, (name, proc.stdout, proc.stderr)
-        assert "%s: no adjoint" % name in proc.stdout.splitlines()
-        assert not [ln for ln in proc.stdout.splitlines() if ln.startswith("{")]
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["", "--f32"])
 def test_sweep_all_kernels_with_adjoint(driver, precision):
@@ -62,17 +49,15 @@ def test_sweep_all_kernels_with_adjoint(driver, precision):
     assert proc.returncode == 0, proc.stdout + proc.stderr
     lines = proc.stdout.splitlines()
     recs = [json.loads(ln) for ln in lines if ln.startswith("{")]
-    assert {r["kernel"] for r in recs} == ADJOINT_KERNELS
-    for name in KERNELS - ADJOINT_KERNELS:
-        assert "%s: no adjoint" % name in lines
+    assert {r["kernel"] for r in recs} == KERNELS  # every stencil has an adjoint
     for r in recs:
         assert r["mode"] == "forward+adjoint" and r["count"] == 3
         assert r["precision"] == ("f32" if precision else "f64")
         assert r["ms_per_call"] > 0 and r["gpts"] > 0
     # the reference's timer line, labelled with the adjoint
-    for name in ADJOINT_KERNELS:
+    for name in KERNELS:
         assert [ln for ln in lines if ln.startswith("%s + adjoint: " % name) and ln.endswith(" ms")], name
-    assert sum(1 for ln in lines if " + adjoint: " in ln) == len(ADJOINT_KERNELS)
+    assert sum(1 for ln in lines if " + adjoint: " in ln) == len(KERNELS)
 
 
 @pytest.mark.gpu
@@ -93,6 +78,14 @@ def test_sweep_all_kernels(driver, precision, algo):
         assert r["precision"] == ("f32" if precision else "f64")
         assert r["domain"] == [48, 48, 10] and r["count"] == 5
         assert r["gpts"] > 0 and r["hbm_gbs"] > 0
+        # the fraction of this GPU's copy rate, which the driver measures itself
+        assert r["copy_gbs"] > 1000 and abs(r["hbm_frac_of_copy"] - r["hbm_gbs"] / r["copy_gbs"]) < 1e-3
+        if precision:
+            # FP32 against the FP64 run of the same variant on the same fills (the FP64 stencils are
+            # the reference's arithmetic bit for bit): storage rounding of the drivers' analytic inputs
+            assert 0.0 <= r["rms_rel_err_vs_f64"] <= r["max_rel_err_vs_f64"] < 1e-2, r
+        else:
+            assert "max_rel_err_vs_f64" not in r
     timer = [ln for ln in lines if " count, avg " in ln]
     assert len(timer) == len(want)
 
