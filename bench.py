@@ -426,6 +426,7 @@ def run_ours(args):
     # each stencil alone: its average launch duration over back-to-back launches (graph)
     iso = {k: _time_isolated(pkg, torch, dev, sets[0][k], k, dom, args.steps, args.warmup) for k in names}
     iso_ms = {k: v[0] for k, v in iso.items()}
+    add_rate, add_rate_clocks = _fp64_add_rate(pkg, local)
     achieved = _algorithmic_bytes(pkg, dom_k) / (iso_ms[dom_k] * 1e-3) / 1e9
     traffic = _ncu_traffic(dom_k)
 
@@ -533,8 +534,9 @@ def run_ours(args):
                      "launch_ms_sequential_pass": round(per_kernel[dom_k], 5),
                      "fp64_pipe_active_pct": _ncu_summary(dom_k, "fp64_pipe_active_pct"),
                      "alu_pipe_active_pct": _ncu_summary(dom_k, "alu_pipe_active_pct"),
-                     "fp64_pipe_roof": _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clock_summary,
-                                                           torch.cuda.get_device_properties(dev).multi_processor_count),
+                     "fp64_pipe_roof": _fp64_pipe_roofline(names, iso_ms, dom_k, ms_step, clock_summary,
+                                                           torch.cuda.get_device_properties(dev).multi_processor_count,
+                                                           add_rate, add_rate_clocks),
                      "note": "the FP64 stencils are compute-bound, not HBM-bound: GB300 issues 1.6 FP64 "
                              "op/clk/SM, so the kernels run as F64i (exact integer-pipe multiply, divide, "
                              "sqrt, compare beside FP64-pipe adds); the pipe figures are ncu's "
@@ -801,31 +803,46 @@ def _ncu_summary(kernel, key):
 
 # FP64-pipe thread instructions (DADD / DMUL / DFMA) per clock per SM on the GB300, measured
 # by a dependent-free DADD throughput loop: 505 G/s at 2070 MHz on 152 SMs.
-FP64_PIPE_PER_CLK_SM = 1.6
 PIPE_MIX_PROFILE = "pipe_mix_ten_stencils_f64"
 
 
-def _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clocks_summary, sms):
+def _fp64_add_rate(pkg, gpu_index):
+    """The FP64 pipe's rate on this GPU, measured here (oeb_probe_fp64_add_rate): FP64 additions
+    a second over all SMs, the clocks sampled while it ran, and the additions of one launch."""
+    import ctypes
+    lib = pkg.load_library()
+    rate, adds = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    with ClockSampler(gpu_index) as clocks:
+        st = lib.oeb_probe_fp64_add_rate(ctypes.byref(rate), ctypes.byref(adds))
+    return (rate.value if st == 0 else None), clocks.summary()
+
+
+def _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clocks_summary, sms, add_rate, rate_clocks):
     """The FP64 pipe as the roof: each kernel's FP64-pipe instructions per interior point
-    (committed ncu counts) x points, over the pipe's rate at the SM clock sampled during the
-    timed region.  For the dominant kernel (sequential pass) and for the whole concurrent
-    step.  None without the counts or a clock sample."""
-    mhz = (clocks_summary or {}).get("sm_mhz")
+    (committed ncu counts) x points, over the FP64 addition rate measured on this GPU just
+    before (oeb_probe_fp64_add_rate), rescaled by the ratio of the SM clock sampled during the
+    timed region to the one sampled during the probe.  For the dominant kernel (iso timing)
+    and for the whole concurrent step.  None without the counts or the rate."""
     per_pt = {k: _ncu_summary(PIPE_MIX_PROFILE, "fp64_instr_per_point_" + k) for k in names}
-    if not mhz or any(v is None for v in per_pt.values()):
+    if not add_rate or any(v is None for v in per_pt.values()):
         return None
-    rate = FP64_PIPE_PER_CLK_SM * sms * mhz * 1e6  # thread instructions / s
+    mhz = (clocks_summary or {}).get("sm_mhz")
+    probe_mhz = (rate_clocks or {}).get("sm_mhz")
+    rate = add_rate * (mhz / probe_mhz if mhz and probe_mhz else 1.0)  # thread instructions / s
     pts = NX * NY * NZ
     k_bound_ms = per_pt[dom_k] * pts / rate * 1e3
     step_bound_ms = sum(per_pt.values()) * pts / rate * 1e3
-    return {"unit": "FP64-pipe instructions", "rate_per_clk_per_sm": FP64_PIPE_PER_CLK_SM, "sms": sms,
-            "sm_mhz": mhz, "kernel": dom_k, "kernel_instr_per_point": per_pt[dom_k],
+    per_clk = add_rate / (sms * probe_mhz * 1e6) if probe_mhz else None
+    return {"unit": "FP64-pipe instructions", "measured_adds_per_s": round(add_rate, 1),
+            "rate_per_clk_per_sm": round(per_clk, 4) if per_clk else None, "probe_sm_mhz": probe_mhz,
+            "sms": sms, "sm_mhz": mhz, "kernel": dom_k, "kernel_instr_per_point": per_pt[dom_k],
             "kernel_bound_ms": round(k_bound_ms, 5), "kernel_frac": round(k_bound_ms / per_kernel[dom_k], 4),
             "step_instr_per_point": round(sum(per_pt.values()), 2), "step_bound_ms": round(step_bound_ms, 5),
             "step_frac": round(step_bound_ms / ms_step, 4),
-            "source": "instructions per point: profiles/ncu_%s_128x128x80.md (ncu "
-                      "sm__inst_executed_pipe_fp64); frac = bound / measured (kernel: sequential pass; step: "
-                      "the concurrent graph)" % PIPE_MIX_PROFILE}
+            "source": "rate: oeb_probe_fp64_add_rate (independent __dadd_rn chains on every SM, timed here); "
+                      "instructions per point: profiles/ncu_%s_128x128x80.md (ncu sm__inst_executed_pipe_fp64); "
+                      "frac = bound / measured (kernel: alone, back-to-back launches; step: the concurrent "
+                      "graph)" % PIPE_MIX_PROFILE}
 
 
 def _ncu_traffic(kernel):
@@ -936,6 +953,53 @@ def _cpu_baseline(pkg, fields, budget_s=15.0, threads=None):
             "per_kernel_ms": {k: round(statistics.mean(v) * 1e3, 3) for k, v in per.items()}}
 
 
+def port_vs_reference(args):
+    """`--port-vs-reference`: the oracle port (oracle/oeb_oracle.c) and the reference's own
+    headers compiled from source (oracle/_ref), timed on the same inputs (the 128x128x80 step,
+    seed 1) with the same host threads, kernel by kernel: how well the port stands in for the
+    reference where the reference tree is absent (the GPU host).  Needs the reference source
+    tree; prints one JSON line."""
+    pkg = graft.load_package()
+    import importlib
+    fields = importlib.import_module("oeb_gb300.fields")
+    from oracle import oracle as orc
+    threads = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    if not orc.reference_available():
+        print(json.dumps({"port_vs_reference": None, "why": "the reference source tree is absent on this host"}))
+        return
+    per = {}
+    for name, spec in pkg.KERNELS.items():
+        inputs = fields.make_inputs(name, NX, NY, NZ, seed=SEED)
+        sc = fields.make_scalars(name, seed=SEED)
+        bufs = {}
+        for kind in ("port", "reference"):
+            b = {**{k: v.copy() for k, v in inputs.items()}, **fields.make_outputs(name, NX, NY, NZ,
+                                                                                     include_scratch=True)}
+            bufs[kind] = b
+
+        def one(kind):
+            if kind == "port":
+                orc.run_oracle(spec, bufs[kind], sc, NX, NY, NZ, HALO)
+            else:
+                orc.run_reference(spec, bufs[kind], sc, NX, NZ, HALO, "openmp")
+
+        times = {"port": [], "reference": []}
+        for rep in range(max(args.warmup, 1) + args.steps):
+            for kind in ("port", "reference"):  # interleaved, so that both see the same host state
+                t = time.perf_counter()
+                one(kind)
+                if rep >= max(args.warmup, 1):
+                    times[kind].append(time.perf_counter() - t)
+        per[name] = {k: round(statistics.median(v) * 1e3, 3) for k, v in times.items()}
+        per[name]["port_over_reference"] = round(per[name]["port"] / per[name]["reference"], 3)
+    step = {k: sum(v[k] for v in per.values()) for k in ("port", "reference")}
+    print(json.dumps({"port_vs_reference": {"workload": WORKLOAD, "threads": threads, "steps": args.steps,
+                                            "step_ms": {k: round(v, 3) for k, v in step.items()},
+                                            "step_port_over_reference": round(step["port"] / step["reference"], 3),
+                                            "per_kernel_ms": per}}), flush=True)
+
+
 def run_reference(args):
     rank, world, _ = _dist_env()
     if rank != 0:
@@ -1021,7 +1085,13 @@ def main():
     ap.add_argument("--shape", type=int, nargs=3, default=[NX, NY, NZ])
     ap.add_argument("--workload", choices=["physical", "fronts", "smooth"], default="physical")
     ap.add_argument("--calls", type=int, default=4)
+    ap.add_argument("--port-vs-reference", action="store_true",
+                    help="time the oracle port against the reference build on this host's cores (needs the "
+                         "reference source tree) and exit")
     args = ap.parse_args()
+    if args.port_vs_reference:
+        port_vs_reference(args)
+        return
     if args.profile_one:
         profile_one(args)
         return

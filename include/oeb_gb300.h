@@ -148,6 +148,12 @@ OEB_API oeb_status oeb_set_host_async(int enable);
  * integer-pipe result.  Synchronous. */
 OEB_API oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int mode, uint64_t* mismatches,
                                      uint64_t* first);
+/* No counterpart in the reference (a measurement of the GPU the FP64 stencils run on): the FP64
+ * pipe's issue rate, as FP64 additions a second over every SM -- eight independent chains of
+ * __dadd_rn a thread, eight CTAs of 256 threads an SM, the fastest of three timed launches
+ * after a warm-up.  `adds_per_launch` (may be NULL) receives the additions of one launch.
+ * Synchronous, on the legacy default stream. */
+OEB_API oeb_status oeb_probe_fp64_add_rate(double* adds_per_second, double* adds_per_launch);
 
 /* ------------------------------------------------------------------------- */
 /* Device storage (the device twin of allocateStorage/freeStorage,           */

@@ -89,8 +89,59 @@ __global__ void selftest_kernel(int op, uint64_t seed, int64_t n, int mode, unsi
   }
 }
 
+// The FP64 pipe's issue rate: every thread runs kChains independent chains of FP64 additions
+// (each addition waits only for the one before it in its chain), enough warps to fill every SM.
+// The sum is stored where nothing reads it only if it is an impossible value, so that the
+// additions are not removed.
+constexpr int kChains = 8;
+__global__ void fp64_add_rate_kernel(int iters, double step, double* sink) {
+  double x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) x[c] = (double)(threadIdx.x + c);
+#pragma unroll 1
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) x[c] = __dadd_rn(x[c], step);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) t = __dadd_rn(t, x[c]);
+  if (t == -1.0) sink[blockIdx.x] = t;  // never true for these operands
+}
+
 }  // namespace
 }  // namespace oeb
+
+extern "C" oeb_status oeb_probe_fp64_add_rate(double* adds_per_second, double* adds_per_launch) {
+  if (!adds_per_second) return OEB_ERR_NULL;
+  int dev = 0, sms = 1;
+  OEB_CUDA_TRY(cudaGetDevice(&dev));
+  OEB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int ctas = sms * 8, threads = 256, iters = 1 << 14;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  OEB_CUDA_TRY(cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // the first launch is the warm-up
+    cudaEventRecord(e0, 0);
+    oeb::fp64_add_rate_kernel<<<ctas, threads>>>(iters, 0.5, nullptr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    oeb::count_launches(1);
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return oeb::cuda_fail(e);
+  const double adds = (double)ctas * threads * iters * oeb::kChains;
+  *adds_per_second = best > 0.f ? adds / (best * 1e-3) : 0.0;
+  if (adds_per_launch) *adds_per_launch = adds;
+  return OEB_OK;
+}
 
 extern "C" oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int mode, uint64_t* mismatches,
                                         uint64_t* first) {

@@ -48,9 +48,12 @@ def test_fp64_pipe_counts_present(bench):
 
 
 def test_fp64_pipe_roofline_arithmetic(bench):
+    # the measured FP64 addition rate, rescaled from the probe's SM clock to the timed region's
     per_kernel = {k: 0.1 for k in NAMES}
-    r = bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {"sm_mhz": 2000.0}, 100)
-    rate = bench.FP64_PIPE_PER_CLK_SM * 100 * 2000e6
+    add_rate = 3.2e11
+    r = bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {"sm_mhz": 1800.0}, 100, add_rate,
+                                  {"sm_mhz": 2000.0})
+    rate = add_rate * 1800.0 / 2000.0
     pts = bench.NX * bench.NY * bench.NZ
     want_k = r["kernel_instr_per_point"] * pts / rate * 1e3
     assert r["kernel_bound_ms"] == pytest.approx(want_k, rel=1e-4)
@@ -58,5 +61,6 @@ def test_fp64_pipe_roofline_arithmetic(bench):
     want_s = sum(bench._ncu_summary(bench.PIPE_MIX_PROFILE, "fp64_instr_per_point_" + k) for k in NAMES) * pts / rate * 1e3
     assert r["step_bound_ms"] == pytest.approx(want_s, rel=1e-4)
     assert r["step_frac"] == pytest.approx(want_s / 1.0, rel=1e-3)
-    # no clock sample: no roof
-    assert bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {}, 100) is None
+    assert r["rate_per_clk_per_sm"] == pytest.approx(add_rate / (100 * 2000e6), rel=1e-3)
+    # no measured rate: no roof
+    assert bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {"sm_mhz": 1800.0}, 100, None, {}) is None

@@ -12,12 +12,15 @@ shift of an addition (a and a 2^-k with changed low bits).
 from __future__ import annotations
 
 import ctypes
+import os
 
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-PAIRS = 1 << 26
+# 2^26 seeded pairs per case by default; OEB_SELFTEST_PAIRS raises it (e.g. 2^30 = 1073741824,
+# about a minute a case) for a longer search of the operand space
+PAIRS = int(os.environ.get("OEB_SELFTEST_PAIRS", 1 << 26))
 
 
 @pytest.mark.parametrize("mode", range(8), ids=["any-bits", "ordinary", "range-ends", "ties", "carries", "exact",
@@ -41,3 +44,16 @@ def test_selftest_rejects_bad_arguments(pkg, cuda):
     assert lib.oeb_selftest_fp64(ctypes.c_int(0), *args, ctypes.c_int(9), ctypes.byref(bad), None) != 0
     assert lib.oeb_selftest_fp64(ctypes.c_int(5), *args, ctypes.c_int(0), ctypes.byref(bad), None) != 0
     assert lib.oeb_selftest_fp64(ctypes.c_int(0), *args, ctypes.c_int(0), None, None) != 0
+
+
+def test_fp64_add_rate_probe(pkg, cuda):
+    # the FP64 pipe's rate, which bench.py's FP64-pipe roofline divides by: on a GB300 it is
+    # about 1.6 additions a clock per SM (152 SMs, up to 2.07 GHz), far below the FP32 rate
+    lib = pkg.load_library()
+    rate, adds = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    assert lib.oeb_probe_fp64_add_rate(ctypes.byref(rate), ctypes.byref(adds)) == 0
+    import torch
+    sms = torch.cuda.get_device_properties(cuda).multi_processor_count
+    per_clk_at_max = rate.value / (sms * 2.07e9)
+    assert adds.value > 1e9 and 0.5 <= per_clk_at_max <= 64.0, (rate.value, per_clk_at_max)
+    assert lib.oeb_probe_fp64_add_rate(None, None) != 0
