@@ -118,6 +118,11 @@ OEB_API oeb_status oeb_stream_synchronize(void* stream);
  * thread; 0 (the default) restores each kernel's own choice.  A tuning knob: results do not
  * depend on it.  Batch plans record and tune their own. */
 OEB_API oeb_status oeb_set_kblock(int kb);
+/* Tile shape of the pointwise advection kernels (hadvuv, hadvuv5th and their adjoint terms),
+ * for every later call on every thread: 0 (the default) 32 x 32 cells a CTA, 1 = 32 x 8,
+ * 2 = 64 x 16.  OEB_ERR_ARGUMENT for any other value.  A tuning knob: results do not depend
+ * on it.  Batch plans choose their own shapes (oeb_batch_autotune). */
+OEB_API oeb_status oeb_set_tile_shape(int shape);
 /* k-slabs of the host entry points' copy/compute/copy pipeline (1..8), for every later call;
  * 0 (the default) picks 8 for synchronous calls that move 8 MB or more, and 1 for smaller
  * and for asynchronous calls.  A tuning knob: results do not depend on it. */
@@ -785,15 +790,18 @@ OEB_API oeb_status oeb_batch_run(oeb_batch_plan* plan, void* stream);
 OEB_API oeb_status oeb_batch_autotune(oeb_batch_plan* plan, void* stream);
 /* Tuning records (no counterpart in the reference: its drivers take no tuning).  A record
  * keeps the autotuner's choices, so that a later process can apply them to a plan over the
- * same ensemble without timing anything again.  It holds two ints per batched launch, in
- * run order: kb (0 = each kernel's default, or 1, 2, 4, 8) and the launch form (0: one
+ * same ensemble without timing anything again.  It holds three ints per batched launch, in
+ * run order: kb (0 = each kernel's default, or 1, 2, 4, 8), the tile shape (0, 1, 2 as for
+ * oeb_set_tile_shape; kernels without shapes ignore it) and the launch form (0: one
  * persistent wave, sized on the device it is applied on; 1: one CTA per tile; 2: one
  * ordinary launch per member).
+ * oeb_batch_autotune times, for every launch, each kb with each tile shape in each form, and
+ *   keeps the fastest.
  * oeb_batch_tuning_get: *count = the plan's launches; with record != NULL it also writes
- *   2 * count ints there (OEB_ERR_TOO_LARGE if capacity, in launches, is below count).
+ *   3 * count ints there (OEB_ERR_TOO_LARGE if capacity, in launches, is below count).
  * oeb_batch_tuning_apply: OEB_ERR_ARGUMENT if count differs from the plan's launches or a
- *   kb or form is not one of the values above.  It records the step again for each kb
- *   named, waits for the device to go idle, then swaps in the new tables.  On any error the
+ *   kb, shape or form is not one of the values above.  It records the step again for each
+ *   (kb, shape) named, waits for the device to go idle, then swaps in the new tables.  On any error the
  *   plan is unchanged.  Results do not depend on the record.  Do not call it during a
  *   stream capture.
  * oeb_batch_signature: a 64-bit hash of the modes, each member's element size and domain

@@ -226,7 +226,7 @@ class BatchPlan:
     def autotune(self, stream=None):
         check(entry("oeb_batch_autotune")(self._plan, ctypes.c_void_p(_stream(stream))), "oeb_batch_autotune")
 
-    TUNING_FORMAT = "oeb-batch-tuning/1"
+    TUNING_FORMAT = "oeb-batch-tuning/2"
 
     @property
     def signature(self) -> int:
@@ -236,23 +236,27 @@ class BatchPlan:
         check(entry("oeb_batch_signature")(self._plan, ctypes.byref(out)), "oeb_batch_signature")
         return int(out.value)
 
-    def tuning(self) -> List[Tuple[int, int]]:
-        """The plan's launch choices, (kb, form) per batched launch in run order
-        (oeb_batch_tuning_get); form 0 is one persistent wave, 1 one CTA per tile, 2 one
+    def tuning(self) -> List[Tuple[int, int, int]]:
+        """The plan's launch choices, (kb, tile shape, form) per batched launch in run order
+        (oeb_batch_tuning_get); shape 0 is 32 x 32 cells a CTA, 1 32 x 8, 2 64 x 16 (for the
+        kernels that take one); form 0 is one persistent wave, 1 one CTA per tile, 2 one
         ordinary launch per member."""
         n = ctypes.c_int()
         check(entry("oeb_batch_tuning_get")(self._plan, None, ctypes.c_int(0), ctypes.byref(n)),
               "oeb_batch_tuning_get")
-        rec = (ctypes.c_int * (2 * max(n.value, 1)))()
+        rec = (ctypes.c_int * (3 * max(n.value, 1)))()
         check(entry("oeb_batch_tuning_get")(self._plan, rec, n, ctypes.byref(n)), "oeb_batch_tuning_get")
-        return [(rec[2 * i], rec[2 * i + 1]) for i in range(n.value)]
+        return [(rec[3 * i], rec[3 * i + 1], rec[3 * i + 2]) for i in range(n.value)]
 
     def apply_tuning(self, choices) -> None:
         """Makes the plan launch as `choices` says (oeb_batch_tuning_apply): as tuning()
         returns them, here or in another process, for a plan with the same signature."""
-        flat = [int(v) for kb_form in choices for v in kb_form]
+        choices = [tuple(c) for c in choices]
+        if any(len(c) != 3 for c in choices):
+            raise OebError("a tuning choice is (kb, shape, form)", 12)
+        flat = [int(v) for c in choices for v in c]
         rec = (ctypes.c_int * max(len(flat), 1))(*flat)
-        check(entry("oeb_batch_tuning_apply")(self._plan, rec, ctypes.c_int(len(flat) // 2)),
+        check(entry("oeb_batch_tuning_apply")(self._plan, rec, ctypes.c_int(len(flat) // 3)),
               "oeb_batch_tuning_apply")
 
     def save_tuning(self, path) -> None:

@@ -81,6 +81,11 @@ std::atomic<int> g_kb_override{0};
 int kb_override() { return g_kb_override.load(std::memory_order_relaxed); }
 
 namespace {
+std::atomic<int> g_shape_override{0};
+}  // namespace
+int shape_override() { return g_shape_override.load(std::memory_order_relaxed); }
+
+namespace {
 thread_local int t_host_in_place = 0;
 }  // namespace
 bool fields_in_host_memory() { return t_host_in_place > 0; }
@@ -432,6 +437,12 @@ static int64_t span_bytes(const M* m) {
 
 extern "C" int64_t oeb_memref3d_span_bytes_f64(const oeb_memref3d_f64* m) { return span_bytes<oeb_memref3d_f64, double>(m); }
 extern "C" int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m) { return span_bytes<oeb_memref3d_f32, float>(m); }
+
+extern "C" oeb_status oeb_set_tile_shape(int shape) {
+  if (shape < 0 || shape >= oeb::kShapes) return OEB_ERR_ARGUMENT;
+  oeb::g_shape_override.store(shape, std::memory_order_relaxed);
+  return OEB_OK;
+}
 
 extern "C" oeb_status oeb_set_kblock(int kb) {
   if (kb < 0 || kb > 1024) return OEB_ERR_ARGUMENT;

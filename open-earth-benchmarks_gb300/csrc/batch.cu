@@ -58,6 +58,8 @@ struct Slot {
   size_t tiles_off = 0, args_off = 0;  // into the device table buffer
   int ctas = 0;
   int kb = 0;
+  int shape = 0;      // the tile shape the slot was recorded with (tuned_shape)
+  int shape_tag = 0;  // its kernel's shape (0: the kernel takes none, so `shape` made no difference)
   bool per_member = false;  // run as one ordinary launch per member
   // per member, in slot order: grid, dynamic shared memory and argument pack (host copy)
   std::vector<dim3> grids;
@@ -161,8 +163,9 @@ oeb_status record(Member& m, int mode, Recorder* rec) {
   return st;
 }
 
-// Recorded sequences of every member for every mode in the plan, with k-blocking kb.
-oeb_status record_all(oeb_batch_plan* p, int kb, std::vector<std::vector<std::vector<LaunchRecord>>>* out) {
+// Recorded sequences of every member for every mode in the plan, with k-blocking kb and tile
+// shape `shape`.
+oeb_status record_all(oeb_batch_plan* p, int kb, int shape, std::vector<std::vector<std::vector<LaunchRecord>>>* out) {
   out->assign(2, {});
   for (int mi = 0; mi < 2; ++mi) {
     if (!(p->modes & kModes[mi])) continue;
@@ -171,6 +174,7 @@ oeb_status record_all(oeb_batch_plan* p, int kb, std::vector<std::vector<std::ve
       Member& m = p->members[i];
       Recorder rec;
       rec.kb = kb;
+      rec.shape = shape;
       rec.arena = p->arena + m.arena_off;
       rec.arena_bytes = m.arena_size;
       OEB_TRY(record(m, kModes[mi], &rec));
@@ -184,7 +188,7 @@ oeb_status record_all(oeb_batch_plan* p, int kb, std::vector<std::vector<std::ve
 // members of one precision record the same launches; the two precisions may record different
 // numbers of them (FP32 fvtp2d is one launch, FP64 two), so positions count per precision.
 oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vector<LaunchRecord>>>& seq, int kb,
-                       std::vector<Slot>* slots, std::vector<char>* host, size_t base) {
+                       int shape, std::vector<Slot>* slots, std::vector<char>* host, size_t base) {
   for (int mi = 0; mi < 2; ++mi) {
     if (!(p->modes & kModes[mi])) continue;
     const auto& per = seq[mi];
@@ -219,6 +223,8 @@ oeb_status build_slots(oeb_batch_plan* p, const std::vector<std::vector<std::vec
         sl.members = (int)who.size();
         sl.smem = 0;
         sl.kb = kb;
+        sl.shape = shape;
+        sl.shape_tag = r0.shape_tag;
         int64_t total = 0;
         std::vector<BatchTile> tiles;
         std::vector<char> args;
@@ -382,9 +388,9 @@ oeb_status create(const oeb_batch_member* in, int count, int modes, oeb_batch_pl
   }
   // 2. recording and 3. tables, default k-blocking
   std::vector<std::vector<std::vector<LaunchRecord>>> seq;
-  oeb_status st = record_all(p, 0, &seq);
+  oeb_status st = record_all(p, 0, 0, &seq);
   std::vector<char> host;
-  if (st == OEB_OK) st = build_slots(p, seq, 0, &p->slots, &host, 0);
+  if (st == OEB_OK) st = build_slots(p, seq, 0, 0, &p->slots, &host, 0);
   if (st == OEB_OK) st = upload(p, host);
   if (st != OEB_OK) return fail(st);
   *out = p;
@@ -394,19 +400,21 @@ oeb_status create(const oeb_batch_member* in, int count, int modes, oeb_batch_pl
 oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
   const int kbs[] = {1, 2, 4, 8};
   constexpr int kReps = 3;
-  // every candidate's slots, in one table buffer
+  // every candidate's slots -- each k-blocking with each tile shape -- in one table buffer
   std::vector<std::vector<Slot>> cand;
   std::vector<char> host;
-  for (int kb : kbs) {
-    std::vector<std::vector<std::vector<LaunchRecord>>> seq;
-    OEB_TRY(record_all(p, kb, &seq));
-    std::vector<Slot> slots;
-    OEB_TRY(build_slots(p, seq, kb, &slots, &host, 0));
-    if (slots.size() != p->slots.size()) return OEB_ERR_UNSUPPORTED;
-    cand.push_back(std::move(slots));
+  for (int shape = 0; shape < kShapes; ++shape) {
+    for (int kb : kbs) {
+      std::vector<std::vector<std::vector<LaunchRecord>>> seq;
+      OEB_TRY(record_all(p, kb, shape, &seq));
+      std::vector<Slot> slots;
+      OEB_TRY(build_slots(p, seq, kb, shape, &slots, &host, 0));
+      if (slots.size() != p->slots.size()) return OEB_ERR_UNSUPPORTED;
+      cand.push_back(std::move(slots));
+    }
   }
   OEB_TRY(upload(p, host));
-  // the default choice of every slot: kb = 4, one persistent wave
+  // the default choice of every slot: kb = 4, the default shape, one persistent wave
   std::vector<Slot> best = cand[2];
   // buffers hold the data of a complete run before single launches are timed
   for (size_t i = 0; i < best.size(); ++i) best[i].ctas = std::min(best[i].total, best[i].occupancy * p->sms);
@@ -422,6 +430,8 @@ oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
     float best_ms = -1.f;
     for (auto& c : cand) {
       const Slot& sl = c[i];
+      // a shape other than the default changes nothing for a kernel that takes none
+      if (sl.shape != 0 && sl.shape_tag == 0) continue;
       const cudaStream_t s = sl.side ? p->side : st;
       // persistent wave, one CTA per tile (batched launches), then per-member launches
       const int wave = std::min(sl.total, sl.occupancy * p->sms);
@@ -456,11 +466,12 @@ oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
 
 // ---- tuning records ------------------------------------------------------------------
 // A record keeps the autotuner's choices so that a later process can reuse them without
-// timing anything: two ints a slot, in run order -- the slot's kb, and its launch form
-// (kFormWave: one persistent wave; kFormPerTile: one CTA per tile; kFormPerMember: one
-// ordinary launch per member).  The wave's CTA count is taken from the device the record is
-// applied on.  kb is one of the values a plan records with: 0 (every kernel's own default,
-// as at creation) or 1, 2, 4, 8 (the autotuner's candidates).
+// timing anything: three ints a slot, in run order -- the slot's kb, its tile shape, and its
+// launch form (kFormWave: one persistent wave; kFormPerTile: one CTA per tile;
+// kFormPerMember: one ordinary launch per member).  The wave's CTA count is taken from the
+// device the record is applied on.  kb is one of the values a plan records with: 0 (every
+// kernel's own default, as at creation) or 1, 2, 4, 8 (the autotuner's candidates); the shape
+// is 0 .. kShapes-1 (tuned_shape).
 constexpr int kFormWave = 0, kFormPerTile = 1, kFormPerMember = 2;
 
 int wave_ctas(const oeb_batch_plan* p, const Slot& sl) { return std::min(sl.total, sl.occupancy * p->sms); }
@@ -496,8 +507,9 @@ oeb_status tuning_get(const oeb_batch_plan* p, int* rec, int capacity, int* coun
   if (capacity < *count) return OEB_ERR_TOO_LARGE;
   for (size_t i = 0; i < p->slots.size(); ++i) {
     const Slot& sl = p->slots[i];
-    rec[2 * i] = sl.kb;
-    rec[2 * i + 1] = sl.per_member ? kFormPerMember : (sl.ctas == wave_ctas(p, sl) ? kFormWave : kFormPerTile);
+    rec[3 * i] = sl.kb;
+    rec[3 * i + 1] = sl.shape;
+    rec[3 * i + 2] = sl.per_member ? kFormPerMember : (sl.ctas == wave_ctas(p, sl) ? kFormWave : kFormPerTile);
   }
   return OEB_OK;
 }
@@ -508,27 +520,29 @@ oeb_status tuning_get(const oeb_batch_plan* p, int* rec, int capacity, int* coun
 oeb_status tuning_apply(oeb_batch_plan* p, const int* rec, int count) {
   if (!rec) return OEB_ERR_NULL;
   if (count != (int)p->slots.size()) return OEB_ERR_ARGUMENT;
-  std::vector<int> kbs;
+  std::vector<std::pair<int, int>> recs;  // the (kb, shape) pairs the record names
   for (int i = 0; i < count; ++i) {
-    const int kb = rec[2 * i], form = rec[2 * i + 1];
-    if (!recorded_kb(kb) || form < kFormWave || form > kFormPerMember) return OEB_ERR_ARGUMENT;
-    if (std::find(kbs.begin(), kbs.end(), kb) == kbs.end()) kbs.push_back(kb);
+    const int kb = rec[3 * i], shape = rec[3 * i + 1], form = rec[3 * i + 2];
+    if (!recorded_kb(kb) || shape < 0 || shape >= kShapes || form < kFormWave || form > kFormPerMember)
+      return OEB_ERR_ARGUMENT;
+    if (std::find(recs.begin(), recs.end(), std::make_pair(kb, shape)) == recs.end()) recs.push_back({kb, shape});
   }
   std::vector<std::vector<Slot>> cand;
   std::vector<char> host;
-  for (int kb : kbs) {
+  for (const auto& ks : recs) {
     std::vector<std::vector<std::vector<LaunchRecord>>> seq;
-    OEB_TRY(record_all(p, kb, &seq));
+    OEB_TRY(record_all(p, ks.first, ks.second, &seq));
     std::vector<Slot> slots;
-    OEB_TRY(build_slots(p, seq, kb, &slots, &host, 0));
+    OEB_TRY(build_slots(p, seq, ks.first, ks.second, &slots, &host, 0));
     if (slots.size() != p->slots.size()) return OEB_ERR_UNSUPPORTED;
     cand.push_back(std::move(slots));
   }
   std::vector<Slot> next(count);
   for (int i = 0; i < count; ++i) {
-    const size_t c = (size_t)(std::find(kbs.begin(), kbs.end(), rec[2 * i]) - kbs.begin());
+    const size_t c = (size_t)(std::find(recs.begin(), recs.end(), std::make_pair(rec[3 * i], rec[3 * i + 1])) -
+                              recs.begin());
     Slot sl = cand[c][i];
-    const int form = rec[2 * i + 1];
+    const int form = rec[3 * i + 2];
     sl.per_member = form == kFormPerMember;
     sl.ctas = form == kFormPerTile ? sl.total : wave_ctas(p, sl);
     next[i] = std::move(sl);

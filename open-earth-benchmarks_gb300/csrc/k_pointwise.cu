@@ -28,6 +28,38 @@ namespace {
 
 constexpr int kTI = 32, kTJ = 32, kRows = kTJ / kTY;
 
+// Tile width and height (cells) of tile shape S (tuned_shape): 32 x 32, 32 x 8, 64 x 16.
+template <int S>
+struct TileOf {
+  static constexpr int I = S == 2 ? 64 : 32;
+  static constexpr int J = S == 0 ? 32 : S == 1 ? 8 : 16;
+};
+
+// Visits the points of this thread in a TI x TJ tile: TI / 32 columns 32 apart, TJ / 8 rows 8
+// apart (U of them unrolled); f(o, j) with o the in-plane offset of (i, j) plus the plane
+// offset of k.
+template <int TI, int TJ, int U, class F>
+__device__ __forceinline__ void for_points_tile(const uint3& blk, const Dims& d, int kb, F&& f) {
+  const int k0 = blk.z * kb;
+  const int k1 = min(k0 + kb, d.nz);
+  const int sj = (int)d.sj;
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll 1
+    for (int c = 0; c < TI / 32; ++c) {
+      const int i = blk.x * TI + 32 * c + threadIdx.x;
+      if (i < d.nx) {
+#pragma unroll U
+        for (int r = 0; r < TJ / kTY; ++r) {
+          const int j = blk.y * TJ + threadIdx.y + kTY * r;
+          if (j < d.ny) f(kofs + i + j * sj, j);
+        }
+      }
+    }
+  }
+}
+
 // Visits the points of this thread: f(o, j) with o the in-plane offset of (i, j) plus the
 // plane offset of k.
 template <int U = kRows, class F>
@@ -246,8 +278,9 @@ __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64
   }
 }
 
-template <class T, int ORDER>
+template <class T, int ORDER, int SHAPE = 0>
 struct hadv_kernel {
+  static constexpr int kShape = SHAPE;
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
                                              const T* __restrict__ uin, const T* __restrict__ vin,
                                              const T* __restrict__ acrlat0, const T* __restrict__ acrlat1,
@@ -256,7 +289,7 @@ struct hadv_kernel {
     const int64_t sj = d.sj;
     constexpr T third = T(1.0) / T(3.0);
     constexpr T rr = earth_radius_recip<T>();
-    for_points<HeavyRowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
+    for_points_tile<TileOf<SHAPE>::I, TileOf<SHAPE>::J, HeavyRowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
       const int64_t jo = (int64_t)j * s1d;
       const T u0 = ld(uin + o), v0 = ld(vin + o);
       const T um = ld(uin + o - 1) + u0;  // uin(i-1)+uin(i), first pair of both averages
@@ -629,9 +662,19 @@ oeb_status hadv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* v
                                                         t0.lo, t0.hi, t1.lo, t1.hi}));
   OEB_RETURN_IF_VALIDATING();
   const int kb = tuned_kb(kKB);
-  return launch<hadv_kernel<T, ORDER>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
-                                       gvi.origin, a0.origin, a1.origin, t0.origin, t1.origin, a0.s, eddlat, eddlon,
-                                       make_dims(*dom, gu), kb);
+  auto go = [&](auto body, int shape) {
+    using B = decltype(body);
+    constexpr int S = B::kShape;
+    (void)shape;
+    return launch<B>(tile_grid((int)dom->nx, (int)dom->ny, (int)dom->nz, TileOf<S>::I, TileOf<S>::J, kb), 0,
+                     (cudaStream_t)stream, gu.origin, gv.origin, gui.origin, gvi.origin, a0.origin, a1.origin,
+                     t0.origin, t1.origin, a0.s, eddlat, eddlon, make_dims(*dom, gu), kb);
+  };
+  switch (tuned_shape()) {
+    case 1: return go(hadv_kernel<T, ORDER, 1>{}, 1);
+    case 2: return go(hadv_kernel<T, ORDER, 2>{}, 2);
+    default: return go(hadv_kernel<T, ORDER, 0>{}, 0);
+  }
 }
 
 // Tangent-linear hadvuv / hadvuv5th: d(uout, vout) = J(uin, vin) d(uin, vin), on Dual<T>.
@@ -719,11 +762,12 @@ __device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t
   return acc;
 }
 
-template <class T, int ORDER>
+template <class T, int ORDER, int SHAPE = 0>
 struct hadv_adj_terms_kernel {
   // FP64: 80 registers instead of 94, three CTAs per SM instead of two (the hadvuv5th
   // adjoint 4 % faster; the same bound on the hdiffsmag and fastwavesuv adjoints was slower)
   static constexpr int kMinCtas = sizeof(T) == 8 ? 3 : 0;
+  static constexpr int kShape = SHAPE;
   static __device__ __forceinline__ void run(const uint3& blk, HadvTerms<T> tm, const T* __restrict__ uin,
                                              const T* __restrict__ vin, const T* __restrict__ acrlat0,
                                              const T* __restrict__ acrlat1, const T* __restrict__ tgrlatda0,
@@ -733,7 +777,7 @@ struct hadv_adj_terms_kernel {
     const int64_t sj = d.sj;
     constexpr T third = T(1.0) / T(3.0);
     constexpr T rr = earth_radius_recip<T>();
-    for_points<RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
+    for_points_tile<TileOf<SHAPE>::I, TileOf<SHAPE>::J, RowUnroll<T>::value>(blk, d, kb, [&](int64_t o, int j) {
       const int64_t jo = (int64_t)j * s1d;
       const T u0 = ld(uin + o), v0 = ld(vin + o);
       const T um = ld(uin + o - 1) + u0;
@@ -859,11 +903,20 @@ oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M
   tm.fl = reinterpret_cast<unsigned char*>(base + 9 * n) + org;
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
   const int kb = tuned_kb(kKB);
-  oeb_status stt = launch<hadv_adj_terms_kernel<T, ORDER>>(
-      grid_for(*dom, kb), 0, st, tm, gui.origin, gvi.origin, (const T*)acrlat0->aligned + acrlat0->offset,
-      (const T*)acrlat1->aligned + acrlat1->offset, (const T*)tgrlatda0->aligned + tgrlatda0->offset,
-      (const T*)tgrlatda1->aligned + tgrlatda1->offset, acrlat0->strides[0], guo.origin, gvo.origin, eddlat, eddlon, d,
-      kb);
+  auto terms = [&](auto body) {
+    using B = decltype(body);
+    constexpr int S = B::kShape;
+    return launch<B>(tile_grid(d.nx, d.ny, d.nz, TileOf<S>::I, TileOf<S>::J, kb), 0, st, tm, gui.origin, gvi.origin,
+                     (const T*)acrlat0->aligned + acrlat0->offset, (const T*)acrlat1->aligned + acrlat1->offset,
+                     (const T*)tgrlatda0->aligned + tgrlatda0->offset, (const T*)tgrlatda1->aligned + tgrlatda1->offset,
+                     acrlat0->strides[0], guo.origin, gvo.origin, eddlat, eddlon, d, kb);
+  };
+  oeb_status stt;
+  switch (tuned_shape()) {
+    case 1: stt = terms(hadv_adj_terms_kernel<T, ORDER, 1>{}); break;
+    case 2: stt = terms(hadv_adj_terms_kernel<T, ORDER, 2>{}); break;
+    default: stt = terms(hadv_adj_terms_kernel<T, ORDER, 0>{}); break;
+  }
   if (stt == OEB_OK)
     stt = launch<hadv_adj_gather_kernel<T, ORDER>>(tile_grid(d.nx + 2 * h, d.ny + 2 * h, d.nz, kTI, kTJ, kb), 0, st,
                                                    gub.origin, gvb.origin, tm, d, kb);

@@ -82,6 +82,17 @@ struct MinCtas<Body, std::void_t<decltype(Body::kMinCtas)>> {
   static constexpr int value = Body::kMinCtas;
 };
 
+// The tile shape a body was instantiated with (kShape, see tuned_shape), 0 for bodies that
+// take no shape.
+template <class Body, class = void>
+struct ShapeOf {
+  static constexpr int value = 0;
+};
+template <class Body>
+struct ShapeOf<Body, std::void_t<decltype(Body::kShape)>> {
+  static constexpr int value = Body::kShape;
+};
+
 // The grid kernel of Body over arguments A...
 template <class Body, class... A>
 constexpr auto grid_entry() {
@@ -128,6 +139,7 @@ using GridLaunchFn = oeb_status (*)(const void* args, dim3 grid, size_t smem, cu
 
 struct LaunchRecord {
   BatchLaunchFn launcher;  // also identifies the kernel (Body and argument types)
+  int shape_tag = 0;       // the body's tile shape (ShapeOf); 0 for bodies that take none
   GridLaunchFn grid_launcher;
   BatchOccupancyFn occupancy;
   dim3 grid;
@@ -145,7 +157,8 @@ struct Recorder {
   // returns; the stack pops every freed allocation on its top, so later calls reuse the space
   // (safe: a batch runs each recorded launch for all members before the next one).
   std::vector<std::pair<size_t, bool>> live;
-  int kb = 0;  // k-levels per CTA for the kernels that take one (0: their default)
+  int kb = 0;     // k-levels per CTA for the kernels that take one (0: their default)
+  int shape = 0;  // tile shape for the kernels that take one (0: their default; tuned_shape)
 };
 
 Recorder* recorder();             // the calling thread's recorder, or nullptr
@@ -158,6 +171,17 @@ inline int tuned_kb(int def) {
   if (r && r->kb > 0) return r->kb;
   const int o = kb_override();
   return o > 0 ? o : def;
+}
+
+// Tile shapes of the pointwise bodies that take one: 0 = 32 x 32 (the default), 1 = 32 x 8,
+// 2 = 64 x 16 (i x j cells a CTA of 32 x 8 threads covers).
+constexpr int kShapes = 3;
+int shape_override();  // set by oeb_set_tile_shape (0: none)
+// The tile shape: the recorder's while recording, else oeb_set_tile_shape's.
+inline int tuned_shape() {
+  const Recorder* r = recorder();
+  if (r) return r->shape;
+  return shape_override();
 }
 
 oeb_status scratch_alloc(void** p, size_t bytes, cudaStream_t st);
@@ -215,6 +239,11 @@ struct Rebind<K<double, N>> {
   using type = K<F64i, N>;
   static constexpr bool on = true;
 };
+template <template <class, int, int> class K, int N, int M>
+struct Rebind<K<double, N, M>> {
+  using type = K<F64i, N, M>;
+  static constexpr bool on = true;
+};
 
 template <class A>
 struct ArgMap {
@@ -263,6 +292,7 @@ oeb_status launch_as(dim3 grid, size_t smem, cudaStream_t st, A... a) {
   if (Recorder* r = recorder()) {
     LaunchRecord rec;
     rec.launcher = &batch_launch<Body, A...>;
+    rec.shape_tag = ShapeOf<Body>::value;
     rec.grid_launcher = &grid_launch_packed<Body, A...>;
     rec.occupancy = &batch_occupancy<Body, A...>;
     rec.grid = grid;

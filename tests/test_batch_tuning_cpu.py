@@ -44,36 +44,36 @@ def test_abi_rejects_a_null_plan(pkg):
     lib = pkg.load_library()
     n = ctypes.c_int(-1)
     sig = ctypes.c_uint64()
-    rec = (ctypes.c_int * 4)()
+    rec = (ctypes.c_int * 6)()
     assert lib.oeb_batch_tuning_get(None, rec, 2, ctypes.byref(n)) == 1  # OEB_ERR_NULL
     assert lib.oeb_batch_tuning_apply(None, rec, 2) == 1
     assert lib.oeb_batch_signature(None, ctypes.byref(sig)) == 1
 
 
 def test_saved_record_is_applied_to_a_plan_with_the_same_signature(chain, tmp_path):
-    choices = [(4, 0), (1, 2), (8, 1), (0, 0)]
+    choices = [(4, 0, 0), (1, 2, 2), (8, 1, 1), (0, 0, 0)]
     a = _stand_in(chain, 0x0123456789ABCDEF, choices)
     path = tmp_path / "t.json"
     a.save_tuning(path)
     rec = json.loads(path.read_text())
     assert rec == {"format": chain.BatchPlan.TUNING_FORMAT, "signature": "0123456789abcdef",
                    "choices": [list(c) for c in choices]}
-    b = _stand_in(chain, 0x0123456789ABCDEF, [(0, 0)] * 4)
+    b = _stand_in(chain, 0x0123456789ABCDEF, [(0, 0, 0)] * 4)
     b.load_tuning(path)
     assert b.applied == choices
 
 
 def test_record_of_another_ensemble_or_format_is_refused(pkg, chain, tmp_path):
     path = tmp_path / "t.json"
-    _stand_in(chain, 7, [(2, 0)]).save_tuning(path)
-    other = _stand_in(chain, 8, [(0, 0)])
+    _stand_in(chain, 7, [(2, 1, 0)]).save_tuning(path)
+    other = _stand_in(chain, 8, [(0, 0, 0)])
     with pytest.raises(pkg.OebError, match="another ensemble"):
         other.load_tuning(path)
     assert other.applied is None
     rec = json.loads(path.read_text())
-    rec["format"] = "oeb-batch-tuning/0"
+    rec["format"] = "oeb-batch-tuning/1"
     path.write_text(json.dumps(rec))
-    same = _stand_in(chain, 7, [(0, 0)])
+    same = _stand_in(chain, 7, [(0, 0, 0)])
     with pytest.raises(pkg.OebError, match="not a batch tuning record"):
         same.load_tuning(path)
     assert same.applied is None

@@ -143,11 +143,11 @@ def test_tuning_record_applies_to_a_new_plan(pkg, fields, chain, cuda, tmp_path)
 
     a = chain.BatchPlan(members(), chain.FORWARD | chain.ADJOINT)
     default = a.tuning()
-    assert default and all(c == (0, 0) for c in default)
+    assert default and all(c == (0, 0, 0) for c in default)
     a.autotune()
     tuned = a.tuning()
     assert len(tuned) == len(default)
-    assert all(kb in (1, 2, 4, 8) and form in (0, 1, 2) for kb, form in tuned)
+    assert all(kb in (1, 2, 4, 8) and shape in (0, 1, 2) and form in (0, 1, 2) for kb, shape, form in tuned)
     path = tmp_path / "tuning.json"
     a.save_tuning(path)
     b_members = members()
@@ -191,7 +191,8 @@ def test_tuning_record_rejected_for_another_plan(pkg, fields, chain, cuda, tmp_p
     with pytest.raises(pkg.OebError):
         c.load_tuning(other)
     n = len(before)
-    for bad in ([(0, 0)] * (n + 1), [(3, 0)] + before[1:], [(1, 3)] + before[1:], [(-1, 0)] + before[1:]):
+    for bad in ([(0, 0, 0)] * (n + 1), [(3, 0, 0)] + before[1:], [(1, 0, 3)] + before[1:], [(-1, 0, 0)] + before[1:],
+                [(1, 3, 0)] + before[1:], [(1, -1, 0)] + before[1:]):
         with pytest.raises(pkg.OebError) as err:
             c.apply_tuning(bad)
         assert err.value.status == 12  # OEB_ERR_ARGUMENT

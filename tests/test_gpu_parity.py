@@ -164,6 +164,56 @@ def test_kblock_does_not_change_results(pkg, fields, orc, cuda, kb):
         lib.oeb_set_kblock(0)
 
 
+@pytest.mark.parametrize("shape", [1, 2], ids=["32x8", "64x16"])
+def test_tile_shape_does_not_change_results(pkg, fields, orc, cuda, shape):
+    # oeb_set_tile_shape changes the tiles of the advection stencils (forward bit-exact with
+    # the oracle; ragged tiles on every edge), never a result
+    lib = pkg.load_library()
+    assert lib.oeb_set_tile_shape(shape) == 0
+    try:
+        for name in ("hadvuv", "hadvuv5th"):
+            _run_both(pkg, fields, orc, cuda, name, 70, 41, 5, seed=15)
+    finally:
+        lib.oeb_set_tile_shape(0)
+    assert lib.oeb_set_tile_shape(3) != 0 and lib.oeb_set_tile_shape(-1) != 0
+
+
+@pytest.mark.parametrize("shape", [1, 2], ids=["32x8", "64x16"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_tile_shape_adjoint_bits(pkg, fields, cuda, shape, dtype):
+    # the advection adjoints (their terms kernel takes the tile shape) give the same bits in
+    # every shape
+    import torch
+    lib = pkg.load_library()
+    nx, ny, nz = 70, 41, 5
+    for name in ("hadvuv", "hadvuv5th"):
+        spec = pkg.KERNELS[name]
+        x = fields.make_inputs(name, nx, ny, nz, seed=16)
+        sc = fields.make_scalars(name, seed=16)
+        rng = np.random.default_rng(16)
+        yb = {n: rng.normal(size=x["uin"].shape) for n in spec.semantic_outputs}
+
+        def dev(a):
+            t = torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(cuda)
+            return pkg.Storage(t, H, nx=nx if t.ndim == 3 else None)
+
+        def adj():
+            xb = {n: dev(np.zeros_like(x["uin"])) for n in pkg.ACTIVE[name]}
+            pkg.adjoint(name, {k: dev(v) for k, v in x.items()}, {k: dev(v) for k, v in yb.items()}, xb, sc,
+                        domain=(nx, ny, nz))
+            torch.cuda.synchronize()
+            return {k: v.numpy() for k, v in xb.items()}
+
+        want = adj()
+        assert lib.oeb_set_tile_shape(shape) == 0
+        try:
+            got = adj()
+        finally:
+            lib.oeb_set_tile_shape(0)
+        for n in want:
+            assert_bitwise_equal(got[n], want[n], "%s adjoint %sb shape %d" % (name, n, shape))
+
+
 @pytest.mark.parametrize("slabs", [2, 3, 8])
 def test_host_slabs_do_not_change_results(pkg, fields, orc, slabs):
     # the staged host path over 2, 3 and 8 k-slabs (7 levels: uneven slabs)
