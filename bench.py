@@ -776,7 +776,9 @@ def _batch_leg(pkg, fields, torch, dev, args):
            "per_member_launches_ms_per_run": round(ms_members, 3),
            "per_member_launches_per_run": g2.kernels,
            "speedup_vs_per_member_launches": round(ms_members / ms_batch, 3),
-           "autotune_s": round(tune_s, 2), "plan_bytes": plan.nbytes}
+           "autotune_s": round(tune_s, 2), "plan_bytes": plan.nbytes,
+           "plan_bytes_per_point": round(plan.nbytes / pts, 1),
+           "tuned": _tuning_summary(plan.tuning())}
     g.close()
     g2.close()
     for cp in plans:
@@ -785,6 +787,18 @@ def _batch_leg(pkg, fields, torch, dev, args):
     del members
     torch.cuda.empty_cache()
     return res
+
+
+def _tuning_summary(choices):
+    """How many of a plan's batched launches the autotuner gave each k-blocking, tile shape
+    and launch form."""
+    hist = {"kb": {}, "shape": {}, "form": {}}
+    names = {"shape": {0: "32x32", 1: "32x8", 2: "64x16"}, "form": {0: "wave", 1: "cta_per_tile", 2: "per_member"}}
+    for kb, shape, form in choices:
+        for key, v in (("kb", kb), ("shape", shape), ("form", form)):
+            label = names.get(key, {}).get(v, str(v))
+            hist[key][label] = hist[key].get(label, 0) + 1
+    return hist
 
 
 def _ncu_summary(kernel, key):

@@ -64,3 +64,9 @@ def test_fp64_pipe_roofline_arithmetic(bench):
     assert r["rate_per_clk_per_sm"] == pytest.approx(add_rate / (100 * 2000e6), rel=1e-3)
     # no measured rate: no roof
     assert bench._fp64_pipe_roofline(NAMES, per_kernel, "fvtp2d", 1.0, {"sm_mhz": 1800.0}, 100, None, {}) is None
+
+
+def test_tuning_summary_counts_each_choice(bench):
+    h = bench._tuning_summary([(4, 0, 0), (4, 2, 2), (1, 1, 0)])
+    assert h == {"kb": {"4": 2, "1": 1}, "shape": {"32x32": 1, "64x16": 1, "32x8": 1},
+                 "form": {"wave": 2, "per_member": 1}}
