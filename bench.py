@@ -1063,20 +1063,34 @@ def run_reference(args):
 
 
 def profile_one(args):
-    """`--profile-one K`: K alone, `--calls` times, for an ncu capture (prints nothing timed)."""
+    """`--profile-one K[,K...]`: each K alone, `--calls` times (with `--adjoint-calls`, its
+    adjoint instead, seeded with N(0, 1) output seeds), for an ncu capture (prints nothing
+    timed)."""
     import torch
     pkg = graft.load_package()
     import importlib
     fields = importlib.import_module("oeb_gb300.fields")
     dtype = np.float64 if args.precision == "f64" else np.float32
     shape = tuple(args.shape)
-    st, sc = _make_set(pkg, fields, torch, torch.device("cuda", 0), 2, [args.profile_one], dtype=dtype, shape=shape,
-                       workload=args.workload)[args.profile_one]
-    for _ in range(args.calls):
-        pkg.call(args.profile_one, st, sc, domain=shape)
+    dev = torch.device("cuda", 0)
+    names = args.profile_one.split(",")
+    for name in names:
+        st, sc = _make_set(pkg, fields, torch, dev, 2, [name], dtype=dtype, shape=shape, workload=args.workload)[name]
+        if args.adjoint_calls:
+            spec = pkg.KERNELS[name]
+            like = st[spec.semantic_outputs[0]]
+            rng = np.random.default_rng(1)
+            yb = {n: pkg.Storage(torch.from_numpy(rng.normal(size=like.data.shape).astype(dtype)).to(dev), HALO)
+                  for n in spec.semantic_outputs}
+            xb = {n: pkg.Storage(torch.zeros_like(like.data), HALO) for n in pkg.ACTIVE[name]}
+            for _ in range(args.calls):
+                pkg.adjoint(name, st, yb, xb, sc, domain=shape)
+        else:
+            for _ in range(args.calls):
+                pkg.call(name, st, sc, domain=shape)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_one": args.profile_one, "precision": args.precision, "shape": list(shape),
-                      "calls": args.calls}))
+    print(json.dumps({"profile_one": names, "adjoint": bool(args.adjoint_calls), "precision": args.precision,
+                      "shape": list(shape), "calls": args.calls}))
 
 
 def main():
@@ -1094,11 +1108,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--kernels", nargs="*", default=None,
                     help="run only these stencils in the step (profiling); the default line uses all ten")
-    ap.add_argument("--profile-one", default=None, help="run only this stencil --calls times (for ncu captures)")
+    ap.add_argument("--profile-one", default=None,
+                    help="run only these stencils (comma-separated) --calls times each (for ncu captures)")
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64")
     ap.add_argument("--shape", type=int, nargs=3, default=[NX, NY, NZ])
     ap.add_argument("--workload", choices=["physical", "fronts", "smooth"], default="physical")
     ap.add_argument("--calls", type=int, default=4)
+    ap.add_argument("--adjoint-calls", action="store_true",
+                    help="with --profile-one: run each stencil's adjoint instead of its forward")
     ap.add_argument("--port-vs-reference", action="store_true",
                     help="time the oracle port against the reference build on this host's cores (needs the "
                          "reference source tree) and exit")
