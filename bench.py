@@ -577,10 +577,21 @@ ADJ_KERNELS = ("hdiffsmag", "hadvuv5th", "fastwavesuv", "fvtp2d", "laplace", "hd
                "p_grad_c")
 
 
+def _queue_behind_sleep(torch, stream, ms):
+    """Enqueues on `stream` a kernel that spins for about `ms` milliseconds (at 2.07 GHz; longer
+    at lower clocks), so that the calls the host enqueues next are all queued before the GPU
+    reaches them: CUDA events between those calls then time the device, not the host's
+    dispatch of each call."""
+    with torch.cuda.stream(stream):
+        torch.cuda._sleep(int(ms * 2.07e6))
+
+
 def _adjoint_leg(pkg, fields, torch, dev, args, dtype, shape=(NX, NY, NZ)):
     """Forward + adjoint pairs of the ten stencils at `shape` (128x128x80 by default, seed 3):
     per kernel, the forward call and the adjoint call timed with CUDA events on the launch
-    stream, two input sets alternating."""
+    stream, two input sets alternating.  The timed calls are queued behind a sleep kernel
+    (`_queue_behind_sleep`) long enough for the host to enqueue them all, so the events time
+    the device even where a call's kernels are shorter than its host-side dispatch."""
     elem = 8 if dtype == np.float64 else 4
     stream = torch.cuda.current_stream(dev)
     dom = tuple(shape)
@@ -618,11 +629,15 @@ def _adjoint_leg(pkg, fields, torch, dev, args, dtype, shape=(NX, NY, NZ)):
             if ev is not None:
                 ev[2].record(stream)
 
+        torch.cuda.synchronize()
+        t = time.perf_counter()
         for w in range(args.warmup):
             run(sets[w % 2])
+        host_ms = (time.perf_counter() - t) * 1e3 / max(args.warmup, 1)
         torch.cuda.synchronize()
         evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
         l0 = lib.oeb_launch_count()
+        _queue_behind_sleep(torch, stream, 3.0 * host_ms * args.steps + 2.0)
         for i in range(args.steps):
             run(sets[i % 2], evs[i])
         torch.cuda.synchronize()
