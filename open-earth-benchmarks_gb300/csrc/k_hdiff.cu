@@ -14,9 +14,11 @@
 // Compiled with --fmad=false (see k_pointwise.cu).  One CTA of 32 x 8 threads per
 // 32 x 32 tile and kb k-levels.
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "precision.cuh"
+#include "stage.cuh"
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
@@ -101,6 +103,95 @@ struct hdiffsa_kernel {
           out[o] = s.in[b + 2][a + 2] + (((s.flx[b][a] - s.flx[b][a + 1]) + s.fly[b][a]) - s.fly[b + 1][a]) * ld(mask + o);
         }
       });
+      __syncthreads();
+    }
+  }
+};
+
+// FP32 hdiffsa.  In FP32 the kernel above is bound by instruction issue, not by HBM (ncu at
+// 256 x 256 x 80: 72 % issue active, "not selected" the top stall, 13 % of DRAM throughput):
+// five shared-memory phases a level, each with its own index arithmetic.  Here a level takes
+// two: the laplacian on its 34 x 34 box straight from the `in` tile (the differences
+// in(j+1) - in and in(j-1) - in formed where they are used; the kernel above stores
+// in(j+1) - in once and negates it, which gives the same bits), then each output forms the
+// four limited fluxes it reads (each flux is formed by the two outputs beside it, with the
+// same operations on the same operands).  The k-levels are marched: the `in` tile of level
+// k+1 is copied by cp.async into a second buffer while level k is computed.  Results are
+// hdiffsa_kernel<float>'s, bit for bit.  kb from staged_kb: about one wave of CTAs.
+// Measured alone (back-to-back launches): 256 x 256 x 80 41.3 -> 38.6 us, 128 x 128 x 80
+// 14.5 -> 12.7 us; 20 % fewer warp instructions (35.7 M -> 28.7 M a launch), still 67 % issue
+// active.  The marching alone, with the five phases, measured 41.2 us: the kernel waits on
+// its instructions, not on its loads.
+struct hdiffsa_f32 {
+  static constexpr int kCtasPerSm = 6;  // by registers (40)
+  struct Smem {
+    float in[2][36][36];  // (i0-2+a, j0-2+b)
+    float lap[34][34];    // (i0-1+a, j0-1+b)
+    float crlato[34], crlatu[34];  // j0-1+b
+  };
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ out, const float* __restrict__ in,
+                                             const float* __restrict__ mask, const float* __restrict__ crlato,
+                                             const float* __restrict__ crlatu, int64_t s1d, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    const int i0 = blk.x * kT, j0 = blk.y * kT;
+    const int sj = (int)d.sj;
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    if (tid < 34) {
+      const int j = j0 - 1 + tid;
+      const bool ok = j >= -1 && j < d.ny + 1;
+      s.crlato[tid] = ok ? ld(crlato + (int64_t)j * s1d) : 0.f;
+      s.crlatu[tid] = ok ? ld(crlatu + (int64_t)j * s1d) : 0.f;
+    }
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const int vx = max(0, min(kT, d.nx - i0)), vy = max(0, min(kT, d.ny - j0));
+    auto issue = [&](int k, float (*t)[36]) {
+      if (k < k1) {
+        const float* pin = in + (int64_t)k * d.sk;
+        for_region_lim<36, 36>(vx + 4, vy + 4, [&](int a, int b) {
+          const int i = i0 - 2 + a, j = j0 - 2 + b;
+          const bool ok = i >= -2 && i < d.nx + 2 && j >= -2 && j < d.ny + 2;
+          cp_async4(&t[b][a], ok ? pin + i + j * sj : pin, ok);
+        });
+      }
+      cp_async_commit();
+    };
+    issue(k0, s.in[0]);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int cur = (k - k0) & 1;
+      issue(k + 1, s.in[cur ^ 1]);  // the buffer level k-1 left
+      const int64_t kofs = (int64_t)k * d.sk;
+      cp_async_wait<1>();  // level k has landed
+      __syncthreads();
+      const float(*t)[36] = s.in[cur];
+      // hdiffsa.h:101: in(i-1)+in(i+1) - 2 in + crlato (in(j+1)-in) + crlatu (in(j-1)-in)
+      for_region_lim<34, 34>(vx + 2, vy + 2, [&](int a, int b) {
+        const float c = t[b + 1][a + 1];
+        s.lap[b][a] = (((t[b + 1][a] + t[b + 1][a + 2]) - 2.f * c) + s.crlato[b] * (t[b + 2][a + 1] - c)) +
+                      s.crlatu[b] * (t[b][a + 1] - c);
+      });
+      __syncthreads();
+      // hdiffsa.h:106-113 (limited fluxes) and :118-119 (the update)
+      const int a = threadIdx.x;
+#pragma unroll
+      for (int r = 0; r < kT / kTY; ++r) {
+        const int b = threadIdx.y + kTY * r;
+        if (a < vx && b < vy) {
+          const float lc = s.lap[b + 1][a + 1];
+          const float ic = t[b + 2][a + 2];
+          float fxw = lc - s.lap[b + 1][a];
+          if (Prec<float>::prod_gt0(fxw, ic - t[b + 2][a + 1])) fxw = 0.f;
+          float fxe = s.lap[b + 1][a + 2] - lc;
+          if (Prec<float>::prod_gt0(fxe, t[b + 2][a + 3] - ic)) fxe = 0.f;
+          float fys = s.crlato[b] * (lc - s.lap[b][a + 1]);
+          if (Prec<float>::prod_gt0(fys, ic - t[b + 1][a + 2])) fys = 0.f;
+          float fyn = s.crlato[b + 1] * (s.lap[b + 2][a + 1] - lc);
+          if (Prec<float>::prod_gt0(fyn, t[b + 3][a + 2] - ic)) fyn = 0.f;
+          const int64_t o = kofs + (i0 + a) + (int64_t)(j0 + b) * sj;
+          out[o] = ic + (((fxw - fxe) + fys) - fyn) * ld(mask + o);
+        }
+      }
       __syncthreads();
     }
   }
@@ -239,6 +330,12 @@ oeb_status hdiffsa_entry(const M3* out, const M3* in, const M3* mask, const M1* 
   OEB_TRY(check_no_alias({gout.lo, gout.hi}, {gin.lo, gin.hi, gmask.lo, gmask.hi, lo.lo, lo.hi, lu.lo, lu.hi}));
   OEB_RETURN_IF_VALIDATING();
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gin.sj, gin.sk};
+  if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
+    const int tiles = ((d.nx + kT - 1) / kT) * ((d.ny + kT - 1) / kT);
+    const int kb = tuned_kb(staged_kb(tiles, d.nz, hdiffsa_f32::kCtasPerSm));
+    return launch<hdiffsa_f32>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(hdiffsa_f32::Smem), (cudaStream_t)stream,
+                               gout.origin, gin.origin, gmask.origin, lo.origin, lu.origin, lo.s, d, kb);
+  }
   const int kb = tuned_kb(kKB);
   return launch<hdiffsa_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, kb), sizeof(HdiffsaSmem<T>), (cudaStream_t)stream,
                                    gout.origin, gin.origin, gmask.origin, lo.origin, lu.origin, lo.s, d, kb);

@@ -45,6 +45,14 @@ __device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
+// cp.async of one 4-byte cell (PTX cp.async.ca.shared.global with a source size): the cell at
+// gmem when ok, else zeros (nothing is read; gmem must still point into the field).  For
+// tiles whose phases index the shared copy directly, with no per-row offset.
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool ok) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(ok ? 4 : 0) : "memory");
+}
+
 // Cells a row of a box lies past its first chunk boundary: (m0 + b * s3) & 3 for row b.
 struct RowMis {
   int m0, s3;

@@ -106,3 +106,39 @@ def test_fp32_error_vs_fp64_oracle(pkg, fields, orc, cuda, name, case):
         assert r["total_max"] <= bound, "%s: total error %.3g > %.1g" % (what, r["total_max"], bound)
         # the FP32 arithmetic is no worse than the naive float reference's (small margin)
         assert r["arith_max"] <= 2.0 * r["naive_arith_max"] + 1e-7, what
+
+
+# FP32 stencils whose device-resident calls march k-levels with cp.async-staged tiles; with
+# the fields in host memory (the host entry points in place) the plain tiled kernels run.
+MARCHED = ("laplace", "hdiffsa", "nh_p_grad")
+
+
+@pytest.mark.parametrize("name", MARCHED)
+@pytest.mark.parametrize("size", [(256, 256, 80), (100, 70, 13), (37, 45, 5)], ids=["256x256x80", "100x70x13",
+                                                                                 "37x45x5"])
+@pytest.mark.parametrize("kb", [0, 1, 3])
+def test_marched_forms_match_plain_kernels(pkg, fields, cuda, name, size, kb):
+    """The staged march computes every output with the plain kernel's arithmetic on the same
+    operands: the same bits, for the default k-blocking and forced ones (ragged chunks)."""
+    import torch
+    spec = pkg.KERNELS[name]
+    nx, ny, nz = size
+    lib = pkg.load_library()
+    inputs = fields.make_inputs(name, nx, ny, nz, seed=11, workload="fronts")
+    sc = fields.make_scalars(name, seed=11)
+    sc32 = {s.name: (sc[s.name] if s.always_double else float(np.float32(sc[s.name]))) for s in spec.scalars}
+    outs = fields.make_outputs(name, nx, ny, nz)
+    arrays = {k: v.astype(np.float32) for k, v in {**inputs, **outs}.items()}
+    assert lib.oeb_set_host_direct(1) == 0
+    assert lib.oeb_set_kblock(kb) == 0
+    try:
+        host = {k: pkg.Storage(torch.from_numpy(v.copy()).pin_memory(), H) for k, v in arrays.items()}
+        pkg.call(name, host, sc32, domain=(nx, ny, nz))
+        dev = {k: pkg.Storage(torch.from_numpy(v.copy()).to(cuda), H) for k, v in arrays.items()}
+        pkg.call(name, dev, sc32, domain=(nx, ny, nz))
+        torch.cuda.synchronize()
+    finally:
+        lib.oeb_set_kblock(0)
+    for a in spec.by_role("out3"):
+        np.testing.assert_array_equal(dev[a.name].numpy().view(np.uint32), host[a.name].numpy().view(np.uint32),
+                                      err_msg="%s.%s marched vs plain" % (name, a.name))
