@@ -514,6 +514,7 @@ def run_ours(args):
     batched = None
     if not args.no_batch:
         batched = _batch_leg(pkg, fields, torch, dev, args)
+    _chain_roofs(chain, batched, add_rate, peak)
 
 
     line = {
@@ -786,6 +787,7 @@ def _batch_leg(pkg, fields, torch, dev, args):
     res = {"workload": "48 members, nx, ny uniform in {48..320 step 16}, nz in {40, 60, 80, 137}, FP64 or FP32 "
                        "(seed 4); chained step forward + adjoint with recomputation; device-generated inputs",
            "members": len(members), "fp64_members": sum(1 for s_ in spec if s_[3] == 8),
+           "fp64_points": sum(a * b * c for a, b, c, e in spec if e == 8),
            "points_per_run": pts, "ms_per_run": round(ms_batch, 3), "gpts": round(pts / (ms_batch * 1e-3) / 1e9, 4),
            "batched_launches_per_run": plan.launches, "launches_counted": round(launches, 1),
            "per_member_launches_ms_per_run": round(ms_members, 3),
@@ -872,6 +874,42 @@ def _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clocks_summary, sms, 
                       "instructions per point: profiles/ncu_%s_128x128x80.md (ncu sm__inst_executed_pipe_fp64); "
                       "frac = bound / measured (kernel: alone, back-to-back launches; step: the concurrent "
                       "graph)" % PIPE_MIX_PROFILE}
+
+
+CHAIN_PROFILE = "pipe_chain"
+
+
+def _chain_roofs(chain, batched, add_rate, peak):
+    """Roofline anchors of the chained and batched legs (in place): the FP64 chained step
+    against its FP64-pipe bound (FP64-pipe instructions a point from the committed ncu
+    counts, over the FP64 addition rate measured in this run), both precisions' DRAM traffic
+    (ncu bytes a point) over the measured step time, and the batched run against the
+    FP64-pipe bound of its FP64 members' points."""
+    instr = _ncu_summary(CHAIN_PROFILE, "fp64_instr_per_point_chain_f64")
+    pts = NX * NY * NZ
+    src = "profiles/ncu_%s_128x128x80.md" % CHAIN_PROFILE
+    if chain is not None:
+        for prec in ("f64", "f32"):
+            r = chain.get(prec)
+            b = _ncu_summary(CHAIN_PROFILE, "dram_bytes_per_point_chain_" + prec)
+            if not r or b is None:
+                continue
+            gbs = b * pts / (r["ms_per_step"] * 1e-3) / 1e9
+            r["dram"] = {"bytes_per_point": b, "gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
+                         "source": src + " (ncu dram__bytes of the same step) over this run's step time"}
+        r = chain.get("f64")
+        if r and instr and add_rate:
+            bound = instr * pts / add_rate * 1e3
+            r["fp64_pipe_roof"] = {"instr_per_point": instr, "bound_ms": round(bound, 4),
+                                   "frac": round(bound / r["ms_per_step"], 4),
+                                   "source": src + " (ncu sm__inst_executed_pipe_fp64) over the FP64 addition "
+                                                   "rate measured in this run"}
+    if batched is not None and instr and add_rate and batched.get("fp64_points"):
+        bound = instr * batched["fp64_points"] / add_rate * 1e3
+        batched["fp64_pipe_roof"] = {
+            "instr_per_point": instr, "bound_ms": round(bound, 3), "frac": round(bound / batched["ms_per_run"], 4),
+            "note": "the FP64 members' points at the 128x128x80 chained step's FP64-pipe instructions a point "
+                    "(smaller members recompute relatively wider halos, so their true count is higher)"}
 
 
 def _ncu_traffic(kernel):
@@ -1108,6 +1146,40 @@ def profile_one(args):
                       "shape": list(shape), "calls": args.calls}))
 
 
+def profile_chain(args):
+    """`--profile-chain`: the chained step forward + adjoint at `--shape` (seed 3), `--calls`
+    times, for an ncu capture of its kernels (prints nothing timed)."""
+    import torch
+    import importlib
+    pkg = graft.load_package()
+    fields = importlib.import_module("oeb_gb300.fields")
+    chain = importlib.import_module("oeb_gb300.chain")
+    dtype = np.float64 if args.precision == "f64" else np.float32
+    nx, ny, nz = args.shape
+    dev = torch.device("cuda", 0)
+    H = fields.CHAIN_HALO
+    x = fields.make_chain_inputs(nx, ny, nz, 3, halo=H)
+    sc = fields.make_chain_scalars(3)
+    st = {k: pkg.Storage(torch.from_numpy(v.astype(dtype)).to(dev), H, nx=nx if v.ndim == 3 else None)
+          for k, v in x.items()}
+    shape = x["u"].shape
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    outs = {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=nx) for n in chain.OUTPUTS}
+    rng = np.random.default_rng(3)
+    seeds = {n: pkg.Storage(torch.from_numpy(rng.normal(0.0, 1.0, size=shape).astype(dtype)).to(dev), H, nx=nx)
+             for n in chain.OUTPUTS}
+    grads = {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=nx) for n in ("u", "v")}
+    plan = chain.ChainPlan(st["u"], (nx, ny, nz), chain.FORWARD | chain.ADJOINT)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.calls):
+        plan.forward(st, sc, outs, stream=stream)
+        plan.adjoint(st, sc, seeds, grads, stream=stream)
+    torch.cuda.synchronize()
+    plan.close()
+    print(json.dumps({"profile_chain": True, "precision": args.precision, "shape": [nx, ny, nz],
+                      "calls": args.calls}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1131,6 +1203,8 @@ def main():
     ap.add_argument("--calls", type=int, default=4)
     ap.add_argument("--adjoint-calls", action="store_true",
                     help="with --profile-one: run each stencil's adjoint instead of its forward")
+    ap.add_argument("--profile-chain", action="store_true",
+                    help="run the chained step forward + adjoint --calls times at --shape (for ncu captures)")
     ap.add_argument("--port-vs-reference", action="store_true",
                     help="time the oracle port against the reference build on this host's cores (needs the "
                          "reference source tree) and exit")
@@ -1140,6 +1214,9 @@ def main():
         return
     if args.profile_one:
         profile_one(args)
+        return
+    if args.profile_chain:
+        profile_chain(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         sys.stderr.write("warning: fewer than 3 warm-up steps\n")

@@ -458,14 +458,12 @@ oeb_status plan_create(const M3* like, const oeb_domain* dom, int modes, oeb_cha
   std::vector<void**> want;
   const bool fwd = modes & OEB_CHAIN_FORWARD, tl = modes & OEB_CHAIN_TL, adj = modes & OEB_CHAIN_ADJOINT;
   for (void** w : {&p->u1, &p->v1, &p->tu, &p->tv, &p->u2, &p->v2}) want.push_back(w);
-  if (fwd) for (void** w : {&p->qi, &p->qj, &p->fx2, &p->fy2}) want.push_back(w);
+  if (fwd || adj) for (void** w : {&p->qi, &p->qj, &p->fx2, &p->fy2}) want.push_back(w);
   if (tl || adj) for (void** w : {&p->u3, &p->v3}) want.push_back(w);
   if (tl)
     for (void** w : {&p->du1, &p->dv1, &p->dtu, &p->dtv, &p->du2, &p->dv2, &p->dqi, &p->dqj, &p->dfx2, &p->dfy2,
                      &p->zero})
       want.push_back(w);
-  if (adj)
-    for (void** w : {&p->qb, &p->v3b, &p->u2b, &p->v2b, &p->wu, &p->wv, &p->utb, &p->vtb, &p->ppb}) want.push_back(w);
   for (void** w : want) {
     void* b = nullptr;
     e = cudaMalloc(&b, p->field_bytes);
@@ -477,6 +475,30 @@ oeb_status plan_create(const M3* like, const oeb_domain* dom, int modes, oeb_cha
     }
     p->bufs.push_back(b);
     *w = b;
+  }
+  if (adj) {
+    // The adjoint step's own fields share the buffers of fields that are dead while they are
+    // live (a plan runs one call at a time, and every call writes a field before it reads it):
+    //   qi, qj, fx2, fy2 are written only by the forward step's fvtp2d and read by nothing;
+    //   tu, tv are dead once stage 3 has formed (u2, v2); v3 is never read by the adjoint
+    //   step and u3 only by its fvtp2d adjoint.  In the adjoint step's order:
+    //     qb (fvtp2d adjoint .. hdiffsmag adjoint)        in qi
+    //     v3b (seed combine .. hdiffsmag adjoint)         in qj
+    //     u2b, v2b (hdiffsmag adjoint .. stage-3 combine) in fx2, fy2
+    //     wu, wv (hadvuv5th adjoint .. fastwavesuv adj.)  in tu, tv
+    //     ppb (fastwavesuv adjoint; qb is dead by then)   in qi
+    //     utb, vtb (fastwavesuv adjoint)                  in v3, u3
+    // No call reads and writes one buffer under two names (every stage's outputs and inputs
+    // stay distinct: the entry points check it).  12 fields instead of 21.
+    p->qb = p->qi;
+    p->v3b = p->qj;
+    p->u2b = p->fx2;
+    p->v2b = p->fy2;
+    p->wu = p->tu;
+    p->wv = p->tv;
+    p->ppb = p->qi;
+    p->utb = p->v3;
+    p->vtb = p->u3;
   }
   if (p->zero) {
     e = cudaMemset(p->zero, 0, p->field_bytes);

@@ -70,3 +70,22 @@ def test_tuning_summary_counts_each_choice(bench):
     h = bench._tuning_summary([(4, 0, 0), (4, 2, 2), (1, 1, 0)])
     assert h == {"kb": {"4": 2, "1": 1}, "shape": {"32x32": 1, "64x16": 1, "32x8": 1},
                  "form": {"wave": 2, "per_member": 1}}
+
+
+def test_chain_and_batch_roofs(bench):
+    # the chained and batched legs' anchors read profiles/ncu_pipe_chain_128x128x80.md
+    instr = bench._ncu_summary(bench.CHAIN_PROFILE, "fp64_instr_per_point_chain_f64")
+    assert instr is not None and 100 <= instr <= 5000
+    for p in ("f64", "f32"):
+        b = bench._ncu_summary(bench.CHAIN_PROFILE, "dram_bytes_per_point_chain_" + p)
+        assert b is not None and 100 <= b <= 10000, p
+    chain = {"f64": {"ms_per_step": 2.0}, "f32": {"ms_per_step": 0.5}}
+    batched = {"ms_per_run": 80.0, "fp64_points": 40_000_000}
+    rate, peak = 5.0e11, 7000.0
+    bench._chain_roofs(chain, batched, rate, peak)
+    pts = bench.NX * bench.NY * bench.NZ
+    assert chain["f64"]["fp64_pipe_roof"]["bound_ms"] == pytest.approx(instr * pts / rate * 1e3, rel=1e-3)
+    assert chain["f64"]["fp64_pipe_roof"]["frac"] == pytest.approx(instr * pts / rate * 1e3 / 2.0, rel=1e-3)
+    b32 = bench._ncu_summary(bench.CHAIN_PROFILE, "dram_bytes_per_point_chain_f32")
+    assert chain["f32"]["dram"]["gbs"] == pytest.approx(b32 * pts / 0.5e-3 / 1e9, rel=1e-3)
+    assert batched["fp64_pipe_roof"]["frac"] == pytest.approx(instr * 40e6 / rate * 1e3 / 80.0, rel=1e-3)

@@ -286,3 +286,36 @@ def test_chain_plan_rejects_a_halo_below_8(pkg):
     st = fn(ctypes.byref(like.memref()), ctypes.byref(pkg.Domain(8, 8, 5)), ctypes.c_int(1), ctypes.byref(plan))
     assert st == 4  # OEB_ERR_HALO
     assert not plan.value
+
+
+@pytest.mark.gpu
+def test_chain_workspace_fields_per_mode(pkg, fields, chain, cuda):
+    """The adjoint step's fields share the buffers of forward fields that are dead while they
+    are live: 10 workspace fields for the forward step, 12 for the adjoint (with or without
+    the forward), 19 for the tangent-linear, 23 for all three."""
+    field_bytes = None
+    for modes, n in ((chain.FORWARD, 10), (chain.ADJOINT, 12), (chain.FORWARD | chain.ADJOINT, 12), (chain.TL, 19),
+                     (chain.FORWARD | chain.TL | chain.ADJOINT, 23)):
+        st = Step(pkg, fields, chain, cuda, 24, 20, 4, 3, modes)
+        field_bytes = st.x["u"].size * 8
+        assert st.plan.nbytes == n * field_bytes, (modes, st.plan.nbytes / field_bytes)
+        st.plan.close()
+
+
+@pytest.mark.gpu
+def test_chain_calls_alternate_on_one_plan(pkg, fields, chain, cuda):
+    """Forward, adjoint and tangent-linear calls on one plan, in turn, give the bits each
+    gives on a plan of its own: no call reads what another left in a shared buffer."""
+    nx, ny, nz = 40, 36, 5
+    both = Step(pkg, fields, chain, cuda, nx, ny, nz, 3, chain.FORWARD | chain.TL | chain.ADJOINT)
+    rng = np.random.default_rng(5)
+    seeds = {k: rng.normal(size=both.shape) for k in chain.OUTPUTS}
+    du, dv = rng.normal(size=both.shape), rng.normal(size=both.shape)
+    alone = {m: Step(pkg, fields, chain, cuda, nx, ny, nz, 3, m) for m in (chain.FORWARD, chain.TL, chain.ADJOINT)}
+    want_f = alone[chain.FORWARD].forward()
+    want_a = alone[chain.ADJOINT].adj(seeds)
+    want_t = alone[chain.TL].tl(du, dv)
+    for _ in range(2):
+        for got, want in ((both.adj(seeds), want_a), (both.forward(), want_f), (both.tl(du, dv), want_t)):
+            for k in want:
+                np.testing.assert_array_equal(got[k].view(np.uint64), want[k].view(np.uint64), err_msg=k)
