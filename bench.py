@@ -1146,6 +1146,22 @@ def profile_one(args):
                       "shape": list(shape), "calls": args.calls}))
 
 
+def probe_shuffles():
+    """`--probe-shuffles`: i-neighbours through L1 against warp shuffles (the library's
+    oeb_probe_shuffle_neighbours: FP32, 256x256x80 + 3-cell halo, a 5-point laplacian and a
+    7-cell window along i, each form timed alone over back-to-back launches)."""
+    import ctypes
+    pkg = graft.load_package()
+    lib = pkg.load_library()
+    us = (ctypes.c_double * 4)()
+    bad = (ctypes.c_uint64 * 2)()
+    st = lib.oeb_probe_shuffle_neighbours(us, bad)
+    print(json.dumps({"probe": "shuffle_neighbours", "status": st, "shape": [256, 256, 80], "dtype": "f32",
+                      "us": {"laplace_l1": round(us[0], 2), "laplace_shuffle": round(us[1], 2),
+                             "window7_l1": round(us[2], 2), "window7_shuffle": round(us[3], 2)},
+                      "mismatched_cells": {"laplace": bad[0], "window7": bad[1]}}))
+
+
 def profile_chain(args):
     """`--profile-chain`: the chained step forward + adjoint at `--shape` (seed 3), `--calls`
     times, for an ncu capture of its kernels (prints nothing timed)."""
@@ -1203,6 +1219,8 @@ def main():
     ap.add_argument("--calls", type=int, default=4)
     ap.add_argument("--adjoint-calls", action="store_true",
                     help="with --profile-one: run each stencil's adjoint instead of its forward")
+    ap.add_argument("--probe-shuffles", action="store_true",
+                    help="time i-neighbours through L1 against warp shuffles (FP32 probe stencils) and exit")
     ap.add_argument("--profile-chain", action="store_true",
                     help="run the chained step forward + adjoint --calls times at --shape (for ncu captures)")
     ap.add_argument("--port-vs-reference", action="store_true",
@@ -1217,6 +1235,9 @@ def main():
         return
     if args.profile_chain:
         profile_chain(args)
+        return
+    if args.probe_shuffles:
+        probe_shuffles()
         return
     if args.warmup < 3 and args.impl == "ours":
         sys.stderr.write("warning: fewer than 3 warm-up steps\n")

@@ -159,6 +159,16 @@ OEB_API oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int m
  * after a warm-up.  `adds_per_launch` (may be NULL) receives the additions of one launch.
  * Synchronous, on the legacy default stream. */
 OEB_API oeb_status oeb_probe_fp64_add_rate(double* adds_per_second, double* adds_per_launch);
+/* No counterpart in the reference (a measurement behind the stencils' design): i-neighbours
+ * read through L1 against warp shuffles, FP32, on a 256 x 256 x 80 interior with a 3-cell
+ * halo.  us[0..3] receive the average launch time (microseconds; the best of three runs of 60
+ * back-to-back launches rotating over 12 input copies, more than the L2) of the 5-point
+ * laplacian with loaded i-neighbours, the same with shuffled ones (lanes 0 and 31 load the
+ * warp's outer cells), a 7-cell window along i loaded, and the same window shuffled.
+ * mismatches[0..1] receive the cells where the two forms of the laplacian and of the window
+ * differ in any bit (0 expected).  Allocates and frees about 330 MB; synchronous, on the
+ * legacy default stream. */
+OEB_API oeb_status oeb_probe_shuffle_neighbours(double* us, uint64_t* mismatches);
 
 /* ------------------------------------------------------------------------- */
 /* Device storage (the device twin of allocateStorage/freeStorage,           */

@@ -1,8 +1,13 @@
 // selftest.cu -- oeb_selftest_fp64: the integer-pipe FP64 multiply, division, addition,
 // subtraction and square root (precision.cuh: fp64::mul, div, add, isub, sqrt) against the
-// FP64 instructions on seeded random operands, on the device.
+// FP64 instructions on seeded random operands, on the device; and two measurements of the
+// GPU the design rests on: the FP64 pipe's addition rate (oeb_probe_fp64_add_rate) and
+// i-neighbours read through L1 against warp shuffles (oeb_probe_shuffle_neighbours).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <vector>
 
 #include "oeb_common.cuh"
 #include "precision.cuh"
@@ -109,8 +114,143 @@ __global__ void fp64_add_rate_kernel(int iters, double step, double* sink) {
   if (t == -1.0) sink[blockIdx.x] = t;  // never true for these operands
 }
 
+// ---- i-neighbours through L1 or through warp shuffles (oeb_probe_shuffle_neighbours) --
+// FP32 fields of a 256 x 256 x 80 interior with a 3-cell halo, one CTA of 32 x 8 threads a
+// 32 x 32 tile and k-level, four rows a thread.
+constexpr int kPNX = 256, kPNY = 256, kPNZ = 80, kPH = 3;
+constexpr int kPSX = kPNX + 2 * kPH, kPSY = kPNY + 2 * kPH;
+constexpr long kPSK = (long)kPSX * kPSY;
+constexpr size_t kPCells = (size_t)kPSK * (kPNZ + 2 * kPH);
+
+__device__ __forceinline__ long probe_offset(int i, int j, int k) {
+  return (long)(k + kPH) * kPSK + (long)(j + kPH) * kPSX + i + kPH;
+}
+
+// the 5-point laplacian, its i-neighbours loaded (through L1)
+__global__ void probe_lap_l1(const float* __restrict__ in, float* __restrict__ out) {
+  const int i = blockIdx.x * 32 + threadIdx.x, k = blockIdx.z;
+  for (int r = 0; r < 4; ++r) {
+    const long o = probe_offset(i, blockIdx.y * 32 + threadIdx.y + 8 * r, k);
+    const float c = __ldg(in + o);
+    out[o] = ((__ldg(in + o - 1) - c) + (__ldg(in + o + 1) - c)) + ((__ldg(in + o + kPSX) - c) + (__ldg(in + o - kPSX) - c));
+  }
+}
+
+// the same, its i-neighbours shuffled from the adjacent lanes; lanes 0 and 31 load the
+// warp's two outer cells
+__global__ void probe_lap_shfl(const float* __restrict__ in, float* __restrict__ out) {
+  const int lane = threadIdx.x, i = blockIdx.x * 32 + lane, k = blockIdx.z;
+  for (int r = 0; r < 4; ++r) {
+    const long o = probe_offset(i, blockIdx.y * 32 + threadIdx.y + 8 * r, k);
+    const float c = __ldg(in + o);
+    const float e = (lane == 0 || lane == 31) ? __ldg(in + o + (lane == 0 ? -1 : 1)) : 0.f;
+    float w = __shfl_up_sync(0xffffffffu, c, 1), x = __shfl_down_sync(0xffffffffu, c, 1);
+    const float e0 = __shfl_sync(0xffffffffu, e, 0), e31 = __shfl_sync(0xffffffffu, e, 31);
+    if (lane == 0) w = e0;
+    if (lane == 31) x = e31;
+    out[o] = ((w - c) + (x - c)) + ((__ldg(in + o + kPSX) - c) + (__ldg(in + o - kPSX) - c));
+  }
+}
+
+// a 7-cell window along i (the shape of the fifth-order advection sums), loaded
+__device__ __constant__ float kProbeCoef[7] = {1.f / 30, -0.25f, 1.f, -1.f / 3, -0.5f, 1.f / 20, 0.1f};
+__global__ void probe_win_l1(const float* __restrict__ in, float* __restrict__ out) {
+  const int i = blockIdx.x * 32 + threadIdx.x, k = blockIdx.z;
+  for (int r = 0; r < 4; ++r) {
+    const long o = probe_offset(i, blockIdx.y * 32 + threadIdx.y + 8 * r, k);
+    float s = 0.f;
+#pragma unroll
+    for (int d = -3; d <= 3; ++d) s = s + kProbeCoef[d + 3] * __ldg(in + o + d);
+    out[o] = s;
+  }
+}
+
+// the same window shuffled: lane l holds cells i0-3+l and (l < 6) i0+29+l of its row
+__global__ void probe_win_shfl(const float* __restrict__ in, float* __restrict__ out) {
+  const int lane = threadIdx.x, k = blockIdx.z;
+  for (int r = 0; r < 4; ++r) {
+    const long row = probe_offset(blockIdx.x * 32, blockIdx.y * 32 + threadIdx.y + 8 * r, k);
+    const float a = __ldg(in + row - 3 + lane);
+    const float b = lane < 6 ? __ldg(in + row + 29 + lane) : 0.f;
+    float s = 0.f;
+#pragma unroll
+    for (int d = -3; d <= 3; ++d) {
+      const int src = lane + d + 3;
+      const float va = __shfl_sync(0xffffffffu, a, src & 31);
+      const float vb = __shfl_sync(0xffffffffu, b, (src - 32) & 31);
+      s = s + kProbeCoef[d + 3] * (src < 32 ? va : vb);
+    }
+    out[row + lane] = s;
+  }
+}
+
 }  // namespace
 }  // namespace oeb
+
+extern "C" oeb_status oeb_probe_shuffle_neighbours(double* us, uint64_t* mismatches) {
+  if (!us || !mismatches) return OEB_ERR_NULL;
+  using namespace oeb;
+  constexpr int kCopies = 12;  // 12 input copies of 23.6 MB: more than the L2, launches rotate over them
+  float *in = nullptr, *o1 = nullptr, *o2 = nullptr;
+  cudaError_t e = cudaMalloc(&in, kPCells * sizeof(float) * kCopies);
+  if (e == cudaSuccess) e = cudaMalloc(&o1, kPCells * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&o2, kPCells * sizeof(float));
+  std::vector<float> h(kPCells), r1, r2;
+  uint64_t x = 0x243F6A8885A308D3ull;
+  for (float& v : h) {  // xorshift values in [0, 1)
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    v = (float)(x >> 40) / (float)(1u << 24);
+  }
+  for (int c = 0; c < kCopies && e == cudaSuccess; ++c)
+    e = cudaMemcpy(in + c * kPCells, h.data(), kPCells * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(o1, 0, kPCells * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(o2, 0, kPCells * sizeof(float));
+  const dim3 grid(kPNX / 32, kPNY / 32, kPNZ), block(32, 8);
+  using Kern = void (*)(const float*, float*);
+  const Kern pairs[2][2] = {{probe_lap_l1, probe_lap_shfl}, {probe_win_l1, probe_win_shfl}};
+  // the two forms of each stencil give the same bits
+  for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
+    pairs[p][0]<<<grid, block>>>(in, o1);
+    pairs[p][1]<<<grid, block>>>(in, o2);
+    count_launches(2);
+    e = cudaDeviceSynchronize();
+    r1.resize(kPCells);
+    r2.resize(kPCells);
+    if (e == cudaSuccess) e = cudaMemcpy(r1.data(), o1, kPCells * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(r2.data(), o2, kPCells * sizeof(float), cudaMemcpyDeviceToHost);
+    uint64_t bad = 0;
+    for (size_t q = 0; q < kPCells; ++q) bad += memcmp(&r1[q], &r2[q], sizeof(float)) != 0;
+    mismatches[p] = bad;
+  }
+  // each form: the best of three averages over 60 back-to-back launches, after 5 warm-up launches
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int f = 0; f < 4 && e == cudaSuccess; ++f) {
+    const Kern kern = pairs[f / 2][f % 2];
+    float best = 0.f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+      for (int w = 0; w < 5; ++w) kern<<<grid, block>>>(in + (w % kCopies) * kPCells, o1);
+      cudaEventRecord(e0, 0);
+      for (int r = 0; r < 60; ++r) kern<<<grid, block>>>(in + (r % kCopies) * kPCells, o1);
+      cudaEventRecord(e1, 0);
+      count_launches(65);
+      e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+      if (best == 0.f || ms < best) best = ms;
+    }
+    us[f] = best / 60.0 * 1e3;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(in);
+  cudaFree(o1);
+  cudaFree(o2);
+  return e == cudaSuccess ? OEB_OK : cuda_fail(e);
+}
 
 extern "C" oeb_status oeb_probe_fp64_add_rate(double* adds_per_second, double* adds_per_launch) {
   if (!adds_per_second) return OEB_ERR_NULL;

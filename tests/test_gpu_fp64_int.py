@@ -57,3 +57,14 @@ def test_fp64_add_rate_probe(pkg, cuda):
     per_clk_at_max = rate.value / (sms * 2.07e9)
     assert adds.value > 1e9 and 0.5 <= per_clk_at_max <= 64.0, (rate.value, per_clk_at_max)
     assert lib.oeb_probe_fp64_add_rate(None, None) != 0
+
+
+def test_probe_shuffle_neighbours(pkg, cuda):
+    # both forms of each probe stencil give the same bits; the four launch times are measured
+    lib = pkg.load_library()
+    us = (ctypes.c_double * 4)()
+    bad = (ctypes.c_uint64 * 2)()
+    assert lib.oeb_probe_shuffle_neighbours(us, bad) == 0
+    assert list(bad) == [0, 0]
+    assert all(0.5 < t < 10000.0 for t in us), list(us)
+    assert lib.oeb_probe_shuffle_neighbours(None, None) != 0
