@@ -750,6 +750,191 @@ struct hdiffsmag_adj_gather_kernel {
   }
 };
 
+// FP32 adjoint in one launch.  The three passes above write six term fields to scratch and
+// read them back (about 48 bytes a point of FP32 traffic beyond the adjoint's own fields, and
+// three launches).  In FP32 the terms are cheap to recompute, so here a CTA forms, for a
+// 32 x 32 tile of (ubar, vbar), everything its outputs gather in shared memory:
+//   u, v   : 36 x 36 from (i0-2, j0-2)     (the fields, 0 outside their reach [-1, N+1)^2)
+//   t      : 35 x 35 from (i0-1, j0-1)     T on [0, N]^2, else 0
+//   s      : 35 x 35 from (i0-2, j0-2)     S on [-1, N)^2, else 0
+//   lu, lv, xu, xv : 34 x 34 from (i0-1, j0-1), at interior points, else 0
+//   tb     : 33 x 33 from (i0, j0)         TB on [0, N]^2, else 0   } over u, v
+//   sb     : 33 x 33 from (i0-1, j0-1)     SB on [-1, N)^2, else 0  } (dead by then)
+// with the output tile at (i0, j0) = (-1 + 32 bx, -1 + 32 by).  Every value is the same
+// expression on the same operands as in the three passes (T and S from the same
+// differences, the terms, TB and SB with the same guarded sums, the gather in the same
+// order), so the results are theirs, bit for bit; the recomputed apron costs about 20 % more
+// arithmetic than the passes.
+struct SmagAdjF32Smem {
+  union {
+    struct {
+      float u[36][36], v[36][36];
+    } f;
+    struct {
+      float tb[33][33], sb[33][33];
+    } g;
+  } x;
+  float t[35][35], s[35][35];
+  float lu[34][34], lv[34][34], xu[34][34], xv[34][34];
+  float acr[36], cto[36], ctu[36], cvo[36], cvu[36];  // rows j0-2+r
+};
+
+struct hdiffsmag_adj_f32 {
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uinb, float* __restrict__ vinb,
+                                             const float* __restrict__ uin, const float* __restrict__ vin,
+                                             const float* __restrict__ mask, const float* __restrict__ crlavo,
+                                             const float* __restrict__ crlavu, const float* __restrict__ crlato,
+                                             const float* __restrict__ crlatu, const float* __restrict__ acrlat0,
+                                             int64_t s1d, const float* __restrict__ uoutb,
+                                             const float* __restrict__ voutb, float eddlat, float eddlon,
+                                             float tau_smag, float weight_smag, Dims d, int kb) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmagAdjF32Smem& s = *reinterpret_cast<SmagAdjF32Smem*>(smem_raw);
+    constexpr float rr = earth_radius_recip<float>();
+    const float c1 = eddlat * rr;
+    const int nx = d.nx, ny = d.ny;
+    const int64_t sj = d.sj;
+    const int i0 = -1 + (int)blk.x * kT, j0 = -1 + (int)blk.y * kT;
+    auto in = [&](int i, int j) { return i >= 0 && i < nx && j >= 0 && j < ny; };
+    auto inT = [&](int i, int j) { return i >= 0 && i <= nx && j >= 0 && j <= ny; };
+    auto inS = [&](int i, int j) { return i >= -1 && i < nx && j >= -1 && j < ny; };
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    if (tid < 36) {
+      const int j = j0 - 2 + tid;
+      const int64_t jo = (int64_t)j * s1d;
+      const bool in1 = j >= -1 && j < ny + 1, in0 = j >= 0 && j < ny;
+      s.acr[tid] = in1 ? ld(acrlat0 + jo) : 0.f;
+      s.cto[tid] = in0 ? ld(crlato + jo) : 0.f;
+      s.ctu[tid] = in0 ? ld(crlatu + jo) : 0.f;
+      s.cvo[tid] = in0 ? ld(crlavo + jo) : 0.f;
+      s.cvu[tid] = in0 ? ld(crlavu + jo) : 0.f;
+    }
+    const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  #pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      for_region<36, 36>([&](int a, int b) {
+        const int i = i0 - 2 + a, j = j0 - 2 + b;
+        const bool ok = i >= -1 && i < nx + 1 && j >= -1 && j < ny + 1;
+        const int64_t o = kofs + i + j * sj;
+        s.x.f.u[b][a] = ok ? ld(uin + o) : 0.f;
+        s.x.f.v[b][a] = ok ? ld(vin + o) : 0.f;
+      });
+      __syncthreads();
+      // T = c1 (v(j-1) - v) - c2 (u(i-1) - u),  S = c1 (u(j+1) - u) + c2 (v(i+1) - v)  (smag_T, smag_S)
+      for_region<35, 35>([&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        float t = 0.f;
+        if (inT(i, j)) {
+          const float c2 = s.acr[b + 1] * eddlon;
+          t = c1 * (s.x.f.v[b][a + 1] - s.x.f.v[b + 1][a + 1]) - c2 * (s.x.f.u[b + 1][a] - s.x.f.u[b + 1][a + 1]);
+        }
+        s.t[b][a] = t;
+      });
+      for_region<35, 35>([&](int a, int b) {
+        const int i = i0 - 2 + a, j = j0 - 2 + b;
+        float v = 0.f;
+        if (inS(i, j)) {
+          const float c2 = s.acr[b] * eddlon;
+          v = c1 * (s.x.f.u[b + 1][a] - s.x.f.u[b][a]) + c2 * (s.x.f.v[b][a + 1] - s.x.f.v[b][a]);
+        }
+        s.s[b][a] = v;
+      });
+      __syncthreads();
+      // the terms at interior points (hdiffsmag_adj_terms_kernel)
+      for_region<34, 34>([&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        float lu = 0.f, lv = 0.f, xu = 0.f, xv = 0.f;
+        if (in(i, j)) {
+          const int64_t o = kofs + i + j * sj;
+          const float ti = s.t[b][a], tip = s.t[b][a + 1], tjp = s.t[b + 1][a];
+          const float si = s.s[b + 1][a + 1], sjm = s.s[b][a + 1], sim = s.s[b + 1][a];
+          const float xuu = 0.5f * (tip * tip + ti * ti) + 0.5f * (sjm * sjm + si * si);
+          const float xvv = 0.5f * (tjp * tjp + ti * ti) + 0.5f * (sim * sim + si * si);
+          const float hdw = weight_smag * ld(mask + o);
+          const float ru = Prec<float>::sqrt_(xuu), rv = Prec<float>::sqrt_(xvv);
+          const float smu = tau_smag * ru - hdw, smv = tau_smag * rv - hdw;
+          const float su = clamp_smag(smu), sv = clamp_smag(smv);
+          const float u0 = s.x.f.u[b + 1][a + 1], v0 = s.x.f.v[b + 1][a + 1];
+          const float lapu = (s.x.f.u[b + 1][a + 2] + s.x.f.u[b + 1][a] - 2.f * u0) +
+                             s.cto[b + 1] * (s.x.f.u[b + 2][a + 1] - u0) + s.ctu[b + 1] * (s.x.f.u[b][a + 1] - u0);
+          const float lapv = (s.x.f.v[b + 1][a + 2] + s.x.f.v[b + 1][a] - 2.f * v0) +
+                             s.cvo[b + 1] * (s.x.f.v[b + 2][a + 1] - v0) + s.cvu[b + 1] * (s.x.f.v[b][a + 1] - v0);
+          const float yu = ld(uoutb + o), yv = ld(voutb + o);
+          lu = su * yu;
+          lv = sv * yv;
+          xu = (smu > 0.f && smu < 0.5f) ? (lapu * yu) * (tau_smag / (2.f * ru)) : 0.f;
+          xv = (smv > 0.f && smv < 0.5f) ? (lapv * yv) * (tau_smag / (2.f * rv)) : 0.f;
+        }
+        s.lu[b][a] = lu;
+        s.lv[b][a] = lv;
+        s.xu[b][a] = xu;
+        s.xv[b][a] = xv;
+      });
+      __syncthreads();
+      // the T and S adjoints (hdiffsmag_adj_ts_kernel), over the dead u, v
+      for_region<33, 33>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        float tb = 0.f;
+        if (inT(i, j)) {
+          float w = 0.f;
+          if (in(i - 1, j)) w = w + s.xu[b + 1][a];
+          if (in(i, j)) w = w + s.xu[b + 1][a + 1] + s.xv[b + 1][a + 1];
+          if (in(i, j - 1)) w = w + s.xv[b][a + 1];
+          tb = (w == 0.f) ? 0.f : s.t[b + 1][a + 1] * w;
+        }
+        s.x.g.tb[b][a] = tb;
+      });
+      for_region<33, 33>([&](int a, int b) {
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        float sb = 0.f;
+        if (inS(i, j)) {
+          float w = 0.f;
+          if (in(i, j + 1)) w = w + s.xu[b + 1][a];
+          if (in(i, j)) w = w + s.xu[b][a] + s.xv[b][a];
+          if (in(i + 1, j)) w = w + s.xv[b][a + 1];
+          sb = (w == 0.f) ? 0.f : s.s[b + 1][a + 1] * w;
+        }
+        s.x.g.sb[b][a] = sb;
+      });
+      __syncthreads();
+      // the gather (hdiffsmag_adj_gather_kernel) on [-1, N+1)^2
+      for_region<32, 32>([&](int a, int b) {
+        const int i = i0 + a, j = j0 + b;
+        if (i >= nx + 1 || j >= ny + 1) return;
+        const int64_t o = kofs + i + j * sj;
+        const float c2 = s.acr[b + 2] * eddlon;
+        float ub = 0.f, vb = 0.f;
+        if (in(i, j)) {
+          ub = ld(uoutb + o) - (2.f + s.cto[b + 2] + s.ctu[b + 2]) * s.lu[b + 1][a + 1];
+          vb = ld(voutb + o) - (2.f + s.cvo[b + 2] + s.cvu[b + 2]) * s.lv[b + 1][a + 1];
+        }
+        if (in(i - 1, j)) ub = ub + s.lu[b + 1][a], vb = vb + s.lv[b + 1][a];
+        if (in(i + 1, j)) ub = ub + s.lu[b + 1][a + 2], vb = vb + s.lv[b + 1][a + 2];
+        if (in(i, j - 1)) {
+          ub = fmaf(s.cto[b + 1], s.lu[b][a + 1], ub);
+          vb = fmaf(s.cvo[b + 1], s.lv[b][a + 1], vb);
+        }
+        if (in(i, j + 1)) {
+          ub = fmaf(s.ctu[b + 3], s.lu[b + 2][a + 1], ub);
+          vb = fmaf(s.cvu[b + 3], s.lv[b + 2][a + 1], vb);
+        }
+        const float tb0 = inT(i, j) ? s.x.g.tb[b][a] : 0.f;
+        const float sb0 = inS(i, j) ? s.x.g.sb[b + 1][a + 1] : 0.f;
+        if (inT(i + 1, j)) ub = fmaf(-c2, s.x.g.tb[b][a + 1], ub);
+        ub = fmaf(-c1, sb0, fmaf(c2, tb0, ub));
+        if (inS(i, j - 1)) ub = fmaf(c1, s.x.g.sb[b][a + 1], ub);
+        if (inT(i, j + 1)) vb = fmaf(c1, s.x.g.tb[b + 1][a], vb);
+        vb = fmaf(-c2, sb0, fmaf(-c1, tb0, vb));
+        if (inS(i - 1, j)) vb = fmaf(c2, s.x.g.sb[b + 1][a], vb);
+        uinb[o] = ub;
+        vinb[o] = vb;
+      });
+      __syncthreads();
+    }
+  }
+};
+
 template <class T, class M3, class M1>
 oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M3* mask,
                                const M1* crlavo, const M1* crlavu, const M1* crlato, const M1* crlatu,
@@ -769,6 +954,17 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
   OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi}, {gui.lo, gui.hi, guo.lo, guo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
+  if constexpr (std::is_same<T, float>::value) {
+    const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
+    const int kb = tuned_kb(kKB);
+    auto org1 = [](const M1* m) { return (const float*)m->aligned + m->offset; };
+    return launch<hdiffsmag_adj_f32>(tile_grid(d.nx + 2, d.ny + 2, d.nz, kT, kT, kb), sizeof(SmagAdjF32Smem), st,
+                                     gub.origin, gvb.origin, gui.origin, (const float*)vin->aligned + vin->offset,
+                                     (const float*)mask->aligned + mask->offset, org1(crlavo), org1(crlavu),
+                                     org1(crlato), org1(crlatu), org1(acrlat0), acrlat0->strides[0], guo.origin,
+                                     (const float*)voutb->aligned + voutb->offset, eddlat, eddlon, tau_smag,
+                                     weight_smag, d, kb);
+  }
   const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
   const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +
                        (uin->sizes[2] - 1) * uin->strides[2];

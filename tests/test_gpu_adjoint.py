@@ -140,6 +140,14 @@ def test_dot_product_f32(pkg, fields, cuda, name):
     _dot_test(Case(pkg, fields, cuda, name, 128, 128, 80, seed=3, dtype=np.float32), 1e-5)
 
 
+@pytest.mark.parametrize("name", ADJ)
+@pytest.mark.parametrize("size", [(70, 97, 9), (1, 1, 1)], ids=["70x97x9", "1x1x1"])
+def test_dot_product_f32_edges(pkg, fields, cuda, name, size):
+    # ragged tiles on every edge and a single cell, in FP32 (whose adjoints may take other
+    # launch forms than FP64's)
+    _dot_test(Case(pkg, fields, cuda, name, *size, seed=5, dtype=np.float32, workload="fronts"), 1e-5)
+
+
 def _flip_cells(case: Case, xp: dict, xm: dict):
     """hdiffsa: the output cells whose limiter flags differ between the two ends of the step
     (tests/branch_flips.py); None for the other stencils, whose flips are counted."""
