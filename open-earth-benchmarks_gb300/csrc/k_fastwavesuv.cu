@@ -8,6 +8,8 @@
 // memory; the output pass then reads its i+1 and j+1 neighbours from there.
 //
 // Compiled with --fmad=false (see k_pointwise.cu).
+#include <type_traits>
+
 #include "precision.cuh"
 #include "stencil_util.cuh"
 #include "tangent.cuh"
@@ -124,6 +126,9 @@ template <class T>
 constexpr int adj_kb() {
   return sizeof(T) == 4 ? 2 : 3;
 }
+// the same for the FP32 march that forms its coefficients itself (each level's are formed
+// (kb + 2) / kb times)
+constexpr int kAdjFusedKB = 4;
 
 template <class T, class M3, class M1>
 oeb_status fastwavesuv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* utens,
@@ -219,38 +224,43 @@ struct FastwavesAdjTerms {
   T *au, *ax, *av, *ay;  // in the layout of the state fields, 0 outside the interior unread
 };
 
+// What the terms are formed from, for a march that forms them itself (FP32: see
+// fastwavesuv_adj_kernel).
+template <class T>
+struct FastwavesAdjState {
+  const T *hhl, *rho, *fx;
+  int64_t s1d;
+  T ed2;
+};
+
+// The coefficients au = -dt qx uoutb and au gx at interior point o (fastwavesuv_adj_terms_kernel's
+// expressions), and av, av gy with dir = sj.
+template <class T, bool U>
+__device__ __forceinline__ T fastwaves_adj_coef(const FastwavesAdjState<T>& st, const T* __restrict__ yb, int64_t o,
+                                                int j, int64_t sj, int64_t sk, T dt, T* ag) {
+  const int64_t s = U ? 1 : sj;
+  const T q = U ? (T(2.0) * ld(st.fx + (int64_t)j * st.s1d)) / (ld(st.rho + o + 1) + ld(st.rho + o))
+                : st.ed2 / (ld(st.rho + o + sj) + ld(st.rho + o));
+  const T a = -(dt * q) * ld(yb + o);
+  T g = T(0);
+  if (a != T(0)) {
+    const T hs0 = ld(st.hhl + o + sk) + ld(st.hhl + o), hs1 = ld(st.hhl + o + s + sk) + ld(st.hhl + o + s);
+    const T hd0 = ld(st.hhl + o + sk) - ld(st.hhl + o), hd1 = ld(st.hhl + o + s + sk) - ld(st.hhl + o + s);
+    g = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
+  }
+  *ag = g;
+  return a;
+}
+
 template <class T>
 struct fastwavesuv_adj_terms_kernel {
-  static __device__ __forceinline__ void run(const uint3& blk, FastwavesAdjTerms<T> tm, const T* __restrict__ hhl,
-                                             const T* __restrict__ rho, const T* __restrict__ fx, int64_t s1d,
-                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T ed2, T dt,
-                                             Dims d, int kb) {
+  static __device__ __forceinline__ void run(const uint3& blk, FastwavesAdjTerms<T> tm, FastwavesAdjState<T> st,
+                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T dt, Dims d,
+                                             int kb) {
     const int64_t sk = d.sk, sj = d.sj;
     for_box<RowUnroll<T>::value>(blk, d, 0, 0, d.nx, d.ny, kb, [&](int64_t o, int, int j) {
-      {
-        const T qx = (T(2.0) * ld(fx + (int64_t)j * s1d)) / (ld(rho + o + 1) + ld(rho + o));
-        const T a = -(dt * qx) * ld(uoutb + o);
-        T ag = T(0);
-        if (a != T(0)) {
-          const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + 1 + sk) + ld(hhl + o + 1);
-          const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + 1 + sk) - ld(hhl + o + 1);
-          ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
-        }
-        tm.au[o] = a;
-        tm.ax[o] = ag;
-      }
-      {
-        const T qy = ed2 / (ld(rho + o + sj) + ld(rho + o));
-        const T a = -(dt * qy) * ld(voutb + o);
-        T ag = T(0);
-        if (a != T(0)) {
-          const T hs0 = ld(hhl + o + sk) + ld(hhl + o), hs1 = ld(hhl + o + sj + sk) + ld(hhl + o + sj);
-          const T hd0 = ld(hhl + o + sk) - ld(hhl + o), hd1 = ld(hhl + o + sj + sk) - ld(hhl + o + sj);
-          ag = a * ((T(0.5) * (hs0 - hs1)) / (hd0 + hd1));
-        }
-        tm.av[o] = a;
-        tm.ay[o] = ag;
-      }
+      tm.au[o] = fastwaves_adj_coef<T, true>(st, uoutb, o, j, sj, sk, dt, &tm.ax[o]);
+      tm.av[o] = fastwaves_adj_coef<T, false>(st, voutb, o, j, sj, sk, dt, &tm.ay[o]);
     });
   }
 };
@@ -263,13 +273,16 @@ struct FastwavesAdjSmem {
   T av[kR][kT];
 };
 
-template <class T>
+// FUSED (1): the march forms au, au gx, av, av gy itself at each level it reads (the FP32 form:
+// its divisions are cheap, and the 16 bytes a point the terms pass writes and the march reads
+// back cost more), from `st`, with the terms pass's expressions; else it reads them from tm.
+template <class T, int FUSED = 0>
 struct fastwavesuv_adj_kernel {
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
                                              T* __restrict__ utensb, T* __restrict__ vtensb, T* __restrict__ ppuvb,
                                              const T* __restrict__ wgtfac, FastwavesAdjTerms<T> tm,
-                                             const T* __restrict__ uoutb, const T* __restrict__ voutb, T dt, Dims d,
-                                             int kb) {
+                                             FastwavesAdjState<T> st, const T* __restrict__ uoutb,
+                                             const T* __restrict__ voutb, T dt, Dims d, int kb) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FastwavesAdjSmem<T>& s = *reinterpret_cast<FastwavesAdjSmem<T>*>(smem_raw);
     const int i0 = blk.x * kT, j0 = blk.y * kT;
@@ -293,6 +306,7 @@ struct fastwavesuv_adj_kernel {
         return T(0);
       }
       const int64_t o = (int64_t)k * sk + i + j * sj;
+      if constexpr (FUSED) return fastwaves_adj_coef<T, true>(st, uoutb, o, j, sj, sk, dt, ag);
       *ag = ld(tm.ax + o);
       return ld(tm.au + o);
     };
@@ -302,6 +316,7 @@ struct fastwavesuv_adj_kernel {
         return T(0);
       }
       const int64_t o = (int64_t)k * sk + i + j * sj;
+      if constexpr (FUSED) return fastwaves_adj_coef<T, false>(st, voutb, o, j, sj, sk, dt, ag);
       *ag = ld(tm.ay + o);
       return ld(tm.av + o);
     };
@@ -384,6 +399,15 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gw.sj, gw.sk};
   const T ed2 = T(2.0) * edadlat;
   cudaStream_t st = (cudaStream_t)stream;
+  const FastwavesAdjState<T> state{gh.origin, gr.origin, lfx.origin, lfx.s, ed2};
+  if constexpr (std::is_same<T, float>::value) {
+    // one launch: the march forms the coefficients at the kb + 2 levels of its k-block
+    const int kb = tuned_kb(kAdjFusedKB);
+    return launch<fastwavesuv_adj_kernel<T, 1>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
+                                                   sizeof(FastwavesAdjSmem<T>), st, gub.origin, gvb.origin,
+                                                   gutb.origin, gvtb.origin, gpb.origin, gw.origin,
+                                                   FastwavesAdjTerms<T>{}, state, guo.origin, gvo.origin, dt, d, kb);
+  }
   // scratch for the four coefficient fields, in uoutb's layout
   const T* start = (uoutb->allocated && uoutb->allocated <= uoutb->aligned) ? uoutb->allocated : uoutb->aligned;
   const int64_t last = (uoutb->sizes[0] - 1) * uoutb->strides[0] + (uoutb->sizes[1] - 1) * uoutb->strides[1] +
@@ -394,16 +418,16 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   OEB_TRY(scratch_alloc(&buf, (size_t)n * 4 * sizeof(T), st));
   T* base = static_cast<T*>(buf);
   const FastwavesAdjTerms<T> tm{base + org, base + n + org, base + 2 * n + org, base + 3 * n + org};
-  oeb_status stt = launch<fastwavesuv_adj_terms_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, 1), 0, st, tm,
-                                                           gh.origin, gr.origin, lfx.origin, lfx.s, guo.origin,
-                                                           gvo.origin, ed2, dt, d, 1);
+  oeb_status stt = launch<fastwavesuv_adj_terms_kernel<T>>(tile_grid(d.nx, d.ny, d.nz, kT, kT, 1), 0, st, tm, state,
+                                                           guo.origin, gvo.origin, dt, d, 1);
   // the march carries a three-level window of ppgc terms up the column; a k-block of kb
   // levels reads the coefficients at kb + 2
   const int kb = tuned_kb(adj_kb<T>());
   if (stt == OEB_OK)
     stt = launch<fastwavesuv_adj_kernel<T>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),
                                             sizeof(FastwavesAdjSmem<T>), st, gub.origin, gvb.origin, gutb.origin,
-                                            gvtb.origin, gpb.origin, gw.origin, tm, guo.origin, gvo.origin, dt, d, kb);
+                                            gvtb.origin, gpb.origin, gw.origin, tm, state, guo.origin, gvo.origin, dt,
+                                            d, kb);
   scratch_free(buf, st);
   return stt;
 }
