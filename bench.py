@@ -783,7 +783,42 @@ def _batch_leg(pkg, fields, torch, dev, args):
     with g2:
         per_member()
     ms_members = timed(g2)
+    # the one-launch form: the whole step of every member in one launch of the step kernel,
+    # with each k-blocking its tasks can be recorded with
+    one = {}
+    for kb in (0, 1, 2, 4):
+        for per_sm in (2, 3, 4):
+            plan.set_form(plan.ONE_LAUNCH, kb, per_sm)
+            plan.run(stream)
+            stream.synchronize()
+            g3 = chain.Graph(stream)
+            with g3:
+                plan.run(stream)
+            l0 = lib.oeb_launch_count()
+            ms = timed(g3)
+            launches_one = (lib.oeb_launch_count() - l0) / (args.steps + args.warmup)
+            status = plan.step_status()
+            wait_us, waits = plan.step_waits()  # of the last run
+            g3.close()
+            one[(kb, per_sm)] = (ms, launches_one, status, wait_us, waits)
+    best = min(one, key=lambda k: one[k][0])
+    plan.set_form(plan.PER_LAUNCH)
     pts = plan.points
+    ms_one = one[best][0]
+    ctas = best[1] * torch.cuda.get_device_properties(dev).multi_processor_count
+    one_launch = {
+        "form": "one persistent launch of the step kernel a run: every member's tasks (its recorded launches, "
+                "forward then adjoint) in one ticket order, each waiting on the device for its member's previous task",
+        "ms_per_run": round(ms_one, 3), "gpts": round(pts / (ms_one * 1e-3) / 1e9, 4), "kb": best[0],
+        "ctas_per_sm": best[1],
+        "ms_per_run_by_kb_and_ctas_per_sm": {"%d/%d" % k: round(v[0], 3) for k, v in one.items()},
+        "wait_frac_by_kb_and_ctas_per_sm": {
+            "%d/%d" % k: round(v[3] * 1e-3 / (v[0] * k[1] * ctas / best[1]), 4) for k, v in one.items()},
+        "waits_by_kb_and_ctas_per_sm": {"%d/%d" % k: v[4] for k, v in one.items()},
+        "launches_per_run": 1, "launches_counted": round(one[best][1], 1),
+        "status_ok": all(v[2] == (0, -1) for v in one.values()),
+        "speedup_vs_per_member_launches": round(ms_members / ms_one, 3),
+        "speedup_vs_per_launch_form": round(ms_batch / ms_one, 3)}
     res = {"workload": "48 members, nx, ny uniform in {48..320 step 16}, nz in {40, 60, 80, 137}, FP64 or FP32 "
                        "(seed 4); chained step forward + adjoint with recomputation; device-generated inputs",
            "members": len(members), "fp64_members": sum(1 for s_ in spec if s_[3] == 8),
@@ -795,7 +830,8 @@ def _batch_leg(pkg, fields, torch, dev, args):
            "speedup_vs_per_member_launches": round(ms_members / ms_batch, 3),
            "autotune_s": round(tune_s, 2), "plan_bytes": plan.nbytes,
            "plan_bytes_per_point": round(plan.nbytes / pts, 1),
-           "tuned": _tuning_summary(plan.tuning())}
+           "tuned": _tuning_summary(plan.tuning()),
+           "one_launch": one_launch}
     g.close()
     g2.close()
     for cp in plans:

@@ -829,6 +829,44 @@ OEB_API int64_t oeb_batch_points(const oeb_batch_plan* plan);
 OEB_API size_t oeb_batch_plan_bytes(const oeb_batch_plan* plan);
 OEB_API oeb_status oeb_batch_plan_destroy(oeb_batch_plan* plan);
 
+/* The one-launch form (no counterpart in the reference).  With OEB_BATCH_FORM_ONE_LAUNCH a
+ * run is ONE launch of a persistent step kernel (plus a memset of its counters) that runs
+ * the whole step of every member, FP64 and FP32 alike: each member's recorded launches,
+ * forward then adjoint, become its tasks, and a task waits on the device until every tile of
+ * its member's previous task is done.  Members do not wait for each other.  The waits are
+ * bounded: one that lasts longer than the plan's wait limit (2 s by default) sets the run's
+ * status to OEB_ERR_TIMEOUT, after which every CTA stops at its next tile and the run's
+ * outputs are incomplete.  Results are bit-identical to the per-launch form.
+ * oeb_batch_set_form: form OEB_BATCH_FORM_PER_LAUNCH (the default) or _ONE_LAUNCH; kb is the
+ *   k-blocking the one-launch tasks are recorded with (0 = each kernel's default, 1, 2, 4,
+ *   8) and ctas_per_sm the build of the step kernel (2, 3 or 4 CTAs an SM: registers capped
+ *   at 128, 80 or 64 a thread; 0 = 2); both ignored for the per-launch form.
+ *   OEB_ERR_ARGUMENT for other values.  Building the one-launch tables records the step
+ *   again and waits for the device to go idle; do not call it during a stream capture.
+ * oeb_batch_get_form: the form, and kb and ctas_per_sm for the one-launch form (-1 for the
+ *   other).
+ * oeb_batch_autotune_form: times whole runs -- the per-launch form as the plan stands, then
+ *   the one-launch form with each kb and each build -- keeps the fastest, and writes its
+ *   time per run (ms) to *ms when ms is not NULL.
+ * oeb_batch_step_waits: waits for the device to go idle, then reads the last one-launch
+ *   run's waits that had to poll: their total time over all CTAs (us) and their number.
+ * oeb_batch_step_status: waits for the device to go idle, then reads the status of the last
+ *   one-launch run: 0, or OEB_ERR_TIMEOUT with *task (if not NULL) the task whose wait gave up.
+ * oeb_batch_set_wait_limit: the longest one wait may last, in ns (> 0).
+ * oeb_batch_withhold: a test of the bounded waits.  on != 0 makes the first task of the
+ *   one-launch form wait for a count that nothing writes, so the next run ends with
+ *   OEB_ERR_TIMEOUT after the wait limit; on == 0 restores it.  OEB_ERR_ARGUMENT before the
+ *   one-launch tables exist. */
+#define OEB_BATCH_FORM_PER_LAUNCH 0
+#define OEB_BATCH_FORM_ONE_LAUNCH 1
+OEB_API oeb_status oeb_batch_set_form(oeb_batch_plan* plan, int form, int kb, int ctas_per_sm);
+OEB_API oeb_status oeb_batch_get_form(const oeb_batch_plan* plan, int* form, int* kb, int* ctas_per_sm);
+OEB_API oeb_status oeb_batch_step_waits(oeb_batch_plan* plan, uint64_t* wait_us, uint64_t* waits);
+OEB_API oeb_status oeb_batch_autotune_form(oeb_batch_plan* plan, void* stream, float* ms);
+OEB_API oeb_status oeb_batch_step_status(oeb_batch_plan* plan, int* status, int* task);
+OEB_API oeb_status oeb_batch_set_wait_limit(oeb_batch_plan* plan, uint64_t ns);
+OEB_API oeb_status oeb_batch_withhold(oeb_batch_plan* plan, int on);
+
 /* ------------------------------------------------------------------------- */
 /* CUDA graphs of library calls.  oeb_graph_begin starts capturing `stream`   */
 /* (thread-local capture mode; not the legacy NULL stream); every library call */

@@ -33,8 +33,16 @@ UNITS = {
     "k_fvtp2d.cu": ["--fmad=false"],
     "chain.cu": ["--fmad=false"],
     "batch.cu": [],
+    "step.cu": ["--fmad=false"],
     "selftest.cu": [],
 }
+
+# Units compiled more than once, each time into an object of its own with extra flags: the
+# step kernel for 2, 3 and 4 CTAs an SM.
+VARIANTS = {"step.cu": [("step_c%d" % n, ["-DOEB_STEP_MIN_CTAS=%d" % n]) for n in (2, 3, 4)]}
+
+# The stencil files step.cu compiles its bodies from.
+STEP_INCLUDES = ("k_fastwavesuv.cu", "k_fvtp2d.cu", "k_hdiff.cu", "k_pointwise.cu", "chain.cu")
 
 
 def nvcc() -> str:
@@ -62,18 +70,22 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     headers = list(CSRC.glob("*.cuh")) + [REPO / "include" / "oeb_gb300.h"]
     units = [u for u in UNITS if (CSRC / u).exists()]
     jobs = []
+    objs = []
     for u in units:
         src = CSRC / u
-        obj = BUILD_DIR / (src.stem + ".o")
-        if force or _stale(obj, [src, *headers]):
-            flags = BASE_FLAGS + UNITS[u] + (["-Xptxas", "-v"] if verbose_ptxas else [])
-            jobs.append((u, [nvcc(), *ARCH, *flags, "-c", str(src), "-o", str(obj)]))
+        # step.cu includes the stencil files themselves (their bodies)
+        extra = [CSRC / f for f in STEP_INCLUDES] if u == "step.cu" else []
+        for stem, vflags in VARIANTS.get(u, [(src.stem, [])]):
+            obj = BUILD_DIR / (stem + ".o")
+            objs.append(obj)
+            if force or _stale(obj, [src, *headers, *extra]):
+                flags = BASE_FLAGS + UNITS[u] + vflags + (["-Xptxas", "-v"] if verbose_ptxas else [])
+                jobs.append((stem, [nvcc(), *ARCH, *flags, "-c", str(src), "-o", str(obj)]))
     logs = {}
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for (u, _), out in zip(jobs, ex.map(lambda j: _run(j[1]), jobs)):
                 logs[u] = out
-    objs = [BUILD_DIR / (Path(u).stem + ".o") for u in units]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp")
         _run([nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])

@@ -278,6 +278,57 @@ class BatchPlan:
                            % (path, rec.get("signature"), self.signature))
         self.apply_tuning(rec["choices"])
 
+    # launch forms (oeb_batch_set_form)
+    PER_LAUNCH, ONE_LAUNCH = 0, 1
+
+    def set_form(self, form: int, kb: int = 0, ctas_per_sm: int = 2) -> None:
+        """Runs the plan as one launch per recorded position and precision (PER_LAUNCH, the
+        default) or as ONE persistent launch of the step kernel (ONE_LAUNCH, its tasks
+        recorded with k-blocking kb: 0 = each kernel's default, 1, 2, 4, 8; the kernel built
+        for ctas_per_sm = 2, 3 or 4 CTAs an SM)."""
+        check(entry("oeb_batch_set_form")(self._plan, ctypes.c_int(form), ctypes.c_int(kb), ctypes.c_int(ctas_per_sm)),
+              "oeb_batch_set_form")
+
+    @property
+    def form(self) -> Tuple[int, int, int]:
+        """(form, kb, ctas_per_sm); kb and ctas_per_sm are -1 for the per-launch form."""
+        f, kb, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(entry("oeb_batch_get_form")(self._plan, ctypes.byref(f), ctypes.byref(kb), ctypes.byref(n)),
+              "oeb_batch_get_form")
+        return int(f.value), int(kb.value), int(n.value)
+
+    def step_waits(self) -> Tuple[int, int]:
+        """(microseconds, count) of the last one-launch run's waits that had to poll, summed
+        over its CTAs.  Waits for the device to go idle."""
+        us, n = ctypes.c_uint64(), ctypes.c_uint64()
+        check(entry("oeb_batch_step_waits")(self._plan, ctypes.byref(us), ctypes.byref(n)), "oeb_batch_step_waits")
+        return int(us.value), int(n.value)
+
+    def autotune_form(self, stream=None) -> float:
+        """Times whole runs of the per-launch form as it stands and of the one-launch form
+        with each kb, keeps the fastest, and returns its milliseconds per run."""
+        ms = ctypes.c_float()
+        check(entry("oeb_batch_autotune_form")(self._plan, ctypes.c_void_p(_stream(stream)), ctypes.byref(ms)),
+              "oeb_batch_autotune_form")
+        return float(ms.value)
+
+    def step_status(self) -> Tuple[int, int]:
+        """(status, task) of the last one-launch run: (0, -1), or (OEB_ERR_TIMEOUT, the task
+        whose wait gave up).  Waits for the device to go idle."""
+        st, task = ctypes.c_int(), ctypes.c_int()
+        check(entry("oeb_batch_step_status")(self._plan, ctypes.byref(st), ctypes.byref(task)),
+              "oeb_batch_step_status")
+        return int(st.value), int(task.value)
+
+    def set_wait_limit(self, ns: int) -> None:
+        """The longest one wait of the step kernel may last, in nanoseconds."""
+        check(entry("oeb_batch_set_wait_limit")(self._plan, ctypes.c_uint64(ns)), "oeb_batch_set_wait_limit")
+
+    def withhold(self, on: bool) -> None:
+        """Test hook: the first task of the one-launch form waits for a count that nothing
+        writes (on), so the next run ends with OEB_ERR_TIMEOUT; off restores it."""
+        check(entry("oeb_batch_withhold")(self._plan, ctypes.c_int(1 if on else 0)), "oeb_batch_withhold")
+
     @property
     def launches(self) -> int:
         return int(entry("oeb_batch_launches")(self._plan))

@@ -20,12 +20,17 @@
 // one ordinary launch per member: no item search, arguments in the kernel's parameter space).
 // It keeps the fastest, so a tuned plan is never slower, position by position, than launching
 // the members one by one.
+//
+// The one-launch form (oeb_batch_set_form) runs a whole run as ONE launch of the step kernel
+// (step.cu): every member's recorded launches, forward then adjoint, become tasks in one ticket
+// order, each waiting on the device (bounded) for its member's previous task.
 #include <algorithm>
 #include <new>
 #include <vector>
 
 #include "launch.cuh"
 #include "oeb_common.cuh"
+#include "step.cuh"
 
 namespace {
 
@@ -81,6 +86,17 @@ struct oeb_batch_plan {
   std::vector<Slot> slots;  // forward positions, then adjoint positions
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  // the one-launch form (step.cu): every member's step in one launch of the step kernel
+  int form = OEB_BATCH_FORM_PER_LAUNCH;
+  int one_kb = -1;          // the k-blocking its tasks were recorded with (-1: not built)
+  char* one_buf = nullptr;  // tasks, argument packs, then the done counters and control words
+  size_t one_bytes = 0, one_done_off = 0, one_ctl_off = 0;
+  int one_tasks = 0, one_total = 0, one_ctas = 0;
+  int one_per_sm = 2;  // the step kernel build: CTAs an SM (2, 3 or 4)
+  size_t one_smem = 0;
+  oeb::StepTask one_first{};  // task 0 as built (oeb_batch_withhold changes it on the device)
+  bool withheld = false;
+  unsigned long long wait_ns = 2000000000ull;
 };
 
 namespace oeb {
@@ -293,7 +309,260 @@ oeb_status run_slot(oeb_batch_plan* p, const Slot& sl, int ctas, bool per_member
                p->tables + sl.args_off, sl.smem, ctas, s);
 }
 
+// ---- the one-launch form --------------------------------------------------------------
+// Records every member's step with k-blocking kb (the default tile shape) and builds the
+// step kernel's tables: each member's launches, forward then adjoint, become its tasks, each
+// waiting for the member's previous one.  The tasks of all members are merged in the order of
+// the fraction of its member's step a task ends, larger members first at equal fractions;
+// every member's tasks keep their order, which is all the step kernel needs (step.cuh).  The
+// new tables are uploaded into a buffer of their own and replace the old ones only when all
+// is done, so a failure leaves the plan as it was.
+oeb_status build_one(oeb_batch_plan* p, int kb) {
+  std::vector<std::vector<std::vector<LaunchRecord>>> seq;
+  OEB_TRY(record_all(p, kb, 0, &seq));
+  const int nm = (int)p->members.size();
+  std::vector<int> rank(nm);  // members by points, largest first
+  {
+    std::vector<int> by(nm);
+    for (int i = 0; i < nm; ++i) by[i] = i;
+    auto points = [&](int i) { return p->members[i].dom.nx * p->members[i].dom.ny * p->members[i].dom.nz; };
+    std::stable_sort(by.begin(), by.end(), [&](int a, int b) { return points(a) > points(b); });
+    for (int r = 0; r < nm; ++r) rank[by[r]] = r;
+  }
+  struct Pending {
+    int member, pos;
+    double key;
+    const LaunchRecord* r;
+  };
+  std::vector<Pending> all;
+  size_t smem = 0;
+  for (int i = 0; i < nm; ++i) {
+    std::vector<const LaunchRecord*> list;
+    for (int mi = 0; mi < 2; ++mi)
+      if (p->modes & kModes[mi])
+        for (const LaunchRecord& r : seq[mi][i]) list.push_back(&r);
+    for (size_t q = 0; q < list.size(); ++q) {
+      const LaunchRecord* r = list[q];
+      if (r->step_op < 0 || !step_has_op(r->step_op)) return OEB_ERR_UNSUPPORTED;
+      all.push_back(Pending{i, (int)q, (q + 0.5) / (double)list.size(), r});
+      smem = std::max(smem, r->smem);
+    }
+  }
+  if (all.empty()) return OEB_ERR_UNSUPPORTED;
+  std::stable_sort(all.begin(), all.end(), [&](const Pending& a, const Pending& b) {
+    if (a.key != b.key) return a.key < b.key;
+    return rank[a.member] < rank[b.member];
+  });
+  const int ntasks = (int)all.size();
+  std::vector<StepTask> tasks(ntasks);
+  std::vector<int> last(nm, -1);
+  std::vector<char> packs;
+  int64_t total = 0;
+  for (int t = 0; t < ntasks; ++t) {
+    const Pending& a = all[t];
+    const dim3 g = a.r->grid;
+    const int64_t tiles = (int64_t)g.x * g.y * g.z;
+    if (tiles > INT32_MAX || total + tiles > INT32_MAX) return OEB_ERR_TOO_LARGE;
+    StepTask& k = tasks[t];
+    k.first = (int)total;
+    k.tiles = (int)tiles;
+    k.gx = (int)g.x;
+    k.gy = (int)g.y;
+    k.op = a.r->step_op;
+    k.dep = last[a.member];
+    k.need = k.dep >= 0 ? (unsigned)tasks[k.dep].tiles : 0u;
+    const size_t at = (packs.size() + 15) & ~size_t(15);  // packs 16-byte aligned
+    packs.resize(at + a.r->step_args.size());
+    memcpy(packs.data() + at, a.r->step_args.data(), a.r->step_args.size());
+    k.args = (int64_t)at;  // made absolute below
+    last[a.member] = t;
+    total += tiles;
+  }
+  auto up = [](size_t n) { return (n + 255) & ~size_t(255); };
+  const size_t tasks_bytes = up(sizeof(StepTask) * ntasks);
+  const size_t done_off = tasks_bytes + up(packs.size());
+  const size_t ctl_off = done_off + up(sizeof(unsigned) * (ntasks + 1));
+  const size_t bytes = ctl_off + up(sizeof(unsigned) * kStepCtlWords);
+  for (StepTask& k : tasks) k.args += (int64_t)tasks_bytes;
+  std::vector<char> host(done_off, 0);
+  memcpy(host.data(), tasks.data(), sizeof(StepTask) * ntasks);
+  memcpy(host.data() + tasks_bytes, packs.data(), packs.size());
+  char* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, bytes);
+  if (e != cudaSuccess) {
+    cuda_fail(e);
+    return OEB_ERR_ALLOC;
+  }
+  e = cudaMemcpy(buf, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(buf + done_off, 0, bytes - done_off);
+  if (e == cudaSuccess && p->one_buf) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    cudaFree(buf);
+    return cuda_fail(e);
+  }
+  if (p->one_buf) cudaFree(p->one_buf);
+  p->one_buf = buf;
+  p->one_bytes = bytes;
+  p->one_done_off = done_off;
+  p->one_ctl_off = ctl_off;
+  p->one_tasks = ntasks;
+  p->one_total = (int)total;
+  p->one_smem = smem;
+  p->one_ctas = step_occupancy(p->one_per_sm, smem) * p->sms;
+  p->one_first = tasks[0];
+  p->one_kb = kb;
+  p->withheld = false;
+  return OEB_OK;
+}
+
+oeb_status run_one(oeb_batch_plan* p, cudaStream_t st) {
+  OEB_CUDA_TRY(cudaMemsetAsync(p->one_buf + p->one_done_off, 0, p->one_bytes - p->one_done_off, st));
+  StepParams P;
+  P.tasks = reinterpret_cast<const StepTask*>(p->one_buf);
+  P.ntasks = p->one_tasks;
+  P.total = p->one_total;
+  P.table = reinterpret_cast<const unsigned char*>(p->one_buf);
+  P.done = reinterpret_cast<unsigned*>(p->one_buf + p->one_done_off);
+  P.ctl = reinterpret_cast<unsigned*>(p->one_buf + p->one_ctl_off);
+  P.wait_ns = p->wait_ns;
+  return step_launch(p->one_per_sm, P, p->one_ctas, p->one_smem, st);
+}
+
+oeb_status run_per_launch(oeb_batch_plan* p, cudaStream_t st);
+
 oeb_status run(oeb_batch_plan* p, cudaStream_t st) {
+  if (p->form == OEB_BATCH_FORM_ONE_LAUNCH) return run_one(p, st);
+  return run_per_launch(p, st);
+}
+
+// The step kernel build with `per_sm` CTAs an SM, sized to fill every SM.
+void use_variant(oeb_batch_plan* p, int per_sm) {
+  p->one_per_sm = per_sm;
+  if (p->one_buf) p->one_ctas = step_occupancy(per_sm, p->one_smem) * p->sms;
+}
+
+oeb_status set_form(oeb_batch_plan* p, int form, int kb, int per_sm) {
+  if (form != OEB_BATCH_FORM_PER_LAUNCH && form != OEB_BATCH_FORM_ONE_LAUNCH) return OEB_ERR_ARGUMENT;
+  if (form == OEB_BATCH_FORM_ONE_LAUNCH) {
+    if (kb != 0 && kb != 1 && kb != 2 && kb != 4 && kb != 8) return OEB_ERR_ARGUMENT;
+    if (per_sm == 0) per_sm = 2;
+    if (!step_variant(per_sm)) return OEB_ERR_ARGUMENT;
+    const int prev = p->one_per_sm;
+    p->one_per_sm = per_sm;
+    if (kb != p->one_kb) {
+      const oeb_status b = build_one(p, kb);
+      if (b != OEB_OK) {
+        p->one_per_sm = prev;
+        return b;
+      }
+    }
+    use_variant(p, per_sm);
+  }
+  p->form = form;
+  return OEB_OK;
+}
+
+// Times a whole run of the plan as it stands, `reps` times after one untimed run.
+oeb_status time_runs(oeb_batch_plan* p, cudaStream_t st, int reps, float* ms) {
+  cudaEvent_t e0, e1;
+  OEB_CUDA_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_fail(cudaGetLastError());
+  }
+  oeb_status r = run(p, st);
+  if (r == OEB_OK && cudaEventRecord(e0, st) != cudaSuccess) r = cuda_fail(cudaGetLastError());
+  for (int i = 0; i < reps && r == OEB_OK; ++i) r = run(p, st);
+  if (r == OEB_OK && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess))
+    r = cuda_fail(cudaGetLastError());
+  if (r == OEB_OK) {
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= (float)reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return r;
+}
+
+// The launch form and, for the one-launch form, the k-blocking and the step kernel build, by
+// timing whole runs: the per-launch form as the plan stands (with the choices of
+// oeb_batch_autotune, if it ran), then the one-launch form with every k-blocking the
+// recordings take, each with every build (2, 3, 4 CTAs an SM).  Keeps the fastest.
+oeb_status autotune_form(oeb_batch_plan* p, cudaStream_t st, float* best_ms_out) {
+  constexpr int kReps = 3;
+  const int kbs[] = {0, 1, 2, 4, 8};
+  float best_ms = 0.f;
+  p->form = OEB_BATCH_FORM_PER_LAUNCH;
+  OEB_TRY(time_runs(p, st, kReps, &best_ms));
+  int best_form = OEB_BATCH_FORM_PER_LAUNCH, best_kb = p->one_kb, best_per_sm = p->one_per_sm;
+  for (int kb : kbs) {
+    const oeb_status b = kb == p->one_kb ? OEB_OK : build_one(p, kb);
+    if (b == OEB_ERR_UNSUPPORTED) break;
+    OEB_TRY(b);
+    p->form = OEB_BATCH_FORM_ONE_LAUNCH;
+    for (int per_sm = 2; per_sm <= 4; ++per_sm) {
+      use_variant(p, per_sm);
+      float ms = 0.f;
+      OEB_TRY(time_runs(p, st, kReps, &ms));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_form = OEB_BATCH_FORM_ONE_LAUNCH;
+        best_kb = kb;
+        best_per_sm = per_sm;
+      }
+    }
+  }
+  if (best_form == OEB_BATCH_FORM_ONE_LAUNCH && best_kb != p->one_kb) OEB_TRY(build_one(p, best_kb));
+  use_variant(p, best_per_sm);
+  p->form = best_form;
+  if (best_ms_out) *best_ms_out = best_ms;
+  return OEB_OK;
+}
+
+// The status word of the last one-launch run: 0, or OEB_ERR_TIMEOUT and the task whose wait
+// gave up.  Waits for the device to be idle first.
+oeb_status step_status(oeb_batch_plan* p, int* status, int* task) {
+  *status = 0;
+  if (task) *task = -1;
+  if (!p->one_buf) return OEB_OK;
+  unsigned ctl[kStepCtlWords];
+  OEB_CUDA_TRY(cudaDeviceSynchronize());
+  OEB_CUDA_TRY(cudaMemcpy(ctl, p->one_buf + p->one_ctl_off, sizeof(ctl), cudaMemcpyDeviceToHost));
+  *status = (int)ctl[1];
+  if (task && ctl[1] != 0u) *task = (int)ctl[2];
+  return OEB_OK;
+}
+
+// The wait statistics of the last one-launch run: the time its CTAs spent in waits that had
+// to poll (us, summed over CTAs) and the number of such waits.
+oeb_status step_waits(oeb_batch_plan* p, uint64_t* wait_us, uint64_t* waits) {
+  *wait_us = 0;
+  *waits = 0;
+  if (!p->one_buf) return OEB_OK;
+  unsigned ctl[kStepCtlWords];
+  OEB_CUDA_TRY(cudaDeviceSynchronize());
+  OEB_CUDA_TRY(cudaMemcpy(ctl, p->one_buf + p->one_ctl_off, sizeof(ctl), cudaMemcpyDeviceToHost));
+  *wait_us = ctl[3];
+  *waits = ctl[4];
+  return OEB_OK;
+}
+
+// Makes the first task of the one-launch form wait for a count that nothing writes (on), or
+// restores it (off): a run then ends with OEB_ERR_TIMEOUT after the wait limit.
+oeb_status withhold(oeb_batch_plan* p, int on) {
+  if (!p->one_buf) return OEB_ERR_ARGUMENT;
+  StepTask t = p->one_first;
+  if (on) {
+    t.dep = p->one_tasks;  // done[ntasks]: never written
+    t.need = 1u;
+  }
+  OEB_CUDA_TRY(cudaDeviceSynchronize());
+  OEB_CUDA_TRY(cudaMemcpy(p->one_buf, &t, sizeof(t), cudaMemcpyHostToDevice));
+  p->withheld = on != 0;
+  return OEB_OK;
+}
+
+oeb_status run_per_launch(oeb_batch_plan* p, cudaStream_t st) {
   OEB_CUDA_TRY(cudaEventRecord(p->fork, st));
   OEB_CUDA_TRY(cudaStreamWaitEvent(p->side, p->fork, 0));
   for (const Slot& sl : p->slots) OEB_TRY(run_slot(p, sl, sl.ctas, sl.per_member, st));
@@ -310,6 +579,7 @@ void destroy(oeb_batch_plan* p) {
     if (m.chain) oeb_chain_plan_destroy(m.chain);
   if (p->arena) cudaFree(p->arena);
   if (p->tables) cudaFree(p->tables);
+  if (p->one_buf) cudaFree(p->one_buf);
   if (p->fork) cudaEventDestroy(p->fork);
   if (p->join) cudaEventDestroy(p->join);
   if (p->side) cudaStreamDestroy(p->side);
@@ -419,7 +689,7 @@ oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
   // buffers hold the data of a complete run before single launches are timed
   for (size_t i = 0; i < best.size(); ++i) best[i].ctas = std::min(best[i].total, best[i].occupancy * p->sms);
   p->slots = best;
-  OEB_TRY(run(p, st));
+  OEB_TRY(run_per_launch(p, st));
   OEB_CUDA_TRY(cudaStreamSynchronize(st));
   OEB_CUDA_TRY(cudaStreamSynchronize(p->side));
   cudaEvent_t e0, e1;
@@ -614,6 +884,7 @@ extern "C" oeb_status oeb_batch_tuning_apply(oeb_batch_plan* p, const int* recor
 }
 
 extern "C" int oeb_batch_launches(const oeb_batch_plan* p) {
+  if (p && p->form == OEB_BATCH_FORM_ONE_LAUNCH) return 1;
   int n = 0;
   if (p)
     for (const Slot& sl : p->slots) n += sl.per_member ? (int)sl.grids.size() : 1;
@@ -629,7 +900,7 @@ extern "C" int64_t oeb_batch_points(const oeb_batch_plan* p) {
 
 extern "C" size_t oeb_batch_plan_bytes(const oeb_batch_plan* p) {
   if (!p) return 0;
-  size_t n = p->arena_bytes + p->table_bytes;
+  size_t n = p->arena_bytes + p->table_bytes + p->one_bytes;
   for (const Member& m : p->members) n += oeb_chain_plan_bytes(m.chain);
   return n;
 }
@@ -638,4 +909,55 @@ extern "C" oeb_status oeb_batch_plan_destroy(oeb_batch_plan* p) {
   if (!p) return OEB_ERR_NULL;
   destroy(p);
   return OEB_OK;
+}
+
+extern "C" oeb_status oeb_batch_set_form(oeb_batch_plan* p, int form, int kb, int ctas_per_sm) {
+  if (!p) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
+  return set_form(p, form, kb, ctas_per_sm);
+}
+
+extern "C" oeb_status oeb_batch_get_form(const oeb_batch_plan* p, int* form, int* kb, int* ctas_per_sm) {
+  if (!p || !form || !kb || !ctas_per_sm) return OEB_ERR_NULL;
+  const bool one = p->form == OEB_BATCH_FORM_ONE_LAUNCH;
+  *form = p->form;
+  *kb = one ? p->one_kb : -1;
+  *ctas_per_sm = one ? p->one_per_sm : -1;
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_batch_step_waits(oeb_batch_plan* p, uint64_t* wait_us, uint64_t* waits) {
+  if (!p || !wait_us || !waits) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
+  return step_waits(p, wait_us, waits);
+}
+
+extern "C" oeb_status oeb_batch_autotune_form(oeb_batch_plan* p, void* stream, float* ms) {
+  if (!p) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
+  return autotune_form(p, (cudaStream_t)stream, ms);
+}
+
+extern "C" oeb_status oeb_batch_step_status(oeb_batch_plan* p, int* status, int* task) {
+  if (!p || !status) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
+  return step_status(p, status, task);
+}
+
+extern "C" oeb_status oeb_batch_set_wait_limit(oeb_batch_plan* p, uint64_t ns) {
+  if (!p) return OEB_ERR_NULL;
+  if (ns == 0) return OEB_ERR_ARGUMENT;
+  p->wait_ns = ns;
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_batch_withhold(oeb_batch_plan* p, int on) {
+  if (!p) return OEB_ERR_NULL;
+  PlanDevice dev(p);
+  if (!dev.ok()) return cuda_fail(cudaGetLastError());
+  return withhold(p, on);
 }

@@ -41,8 +41,13 @@ struct oeb_graph {
   uint64_t kernels;
 };
 
+// Built on its own, this file's bodies and helpers are local to it; the step kernel
+// (step.cu) includes it with OEB_BODIES_ONLY and a namespace of its own instead.
+#ifndef OEB_BODIES_NS
+#define OEB_BODIES_NS
+#endif
 namespace oeb {
-namespace {
+namespace OEB_BODIES_NS {
 
 // Halo widths of the stages (cells added on each side of the interior in i and j).
 constexpr int kE1 = 7, kE2 = 4, kE3 = 3;
@@ -92,6 +97,7 @@ struct Abi<float> {
 // x may be null (0) and may alias out.
 template <class T>
 struct combine_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpCombine);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* out, const T* x, T alpha, const T* __restrict__ y,
                                              int ey, Dims d, int e, int kb) {
     for_box(blk, d, -e, -e, d.nx + 2 * e, d.ny + 2 * e, kb, [&](int64_t o, int i, int j) {
@@ -516,6 +522,8 @@ oeb_status plan_create(const M3* like, const oeb_domain* dom, int modes, oeb_cha
 }  // namespace
 }  // namespace oeb
 
+#ifndef OEB_BODIES_ONLY  // the entry points
+
 using namespace oeb;
 
 extern "C" oeb_status oeb_chain_plan_create_f64(const oeb_memref3d_f64* like, const oeb_domain* dom, int modes,
@@ -613,3 +621,5 @@ extern "C" oeb_status oeb_graph_destroy(oeb_graph* g) {
   delete g;
   return OEB_OK;
 }
+
+#endif  // OEB_BODIES_ONLY

@@ -71,7 +71,11 @@ OEB_DUAL_CMP(>=)
 template <class T>
 __device__ __forceinline__ Dual<T> ld(const Dual<T>* p) {
   const T* q = reinterpret_cast<const T*>(p);
+#ifdef OEB_COHERENT_LOADS  // the step kernel: see ld() in stencil_util.cuh
+  return Dual<T>(__ldca(q), __ldca(q + 1));
+#else
   return Dual<T>(__ldg(q), __ldg(q + 1));
+#endif
 }
 
 template <class T>

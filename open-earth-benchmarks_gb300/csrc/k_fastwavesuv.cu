@@ -14,8 +14,13 @@
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
+// Built on its own, this file's bodies and helpers are local to it; the step kernel
+// (step.cu) includes it with OEB_BODIES_ONLY and a namespace of its own instead.
+#ifndef OEB_BODIES_NS
+#define OEB_BODIES_NS
+#endif
 namespace oeb {
-namespace {
+namespace OEB_BODIES_NS {
 
 constexpr int kT = 32;
 constexpr int kR = kT + 1;                                // apron of one cell in i and j
@@ -31,6 +36,7 @@ struct FastwavesSmem {
 
 template <class T>
 struct fastwavesuv_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFwsFwd);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
                                              const T* __restrict__ uin, const T* __restrict__ vin,
                                              const T* __restrict__ utens, const T* __restrict__ vtens,
@@ -254,6 +260,7 @@ __device__ __forceinline__ T fastwaves_adj_coef(const FastwavesAdjState<T>& st, 
 
 template <class T>
 struct fastwavesuv_adj_terms_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFwsAdjTerms);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, FastwavesAdjTerms<T> tm, FastwavesAdjState<T> st,
                                              const T* __restrict__ uoutb, const T* __restrict__ voutb, T dt, Dims d,
                                              int kb) {
@@ -278,6 +285,7 @@ struct FastwavesAdjSmem {
 // back cost more), from `st`, with the terms pass's expressions; else it reads them from tm.
 template <class T, int FUSED = 0>
 struct fastwavesuv_adj_kernel {
+  static constexpr int kStepOp = step_op<T>(FUSED ? kOpFwsAdjFused : kOpFwsAdj);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
                                              T* __restrict__ utensb, T* __restrict__ vtensb, T* __restrict__ ppuvb,
                                              const T* __restrict__ wgtfac, FastwavesAdjTerms<T> tm,
@@ -435,6 +443,8 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
 }  // namespace
 }  // namespace oeb
 
+#ifndef OEB_BODIES_ONLY  // the entry points
+
 using namespace oeb;
 
 #define OEB_FW_ENTRY(S, T)                                                                                          \
@@ -470,3 +480,5 @@ using namespace oeb;
 
 OEB_FW_ENTRY(f64, double)
 OEB_FW_ENTRY(f32, float)
+
+#endif  // OEB_BODIES_ONLY

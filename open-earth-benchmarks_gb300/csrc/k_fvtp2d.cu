@@ -23,8 +23,13 @@
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
+// Built on its own, this file's bodies and helpers are local to it; the step kernel
+// (step.cu) includes it with OEB_BODIES_ONLY and a namespace of its own instead.
+#ifndef OEB_BODIES_NS
+#define OEB_BODIES_NS
+#endif
 namespace oeb {
-namespace {
+namespace OEB_BODIES_NS {
 
 constexpr int kT = 32;
 
@@ -99,6 +104,7 @@ struct FvQSmem {
 
 template <class T>
 struct fvtp2d_q_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFvQ);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ q_i, T* __restrict__ q_j,
                                              T* __restrict__ fx2, T* __restrict__ fy2, const T* __restrict__ q,
                                              const T* __restrict__ crx, const T* __restrict__ cry,
@@ -243,6 +249,7 @@ struct FvFluxSmem {
 
 template <class T>
 struct fvtp2d_flux_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFvFlux);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ fx1, T* __restrict__ fy1,
                                              const T* __restrict__ q_i, const T* __restrict__ q_j,
                                              const T* __restrict__ fx2, const T* __restrict__ fy2,
@@ -386,6 +393,7 @@ __device__ __forceinline__ void prefetch_box(const T* f, int64_t kofs, int ilo, 
 
 template <class T>
 struct fvtp2d_fused_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFvFused);  // the step kernel's id
   static constexpr int kCtasPerSm = 4;
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ q_i, T* __restrict__ q_j,
                                              T* __restrict__ fx1, T* __restrict__ fx2, T* __restrict__ fy1,
@@ -779,6 +787,7 @@ __device__ __forceinline__ void ppm_sweep_adjoint(PpmAdjSmem<T, LN>& s, int A, i
 // Pass 1: q_ib over i in [-3,N+2), j in [0,N) and q_jb over i in [0,N), j in [-3,N+2).
 template <class T>
 struct fvtp2d_adj_qij_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFvAdjQij);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ qib, T* __restrict__ qjb,
                                              const T* __restrict__ q_i, const T* __restrict__ q_j,
                                              const T* __restrict__ crx, const T* __restrict__ cry,
@@ -836,6 +845,7 @@ struct AdjF2Smem {
 
 template <class T>
 struct fvtp2d_adj_f2_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFvAdjF2);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ fx2b, T* __restrict__ fy2b,
                                              const T* __restrict__ qib, const T* __restrict__ qjb,
                                              const T* __restrict__ xfx, const T* __restrict__ yfx,
@@ -885,6 +895,7 @@ struct fvtp2d_adj_f2_kernel {
 // pass 4: + PPMy^T(fy2b) (y sweep, adds).
 template <class T>
 struct fvtp2d_adj_q_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpFvAdjQ);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ qb, const T* __restrict__ q,
                                              const T* __restrict__ crx, const T* __restrict__ cry,
                                              const T* __restrict__ area, const T* __restrict__ ra_x,
@@ -1000,6 +1011,8 @@ oeb_status fvtp2d_adj_entry(const M3* qb, const M3* q, const M3* crx, const M3* 
 }  // namespace
 }  // namespace oeb
 
+#ifndef OEB_BODIES_ONLY  // the entry points
+
 using namespace oeb;
 
 #define OEB_FV_ENTRY(S, T)                                                                                          \
@@ -1033,3 +1046,5 @@ using namespace oeb;
 
 OEB_FV_ENTRY(f64, double)
 OEB_FV_ENTRY(f32, float)
+
+#endif  // OEB_BODIES_ONLY

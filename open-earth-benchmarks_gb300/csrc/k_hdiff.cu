@@ -22,8 +22,13 @@
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
+// Built on its own, this file's bodies and helpers are local to it; the step kernel
+// (step.cu) includes it with OEB_BODIES_ONLY and a namespace of its own instead.
+#ifndef OEB_BODIES_NS
+#define OEB_BODIES_NS
+#endif
 namespace oeb {
-namespace {
+namespace OEB_BODIES_NS {
 
 constexpr int kT = 32;  // tile edge
 
@@ -221,6 +226,7 @@ struct HdiffsmagSmem {
 
 template <class T>
 struct hdiffsmag_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpSmagFwd);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
                                              const T* __restrict__ uin, const T* __restrict__ vin,
                                              const T* __restrict__ mask, const T* __restrict__ crlavo,
@@ -615,6 +621,7 @@ struct SmagAdjSmem {
 
 template <class T>
 struct hdiffsmag_adj_terms_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpSmagAdjTerms);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, SmagTerms<T> tm, const T* __restrict__ uin,
                                              const T* __restrict__ vin, const T* __restrict__ mask,
                                              const T* __restrict__ crlavo, const T* __restrict__ crlavu,
@@ -675,6 +682,7 @@ struct hdiffsmag_adj_terms_kernel {
 
 template <class T>
 struct hdiffsmag_adj_ts_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpSmagAdjTs);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, SmagTerms<T> tm, const T* __restrict__ uin,
                                              const T* __restrict__ vin, const T* __restrict__ acrlat0, int64_t s1d,
                                              T eddlat, T eddlon, Dims d, int kb) {
@@ -704,6 +712,7 @@ struct hdiffsmag_adj_ts_kernel {
 
 template <class T>
 struct hdiffsmag_adj_gather_kernel {
+  static constexpr int kStepOp = step_op<T>(kOpSmagAdjGather);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
                                              SmagTerms<T> tm, const T* __restrict__ uoutb,
                                              const T* __restrict__ voutb, const T* __restrict__ crlavo,
@@ -780,6 +789,7 @@ struct SmagAdjF32Smem {
 };
 
 struct hdiffsmag_adj_f32 {
+  static constexpr int kStepOp = step_op<float>(kOpSmagAdjFused);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uinb, float* __restrict__ vinb,
                                              const float* __restrict__ uin, const float* __restrict__ vin,
                                              const float* __restrict__ mask, const float* __restrict__ crlavo,
@@ -996,6 +1006,7 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
   return stt;
 }
 
+#ifndef OEB_BODIES_ONLY
 // ==================== hdiffsmag adjoint without any allocation (FP64) ====================
 // oeb_hdiffsmag_adj_noalloc_f64 is for callers that cannot allocate device memory while they
 // run: a host whose own allocator has already claimed the GPU's memory up front (an
@@ -1084,9 +1095,12 @@ oeb_status hdiffsmag_adj_noalloc_entry(const oeb_memref3d_f64* uinb, const oeb_m
       (const T*)voutb->aligned + voutb->offset, org1(crlavo), org1(crlavu), org1(crlato), org1(crlatu), org1(acrlat0),
       s1d, eddlat, eddlon, d, kKB);
 }
+#endif  // OEB_BODIES_ONLY
 
 }  // namespace
 }  // namespace oeb
+
+#ifndef OEB_BODIES_ONLY  // the entry points
 
 using namespace oeb;
 
@@ -1152,3 +1166,5 @@ extern "C" oeb_status oeb_hdiffsmag_adj_noalloc_f64(
   return hdiffsmag_adj_noalloc_entry(uinb, vinb, uin, vin, mask, crlavo, crlavu, crlato, crlatu, acrlat0, uoutb, voutb,
                                      eddlat, eddlon, tau_smag, weight_smag, dom, stream);
 }
+
+#endif  // OEB_BODIES_ONLY

@@ -23,8 +23,13 @@
 #include "stencil_util.cuh"
 #include "tangent.cuh"
 
+// Built on its own, this file's bodies and helpers are local to it; the step kernel
+// (step.cu) includes it with OEB_BODIES_ONLY and a namespace of its own instead.
+#ifndef OEB_BODIES_NS
+#define OEB_BODIES_NS
+#endif
 namespace oeb {
-namespace {
+namespace OEB_BODIES_NS {
 
 constexpr int kTI = 32, kTJ = 32, kRows = kTJ / kTY;
 
@@ -280,6 +285,7 @@ __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64
 
 template <class T, int ORDER, int SHAPE = 0>
 struct hadv_kernel {
+  static constexpr int kStepOp = step_op<T>(ORDER == 5 ? kOpHadv5Fwd + SHAPE : -1);  // the step kernel's id
   static constexpr int kShape = SHAPE;
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uout, T* __restrict__ vout,
                                              const T* __restrict__ uin, const T* __restrict__ vin,
@@ -764,6 +770,7 @@ __device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t
 
 template <class T, int ORDER, int SHAPE = 0>
 struct hadv_adj_terms_kernel {
+  static constexpr int kStepOp = step_op<T>(ORDER == 5 ? kOpHadv5AdjTerms + SHAPE : -1);  // the step kernel's id
   // FP64: 80 registers instead of 94, three CTAs per SM instead of two (the hadvuv5th
   // adjoint 4 % faster; the same bound on the hdiffsmag and fastwavesuv adjoints was slower)
   static constexpr int kMinCtas = sizeof(T) == 8 ? 3 : 0;
@@ -825,6 +832,7 @@ __device__ __forceinline__ void for_box_points(const uint3& blk, const Dims& d, 
 
 template <class T, int ORDER>
 struct hadv_adj_gather_kernel {
+  static constexpr int kStepOp = step_op<T>(ORDER == 5 ? kOpHadv5AdjGather : -1);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
                                              HadvTerms<T> tm, Dims d, int kb) {
     constexpr int h = ORDER == 3 ? 2 : 3;
@@ -1458,6 +1466,8 @@ oeb_status nh_p_grad_adj_entry(const M3* uinb, const M3* vinb, const M3* gzb, co
 }  // namespace
 }  // namespace oeb
 
+#ifndef OEB_BODIES_ONLY  // the entry points
+
 using namespace oeb;
 
 #define OEB_M3(S) oeb_memref3d_##S
@@ -1594,3 +1604,5 @@ OEB_POINTWISE_ENTRIES(f64, double)
 OEB_POINTWISE_ENTRIES(f32, float)
 OEB_POINTWISE_DIFF_ENTRIES(f64, double)
 OEB_POINTWISE_DIFF_ENTRIES(f32, float)
+
+#endif  // OEB_BODIES_ONLY

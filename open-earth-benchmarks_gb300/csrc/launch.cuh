@@ -6,8 +6,9 @@
 // installed on the calling thread -- records the grid and the arguments instead.  A batch plan
 // (batch.cu) records the same sequence of calls for many ensemble members and then replays
 // each recorded position as ONE persistent launch over all members: batch_kernel, whose CTAs
-// walk a list of (member, tile) items.  The bodies never read blockIdx or gridDim, so a tile
-// computes the same results in either form.
+// walk a list of (member, tile) items -- or runs every member's whole step in one launch of the
+// step kernel (step.cu), which calls the bodies that declare a kStepOp.  The bodies never read
+// blockIdx or gridDim, so a tile computes the same results in every form.
 //
 // Every kernel instantiated for double runs as the same kernel instantiated for F64i
 // (precision.cuh): double arithmetic with the multiplications on the integer pipe, bit for
@@ -24,6 +25,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -102,6 +104,66 @@ constexpr auto grid_entry() {
     return &grid_kernel<Body, A...>;
 }
 
+// ---- the one-launch step (step.cu) --------------------------------------------------------
+// A batch plan can also run every member's whole step as ONE persistent launch of the step
+// kernel, which calls the bodies of the chained step from a single switch.  A body that may
+// run there declares `static constexpr int kStepOp = step_op<T>(kOp...)`: an id unique over
+// both precisions.  Bodies without one (or instantiated for another T, e.g. Dual) are -1.
+enum StepOpBase : int {
+  kOpCombine,
+  kOpFwsFwd,
+  kOpFwsAdjTerms,
+  kOpFwsAdj,       // fastwavesuv_adj_kernel<T, 0>: the march over the terms pass's coefficients
+  kOpFwsAdjFused,  // fastwavesuv_adj_kernel<T, 1>: the march that forms them itself
+  kOpHadv5Fwd,     // + tile shape (3 shapes)
+  kOpHadv5AdjTerms = kOpHadv5Fwd + 3,  // + tile shape
+  kOpHadv5AdjGather = kOpHadv5AdjTerms + 3,
+  kOpSmagFwd,
+  kOpSmagAdjTerms,
+  kOpSmagAdjTs,
+  kOpSmagAdjGather,
+  kOpSmagAdjFused,
+  kOpFvQ,
+  kOpFvFlux,
+  kOpFvFused,
+  kOpFvAdjQij,
+  kOpFvAdjF2,
+  kOpFvAdjQ,
+  kStepOpBases
+};
+template <class T>
+constexpr int step_op(int base) {
+  return base < 0 ? -1 : std::is_same<T, F64i>::value ? 2 * base : std::is_same<T, float>::value ? 2 * base + 1 : -1;
+}
+constexpr int kStepOps = 2 * kStepOpBases;
+
+template <class Body, class = void>
+struct StepOpOf {
+  static constexpr int value = -1;
+};
+template <class Body>
+struct StepOpOf<Body, std::void_t<decltype(Body::kStepOp)>> {
+  static constexpr int value = Body::kStepOp;
+};
+
+// The argument pack of a body's run() parameters (after the tile index), decayed: what the
+// step kernel reads.  A recording converts the call's arguments to these types on the host,
+// as an ordinary launch converts them when it calls run().
+template <class... P>
+Pack<std::decay_t<P>...> run_pack_of(void (*)(const uint3&, P...));
+template <class Body>
+using RunPack = decltype(run_pack_of(&Body::run));
+template <class P>
+struct PackFrom;
+template <class... P>
+struct PackFrom<Pack<P...>> {
+  template <class... A>
+  static Pack<P...> make(A... a) {
+    static_assert(sizeof...(A) == sizeof...(P), "run() takes a different number of arguments");
+    return make_pack(static_cast<P>(a)...);
+  }
+};
+
 // One item per (member, tile); tiles[m] = {first item of member m, tiles along x, along y}.
 struct BatchTile {
   int first, gx, gy, pad;
@@ -145,6 +207,8 @@ struct LaunchRecord {
   dim3 grid;
   size_t smem;
   std::vector<unsigned char> args;  // Pack<A...>
+  int step_op = -1;                      // the body's kStepOp (-1: the step kernel cannot run it)
+  std::vector<unsigned char> step_args;  // RunPack<Body>, for the step kernel
 };
 
 struct Recorder {
@@ -300,6 +364,12 @@ oeb_status launch_as(dim3 grid, size_t smem, cudaStream_t st, A... a) {
     const Pack<A...> p = make_pack(a...);
     rec.args.resize(sizeof(p));
     memcpy(rec.args.data(), &p, sizeof(p));
+    if constexpr (StepOpOf<Body>::value >= 0) {
+      const RunPack<Body> rp = PackFrom<RunPack<Body>>::make(a...);
+      rec.step_op = StepOpOf<Body>::value;
+      rec.step_args.resize(sizeof(rp));
+      memcpy(rec.step_args.data(), &rp, sizeof(rp));
+    }
     r->records.push_back(std::move(rec));
     return OEB_OK;
   }

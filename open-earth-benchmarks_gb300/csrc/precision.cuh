@@ -440,7 +440,11 @@ __device__ __forceinline__ bool operator!=(F64i a, F64i b) { return !fp64::eq(a.
 // float and double overloads stay visible beside it
 using ::fma;
 __device__ __forceinline__ F64i fma(F64i a, F64i b, F64i c) { return F64i(::fma(a.v, b.v, c.v)); }
+#ifdef OEB_COHERENT_LOADS  // the step kernel: see ld() in stencil_util.cuh
+__device__ __forceinline__ F64i ld(const F64i* p) { return F64i(__ldca(reinterpret_cast<const double*>(p))); }
+#else
 __device__ __forceinline__ F64i ld(const F64i* p) { return F64i(__ldg(reinterpret_cast<const double*>(p))); }
+#endif
 
 template <>
 struct Prec<F64i> {

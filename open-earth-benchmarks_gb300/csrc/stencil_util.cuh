@@ -67,10 +67,18 @@ __device__ __forceinline__ void prefetch_tile(const T* const (&fields)[N], int64
   }
 }
 
-// Read-only global load through the non-coherent path.
+// Read-only global load through the non-coherent path.  The step kernel (step.cu), whose later
+// tasks read what earlier tasks of the same launch wrote, compiles the bodies with
+// OEB_COHERENT_LOADS: an ordinary cached load, which observes those writes once the task's wait
+// (an acquire, then a CTA barrier) has seen them counted; the non-coherent path is defined only
+// for data that nothing writes while the kernel runs.
 template <class T>
 __device__ __forceinline__ T ld(const T* p) {
+#ifdef OEB_COHERENT_LOADS
+  return __ldca(p);
+#else
   return __ldg(p);
+#endif
 }
 
 // std::min(0.5, std::max(0.0, x)) with libstdc++'s comparisons (hdiffsmag.h:236, :251):

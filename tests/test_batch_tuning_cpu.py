@@ -48,6 +48,16 @@ def test_abi_rejects_a_null_plan(pkg):
     assert lib.oeb_batch_tuning_get(None, rec, 2, ctypes.byref(n)) == 1  # OEB_ERR_NULL
     assert lib.oeb_batch_tuning_apply(None, rec, 2) == 1
     assert lib.oeb_batch_signature(None, ctypes.byref(sig)) == 1
+    # the one-launch form's entry points
+    form, kb, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert lib.oeb_batch_set_form(None, 1, 0, 2) == 1
+    assert lib.oeb_batch_get_form(None, ctypes.byref(form), ctypes.byref(kb), ctypes.byref(st)) == 1
+    us, n = ctypes.c_uint64(), ctypes.c_uint64()
+    assert lib.oeb_batch_step_waits(None, ctypes.byref(us), ctypes.byref(n)) == 1
+    assert lib.oeb_batch_autotune_form(None, None, None) == 1
+    assert lib.oeb_batch_step_status(None, ctypes.byref(st), None) == 1
+    assert lib.oeb_batch_set_wait_limit(None, ctypes.c_uint64(1000)) == 1
+    assert lib.oeb_batch_withhold(None, 1) == 1
 
 
 def test_saved_record_is_applied_to_a_plan_with_the_same_signature(chain, tmp_path):
