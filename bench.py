@@ -660,6 +660,23 @@ def _adjoint_leg(pkg, fields, torch, dev, args, dtype, shape=(NX, NY, NZ)):
 
 
 def _chain_leg(pkg, fields, torch, dev, args, dtype):
+    """The chained step in both fusion groupings: separate kernels (the line's figures) and
+    hadvuv5th fused with the update (``fused``)."""
+    import ctypes
+    lib = pkg.load_library()
+    res = _chain_leg_grouping(pkg, fields, torch, dev, args, dtype)
+    lib.oeb_set_fusion(ctypes.c_int(1))
+    try:
+        fused = _chain_leg_grouping(pkg, fields, torch, dev, args, dtype)
+    finally:
+        lib.oeb_set_fusion(ctypes.c_int(0))
+    res["fused"] = {"grouping": "hadvuv5th and the update as one kernel (OEB_FUSE_HADV_UPDATE)",
+                    **{k: fused[k] for k in ("ms_per_step", "gpts", "kernels_per_step", "launches_per_step")},
+                    "speedup": round(res["ms_per_step"] / fused["ms_per_step"], 3)}
+    return res
+
+
+def _chain_leg_grouping(pkg, fields, torch, dev, args, dtype):
     """The chained dycore step forward + adjoint at 128x128x80 (i/j halo 8, seed 3), captured
     once per input set in a CUDA graph; two graphs on two input sets alternate."""
     import importlib
@@ -830,7 +847,7 @@ def _batch_leg(pkg, fields, torch, dev, args):
            "speedup_vs_per_member_launches": round(ms_members / ms_batch, 3),
            "autotune_s": round(tune_s, 2), "plan_bytes": plan.nbytes,
            "plan_bytes_per_point": round(plan.nbytes / pts, 1),
-           "tuned": _tuning_summary(plan.tuning()),
+           "tuned": _tuning_summary(plan.tuning()), "fusion": plan.fusion,
            "one_launch": one_launch}
     g.close()
     g2.close()

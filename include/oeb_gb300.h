@@ -123,6 +123,16 @@ OEB_API oeb_status oeb_set_kblock(int kb);
  * 2 = 64 x 16.  OEB_ERR_ARGUMENT for any other value.  A tuning knob: results do not depend
  * on it.  Batch plans choose their own shapes (oeb_batch_autotune). */
 OEB_API oeb_status oeb_set_tile_shape(int shape);
+/* Fusion groupings of the chained step (no counterpart in the reference, which has no chained
+ * step): a bit mask of stages that run as one kernel in every later oeb_chain_* call.
+ * OEB_FUSE_HADV_UPDATE: hadvuv5th and the explicit update u2 = u1 + dt_adv * tendency in one
+ * kernel (the advection writes u2, v2 directly), and in the adjoint step the hadvuv5th
+ * gather and the update's transpose in one kernel.  0 (the default): separate kernels.
+ * OEB_ERR_ARGUMENT for other bits.  A tuning knob: results do not depend on it.  Batch plans
+ * choose their own grouping (oeb_batch_autotune, oeb_batch_set_fusion). */
+#define OEB_FUSE_HADV_UPDATE 1
+#define OEB_FUSE_ALL 1
+OEB_API oeb_status oeb_set_fusion(int mask);
 /* k-slabs of the host entry points' copy/compute/copy pipeline (1..8), for every later call;
  * 0 (the default) picks 8 for synchronous calls that move 8 MB or more, and 1 for smaller
  * and for asynchronous calls.  A tuning knob: results do not depend on it. */
@@ -815,8 +825,17 @@ OEB_API oeb_status oeb_batch_autotune(oeb_batch_plan* plan, void* stream);
  *   plan is unchanged.  Results do not depend on the record.  Do not call it during a
  *   stream capture.
  * oeb_batch_signature: a 64-bit hash of the modes, each member's element size and domain
- *   (in order) and the launch count.  A record saved with one signature fits any plan
- *   with the same signature. */
+ *   (in order) and the launch count without fusion.  A record saved with one signature fits
+ *   any plan with the same signature, in the same fusion grouping. */
+/* Fusion grouping of a batch plan (OEB_FUSE_* as for oeb_set_fusion): which stages of the
+ * chained step each member runs as one kernel.  oeb_batch_autotune tunes the launches of each
+ * grouping, times a whole run of each, and keeps the faster grouping with its choices; a
+ * tuning record fits the grouping it was taken with, so set that grouping before applying it.
+ * oeb_batch_set_fusion records the step again with `mask` and the default choices (as at
+ * creation), and rebuilds the one-launch tables if the plan has them; it waits for the device
+ * to go idle.  OEB_ERR_ARGUMENT for unknown bits.  Results do not depend on the grouping. */
+OEB_API oeb_status oeb_batch_set_fusion(oeb_batch_plan* plan, int mask);
+OEB_API oeb_status oeb_batch_get_fusion(const oeb_batch_plan* plan, int* mask);
 OEB_API oeb_status oeb_batch_tuning_get(const oeb_batch_plan* plan, int* record, int capacity, int* count);
 OEB_API oeb_status oeb_batch_tuning_apply(oeb_batch_plan* plan, const int* record, int count);
 OEB_API oeb_status oeb_batch_signature(const oeb_batch_plan* plan, uint64_t* out);

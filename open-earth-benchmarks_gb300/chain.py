@@ -27,6 +27,7 @@ from .abi import OebError, check, entry, load_library
 from .storage import Domain, Memref1d, Memref3d, Storage
 
 FORWARD, TL, ADJOINT = 1, 2, 4
+FUSE_HADV_UPDATE = 1  # hadvuv5th and the explicit update as one kernel (oeb_set_fusion)
 HALO = 8  # i/j halo the step's inputs need
 
 FIELDS3 = ("u", "v", "utens", "vtens", "wgtfac", "ppuv", "hhl", "rho")
@@ -226,7 +227,7 @@ class BatchPlan:
     def autotune(self, stream=None):
         check(entry("oeb_batch_autotune")(self._plan, ctypes.c_void_p(_stream(stream))), "oeb_batch_autotune")
 
-    TUNING_FORMAT = "oeb-batch-tuning/2"
+    TUNING_FORMAT = "oeb-batch-tuning/3"
 
     @property
     def signature(self) -> int:
@@ -259,11 +260,23 @@ class BatchPlan:
         check(entry("oeb_batch_tuning_apply")(self._plan, rec, ctypes.c_int(len(flat) // 3)),
               "oeb_batch_tuning_apply")
 
+    @property
+    def fusion(self) -> int:
+        """The fusion grouping the plan's launches were recorded with (FUSE_* bits)."""
+        m = ctypes.c_int()
+        check(entry("oeb_batch_get_fusion")(self._plan, ctypes.byref(m)), "oeb_batch_get_fusion")
+        return int(m.value)
+
+    def set_fusion(self, mask: int) -> None:
+        """Records the step again with fusion grouping `mask` and the default choices."""
+        check(entry("oeb_batch_set_fusion")(self._plan, ctypes.c_int(mask)), "oeb_batch_set_fusion")
+
     def save_tuning(self, path) -> None:
-        """Writes the plan's choices as a JSON tuning record, keyed by its signature."""
+        """Writes the plan's fusion grouping and choices as a JSON tuning record, keyed by its
+        signature."""
         with open(path, "w") as f:
             json.dump({"format": self.TUNING_FORMAT, "signature": "%016x" % self.signature,
-                       "choices": [list(c) for c in self.tuning()]}, f)
+                       "fusion": self.fusion, "choices": [list(c) for c in self.tuning()]}, f)
 
     def load_tuning(self, path) -> None:
         """Applies a record written by save_tuning.  Raises OebError, leaving the plan as it
@@ -276,6 +289,8 @@ class BatchPlan:
         if rec.get("signature") != "%016x" % self.signature:
             raise OebError("%s: saved for another ensemble (signature %s, this plan %016x)"
                            % (path, rec.get("signature"), self.signature))
+        if self.fusion != rec.get("fusion", 0):
+            self.set_fusion(int(rec.get("fusion", 0)))
         self.apply_tuning(rec["choices"])
 
     # launch forms (oeb_batch_set_form)

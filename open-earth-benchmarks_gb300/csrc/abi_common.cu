@@ -84,6 +84,8 @@ namespace {
 std::atomic<int> g_shape_override{0};
 }  // namespace
 int shape_override() { return g_shape_override.load(std::memory_order_relaxed); }
+std::atomic<int> g_fusion_override{0};
+int fusion_override() { return g_fusion_override.load(std::memory_order_relaxed); }
 
 namespace {
 thread_local int t_host_in_place = 0;
@@ -441,6 +443,12 @@ extern "C" int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m) { retu
 extern "C" oeb_status oeb_set_tile_shape(int shape) {
   if (shape < 0 || shape >= oeb::kShapes) return OEB_ERR_ARGUMENT;
   oeb::g_shape_override.store(shape, std::memory_order_relaxed);
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_set_fusion(int mask) {
+  if (mask & ~OEB_FUSE_ALL) return OEB_ERR_ARGUMENT;
+  oeb::g_fusion_override.store(mask, std::memory_order_relaxed);
   return OEB_OK;
 }
 

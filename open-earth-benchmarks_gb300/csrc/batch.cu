@@ -87,6 +87,8 @@ struct oeb_batch_plan {
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   // the one-launch form (step.cu): every member's step in one launch of the step kernel
+  int fusion = 0;         // the fusion grouping its launches were recorded with (OEB_FUSE_*)
+  size_t base_slots = 0;  // slots of the grouping 0 (in the signature, which any grouping shares)
   int form = OEB_BATCH_FORM_PER_LAUNCH;
   int one_kb = -1;          // the k-blocking its tasks were recorded with (-1: not built)
   char* one_buf = nullptr;  // tasks, argument packs, then the done counters and control words
@@ -191,6 +193,7 @@ oeb_status record_all(oeb_batch_plan* p, int kb, int shape, std::vector<std::vec
       Recorder rec;
       rec.kb = kb;
       rec.shape = shape;
+      rec.fusion = p->fusion;
       rec.arena = p->arena + m.arena_off;
       rec.arena_bytes = m.arena_size;
       OEB_TRY(record(m, kModes[mi], &rec));
@@ -663,11 +666,12 @@ oeb_status create(const oeb_batch_member* in, int count, int modes, oeb_batch_pl
   if (st == OEB_OK) st = build_slots(p, seq, 0, 0, &p->slots, &host, 0);
   if (st == OEB_OK) st = upload(p, host);
   if (st != OEB_OK) return fail(st);
+  p->base_slots = p->slots.size();
   *out = p;
   return OEB_OK;
 }
 
-oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
+oeb_status autotune_slots(oeb_batch_plan* p, cudaStream_t st) {
   const int kbs[] = {1, 2, 4, 8};
   constexpr int kReps = 3;
   // every candidate's slots -- each k-blocking with each tile shape -- in one table buffer
@@ -766,7 +770,7 @@ uint64_t signature(const oeb_batch_plan* p) {
     mix(m.dom.ny);
     mix(m.dom.nz);
   }
-  mix((int64_t)p->slots.size());
+  mix((int64_t)p->base_slots);
   return h;
 }
 
@@ -820,6 +824,76 @@ oeb_status tuning_apply(oeb_batch_plan* p, const int* rec, int count) {
   OEB_TRY(upload(p, host));
   p->slots = std::move(next);
   return OEB_OK;
+}
+
+// Records the step with fusion grouping `mask` and replaces the plan's launches by its
+// default choices (kb 0, the default shape, one persistent wave), as at creation.  The
+// one-launch tables, if built, are rebuilt for the new grouping; if that fails they are
+// dropped (and a one-launch plan falls back to the per-launch form).  On any earlier error
+// the plan is unchanged.
+oeb_status set_fusion(oeb_batch_plan* p, int mask) {
+  if (mask & ~OEB_FUSE_ALL) return OEB_ERR_ARGUMENT;
+  const int prev = p->fusion;
+  p->fusion = mask;
+  std::vector<std::vector<std::vector<LaunchRecord>>> seq;
+  std::vector<Slot> slots;
+  std::vector<char> host;
+  oeb_status st = record_all(p, 0, 0, &seq);
+  if (st == OEB_OK) st = build_slots(p, seq, 0, 0, &slots, &host, 0);
+  if (st == OEB_OK) st = upload(p, host);
+  if (st != OEB_OK) {
+    p->fusion = prev;
+    return st;
+  }
+  p->slots = std::move(slots);
+  if (p->one_buf) {
+    st = build_one(p, p->one_kb);
+    if (st != OEB_OK) {
+      cudaDeviceSynchronize();
+      cudaFree(p->one_buf);
+      p->one_buf = nullptr;
+      p->one_bytes = 0;
+      p->one_kb = -1;
+      p->form = OEB_BATCH_FORM_PER_LAUNCH;
+      return st;
+    }
+  }
+  return OEB_OK;
+}
+
+// The autotuner: for each fusion grouping, the per-launch choices (autotune_slots) and the
+// time of a whole run with them; keeps the grouping whose run is faster, with its choices.
+// Times the per-launch form whatever the plan's form; leaves the form as it was.
+oeb_status autotune(oeb_batch_plan* p, cudaStream_t st) {
+  const int form = p->form;
+  p->form = OEB_BATCH_FORM_PER_LAUNCH;
+  const int masks[] = {0, OEB_FUSE_HADV_UPDATE};
+  float best_ms = -1.f;
+  int best_mask = p->fusion;
+  std::vector<int> best_rec;
+  oeb_status r = OEB_OK;
+  for (int mask : masks) {
+    r = set_fusion(p, mask);
+    if (r == OEB_OK) r = autotune_slots(p, st);
+    float ms = 0.f;
+    if (r == OEB_OK) r = time_runs(p, st, 3, &ms);
+    if (r != OEB_OK) break;
+    if (best_ms < 0.f || ms < best_ms) {
+      best_ms = ms;
+      best_mask = mask;
+      int n = 0;
+      tuning_get(p, nullptr, 0, &n);
+      best_rec.assign(3 * (size_t)n, 0);
+      r = tuning_get(p, best_rec.data(), n, &n);
+      if (r != OEB_OK) break;
+    }
+  }
+  if (r == OEB_OK && best_mask != p->fusion) {
+    r = set_fusion(p, best_mask);
+    if (r == OEB_OK) r = tuning_apply(p, best_rec.data(), (int)(best_rec.size() / 3));
+  }
+  if (p->one_buf) p->form = form;
+  return r;
 }
 
 // Makes the plan's device current for the lifetime of the guard and restores the caller's
@@ -960,4 +1034,17 @@ extern "C" oeb_status oeb_batch_withhold(oeb_batch_plan* p, int on) {
   PlanDevice dev(p);
   if (!dev.ok()) return cuda_fail(cudaGetLastError());
   return withhold(p, on);
+}
+
+extern "C" oeb_status oeb_batch_set_fusion(oeb_batch_plan* p, int mask) {
+  if (!p) return OEB_ERR_NULL;
+  PlanDevice on(p);
+  if (!on.ok()) return cuda_fail(cudaGetLastError());
+  return set_fusion(p, mask);
+}
+
+extern "C" oeb_status oeb_batch_get_fusion(const oeb_batch_plan* p, int* mask) {
+  if (!p || !mask) return OEB_ERR_NULL;
+  *mask = p->fusion;
+  return OEB_OK;
 }

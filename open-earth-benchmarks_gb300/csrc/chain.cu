@@ -17,6 +17,7 @@
 #include <new>
 #include <vector>
 
+#include "fused.cuh"
 #include "oeb_common.cuh"
 #include "stencil_util.cuh"
 
@@ -220,11 +221,16 @@ oeb_status run_stages_123(oeb_chain_plan* p, const typename Abi<T>::Fields* f, c
     const M1 fx = widen1(f->fx, kE1);
     OEB_TRY(A::fastwavesuv(&o_u, &o_v, &u, &v, &ut, &vt, &w, &pp, &h, &r, &fx, T(s->edadlat), T(s->dt), &d1, stream));
   }
+  const M1 a0 = widen1(f->acrlat0, kE2), a1 = widen1(f->acrlat1, kE2), t0 = widen1(f->tgrlatda0, kE2),
+           t1 = widen1(f->tgrlatda1, kE2);
+  const M3 u = wsw<T>(p, p->u1, kE2), v = wsw<T>(p, p->v1, kE2);
+  if (tuned_fusion() & OEB_FUSE_HADV_UPDATE) {  // stages 2 and 3 in one kernel: (u2, v2) directly
+    const M3 o_u = wsw<T>(p, p->u2, kE2), o_v = wsw<T>(p, p->v2, kE2);
+    return hadvuv5th_update(&o_u, &o_v, &u, &v, &a0, &a1, &t0, &t1, T(s->eddlat), T(s->eddlon), T(s->dt_adv), &d2,
+                            stream);
+  }
   {
     const M3 o_u = wsw<T>(p, p->tu, kE2), o_v = wsw<T>(p, p->tv, kE2);
-    const M3 u = wsw<T>(p, p->u1, kE2), v = wsw<T>(p, p->v1, kE2);
-    const M1 a0 = widen1(f->acrlat0, kE2), a1 = widen1(f->acrlat1, kE2), t0 = widen1(f->tgrlatda0, kE2),
-             t1 = widen1(f->tgrlatda1, kE2);
     OEB_TRY(A::hadvuv5th(&o_u, &o_v, &u, &v, &a0, &a1, &t0, &t1, T(s->eddlat), T(s->eddlon), &d2, stream));
   }
   if (validating()) return OEB_OK;
@@ -373,6 +379,7 @@ oeb_status chain_adj(oeb_chain_plan* p, const typename Abi<T>::Fields* f, const 
   }
   const oeb_domain d1 = widen_dom(p->dom, kE1), d2 = widen_dom(p->dom, kE2), d3 = widen_dom(p->dom, kE3);
   cudaStream_t cs = (cudaStream_t)stream;
+  const bool fused = (tuned_fusion() & OEB_FUSE_HADV_UPDATE) != 0;
   auto run = [&]() -> oeb_status {
     // recompute the forward intermediates
     oeb_status st = run_stages_123<T>(p, f, s, stream);
@@ -405,10 +412,13 @@ oeb_status chain_adj(oeb_chain_plan* p, const typename Abi<T>::Fields* f, const 
                yu = wsw<T>(p, p->u2b, kE2), yv = wsw<T>(p, p->v2b, kE2);
       const M1 a0 = widen1(f->acrlat0, kE2), a1 = widen1(f->acrlat1, kE2), t0 = widen1(f->tgrlatda0, kE2),
                t1 = widen1(f->tgrlatda1, kE2);
-      st = A::hadvuv5th_adj(&o_u, &o_v, &u, &v, &a0, &a1, &t0, &t1, &yu, &yv, T(s->eddlat), T(s->eddlon), &d2,
-                            stream);
+      st = fused ? hadvuv5th_adj_update(&o_u, &o_v, &u, &v, &a0, &a1, &t0, &t1, &yu, &yv, T(s->eddlat),
+                                        T(s->eddlon), T(s->dt_adv), &d2, stream)
+                 : A::hadvuv5th_adj(&o_u, &o_v, &u, &v, &a0, &a1, &t0, &t1, &yu, &yv, T(s->eddlat), T(s->eddlon),
+                                    &d2, stream);
     }
-    if (st == OEB_OK && !validating()) {  // stage 3: (u1b, v1b) = dt_adv (wu, wv) + (u2b, v2b)
+    // stage 3: (u1b, v1b) = dt_adv (wu, wv) + (u2b, v2b), unless the gather above added it
+    if (st == OEB_OK && !validating() && !fused) {
       st = launch_combine<T>(p, p->wu, p->wu, T(s->dt_adv), p->u2b, kE2, kE1, cs);
       if (st == OEB_OK) st = launch_combine<T>(p, p->wv, p->wv, T(s->dt_adv), p->v2b, kE2, kE1, cs);
     }

@@ -22,6 +22,7 @@
 #include "stage.cuh"
 #include "stencil_util.cuh"
 #include "tangent.cuh"
+#include "fused.cuh"
 
 // Built on its own, this file's bodies and helpers are local to it; the step kernel
 // (step.cu) includes it with OEB_BODIES_ONLY and a namespace of its own instead.
@@ -283,6 +284,9 @@ __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64
   }
 }
 
+// update != 0 fuses the chained step's explicit update into the epilogue: the outputs are
+// alpha * (the tendency) + (the input), the same two roundings as the tendency stored and then
+// combined by a separate kernel.
 template <class T, int ORDER, int SHAPE = 0>
 struct hadv_kernel {
   static constexpr int kStepOp = step_op<T>(ORDER == 5 ? kOpHadv5Fwd + SHAPE : -1);  // the step kernel's id
@@ -291,7 +295,7 @@ struct hadv_kernel {
                                              const T* __restrict__ uin, const T* __restrict__ vin,
                                              const T* __restrict__ acrlat0, const T* __restrict__ acrlat1,
                                              const T* __restrict__ tgrlatda0, const T* __restrict__ tgrlatda1,
-                                             int64_t s1d, T eddlat, T eddlon, Dims d, int kb) {
+                                             int64_t s1d, T eddlat, T eddlon, Dims d, int kb, T alpha, int update) {
     const int64_t sj = d.sj;
     constexpr T third = T(1.0) / T(3.0);
     constexpr T rr = earth_radius_recip<T>();
@@ -313,7 +317,8 @@ struct hadv_kernel {
         ry = adv5_axis(uin, o, sj, va);
       }
       const T ures = eddlat * rx + eddlon * ry;
-      uout[o] = ures + (ld(tgrlatda0 + jo) * u0) * v_atupos;
+      const T ut = ures + (ld(tgrlatda0 + jo) * u0) * v_atupos;
+      uout[o] = update ? alpha * ut + u0 : ut;
       // u and v at the v-position (hadvuv.h:197-206)
       const T u_atvpos = scale2<-2>(((um) + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
       const T v_atvpos = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
@@ -327,7 +332,8 @@ struct hadv_kernel {
         ry = adv5_axis(vin, o, sj, va);
       }
       const T vres = eddlat * rx + eddlon * ry;
-      vout[o] = vres - (ld(tgrlatda1 + jo) * u_atvpos) * u_atvpos;
+      const T vt = vres - (ld(tgrlatda1 + jo) * u_atvpos) * u_atvpos;
+      vout[o] = update ? alpha * vt + v0 : vt;
     });
   }
 };
@@ -648,7 +654,7 @@ oeb_status nh_p_grad_entry(const M3* uout, const M3* vout, const M3* uin, const 
 template <class T, int ORDER, class M3, class M1>
 oeb_status hadv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M1* acrlat0,
                       const M1* acrlat1, const M1* tgrlatda0, const M1* tgrlatda1, T eddlat, T eddlon,
-                      const oeb_domain* dom, void* stream) {
+                      const oeb_domain* dom, void* stream, T alpha = T(0), int update = 0) {
   OEB_TRY(check_domain(dom));
   const int h = ORDER == 3 ? 2 : 3;
   Grid<T> gu, gv, gui, gvi;
@@ -674,7 +680,7 @@ oeb_status hadv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* v
     (void)shape;
     return launch<B>(tile_grid((int)dom->nx, (int)dom->ny, (int)dom->nz, TileOf<S>::I, TileOf<S>::J, kb), 0,
                      (cudaStream_t)stream, gu.origin, gv.origin, gui.origin, gvi.origin, a0.origin, a1.origin,
-                     t0.origin, t1.origin, a0.s, eddlat, eddlon, make_dims(*dom, gu), kb);
+                     t0.origin, t1.origin, a0.s, eddlat, eddlon, make_dims(*dom, gu), kb, alpha, update);
   };
   switch (tuned_shape()) {
     case 1: return go(hadv_kernel<T, ORDER, 1>{}, 1);
@@ -710,7 +716,7 @@ oeb_status hadv_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const 
   const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, uin->strides[1], uin->strides[0]};
   const int kb = tuned_kb(kKB);
   OEB_TRY((launch<hadv_kernel<D, ORDER>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, ou, ov, u, v, a0, a1, t0, t1,
-                                         acrlat0->strides[0], D(eddlat), D(eddlon), d, kb)));
+                                         acrlat0->strides[0], D(eddlat), D(eddlon), d, kb, D(0), 0)));
   OEB_TRY(arr.unpack(duout->aligned + duout->offset, ou, *dom, kInterior, d.sj, d.sk));
   return arr.unpack(dvout->aligned + dvout->offset, ov, *dom, kInterior, d.sj, d.sk);
 }
@@ -830,11 +836,15 @@ __device__ __forceinline__ void for_box_points(const uint3& blk, const Dims& d, 
   }
 }
 
+// update != 0 fuses the transpose of the chained step's update: the outputs are alpha * (the
+// gathered gradient), plus the seeds (yu, yv) inside the interior -- the same two roundings as
+// the gradient stored and then combined by a separate kernel.
 template <class T, int ORDER>
 struct hadv_adj_gather_kernel {
   static constexpr int kStepOp = step_op<T>(ORDER == 5 ? kOpHadv5AdjGather : -1);  // the step kernel's id
   static __device__ __forceinline__ void run(const uint3& blk, T* __restrict__ uinb, T* __restrict__ vinb,
-                                             HadvTerms<T> tm, Dims d, int kb) {
+                                             HadvTerms<T> tm, Dims d, int kb, const T* __restrict__ yu,
+                                             const T* __restrict__ yv, T alpha, int update) {
     constexpr int h = ORDER == 3 ? 2 : 3;
     const int64_t sj = d.sj;
     for_box_points(blk, d, h, kb, [&](int64_t o, int a, int b) {
@@ -868,8 +878,15 @@ struct hadv_adj_gather_kernel {
       if (in(a, b)) vb = (vb + tm.by[o]) + tm.ey[o];
       if (in(a, b + 1)) vb = (vb + tm.by[o + sj]) + tm.ey[o + sj];
       if (in(a, b - 1)) vb = vb + tm.ey[o - sj];
-      uinb[o] = ub;
-      vinb[o] = vb;
+      if (update) {
+        const T au = alpha * ub, av = alpha * vb;
+        const bool inside = in(a, b);
+        uinb[o] = inside ? au + yu[o] : au;
+        vinb[o] = inside ? av + yv[o] : av;
+      } else {
+        uinb[o] = ub;
+        vinb[o] = vb;
+      }
     });
   }
 };
@@ -877,7 +894,8 @@ struct hadv_adj_gather_kernel {
 template <class T, int ORDER, class M3, class M1>
 oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M1* acrlat0,
                           const M1* acrlat1, const M1* tgrlatda0, const M1* tgrlatda1, const M3* uoutb,
-                          const M3* voutb, T eddlat, T eddlon, const oeb_domain* dom, void* stream) {
+                          const M3* voutb, T eddlat, T eddlon, const oeb_domain* dom, void* stream,
+                          T alpha = T(0), int update = 0) {
   {
     ValidateOnly guard;
     OEB_TRY((hadv_entry<T, ORDER>(uoutb, voutb, uin, vin, acrlat0, acrlat1, tgrlatda0, tgrlatda1, eddlat, eddlon,
@@ -927,7 +945,8 @@ oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M
   }
   if (stt == OEB_OK)
     stt = launch<hadv_adj_gather_kernel<T, ORDER>>(tile_grid(d.nx + 2 * h, d.ny + 2 * h, d.nz, kTI, kTJ, kb), 0, st,
-                                                   gub.origin, gvb.origin, tm, d, kb);
+                                                   gub.origin, gvb.origin, tm, d, kb, update ? guo.origin : nullptr,
+                                                   update ? gvo.origin : nullptr, alpha, update);
   scratch_free(buf, st);
   return stt;
 }
@@ -1604,5 +1623,26 @@ OEB_POINTWISE_ENTRIES(f64, double)
 OEB_POINTWISE_ENTRIES(f32, float)
 OEB_POINTWISE_DIFF_ENTRIES(f64, double)
 OEB_POINTWISE_DIFF_ENTRIES(f32, float)
+
+// The chained step's fused stages (fused.cuh).
+#define OEB_FUSED_ENTRIES(S, T)                                                                                    \
+  oeb_status oeb::hadvuv5th_update(const OEB_M3(S) * u2, const OEB_M3(S) * v2, const OEB_M3(S) * u1,               \
+                                   const OEB_M3(S) * v1, const OEB_M1(S) * acrlat0, const OEB_M1(S) * acrlat1,     \
+                                   const OEB_M1(S) * tgrlatda0, const OEB_M1(S) * tgrlatda1, T eddlat, T eddlon,   \
+                                   T alpha, const oeb_domain* dom, void* stream) {                                 \
+    return hadv_entry<T, 5>(u2, v2, u1, v1, acrlat0, acrlat1, tgrlatda0, tgrlatda1, eddlat, eddlon, dom, stream,   \
+                            alpha, 1);                                                                             \
+  }                                                                                                                \
+  oeb_status oeb::hadvuv5th_adj_update(const OEB_M3(S) * u1b, const OEB_M3(S) * v1b, const OEB_M3(S) * u1,         \
+                                       const OEB_M3(S) * v1, const OEB_M1(S) * acrlat0, const OEB_M1(S) * acrlat1, \
+                                       const OEB_M1(S) * tgrlatda0, const OEB_M1(S) * tgrlatda1,                   \
+                                       const OEB_M3(S) * u2b, const OEB_M3(S) * v2b, T eddlat, T eddlon, T alpha,  \
+                                       const oeb_domain* dom, void* stream) {                                      \
+    return hadv_adj_entry<T, 5>(u1b, v1b, u1, v1, acrlat0, acrlat1, tgrlatda0, tgrlatda1, u2b, v2b, eddlat, eddlon, \
+                                dom, stream, alpha, 1);                                                            \
+  }
+
+OEB_FUSED_ENTRIES(f64, double)
+OEB_FUSED_ENTRIES(f32, float)
 
 #endif  // OEB_BODIES_ONLY

@@ -223,6 +223,7 @@ struct Recorder {
   std::vector<std::pair<size_t, bool>> live;
   int kb = 0;     // k-levels per CTA for the kernels that take one (0: their default)
   int shape = 0;  // tile shape for the kernels that take one (0: their default; tuned_shape)
+  int fusion = 0;  // fusion grouping of the chained step (tuned_fusion)
 };
 
 Recorder* recorder();             // the calling thread's recorder, or nullptr
@@ -246,6 +247,15 @@ inline int tuned_shape() {
   const Recorder* r = recorder();
   if (r) return r->shape;
   return shape_override();
+}
+
+// Fusion groupings of the chained step, a bit mask (OEB_FUSE_* in oeb_gb300.h): which stages
+// run as one kernel.  The recorder's while recording, else oeb_set_fusion's (0: none).
+int fusion_override();
+inline int tuned_fusion() {
+  const Recorder* r = recorder();
+  if (r) return r->fusion;
+  return fusion_override();
 }
 
 oeb_status scratch_alloc(void** p, size_t bytes, cudaStream_t st);

@@ -18,15 +18,23 @@ def chain(pkg):
     return importlib.import_module("oeb_gb300.chain")
 
 
-def _stand_in(chain, signature, choices):
+def _stand_in(chain, signature, choices, fusion=0):
     class Plan(chain.BatchPlan):
         def __init__(self):
             self._plan = ctypes.c_void_p()
             self.applied = None
+            self._fusion = fusion
 
         @property
         def signature(self):
             return signature
+
+        @property
+        def fusion(self):
+            return self._fusion
+
+        def set_fusion(self, mask):
+            self._fusion = mask
 
         def tuning(self):
             return list(choices)
@@ -58,18 +66,25 @@ def test_abi_rejects_a_null_plan(pkg):
     assert lib.oeb_batch_step_status(None, ctypes.byref(st), None) == 1
     assert lib.oeb_batch_set_wait_limit(None, ctypes.c_uint64(1000)) == 1
     assert lib.oeb_batch_withhold(None, 1) == 1
+    mask = ctypes.c_int()
+    assert lib.oeb_batch_set_fusion(None, 1) == 1
+    assert lib.oeb_batch_get_fusion(None, ctypes.byref(mask)) == 1
+    assert lib.oeb_set_fusion(2) == 12  # OEB_ERR_ARGUMENT: no such grouping
+    assert lib.oeb_set_fusion(0) == 0
 
 
 def test_saved_record_is_applied_to_a_plan_with_the_same_signature(chain, tmp_path):
     choices = [(4, 0, 0), (1, 2, 2), (8, 1, 1), (0, 0, 0)]
-    a = _stand_in(chain, 0x0123456789ABCDEF, choices)
+    a = _stand_in(chain, 0x0123456789ABCDEF, choices, fusion=chain.FUSE_HADV_UPDATE)
     path = tmp_path / "t.json"
     a.save_tuning(path)
     rec = json.loads(path.read_text())
     assert rec == {"format": chain.BatchPlan.TUNING_FORMAT, "signature": "0123456789abcdef",
-                   "choices": [list(c) for c in choices]}
-    b = _stand_in(chain, 0x0123456789ABCDEF, [(0, 0, 0)] * 4)
+                   "fusion": chain.FUSE_HADV_UPDATE, "choices": [list(c) for c in choices]}
+    # the record's fusion grouping is set before its choices are applied
+    b = _stand_in(chain, 0x0123456789ABCDEF, [(0, 0, 0)] * 5)
     b.load_tuning(path)
+    assert b.fusion == chain.FUSE_HADV_UPDATE
     assert b.applied == choices
 
 

@@ -146,7 +146,10 @@ def test_tuning_record_applies_to_a_new_plan(pkg, fields, chain, cuda, tmp_path)
     assert default and all(c == (0, 0, 0) for c in default)
     a.autotune()
     tuned = a.tuning()
-    assert len(tuned) == len(default)
+    # the autotuner may pick the fused grouping (hadvuv5th and the update as one kernel), which
+    # records fewer launches
+    assert a.fusion in (0, chain.FUSE_HADV_UPDATE)
+    assert len(tuned) == len(default) if a.fusion == 0 else len(tuned) < len(default)
     assert all(kb in (1, 2, 4, 8) and shape in (0, 1, 2) and form in (0, 1, 2) for kb, shape, form in tuned)
     path = tmp_path / "tuning.json"
     a.save_tuning(path)
@@ -162,7 +165,8 @@ def test_tuning_record_applies_to_a_new_plan(pkg, fields, chain, cuda, tmp_path)
     torch.cuda.synchronize()
     assert lib.oeb_launch_count() - before == b.launches
     _check(chain, b_members, "tuning record applied")
-    # the default choices as a record put the plan back
+    # the default choices as a record, in the default grouping, put the plan back
+    b.set_fusion(0)
     b.apply_tuning(default)
     assert b.tuning() == default
     _reset(b_members)
