@@ -1026,8 +1026,16 @@ def _e2e(pkg, fields, torch, args, names):
     finally:
         lib.oeb_set_host_async(0)
     pts = len(names) * NX * NY * NZ
+    link = _link_rates(torch)
+    # the step's transfer floor: the input bytes at the one-way rate, or all bytes at the rate
+    # of both directions at once, whichever is longer (the kernels overlap the copies)
+    floor_s = max(h2d / (link["h2d_gbs"] * 1e9), (h2d + d2h) / (link["bidirectional_gbs"] * 1e9))
+    link.update({"floor_ms": round(floor_s * 1e3, 3), "frac_of_floor": round(floor_s / dt, 4),
+                 "how": "pinned host <-> device copies of 256 MB (cudaMemcpyAsync through torch), best of 5; "
+                        "bidirectional: one copy each way on two streams at once"})
     return {"value": round(pts / dt / 1e9, 4), "unit": "GPts/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(dt * 1e3, 3),
+            "link_roofline": link,
             "path": "oeb_<k>_f64_host on pinned host buffers with oeb_set_host_async(1): the ten calls are enqueued on "
                     "one stream, most output fields first, and the step ends with its synchronisation; "
                     "each call stages the k-planes its kernel reads through device memory, and the copy-in of one "
@@ -1038,9 +1046,42 @@ def _e2e(pkg, fields, torch, args, names):
             "synchronous_staged": {"value": round(pts / dt_staged / 1e9, 4), "ms_per_step": round(dt_staged * 1e3, 3),
                                    "path": "the same calls, each returning when its outputs are in host memory, "
                                            "copy-in / compute / copy-out pipelined over k-slabs within the call"},
-            "link_ceiling": "pinned host-to-device copies reach 211 GB/s (189 GB/s beside a device-to-host copy) "
-                            "on this GB300: the step's %d MB of input planes alone take %.1f ms"
-                            % (h2d // 1000000, h2d / 211e9 * 1e3)}
+            }
+
+
+def _link_rates(torch, mb=256, reps=5):
+    """Host <-> device copy rates (GB/s) between pinned host memory and device memory, measured
+    here: one way each, and both ways at once on two streams (their summed bytes)."""
+    n = mb << 20
+    h1 = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    d1 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def best(fn, nbytes):
+        t = []
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            if r:
+                t.append(time.perf_counter() - t0)
+        return nbytes / min(t) / 1e9
+
+    def both():
+        with torch.cuda.stream(s1):
+            d1.copy_(h1, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    res = {"h2d_gbs": round(best(lambda: d1.copy_(h1, non_blocking=True), n), 1),
+           "d2h_gbs": round(best(lambda: h2.copy_(d2, non_blocking=True), n), 1),
+           "bidirectional_gbs": round(best(both, 2 * n), 1)}
+    del h1, h2, d1, d2
+    torch.cuda.empty_cache()
+    return res
 
 
 def _cpu_baseline(pkg, fields, budget_s=15.0, threads=None):

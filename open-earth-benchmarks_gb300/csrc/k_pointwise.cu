@@ -777,9 +777,10 @@ __device__ __forceinline__ T adv_sum(const T* __restrict__ f, int64_t o, int64_t
 template <class T, int ORDER, int SHAPE = 0>
 struct hadv_adj_terms_kernel {
   static constexpr int kStepOp = step_op<T>(ORDER == 5 ? kOpHadv5AdjTerms + SHAPE : -1);  // the step kernel's id
-  // FP64: 80 registers instead of 94, three CTAs per SM instead of two (the hadvuv5th
-  // adjoint 4 % faster; the same bound on the hdiffsmag and fastwavesuv adjoints was slower)
-  static constexpr int kMinCtas = sizeof(T) == 8 ? 3 : 0;
+  // Three CTAs per SM: FP64 80 registers instead of 94 (the hadvuv5th adjoint 4 % faster; the
+  // same bound on the hdiffsmag and fastwavesuv adjoints was slower), FP32 80 instead of 128
+  // (the FP32 hadvuv5th adjoint 0.268 -> 0.229 ms at 256 x 256 x 80, hadvuv 0.258 -> 0.248)
+  static constexpr int kMinCtas = 3;
   static constexpr int kShape = SHAPE;
   static __device__ __forceinline__ void run(const uint3& blk, HadvTerms<T> tm, const T* __restrict__ uin,
                                              const T* __restrict__ vin, const T* __restrict__ acrlat0,
