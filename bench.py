@@ -1290,6 +1290,50 @@ def profile_chain(args):
                       "calls": args.calls}))
 
 
+# A small uneven ensemble for ncu captures of the batched forms (nx, ny, nz, element size):
+# about 0.4 M points a member, 1.2 GB on the device in all.
+PROFILE_MEMBERS = [(96, 64, 40, 8), (64, 80, 60, 4), (128, 48, 40, 8), (48, 112, 60, 4), (80, 80, 40, 8),
+                   (112, 64, 40, 4), (64, 64, 60, 8), (96, 96, 40, 4)]
+
+
+def profile_batch(args):
+    """`--profile-batch`: the chained step forward + adjoint of a small uneven ensemble
+    (PROFILE_MEMBERS) as one run of the per-launch form, then `--calls` runs of the one-launch
+    form (kb 4, `--ctas-per-sm` CTAs an SM), for an ncu capture of the step kernel."""
+    import torch
+    import importlib
+    pkg = graft.load_package()
+    fields = importlib.import_module("oeb_gb300.fields")
+    chain = importlib.import_module("oeb_gb300.chain")
+    dev = torch.device("cuda", 0)
+    H = fields.CHAIN_HALO
+    members = []
+    for idx, (nx, ny, nz, item) in enumerate(PROFILE_MEMBERS):
+        dt = np.float64 if item == 8 else np.float32
+        x = fields.make_chain_inputs_device(nx, ny, nz, 4000 + idx, dev, dt, halo=H)
+        shape = tuple(x["u"].shape)
+        tdt = x["u"].dtype
+        gen = torch.Generator(device=dev).manual_seed(idx)
+        members.append({
+            "fields": {k: pkg.Storage(v, H, nx=nx if v.dim() == 3 else None) for k, v in x.items()},
+            "scalars": fields.make_chain_scalars(4), "domain": (nx, ny, nz),
+            "outs": {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=nx) for n in chain.OUTPUTS},
+            "seeds": {n: pkg.Storage(torch.randn(shape, generator=gen, device=dev, dtype=tdt), H, nx=nx)
+                      for n in chain.OUTPUTS},
+            "grads": {n: pkg.Storage(torch.zeros(shape, dtype=tdt, device=dev), H, nx=nx) for n in ("u", "v")}})
+    plan = chain.BatchPlan(members, chain.FORWARD | chain.ADJOINT)
+    stream = torch.cuda.current_stream(dev)
+    plan.run(stream)
+    plan.set_form(plan.ONE_LAUNCH, 4, args.ctas_per_sm)
+    for _ in range(args.calls):
+        plan.run(stream)
+    torch.cuda.synchronize()
+    status = plan.step_status()
+    plan.close()
+    print(json.dumps({"profile_batch": True, "members": len(members), "calls": args.calls,
+                      "ctas_per_sm": args.ctas_per_sm, "status": list(status)}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1317,6 +1361,9 @@ def main():
                     help="time i-neighbours through L1 against warp shuffles (FP32 probe stencils) and exit")
     ap.add_argument("--profile-chain", action="store_true",
                     help="run the chained step forward + adjoint --calls times at --shape (for ncu captures)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="run a small uneven ensemble's step in the one-launch form --calls times (for ncu captures)")
+    ap.add_argument("--ctas-per-sm", type=int, default=4, help="with --profile-batch: the step kernel build (2, 3, 4)")
     ap.add_argument("--port-vs-reference", action="store_true",
                     help="time the oracle port against the reference build on this host's cores (needs the "
                          "reference source tree) and exit")
@@ -1329,6 +1376,9 @@ def main():
         return
     if args.profile_chain:
         profile_chain(args)
+        return
+    if args.profile_batch:
+        profile_batch(args)
         return
     if args.probe_shuffles:
         probe_shuffles()
