@@ -885,6 +885,13 @@ OEB_API oeb_status oeb_batch_autotune_form(oeb_batch_plan* plan, void* stream, f
 OEB_API oeb_status oeb_batch_step_status(oeb_batch_plan* plan, int* status, int* task);
 OEB_API oeb_status oeb_batch_set_wait_limit(oeb_batch_plan* plan, uint64_t ns);
 OEB_API oeb_status oeb_batch_withhold(oeb_batch_plan* plan, int on);
+/* The one-launch form's ticket order, without a GPU (for tests and tools): for `members`
+ * members with counts[m] tasks each and points[m] grid points, writes for every ticket t
+ * (sum of counts entries) the task's member, its position in the member's sequence, and the
+ * ticket of the task it waits for (its member's previous task; -1 for a member's first).
+ * OEB_ERR_NULL for a NULL array, OEB_ERR_ARGUMENT for members < 1 or a negative count. */
+OEB_API oeb_status oeb_batch_step_order(int members, const int* counts, const int64_t* points, int* member,
+                                        int* position, int* dep);
 
 /* ------------------------------------------------------------------------- */
 /* CUDA graphs of library calls.  oeb_graph_begin starts capturing `stream`   */

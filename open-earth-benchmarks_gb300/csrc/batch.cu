@@ -313,6 +313,33 @@ oeb_status run_slot(oeb_batch_plan* p, const Slot& sl, int ctas, bool per_member
 }
 
 // ---- the one-launch form --------------------------------------------------------------
+// The ticket order of the members' tasks: member m has counts[m] tasks, taken in order; the
+// result lists (member, position) pairs by the fraction of its member's step each task ends
+// ((position + 1/2) / count), larger members (points) first at equal fractions.  Every
+// member's tasks keep their order, so a task's predecessor always holds an earlier ticket.
+std::vector<std::pair<int, int>> step_order(const std::vector<int>& counts, const std::vector<int64_t>& points) {
+  const int nm = (int)counts.size();
+  std::vector<int> by(nm), rank(nm);
+  for (int i = 0; i < nm; ++i) by[i] = i;
+  std::stable_sort(by.begin(), by.end(), [&](int a, int b) { return points[a] > points[b]; });
+  for (int r = 0; r < nm; ++r) rank[by[r]] = r;
+  struct Pending {
+    int member, pos;
+    double key;
+  };
+  std::vector<Pending> all;
+  for (int i = 0; i < nm; ++i)
+    for (int q = 0; q < counts[i]; ++q) all.push_back(Pending{i, q, (q + 0.5) / (double)counts[i]});
+  std::stable_sort(all.begin(), all.end(), [&](const Pending& a, const Pending& b) {
+    if (a.key != b.key) return a.key < b.key;
+    return rank[a.member] < rank[b.member];
+  });
+  std::vector<std::pair<int, int>> out;
+  out.reserve(all.size());
+  for (const Pending& a : all) out.emplace_back(a.member, a.pos);
+  return out;
+}
+
 // Records every member's step with k-blocking kb (the default tile shape) and builds the
 // step kernel's tables: each member's launches, forward then adjoint, become its tasks, each
 // waiting for the member's previous one.  The tasks of all members are merged in the order of
@@ -324,45 +351,33 @@ oeb_status build_one(oeb_batch_plan* p, int kb) {
   std::vector<std::vector<std::vector<LaunchRecord>>> seq;
   OEB_TRY(record_all(p, kb, 0, &seq));
   const int nm = (int)p->members.size();
-  std::vector<int> rank(nm);  // members by points, largest first
-  {
-    std::vector<int> by(nm);
-    for (int i = 0; i < nm; ++i) by[i] = i;
-    auto points = [&](int i) { return p->members[i].dom.nx * p->members[i].dom.ny * p->members[i].dom.nz; };
-    std::stable_sort(by.begin(), by.end(), [&](int a, int b) { return points(a) > points(b); });
-    for (int r = 0; r < nm; ++r) rank[by[r]] = r;
-  }
-  struct Pending {
-    int member, pos;
-    double key;
-    const LaunchRecord* r;
-  };
-  std::vector<Pending> all;
+  std::vector<std::vector<const LaunchRecord*>> lists(nm);  // each member's launches, forward then adjoint
+  std::vector<int> counts(nm);
+  std::vector<int64_t> points(nm);
   size_t smem = 0;
   for (int i = 0; i < nm; ++i) {
-    std::vector<const LaunchRecord*> list;
     for (int mi = 0; mi < 2; ++mi)
       if (p->modes & kModes[mi])
-        for (const LaunchRecord& r : seq[mi][i]) list.push_back(&r);
-    for (size_t q = 0; q < list.size(); ++q) {
-      const LaunchRecord* r = list[q];
+        for (const LaunchRecord& r : seq[mi][i]) lists[i].push_back(&r);
+    for (const LaunchRecord* r : lists[i]) {
       if (r->step_op < 0 || !step_has_op(r->step_op)) return OEB_ERR_UNSUPPORTED;
-      all.push_back(Pending{i, (int)q, (q + 0.5) / (double)list.size(), r});
       smem = std::max(smem, r->smem);
     }
+    counts[i] = (int)lists[i].size();
+    points[i] = (int64_t)p->members[i].dom.nx * p->members[i].dom.ny * p->members[i].dom.nz;
   }
-  if (all.empty()) return OEB_ERR_UNSUPPORTED;
-  std::stable_sort(all.begin(), all.end(), [&](const Pending& a, const Pending& b) {
-    if (a.key != b.key) return a.key < b.key;
-    return rank[a.member] < rank[b.member];
-  });
-  const int ntasks = (int)all.size();
+  const std::vector<std::pair<int, int>> order = step_order(counts, points);
+  if (order.empty()) return OEB_ERR_UNSUPPORTED;
+  const int ntasks = (int)order.size();
   std::vector<StepTask> tasks(ntasks);
   std::vector<int> last(nm, -1);
   std::vector<char> packs;
   int64_t total = 0;
   for (int t = 0; t < ntasks; ++t) {
-    const Pending& a = all[t];
+    struct {
+      int member;
+      const LaunchRecord* r;
+    } a{order[t].first, lists[order[t].first][order[t].second]};
     const dim3 g = a.r->grid;
     const int64_t tiles = (int64_t)g.x * g.y * g.z;
     if (tiles > INT32_MAX || total + tiles > INT32_MAX) return OEB_ERR_TOO_LARGE;
@@ -1046,5 +1061,23 @@ extern "C" oeb_status oeb_batch_set_fusion(oeb_batch_plan* p, int mask) {
 extern "C" oeb_status oeb_batch_get_fusion(const oeb_batch_plan* p, int* mask) {
   if (!p || !mask) return OEB_ERR_NULL;
   *mask = p->fusion;
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_batch_step_order(int members, const int* counts, const int64_t* points, int* member,
+                                           int* position, int* dep) {
+  if (!counts || !points || !member || !position || !dep) return OEB_ERR_NULL;
+  if (members < 1) return OEB_ERR_ARGUMENT;
+  std::vector<int> c(counts, counts + members);
+  for (int v : c)
+    if (v < 0) return OEB_ERR_ARGUMENT;
+  const auto order = oeb::step_order(c, std::vector<int64_t>(points, points + members));
+  std::vector<int> last(members, -1);
+  for (size_t t = 0; t < order.size(); ++t) {
+    member[t] = order[t].first;
+    position[t] = order[t].second;
+    dep[t] = last[order[t].first];
+    last[order[t].first] = (int)t;
+  }
   return OEB_OK;
 }

@@ -102,3 +102,59 @@ def test_record_of_another_ensemble_or_format_is_refused(pkg, chain, tmp_path):
     with pytest.raises(pkg.OebError, match="not a batch tuning record"):
         same.load_tuning(path)
     assert same.applied is None
+
+
+def test_one_launch_ticket_order_keeps_every_member_in_order(pkg):
+    # The step kernel's waits end because a task waits only for its member's previous task,
+    # which always holds an earlier ticket: checked on the plan's own ordering function over
+    # random uneven ensembles, then by playing the tickets through a few CTAs that each wait
+    # only for what earlier tickets complete.
+    import numpy as np
+    lib = pkg.load_library()
+    rng = np.random.default_rng(12)
+    for trial in range(40):
+        m = int(rng.integers(1, 60))
+        counts = rng.integers(0 if trial % 5 == 0 else 1, 40, size=m).astype(np.int32)
+        points = rng.integers(1, 1 << 24, size=m).astype(np.int64)
+        if trial % 7 == 0:
+            points[:] = 1000  # ties everywhere
+        n = int(counts.sum())
+        member = np.full(max(n, 1), -9, np.int32)
+        pos = np.full(max(n, 1), -9, np.int32)
+        dep = np.full(max(n, 1), -9, np.int32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        assert lib.oeb_batch_step_order(ctypes.c_int(m), p(counts), p(points), p(member), p(pos), p(dep)) == 0
+        seen = {}
+        for t in range(n):
+            mb, q = int(member[t]), int(pos[t])
+            assert 0 <= mb < m and q == seen.get(mb, 0), (trial, t, mb, q)  # each member in order
+            seen[mb] = q + 1
+            if q == 0:
+                assert dep[t] == -1
+            else:
+                d = int(dep[t])
+                assert 0 <= d < t and member[d] == mb and pos[d] == q - 1, (trial, t)
+        assert all(seen.get(i, 0) == counts[i] for i in range(m))
+        # a few CTAs take tickets in order; a CTA holding ticket t runs once dep[t] is done
+        done = np.zeros(max(n, 1), bool)
+        ctas = int(rng.integers(1, 9))
+        next_ticket, held = 0, []
+        for _ in range(4 * n + 10):
+            while len(held) < ctas and next_ticket < n:
+                held.append(next_ticket)
+                next_ticket += 1
+            runnable = [t for t in held if dep[t] < 0 or done[dep[t]]]
+            if not runnable:
+                break
+            done[runnable[0]] = True
+            held.remove(runnable[0])
+        assert next_ticket == n and not held, "tickets left waiting: %d of %d" % (n - int(done.sum()), n)
+    # argument checks
+    one = np.ones(1, np.int32)
+    pts = np.ones(1, np.int64)
+    out = np.zeros(1, np.int32)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.oeb_batch_step_order(0, p(one), p(pts), p(out), p(out), p(out)) == 12
+    assert lib.oeb_batch_step_order(1, None, p(pts), p(out), p(out), p(out)) == 1
+    neg = np.full(1, -1, np.int32)
+    assert lib.oeb_batch_step_order(1, p(neg), p(pts), p(out), p(out), p(out)) == 12
