@@ -130,6 +130,12 @@ OEB_API oeb_status oeb_set_tile_shape(int shape);
  * gather and the update's transpose in one kernel.  0 (the default): separate kernels.
  * OEB_ERR_ARGUMENT for other bits.  A tuning knob: results do not depend on it.  Batch plans
  * choose their own grouping (oeb_batch_autotune, oeb_batch_set_fusion). */
+/* 1 (the default): the FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th and fastwavesuv run as
+ * one tiled launch that forms its terms (coefficients) in shared memory; 0: as their
+ * multi-pass form, the terms in scratch.  No counterpart in the reference.  Results do not
+ * depend on it (the same operations on the same operands); OEB_ERR_ARGUMENT for other
+ * values. */
+OEB_API oeb_status oeb_set_adjoint_tiles(int on);
 #define OEB_FUSE_HADV_UPDATE 1
 #define OEB_FUSE_ALL 1
 OEB_API oeb_status oeb_set_fusion(int mask);

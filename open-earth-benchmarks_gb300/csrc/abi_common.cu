@@ -85,6 +85,8 @@ std::atomic<int> g_shape_override{0};
 }  // namespace
 int shape_override() { return g_shape_override.load(std::memory_order_relaxed); }
 std::atomic<int> g_fusion_override{0};
+std::atomic<int> g_adjoint_tiles{1};
+int adjoint_tiles() { return g_adjoint_tiles.load(std::memory_order_relaxed); }
 int fusion_override() { return g_fusion_override.load(std::memory_order_relaxed); }
 
 namespace {
@@ -443,6 +445,12 @@ extern "C" int64_t oeb_memref3d_span_bytes_f32(const oeb_memref3d_f32* m) { retu
 extern "C" oeb_status oeb_set_tile_shape(int shape) {
   if (shape < 0 || shape >= oeb::kShapes) return OEB_ERR_ARGUMENT;
   oeb::g_shape_override.store(shape, std::memory_order_relaxed);
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_set_adjoint_tiles(int on) {
+  if (on != 0 && on != 1) return OEB_ERR_ARGUMENT;
+  oeb::g_adjoint_tiles.store(on, std::memory_order_relaxed);
   return OEB_OK;
 }
 

@@ -408,7 +408,7 @@ oeb_status fastwavesuv_adj_entry(const M3* uinb, const M3* vinb, const M3* utens
   const T ed2 = T(2.0) * edadlat;
   cudaStream_t st = (cudaStream_t)stream;
   const FastwavesAdjState<T> state{gh.origin, gr.origin, lfx.origin, lfx.s, ed2};
-  if constexpr (std::is_same<T, float>::value) {
+  if constexpr (std::is_same<T, float>::value) if (adjoint_tiles()) {
     // one launch: the march forms the coefficients at the kb + 2 levels of its k-block
     const int kb = tuned_kb(kAdjFusedKB);
     return launch<fastwavesuv_adj_kernel<T, 1>>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 2, kT, kT, kb),

@@ -964,7 +964,7 @@ oeb_status hdiffsmag_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, co
   OEB_TRY(check_no_alias({gub.lo, gub.hi, gvb.lo, gvb.hi}, {gui.lo, gui.hi, guo.lo, guo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
-  if constexpr (std::is_same<T, float>::value) {
+  if constexpr (std::is_same<T, float>::value) if (adjoint_tiles()) {
     const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
     const int kb = tuned_kb(kKB);
     auto org1 = [](const M1* m) { return (const float*)m->aligned + m->offset; };

@@ -892,6 +892,128 @@ struct hadv_adj_gather_kernel {
   }
 };
 
+// ---- FP32 hadvuv / hadvuv5th adjoint in one tiled launch ----------------------------
+// A CTA owns a 32 x 32 tile of the gradient box [-h, n+h)^2 and a chunk of k-levels.  At each
+// level it forms, in shared memory, the terms and flags of every interior point its cells
+// gather from -- the tile widened by h on each side -- with the terms pass's expressions
+// (hadv_adj_terms_kernel), then each cell gathers them as hadv_adj_gather_kernel does: the
+// same operations on the same operands in the same order, so the same bits.  The apron
+// recomputes (32 + 2h)^2 / 32^2 - 1 = 41 % more terms (h = 3), and the 37 bytes a point of
+// term scratch are neither written nor read back.
+template <int ORDER>
+struct HadvAdjF32Smem {
+  static constexpr int kH = ORDER == 3 ? 2 : 3;
+  static constexpr int kAW = 32 + 2 * kH;  // term region edge
+  float t[9][kAW][kAW];                     // ax ay bx by dd gx gy ex ey
+  unsigned char fl[kAW][kAW];
+};
+
+template <int ORDER>
+struct hadv_adj_f32 {
+  static constexpr int kStepOp = step_op<float>(ORDER == 5 ? kOpHadv5AdjTiled : -1);  // the step kernel's id
+  static constexpr int kMinCtas = 3;
+  using Smem = HadvAdjF32Smem<ORDER>;
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uinb, float* __restrict__ vinb,
+                                             const float* __restrict__ uin, const float* __restrict__ vin,
+                                             const float* __restrict__ acrlat0, const float* __restrict__ acrlat1,
+                                             const float* __restrict__ tgrlatda0, const float* __restrict__ tgrlatda1,
+                                             int64_t s1d, const float* __restrict__ uoutb,
+                                             const float* __restrict__ voutb, float eddlat, float eddlon, Dims d,
+                                             int kb, float alpha, int update) {
+    using T = float;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    constexpr int h = Smem::kH, W = Smem::kAW;
+    enum { AX, AY, BX, BY, DD, GX, GY, EX, EY };
+    const int64_t sj = d.sj;
+    constexpr T third = T(1.0) / T(3.0);
+    constexpr T rr = earth_radius_recip<T>();
+    const int ci0 = -h + (int)blk.x * 32, cj0 = -h + (int)blk.y * 32;  // the tile's first cell
+    const int pi0 = ci0 - h, pj0 = cj0 - h;                            // its term region's first point
+    const int k0 = (int)blk.z * kb, k1 = min(k0 + kb, d.nz);
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    auto in = [&](int i, int j) { return i >= 0 && i < d.nx && j >= 0 && j < d.ny; };
+#pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const int64_t kofs = (int64_t)k * d.sk;
+      // the terms (hadv_adj_terms_kernel) of the interior points of the region
+      for (int e = tid; e < W * W; e += kThreads) {
+        const int li = e % W, lj = e / W;
+        const int i = pi0 + li, j = pj0 + lj;
+        if (!in(i, j)) continue;
+        const int64_t o = kofs + i + (int64_t)j * sj;
+        const int64_t jo = (int64_t)j * s1d;
+        const T u0 = ld(uin + o), v0 = ld(vin + o);
+        const T um = ld(uin + o - 1) + u0;
+        const T ua = third * (um + ld(uin + o + 1));
+        const T va = T(0.25) * (((ld(vin + o + 1) + ld(vin + o + 1 - sj)) + v0) + ld(vin + o - sj));
+        const T ub = T(0.25) * ((um + ld(uin + o + sj)) + ld(uin + o - 1 + sj));
+        const T vb = third * ((ld(vin + o - sj) + v0) + ld(vin + o + sj));
+        const T a0 = ld(acrlat0 + jo), a1 = ld(acrlat1 + jo), t0 = ld(tgrlatda0 + jo), t1 = ld(tgrlatda1 + jo);
+        const T Ax = a0 * ua, Ay = rr * va, Bx = a1 * ub, By = rr * vb;
+        const bool px = Ax > 0, py = Ay > 0, qx = Bx > 0, qy = By > 0;
+        const T Px = adv_sum<T, ORDER>(uin, o, 1, px), Py = adv_sum<T, ORDER>(uin, o, sj, py);
+        const T Qx = adv_sum<T, ORDER>(vin, o, 1, qx), Qy = adv_sum<T, ORDER>(vin, o, sj, qy);
+        const T yu = ld(uoutb + o), yv = ld(voutb + o);
+        s.t[AX][lj][li] = (eddlat * Ax) * yu;
+        s.t[AY][lj][li] = (eddlon * Ay) * yu;
+        s.t[BX][lj][li] = ((eddlat * Px) * a0) * (third * yu);
+        s.t[BY][lj][li] = ((eddlon * Py) * rr + t0 * u0) * (T(0.25) * yu);
+        s.t[DD][lj][li] = (t0 * va) * yu;
+        s.t[GX][lj][li] = (eddlat * Bx) * yv;
+        s.t[GY][lj][li] = (eddlon * By) * yv;
+        s.t[EX][lj][li] = ((eddlat * Qx) * a1 - (T(2) * t1) * ub) * (T(0.25) * yv);
+        s.t[EY][lj][li] = ((eddlon * Qy) * rr) * (third * yv);
+        s.fl[lj][li] = (unsigned char)((px ? 1 : 0) | (py ? 2 : 0) | (qx ? 4 : 0) | (qy ? 8 : 0));
+      }
+      __syncthreads();
+      // the gather (hadv_adj_gather_kernel) of the tile's cells, four rows a thread
+#pragma unroll 1
+      for (int r = 0; r < 4; ++r) {
+        const int a = ci0 + (int)threadIdx.x, b = cj0 + (int)threadIdx.y + 8 * r;
+        if (a >= d.nx + h || b >= d.ny + h) continue;
+        const int li = a - pi0, lj = b - pj0;
+        auto tm = [&](int q, int di, int dj) { return s.t[q][lj + dj][li + di]; };
+        T ub = T(0), vb = T(0);
+#pragma unroll
+        for (int m = -h; m <= h; ++m) {
+          if (in(a - m, b)) {
+            const unsigned char f = s.fl[lj][li - m];
+            ub = fma(upwind_weight<T, ORDER>(f & 1, m), tm(AX, -m, 0), ub);
+            vb = fma(upwind_weight<T, ORDER>(f & 4, m), tm(GX, -m, 0), vb);
+          }
+          if (in(a, b - m)) {
+            const unsigned char f = s.fl[lj - m][li];
+            ub = fma(upwind_weight<T, ORDER>(f & 2, m), tm(AY, 0, -m), ub);
+            vb = fma(upwind_weight<T, ORDER>(f & 8, m), tm(GY, 0, -m), vb);
+          }
+        }
+        if (in(a - 1, b)) ub = ub + tm(BX, -1, 0);
+        if (in(a, b)) ub = (ub + tm(BX, 0, 0)) + (tm(DD, 0, 0) + tm(EX, 0, 0));
+        if (in(a + 1, b)) ub = (ub + tm(BX, 1, 0)) + tm(EX, 1, 0);
+        if (in(a, b - 1)) ub = ub + tm(EX, 0, -1);
+        if (in(a + 1, b - 1)) ub = ub + tm(EX, 1, -1);
+        if (in(a - 1, b)) vb = vb + tm(BY, -1, 0);
+        if (in(a - 1, b + 1)) vb = vb + tm(BY, -1, 1);
+        if (in(a, b)) vb = (vb + tm(BY, 0, 0)) + tm(EY, 0, 0);
+        if (in(a, b + 1)) vb = (vb + tm(BY, 0, 1)) + tm(EY, 0, 1);
+        if (in(a, b - 1)) vb = vb + tm(EY, 0, -1);
+        const int64_t o = kofs + a + (int64_t)b * sj;
+        if (update) {
+          const T au = alpha * ub, av = alpha * vb;
+          const bool inside = in(a, b);
+          uinb[o] = inside ? au + uoutb[o] : au;
+          vinb[o] = inside ? av + voutb[o] : av;
+        } else {
+          uinb[o] = ub;
+          vinb[o] = vb;
+        }
+      }
+      __syncthreads();  // the next level's terms replace these
+    }
+  }
+};
+
 template <class T, int ORDER, class M3, class M1>
 oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M3* vin, const M1* acrlat0,
                           const M1* acrlat1, const M1* tgrlatda0, const M1* tgrlatda1, const M3* uoutb,
@@ -915,6 +1037,18 @@ oeb_status hadv_adj_entry(const M3* uinb, const M3* vinb, const M3* uin, const M
                          {gui.lo, gui.hi, gvi.lo, gvi.hi, guo.lo, guo.hi, gvo.lo, gvo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
+  if constexpr (std::is_same<T, float>::value) {
+    if (adjoint_tiles()) {  // one tiled launch, no scratch
+      const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, gui.sj, gui.sk};
+      const int kb = tuned_kb(kKB);
+      return launch<hadv_adj_f32<ORDER>>(
+          tile_grid(d.nx + 2 * h, d.ny + 2 * h, d.nz, kTI, kTJ, kb), sizeof(HadvAdjF32Smem<ORDER>), st, gub.origin,
+          gvb.origin, gui.origin, gvi.origin, (const T*)acrlat0->aligned + acrlat0->offset,
+          (const T*)acrlat1->aligned + acrlat1->offset, (const T*)tgrlatda0->aligned + tgrlatda0->offset,
+          (const T*)tgrlatda1->aligned + tgrlatda1->offset, acrlat0->strides[0], guo.origin, gvo.origin, eddlat, eddlon,
+          d, kb, alpha, update);
+    }
+  }
   // scratch: nine term fields and the flags, in uin's layout (terms are read at interior points only)
   const T* start = (uin->allocated && uin->allocated <= uin->aligned) ? uin->allocated : uin->aligned;
   const int64_t last = (uin->sizes[0] - 1) * uin->strides[0] + (uin->sizes[1] - 1) * uin->strides[1] +

@@ -129,6 +129,7 @@ enum StepOpBase : int {
   kOpFvAdjQij,
   kOpFvAdjF2,
   kOpFvAdjQ,
+  kOpHadv5AdjTiled,  // hadv_adj_f32<5>: the FP32 advection adjoint in one tiled launch
   kStepOpBases
 };
 template <class T>
@@ -230,6 +231,9 @@ Recorder* recorder();             // the calling thread's recorder, or nullptr
 void set_recorder(Recorder* r);  // installs (or with nullptr removes) it
 // k-levels per CTA set by oeb_set_kblock (0: none).
 int kb_override();
+// Whether the FP32 adjoints that have a tiled one-launch form use it (oeb_set_adjoint_tiles;
+// default 1).
+int adjoint_tiles();
 // k-levels per CTA: the recorder's choice while recording, else oeb_set_kblock's, else `def`.
 inline int tuned_kb(int def) {
   const Recorder* r = recorder();

@@ -60,7 +60,8 @@ namespace OEB_STEP_CAT(step_c, OEB_STEP_MIN_CTAS) {
 template <class... B>
 struct OpList {};
 
-// Every body the chained step records, in both precisions (FP64 runs as F64i).
+// Every body the chained step records, in both precisions (FP64 runs as F64i), with the FP32
+// adjoints in either form (oeb_set_adjoint_tiles).
 using StepBodies = OpList<
     step_ch::combine_kernel<F64i>, step_ch::combine_kernel<float>,
     step_fws::fastwavesuv_kernel<F64i>, step_fws::fastwavesuv_kernel<float>,
@@ -75,6 +76,9 @@ using StepBodies = OpList<
     step_hd::hdiffsmag_kernel<F64i>, step_hd::hdiffsmag_kernel<float>,
     step_hd::hdiffsmag_adj_terms_kernel<F64i>, step_hd::hdiffsmag_adj_ts_kernel<F64i>,
     step_hd::hdiffsmag_adj_gather_kernel<F64i>, step_hd::hdiffsmag_adj_f32,
+    step_hd::hdiffsmag_adj_terms_kernel<float>, step_hd::hdiffsmag_adj_ts_kernel<float>,
+    step_hd::hdiffsmag_adj_gather_kernel<float>, step_pw::hadv_adj_f32<5>,
+    step_fws::fastwavesuv_adj_terms_kernel<float>, step_fws::fastwavesuv_adj_kernel<float, 0>,
     step_fv::fvtp2d_q_kernel<F64i>, step_fv::fvtp2d_q_kernel<float>, step_fv::fvtp2d_flux_kernel<F64i>,
     step_fv::fvtp2d_fused_kernel<float>, step_fv::fvtp2d_adj_qij_kernel<F64i>,
     step_fv::fvtp2d_adj_qij_kernel<float>, step_fv::fvtp2d_adj_f2_kernel<F64i>,

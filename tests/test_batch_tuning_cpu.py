@@ -71,6 +71,8 @@ def test_abi_rejects_a_null_plan(pkg):
     assert lib.oeb_batch_get_fusion(None, ctypes.byref(mask)) == 1
     assert lib.oeb_set_fusion(2) == 12  # OEB_ERR_ARGUMENT: no such grouping
     assert lib.oeb_set_fusion(0) == 0
+    assert lib.oeb_set_adjoint_tiles(2) == 12  # OEB_ERR_ARGUMENT: 0 or 1
+    assert lib.oeb_set_adjoint_tiles(1) == 0
 
 
 def test_saved_record_is_applied_to_a_plan_with_the_same_signature(chain, tmp_path):
