@@ -40,6 +40,13 @@ SCALARS = ("edadlat", "dt", "eddlat", "eddlon", "dt_adv", "tau_smag", "weight_sm
 OUTPUTS = ("uout", "vout", "fx1", "fy1")
 
 
+def set_fusion(mask: int) -> None:
+    """The fusion grouping of every later single chained step (oeb_set_fusion): 0 (the
+    default) runs each stage as its own kernels, FUSE_HADV_UPDATE runs hadvuv5th and the
+    explicit update as one kernel.  Results do not depend on it."""
+    check(entry("oeb_set_fusion")(ctypes.c_int(mask)), "oeb_set_fusion")
+
+
 class ChainFields(ctypes.Structure):
     """oeb_chain_fields_{f64,f32}: one descriptor pointer per input, in ORDER."""
     _fields_ = [(n, ctypes.POINTER(Memref1d if n in RANK1 else Memref3d)) for n in ORDER]

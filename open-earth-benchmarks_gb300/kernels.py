@@ -24,7 +24,7 @@ from typing import Dict, Optional, Sequence
 
 import numpy as np
 
-from .abi import check, entry
+from .abi import check, entry, load_library
 from .specs import ACTIVE, DRIVER_SCALARS, KERNELS
 from .storage import Domain, Storage
 
@@ -50,6 +50,14 @@ def _stream_handle(stream, on_device: bool) -> int:
     if hasattr(stream, "cuda_stream"):
         return stream.cuda_stream
     return int(stream)
+
+
+def set_adjoint_tiles(on: bool) -> None:
+    """FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th and fastwavesuv as one tiled launch
+    (True, the default) or in their multi-pass forms (oeb_set_adjoint_tiles); the same bits
+    either way."""
+    lib = load_library()
+    check(lib.oeb_set_adjoint_tiles(ctypes.c_int(1 if on else 0)), "oeb_set_adjoint_tiles")
 
 
 def entry_name(kernel: str, precision: str, on_device: bool) -> str:
