@@ -127,9 +127,10 @@ OEB_API oeb_status oeb_set_tile_shape(int shape);
  * step): a bit mask of stages that run as one kernel in every later oeb_chain_* call.
  * OEB_FUSE_HADV_UPDATE: hadvuv5th and the explicit update u2 = u1 + dt_adv * tendency in one
  * kernel (the advection writes u2, v2 directly), and in the adjoint step the hadvuv5th
- * gather and the update's transpose in one kernel.  0 (the default): separate kernels.
- * OEB_ERR_ARGUMENT for other bits.  A tuning knob: results do not depend on it.  Batch plans
- * choose their own grouping (oeb_batch_autotune, oeb_batch_set_fusion). */
+ * gather and the update's transpose in one kernel; the default (faster in both precisions).
+ * 0: separate kernels.  OEB_ERR_ARGUMENT for other bits.  A tuning knob: results do not
+ * depend on it.  Batch plans choose their own grouping (created with 0; oeb_batch_autotune,
+ * oeb_batch_set_fusion). */
 /* 1 (the default): the FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th and fastwavesuv run as
  * one tiled launch that forms its terms (coefficients) in shared memory; 0: as their
  * multi-pass form, the terms in scratch.  No counterpart in the reference.  Results do not

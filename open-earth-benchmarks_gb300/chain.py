@@ -41,9 +41,9 @@ OUTPUTS = ("uout", "vout", "fx1", "fy1")
 
 
 def set_fusion(mask: int) -> None:
-    """The fusion grouping of every later single chained step (oeb_set_fusion): 0 (the
-    default) runs each stage as its own kernels, FUSE_HADV_UPDATE runs hadvuv5th and the
-    explicit update as one kernel.  Results do not depend on it."""
+    """The fusion grouping of every later single chained step (oeb_set_fusion):
+    FUSE_HADV_UPDATE (the default) runs hadvuv5th and the explicit update as one kernel, 0 runs
+    each stage as its own kernels.  Results do not depend on it."""
     check(entry("oeb_set_fusion")(ctypes.c_int(mask)), "oeb_set_fusion")
 
 

@@ -84,7 +84,7 @@ namespace {
 std::atomic<int> g_shape_override{0};
 }  // namespace
 int shape_override() { return g_shape_override.load(std::memory_order_relaxed); }
-std::atomic<int> g_fusion_override{0};
+std::atomic<int> g_fusion_override{OEB_FUSE_HADV_UPDATE};  // oeb_set_fusion
 std::atomic<int> g_adjoint_tiles{1};
 int adjoint_tiles() { return g_adjoint_tiles.load(std::memory_order_relaxed); }
 int fusion_override() { return g_fusion_override.load(std::memory_order_relaxed); }

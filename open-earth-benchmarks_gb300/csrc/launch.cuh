@@ -254,7 +254,8 @@ inline int tuned_shape() {
 }
 
 // Fusion groupings of the chained step, a bit mask (OEB_FUSE_* in oeb_gb300.h): which stages
-// run as one kernel.  The recorder's while recording, else oeb_set_fusion's (0: none).
+// run as one kernel.  The recorder's while recording (a batch plan's grouping), else
+// oeb_set_fusion's (OEB_FUSE_HADV_UPDATE by default).
 int fusion_override();
 inline int tuned_fusion() {
   const Recorder* r = recorder();

@@ -53,7 +53,7 @@ def test_fused_step_matches_unfused(pkg, fields, chain, cuda, size, dtype):
             l2 = lib.oeb_launch_count()
             runs[mask] = (fwd, adj, l1 - l0, l2 - l1)
     finally:
-        _set_fusion(pkg, 0)
+        _set_fusion(pkg, chain.FUSE_HADV_UPDATE)  # the default
     (f0, a0, lf0, la0), (f1, a1, lf1, la1) = runs[0], runs[chain.FUSE_HADV_UPDATE]
     for n in chain.OUTPUTS:
         assert_bitwise_equal(f1[n], f0[n], "fused forward %s" % n)
