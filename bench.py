@@ -538,6 +538,8 @@ def run_ours(args):
                      "fp64_pipe_roof": _fp64_pipe_roofline(names, iso_ms, dom_k, ms_step, clock_summary,
                                                            torch.cuda.get_device_properties(dev).multi_processor_count,
                                                            add_rate, add_rate_clocks),
+                     "fp64_op_rates": _fp64_op_rates(pkg, torch.cuda.get_device_properties(dev).multi_processor_count,
+                                                     (add_rate_clocks or {}).get("sm_mhz")),
                      "note": "the FP64 stencils are compute-bound, not HBM-bound: GB300 issues 1.6 FP64 "
                              "op/clk/SM, so the kernels run as F64i (exact integer-pipe multiply, divide, "
                              "sqrt, compare beside FP64-pipe adds); the pipe figures are ncu's "
@@ -901,6 +903,23 @@ def _fp64_add_rate(pkg, gpu_index):
     with ClockSampler(gpu_index) as clocks:
         st = lib.oeb_probe_fp64_add_rate(ctypes.byref(rate), ctypes.byref(adds))
     return (rate.value if st == 0 else None), clocks.summary()
+
+
+def _fp64_op_rates(pkg, sms, probe_mhz):
+    """Each FP64 operation's rate on this GPU (oeb_probe_fp64_rate), in G operations a
+    second and per clock per SM (at the SM clock sampled during the addition probe)."""
+    import ctypes
+    lib = pkg.load_library()
+    out = {}
+    for op, name in enumerate(("add", "mul", "fma", "div", "sqrt")):
+        r = ctypes.c_double(0.0)
+        if lib.oeb_probe_fp64_rate(ctypes.c_int(op), ctypes.byref(r), None) != 0:
+            return None
+        out[name] = {"gops": round(r.value / 1e9, 2),
+                     "per_clk_per_sm": round(r.value / (sms * probe_mhz * 1e6), 3) if probe_mhz else None}
+    out["how"] = ("oeb_probe_fp64_rate: 8 independent chains of the operation a thread, 8 CTAs of 256 threads an "
+                  "SM, the best of 3 timed launches; div and sqrt are the compiler's IEEE-rounded sequences")
+    return out
 
 
 def _fp64_pipe_roofline(names, per_kernel, dom_k, ms_step, clocks_summary, sms, add_rate, rate_clocks):

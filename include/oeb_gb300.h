@@ -176,6 +176,11 @@ OEB_API oeb_status oeb_selftest_fp64(int op, int64_t pairs, uint64_t seed, int m
  * after a warm-up.  `adds_per_launch` (may be NULL) receives the additions of one launch.
  * Synchronous, on the legacy default stream. */
 OEB_API oeb_status oeb_probe_fp64_add_rate(double* adds_per_second, double* adds_per_launch);
+/* The rate of one FP64 operation on this GPU, measured the same way (no counterpart in the
+ * reference): op 0 addition, 1 multiplication, 2 fused multiply-add, 3 division, 4 square
+ * root (3 and 4: the compiler's IEEE-rounded instruction sequences), in operations a second,
+ * and the operations one timed launch performs.  OEB_ERR_ARGUMENT for another op. */
+OEB_API oeb_status oeb_probe_fp64_rate(int op, double* ops_per_second, double* ops_per_launch);
 /* No counterpart in the reference (a measurement behind the stencils' design): i-neighbours
  * read through L1 against warp shuffles, FP32, on a 256 x 256 x 80 interior with a 3-cell
  * halo.  us[0..3] receive the average launch time (microseconds; the best of three runs of 60

@@ -114,6 +114,32 @@ __global__ void fp64_add_rate_kernel(int iters, double step, double* sink) {
   if (t == -1.0) sink[blockIdx.x] = t;  // never true for these operands
 }
 
+// The same for each FP64 operation the stencils use (oeb_probe_fp64_rate): OP 0 addition, 1
+// multiplication, 2 fused multiply-add, 3 division, 4 square root (the division and the square
+// root are the compiler's instruction sequences).  The operands keep every chain finite and
+// normal.
+template <int OP>
+__global__ void fp64_op_rate_kernel(int iters, double step, double* sink) {
+  double x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) x[c] = 1.0 + 0.125 * (double)(threadIdx.x + c);
+#pragma unroll 1
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) {
+      if (OP == 0) x[c] = __dadd_rn(x[c], step);
+      if (OP == 1) x[c] = __dmul_rn(x[c], 1.0 + step);
+      if (OP == 2) x[c] = __fma_rn(x[c], 1.0 - step, step);
+      if (OP == 3) x[c] = __ddiv_rn(x[c], 1.0 + step);
+      if (OP == 4) x[c] = __dsqrt_rn(x[c] + 1.0);
+    }
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) t = __dadd_rn(t, x[c]);
+  if (t == -1.0) sink[blockIdx.x] = t;  // never true for these operands
+}
+
 // ---- i-neighbours through L1 or through warp shuffles (oeb_probe_shuffle_neighbours) --
 // FP32 fields of a 256 x 256 x 80 interior with a 3-cell halo, one CTA of 32 x 8 threads a
 // 32 x 32 tile and k-level, four rows a thread.
@@ -280,6 +306,42 @@ extern "C" oeb_status oeb_probe_fp64_add_rate(double* adds_per_second, double* a
   const double adds = (double)ctas * threads * iters * oeb::kChains;
   *adds_per_second = best > 0.f ? adds / (best * 1e-3) : 0.0;
   if (adds_per_launch) *adds_per_launch = adds;
+  return OEB_OK;
+}
+
+extern "C" oeb_status oeb_probe_fp64_rate(int op, double* ops_per_second, double* ops_per_launch) {
+  if (!ops_per_second) return OEB_ERR_NULL;
+  if (op < 0 || op > 4) return OEB_ERR_ARGUMENT;
+  using Kern = void (*)(int, double, double*);
+  const Kern kerns[5] = {oeb::fp64_op_rate_kernel<0>, oeb::fp64_op_rate_kernel<1>, oeb::fp64_op_rate_kernel<2>,
+                         oeb::fp64_op_rate_kernel<3>, oeb::fp64_op_rate_kernel<4>};
+  int dev = 0, sms = 1;
+  OEB_CUDA_TRY(cudaGetDevice(&dev));
+  OEB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // the division and the square root are sequences of several instructions: fewer iterations
+  const int ctas = sms * 8, threads = 256, iters = op >= 3 ? 1 << 11 : 1 << 14;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  OEB_CUDA_TRY(cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // the first launch is the warm-up
+    cudaEventRecord(e0, 0);
+    kerns[op]<<<ctas, threads>>>(iters, 1.0 / 1024.0, nullptr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    oeb::count_launches(1);
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return oeb::cuda_fail(e);
+  const double ops = (double)ctas * threads * iters * oeb::kChains;
+  *ops_per_second = best > 0.f ? ops / (best * 1e-3) : 0.0;
+  if (ops_per_launch) *ops_per_launch = ops;
   return OEB_OK;
 }
 

@@ -59,6 +59,24 @@ def test_fp64_add_rate_probe(pkg, cuda):
     assert lib.oeb_probe_fp64_add_rate(None, None) != 0
 
 
+def test_fp64_op_rate_probe(pkg, cuda):
+    # the FP64 rate of each operation the stencils use; the addition agrees with the addition
+    # probe, and the division and square root (instruction sequences) are slower
+    lib = pkg.load_library()
+    rates = []
+    for op in range(5):
+        r, n = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        assert lib.oeb_probe_fp64_rate(ctypes.c_int(op), ctypes.byref(r), ctypes.byref(n)) == 0
+        assert r.value > 1e9 and n.value > 1e8, (op, r.value, n.value)
+        rates.append(r.value)
+    add = ctypes.c_double(0.0)
+    assert lib.oeb_probe_fp64_add_rate(ctypes.byref(add), None) == 0
+    assert 0.75 <= rates[0] / add.value <= 1.33, (rates[0], add.value)
+    assert rates[3] < rates[0] and rates[4] < rates[0], rates
+    assert lib.oeb_probe_fp64_rate(ctypes.c_int(5), ctypes.byref(add), None) == 12
+    assert lib.oeb_probe_fp64_rate(ctypes.c_int(0), None, None) == 1
+
+
 def test_probe_shuffle_neighbours(pkg, cuda):
     # both forms of each probe stencil give the same bits; the four launch times are measured
     lib = pkg.load_library()
