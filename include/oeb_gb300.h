@@ -131,9 +131,9 @@ OEB_API oeb_status oeb_set_tile_shape(int shape);
  * 0: separate kernels.  OEB_ERR_ARGUMENT for other bits.  A tuning knob: results do not
  * depend on it.  Batch plans choose their own grouping (created with 0; oeb_batch_autotune,
  * oeb_batch_set_fusion). */
-/* 1 (the default): the FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th and fastwavesuv run as
- * one tiled launch that forms its terms (coefficients) in shared memory; 0: as their
- * multi-pass form, the terms in scratch.  No counterpart in the reference.  Results do not
+/* 1 (the default): the FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th, fastwavesuv, p_grad_c
+ * and nh_p_grad run as one tiled launch that forms its terms (coefficients) in shared memory;
+ * 0: as their multi-pass form, the terms in scratch.  No counterpart in the reference.  Results do not
  * depend on it (the same operations on the same operands); OEB_ERR_ARGUMENT for other
  * values. */
 OEB_API oeb_status oeb_set_adjoint_tiles(int on);

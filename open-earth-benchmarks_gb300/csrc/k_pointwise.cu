@@ -1267,20 +1267,32 @@ struct PgcTerms {
   T* t[10];  // per axis (u: 0-4, v: 5-9): sb, fb B1, fb B2, fb A1, fb A2
 };
 
+// The five terms of point o along the axis of stride s (both forms of the adjoint use these
+// expressions).
 template <class T>
-__device__ __forceinline__ void pgc_adj_axis(T* const* t, const T* __restrict__ gz, const T* __restrict__ pkc,
-                                             const T* __restrict__ delpc, int64_t o, int64_t s, int64_t sk, T gz0,
-                                             T gz1, T pk0, T pk1, T wk, T coef, T y) {
+__device__ __forceinline__ void pgc_adj_terms(T (&t)[5], const T* __restrict__ gz, const T* __restrict__ pkc,
+                                              const T* __restrict__ delpc, int64_t o, int64_t s, int64_t sk, T gz0,
+                                              T gz1, T pk0, T pk1, T wk, T coef, T y) {
   const T A1 = ld(gz + o - s + sk) - gz0, B1 = pk1 - ld(pkc + o - s);
   const T A2 = ld(gz + o - s) - gz1, B2 = ld(pkc + o - s + sk) - pk0;
   const T f = A1 * B1 + A2 * B2;
   const T r = T(1) / (ld(delpc + o - s) + wk);
   const T fb = (y * coef) * r;
-  t[0][o] = -(fb * f) * r;
-  t[1][o] = fb * B1;
-  t[2][o] = fb * B2;
-  t[3][o] = fb * A1;
-  t[4][o] = fb * A2;
+  t[0] = -(fb * f) * r;
+  t[1] = fb * B1;
+  t[2] = fb * B2;
+  t[3] = fb * A1;
+  t[4] = fb * A2;
+}
+
+template <class T>
+__device__ __forceinline__ void pgc_adj_axis(T* const* t, const T* __restrict__ gz, const T* __restrict__ pkc,
+                                             const T* __restrict__ delpc, int64_t o, int64_t s, int64_t sk, T gz0,
+                                             T gz1, T pk0, T pk1, T wk, T coef, T y) {
+  T v[5];
+  pgc_adj_terms(v, gz, pkc, delpc, o, s, sk, gz0, gz1, pk0, pk1, wk, coef, y);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) t[q][o] = v[q];
 }
 
 template <class T>
@@ -1345,6 +1357,115 @@ struct p_grad_c_adj_gather_kernel {
   }
 };
 
+// ---- FP32 p_grad_c adjoint in one tiled launch -----------------------------------------
+// A CTA owns a 32 x 16 tile of the gather box [-1, N)^2 and a chunk of its levels [0, Nz], and
+// marches k.  At each level it forms the terms (pgc_adj_terms, as the terms pass) of the
+// interior points its cells read -- for the x axis the tile and one more column, for the y
+// axis the tile and one more row -- into a two-level ring in shared memory, and its cells
+// gather the terms of levels k and k-1 in the gather pass's order: the same bits as the two
+// passes, without the 40 bytes a point of term scratch.  A chunk first forms the level below
+// its first one.
+constexpr int kPgcTJ = 16;  // rows of a tile
+struct PgcAdjF32Smem {
+  float tx[2][5][kPgcTJ][33];      // x-axis terms: rows cj0 .., columns ci0 .. ci0 + 32
+  float ty[2][5][kPgcTJ + 1][32];  // y-axis terms: rows cj0 .. cj0 + 16, columns ci0 ..
+};
+
+struct p_grad_c_adj_f32 {
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uinb, float* __restrict__ vinb,
+                                             float* __restrict__ delpcb, float* __restrict__ gzb,
+                                             float* __restrict__ pkcb, const float* __restrict__ rdxc,
+                                             const float* __restrict__ rdyc, const float* __restrict__ delpc,
+                                             const float* __restrict__ gz, const float* __restrict__ pkc,
+                                             const float* __restrict__ uoutb, const float* __restrict__ voutb,
+                                             float dt2, Dims d, int kb) {
+    using T = float;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PgcAdjF32Smem& s = *reinterpret_cast<PgcAdjF32Smem*>(smem_raw);
+    const int64_t sj = d.sj, sk = d.sk;
+    const int ci0 = -1 + (int)blk.x * 32, cj0 = -1 + (int)blk.y * kPgcTJ;  // the tile's first cell
+    const int kz0 = (int)blk.z * kb, kz1 = min(kz0 + kb, d.nz + 1);       // its levels of [0, nz]
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    // the terms of level k into ring slot k & 1, and (own = true) uinb, vinb of the points this
+    // tile owns
+    auto terms = [&](int k, bool own) {
+      const int slot = k & 1;
+      const int64_t kofs = (int64_t)k * sk;
+      for (int e = tid; e < 33 * (kPgcTJ + 1); e += kThreads) {
+        const int a = e % 33, b = e / 33;
+        const int i = ci0 + a, j = cj0 + b;
+        const bool xs = b < kPgcTJ, ys = a < 32;  // in the x-axis / y-axis region
+        if (!(xs || ys) || !inside(d, i, j, k)) continue;
+        const int64_t o = kofs + i + (int64_t)j * sj;
+        const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
+        const T wk = ld(delpc + o);
+        const T yu = ld(uoutb + o), yv = ld(voutb + o);
+        if (own && xs && ys) {  // the tile's own cells
+          uinb[o] = yu;
+          vinb[o] = yv;
+        }
+        T v[5];
+        if (xs) {
+          pgc_adj_terms(v, gz, pkc, delpc, o, 1, sk, gz0, gz1, pk0, pk1, wk, dt2 * ld(rdxc + o), yu);
+#pragma unroll
+          for (int q = 0; q < 5; ++q) s.tx[slot][q][b][a] = v[q];
+        }
+        if (ys) {
+          pgc_adj_terms(v, gz, pkc, delpc, o, sj, sk, gz0, gz1, pk0, pk1, wk, dt2 * ld(rdyc + o), yv);
+#pragma unroll
+          for (int q = 0; q < 5; ++q) s.ty[slot][q][b][a] = v[q];
+        }
+      }
+    };
+    if (kz0 >= 1) terms(kz0 - 1, false);  // the level below the chunk's first (its cells read it)
+#pragma unroll 1
+    for (int k = kz0; k < kz1; ++k) {
+      if (k < d.nz) terms(k, true);
+      __syncthreads();
+      const int cur = k & 1, prev = (k - 1) & 1;
+      const int64_t kofs = (int64_t)k * sk;
+#pragma unroll
+      for (int r = 0; r < kPgcTJ / kTY; ++r) {
+        const int a = threadIdx.x, b = threadIdx.y + kTY * r;
+        const int i = ci0 + a, j = cj0 + b;
+        if (i >= d.nx || j >= d.ny) continue;  // the gather box is [-1, N)^2
+        T db = T(0), gb = T(0), pb = T(0);
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+          const int di = ax == 0 ? 1 : 0, dj = 1 - di;
+          // term q of axis ax at the point (i + ei, j + ej) of level slot sl
+          auto t = [&](int sl, int q, int ei, int ej) {
+            return ax == 0 ? s.tx[sl][q][b + ej][a + ei] : s.ty[sl][q][b + ej][a + ei];
+          };
+          if (inside(d, i, j, k)) {  // p = c
+            db = db + t(cur, 0, 0, 0);
+            gb = gb - t(cur, 1, 0, 0);
+            pb = pb - t(cur, 4, 0, 0);
+          }
+          if (inside(d, i + di, j + dj, k)) {  // p = c + s
+            db = db + t(cur, 0, di, dj);
+            gb = gb + t(cur, 2, di, dj);
+            pb = pb - t(cur, 3, di, dj);
+          }
+          if (inside(d, i, j, k - 1)) {  // p = c - k
+            gb = gb - t(prev, 2, 0, 0);
+            pb = pb + t(prev, 3, 0, 0);
+          }
+          if (inside(d, i + di, j + dj, k - 1)) {  // p = c + s - k
+            gb = gb + t(prev, 1, di, dj);
+            pb = pb + t(prev, 4, di, dj);
+          }
+        }
+        const int64_t o = kofs + i + (int64_t)j * sj;
+        if (k < d.nz) delpcb[o] = db;
+        gzb[o] = gb;
+        pkcb[o] = pb;
+      }
+      __syncthreads();  // level k + 1's terms replace level k - 1's
+    }
+  }
+};
+
 template <class T, class M3>
 oeb_status p_grad_c_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M3* rdxc,
                              const M3* rdyc, const M3* delpc, const M3* gz, const M3* pkc, const M3* duin,
@@ -1405,6 +1526,17 @@ oeb_status p_grad_c_adj_entry(const M3* uinb, const M3* vinb, const M3* delpcb, 
                           guo.hi, gvo.lo, gvo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
+  if constexpr (std::is_same<T, float>::value) {
+    if (adjoint_tiles()) {  // one tiled launch, no scratch
+      const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, guo.sj, guo.sk};
+      const int tiles = ((d.nx + 1 + 31) / 32) * ((d.ny + 1 + kPgcTJ - 1) / kPgcTJ);
+      const int kb = tuned_kb(staged_kb(tiles, d.nz + 1, 4));
+      return launch<p_grad_c_adj_f32>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 1, 32, kPgcTJ, kb),
+                                      sizeof(PgcAdjF32Smem), st, gub.origin, gvb.origin, gdb.origin, ggb.origin,
+                                      gpb.origin, grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin,
+                                      guo.origin, gvo.origin, dt2, d, kb);
+    }
+  }
   const TermLayout lay = term_layout(uoutb);
   void* buf = nullptr;
   OEB_TRY(scratch_alloc(&buf, (size_t)lay.n * 10 * sizeof(T), st));
@@ -1441,11 +1573,13 @@ struct NhpTerms {
   T* t[14];  // per axis (u: 0-6, v: 7-13): a1, a2, c1, c2, e1, e2, wb
 };
 
+// The seven terms of point o along the axis of stride s (both forms of the adjoint use these
+// expressions).
 template <class T>
-__device__ __forceinline__ void nhp_adj_axis(T* const* t, const T* __restrict__ gz, const T* __restrict__ pp,
-                                             const T* __restrict__ pk3, const T* __restrict__ wk1, int64_t o,
-                                             int64_t s, int64_t sk, T gz0, T gz1, T pk0, T pk1, T pp0, T pp1, T w1,
-                                             T dt, T U) {
+__device__ __forceinline__ void nhp_adj_terms(T (&t)[7], const T* __restrict__ gz, const T* __restrict__ pp,
+                                              const T* __restrict__ pk3, const T* __restrict__ wk1, int64_t o,
+                                              int64_t s, int64_t sk, T gz0, T gz1, T pk0, T pk1, T pp0, T pp1, T w1,
+                                              T dt, T U) {
   const T gx0 = ld(gz + o + s), gx1 = ld(gz + o + s + sk);
   const T pkx0 = ld(pk3 + o + s), pkx1 = ld(pk3 + o + s + sk);
   const T ppx0 = ld(pp + o + s), ppx1 = ld(pp + o + s + sk);
@@ -1458,13 +1592,24 @@ __device__ __forceinline__ void nhp_adj_axis(T* const* t, const T* __restrict__ 
   const T Ud = U * dt;
   const T fkb = Ud * rs, fpb = Ud * rw;
   const T sb = -(fkb * fk) * rs;
-  t[0][o] = fkb * B1 + fpb * P1;
-  t[1][o] = fkb * B2 + fpb * P2;
-  t[2][o] = fkb * A1 + sb;
-  t[3][o] = fkb * A2 + sb;
-  t[4][o] = fpb * A1;
-  t[5][o] = fpb * A2;
-  t[6][o] = -(fpb * fp) * rw;
+  t[0] = fkb * B1 + fpb * P1;
+  t[1] = fkb * B2 + fpb * P2;
+  t[2] = fkb * A1 + sb;
+  t[3] = fkb * A2 + sb;
+  t[4] = fpb * A1;
+  t[5] = fpb * A2;
+  t[6] = -(fpb * fp) * rw;
+}
+
+template <class T>
+__device__ __forceinline__ void nhp_adj_axis(T* const* t, const T* __restrict__ gz, const T* __restrict__ pp,
+                                             const T* __restrict__ pk3, const T* __restrict__ wk1, int64_t o,
+                                             int64_t s, int64_t sk, T gz0, T gz1, T pk0, T pk1, T pp0, T pp1, T w1,
+                                             T dt, T U) {
+  T v[7];
+  nhp_adj_terms(v, gz, pp, pk3, wk1, o, s, sk, gz0, gz1, pk0, pk1, pp0, pp1, w1, dt, U);
+#pragma unroll
+  for (int q = 0; q < 7; ++q) t[q][o] = v[q];
 }
 
 template <class T>
@@ -1535,6 +1680,115 @@ struct nh_p_grad_adj_gather_kernel {
   }
 };
 
+// ---- FP32 nh_p_grad adjoint in one tiled launch ------------------------------------------
+// As p_grad_c_adj_f32: a CTA owns a 32 x 16 tile of the gather box [0, N]^2 and a chunk of its
+// levels [0, Nz], and marches k with the terms (nhp_adj_terms) of levels k and k-1 in a
+// two-level shared-memory ring; here a cell reads the points c and c - s, so the x-axis terms
+// cover the tile and one more column on its left, the y-axis terms one more row below.
+struct NhpAdjF32Smem {
+  float tx[2][7][kPgcTJ][33];      // x-axis terms: rows cj0 .., columns ci0 - 1 .. ci0 + 31
+  float ty[2][7][kPgcTJ + 1][32];  // y-axis terms: rows cj0 - 1 .. cj0 + 15, columns ci0 ..
+};
+
+struct nh_p_grad_adj_f32 {
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uinb, float* __restrict__ vinb,
+                                             float* __restrict__ gzb, float* __restrict__ ppb,
+                                             float* __restrict__ pk3b, float* __restrict__ wk1b,
+                                             const float* __restrict__ rdx, const float* __restrict__ rdy,
+                                             const float* __restrict__ gz, const float* __restrict__ pp,
+                                             const float* __restrict__ pk3, const float* __restrict__ wk1,
+                                             const float* __restrict__ uoutb, const float* __restrict__ voutb,
+                                             float dt, Dims d, int kb) {
+    using T = float;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NhpAdjF32Smem& s = *reinterpret_cast<NhpAdjF32Smem*>(smem_raw);
+    const int64_t sj = d.sj, sk = d.sk;
+    const int ci0 = (int)blk.x * 32, cj0 = (int)blk.y * kPgcTJ;     // the tile's first cell
+    const int kz0 = (int)blk.z * kb, kz1 = min(kz0 + kb, d.nz + 1);  // its levels of [0, nz]
+    const int tid = threadIdx.y * kTX + threadIdx.x;
+    auto terms = [&](int k, bool own) {
+      const int slot = k & 1;
+      const int64_t kofs = (int64_t)k * sk;
+      for (int e = tid; e < 33 * (kPgcTJ + 1); e += kThreads) {
+        const int a = e % 33, b = e / 33;            // point (ci0 - 1 + a, cj0 - 1 + b)
+        const int i = ci0 - 1 + a, j = cj0 - 1 + b;
+        const bool xs = b >= 1, ys = a >= 1;          // in the x-axis / y-axis region
+        if (!(xs || ys) || !inside(d, i, j, k)) continue;
+        const int64_t o = kofs + i + (int64_t)j * sj;
+        const T gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
+        const T pp0 = ld(pp + o), pp1 = ld(pp + o + sk), w1 = ld(wk1 + o);
+        const T U = ld(uoutb + o) * ld(rdx + o), V = ld(voutb + o) * ld(rdy + o);
+        if (own && xs && ys) {  // the tile's own cells
+          uinb[o] = U;
+          vinb[o] = V;
+        }
+        T v[7];
+        if (xs) {
+          nhp_adj_terms(v, gz, pp, pk3, wk1, o, 1, sk, gz0, gz1, pk0, pk1, pp0, pp1, w1, dt, U);
+#pragma unroll
+          for (int q = 0; q < 7; ++q) s.tx[slot][q][b - 1][a] = v[q];
+        }
+        if (ys) {
+          nhp_adj_terms(v, gz, pp, pk3, wk1, o, sj, sk, gz0, gz1, pk0, pk1, pp0, pp1, w1, dt, V);
+#pragma unroll
+          for (int q = 0; q < 7; ++q) s.ty[slot][q][b][a - 1] = v[q];
+        }
+      }
+    };
+    if (kz0 >= 1) terms(kz0 - 1, false);  // the level below the chunk's first (its cells read it)
+#pragma unroll 1
+    for (int k = kz0; k < kz1; ++k) {
+      if (k < d.nz) terms(k, true);
+      __syncthreads();
+      const int cur = k & 1, prev = (k - 1) & 1;
+      const int64_t kofs = (int64_t)k * sk;
+#pragma unroll
+      for (int r = 0; r < kPgcTJ / kTY; ++r) {
+        const int ta = threadIdx.x, tb = threadIdx.y + kTY * r;
+        const int i = ci0 + ta, j = cj0 + tb;
+        if (i > d.nx || j > d.ny) continue;  // the gather box is [0, N]^2
+        T gb = T(0), pb = T(0), kb3 = T(0), wb = T(0);
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+          const int di = ax == 0 ? 1 : 0, dj = 1 - di;
+          // term q of axis ax at the point c (back = 0) or c - s (back = 1) of ring slot sl
+          auto t = [&](int sl, int q, int back) {
+            return ax == 0 ? s.tx[sl][q][tb][ta + 1 - back] : s.ty[sl][q][tb + 1 - back][ta];
+          };
+          if (inside(d, i, j, k)) {  // p = c
+            gb = gb + t(cur, 1, 0);
+            kb3 = kb3 - t(cur, 2, 0);
+            pb = pb - t(cur, 4, 0);
+            wb = wb + t(cur, 6, 0);
+          }
+          if (inside(d, i - di, j - dj, k)) {  // p = c - s
+            gb = gb - t(cur, 0, 1);
+            kb3 = kb3 - t(cur, 3, 1);
+            pb = pb - t(cur, 5, 1);
+            wb = wb + t(cur, 6, 1);
+          }
+          if (inside(d, i, j, k - 1)) {  // p = c - k
+            gb = gb + t(prev, 0, 0);
+            kb3 = kb3 + t(prev, 3, 0);
+            pb = pb + t(prev, 5, 0);
+          }
+          if (inside(d, i - di, j - dj, k - 1)) {  // p = c - s - k
+            gb = gb - t(prev, 1, 1);
+            kb3 = kb3 + t(prev, 2, 1);
+            pb = pb + t(prev, 4, 1);
+          }
+        }
+        const int64_t o = kofs + i + (int64_t)j * sj;
+        gzb[o] = gb;
+        ppb[o] = pb;
+        pk3b[o] = kb3;
+        if (k < d.nz) wk1b[o] = wb;
+      }
+      __syncthreads();  // level k + 1's terms replace level k - 1's
+    }
+  }
+};
+
 template <class T, class M3>
 oeb_status nh_p_grad_tl_entry(const M3* duout, const M3* dvout, const M3* uin, const M3* vin, const M3* rdx,
                               const M3* rdy, const M3* gz, const M3* pp, const M3* pk3, const M3* wk1,
@@ -1600,6 +1854,17 @@ oeb_status nh_p_grad_adj_entry(const M3* uinb, const M3* vinb, const M3* gzb, co
                           gw1.hi, guo.lo, guo.hi, gvo.lo, gvo.hi}));
   OEB_RETURN_IF_VALIDATING();
   cudaStream_t st = (cudaStream_t)stream;
+  if constexpr (std::is_same<T, float>::value) {
+    if (adjoint_tiles()) {  // one tiled launch, no scratch
+      const Dims d{(int)dom->nx, (int)dom->ny, (int)dom->nz, guo.sj, guo.sk};
+      const int tiles = ((d.nx + 1 + 31) / 32) * ((d.ny + 1 + kPgcTJ - 1) / kPgcTJ);
+      const int kb = tuned_kb(staged_kb(tiles, d.nz + 1, 3));
+      return launch<nh_p_grad_adj_f32>(tile_grid(d.nx + 1, d.ny + 1, d.nz + 1, 32, kPgcTJ, kb),
+                                       sizeof(NhpAdjF32Smem), st, gub.origin, gvb.origin, ggb.origin, gpb.origin,
+                                       gkb.origin, gwb.origin, grx.origin, gry.origin, ggz.origin, gpp.origin,
+                                       gpk.origin, gw1.origin, guo.origin, gvo.origin, dt, d, kb);
+    }
+  }
   const TermLayout lay = term_layout(uoutb);
   void* buf = nullptr;
   OEB_TRY(scratch_alloc(&buf, (size_t)lay.n * 14 * sizeof(T), st));

@@ -53,7 +53,7 @@ def _stream_handle(stream, on_device: bool) -> int:
 
 
 def set_adjoint_tiles(on: bool) -> None:
-    """FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th and fastwavesuv as one tiled launch
+    """FP32 adjoints of hdiffsmag, hadvuv, hadvuv5th, fastwavesuv, p_grad_c and nh_p_grad as one tiled launch
     (True, the default) or in their multi-pass forms (oeb_set_adjoint_tiles); the same bits
     either way."""
     lib = load_library()
