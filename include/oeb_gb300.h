@@ -443,6 +443,31 @@ OEB_API oeb_status oeb_p_grad_c_f32(const oeb_memref3d_f32* uout, const oeb_memr
                             const oeb_memref3d_f32* rdyc, const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz,
                             const oeb_memref3d_f32* pkc, float dt2, const oeb_domain* dom, void* stream);
 
+/* FP32 pressure gradients on profile-relative fields (no reference counterpart; the same
+ * stencils as oeb_p_grad_c_f32 / oeb_nh_p_grad_f32).  gz, pkc (p_grad_c) and gz, pp, pk3
+ * (nh_p_grad) hold FP32 perturbations from an FP64 per-level base profile: the field's value at
+ * interior level k is base[k] + field[k].  Each *_base is a DEVICE array of nz + 1 doubles
+ * (interior levels 0 .. nz, the stencils read level k + 1).  Differences between levels then
+ * take the base difference in FP64 (rounded once to FP32) and differences within a level the
+ * perturbations alone, so the outputs keep the accuracy the FP32 storage of full-value fields
+ * loses (their profiles nearly cancel in the stencils' differences).  Fields and checks as the
+ * standard entries; OEB_ERR_NULL for a NULL base. */
+OEB_API oeb_status oeb_p_grad_c_f32_profiled(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                             const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                             const oeb_memref3d_f32* rdxc, const oeb_memref3d_f32* rdyc,
+                                             const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz,
+                                             const oeb_memref3d_f32* pkc, const double* gz_base,
+                                             const double* pkc_base, float dt2, const oeb_domain* dom,
+                                             void* stream);
+OEB_API oeb_status oeb_nh_p_grad_f32_profiled(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                              const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                              const oeb_memref3d_f32* rdx, const oeb_memref3d_f32* rdy,
+                                              const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp,
+                                              const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1,
+                                              const double* gz_base, const double* pp_base,
+                                              const double* pk3_base, float dt, const oeb_domain* dom,
+                                              void* stream);
+
 /* FP32 of kernels/fvtp2d.h:4-7 -- fvtp2d(q_i, q_j, fx1, fx2, fy1, fy2, q, crx, cry, ra_x, ra_y, xfx, yfx, area,
  *                                fxx, fyy, al, almq, br, b0, smt5); p1, p2 are the driver macros
  * (src/fvtp2d.cpp:11-12).  q_i, q_j, fx2 and fy2 are written over the same extended ranges as the

@@ -590,52 +590,60 @@ oeb_status uvbke_entry(const M3* ub, const M3* vb, const M3* uc, const M3* vc, c
                                  gvc.origin, gca.origin, grs.origin, dt5_hi, dt5_lo, make_dims(*dom, gub), kb);
 }
 
+// The descriptors' checks of p_grad_c (g: uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc).
+template <class T, class M3>
+oeb_status p_grad_c_check(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* rdxc,
+                          const M3* rdyc, const M3* delpc, const M3* gz, const M3* pkc, const oeb_domain* dom,
+                          Grid<T> (&g)[9]) {
+  OEB_TRY(check_domain(dom));
+  const M3* f[9] = {uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc};
+  const Reach reach[9] = {kInterior, kInterior, kInterior, kInterior, kInterior, kInterior,
+                          Reach{1, 0, 1, 0, 0, 0}, Reach{1, 0, 1, 0, 0, 1}, Reach{1, 0, 1, 0, 0, 1}};
+  for (int q = 0; q < 9; ++q) OEB_TRY((check_field3<T>(f[q], *dom, reach[q], &g[q])));
+  OEB_TRY(check_same_strides<T>({&g[0], &g[1], &g[2], &g[3], &g[4], &g[5], &g[6], &g[7], &g[8]}));
+  return check_no_alias({g[0].lo, g[0].hi, g[1].lo, g[1].hi},
+                        {g[2].lo, g[2].hi, g[3].lo, g[3].hi, g[4].lo, g[4].hi, g[5].lo, g[5].hi, g[6].lo, g[6].hi,
+                         g[7].lo, g[7].hi, g[8].lo, g[8].hi});
+}
+
 template <class T, class M3>
 oeb_status p_grad_c_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* rdxc,
                           const M3* rdyc, const M3* delpc, const M3* gz, const M3* pkc, T dt2,
                           const oeb_domain* dom, void* stream) {
-  OEB_TRY(check_domain(dom));
-  Grid<T> gu, gv, gui, gvi, grx, gry, gdp, ggz, gpk;
-  OEB_TRY((check_field3<T>(uout, *dom, kInterior, &gu)));
-  OEB_TRY((check_field3<T>(vout, *dom, kInterior, &gv)));
-  OEB_TRY((check_field3<T>(uin, *dom, kInterior, &gui)));
-  OEB_TRY((check_field3<T>(vin, *dom, kInterior, &gvi)));
-  OEB_TRY((check_field3<T>(rdxc, *dom, kInterior, &grx)));
-  OEB_TRY((check_field3<T>(rdyc, *dom, kInterior, &gry)));
-  OEB_TRY((check_field3<T>(delpc, *dom, Reach{1, 0, 1, 0, 0, 0}, &gdp)));
-  OEB_TRY((check_field3<T>(gz, *dom, Reach{1, 0, 1, 0, 0, 1}, &ggz)));
-  OEB_TRY((check_field3<T>(pkc, *dom, Reach{1, 0, 1, 0, 0, 1}, &gpk)));
-  OEB_TRY(check_same_strides<T>({&gu, &gv, &gui, &gvi, &grx, &gry, &gdp, &ggz, &gpk}));
-  OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi}, {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo,
-                                                        gry.hi, gdp.lo, gdp.hi, ggz.lo, ggz.hi, gpk.lo, gpk.hi}));
+  Grid<T> g[9];
+  OEB_TRY(p_grad_c_check<T>(uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc, dom, g));
   OEB_RETURN_IF_VALIDATING();
   const int kb = tuned_kb(kKB);
-  return launch<p_grad_c_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
-                                    gvi.origin, grx.origin, gry.origin, gdp.origin, ggz.origin, gpk.origin, dt2,
-                                    make_dims(*dom, gu), kb);
+  return launch<p_grad_c_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, g[0].origin, g[1].origin,
+                                    g[2].origin, g[3].origin, g[4].origin, g[5].origin, g[6].origin, g[7].origin,
+                                    g[8].origin, dt2, make_dims(*dom, g[0]), kb);
+}
+
+// The descriptors' checks of nh_p_grad (g: uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1).
+template <class T, class M3>
+oeb_status nh_p_grad_check(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* rdx,
+                           const M3* rdy, const M3* gz, const M3* pp, const M3* pk3, const M3* wk1,
+                           const oeb_domain* dom, Grid<T> (&g)[10]) {
+  OEB_TRY(check_domain(dom));
+  const M3* f[10] = {uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1};
+  const Reach r11 = Reach{0, 1, 0, 1, 0, 1};
+  const Reach reach[10] = {kInterior, kInterior, kInterior, kInterior, kInterior, kInterior, r11, r11, r11,
+                           Reach{0, 1, 0, 1, 0, 0}};
+  for (int q = 0; q < 10; ++q) OEB_TRY((check_field3<T>(f[q], *dom, reach[q], &g[q])));
+  OEB_TRY(check_same_strides<T>({&g[0], &g[1], &g[2], &g[3], &g[4], &g[5], &g[6], &g[7], &g[8], &g[9]}));
+  return check_no_alias({g[0].lo, g[0].hi, g[1].lo, g[1].hi},
+                        {g[2].lo, g[2].hi, g[3].lo, g[3].hi, g[4].lo, g[4].hi, g[5].lo, g[5].hi, g[6].lo, g[6].hi,
+                         g[7].lo, g[7].hi, g[8].lo, g[8].hi, g[9].lo, g[9].hi});
 }
 
 template <class T, class M3>
 oeb_status nh_p_grad_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M3* rdx,
                            const M3* rdy, const M3* gz, const M3* pp, const M3* pk3, const M3* wk1, T dt,
                            const oeb_domain* dom, void* stream) {
-  OEB_TRY(check_domain(dom));
-  Grid<T> gu, gv, gui, gvi, grx, gry, ggz, gpp, gpk, gw1;
-  const Reach r11 = Reach{0, 1, 0, 1, 0, 1};
-  OEB_TRY((check_field3<T>(uout, *dom, kInterior, &gu)));
-  OEB_TRY((check_field3<T>(vout, *dom, kInterior, &gv)));
-  OEB_TRY((check_field3<T>(uin, *dom, kInterior, &gui)));
-  OEB_TRY((check_field3<T>(vin, *dom, kInterior, &gvi)));
-  OEB_TRY((check_field3<T>(rdx, *dom, kInterior, &grx)));
-  OEB_TRY((check_field3<T>(rdy, *dom, kInterior, &gry)));
-  OEB_TRY((check_field3<T>(gz, *dom, r11, &ggz)));
-  OEB_TRY((check_field3<T>(pp, *dom, r11, &gpp)));
-  OEB_TRY((check_field3<T>(pk3, *dom, r11, &gpk)));
-  OEB_TRY((check_field3<T>(wk1, *dom, Reach{0, 1, 0, 1, 0, 0}, &gw1)));
-  OEB_TRY(check_same_strides<T>({&gu, &gv, &gui, &gvi, &grx, &gry, &ggz, &gpp, &gpk, &gw1}));
-  OEB_TRY(check_no_alias({gu.lo, gu.hi, gv.lo, gv.hi},
-                         {gui.lo, gui.hi, gvi.lo, gvi.hi, grx.lo, grx.hi, gry.lo, gry.hi, ggz.lo, ggz.hi, gpp.lo,
-                          gpp.hi, gpk.lo, gpk.hi, gw1.lo, gw1.hi}));
+  Grid<T> g[10];
+  OEB_TRY(nh_p_grad_check<T>(uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, dom, g));
+  Grid<T>&gu = g[0], &gv = g[1], &gui = g[2], &gvi = g[3], &grx = g[4], &gry = g[5], &ggz = g[6], &gpp = g[7],
+         &gpk = g[8], &gw1 = g[9];
   OEB_RETURN_IF_VALIDATING();
   if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
     dim3 grid;
@@ -650,6 +658,153 @@ oeb_status nh_p_grad_entry(const M3* uout, const M3* vout, const M3* uin, const 
                                      gvi.origin, grx.origin, gry.origin, ggz.origin, gpp.origin, gpk.origin,
                                      gw1.origin, dt, make_dims(*dom, gu), kb);
 }
+
+// ---- FP32 pressure gradients on profile-relative fields ---------------------------------
+// The pressure, geopotential and Exner fields of these stencils are a per-level profile plus
+// a small perturbation, and the stencils difference them between neighbouring points and
+// levels, where the profile nearly cancels: stored in FP32, their rounding (2^-24 of values
+// about 100 times the perturbations) then dominates the outputs' error.  These forms take the
+// fields as FP32 perturbations from an FP64 base profile b(k) (one value a level): a
+// difference between levels k + 1 and k is the base difference b(k+1) - b(k) (formed once a
+// level in FP64, rounded once to FP32) plus the perturbations' difference, and one between
+// points of a level is the perturbations' difference alone.  Same expression trees as
+// p_grad_c_kernel / nh_p_grad_kernel in FP32, with diff_dot_based for the paired products.
+
+// Visits this thread's points of the CTA's 32 x 32 tile at its levels [k0, k1); f(o, D) gets
+// D[q] = float(base_q[k+1] - base_q[k]) of the point's level k.  FP64 is a narrow pipe on this
+// GPU, so the differences are formed once a CTA or a warp, not a thread, in one of two ways
+// (measured at 256 x 256 x 80, one level a CTA):
+// * SMEM: before each chunk of up to kLevelChunk levels, NB x chunk threads write them to
+//   shared memory between two barriers (p_grad_c 59-63 us, 65 us by shuffles);
+// * shuffles: a warp is one row of 32 threads, all at the same level; lane q < NB forms D[q]
+//   and the warp shares it by __shfl_sync, with no barrier (nh_p_grad 101 us, 119 us in
+//   shared memory).
+// Every thread of the CTA reaches each barrier and shuffle: the chunk and level loops depend
+// on blk only, and threads outside the tile skip the work, not the loops.
+constexpr int kLevelChunk = 32;
+template <int NB, int U, bool SMEM, class F>
+__device__ __forceinline__ void for_points_profiled(const uint3& blk, const Dims& d, int kb,
+                                                    const double* const (&base)[NB], F&& f) {
+  static_assert(NB * kLevelChunk <= kThreads && kTX == 32, "a warp is one row of threads");
+  const int k0 = blk.z * kb, k1 = min(k0 + kb, d.nz);
+  const int lane = threadIdx.x;
+  const int i = blk.x * kTI + lane;
+  const int sj = (int)d.sj;
+  auto rows = [&](int k, const float (&D)[NB]) {
+    if (i >= d.nx) return;
+    const int64_t kofs = (int64_t)k * d.sk;
+#pragma unroll U
+    for (int r = 0; r < kRows; ++r) {
+      const int j = blk.y * kTJ + threadIdx.y + kTY * r;
+      if (j < d.ny) f(kofs + i + j * sj, D);
+    }
+  };
+  // base[q] for a run-time q, by constant indices (no local-memory copy of base)
+  auto pick = [&](int q) {
+    const double* b = base[0];
+#pragma unroll
+    for (int p = 1; p < NB; ++p)
+      if (q == p) b = base[p];
+    return b;
+  };
+  if constexpr (SMEM) {
+    __shared__ float lv[NB][kLevelChunk];
+    const int t = threadIdx.y * kTX + lane;
+    for (int c0 = k0; c0 < k1; c0 += kLevelChunk) {
+      const int c1 = min(c0 + kLevelChunk, k1);
+      __syncthreads();  // the previous chunk's readers are done with lv
+      if (t < NB * kLevelChunk) {
+        const int q = t / kLevelChunk, k = c0 + t % kLevelChunk;
+        const double* bq = pick(q);
+        if (k < c1) lv[q][k - c0] = (float)(ld(bq + k + 1) - ld(bq + k));
+      }
+      __syncthreads();
+#pragma unroll 1
+      for (int k = c0; k < c1; ++k) {
+        float D[NB];
+#pragma unroll
+        for (int q = 0; q < NB; ++q) D[q] = lv[q][k - c0];
+        rows(k, D);
+      }
+    }
+  } else {
+    const double* bl = pick(lane);
+#pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+      const float mine = lane < NB ? (float)(ld(bl + k + 1) - ld(bl + k)) : 0.0f;
+      float D[NB];
+#pragma unroll
+      for (int q = 0; q < NB; ++q) D[q] = __shfl_sync(0xffffffffu, mine, q);
+      rows(k, D);
+    }
+  }
+}
+
+struct p_grad_c_profiled_f32 {
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uout, float* __restrict__ vout,
+                                             const float* __restrict__ uin, const float* __restrict__ vin,
+                                             const float* __restrict__ rdxc, const float* __restrict__ rdyc,
+                                             const float* __restrict__ delpc, const float* __restrict__ gz,
+                                             const float* __restrict__ pkc, const double* __restrict__ gz_base,
+                                             const double* __restrict__ pkc_base, float dt2, Dims d, int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    const double* const base[2] = {gz_base, pkc_base};
+    for_points_profiled<2, RowUnroll<float>::value, true>(blk, d, kb, base, [&](int64_t o, const float (&D)[2]) {
+      const float G = D[0], K = D[1];
+      const float wk = ld(delpc + o);
+      const float gz0 = ld(gz + o), gz1 = ld(gz + o + sk), pk0 = ld(pkc + o), pk1 = ld(pkc + o + sk);
+      // gz(p-s,k+1) - gz0, pk1 - pkc(p-s), gz(p-s) - gz1, pkc(p-s,k+1) - pk0 (p_grad_c.h:90-97)
+      const float fu = diff_dot_based(G, ld(gz + o - 1 + sk), gz0, K, pk1, ld(pkc + o - 1), -G, ld(gz + o - 1), gz1,
+                                      K, ld(pkc + o - 1 + sk), pk0);
+      uout[o] = (ld(uin + o) + (((dt2 * ld(rdxc + o)) / (ld(delpc + o - 1) + wk)) * fu));
+      const float fv = diff_dot_based(G, ld(gz + o - sj + sk), gz0, K, pk1, ld(pkc + o - sj), -G, ld(gz + o - sj), gz1,
+                                      K, ld(pkc + o - sj + sk), pk0);
+      vout[o] = (ld(vin + o) + (((dt2 * ld(rdyc + o)) / (ld(delpc + o - sj) + wk)) * fv));
+    });
+  }
+};
+
+struct nh_p_grad_profiled_f32 {
+  static __device__ __forceinline__ void run(const uint3& blk, float* __restrict__ uout, float* __restrict__ vout,
+                                             const float* __restrict__ uin, const float* __restrict__ vin,
+                                             const float* __restrict__ rdx, const float* __restrict__ rdy,
+                                             const float* __restrict__ gz, const float* __restrict__ pp,
+                                             const float* __restrict__ pk3, const float* __restrict__ wk1,
+                                             const double* __restrict__ gz_base, const double* __restrict__ pp_base,
+                                             const double* __restrict__ pk3_base, float dt, Dims d, int kb) {
+    const int64_t sj = d.sj, sk = d.sk;
+    const double* const base[3] = {gz_base, pp_base, pk3_base};
+    for_points_profiled<3, kRows, false>(blk, d, kb, base, [&](int64_t o, const float (&D)[3]) {
+      const float G = D[0], P = D[1], K = D[2];
+      const float pk0 = ld(pk3 + o), pk1 = ld(pk3 + o + sk);
+      const float gz0 = ld(gz + o), gz1 = ld(gz + o + sk);
+      const float pp0 = ld(pp + o), pp1 = ld(pp + o + sk);
+      const float w1 = ld(wk1 + o);
+      const float wk = K + (pk1 - pk0);  // pk3(k+1) - pk3(k)
+      // u: neighbour i+1 (nh_p_grad.h:121-131)
+      {
+        const float pkx0 = ld(pk3 + o + 1), pkx1 = ld(pk3 + o + 1 + sk);
+        const float wkx = K + (pkx1 - pkx0);
+        const float gx0 = ld(gz + o + 1), gx1 = ld(gz + o + 1 + sk);
+        const float fk = diff_dot_based(G, gz1, gx0, K, pkx1, pk0, -G, gz0, gx1, K, pk1, pkx0);
+        const float fp = diff_dot_based(G, gz1, gx0, P, ld(pp + o + 1 + sk), pp0, -G, gz0, gx1, P, pp1, ld(pp + o + 1));
+        const float du = ((dt / (wk + wkx)) * fk);
+        uout[o] = (((ld(uin + o) + du) + ((dt / (w1 + ld(wk1 + o + 1))) * fp)) * ld(rdx + o));
+      }
+      // v: neighbour j+1 (nh_p_grad.h:132-142)
+      {
+        const float pky0 = ld(pk3 + o + sj), pky1 = ld(pk3 + o + sj + sk);
+        const float wky = K + (pky1 - pky0);
+        const float gy0 = ld(gz + o + sj), gy1 = ld(gz + o + sj + sk);
+        const float fk = diff_dot_based(G, gz1, gy0, K, pky1, pk0, -G, gz0, gy1, K, pk1, pky0);
+        const float fp =
+            diff_dot_based(G, gz1, gy0, P, ld(pp + o + sj + sk), pp0, -G, gz0, gy1, P, pp1, ld(pp + o + sj));
+        const float dv = ((dt / (wk + wky)) * fk);
+        vout[o] = (((ld(vin + o) + dv) + ((dt / (w1 + ld(wk1 + o + sj))) * fp)) * ld(rdy + o));
+      }
+    });
+  }
+};
 
 template <class T, int ORDER, class M3, class M1>
 oeb_status hadv_entry(const M3* uout, const M3* vout, const M3* uin, const M3* vin, const M1* acrlat0,
@@ -2027,6 +2182,62 @@ OEB_POINTWISE_DIFF_ENTRIES(f64, double)
 OEB_POINTWISE_DIFF_ENTRIES(f32, float)
 
 // The chained step's fused stages (fused.cuh).
+static oeb_status p_grad_c_profiled_entry(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                   const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                   const oeb_memref3d_f32* rdxc, const oeb_memref3d_f32* rdyc,
+                                   const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz,
+                                   const oeb_memref3d_f32* pkc, const double* gz_base, const double* pkc_base,
+                                   float dt2, const oeb_domain* dom, void* stream) {
+  Grid<float> g[9];
+  OEB_TRY(p_grad_c_check<float>(uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc, dom, g));
+  if (!gz_base || !pkc_base) return OEB_ERR_NULL;
+  OEB_RETURN_IF_VALIDATING();
+  const int kb = tuned_kb(kKB);
+  return launch<p_grad_c_profiled_f32>(grid_for(*dom, kb), 0, (cudaStream_t)stream, g[0].origin, g[1].origin,
+                                       g[2].origin, g[3].origin, g[4].origin, g[5].origin, g[6].origin, g[7].origin,
+                                       g[8].origin, gz_base, pkc_base, dt2, make_dims(*dom, g[0]), kb);
+}
+
+static oeb_status nh_p_grad_profiled_entry(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                    const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                    const oeb_memref3d_f32* rdx, const oeb_memref3d_f32* rdy,
+                                    const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp,
+                                    const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1, const double* gz_base,
+                                    const double* pp_base, const double* pk3_base, float dt,
+                                    const oeb_domain* dom, void* stream) {
+  Grid<float> g[10];
+  OEB_TRY(nh_p_grad_check<float>(uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, dom, g));
+  if (!gz_base || !pp_base || !pk3_base) return OEB_ERR_NULL;
+  OEB_RETURN_IF_VALIDATING();
+  const int kb = tuned_kb(kKB);
+  return launch<nh_p_grad_profiled_f32>(grid_for(*dom, kb), 0, (cudaStream_t)stream, g[0].origin, g[1].origin,
+                                        g[2].origin, g[3].origin, g[4].origin, g[5].origin, g[6].origin,
+                                        g[7].origin, g[8].origin, g[9].origin, gz_base, pp_base, pk3_base, dt,
+                                        make_dims(*dom, g[0]), kb);
+}
+
+extern "C" oeb_status oeb_p_grad_c_f32_profiled(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                             const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                             const oeb_memref3d_f32* rdxc, const oeb_memref3d_f32* rdyc,
+                                             const oeb_memref3d_f32* delpc, const oeb_memref3d_f32* gz,
+                                             const oeb_memref3d_f32* pkc, const double* gz_base,
+                                             const double* pkc_base, float dt2, const oeb_domain* dom,
+                                             void* stream) {
+  return p_grad_c_profiled_entry(uout, vout, uin, vin, rdxc, rdyc, delpc, gz, pkc, gz_base, pkc_base, dt2, dom,
+                                 stream);
+}
+extern "C" oeb_status oeb_nh_p_grad_f32_profiled(const oeb_memref3d_f32* uout, const oeb_memref3d_f32* vout,
+                                              const oeb_memref3d_f32* uin, const oeb_memref3d_f32* vin,
+                                              const oeb_memref3d_f32* rdx, const oeb_memref3d_f32* rdy,
+                                              const oeb_memref3d_f32* gz, const oeb_memref3d_f32* pp,
+                                              const oeb_memref3d_f32* pk3, const oeb_memref3d_f32* wk1,
+                                              const double* gz_base, const double* pp_base,
+                                              const double* pk3_base, float dt, const oeb_domain* dom,
+                                              void* stream) {
+  return nh_p_grad_profiled_entry(uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, gz_base, pp_base, pk3_base, dt,
+                                  dom, stream);
+}
+
 #define OEB_FUSED_ENTRIES(S, T)                                                                                    \
   oeb_status oeb::hadvuv5th_update(const OEB_M3(S) * u2, const OEB_M3(S) * v2, const OEB_M3(S) * u1,               \
                                    const OEB_M3(S) * v1, const OEB_M1(S) * acrlat0, const OEB_M1(S) * acrlat1,     \

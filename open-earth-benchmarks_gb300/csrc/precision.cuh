@@ -573,4 +573,29 @@ __device__ __forceinline__ T diff_dot(T a, T b, T c, T d, T e, T f, T g, T h) {
   }
 }
 
+// The same paired products for fields stored as an FP64 per-level base profile plus FP32
+// perturbations: each difference is a base difference between two levels, D (FP32, formed once
+// a level from the FP64 profile), plus the difference of the perturbations, a - b.  a - b is a
+// TwoSum pair, D is added to it by a second TwoSum, and the two low parts join the first-order
+// terms of diff_dot: (D1 + a - b)(D2 + c - d) + (D3 + e - f)(D4 + g - h).
+__device__ __forceinline__ void based_diff(float D, float a, float b, float& x, float& xl) {
+  float p, pl, t;
+  detail::two_sum(a, -b, p, pl);
+  detail::two_sum(D, p, x, t);
+  xl = t + pl;
+}
+__device__ __forceinline__ float diff_dot_based(float D1, float a, float b, float D2, float c, float d, float D3,
+                                                float e, float f, float D4, float g, float h) {
+  float x, xl, y, yl, z, zl, w, wl;
+  based_diff(D1, a, b, x, xl);
+  based_diff(D2, c, d, y, yl);
+  based_diff(D3, e, f, z, zl);
+  based_diff(D4, g, h, w, wl);
+  const float q = z * w;
+  const float qe = fmaf(z, w, -q);
+  const float m = fmaf(x, y, q);
+  const float low = fmaf(x, yl, fmaf(xl, y, fmaf(z, wl, fmaf(zl, w, qe))));
+  return m + low;
+}
+
 }  // namespace oeb

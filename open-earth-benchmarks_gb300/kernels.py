@@ -99,6 +99,41 @@ def call(kernel: str, fields: Dict[str, Storage], scalars: Optional[Dict[str, fl
     check(entry(name)(*cargs), name)
 
 
+# The fields of the FP32 pressure-gradient stencils that the profiled entry points take as
+# perturbations from an FP64 per-level base profile, in the entry points' argument order.
+PROFILED_FIELDS = {"p_grad_c": ("gz", "pkc"), "nh_p_grad": ("gz", "pp", "pk3")}
+
+
+def call_profiled(kernel: str, fields: Dict[str, Storage], bases, scalars: Optional[Dict[str, float]] = None,
+                  domain=None, stream=None) -> None:
+    """FP32 p_grad_c / nh_p_grad on profile-relative fields (oeb_<kernel>_f32_profiled).
+
+    ``fields`` are FP32 device Storages as for :func:`call`, except that those named by
+    ``PROFILED_FIELDS[kernel]`` hold perturbations: the field at interior level k is
+    ``bases[name][k] + fields[name][k]``.  ``bases[name]`` is a float64 CUDA tensor of nz + 1
+    values (interior levels 0 .. nz)."""
+    if kernel not in PROFILED_FIELDS:
+        raise ValueError("%s has no profiled form (only %s)" % (kernel, sorted(PROFILED_FIELDS)))
+    spec = KERNELS[kernel]
+    st = [fields[a.name] for a in spec.abi_args]
+    if any(not isinstance(f, Storage) or not f.is_cuda or f.dtype != np.float32 for f in st):
+        raise TypeError("%s: the profiled form takes FP32 device Storages" % kernel)
+    dom = _domain(domain)
+    ptrs = []
+    for n in PROFILED_FIELDS[kernel]:
+        b = bases[n]
+        if not b.is_cuda or str(b.dtype) != "torch.float64" or b.numel() != dom.nz + 1 or not b.is_contiguous():
+            raise ValueError("%s: base profile %r must be a contiguous float64 CUDA tensor of nz + 1 = %d values"
+                             % (kernel, n, dom.nz + 1))
+        ptrs.append(ctypes.c_void_p(b.data_ptr()))
+    vals = dict(DRIVER_SCALARS.get(kernel, {}))
+    vals.update(scalars or {})
+    cargs = [ctypes.byref(f.memref()) for f in st] + ptrs + _scalar_args(spec, vals, "f32")
+    cargs += [ctypes.byref(dom), ctypes.c_void_p(_stream_handle(stream, True))]
+    name = "oeb_%s_f32_profiled" % kernel
+    check(entry(name)(*cargs), name)
+
+
 def _scalar_args(spec, vals, precision):
     out = []
     for s in spec.scalars:
