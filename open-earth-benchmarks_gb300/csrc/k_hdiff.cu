@@ -292,7 +292,10 @@ struct hdiffsmag_kernel {
                      hdweight;
           smag_u = clamp_smag(smag_u);
           const T uc = s.u[b + 1][a + 1];
-          // u(i+1) + u(i-1) - 2u + crlato (u(j+1) - u) + crlatu (u(j-1) - u)
+          // u(i+1) + u(i-1) - 2u + crlato (u(j+1) - u) + crlatu (u(j-1) - u), the reference's
+          // sum in every precision: FP32 is then bit-identical to the reference compiled for
+          // float.  A compensated FP32 sum (TwoSum / TwoProduct) measured the same largest error
+          // against the FP64 oracle (5.5e-8) at about five times the sum's operations.
           Acc<T> lu(s.u[b + 1][a + 2]);
           lu.add(s.u[b + 1][a]);
           lu.add(-scale2<1>(uc));

@@ -3,19 +3,21 @@
 // FP64 (Prec<double>): the reference's own arithmetic, operation for operation, so that with
 // FP contraction off the results are bit-identical to the reference's OpenMP kernels.
 //
-// FP32 (Prec<float>): fields stored and computed in FP32, with two safeguards:
+// FP32 (Prec<float>): fields stored and computed in FP32.  Where the reference's float
+// sequence is as accurate as anything cheaper-than-FP64 (measured against the FP64 oracle),
+// the kernels run exactly that sequence and are bit-identical to the reference compiled for
+// float: the advection drivers (hadvuv.h:10-24, hadvuv5th.h:10-36) and hdiffsmag.  Elsewhere:
 //  * branch tests on the sign of a product -- the hdiffsa flux limiter (hdiffsa.h:106-113)
 //    and the fvtp2d PPM monotonicity flag (fvtp2d.h:23) -- are decided on the exact
 //    product, which is what an FP64 product of two floats gives (it is exact in FP64 and
 //    cannot underflow); here without any FP64 instruction, from the operands' signs;
-//  * the sums whose large terms cancel -- the flux sums of hdiffsmag (its laplacians,
-//    hdiffsmag.h:239-241, 254-256) and of the advection drivers (hadvuv.h:10-24,
-//    hadvuv5th.h:10-36) and the laplacian (laplace.h:39) -- are accumulated with
-//    error-free transformations (TwoSum, and TwoProduct via fmaf), i.e. compensated
-//    summation, so cancellation between their large terms does not cost FP32 digits;
+//  * the laplacian (laplace.h:39), whose centre term nearly cancels the neighbour sum, is
+//    formed as a sum of neighbour differences (k_pointwise.cu);
 //  * the paired products of the pressure gradients (nh_p_grad.h:126-142,
 //    p_grad_c.h:90-97) are summed with Kahan's FMA algorithm over error-free
-//    differences (diff_dot below).
+//    differences (diff_dot below);
+//  * uvbke's double dt5 multiplies as a float pair (k_pointwise.cu).
+// kCompensated selects these forms.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -499,10 +501,8 @@ __device__ __forceinline__ T scale2v(T x, int k) {
   return Prec<T>::scale2v(x, k);
 }
 
-// Left-to-right sum of terms.  Plain for FP64 (the reference's order and rounding); for FP32
-// a compensated sum: every addition is a TwoSum and every product a TwoProduct, the
-// rounding errors are summed separately and added back at the end.
-template <class T, bool C = Prec<T>::kCompensated>
+// Left-to-right sum of terms, in the reference's order and rounding (every precision).
+template <class T>
 struct Acc {
   T s;
   __device__ __forceinline__ explicit Acc(T x) : s(x) {}
@@ -510,31 +510,6 @@ struct Acc {
   __device__ __forceinline__ void add(T x) { s = s + x; }
   __device__ __forceinline__ void add_prod(T a, T b) { s = s + a * b; }
   __device__ __forceinline__ T get() const { return s; }
-};
-
-template <>
-struct Acc<float, true> {
-  float s, c;
-  __device__ __forceinline__ explicit Acc(float x) : s(x), c(0.f) {}
-  __device__ __forceinline__ static Acc prod(float a, float b) {
-    Acc r(a * b);
-    r.c = fmaf(a, b, -r.s);
-    return r;
-  }
-  // TwoSum (Knuth): s + x = t + e exactly
-  __device__ __forceinline__ void add(float x) {
-    const float t = s + x;
-    const float bb = t - s;
-    const float e = (s - (t - bb)) + (x - bb);
-    s = t;
-    c += e;
-  }
-  __device__ __forceinline__ void add_prod(float a, float b) {
-    const float p = a * b;
-    c += fmaf(a, b, -p);
-    add(p);
-  }
-  __device__ __forceinline__ float get() const { return s + c; }
 };
 
 namespace detail {

@@ -142,3 +142,35 @@ def test_marched_forms_match_plain_kernels(pkg, fields, cuda, name, size, kb):
     for a in spec.by_role("out3"):
         np.testing.assert_array_equal(dev[a.name].numpy().view(np.uint32), host[a.name].numpy().view(np.uint32),
                                       err_msg="%s.%s marched vs plain" % (name, a.name))
+
+
+# The FP32 advection stencils and hdiffsmag run the reference's operation sequence in float, so
+# they are bit-identical to the reference compiled for float (the oracle's float instantiation,
+# pinned to that build by tests/golden/), in every tile shape (hdiffsmag has one).
+@pytest.mark.parametrize("name", ("hadvuv", "hadvuv5th", "hdiffsmag"))
+@pytest.mark.parametrize("case", [("fronts", 256, 256, 80, 2), ("physical", 100, 70, 13, 5), ("fronts", 37, 45, 5, 9)])
+@pytest.mark.parametrize("shape", [0, 1, 2])
+def test_fp32_is_the_float_reference(pkg, fields, orc, cuda, name, case, shape):
+    import torch
+    if name == "hdiffsmag" and shape:
+        pytest.skip("hdiffsmag has one tile shape")
+    workload, nx, ny, nz, seed = case
+    spec = pkg.KERNELS[name]
+    inputs = fields.make_inputs(name, nx, ny, nz, seed=seed, workload=workload)
+    sc = fields.make_scalars(name, seed=seed)
+    outs = fields.make_outputs(name, nx, ny, nz)
+    sc32 = {s.name: float(np.float32(sc[s.name])) for s in spec.scalars}
+    naive = {k: v.astype(np.float32) for k, v in {**inputs, **outs}.items()}
+    orc.run_oracle(spec, naive, sc32, nx, ny, nz, H)
+    lib = pkg.load_library()
+    assert lib.oeb_set_tile_shape(shape) == 0
+    try:
+        dev = {k: pkg.Storage(torch.from_numpy(v.astype(np.float32)).to(cuda), H)
+               for k, v in {**inputs, **outs}.items()}
+        pkg.call(name, dev, sc32, domain=(nx, ny, nz))
+        torch.cuda.synchronize()
+    finally:
+        lib.oeb_set_tile_shape(0)
+    for a in spec.by_role("out3"):
+        np.testing.assert_array_equal(dev[a.name].numpy().view(np.uint32), naive[a.name].view(np.uint32),
+                                      err_msg="%s.%s %s shape %d vs the float reference" % (name, a.name, case, shape))
