@@ -144,16 +144,17 @@ def test_marched_forms_match_plain_kernels(pkg, fields, cuda, name, size, kb):
                                       err_msg="%s.%s marched vs plain" % (name, a.name))
 
 
-# The FP32 advection stencils and hdiffsmag run the reference's operation sequence in float, so
-# they are bit-identical to the reference compiled for float (the oracle's float instantiation,
-# pinned to that build by tests/golden/), in every tile shape (hdiffsmag has one).
-@pytest.mark.parametrize("name", ("hadvuv", "hadvuv5th", "hdiffsmag"))
+# The FP32 advection stencils, hdiffsmag and fastwavesuv run the reference's operation sequence
+# in float, so they are bit-identical to the reference compiled for float (the oracle's float
+# instantiation, pinned to that build by tests/golden/), in every tile shape (only the
+# advection stencils have more than one).
+@pytest.mark.parametrize("name", ("hadvuv", "hadvuv5th", "hdiffsmag", "fastwavesuv"))
 @pytest.mark.parametrize("case", [("fronts", 256, 256, 80, 2), ("physical", 100, 70, 13, 5), ("fronts", 37, 45, 5, 9)])
 @pytest.mark.parametrize("shape", [0, 1, 2])
 def test_fp32_is_the_float_reference(pkg, fields, orc, cuda, name, case, shape):
     import torch
-    if name == "hdiffsmag" and shape:
-        pytest.skip("hdiffsmag has one tile shape")
+    if name not in ("hadvuv", "hadvuv5th") and shape:
+        pytest.skip("%s has one tile shape" % name)
     workload, nx, ny, nz, seed = case
     spec = pkg.KERNELS[name]
     inputs = fields.make_inputs(name, nx, ny, nz, seed=seed, workload=workload)
