@@ -247,12 +247,11 @@ struct nh_p_grad_kernel {
 //   else :  ((c3 f[-1] + ch f[0]) + f[1]) + c6 f[2]
 template <class T>
 __device__ __forceinline__ T adv3_axis(const T* __restrict__ f, int64_t o, int64_t s, T a) {
-  constexpr T c6 = T(-1.0) / T(6.0), c3 = T(-1.0) / T(3.0), ch = T(-0.5);
+  constexpr T c6 = T(-1.0) / T(6.0), c3 = T(-1.0) / T(3.0);
   const bool pos = gt0(a);
   const T fa = ld(f + o + (pos ? -2 : -1) * s), fb = ld(f + o - s), f0 = ld(f + o), fc = ld(f + o + s),
           fd = ld(f + o + (pos ? 1 : 2) * s);
-  (void)ch;
-  const T p0 = (pos ? c6 : c3) * fa, ph = -scale2<-1>(f0), p3 = (pos ? c3 : c6) * fd;  // ch = -1/2
+  const T p0 = (pos ? c6 : c3) * fa, ph = -scale2<-1>(f0), p3 = (pos ? c3 : c6) * fd;  // the -1/2 term: an exact scaling
   return (pos ? a : -a) * (((p0 + (pos ? fb : ph)) + (pos ? ph : fc)) + p3);
 }
 
@@ -261,15 +260,12 @@ __device__ __forceinline__ T adv3_axis(const T* __restrict__ f, int64_t o, int64
 //   else :  ((((c20 f[-2] + c2 f[-1]) + c3 f[0]) + f[1]) + c4 f[2]) + c30 f[3]
 template <class T>
 __device__ __forceinline__ T adv5_axis(const T* __restrict__ f, int64_t o, int64_t s, T a) {
-  constexpr T c30 = T(1.0) / T(30.0), c4 = T(-1.0) / T(4.0), c3 = T(-1.0) / T(3.0), c2 = T(-1.0) / T(2.0),
-              c20 = T(1.0) / T(20.0);
+  constexpr T c30 = T(1.0) / T(30.0), c3 = T(-1.0) / T(3.0), c20 = T(1.0) / T(20.0);
   const bool pos = gt0(a);
   const int64_t sh = pos ? 0 : s;  // the negative branch reads one cell further along the axis
   const T x0 = ld(f + o - 3 * s + sh), x1 = ld(f + o - 2 * s + sh), fm1 = ld(f + o - s), f0 = ld(f + o),
           fp1 = ld(f + o + s), x4 = ld(f + o + s + sh), x5 = ld(f + o + 2 * s + sh);
-  (void)c4;
-  (void)c2;
-  // c4 = -1/4 and c2 = -1/2: the products by them are exact power-of-two scalings
+  // the -1/4 and -1/2 terms: exact power-of-two scalings
   const T p0 = (pos ? c30 : c20) * x0, p1 = -scale2v(x1, pos ? -2 : -1), pm = c3 * f0, p4 = -scale2v(x4, pos ? -1 : -2),
           p5 = (pos ? c20 : c30) * x5;
   return (pos ? a : -a) * (((((p0 + p1) + (pos ? fm1 : pm)) + (pos ? pm : fp1)) + p4) + p5);
