@@ -494,7 +494,7 @@ def run_ours(args):
                "per_kernel_isolated_ms": {k: round(v, 5) for k, v in iso32.items()},
                "per_kernel_isolated_frac": {k: round(_algorithmic_bytes(pkg, k, 4) / (v * 1e-3) / 1e9 /
                                                      _measured_peak()[0], 4) for k, v in iso32.items()},
-               "note": "FP32 storage and arithmetic, exact limiter sign tests, compensated flux sums; "
+               "note": "FP32 storage and arithmetic, exact limiter sign tests, error-free pressure-gradient products; "
                        "normwise error vs the FP64 oracle is stated per kernel by tests/test_gpu_fp32.py"}
 
     adjoint = None

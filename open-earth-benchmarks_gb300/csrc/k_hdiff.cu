@@ -1,7 +1,8 @@
 // k_hdiff.cu -- horizontal diffusion stencils whose intermediates are shared by neighbouring
 // points: hdiffsa (kernels/hdiffsa.h:95-123) and hdiffsmag (kernels/hdiffsmag.h:205-263), in
-// FP64 (bit-identical to the reference) and FP32 (exact limiter sign tests, compensated
-// laplacian sums; precision.cuh).
+// FP64 (bit-identical to the reference) and FP32 (hdiffsa with exact limiter sign tests;
+// hdiffsmag the reference's float sequence, bit-identical to the reference compiled for
+// float; precision.cuh).
 //
 // The reference's OpenMP variants recompute each intermediate for every point that uses it
 // (three laplacians per point in hdiffsa, three T^2 and three S^2 per point in hdiffsmag).

@@ -6,9 +6,10 @@
 // round-to-nearest on both sides, so the results are bit-identical to the reference
 // OpenMP kernels.  Expression trees keep the reference's order and parenthesisation; a
 // subexpression that occurs twice in the reference is computed once here (same operands,
-// same value).  FP32: the same trees in float, with the sums that cancel compensated
-// (precision.cuh): the advection flux sums and the laplacian, and the paired products of
-// the pressure-gradient stencils in float-float.
+// same value).  FP32: the same trees in float (the advection stencils are then bit-identical
+// to the reference compiled for float), except where cancellation costs digits
+// (precision.cuh): the laplacian as a sum of neighbour differences, and the paired products
+// of the pressure-gradient stencils by Kahan's FMA algorithm over error-free differences.
 //
 // The adjoint kernels reproduce no reference arithmetic: their accumulations use explicit
 // fma() (one rounding, half the FP64 instructions), which --fmad=false does not affect.  The

@@ -3,7 +3,7 @@
 Two errors per output (normwise: max |e| / max |fp64| over the written box):
 
 * ``arith``  -- the FP32 kernel against the FP64 oracle run on the SAME inputs rounded to
-  FP32: the error of the FP32 arithmetic alone (compensated flux sums, exact sign tests).
+  FP32: the error of the FP32 arithmetic alone (exact sign tests, error-free products).
 * ``total``  -- the FP32 kernel against the FP64 oracle on the original FP64 inputs: adds
   the quantisation of the inputs to FP32, which dominates wherever a stencil differences
   large, nearly equal values (pressure ~1000 with differences ~10 in nh_p_grad/p_grad_c).
