@@ -252,7 +252,8 @@ __device__ __forceinline__ T adv3_axis(const T* __restrict__ f, int64_t o, int64
   const bool pos = gt0(a);
   const T fa = ld(f + o + (pos ? -2 : -1) * s), fb = ld(f + o - s), f0 = ld(f + o), fc = ld(f + o + s),
           fd = ld(f + o + (pos ? 1 : 2) * s);
-  const T p0 = (pos ? c6 : c3) * fa, ph = -scale2<-1>(f0), p3 = (pos ? c3 : c6) * fd;  // the -1/2 term: an exact scaling
+  // the -1/2 term: an exact scaling
+  const T p0 = (pos ? c6 : c3) * fa, ph = -scale2<-1>(f0), p3 = (pos ? c3 : c6) * fd;
   return (pos ? a : -a) * (((p0 + (pos ? fb : ph)) + (pos ? ph : fc)) + p3);
 }
 
@@ -630,21 +631,19 @@ oeb_status nh_p_grad_entry(const M3* uout, const M3* vout, const M3* uin, const 
                            const oeb_domain* dom, void* stream) {
   Grid<T> g[10];
   OEB_TRY(nh_p_grad_check<T>(uout, vout, uin, vin, rdx, rdy, gz, pp, pk3, wk1, dom, g));
-  Grid<T>&gu = g[0], &gv = g[1], &gui = g[2], &gvi = g[3], &grx = g[4], &gry = g[5], &ggz = g[6], &gpp = g[7],
-         &gpk = g[8], &gw1 = g[9];
   OEB_RETURN_IF_VALIDATING();
   if constexpr (std::is_same<T, float>::value) if (!fields_in_host_memory()) {
     dim3 grid;
     int kb;
     staged_launch_shape<nh_p_grad_staged_f32>(*dom, &grid, &kb);
-    return launch<nh_p_grad_staged_f32>(grid, sizeof(nh_p_grad_staged_f32::Smem), (cudaStream_t)stream, gu.origin,
-                                        gv.origin, gui.origin, gvi.origin, grx.origin, gry.origin, ggz.origin,
-                                        gpp.origin, gpk.origin, gw1.origin, dt, make_dims(*dom, gu), kb);
+    return launch<nh_p_grad_staged_f32>(grid, sizeof(nh_p_grad_staged_f32::Smem), (cudaStream_t)stream, g[0].origin,
+                                        g[1].origin, g[2].origin, g[3].origin, g[4].origin, g[5].origin, g[6].origin,
+                                        g[7].origin, g[8].origin, g[9].origin, dt, make_dims(*dom, g[0]), kb);
   }
   const int kb = tuned_kb(kKB);
-  return launch<nh_p_grad_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, gu.origin, gv.origin, gui.origin,
-                                     gvi.origin, grx.origin, gry.origin, ggz.origin, gpp.origin, gpk.origin,
-                                     gw1.origin, dt, make_dims(*dom, gu), kb);
+  return launch<nh_p_grad_kernel<T>>(grid_for(*dom, kb), 0, (cudaStream_t)stream, g[0].origin, g[1].origin,
+                                     g[2].origin, g[3].origin, g[4].origin, g[5].origin, g[6].origin, g[7].origin,
+                                     g[8].origin, g[9].origin, dt, make_dims(*dom, g[0]), kb);
 }
 
 // ---- FP32 pressure gradients on profile-relative fields ---------------------------------
