@@ -1,8 +1,10 @@
-"""The profiled FP32 pressure-gradient entry points without a GPU: argument checks.
+"""The profiled FP32 pressure-gradient entry points without a GPU.
 
-oeb_p_grad_c_f32_profiled / oeb_nh_p_grad_f32_profiled check their descriptors exactly as
-the standard FP32 entry points do, then their base-profile pointers, all before any CUDA call;
-these calls return at one of those checks, so nothing is launched or dereferenced.
+* Argument checks: oeb_p_grad_c_f32_profiled / oeb_nh_p_grad_f32_profiled check their
+  descriptors exactly as the standard FP32 entry points do, then their base-profile pointers,
+  all before any CUDA call; these calls return at one of those checks, so nothing is launched
+  or dereferenced.
+* The storage format's own error floor, through the FP64 oracle.
 """
 from __future__ import annotations
 
@@ -52,3 +54,36 @@ def test_python_wrapper_checks_its_arguments(pkg, fields):
     with pytest.raises(TypeError, match="FP32 device Storages"):
         pkg.kernels.call_profiled("p_grad_c", st, {}, domain=(8, 8, 2))
     assert pkg.kernels.PROFILED_FIELDS == {"p_grad_c": ("gz", "pkc"), "nh_p_grad": ("gz", "pp", "pk3")}
+
+
+@pytest.mark.parametrize("name", sorted(PROFILED))
+@pytest.mark.parametrize("case", [("fronts", 37, 45, 5, 9), ("physical", 64, 48, 20, 1)])
+def test_profiled_storage_floor(pkg, fields, orc, name, case):
+    """The storage format alone, through the FP64 oracle: outputs from the fields as an FP64
+    per-level base plus FP32 perturbations are within 1e-6 of those from the FP64 fields (the
+    floor the GPU kernels' total error sits on), while full-value FP32 fields are not."""
+    workload, nx, ny, nz, seed = case
+    spec = pkg.KERNELS[name]
+    inputs = fields.make_inputs(name, nx, ny, nz, seed=seed, workload=workload)
+    outs = fields.make_outputs(name, nx, ny, nz)
+    sc = fields.make_scalars(name, seed=seed)
+    ref = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+    orc.run_oracle(spec, ref, sc, nx, ny, nz, H)
+    prof = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+    full = {k: v.copy() for k, v in {**inputs, **outs}.items()}
+    for f in pkg.kernels.PROFILED_FIELDS[name]:
+        a = inputs[f]
+        base = a[H:H + nz + 1].mean(axis=(1, 2))
+        pert = (a[H:H + nz + 1] - base[:, None, None]).astype(np.float32)
+        prof[f][H:H + nz + 1] = base[:, None, None] + pert.astype(np.float64)
+        full[f] = a.astype(np.float32).astype(np.float64)
+    orc.run_oracle(spec, prof, sc, nx, ny, nz, H)
+    orc.run_oracle(spec, full, sc, nx, ny, nz, H)
+    box = (slice(H, H + nz), slice(H, H + ny), slice(H, H + nx))
+    for a in spec.by_role("out3"):
+        want = ref[a.name][box]
+        scale = np.abs(want).max()
+        e_prof = np.abs(prof[a.name][box] - want).max() / scale
+        e_full = np.abs(full[a.name][box] - want).max() / scale
+        assert e_prof <= 3e-7, (name, a.name, e_prof)
+        assert e_full > 1e-6, (name, a.name, e_full)
