@@ -109,7 +109,8 @@ struct RowUnroll<F64i> {
 };
 // The same for the stencils whose per-point work is longest (advection, pressure gradient):
 // FP32 unrolls two rows (measured at 256 x 256 x 80: hadvuv 89 -> 62 us, hadvuv5th 107 ->
-// 77 us, nh_p_grad 101 -> 94 us against four), FP64 one.
+// 77 us, nh_p_grad 101 -> 94 us against four; the advection times are those of a build with
+// compensated flux sums, since replaced by the plain float sums), FP64 one.
 template <class T>
 struct HeavyRowUnroll {
   static constexpr int value = 2;
